@@ -1,0 +1,242 @@
+/*
+ * xg.h — C ABI of the GB300 Newton-load engine (libxg).
+ *
+ * The engine evaluates SPICE device models (MOSFET level 1, BSIM3 v3.2, junction
+ * diode, resistor, capacitor, independent V/I sources) in FP64 on one GPU and
+ * stamps their residual and Jacobian contributions into the sparse MNA system.
+ * Every sum is taken in a fixed order — device type, then instance, then the
+ * statement order of the reference load loop — so F, Q, dF/dx and dQ/dx are
+ * identical run to run and match a serial CPU load bit for bit wherever the
+ * per-term arithmetic matches.
+ *
+ * Reference interfaces replaced (paths inside the Xyce source tree):
+ *   Device::updateState / updateSecondaryState / loadDAEVectors / loadDAEMatrices
+ *       src/DeviceModelPKG/Core/include/N_DEV_Device.h:200-265
+ *   DeviceMgr::updateState / loadDAEVectors / loadDAEMatrices (orchestration)
+ *       src/DeviceModelPKG/Core/src/N_DEV_DeviceMgr.C:2201-2285, 2329-2479, 2520-2661
+ *   Topology stamp -> CSR offset registration
+ *       src/TopoManagerPKG/src/N_TOP_CktGraphBasic.C:1092-1142
+ *   N_LAS_Matrix row access + linearCombo, N_LAS_Solver::solve
+ *       src/LinearAlgebraServicesPKG/src/N_LAS_Matrix.C:835-879
+ *       src/LinearAlgebraServicesPKG/include/N_LAS_Solver.h:60-125
+ *
+ * Conventions
+ *   - Every entry point returns int: XG_OK (0) or a negative XG_ERR_* code.
+ *     No C++ exception crosses this boundary. xg_last_error() gives a message.
+ *   - Pointers named host_* are host memory; pointers named dev_* are device
+ *     memory on the context's GPU. Sizes are element counts unless noted.
+ *   - Node numbering: circuit nodes are 0..n_nodes-1, ground is -1.  Solution
+ *     vectors have one extra trailing slot (index n_unknowns) holding ground,
+ *     like the reference's SOLUTION_OVERLAP_GND map (N_LAS_Builder.C:334-341);
+ *     contributions to ground are discarded and never reach the solved system.
+ *   - Unknown order: circuit nodes first, then each device's internal
+ *     unknowns (source branch currents, MOSFET drain'/source' nodes, diode
+ *     anode' node) in device-type load order, instance order.
+ *   - State (sta) and store (sto) slots are laid out per device type in load
+ *     order, instance order, each instance's slots contiguous in the order the
+ *     reference registers them (registerStateLIDs / registerStoreLIDs).
+ */
+#ifndef XG_H
+#define XG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define XG_ABI_VERSION 1
+
+/* ---- status codes --------------------------------------------------------- */
+#define XG_OK               0
+#define XG_ERR_ARG         -1   /* bad argument / size / index                   */
+#define XG_ERR_CUDA        -2   /* CUDA runtime error                            */
+#define XG_ERR_OOM         -3   /* device or host allocation failed              */
+#define XG_ERR_SINGULAR    -4   /* zero pivot in LU refactorisation              */
+#define XG_ERR_NAN         -5   /* non-finite value in a load or solve           */
+#define XG_ERR_TIMEOUT     -6   /* a bounded device wait gave up                 */
+#define XG_ERR_STATE       -7   /* call made in the wrong order                  */
+#define XG_ERR_UNSUPPORTED -8   /* model option / parameter not implemented      */
+#define XG_ERR_NOCONV      -9   /* Newton iteration did not converge             */
+
+/* ---- device types (also the default load order) ---------------------------- */
+enum xg_dev_type {
+  XG_DEV_RES   = 0,   /* resistor            N_DEV_Resistor.C   */
+  XG_DEV_CAP   = 1,   /* capacitor           N_DEV_Capacitor.C  */
+  XG_DEV_VSRC  = 2,   /* independent V src   N_DEV_Vsrc.C       */
+  XG_DEV_ISRC  = 3,   /* independent I src   N_DEV_ISRC.C       */
+  XG_DEV_DIODE = 4,   /* junction diode      N_DEV_Diode.C      */
+  XG_DEV_MOS1  = 5,   /* MOSFET level 1      N_DEV_MOSFET1.C    */
+  XG_DEV_BSIM3 = 6,   /* BSIM3 v3.2 (lvl 9/49) N_DEV_MOSFET_B3.C */
+  XG_NUM_DEV_TYPES = 7
+};
+
+/* Source waveform kinds for XG_DEV_VSRC / XG_DEV_ISRC (N_DEV_SourceData.C). */
+enum xg_src_kind { XG_SRC_DC = 0, XG_SRC_PULSE = 1 };
+
+/* ---- netlist description (input to setup) ---------------------------------- */
+
+/* A .MODEL card: parameters by (case-insensitive) name, as in a netlist.
+ * polarity: +1 for NMOS / diode, -1 for PMOS (the reference's model dtype). */
+typedef struct {
+  int type;                 /* enum xg_dev_type: XG_DEV_DIODE, XG_DEV_MOS1, XG_DEV_BSIM3 */
+  int polarity;
+  int n_params;
+  const char *const *names;
+  const double *values;
+} xg_model_desc;
+
+/* MOSFET instances (level 1 or BSIM3). Optional arrays may be NULL (default). */
+typedef struct {
+  int n;
+  const int *d, *g, *s, *b;   /* terminal nodes                             */
+  const int *model;           /* index into xg_netlist.models               */
+  const double *w, *l;        /* channel width / length [m]                 */
+  const double *ad, *as;      /* drain / source area   [m^2]   (optional)   */
+  const double *pd, *ps;      /* drain / source perim. [m]     (optional)   */
+  const double *nrd, *nrs;    /* drain / source squares        (optional)   */
+  const double *m;            /* parallel multiplier           (optional)   */
+} xg_mos_desc;
+
+typedef struct {
+  int n;
+  const int *a, *c;           /* anode / cathode */
+  const int *model;
+  const double *area;         /* optional, default 1 */
+} xg_diode_desc;
+
+/* Two-terminal linear elements: resistor [ohm], capacitor [F], DC current [A]. */
+typedef struct {
+  int n;
+  const int *p, *m;
+  const double *value;
+} xg_twoterm_desc;
+
+/* Independent voltage / current sources. wave holds 7 doubles per source:
+ *   DC:    {v, 0, 0, 0, 0, 0, 0}
+ *   PULSE: {v1, v2, td, tr, tf, pw, per}   (N_DEV_SourceData.C:775-1031)   */
+typedef struct {
+  int n;
+  const int *p, *m;
+  const int *kind;            /* enum xg_src_kind */
+  const double *wave;         /* 7 * n */
+} xg_src_desc;
+
+typedef struct {
+  int n_nodes;                /* circuit nodes, ground excluded */
+  int n_models;
+  const xg_model_desc *models;
+  /* Load order of device types; NULL = enum order. n_type_order entries. */
+  int n_type_order;
+  const int *type_order;
+  xg_twoterm_desc res, cap;
+  xg_src_desc vsrc, isrc;
+  xg_diode_desc diode;
+  xg_mos_desc mos1, bsim3;
+} xg_netlist;
+
+/* Device options (DeviceOptions, N_DEV_DeviceOptions.C:66-160). */
+typedef struct {
+  double gmin;                /* default 1e-12 */
+  double temp;                /* circuit temperature [K], default 300.15 */
+  double tnom;                /* nominal temperature [K], default 300.15 */
+  int    voltlim;             /* voltageLimiterFlag, default 1 */
+  int    newmeyer;            /* must be 0 (Meyer back-averaging path) */
+  int    fma;                 /* 0: every product/sum rounded separately, bit-
+                                 identical to a serial CPU load; 1: kernels built
+                                 with fused multiply-add (faster, ~1 ulp/term) */
+} xg_device_options;
+
+/* Per-load solver flags (SolverState, N_DEV_SolverState.h:85-160). */
+typedef struct {
+  int dcop, tranop, acop, transient;
+  int init_jct, init_fix;
+  int newton_iter;
+  int inputop;
+  double pdt;                 /* alpha / h of the integrator */
+  double time;                /* current time [s], for PULSE sources */
+} xg_load_flags;
+
+/* ---- vector ids ------------------------------------------------------------ */
+enum xg_vec_id {
+  XG_VEC_SOL_NEXT = 0, XG_VEC_SOL_CURR, XG_VEC_SOL_LAST,   /* n_unknowns + 1 */
+  XG_VEC_STA_NEXT, XG_VEC_STA_CURR, XG_VEC_STA_LAST,       /* n_state        */
+  XG_VEC_STO_NEXT, XG_VEC_STO_CURR, XG_VEC_STO_LAST,       /* n_store        */
+  XG_VEC_F, XG_VEC_Q, XG_VEC_DFDXDVP, XG_VEC_DQDXDVP,      /* n_unknowns + 1 */
+  XG_VEC_DFDX, XG_VEC_DQDX,                                /* nnz values     */
+  XG_NUM_VECS
+};
+
+typedef struct xg_ctx xg_ctx;
+typedef struct xg_circuit xg_circuit;
+
+typedef struct {
+  int n_unknowns;             /* solved unknowns (ground excluded) */
+  int n_state, n_store;
+  int64_t nnz;                /* non-zeros of the solved Jacobian pattern */
+  int64_t n_terms;            /* stamp terms produced per load */
+  int64_t scratch_bytes;      /* device scratch held for per-load terms */
+  int n_instances[XG_NUM_DEV_TYPES];
+} xg_circuit_info;
+
+/* ---- library ----------------------------------------------------------------- */
+int  xg_abi_version(void);
+const char *xg_last_error(void);
+const char *xg_status_string(int status);
+
+/* ---- context: one GPU, one stream (replaces the DeviceMgr singleton) -------- */
+int xg_ctx_create(int cuda_device, xg_ctx **out);
+int xg_ctx_destroy(xg_ctx *ctx);
+int xg_ctx_set_options(xg_ctx *ctx, const xg_device_options *opt);
+int xg_ctx_get_options(const xg_ctx *ctx, xg_device_options *opt);
+int xg_ctx_synchronize(xg_ctx *ctx);
+/* The CUDA stream all work of this context is queued on (cudaStream_t). */
+int xg_ctx_stream(xg_ctx *ctx, void **stream_out);
+
+/* ---- circuit setup (DeviceMgr::addDeviceModel/addDeviceInstance, Topology
+ *      registerLIDs/registerJacLIDs, Instance::updateTemperature) ----------- */
+int xg_circuit_create(xg_ctx *ctx, const xg_netlist *nl, xg_circuit **out);
+int xg_circuit_destroy(xg_circuit *c);
+int xg_circuit_get_info(const xg_circuit *c, xg_circuit_info *info);
+/* CSR pattern of the solved Jacobian (ground row/col excluded): rowptr has
+ * n_unknowns+1 entries, colidx nnz entries, columns ascending in each row. */
+int xg_circuit_get_pattern(const xg_circuit *c, int *host_rowptr, int *host_colidx);
+/* Per-instance parameter block of one device type as derived by setup
+ * (layout: include/xg_params.h, column k of instance i at [k*n + i]).
+ * host_out may be NULL to query n_params / n_instances only. */
+int xg_circuit_get_params(const xg_circuit *c, int dev_type, double *host_out,
+                          int *n_params, int *n_instances);
+/* The same parameter block computed on the host alone (no GPU needed): for
+ * callers that inspect setup, and for CPU-side checks of it. */
+int xg_setup_params(const xg_netlist *nl, const xg_device_options *opt, int dev_type,
+                    double *host_out, int *n_params, int *n_instances);
+
+/* ---- vectors ------------------------------------------------------------------ */
+int xg_vec_size(const xg_circuit *c, int vec_id, int64_t *n);
+int xg_vec_upload(xg_circuit *c, int vec_id, const double *host_src);
+int xg_vec_download(xg_circuit *c, int vec_id, double *host_dst);
+int xg_vec_device_ptr(xg_circuit *c, int vec_id, double **dev_ptr);
+/* next <- curr <- last rotation of sol/sta/sto after an accepted step. */
+int xg_rotate_history(xg_circuit *c);
+
+/* ---- the Newton load ---------------------------------------------------------
+ * xg_update_state       : Device::updateState for every type/instance: limited
+ *                         junction voltages, currents, charges, caps; writes
+ *                         next sta/sto and the per-instance stamp terms.
+ * xg_load_dae_vectors   : Device::loadDAEVectors: F, Q, dFdxdVp, dQdxdVp.
+ * xg_load_dae_matrices  : Device::loadDAEMatrices: dFdx, dQdx values.
+ * xg_load               : all three, fused (the path a Newton iteration uses).
+ * Outputs are zeroed inside the call (the reference's caller zeroes them,
+ * N_TIA_Assembler.C:156-161). All calls are asynchronous on the context stream.
+ */
+int xg_update_state(xg_circuit *c, const xg_load_flags *flags);
+int xg_load_dae_vectors(xg_circuit *c);
+int xg_load_dae_matrices(xg_circuit *c);
+int xg_load(xg_circuit *c, const xg_load_flags *flags);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* XG_H */

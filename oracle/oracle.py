@@ -1,0 +1,120 @@
+"""Python driver for the C oracle (oracle/_build/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py as the checker; never by the engine.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from xyce_gb300 import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            from xyce_gb300 import build
+            build.build_oracle()
+        L = C.CDLL(LIB_PATH)
+        vp = C.c_void_p
+        L.xgo_build.argtypes = [C.POINTER(abi.XgNetlist), C.POINTER(abi.XgDeviceOptions), vp,
+                                C.POINTER(vp)]
+        L.xgo_free.argtypes = [vp]
+        L.xgo_sizes.argtypes = [vp] + [C.POINTER(C.c_int)] * 3 + [C.POINTER(C.c_int64)]
+        L.xgo_pattern.argtypes = [vp, vp, vp]
+        L.xgo_reset_members.argtypes = [vp]
+        L.xgo_load.argtypes = [vp, C.POINTER(abi.XgLoadFlags), vp] + [vp] * 8
+        L.xgo_load_range.argtypes = [vp, C.POINTER(abi.XgLoadFlags), vp, C.c_int, C.c_int,
+                                     C.c_int] + [vp] * 8
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class OracleCircuit:
+    """params: dict dev_type -> (n_params, n_instances) array from setup."""
+
+    def __init__(self, netlist, params, options=None):
+        self._nl = netlist.to_c()
+        self._opt = options or abi.device_options()
+        self._blocks = {t: np.ascontiguousarray(p, np.float64) for t, p in params.items()}
+        arr = (C.c_void_p * abi.NUM_DEV_TYPES)()
+        for t, b in self._blocks.items():
+            arr[t] = _ptr(b)
+        self._arr = arr
+        h = C.c_void_p()
+        rc = lib().xgo_build(C.byref(self._nl), C.byref(self._opt), arr, C.byref(h))
+        if rc != 0:
+            raise RuntimeError(f"xgo_build failed: {rc}")
+        self.h = h
+        n, s, t, z = C.c_int(), C.c_int(), C.c_int(), C.c_int64()
+        lib().xgo_sizes(h, C.byref(n), C.byref(s), C.byref(t), C.byref(z))
+        self.n_unknowns, self.n_state, self.n_store, self.nnz = n.value, s.value, t.value, z.value
+        self.rowptr = np.zeros(self.n_unknowns + 1, np.int32)
+        self.col = np.zeros(max(1, self.nnz), np.int32)
+        lib().xgo_pattern(h, _ptr(self.rowptr), _ptr(self.col))
+        self.col = self.col[: self.nnz]
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().xgo_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def reset_members(self):
+        lib().xgo_reset_members(self.h)
+
+    def _inputs(self, sol, sta, sto):
+        ins = [np.ascontiguousarray(v, np.float64) for v in list(sol) + list(sta) + list(sto)]
+        ins = [v if v.size else np.zeros(1) for v in ins]
+        return ins, (C.c_void_p * 9)(*[_ptr(a) for a in ins])
+
+    def load(self, flags, sol, sta, sto):
+        nr = self.n_unknowns + 1
+        ins, arr = self._inputs(sol, sta, sto)
+        out = {k: np.zeros(nr) for k in ("F", "Q", "dFdxdVp", "dQdxdVp")}
+        out["sta_next"] = np.zeros(max(1, self.n_state))
+        out["sto_next"] = np.zeros(max(1, self.n_store))
+        out["dFdx"] = np.zeros(max(1, self.nnz))
+        out["dQdx"] = np.zeros(max(1, self.nnz))
+        rc = lib().xgo_load(self.h, C.byref(flags), arr, *[_ptr(out[k]) for k in (
+            "F", "Q", "dFdxdVp", "dQdxdVp", "sta_next", "sto_next", "dFdx", "dQdx")])
+        if rc != 0:
+            raise RuntimeError(f"xgo_load failed: {rc}")
+        for k in ("F", "Q", "dFdxdVp", "dQdxdVp"):
+            out[k] = out[k][: self.n_unknowns]
+        out["sta_next"] = out["sta_next"][: self.n_state]
+        out["sto_next"] = out["sto_next"][: self.n_store]
+        out["dFdx"] = out["dFdx"][: self.nnz]
+        out["dQdx"] = out["dQdx"][: self.nnz]
+        out["rows"] = np.repeat(np.arange(self.n_unknowns, dtype=np.int32), np.diff(self.rowptr))
+        out["cols"] = self.col.copy()
+        return out
+
+    def load_range_timed(self, flags, sol, sta, sto, dev_type, i0, i1, scratch=None):
+        """Load instances [i0, i1) of one type into scratch outputs; returns scratch."""
+        nr = self.n_unknowns + 1
+        ins, arr = self._inputs(sol, sta, sto)
+        if scratch is None:
+            scratch = [np.zeros(nr) for _ in range(4)] + [
+                np.array(ins[3], copy=True), np.array(ins[6], copy=True),
+                np.zeros(max(1, self.nnz)), np.zeros(max(1, self.nnz))]
+        rc = lib().xgo_load_range(self.h, C.byref(flags), arr, dev_type, i0, i1,
+                                  *[_ptr(a) for a in scratch])
+        if rc != 0:
+            raise RuntimeError(f"xgo_load_range failed: {rc}")
+        return scratch

@@ -1,0 +1,102 @@
+"""Python driver for oracle/_ref/libxyceref.so — the reference's own device
+code compiled by oracle/ref_build/build_ref.py.  Test infrastructure only:
+used to pin the C oracle and to generate golden fixtures, never by the product.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from xyce_gb300 import abi
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_ref", "libxyceref.so")
+_lib = None
+
+
+def available():
+    return os.path.exists(LIB_PATH)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(LIB_PATH)
+        _lib.xref_build.argtypes = [C.POINTER(abi.XgNetlist), C.POINTER(abi.XgDeviceOptions),
+                                    C.POINTER(C.c_void_p)]
+        _lib.xref_free.argtypes = [C.c_void_p]
+        _lib.xref_sizes.argtypes = [C.c_void_p] + [C.POINTER(C.c_int)] * 3 + [C.POINTER(C.c_int64)]
+        _lib.xref_pattern.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.xref_load.argtypes = [C.c_void_p, C.POINTER(abi.XgLoadFlags), C.c_void_p] + [C.c_void_p] * 8
+        _lib.xref_params.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(C.c_int)]
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class RefCircuit:
+    """One circuit built inside the reference device code."""
+
+    def __init__(self, netlist, options=None):
+        self._nl = netlist.to_c()
+        self._opt = options or abi.device_options()
+        h = C.c_void_p()
+        rc = lib().xref_build(C.byref(self._nl), C.byref(self._opt), C.byref(h))
+        if rc != 0:
+            raise RuntimeError(f"xref_build failed: {rc}")
+        self.h = h
+        n, s, t, z = C.c_int(), C.c_int(), C.c_int(), C.c_int64()
+        lib().xref_sizes(h, C.byref(n), C.byref(s), C.byref(t), C.byref(z))
+        self.n_unknowns, self.n_state, self.n_store, self.nnz_gnd = n.value, s.value, t.value, z.value
+        self.rowptr = np.zeros(self.n_unknowns + 2, np.int32)
+        self.col = np.zeros(self.nnz_gnd, np.int32)
+        lib().xref_pattern(h, _ptr(self.rowptr), _ptr(self.col))
+
+    def close(self):
+        if self.h:
+            lib().xref_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self, dev_type):
+        """Derived parameters of one device type as the reference computed them,
+        shape (n_params, n_instances) in the layout of include/xg_params.h."""
+        npar = C.c_int(0)
+        n = lib().xref_params(self.h, dev_type, None, C.byref(npar))
+        if n <= 0:
+            return np.zeros((0, 0))
+        out = np.zeros(npar.value * n)
+        lib().xref_params(self.h, dev_type, _ptr(out), C.byref(npar))
+        return out.reshape(npar.value, n)
+
+    def load(self, flags, sol, sta, sto):
+        """sol/sta/sto: sequences (next, curr, last). Returns dict of outputs;
+        matrices are returned as dense-free COO over the ground-excluded pattern."""
+        nr = self.n_unknowns + 1
+        ins = [np.ascontiguousarray(v, np.float64) for v in list(sol) + list(sta) + list(sto)]
+        arr = (C.c_void_p * 9)(*[_ptr(a) for a in ins])
+        out = {k: np.zeros(nr) for k in ("F", "Q", "dFdxdVp", "dQdxdVp")}
+        out["sta_next"] = np.zeros(max(1, self.n_state))
+        out["sto_next"] = np.zeros(max(1, self.n_store))
+        dfdx = np.zeros(self.nnz_gnd)
+        dqdx = np.zeros(self.nnz_gnd)
+        rc = lib().xref_load(self.h, C.byref(flags), arr, _ptr(out["F"]), _ptr(out["Q"]),
+                             _ptr(out["dFdxdVp"]), _ptr(out["dQdxdVp"]), _ptr(out["sta_next"]),
+                             _ptr(out["sto_next"]), _ptr(dfdx), _ptr(dqdx))
+        if rc != 0:
+            raise RuntimeError(f"xref_load failed: {rc}")
+        out["sta_next"] = out["sta_next"][: self.n_state]
+        out["sto_next"] = out["sto_next"][: self.n_store]
+        rows = np.repeat(np.arange(nr, dtype=np.int32), np.diff(self.rowptr))
+        keep = (rows < self.n_unknowns) & (self.col < self.n_unknowns)
+        out["rows"], out["cols"] = rows[keep], self.col[keep]
+        out["dFdx"], out["dQdx"] = dfdx[keep], dqdx[keep]
+        for k in ("F", "Q", "dFdxdVp", "dQdxdVp"):
+            out[k] = out[k][: self.n_unknowns]
+        return out

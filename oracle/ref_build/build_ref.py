@@ -1,0 +1,89 @@
+"""Build recipe for oracle/_ref/libxyceref.so: the reference Xyce device code,
+compiled from its own unmodified sources, plus the harness in this folder.
+
+Test infrastructure only.  Runs where the reference source tree is present
+(it is not copied into this repository); writes only under oracle/_ref/.
+Usage:  python oracle/ref_build/build_ref.py [--ref /path/to/reference] [-j N]
+"""
+import argparse
+import concurrent.futures as cf
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(os.path.dirname(HERE), "_ref")
+REPO = os.path.dirname(os.path.dirname(HERE))
+
+OPEN_MODELS = ["MOSFET1", "MOSFET_B3", "Diode", "Resistor", "Capacitor", "Vsrc"]
+# Core files left out: the device manager itself (replaced by the harness) and
+# the reaction/TCAD machinery that needs Sacado.
+CORE_SKIP = {"N_DEV_DeviceMgr", "N_DEV_RxnSet", "N_DEV_SpecieSource", "N_DEV_Region",
+             "N_DEV_RegionData", "N_DEV_Reaction", "N_DEV_ReactionNetwork",
+             "N_DEV_RateConstantCalculators", "N_DEV_DeviceInterface",
+             "N_DEV_RegisterDevices", "N_DEV_DeviceSensitivities"}
+UTIL_SKIP = {"N_UTL_FFTInterface", "N_UTL_FFTW_Interface", "N_UTL_IntelFFT_Interface",
+             "N_UTL_Timer", "N_UTL_MPI", "N_UTL_ExpressionData", "N_UTL_Version"}
+ERH_SKIP = {"null_streambuf", "mpi_filebuf"}
+
+
+def sources(ref):
+    src = os.path.join(ref, "src")
+    out = [os.path.join(src, "DeviceModelPKG/OpenModels/src", f"N_DEV_{m}.C") for m in OPEN_MODELS]
+    for d, skip in (("DeviceModelPKG/Core/src", CORE_SKIP), ("UtilityPKG/src", UTIL_SKIP),
+                    ("ErrorHandlingPKG/src", ERH_SKIP)):
+        full = os.path.join(src, d)
+        for f in sorted(os.listdir(full)):
+            if f.endswith(".C") and f[:-2] not in skip:
+                out.append(os.path.join(full, f))
+    return out
+
+
+def include_dirs(ref):
+    dirs = []
+    for root, _, _ in os.walk(os.path.join(ref, "src")):
+        if root.endswith("/include") and "/test" not in root:
+            dirs.append(root)
+    return sorted(dirs)
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default=os.environ.get("XYCE_REFERENCE", "/root/reference"))
+    ap.add_argument("-j", type=int, default=os.cpu_count() or 4)
+    a = ap.parse_args(argv)
+    if not os.path.isdir(os.path.join(a.ref, "src", "DeviceModelPKG")):
+        print(f"reference tree not found at {a.ref}; skipping", file=sys.stderr)
+        return 0
+    objdir = os.path.join(OUT, "obj")
+    os.makedirs(objdir, exist_ok=True)
+    incs = ["-I" + os.path.join(HERE, "shim"), "-I" + os.path.join(REPO, "include")]
+    incs += ["-I" + d for d in include_dirs(a.ref)]
+    # -ffp-contract=off: no fused multiply-add, so every product and sum is
+    # rounded separately, as on the reference's x86-64 build.
+    flags = ["g++", "-std=c++11", "-O2", "-fPIC", "-w", "-ffp-contract=off",
+             "-include", "set", "-include", "iomanip", "-include", "cstring"]
+
+    def compile_one(path):
+        obj = os.path.join(objdir, os.path.basename(path)[:-2] + ".o")
+        if os.path.exists(obj) and os.path.getmtime(obj) >= os.path.getmtime(path):
+            return obj
+        r = subprocess.run(flags + incs + ["-c", path, "-o", obj], capture_output=True, text=True)
+        if r.returncode:
+            raise RuntimeError(f"compile failed: {path}\n{r.stderr[-3000:]}")
+        return obj
+
+    srcs = sources(a.ref) + [os.path.join(HERE, "xref_harness.C")]
+    with cf.ThreadPoolExecutor(a.j) as ex:
+        objs = list(ex.map(compile_one, srcs))
+    lib = os.path.join(OUT, "libxyceref.so")
+    r = subprocess.run(["g++", "-shared", "-o", lib] + objs + ["-Wl,--no-undefined", "-ldl"],
+                       capture_output=True, text=True)
+    if r.returncode:
+        raise RuntimeError("link failed\n" + r.stderr[-6000:])
+    print(lib)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

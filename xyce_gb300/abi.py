@@ -1,0 +1,181 @@
+"""ctypes mirror of include/xg.h: the netlist description, option and flag
+structs shared by the engine (libxg), and plain-numpy builders for them.
+
+A `Netlist` holds numpy arrays per device type; `Netlist.to_c()` returns an
+`XgNetlist` ctypes struct whose pointers stay valid while the Netlist lives.
+"""
+import ctypes as C
+
+import numpy as np
+
+# device types (enum xg_dev_type)
+DEV_RES, DEV_CAP, DEV_VSRC, DEV_ISRC, DEV_DIODE, DEV_MOS1, DEV_BSIM3 = range(7)
+NUM_DEV_TYPES = 7
+SRC_DC, SRC_PULSE = 0, 1
+
+# vector ids (enum xg_vec_id)
+(VEC_SOL_NEXT, VEC_SOL_CURR, VEC_SOL_LAST, VEC_STA_NEXT, VEC_STA_CURR, VEC_STA_LAST,
+ VEC_STO_NEXT, VEC_STO_CURR, VEC_STO_LAST, VEC_F, VEC_Q, VEC_DFDXDVP, VEC_DQDXDVP,
+ VEC_DFDX, VEC_DQDX) = range(15)
+
+STATUS = {0: "XG_OK", -1: "XG_ERR_ARG", -2: "XG_ERR_CUDA", -3: "XG_ERR_OOM",
+          -4: "XG_ERR_SINGULAR", -5: "XG_ERR_NAN", -6: "XG_ERR_TIMEOUT", -7: "XG_ERR_STATE",
+          -8: "XG_ERR_UNSUPPORTED", -9: "XG_ERR_NOCONV"}
+
+_ip = C.POINTER(C.c_int)
+_dp = C.POINTER(C.c_double)
+
+
+class XgModelDesc(C.Structure):
+    _fields_ = [("type", C.c_int), ("polarity", C.c_int), ("n_params", C.c_int),
+                ("names", C.POINTER(C.c_char_p)), ("values", _dp)]
+
+
+class XgMosDesc(C.Structure):
+    _fields_ = [("n", C.c_int), ("d", _ip), ("g", _ip), ("s", _ip), ("b", _ip), ("model", _ip),
+                ("w", _dp), ("l", _dp), ("ad", _dp), ("as_", _dp), ("pd", _dp), ("ps", _dp),
+                ("nrd", _dp), ("nrs", _dp), ("m", _dp)]
+
+
+class XgDiodeDesc(C.Structure):
+    _fields_ = [("n", C.c_int), ("a", _ip), ("c", _ip), ("model", _ip), ("area", _dp)]
+
+
+class XgTwoTermDesc(C.Structure):
+    _fields_ = [("n", C.c_int), ("p", _ip), ("m", _ip), ("value", _dp)]
+
+
+class XgSrcDesc(C.Structure):
+    _fields_ = [("n", C.c_int), ("p", _ip), ("m", _ip), ("kind", _ip), ("wave", _dp)]
+
+
+class XgNetlist(C.Structure):
+    _fields_ = [("n_nodes", C.c_int), ("n_models", C.c_int), ("models", C.POINTER(XgModelDesc)),
+                ("n_type_order", C.c_int), ("type_order", _ip),
+                ("res", XgTwoTermDesc), ("cap", XgTwoTermDesc),
+                ("vsrc", XgSrcDesc), ("isrc", XgSrcDesc),
+                ("diode", XgDiodeDesc), ("mos1", XgMosDesc), ("bsim3", XgMosDesc)]
+
+
+class XgDeviceOptions(C.Structure):
+    _fields_ = [("gmin", C.c_double), ("temp", C.c_double), ("tnom", C.c_double),
+                ("voltlim", C.c_int), ("newmeyer", C.c_int), ("fma", C.c_int)]
+
+
+class XgLoadFlags(C.Structure):
+    _fields_ = [("dcop", C.c_int), ("tranop", C.c_int), ("acop", C.c_int), ("transient", C.c_int),
+                ("init_jct", C.c_int), ("init_fix", C.c_int), ("newton_iter", C.c_int),
+                ("inputop", C.c_int), ("pdt", C.c_double), ("time", C.c_double)]
+
+
+class XgCircuitInfo(C.Structure):
+    _fields_ = [("n_unknowns", C.c_int), ("n_state", C.c_int), ("n_store", C.c_int),
+                ("nnz", C.c_int64), ("n_terms", C.c_int64), ("scratch_bytes", C.c_int64),
+                ("n_instances", C.c_int * NUM_DEV_TYPES)]
+
+
+def device_options(gmin=1e-12, temp=300.15, tnom=300.15, voltlim=1, newmeyer=0, fma=0):
+    return XgDeviceOptions(gmin, temp, tnom, voltlim, newmeyer, fma)
+
+
+def load_flags(dcop=0, tranop=0, acop=0, transient=1, init_jct=0, init_fix=0, newton_iter=1,
+               inputop=0, pdt=0.0, time=0.0):
+    return XgLoadFlags(dcop, tranop, acop, transient, init_jct, init_fix, newton_iter, inputop,
+                       pdt, time)
+
+
+def _iarr(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _darr(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _p(a, t):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+class Model:
+    """A .MODEL card: type (DEV_DIODE/DEV_MOS1/DEV_BSIM3), polarity (+1/-1), params."""
+
+    def __init__(self, type_, polarity=1, **params):
+        self.type = type_
+        self.polarity = polarity
+        self.params = {k.upper(): float(v) for k, v in params.items()}
+
+
+class Netlist:
+    """Device arrays per type; node -1 is ground."""
+
+    def __init__(self, n_nodes):
+        self.n_nodes = int(n_nodes)
+        self.models = []
+        self.type_order = None
+        self.res = None     # dict p, m, value
+        self.cap = None
+        self.vsrc = None    # dict p, m, kind, wave (n x 7)
+        self.isrc = None
+        self.diode = None   # dict a, c, model, area
+        self.mos1 = None    # dict d, g, s, b, model, w, l, (ad, as, pd, ps, nrd, nrs, m)
+        self.bsim3 = None
+
+    def add_model(self, model):
+        self.models.append(model)
+        return len(self.models) - 1
+
+    def count(self, t):
+        d = [self.res, self.cap, self.vsrc, self.isrc, self.diode, self.mos1, self.bsim3][t]
+        if d is None:
+            return 0
+        return len(d[next(iter(d))])
+
+    def to_c(self):
+        keep = []
+        nl = XgNetlist()
+        nl.n_nodes = self.n_nodes
+        mods = (XgModelDesc * max(1, len(self.models)))()
+        for i, m in enumerate(self.models):
+            names = (C.c_char_p * max(1, len(m.params)))(*[k.encode() for k in m.params])
+            vals = _darr(list(m.params.values()) or [0.0])
+            keep += [names, vals]
+            mods[i] = XgModelDesc(m.type, m.polarity, len(m.params), names, _p(vals, _dp))
+        keep.append(mods)
+        nl.n_models = len(self.models)
+        nl.models = mods
+        if self.type_order is not None:
+            to = _iarr(self.type_order)
+            keep.append(to)
+            nl.n_type_order = len(to)
+            nl.type_order = _p(to, _ip)
+
+        def arr(d, k, f):
+            if d is None or d.get(k) is None:
+                return None
+            a = f(d[k])
+            keep.append(a)
+            return a
+
+        for field, d in (("res", self.res), ("cap", self.cap)):
+            if d is not None:
+                p, m, v = arr(d, "p", _iarr), arr(d, "m", _iarr), arr(d, "value", _darr)
+                setattr(nl, field, XgTwoTermDesc(len(p), _p(p, _ip), _p(m, _ip), _p(v, _dp)))
+        for field, d in (("vsrc", self.vsrc), ("isrc", self.isrc)):
+            if d is not None:
+                p, m, k = arr(d, "p", _iarr), arr(d, "m", _iarr), arr(d, "kind", _iarr)
+                w = arr(d, "wave", lambda x: _darr(np.asarray(x).reshape(-1)))
+                setattr(nl, field, XgSrcDesc(len(p), _p(p, _ip), _p(m, _ip), _p(k, _ip),
+                                             _p(w, _dp)))
+        if self.diode is not None:
+            d = self.diode
+            a, c_, mo = arr(d, "a", _iarr), arr(d, "c", _iarr), arr(d, "model", _iarr)
+            ar = arr(d, "area", _darr)
+            nl.diode = XgDiodeDesc(len(a), _p(a, _ip), _p(c_, _ip), _p(mo, _ip), _p(ar, _dp))
+        for field, d in (("mos1", self.mos1), ("bsim3", self.bsim3)):
+            if d is not None:
+                ints = [arr(d, k, _iarr) for k in ("d", "g", "s", "b", "model")]
+                dbl = [arr(d, k, _darr) for k in ("w", "l", "ad", "as", "pd", "ps", "nrd", "nrs", "m")]
+                setattr(nl, field, XgMosDesc(len(ints[0]), *[_p(a, _ip) for a in ints],
+                                             *[_p(a, _dp) for a in dbl]))
+        nl._keep = keep
+        return nl

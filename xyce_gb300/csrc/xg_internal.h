@@ -1,0 +1,117 @@
+// xg_internal.h — structures shared by the host setup (setup.cpp), the C ABI
+// (api.cpp) and the load kernels (load_kernels.cu).
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "xg.h"
+#include "xg_params.h"
+
+namespace xg {
+
+// Where a stamp term lands.  Vector outputs address (kind, LID slot j);
+// matrix outputs address (kind, row LID slot j, col LID slot j2).  LID slots
+// index the instance's LID list (terminals then internal unknowns).
+enum OutKind : int8_t { OUT_F = 0, OUT_Q, OUT_DFDXDVP, OUT_DQDXDVP, OUT_DFDX, OUT_DQDX };
+
+struct TermDef {
+  OutKind kind;
+  int8_t row;   // LID slot of the equation (row)
+  int8_t col;   // LID slot of the unknown (column), matrices only
+};
+
+// Per-type static description: LIDs per instance and the ordered stamp
+// terms the load kernel writes (the statement order of the reference Master
+// loops).  Defined in setup.cpp.
+struct TypeLayout {
+  int nlid;
+  int nterm;
+  const TermDef *terms;
+  int np;
+  int nsta, nsto;
+};
+const TypeLayout &type_layout(int dev_type);
+
+// Per-type data prepared by setup.
+struct TypeData {
+  int n = 0;                   // instances
+  int np = 0, nlid = 0, nterm = 0, nsta = 0, nsto = 0;
+  int sta0 = 0, sto0 = 0;      // first state / store slot
+  int64_t term0 = 0;           // first term in the per-load term buffer
+  std::vector<double> params;  // SoA: params[k * n + i]
+  std::vector<int> lid;        // SoA: lid[j * n + i]; ground = n_unknowns
+  // device copies
+  double *d_params = nullptr;
+  int *d_lid = nullptr;
+};
+
+// Device-side view of one device type, passed to kernels by value.
+struct DevType {
+  int n;
+  int nterm;
+  int sta0, sto0;
+  int64_t term0;
+  const double *p;   // SoA params
+  const int *lid;    // SoA LIDs
+};
+
+struct DevOptions {
+  double gmin;
+  int voltlim;
+};
+
+struct Flags {
+  int dcop, tranop, acop, transient, init_jct, init_fix, newton_iter, inputop;
+  double pdt, time;
+};
+
+// Vectors the load kernels read and write (device pointers).
+struct LoadIO {
+  const double *sol;        // next solution, n_unknowns + 1 (ground = 0)
+  const double *sta_curr, *sto_curr;
+  double *sta, *sto;        // next state / store (sto holds previous iterate on entry)
+  double *terms;            // per-load stamp terms
+  double *diode_vd;         // Diode Instance::Vd carried between loads
+};
+
+// Everything setup derives from a netlist (host side).
+struct Plan {
+  int n_nodes = 0, n_unknowns = 0, n_state = 0, n_store = 0;
+  int order[XG_NUM_DEV_TYPES];
+  int n_order = 0;
+  TypeData T[XG_NUM_DEV_TYPES];
+  // solved Jacobian pattern (ground excluded)
+  std::vector<int> rowptr, colidx;
+  int64_t nnz = 0;
+  // output space: [F | Q | dFdxdVp | dQdxdVp] (n_unknowns+1 each) then dFdx, dQdx (nnz each)
+  int64_t n_out = 0, n_vec_out = 0;
+  int64_t n_terms = 0;
+  // fixed-order reduction: red_ptr[o]..red_ptr[o+1] are the term indices
+  // summed, in reference order, into output o
+  std::vector<int64_t> red_ptr;
+  std::vector<uint32_t> red_idx;
+};
+
+// setup.cpp
+// params_only: stop after the per-instance parameter blocks (no numbering,
+// pattern or term plan).
+int build_plan(const xg_netlist *nl, const xg_device_options *opt, Plan *plan, std::string *err,
+               bool params_only = false);
+
+// load_kernels.cu (two builds: bit-exact and FMA-contracted)
+namespace exact {
+int launch_eval(int dev_type, const DevType &t, const DevOptions &o, const Flags &f,
+                const LoadIO &io, void *stream);
+int launch_reduce(const double *terms, const int64_t *red_ptr, const uint32_t *red_idx,
+                  double *out, int64_t o0, int64_t o1, void *stream);
+}  // namespace exact
+namespace fast {
+int launch_eval(int dev_type, const DevType &t, const DevOptions &o, const Flags &f,
+                const LoadIO &io, void *stream);
+int launch_reduce(const double *terms, const int64_t *red_ptr, const uint32_t *red_idx,
+                  double *out, int64_t o0, int64_t o1, void *stream);
+}  // namespace fast
+
+}  // namespace xg

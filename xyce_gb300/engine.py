@@ -1,0 +1,219 @@
+"""Python host API over libxg's C ABI (include/xg.h).
+
+Mirrors the reference's load interface: a `Circuit` is the set of device
+Masters of one netlist, `update_state` / `load_dae_vectors` /
+`load_dae_matrices` are Device::updateState / loadDAEVectors /
+loadDAEMatrices, and `load` runs all three.  Every call goes to the CUDA
+engine; there is no CPU fallback — a missing library or GPU raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libxg.so")
+_lib = None
+
+
+class XgError(RuntimeError):
+    def __init__(self, status, msg=""):
+        self.status = status
+        super().__init__(f"{abi.STATUS.get(status, status)}: {msg}")
+
+
+def lib():
+    """Load libxg.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"libxg.so not built ({LIB_PATH}); run python -m xyce_gb300.build")
+    L = C.CDLL(LIB_PATH)
+    vp, i, i64p = C.c_void_p, C.c_int, C.POINTER(C.c_int64)
+    L.xg_abi_version.restype = i
+    L.xg_last_error.restype = C.c_char_p
+    L.xg_status_string.restype = C.c_char_p
+    L.xg_status_string.argtypes = [i]
+    L.xg_ctx_create.argtypes = [i, C.POINTER(vp)]
+    L.xg_ctx_destroy.argtypes = [vp]
+    L.xg_ctx_set_options.argtypes = [vp, C.POINTER(abi.XgDeviceOptions)]
+    L.xg_ctx_get_options.argtypes = [vp, C.POINTER(abi.XgDeviceOptions)]
+    L.xg_ctx_synchronize.argtypes = [vp]
+    L.xg_ctx_stream.argtypes = [vp, C.POINTER(vp)]
+    L.xg_circuit_create.argtypes = [vp, C.POINTER(abi.XgNetlist), C.POINTER(vp)]
+    L.xg_circuit_destroy.argtypes = [vp]
+    L.xg_circuit_get_info.argtypes = [vp, C.POINTER(abi.XgCircuitInfo)]
+    L.xg_circuit_get_pattern.argtypes = [vp, vp, vp]
+    L.xg_circuit_get_params.argtypes = [vp, i, vp, C.POINTER(i), C.POINTER(i)]
+    L.xg_setup_params.argtypes = [C.POINTER(abi.XgNetlist), C.POINTER(abi.XgDeviceOptions), i, vp,
+                                  C.POINTER(i), C.POINTER(i)]
+    L.xg_vec_size.argtypes = [vp, i, i64p]
+    L.xg_vec_upload.argtypes = [vp, i, vp]
+    L.xg_vec_download.argtypes = [vp, i, vp]
+    L.xg_vec_device_ptr.argtypes = [vp, i, C.POINTER(vp)]
+    L.xg_rotate_history.argtypes = [vp]
+    L.xg_update_state.argtypes = [vp, C.POINTER(abi.XgLoadFlags)]
+    L.xg_load_dae_vectors.argtypes = [vp]
+    L.xg_load_dae_matrices.argtypes = [vp]
+    L.xg_load.argtypes = [vp, C.POINTER(abi.XgLoadFlags)]
+    _lib = L
+    return L
+
+
+def check(rc):
+    if rc != 0:
+        raise XgError(rc, lib().xg_last_error().decode())
+    return rc
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def setup_params(netlist, dev_type, options=None):
+    """Host-only setup: the derived parameter block of one device type,
+    shape (n_params, n_instances) (include/xg_params.h)."""
+    nl = netlist if isinstance(netlist, abi.XgNetlist) else netlist.to_c()
+    opt = options or abi.device_options()
+    npar, ninst = C.c_int(), C.c_int()
+    check(lib().xg_setup_params(C.byref(nl), C.byref(opt), dev_type, None, C.byref(npar),
+                                C.byref(ninst)))
+    out = np.zeros(max(1, npar.value * ninst.value))
+    check(lib().xg_setup_params(C.byref(nl), C.byref(opt), dev_type, _ptr(out), C.byref(npar),
+                                C.byref(ninst)))
+    return out[: npar.value * ninst.value].reshape(npar.value, ninst.value)
+
+
+class Context:
+    """One GPU and one CUDA stream (the DeviceMgr of one simulation)."""
+
+    def __init__(self, device=0, options=None):
+        h = C.c_void_p()
+        check(lib().xg_ctx_create(device, C.byref(h)))
+        self.h = h
+        if options is not None:
+            self.set_options(options)
+
+    def set_options(self, options):
+        check(lib().xg_ctx_set_options(self.h, C.byref(options)))
+
+    def synchronize(self):
+        check(lib().xg_ctx_synchronize(self.h))
+
+    def stream(self):
+        s = C.c_void_p()
+        check(lib().xg_ctx_stream(self.h, C.byref(s)))
+        return s.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().xg_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Circuit:
+    """A netlist set up on the GPU: parameters, numbering, pattern, load plan."""
+
+    def __init__(self, ctx, netlist):
+        self.ctx = ctx
+        self._nl = netlist.to_c()
+        h = C.c_void_p()
+        check(lib().xg_circuit_create(ctx.h, C.byref(self._nl), C.byref(h)))
+        self.h = h
+        info = abi.XgCircuitInfo()
+        check(lib().xg_circuit_get_info(h, C.byref(info)))
+        self.info = info
+        self.n_unknowns, self.n_state, self.n_store = info.n_unknowns, info.n_state, info.n_store
+        self.nnz = info.nnz
+        self.rowptr = np.zeros(self.n_unknowns + 1, np.int32)
+        self.colidx = np.zeros(max(1, self.nnz), np.int32)
+        check(lib().xg_circuit_get_pattern(h, _ptr(self.rowptr), _ptr(self.colidx)))
+        self.colidx = self.colidx[: self.nnz]
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().xg_circuit_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self, dev_type):
+        npar, ninst = C.c_int(), C.c_int()
+        check(lib().xg_circuit_get_params(self.h, dev_type, None, C.byref(npar), C.byref(ninst)))
+        out = np.zeros(max(1, npar.value * ninst.value))
+        check(lib().xg_circuit_get_params(self.h, dev_type, _ptr(out), None, None))
+        return out[: npar.value * ninst.value].reshape(npar.value, ninst.value)
+
+    def vec_size(self, vec_id):
+        n = C.c_int64()
+        check(lib().xg_vec_size(self.h, vec_id, C.byref(n)))
+        return n.value
+
+    def upload(self, vec_id, values):
+        a = np.ascontiguousarray(values, dtype=np.float64)
+        if a.size != self.vec_size(vec_id):
+            raise ValueError(f"vector {vec_id}: expected {self.vec_size(vec_id)} values, got {a.size}")
+        check(lib().xg_vec_upload(self.h, vec_id, _ptr(a)))
+
+    def download(self, vec_id):
+        a = np.zeros(self.vec_size(vec_id))
+        if a.size:
+            check(lib().xg_vec_download(self.h, vec_id, _ptr(a)))
+        return a
+
+    def device_ptr(self, vec_id):
+        p = C.c_void_p()
+        check(lib().xg_vec_device_ptr(self.h, vec_id, C.byref(p)))
+        return p.value
+
+    def rotate_history(self):
+        check(lib().xg_rotate_history(self.h))
+
+    def update_state(self, flags):
+        check(lib().xg_update_state(self.h, C.byref(flags)))
+
+    def load_dae_vectors(self):
+        check(lib().xg_load_dae_vectors(self.h))
+
+    def load_dae_matrices(self):
+        check(lib().xg_load_dae_matrices(self.h))
+
+    def load(self, flags):
+        check(lib().xg_load(self.h, C.byref(flags)))
+
+    def set_state(self, sol, sta, sto):
+        """sol/sta/sto: (next, curr, last) host vectors; sto next = previous iterate."""
+        for k, vid in enumerate((abi.VEC_SOL_NEXT, abi.VEC_SOL_CURR, abi.VEC_SOL_LAST)):
+            self.upload(vid, sol[k])
+        for k, vid in enumerate((abi.VEC_STA_NEXT, abi.VEC_STA_CURR, abi.VEC_STA_LAST)):
+            if self.n_state:
+                self.upload(vid, sta[k])
+        for k, vid in enumerate((abi.VEC_STO_NEXT, abi.VEC_STO_CURR, abi.VEC_STO_LAST)):
+            if self.n_store:
+                self.upload(vid, sto[k])
+
+    def outputs(self):
+        """F, Q, dFdxdVp, dQdxdVp (ground row dropped), next sta/sto, dFdx/dQdx values."""
+        n = self.n_unknowns
+        out = {
+            "F": self.download(abi.VEC_F)[:n], "Q": self.download(abi.VEC_Q)[:n],
+            "dFdxdVp": self.download(abi.VEC_DFDXDVP)[:n],
+            "dQdxdVp": self.download(abi.VEC_DQDXDVP)[:n],
+            "sta_next": self.download(abi.VEC_STA_NEXT), "sto_next": self.download(abi.VEC_STO_NEXT),
+            "dFdx": self.download(abi.VEC_DFDX), "dQdx": self.download(abi.VEC_DQDX),
+        }
+        out["rows"] = np.repeat(np.arange(n, dtype=np.int32), np.diff(self.rowptr))
+        out["cols"] = self.colidx.copy()
+        return out
