@@ -1,0 +1,405 @@
+"""Benchmark of the Newton load: device loads per second on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl xg|reference]
+                    [--workload single_load_mos1_1M] [--fma]
+
+A step is one Newton load (Device::updateState + loadDAEVectors +
+loadDAEMatrices for every instance) of the whole workload with inputs already
+resident in HBM; value = device instances loaded per second.  e2e is the same
+metric through the C ABI with host buffers: each step uploads the solution
+vector from pinned host memory, loads, and reads F, Q, dFdxdVp, dQdxdVp, dF/dx
+and dQ/dx back.  Inputs (parameter blocks alone are ~300 MB) exceed the
+129 MB L2, so no flush is needed between steps.
+
+--impl reference times the CPU restatement of the reference's load loops
+(the oracle; the reference's own sources are not available where this runs)
+on all host cores, on the same workload, one process per core over an equal
+share of the instances.
+
+Under torchrun (--gpus N > 1) every rank loads its own replica of the workload
+(the load of independent circuits does not exchange data): weak scaling,
+value = instances of all ranks / max rank time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+from xyce_gb300 import abi, netlists  # noqa: E402
+
+# Per-instance algorithmic bytes of one load, by device type: the parameter
+# block and LIDs the kernel reads, plus state/store history read and written
+# (MOSFET1: 14 doubles read, 13 written; diode: 2 read, 1 written; capacitor:
+# 1 written).  Solution reads and output writes are counted once per node /
+# non-zero in load_bytes().
+HIST_BYTES = {abi.DEV_MOS1: 27 * 8, abi.DEV_DIODE: 3 * 8, abi.DEV_CAP: 8, abi.DEV_RES: 0,
+              abi.DEV_VSRC: 0}
+NPARAMS = {abi.DEV_RES: 1, abi.DEV_CAP: 1, abi.DEV_VSRC: 8, abi.DEV_DIODE: 19, abi.DEV_MOS1: 37}
+NLID = {abi.DEV_RES: 2, abi.DEV_CAP: 2, abi.DEV_VSRC: 3, abi.DEV_DIODE: 3, abi.DEV_MOS1: 6}
+
+WORKLOADS = {
+    # config-2 shape (1,000,000 MOSFETs, half NMOS / half PMOS, W~U[0.2,10]um,
+    # L~U[0.1,1]um, random 250k-node netlist, node voltages U[0,1.8]V) on the
+    # level-1 model
+    "single_load_mos1_1M": dict(kind="random", n_dev=1_000_000, n_nodes=250_000,
+                                dev_type=abi.DEV_MOS1),
+    "single_load_mos1_100k": dict(kind="random", n_dev=100_000, n_nodes=25_000,
+                                  dev_type=abi.DEV_MOS1),
+    "power_grid_200x200": dict(kind="grid"),
+}
+METRIC = "device-loads/sec"
+
+
+def build_workload(name):
+    w = WORKLOADS[name]
+    if w["kind"] == "random":
+        nl = netlists.random_mos_netlist(w["n_dev"], w["n_nodes"], dev_type=w["dev_type"], seed=2)
+    else:
+        nl = netlists.power_grid(200, 200, 40000, seed=0)
+    return nl
+
+
+def n_instances(nl):
+    return sum(nl.count(t) for t in range(abi.NUM_DEV_TYPES))
+
+
+def load_bytes(nl, n_unknowns, nnz):
+    b = 0
+    for t in range(abi.NUM_DEV_TYPES):
+        n = nl.count(t)
+        if n:
+            b += n * (NPARAMS[t] * 8 + NLID[t] * 4 + HIST_BYTES[t])
+    b += 8 * (n_unknowns + 1)                 # solution read
+    b += 4 * 8 * (n_unknowns + 1)             # F, Q, dFdxdVp, dQdxdVp written
+    b += 2 * 8 * nnz                          # dF/dx, dQ/dx values written
+    return b
+
+
+def eval_bytes(nl, n_unknowns):
+    b = 8 * (n_unknowns + 1)
+    for t in range(abi.NUM_DEV_TYPES):
+        n = nl.count(t)
+        if n:
+            b += n * (NPARAMS[t] * 8 + NLID[t] * 4 + HIST_BYTES[t])
+    return b
+
+
+def measured_peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 6:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[2:6]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "xg" else "gloo"
+        if args.impl == "xg":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return world, rank, local, dist
+
+
+def cpu_baseline_sample(nl, params, opt, seconds=10.0):
+    """The oracle on one core over a bounded sample of the workload."""
+    from oracle.oracle import OracleCircuit
+    oc = OracleCircuit(nl, params, opt)
+    sol, sta, sto = netlists.random_state(oc.n_unknowns, oc.n_state, oc.n_store, seed=9)
+    flags = abi.load_flags(transient=1, newton_iter=1, pdt=1e11)
+    done = 0
+    scratch = None
+    t0 = time.perf_counter()
+    chunk = 20000
+    types = [t for t in range(abi.NUM_DEV_TYPES) if nl.count(t)]
+    while time.perf_counter() - t0 < seconds:
+        for t in types:
+            n = nl.count(t)
+            i0 = done % n
+            i1 = min(n, i0 + chunk)
+            scratch = oc.load_range_timed(flags, sol, sta, sto, t, i0, i1, scratch)
+            done += i1 - i0
+    dt = time.perf_counter() - t0
+    oc.close()
+    return done / dt, done
+
+
+def _ref_worker(args):
+    """One host process of the reference arm: loads instances [i0, i1)."""
+    name, i0, i1, steps, warmup = args
+    from xyce_gb300 import engine
+    from oracle.oracle import OracleCircuit
+    nl = build_workload(name)
+    opt = abi.device_options()
+    params = {t: engine.setup_params(nl, t, opt) for t in range(abi.NUM_DEV_TYPES) if nl.count(t)}
+    oc = OracleCircuit(nl, params, opt)
+    sol, sta, sto = netlists.random_state(oc.n_unknowns, oc.n_state, oc.n_store, seed=9)
+    flags = abi.load_flags(transient=1, newton_iter=1, pdt=1e11)
+    t = [t for t in range(abi.NUM_DEV_TYPES) if nl.count(t)][0]
+    scratch = None
+    times = []
+    for k in range(warmup + steps):
+        t0 = time.perf_counter()
+        scratch = oc.load_range_timed(flags, sol, sta, sto, t, i0, i1, scratch)
+        if k >= warmup:
+            times.append(time.perf_counter() - t0)
+    return times
+
+
+def run_reference(args, world, rank):
+    """CPU arm: the oracle port on all host cores (rank 0 only)."""
+    if rank != 0:
+        return 0
+    import multiprocessing as mp
+    nl = build_workload(args.workload)
+    types = [t for t in range(abi.NUM_DEV_TYPES) if nl.count(t)]
+    if len(types) != 1:
+        print(json.dumps({"impl": "reference", "unavailable": "reference arm supports single-type workloads"}))
+        return 0
+    n = nl.count(types[0])
+    cores = os.cpu_count() or 1
+    # a bounded sample: each process loads its share of at most 2M instances
+    sample = min(n, 2_000_000)
+    bounds = np.linspace(0, sample, cores + 1).astype(int)
+    jobs = [(args.workload, int(bounds[k]), int(bounds[k + 1]), args.steps, args.warmup)
+            for k in range(cores) if bounds[k + 1] > bounds[k]]
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(len(jobs)) as pool:
+        res = pool.map(_ref_worker, jobs)
+    per_step = np.max(np.array(res), axis=0)       # slowest process per step
+    t = float(np.mean(per_step))
+    value = sample / t
+    line = {"metric": METRIC, "value": value, "unit": "instances/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3 * n / sample,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)", "impl": "reference",
+            "config": {"workload": args.workload, "instances": n, "sample_instances": sample},
+            "cpu_baseline": {"value": value, "unit": "instances/s", "cores": len(jobs),
+                             "kind": "port",
+                             "sample": f"{sample} of {n} instances per step, {len(jobs)} processes"},
+            "e2e": {"value": value, "unit": "instances/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_xg(args, world, rank, local, dist):
+    import ctypes as C
+
+    import torch
+
+    from xyce_gb300 import engine
+
+    torch.cuda.set_device(local)
+    nl = build_workload(args.workload)
+    opt = abi.device_options(fma=1 if args.fma else 0)
+    ctx = engine.Context(local, opt)
+    t_setup = time.perf_counter()
+    c = engine.Circuit(ctx, nl)
+    t_setup = time.perf_counter() - t_setup
+    sol, sta, sto = netlists.random_state(c.n_unknowns, c.n_state, c.n_store, seed=9)
+    c.set_state(sol, sta, sto)
+    flags = abi.load_flags(transient=1, newton_iter=1, pdt=1e11)
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=local)
+    n_inst = n_instances(nl)
+    n_types = sum(1 for t in range(abi.NUM_DEV_TYPES) if nl.count(t))
+
+    for _ in range(args.warmup):
+        c.update_state(flags)
+        c.load_dae_vectors()
+        c.load_dae_matrices()
+    ctx.synchronize()
+
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            ev[k][0].record(stream)
+            c.update_state(flags)
+            ev[k][1].record(stream)
+            c.load_dae_vectors()
+            c.load_dae_matrices()
+            ev[k][2].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    eval_ms = [ev[k][0].elapsed_time(ev[k][1]) for k in range(args.steps)]
+    red_ms = [ev[k][1].elapsed_time(ev[k][2]) for k in range(args.steps)]
+    step_ms = float(np.mean([a + b for a, b in zip(eval_ms, red_ms)]))
+    step_s = step_ms / 1e3
+    if dist:
+        tt = torch.tensor([step_s], device=f"cuda:{local}")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        step_s = float(tt.item())
+    value = world * n_inst / step_s
+
+    # e2e through the C ABI with host buffers.
+    host_sol = torch.empty(c.n_unknowns + 1, dtype=torch.float64, pin_memory=True)
+    host_sol.copy_(torch.from_numpy(sol[0]))
+    outs = {vid: torch.empty(c.vec_size(vid), dtype=torch.float64, pin_memory=True)
+            for vid in (abi.VEC_F, abi.VEC_Q, abi.VEC_DFDXDVP, abi.VEC_DQDXDVP, abi.VEC_DFDX,
+                        abi.VEC_DQDX)}
+    L = engine.lib()
+    h2d = 8 * (c.n_unknowns + 1)
+    d2h = sum(8 * t.numel() for t in outs.values())
+
+    def e2e_step():
+        engine.check(L.xg_vec_upload(c.h, abi.VEC_SOL_NEXT, C.c_void_p(host_sol.data_ptr())))
+        c.load(flags)
+        for vid, t in outs.items():
+            engine.check(L.xg_vec_download(c.h, vid, C.c_void_p(t.data_ptr())))
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if dist:
+        tt = torch.tensor([e2e_s], device=f"cuda:{local}")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+
+    if rank != 0:
+        c.close()
+        return 0
+
+    hbm, peak_kind = measured_peaks()
+    ev_ms = float(np.mean(eval_ms))
+    rd_ms = float(np.mean(red_ms))
+    b_load = load_bytes(nl, c.n_unknowns, c.nnz)
+    b_eval = eval_bytes(nl, c.n_unknowns)
+    b_red = 4 * 8 * (c.n_unknowns + 1) + 2 * 8 * c.nnz
+    dom = "eval" if ev_ms >= rd_ms else "reduce"
+    ach = (b_eval / (ev_ms / 1e3) if dom == "eval" else b_red / (rd_ms / 1e3)) / 1e9
+    traffic = None
+    prof = os.path.join(HERE, "profiles", "traffic.json")
+    if os.path.exists(prof):
+        with open(prof) as f:
+            traffic = json.load(f).get(args.workload, {}).get(dom)
+    params = {t: c.params(t) for t in range(abi.NUM_DEV_TYPES) if nl.count(t)}
+    c.close()
+    cpu_v, cpu_n = cpu_baseline_sample(nl, params, opt, seconds=args.cpu_seconds)
+    clk = clocks.summary()
+    line = {
+        "metric": METRIC, "value": value, "unit": "instances/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded random netlist and node voltages)",
+        "config": {"workload": args.workload, "instances": n_inst, "unknowns": c.n_unknowns,
+                   "nnz": c.nnz, "fma": bool(args.fma),
+                   "l2": "inputs larger than L2 (parameter blocks alone exceed 129 MB)",
+                   "setup_s": round(t_setup, 3)},
+        "kernels_ms": {"eval": ev_ms, "reduce": rd_ms},
+        "roofline": {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": hbm,
+                     "unit": "GB/s", "frac": ach / hbm, "traffic": traffic,
+                     "peak_source": peak_kind,
+                     "algorithmic_bytes": b_eval if dom == "eval" else b_red},
+        "roofline_load": {"achieved": b_load / step_s / 1e9, "unit": "GB/s",
+                          "frac": b_load / step_s / 1e9 / hbm, "algorithmic_bytes": b_load},
+        "e2e": {"value": world * n_inst / e2e_s, "unit": "instances/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": args.steps * (n_types + 2),
+        "clocks": clk,
+        "cpu_baseline": {"value": cpu_v, "unit": "instances/s", "cores": 1, "kind": "port",
+                         "sample": f"{cpu_n} instance loads in ~{args.cpu_seconds:.0f} s, one core"},
+        "wall_s": wall,
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="xg", choices=["xg", "reference"])
+    ap.add_argument("--workload", default="single_load_mos1_1M", choices=sorted(WORKLOADS))
+    ap.add_argument("--fma", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    args = ap.parse_args()
+    world, rank, local, dist = dist_setup(args)
+    if args.impl == "reference":
+        rc = run_reference(args, world, rank)
+    else:
+        rc = run_xg(args, world, rank, local, dist)
+    if dist:
+        dist.destroy_process_group()
+    return rc
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -156,6 +156,7 @@ typedef struct {
   int inputop;
   double pdt;                 /* alpha / h of the integrator */
   double time;                /* current time [s], for PULSE sources */
+  int init_tran;              /* first transient step (SolverState::initTranFlag) */
 } xg_load_flags;
 
 /* ---- vector ids ------------------------------------------------------------ */

@@ -71,6 +71,44 @@ enum xg_diode_param {
   XG_D_NPARAMS
 };
 
+/* BSIM3 v3.2 — N_DEV_MOSFET_B3.C.  Columns 0..XG_B3_NRAW-1 are reference
+ * members: the instance's SizeDependParam (updateTemperature :3736-4470), the
+ * model constants the evaluation reads (Model::processParams :8488-8570) and
+ * the instance temperature values (:3639-3727, :4472-4511).  The columns after
+ * XG_B3_NRAW are instance constants the evaluation would otherwise recompute
+ * at every load, formed on the host by the same expressions. */
+enum xg_b3_param {
+  /* model */
+  XG_B3_DTYPE = 0, XG_B3_MOBMOD, XG_B3_CAPMOD, XG_B3_XPART, XG_B3_TOX, XG_B3_COX,
+  XG_B3_FACTOR1, XG_B3_VCRIT, XG_B3_NJ, XG_B3_IJTH, XG_B3_MJ, XG_B3_MJSW, XG_B3_MJSWG,
+  XG_B3_TNOM,
+  /* instance temperature / geometry */
+  XG_B3_TEMP, XG_B3_VTM, XG_B3_JSTEMP, XG_B3_JSWTEMP, XG_B3_CJTEMP, XG_B3_CJSWTEMP,
+  XG_B3_CJSWGTEMP, XG_B3_PHIB, XG_B3_PHIBSW, XG_B3_PHIBSWG, XG_B3_VJSM, XG_B3_ISEVJSM,
+  XG_B3_VJDM, XG_B3_ISEVJDM, XG_B3_AD, XG_B3_AS, XG_B3_PD, XG_B3_PS, XG_B3_GD, XG_B3_GS,
+  XG_B3_M, XG_B3_FLAGS /* bit0 OFF */,
+  /* SizeDependParam */
+  XG_B3_VTH0, XG_B3_VBSC, XG_B3_PHI, XG_B3_PHIS3, XG_B3_SQRTPHI, XG_B3_XDEP0, XG_B3_LEFF,
+  XG_B3_WEFF, XG_B3_VBI, XG_B3_DVT0, XG_B3_DVT1, XG_B3_DVT2, XG_B3_DVT0W, XG_B3_DVT1W,
+  XG_B3_DVT2W, XG_B3_NLX, XG_B3_K1, XG_B3_K1OX, XG_B3_K2OX, XG_B3_K3, XG_B3_K3B, XG_B3_KT1,
+  XG_B3_KT1L, XG_B3_KT2, XG_B3_W0, XG_B3_ETA0, XG_B3_ETAB, XG_B3_THETA0VB0, XG_B3_NFACTOR,
+  XG_B3_CDSC, XG_B3_CDSCB, XG_B3_CDSCD, XG_B3_CIT, XG_B3_VFB, XG_B3_NGATE, XG_B3_VOFF,
+  XG_B3_CDEP0, XG_B3_DWG, XG_B3_DWB, XG_B3_PRWG, XG_B3_PRWB, XG_B3_RDS0, XG_B3_XJ, XG_B3_A0,
+  XG_B3_B0, XG_B3_B1, XG_B3_AGS, XG_B3_KETA, XG_B3_UA, XG_B3_UB, XG_B3_UC, XG_B3_U0TEMP,
+  XG_B3_VSATTEMP, XG_B3_A1, XG_B3_A2, XG_B3_DELTA, XG_B3_PCLM, XG_B3_LITL, XG_B3_THETAROUT,
+  XG_B3_PDIBLB, XG_B3_PVAG, XG_B3_PSCBE1, XG_B3_PSCBE2, XG_B3_ALPHA0, XG_B3_ALPHA1,
+  XG_B3_BETA0, XG_B3_VFBCV, XG_B3_WEFFCV, XG_B3_LEFFCV, XG_B3_ABULKCVFACTOR, XG_B3_NOFF,
+  XG_B3_VOFFCV, XG_B3_VFBZB, XG_B3_ACDE, XG_B3_LDEB, XG_B3_MOIN, XG_B3_CGDO, XG_B3_CGSO,
+  XG_B3_CGBO, XG_B3_CKAPPA, XG_B3_CGDL, XG_B3_CGSL,
+  XG_B3_NRAW,
+  /* instance constants hoisted out of the per-load evaluation */
+  XG_B3_SSAT = XG_B3_NRAW,  /* SourceSatCurrent                        */
+  XG_B3_DSAT,               /* DrainSatCurrent                         */
+  XG_B3_NVTM,               /* vtm * NJ                                */
+  XG_B3_CZBD, XG_B3_CZBS, XG_B3_CZBDSW, XG_B3_CZBDSWG, XG_B3_CZBSSW, XG_B3_CZBSSWG,
+  XG_B3_NPARAMS
+};
+
 /* Linear elements: one value each. */
 enum xg_res_param { XG_R_G = 0, XG_R_NPARAMS };          /* 1/R       */
 enum xg_cap_param { XG_C_C = 0, XG_C_NPARAMS };          /* C         */

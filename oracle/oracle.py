@@ -79,7 +79,10 @@ class OracleCircuit:
         lib().xgo_reset_members(self.h)
 
     def _inputs(self, sol, sta, sto):
-        ins = [np.ascontiguousarray(v, np.float64) for v in list(sol) + list(sta) + list(sto)]
+        # copies: a BSIM3 load on the first transient step writes the current
+        # state vector (N_DEV_MOSFET_B3.C:9264-9278), which must not reach the
+        # caller's arrays
+        ins = [np.array(v, dtype=np.float64, copy=True) for v in list(sol) + list(sta) + list(sto)]
         ins = [v if v.size else np.zeros(1) for v in ins]
         return ins, (C.c_void_p * 9)(*[_ptr(a) for a in ins])
 

@@ -492,7 +492,7 @@ int xref_params(XRef *x, int type, double *out, int *n_params) {
     if (e.type != type) continue;
     const int n = (int)e.inst.size();
     for (int i = 0; i < n; ++i) {
-      double v[64] = {0};
+      double v[256] = {0};
       int np = 0;
       if (type == XG_DEV_MOS1) {
         MOSFET1::Instance &m = *static_cast<MOSFET1::Instance *>(e.inst[i]);
@@ -569,6 +569,145 @@ int xref_params(XRef *x, int type, double *out, int *n_params) {
       } else if (type == XG_DEV_CAP) {
         np = XG_C_NPARAMS;
         v[XG_C_C] = static_cast<Capacitor::Instance *>(e.inst[i])->C;
+      } else if (type == XG_DEV_BSIM3) {
+        // Raw columns only (0..XG_B3_NRAW-1); the hoisted constants after
+        // them are checked through the load results.
+        MOSFET_B3::Instance &b = *static_cast<MOSFET_B3::Instance *>(e.inst[i]);
+        const MOSFET_B3::Model &mo = b.model_;
+        const MOSFET_B3::SizeDependParam &p = *b.paramPtr;
+        np = XG_B3_NRAW;
+        v[XG_B3_DTYPE] = mo.dtype;
+        v[XG_B3_MOBMOD] = mo.mobMod;
+        v[XG_B3_CAPMOD] = mo.capMod;
+        v[XG_B3_XPART] = mo.xpart;
+        v[XG_B3_TOX] = mo.tox;
+        v[XG_B3_COX] = mo.cox;
+        v[XG_B3_FACTOR1] = mo.factor1;
+        v[XG_B3_VCRIT] = mo.vcrit;
+        v[XG_B3_NJ] = mo.jctEmissionCoeff;
+        v[XG_B3_IJTH] = mo.ijth;
+        v[XG_B3_MJ] = mo.bulkJctBotGradingCoeff;
+        v[XG_B3_MJSW] = mo.bulkJctSideGradingCoeff;
+        v[XG_B3_MJSWG] = mo.bulkJctGateSideGradingCoeff;
+        v[XG_B3_TNOM] = mo.tnom;
+        v[XG_B3_TEMP] = b.temp;
+        v[XG_B3_VTM] = b.vtm;
+        v[XG_B3_JSTEMP] = b.jctTempSatCurDensity;
+        v[XG_B3_JSWTEMP] = b.jctSidewallTempSatCurDensity;
+        v[XG_B3_CJTEMP] = b.unitAreaJctCapTemp;
+        v[XG_B3_CJSWTEMP] = b.unitLengthSidewallJctCapTemp;
+        v[XG_B3_CJSWGTEMP] = b.unitLengthGateSidewallJctCapTemp;
+        v[XG_B3_PHIB] = b.PhiBTemp;
+        v[XG_B3_PHIBSW] = b.PhiBSWTemp;
+        v[XG_B3_PHIBSWG] = b.PhiBSWGTemp;
+        v[XG_B3_VJSM] = b.vjsm;
+        v[XG_B3_ISEVJSM] = b.IsEvjsm;
+        v[XG_B3_VJDM] = b.vjdm;
+        v[XG_B3_ISEVJDM] = b.IsEvjdm;
+        v[XG_B3_AD] = b.drainArea;
+        v[XG_B3_AS] = b.sourceArea;
+        v[XG_B3_PD] = b.drainPerimeter;
+        v[XG_B3_PS] = b.sourcePerimeter;
+        v[XG_B3_GD] = b.drainConductance;
+        v[XG_B3_GS] = b.sourceConductance;
+        v[XG_B3_M] = b.numberParallel;
+        v[XG_B3_FLAGS] = b.OFF ? 1 : 0;
+        v[XG_B3_VTH0] = p.vth0;
+        v[XG_B3_VBSC] = p.vbsc;
+        v[XG_B3_PHI] = p.phi;
+        v[XG_B3_PHIS3] = p.phis3;
+        v[XG_B3_SQRTPHI] = p.sqrtPhi;
+        v[XG_B3_XDEP0] = p.Xdep0;
+        v[XG_B3_LEFF] = p.leff;
+        v[XG_B3_WEFF] = p.weff;
+        v[XG_B3_VBI] = p.vbi;
+        v[XG_B3_DVT0] = p.dvt0;
+        v[XG_B3_DVT1] = p.dvt1;
+        v[XG_B3_DVT2] = p.dvt2;
+        v[XG_B3_DVT0W] = p.dvt0w;
+        v[XG_B3_DVT1W] = p.dvt1w;
+        v[XG_B3_DVT2W] = p.dvt2w;
+        v[XG_B3_NLX] = p.nlx;
+        v[XG_B3_K1] = p.k1;
+        v[XG_B3_K1OX] = p.k1ox;
+        v[XG_B3_K2OX] = p.k2ox;
+        v[XG_B3_K3] = p.k3;
+        v[XG_B3_K3B] = p.k3b;
+        v[XG_B3_KT1] = p.kt1;
+        v[XG_B3_KT1L] = p.kt1l;
+        v[XG_B3_KT2] = p.kt2;
+        v[XG_B3_W0] = p.w0;
+        v[XG_B3_ETA0] = p.eta0;
+        v[XG_B3_ETAB] = p.etab;
+        v[XG_B3_THETA0VB0] = p.theta0vb0;
+        v[XG_B3_NFACTOR] = p.nfactor;
+        v[XG_B3_CDSC] = p.cdsc;
+        v[XG_B3_CDSCB] = p.cdscb;
+        v[XG_B3_CDSCD] = p.cdscd;
+        v[XG_B3_CIT] = p.cit;
+        v[XG_B3_VFB] = p.vfb;
+        v[XG_B3_NGATE] = p.ngate;
+        v[XG_B3_VOFF] = p.voff;
+        v[XG_B3_CDEP0] = p.cdep0;
+        v[XG_B3_DWG] = p.dwg;
+        v[XG_B3_DWB] = p.dwb;
+        v[XG_B3_PRWG] = p.prwg;
+        v[XG_B3_PRWB] = p.prwb;
+        v[XG_B3_RDS0] = p.rds0;
+        v[XG_B3_XJ] = p.xj;
+        v[XG_B3_A0] = p.a0;
+        v[XG_B3_B0] = p.b0;
+        v[XG_B3_B1] = p.b1;
+        v[XG_B3_AGS] = p.ags;
+        v[XG_B3_KETA] = p.keta;
+        v[XG_B3_UA] = p.ua;
+        v[XG_B3_UB] = p.ub;
+        v[XG_B3_UC] = p.uc;
+        v[XG_B3_U0TEMP] = p.u0temp;
+        v[XG_B3_VSATTEMP] = p.vsattemp;
+        v[XG_B3_A1] = p.a1;
+        v[XG_B3_A2] = p.a2;
+        v[XG_B3_DELTA] = p.delta;
+        v[XG_B3_PCLM] = p.pclm;
+        v[XG_B3_LITL] = p.litl;
+        v[XG_B3_THETAROUT] = p.thetaRout;
+        v[XG_B3_PDIBLB] = p.pdiblb;
+        v[XG_B3_PVAG] = p.pvag;
+        v[XG_B3_PSCBE1] = p.pscbe1;
+        v[XG_B3_PSCBE2] = p.pscbe2;
+        v[XG_B3_ALPHA0] = p.alpha0;
+        v[XG_B3_ALPHA1] = p.alpha1;
+        v[XG_B3_BETA0] = p.beta0;
+        v[XG_B3_VFBCV] = p.vfbcv;
+        v[XG_B3_WEFFCV] = p.weffCV;
+        v[XG_B3_LEFFCV] = p.leffCV;
+        v[XG_B3_ABULKCVFACTOR] = p.abulkCVfactor;
+        v[XG_B3_NOFF] = p.noff;
+        v[XG_B3_VOFFCV] = p.voffcv;
+        v[XG_B3_VFBZB] = p.vfbzb;
+        v[XG_B3_ACDE] = p.acde;
+        v[XG_B3_LDEB] = p.ldeb;
+        v[XG_B3_MOIN] = p.moin;
+        v[XG_B3_CGDO] = p.cgdo;
+        v[XG_B3_CGSO] = p.cgso;
+        v[XG_B3_CGBO] = p.cgbo;
+        v[XG_B3_CKAPPA] = p.ckappa;
+        v[XG_B3_CGDL] = p.cgdl;
+        v[XG_B3_CGSL] = p.cgsl;
+      } else if (type == XG_DEV_VSRC) {
+        // PulseData / ConstData parameters (N_DEV_SourceData.C:1033-1045, 2065-2070)
+        Vsrc::Instance &s = *static_cast<Vsrc::Instance *>(e.inst[i]);
+        np = XG_V_NPARAMS;
+        double w[16] = {0};
+        if (s.Data_ptr && s.TRANSIENTSOURCETYPE == _PULSE_DATA) {
+          v[XG_V_KIND] = XG_SRC_PULSE;
+          s.Data_ptr->getParams(w);
+          for (int k = 0; k < 7; ++k) v[XG_V_V1 + k] = w[k];
+        } else {
+          v[XG_V_KIND] = XG_SRC_DC;
+          if (s.dcData_ptr) s.dcData_ptr->getParams(w);
+          v[XG_V_V1] = w[0];
+        }
       } else {
         return -1;
       }
@@ -599,6 +738,7 @@ int xref_load(XRef *x, const xg_load_flags *fl, const double *const *in_vecs, do
   ss.inputOPFlag = fl->inputop != 0;
   ss.pdt = fl->pdt;
   ss.currTime = fl->time;
+  ss.initTranFlag = fl->init_tran != 0;
   const int nr = x->n_unknowns + 1;
   for (int i = 0; i < 3; ++i) std::copy(in_vecs[i], in_vecs[i] + nr, x->sol[i].data.begin());
   for (int i = 0; i < 3; ++i)

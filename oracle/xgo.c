@@ -122,7 +122,13 @@ int xgo_build(const xg_netlist *nl, const xg_device_options *opt,
     T->sto0 = sto;
     T->nsta = xgo_nsta(c, t);
     T->nsto = xgo_nsto(t);
-    sta += T->nsta * T->n;
+    if (t == XG_DEV_DIODE) {
+      /* one state slot per diode whose CJO == 0 (N_DEV_Diode.C:392-393);
+       * the load never touches it, it only shifts later types' slots */
+      for (int i = 0; i < T->n; ++i) sta += P(T, XG_D_TJCTCAP, i) == 0.0 ? 1 : 0;
+    } else {
+      sta += T->nsta * T->n;
+    }
     sto += T->nsto * T->n;
   }
   c->n_sta = sta;

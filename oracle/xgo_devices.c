@@ -78,8 +78,9 @@ void xgo_assign_lids(xgo_circuit *c, const xg_netlist *nl, int t, int i, int *ne
 int xgo_nsta(const xgo_circuit *c, int t) {
   switch (t) {
     case XG_DEV_CAP: return 1;
-    case XG_DEV_DIODE: /* N_DEV_Diode.C:392-393: one state slot iff CJO == 0 */
-      return (c->T[t].n && P(&c->T[t], XG_D_TJCTCAP, 0) == 0.0) ? 1 : 0;
+    case XG_DEV_DIODE: /* per instance, counted in xgo_build */
+      (void)c;
+      return 0;
     case XG_DEV_MOS1: return 8;
     case XG_DEV_BSIM3: return 12;
   }

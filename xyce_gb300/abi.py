@@ -65,7 +65,8 @@ class XgDeviceOptions(C.Structure):
 class XgLoadFlags(C.Structure):
     _fields_ = [("dcop", C.c_int), ("tranop", C.c_int), ("acop", C.c_int), ("transient", C.c_int),
                 ("init_jct", C.c_int), ("init_fix", C.c_int), ("newton_iter", C.c_int),
-                ("inputop", C.c_int), ("pdt", C.c_double), ("time", C.c_double)]
+                ("inputop", C.c_int), ("pdt", C.c_double), ("time", C.c_double),
+                ("init_tran", C.c_int)]
 
 
 class XgCircuitInfo(C.Structure):
@@ -79,9 +80,9 @@ def device_options(gmin=1e-12, temp=300.15, tnom=300.15, voltlim=1, newmeyer=0, 
 
 
 def load_flags(dcop=0, tranop=0, acop=0, transient=1, init_jct=0, init_fix=0, newton_iter=1,
-               inputop=0, pdt=0.0, time=0.0):
+               inputop=0, pdt=0.0, time=0.0, init_tran=0):
     return XgLoadFlags(dcop, tranop, acop, transient, init_jct, init_fix, newton_iter, inputop,
-                       pdt, time)
+                       pdt, time, init_tran)
 
 
 def _iarr(a):
@@ -123,6 +124,44 @@ class Netlist:
     def add_model(self, model):
         self.models.append(model)
         return len(self.models) - 1
+
+    _GROUPS = ("res", "cap", "vsrc", "isrc", "diode", "mos1", "bsim3")
+
+    def to_arrays(self):
+        """Flat dict of numpy arrays (for np.savez); inverse of from_arrays."""
+        out = {"n_nodes": np.array(self.n_nodes)}
+        if self.type_order is not None:
+            out["type_order"] = np.asarray(self.type_order, np.int32)
+        for mi, m in enumerate(self.models):
+            out[f"model{mi}.meta"] = np.array([m.type, m.polarity])
+            out[f"model{mi}.names"] = np.array(list(m.params.keys()), dtype="U16")
+            out[f"model{mi}.values"] = np.array(list(m.params.values()), np.float64)
+        for g in self._GROUPS:
+            d = getattr(self, g)
+            if d is None:
+                continue
+            for k, v in d.items():
+                if v is not None:
+                    out[f"{g}.{k}"] = np.asarray(v)
+        return out
+
+    @classmethod
+    def from_arrays(cls, a):
+        nl = cls(int(a["n_nodes"]))
+        if "type_order" in a:
+            nl.type_order = [int(x) for x in a["type_order"]]
+        mi = 0
+        while f"model{mi}.meta" in a:
+            t, pol = (int(x) for x in a[f"model{mi}.meta"])
+            m = Model(t, pol)
+            m.params = {str(k): float(v) for k, v in zip(a[f"model{mi}.names"], a[f"model{mi}.values"])}
+            nl.models.append(m)
+            mi += 1
+        for g in cls._GROUPS:
+            keys = [k for k in a if k.startswith(g + ".")]
+            if keys:
+                setattr(nl, g, {k[len(g) + 1:]: np.array(a[k]) for k in keys})
+        return nl
 
     def count(self, t):
         d = [self.res, self.cap, self.vsrc, self.isrc, self.diode, self.mos1, self.bsim3][t]

@@ -419,7 +419,8 @@ int xg_update_state(xg_circuit *c, const xg_load_flags *flags) {
   xg::Plan &P = c->plan;
   xg::DevOptions o{c->opt.gmin, c->opt.voltlim};
   xg::Flags f{flags->dcop, flags->tranop, flags->acop, flags->transient, flags->init_jct,
-              flags->init_fix, flags->newton_iter, flags->inputop, flags->pdt, flags->time};
+              flags->init_fix, flags->newton_iter, flags->inputop, flags->pdt, flags->time,
+              flags->init_tran};
   xg::LoadIO io{c->d_sol[0], c->d_sta[1], c->d_sto[1], c->d_sta[0], c->d_sto[0], c->d_terms,
                 c->d_diode_vd};
   for (int k = 0; k < P.n_order; ++k) {

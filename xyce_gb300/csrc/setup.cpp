@@ -675,11 +675,16 @@ int build_plan(const xg_netlist *nl, const xg_device_options *opt, Plan *plan, s
     int t = P.order[k];
     TypeData &T = P.T[t];
     if (!T.n) continue;
-    if (t == XG_DEV_DIODE)  // one state slot iff CJO == 0 (N_DEV_Diode.C:392-393)
-      T.nsta = T.params[(size_t)XG_D_TJCTCAP * T.n] == 0.0 ? 1 : 0;
     T.sta0 = sta;
     T.sto0 = sto;
-    sta += T.nsta * T.n;
+    if (t == XG_DEV_DIODE) {
+      // One state slot per diode whose CJO == 0 (N_DEV_Diode.C:392-393).  The
+      // load never reads or writes it; it only shifts the slots that follow.
+      T.nsta = 0;
+      for (int i = 0; i < T.n; ++i) sta += T.params[(size_t)XG_D_TJCTCAP * T.n + i] == 0.0 ? 1 : 0;
+    } else {
+      sta += T.nsta * T.n;
+    }
     sto += T.nsto * T.n;
   }
   P.n_state = sta;

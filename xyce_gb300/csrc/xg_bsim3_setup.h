@@ -1,6 +1,7 @@
 // xg_bsim3_setup.h — BSIM3 v3.2 host setup interface (bsim3_setup.cpp).
 #pragma once
 
+#include <map>
 #include <string>
 
 #include "xg.h"
@@ -8,12 +9,22 @@
 
 namespace xg {
 
-// Per-instance parameter block width for BSIM3 (see bsim3_setup.cpp for the
-// column meanings).
-enum { XG_B3_NPARAMS = 1 };
+enum { XG_B3_NPARAMS_ = XG_B3_NPARAMS };
 
+// A BSIM3 model card after Model::Model and Model::processParams
+// (N_DEV_MOSFET_B3.C:8488-8570, 8603-9105): every parameter by its netlist
+// name, the given flags, and the derived model constants.
 struct B3Model {
   int dtype = 1;
+  std::map<std::string, double> v;   // every parameter, defaults filled in
+  std::map<std::string, bool> given;
+  bool g(const char *k) const {
+    auto it = given.find(k);
+    return it != given.end() && it->second;
+  }
+  double operator[](const char *k) const { return v.at(k); }
+  // processParams outputs
+  double cox = 0, vcrit = 0, factor1 = 0, Vtm0 = 0, Eg0 = 0, ni = 0, tnom = 0;
 };
 
 int b3_nlid();

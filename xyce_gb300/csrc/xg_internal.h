@@ -65,6 +65,7 @@ struct DevOptions {
 struct Flags {
   int dcop, tranop, acop, transient, init_jct, init_fix, newton_iter, inputop;
   double pdt, time;
+  int init_tran;
 };
 
 // Vectors the load kernels read and write (device pointers).

@@ -1,0 +1,142 @@
+"""Seeded synthetic circuits with the shapes of the workloads the engine is
+measured on.  No external netlists or datasets are used; every circuit is
+built from a numpy seed.
+
+  inverter_chain(stages)        1,000-stage CMOS inverter chain, MOSFET level 1
+  random_mos_netlist(n_dev, ...) n MOSFETs (half NMOS, half PMOS) on a random
+                                 node set, W~U[0.2,10]um, L~U[0.1,1]um, for a
+                                 single Newton load with random node voltages
+  power_grid(nx, ny, n_sinks)   resistive mesh with diode-clamped MOSFET sinks
+                                 switched by PULSE sources
+  ring_oscillator(stages, ...)  odd-stage CMOS ring, VTO/KP perturbed
+"""
+import numpy as np
+
+from . import abi
+
+# Level-1 model cards of the inverter-chain workload: NMOS VTO=0.7 KP=110u,
+# PMOS VTO=-0.7 KP=50u (no TOX/CJ given: no gate or junction capacitance).
+NMOS1 = dict(VTO=0.7, KP=110e-6)
+PMOS1 = dict(VTO=-0.7, KP=50e-6)
+
+
+def inverter_chain(stages=1000, cload=10e-15, vdd=1.8, tr=100e-12, per=2e-9):
+    """Nodes: 0 vdd, 1 input, 2.. stage outputs.  PULSE 0->vdd, 50% duty."""
+    n_nodes = stages + 2
+    nl = abi.Netlist(n_nodes)
+    mn = nl.add_model(abi.Model(abi.DEV_MOS1, 1, **NMOS1))
+    mp = nl.add_model(abi.Model(abi.DEV_MOS1, -1, **PMOS1))
+    ins = np.arange(1, stages + 1)
+    outs = np.arange(2, stages + 2)
+    gnd = np.full(stages, -1)
+    vddn = np.zeros(stages, int)
+    nl.mos1 = dict(d=np.r_[outs, outs], g=np.r_[ins, ins], s=np.r_[gnd, vddn], b=np.r_[gnd, vddn],
+                   model=np.r_[np.full(stages, mn), np.full(stages, mp)],
+                   w=np.r_[np.full(stages, 2e-6), np.full(stages, 4e-6)],
+                   l=np.full(2 * stages, 1e-6))
+    # interleave so instance order follows the chain: N0, P0, N1, P1, ...
+    order = np.ravel(np.column_stack([np.arange(stages), np.arange(stages) + stages]))
+    nl.mos1 = {k: np.asarray(v)[order] for k, v in nl.mos1.items()}
+    nl.cap = dict(p=outs, m=gnd, value=np.full(stages, cload))
+    pw = per / 2 - tr
+    nl.vsrc = dict(p=[0, 1], m=[-1, -1], kind=[abi.SRC_DC, abi.SRC_PULSE],
+                   wave=[[vdd, 0, 0, 0, 0, 0, 0], [0.0, vdd, 0.0, tr, tr, pw, per]])
+    nl.type_order = [abi.DEV_VSRC, abi.DEV_MOS1, abi.DEV_CAP, abi.DEV_RES, abi.DEV_ISRC,
+                     abi.DEV_DIODE, abi.DEV_BSIM3]
+    return nl
+
+
+def random_mos_netlist(n_dev, n_nodes, dev_type=abi.DEV_MOS1, seed=0, models=None):
+    """n_dev MOSFETs whose terminals are drawn uniformly from n_nodes nodes
+    (about 4*n_dev/n_nodes attachments per node), first half NMOS, second half
+    PMOS, W~U[0.2,10]um, L~U[0.1,1]um."""
+    rng = np.random.default_rng(seed)
+    nl = abi.Netlist(n_nodes)
+    if models is None:
+        models = (abi.Model(dev_type, 1, **NMOS1), abi.Model(dev_type, -1, **PMOS1))
+    mn, mp = nl.add_model(models[0]), nl.add_model(models[1])
+    term = rng.integers(0, n_nodes, size=(4, n_dev), dtype=np.int64)
+    half = n_dev // 2
+    d = dict(d=term[0], g=term[1], s=term[2], b=term[3],
+             model=np.r_[np.full(half, mn), np.full(n_dev - half, mp)],
+             w=rng.uniform(0.2e-6, 10e-6, n_dev), l=rng.uniform(0.1e-6, 1e-6, n_dev))
+    if dev_type == abi.DEV_MOS1:
+        nl.mos1 = d
+    else:
+        nl.bsim3 = d
+    return nl
+
+
+def power_grid(nx=200, ny=200, n_sinks=40000, seed=0, r_seg=0.1, c_node=1e-15, vdd=1.8):
+    """nx*ny resistive mesh (r_seg per segment, c_node per node) fed by a DC
+    supply at one corner; n_sinks level-1 NMOS current sinks from mesh nodes to
+    ground, each gate driven by its own PULSE source (delay ~U[0,5ns]) and
+    clamped to ground by a diode."""
+    rng = np.random.default_rng(seed)
+    n_mesh = nx * ny
+    n_nodes = n_mesh + 1 + n_sinks          # mesh, supply pin, sink gates
+    supply = n_mesh
+    gates = n_mesh + 1 + np.arange(n_sinks)
+    nl = abi.Netlist(n_nodes)
+    mn = nl.add_model(abi.Model(abi.DEV_MOS1, 1, **NMOS1))
+    dm = nl.add_model(abi.Model(abi.DEV_DIODE, 1, IS=1e-14))
+    idx = np.arange(n_mesh).reshape(ny, nx)
+    h = np.c_[idx[:, :-1].ravel(), idx[:, 1:].ravel()]
+    v = np.c_[idx[:-1, :].ravel(), idx[1:, :].ravel()]
+    seg = np.r_[h, v]
+    nl.res = dict(p=np.r_[seg[:, 0], supply], m=np.r_[seg[:, 1], 0],
+                  value=np.r_[np.full(len(seg), r_seg), r_seg])
+    nl.cap = dict(p=np.arange(n_mesh), m=np.full(n_mesh, -1), value=np.full(n_mesh, c_node))
+    sink_nodes = rng.choice(n_mesh, size=n_sinks, replace=n_sinks > n_mesh)
+    nl.mos1 = dict(d=sink_nodes, g=gates, s=np.full(n_sinks, -1), b=np.full(n_sinks, -1),
+                   model=np.full(n_sinks, mn), w=np.full(n_sinks, 2e-6), l=np.full(n_sinks, 1e-6))
+    nl.diode = dict(a=np.full(n_sinks, -1), c=gates, model=np.full(n_sinks, dm))
+    td = rng.uniform(0, 5e-9, n_sinks)
+    wave = np.zeros((n_sinks + 1, 7))
+    wave[0, 0] = vdd
+    wave[1:, 1] = vdd
+    wave[1:, 2] = td
+    wave[1:, 3] = 100e-12
+    wave[1:, 4] = 100e-12
+    wave[1:, 5] = 0.9e-9
+    wave[1:, 6] = 2e-9
+    nl.vsrc = dict(p=np.r_[supply, gates], m=np.full(n_sinks + 1, -1),
+                   kind=np.r_[abi.SRC_DC, np.full(n_sinks, abi.SRC_PULSE)], wave=wave)
+    return nl
+
+
+def ring_oscillator(stages=5, seed=0, sigma=0.10 / 3, cload=10e-15, vdd=1.8):
+    """Odd-stage CMOS ring; each stage's VTO and KP scaled by (1+d), d~N(0,
+    sigma) truncated at +-10% (a Monte-Carlo variant per seed)."""
+    assert stages % 2 == 1
+    rng = np.random.default_rng(seed)
+    nl = abi.Netlist(stages + 1)          # 0 vdd, 1..stages ring nodes
+    nodes = np.arange(1, stages + 1)
+    nxt = np.roll(nodes, -1)
+    dv = np.clip(rng.normal(0, sigma, (2, stages)), -0.1, 0.1)
+    dk = np.clip(rng.normal(0, sigma, (2, stages)), -0.1, 0.1)
+    mods = []
+    for k in range(stages):
+        mods.append(nl.add_model(abi.Model(abi.DEV_MOS1, 1, VTO=0.7 * (1 + dv[0, k]),
+                                           KP=110e-6 * (1 + dk[0, k]))))
+        mods.append(nl.add_model(abi.Model(abi.DEV_MOS1, -1, VTO=-0.7 * (1 + dv[1, k]),
+                                           KP=50e-6 * (1 + dk[1, k]))))
+    d = np.repeat(nxt, 2)
+    g = np.repeat(nodes, 2)
+    s = np.ravel(np.column_stack([np.full(stages, -1), np.zeros(stages, int)]))
+    nl.mos1 = dict(d=d, g=g, s=s, b=s.copy(), model=np.array(mods),
+                   w=np.tile([2e-6, 4e-6], stages), l=np.full(2 * stages, 1e-6))
+    nl.cap = dict(p=nodes, m=np.full(stages, -1), value=np.full(stages, cload))
+    nl.vsrc = dict(p=[0], m=[-1], kind=[abi.SRC_DC], wave=[[vdd, 0, 0, 0, 0, 0, 0]])
+    return nl
+
+
+def random_state(n_unknowns, n_state, n_store, seed=0, vmax=1.8):
+    """Node voltages i.i.d. U[0, vmax] (next/curr/last) and seeded state/store
+    history: a second draw supplies the previous Newton iterate so the
+    limiters take their limiting branches."""
+    rng = np.random.default_rng(seed)
+    sol = [np.r_[rng.uniform(0.0, vmax, n_unknowns), 0.0] for _ in range(3)]
+    sta = [rng.uniform(0.0, 1e-14, n_state) for _ in range(3)]
+    sto = [rng.uniform(-0.5, vmax, n_store) for _ in range(3)]
+    return sol, sta, sto
