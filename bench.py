@@ -40,13 +40,22 @@ from xyce_gb300 import abi, netlists  # noqa: E402
 # (MOSFET1: 14 doubles read, 13 written; diode: 2 read, 1 written; capacitor:
 # 1 written).  Solution reads and output writes are counted once per node /
 # non-zero in load_bytes().
+# BSIM3: 5 store values of the previous iterate read, 5 store and 5 state
+# values written, 20 members carried between loads read and written.
 HIST_BYTES = {abi.DEV_MOS1: 27 * 8, abi.DEV_DIODE: 3 * 8, abi.DEV_CAP: 8, abi.DEV_RES: 0,
-              abi.DEV_VSRC: 0}
-NPARAMS = {abi.DEV_RES: 1, abi.DEV_CAP: 1, abi.DEV_VSRC: 8, abi.DEV_DIODE: 19, abi.DEV_MOS1: 37}
-NLID = {abi.DEV_RES: 2, abi.DEV_CAP: 2, abi.DEV_VSRC: 3, abi.DEV_DIODE: 3, abi.DEV_MOS1: 6}
+              abi.DEV_VSRC: 0, abi.DEV_BSIM3: 55 * 8}
+NLID = {abi.DEV_RES: 2, abi.DEV_CAP: 2, abi.DEV_VSRC: 3, abi.DEV_DIODE: 3, abi.DEV_MOS1: 6,
+        abi.DEV_BSIM3: 6}
 
 WORKLOADS = {
-    # config-2 shape (1,000,000 MOSFETs, half NMOS / half PMOS, W~U[0.2,10]um,
+    # Single Newton load of 1,000,000 BSIM3 instances (default level-9 model
+    # cards, half NMOS / half PMOS, W~U[0.2,10]um, L~U[0.1,1]um) on a random
+    # 250k-node netlist, node voltages U[0,1.8]V
+    "single_load_bsim3_1M": dict(kind="random", n_dev=1_000_000, n_nodes=250_000,
+                                 dev_type=abi.DEV_BSIM3),
+    "single_load_bsim3_100k": dict(kind="random", n_dev=100_000, n_nodes=25_000,
+                                   dev_type=abi.DEV_BSIM3),
+    # the same shape (1,000,000 MOSFETs, half NMOS / half PMOS, W~U[0.2,10]um,
     # L~U[0.1,1]um, random 250k-node netlist, node voltages U[0,1.8]V) on the
     # level-1 model
     "single_load_mos1_1M": dict(kind="random", n_dev=1_000_000, n_nodes=250_000,
@@ -61,7 +70,11 @@ METRIC = "device-loads/sec"
 def build_workload(name):
     w = WORKLOADS[name]
     if w["kind"] == "random":
-        nl = netlists.random_mos_netlist(w["n_dev"], w["n_nodes"], dev_type=w["dev_type"], seed=2)
+        models = None
+        if w["dev_type"] == abi.DEV_BSIM3:
+            models = (abi.Model(abi.DEV_BSIM3, 1), abi.Model(abi.DEV_BSIM3, -1))
+        nl = netlists.random_mos_netlist(w["n_dev"], w["n_nodes"], dev_type=w["dev_type"], seed=2,
+                                         models=models)
     else:
         nl = netlists.power_grid(200, 200, 40000, seed=0)
     return nl
@@ -71,24 +84,24 @@ def n_instances(nl):
     return sum(nl.count(t) for t in range(abi.NUM_DEV_TYPES))
 
 
-def load_bytes(nl, n_unknowns, nnz):
+def load_bytes(nl, n_unknowns, nnz, nparams):
     b = 0
     for t in range(abi.NUM_DEV_TYPES):
         n = nl.count(t)
         if n:
-            b += n * (NPARAMS[t] * 8 + NLID[t] * 4 + HIST_BYTES[t])
+            b += n * (nparams[t] * 8 + NLID[t] * 4 + HIST_BYTES[t])
     b += 8 * (n_unknowns + 1)                 # solution read
     b += 4 * 8 * (n_unknowns + 1)             # F, Q, dFdxdVp, dQdxdVp written
     b += 2 * 8 * nnz                          # dF/dx, dQ/dx values written
     return b
 
 
-def eval_bytes(nl, n_unknowns):
+def eval_bytes(nl, n_unknowns, nparams):
     b = 8 * (n_unknowns + 1)
     for t in range(abi.NUM_DEV_TYPES):
         n = nl.count(t)
         if n:
-            b += n * (NPARAMS[t] * 8 + NLID[t] * 4 + HIST_BYTES[t])
+            b += n * (nparams[t] * 8 + NLID[t] * 4 + HIST_BYTES[t])
     return b
 
 
@@ -169,9 +182,22 @@ def dist_setup(args):
     return world, rank, local, dist
 
 
-def cpu_baseline_sample(nl, params, opt, seconds=10.0):
+def slice_netlist(nl, params, t, i0, i1):
+    """The instances [i0, i1) of single-type workload nl, with their parameter
+    columns: a bounded sample whose load is the same per-instance work."""
+    sub = abi.Netlist(nl.n_nodes)
+    sub.models = nl.models
+    grp = abi.Netlist._GROUPS[t]
+    setattr(sub, grp, {k: np.asarray(v)[i0:i1] for k, v in getattr(nl, grp).items()
+                       if v is not None})
+    return sub, {t: np.ascontiguousarray(params[t][:, i0:i1])}
+
+
+def cpu_baseline_sample(nl, params, opt, seconds=10.0, max_instances=200_000):
     """The oracle on one core over a bounded sample of the workload."""
     from oracle.oracle import OracleCircuit
+    t = [k for k in range(abi.NUM_DEV_TYPES) if nl.count(k)][0]
+    nl, params = slice_netlist(nl, params, t, 0, min(nl.count(t), max_instances))
     oc = OracleCircuit(nl, params, opt)
     sol, sta, sto = netlists.random_state(oc.n_unknowns, oc.n_state, oc.n_store, seed=9)
     flags = abi.load_flags(transient=1, newton_iter=1, pdt=1e11)
@@ -199,11 +225,13 @@ def _ref_worker(args):
     from oracle.oracle import OracleCircuit
     nl = build_workload(name)
     opt = abi.device_options()
-    params = {t: engine.setup_params(nl, t, opt) for t in range(abi.NUM_DEV_TYPES) if nl.count(t)}
-    oc = OracleCircuit(nl, params, opt)
+    t = [t for t in range(abi.NUM_DEV_TYPES) if nl.count(t)][0]
+    sub = slice_netlist(nl, {t: np.zeros((1, nl.count(t)))}, t, i0, i1)[0]
+    params = {t: engine.setup_params(sub, t, opt)}
+    oc = OracleCircuit(sub, params, opt)
     sol, sta, sto = netlists.random_state(oc.n_unknowns, oc.n_state, oc.n_store, seed=9)
     flags = abi.load_flags(transient=1, newton_iter=1, pdt=1e11)
-    t = [t for t in range(abi.NUM_DEV_TYPES) if nl.count(t)][0]
+    i0, i1 = 0, i1 - i0
     scratch = None
     times = []
     for k in range(warmup + steps):
@@ -339,8 +367,10 @@ def run_xg(args, world, rank, local, dist):
     hbm, peak_kind = measured_peaks()
     ev_ms = float(np.mean(eval_ms))
     rd_ms = float(np.mean(red_ms))
-    b_load = load_bytes(nl, c.n_unknowns, c.nnz)
-    b_eval = eval_bytes(nl, c.n_unknowns)
+    params = {t: c.params(t) for t in range(abi.NUM_DEV_TYPES) if nl.count(t)}
+    nparams = {t: p.shape[0] for t, p in params.items()}
+    b_load = load_bytes(nl, c.n_unknowns, c.nnz, nparams)
+    b_eval = eval_bytes(nl, c.n_unknowns, nparams)
     b_red = 4 * 8 * (c.n_unknowns + 1) + 2 * 8 * c.nnz
     dom = "eval" if ev_ms >= rd_ms else "reduce"
     ach = (b_eval / (ev_ms / 1e3) if dom == "eval" else b_red / (rd_ms / 1e3)) / 1e9
@@ -349,7 +379,6 @@ def run_xg(args, world, rank, local, dist):
     if os.path.exists(prof):
         with open(prof) as f:
             traffic = json.load(f).get(args.workload, {}).get(dom)
-    params = {t: c.params(t) for t in range(abi.NUM_DEV_TYPES) if nl.count(t)}
     c.close()
     cpu_v, cpu_n = cpu_baseline_sample(nl, params, opt, seconds=args.cpu_seconds)
     clk = clocks.summary()
@@ -387,7 +416,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="xg", choices=["xg", "reference"])
-    ap.add_argument("--workload", default="single_load_mos1_1M", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="single_load_bsim3_1M", choices=sorted(WORKLOADS))
     ap.add_argument("--fma", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args()

@@ -68,6 +68,29 @@ def test_gpu_matches_oracle_random(fma, gpu_ctx, oracle_lib):
         assert not bad, (fma, k, bad)
 
 
+@pytest.mark.parametrize("fma", [0, 1])
+@pytest.mark.parametrize("variant", [0, 1, 2])
+def test_gpu_bsim3_matches_oracle(variant, fma, gpu_ctx, oracle_lib):
+    """BSIM3 variants (default cards; capMod 2 / mobMod 2 / RSH; capMod 1 and 3
+    with binning and temperature) on 3,000 instances, the whole load
+    sequence, against the oracle."""
+    from golden import circuits
+    nl = circuits.bsim3(variant, seed=40)
+    nl = netlists.random_mos_netlist(3000, 700, dev_type=abi.DEV_BSIM3, seed=41 + variant,
+                                     models=tuple(nl.models))
+    opt = abi.device_options(fma=fma, temp=320.0 if variant == 2 else 300.15)
+    params = {abi.DEV_BSIM3: engine.setup_params(nl, abi.DEV_BSIM3, opt)}
+    oc = _oracle(nl, opt, params)
+    loads = []
+    for k, fl in enumerate(circuits.FLAG_SEQUENCE):
+        flags = abi.load_flags(**{**dict(transient=0), **fl})
+        loads.append((flags, circuits.load_inputs(oc.n_unknowns, oc.n_state, oc.n_store, seed=700 + k)))
+    outs = _gpu_run(gpu_ctx, nl, opt, loads)
+    for k, (flags, ins) in enumerate(loads):
+        rep, bad = compare(outs[k], oc.load(flags, *ins), exact=False)
+        assert not bad, (variant, fma, k, bad)
+
+
 def test_gpu_deterministic_and_split_equals_fused(gpu_ctx):
     """Three fresh circuits, same inputs: two fused loads and one split
     load give identical bits.  (Fresh circuits, because a diode carries its
@@ -124,3 +147,28 @@ def test_gpu_full_size_single_load_matches_oracle(gpu_ctx, oracle_lib):
     assert not bad, bad
     for k in ("F", "dFdx", "sto_next"):
         assert np.isfinite(got[k]).all()
+
+
+def test_gpu_full_size_bsim3_single_load_matches_oracle(gpu_ctx, oracle_lib):
+    """1,000,000 BSIM3 instances (default level-9 model cards, half NMOS,
+    half PMOS, W~U[0.2,10]um, L~U[0.1,1]um) on 250k random nodes, node
+    voltages U[0,1.8] V, one transient Newton load, every output entry
+    against the oracle."""
+    nl = netlists.random_mos_netlist(1_000_000, 250_000, dev_type=abi.DEV_BSIM3, seed=2,
+                                     models=(abi.Model(abi.DEV_BSIM3, 1), abi.Model(abi.DEV_BSIM3, -1)))
+    opt = abi.device_options()
+    gpu_ctx.set_options(opt)
+    c = engine.Circuit(gpu_ctx, nl)
+    ins = netlists.random_state(c.n_unknowns, c.n_state, c.n_store, seed=9)
+    flags = abi.load_flags(transient=1, newton_iter=1, time=0.0, pdt=1e11)
+    c.set_state(*ins)
+    c.load(flags)
+    got = c.outputs()
+    params = {abi.DEV_BSIM3: c.params(abi.DEV_BSIM3)}
+    c.close()
+    want = _oracle(nl, opt, params).load(flags, *ins)
+    rep, bad = compare(got, want, exact=False)
+    assert not bad, bad
+    total = sum(v[0] for v in rep.values())
+    ident = sum(v[0] - v[1] for v in rep.values())
+    assert ident / total > 0.99, f"{ident}/{total} bit-identical"

@@ -69,8 +69,11 @@ struct xg_circuit {
   int64_t *d_red_ptr = nullptr;
   uint32_t *d_red_idx = nullptr;
   double *d_diode_vd = nullptr;  // Diode Instance::Vd carried between loads
+  double *d_b3_mem = nullptr;    // BSIM3 members carried between loads
   bool state_done = false;
 };
+// Members carried between loads per BSIM3 instance (bsim3_eval.cuh, B3Mem).
+static const int kB3MemPerInstance = 20;
 
 namespace {
 
@@ -94,6 +97,7 @@ void free_circuit(xg_circuit *c) {
   cudaFree(c->d_red_ptr);
   cudaFree(c->d_red_idx);
   cudaFree(c->d_diode_vd);
+  cudaFree(c->d_b3_mem);
   for (int t = 0; t < XG_NUM_DEV_TYPES; ++t) {
     cudaFree(c->plan.T[t].d_params);
     cudaFree(c->plan.T[t].d_lid);
@@ -250,6 +254,7 @@ int xg_circuit_create(xg_ctx *ctx, const xg_netlist *nl, xg_circuit **out) {
   if (!rc) rc = dalloc(&c->d_red_ptr, P.n_out + 1);
   if (!rc) rc = dalloc(&c->d_red_idx, (int64_t)P.red_idx.size());
   if (!rc) rc = dalloc(&c->d_diode_vd, P.T[XG_DEV_DIODE].n);
+  if (!rc) rc = dalloc(&c->d_b3_mem, (int64_t)kB3MemPerInstance * P.T[XG_DEV_BSIM3].n);
   for (int t = 0; t < XG_NUM_DEV_TYPES && !rc; ++t) {
     xg::TypeData &T = P.T[t];
     if (!T.n) continue;
@@ -275,6 +280,9 @@ int xg_circuit_create(xg_ctx *ctx, const xg_netlist *nl, xg_circuit **out) {
     if (e == cudaSuccess) e = cudaMemset(c->d_out, 0, P.n_out * sizeof(double));
     if (e == cudaSuccess && P.T[XG_DEV_DIODE].n)
       e = cudaMemset(c->d_diode_vd, 0, P.T[XG_DEV_DIODE].n * sizeof(double));
+    if (e == cudaSuccess && P.T[XG_DEV_BSIM3].n)
+      e = cudaMemset(c->d_b3_mem, 0,
+                     (size_t)kB3MemPerInstance * P.T[XG_DEV_BSIM3].n * sizeof(double));
     if (e != cudaSuccess) rc = cuda_fail(e, "initialise vectors");
   }
   if (rc) {
@@ -422,7 +430,7 @@ int xg_update_state(xg_circuit *c, const xg_load_flags *flags) {
               flags->init_fix, flags->newton_iter, flags->inputop, flags->pdt, flags->time,
               flags->init_tran};
   xg::LoadIO io{c->d_sol[0], c->d_sta[1], c->d_sto[1], c->d_sta[0], c->d_sto[0], c->d_terms,
-                c->d_diode_vd};
+                c->d_diode_vd, c->d_b3_mem, c->d_sta[1]};
   for (int k = 0; k < P.n_order; ++k) {
     int t = P.order[k];
     const xg::TypeData &T = P.T[t];

@@ -644,6 +644,8 @@ __global__ void __launch_bounds__(128) mos1_kernel(DevType t, DevOptions o, Flag
   T.put(47, i, (+gcbs + gcgs) * M);
 }
 
+#include "bsim3_eval.cuh"
+
 // ---- fixed-order reduction ---------------------------------------------------
 __global__ void __launch_bounds__(256) reduce_kernel(const double *__restrict__ terms,
                                                      const int64_t *__restrict__ red_ptr,
@@ -672,6 +674,7 @@ int launch_eval(int dev_type, const DevType &t, const DevOptions &o, const Flags
     case XG_DEV_VSRC: vsrc_kernel<<<grid_for(t.n, 256), 256, 0, s>>>(t, f, io); break;
     case XG_DEV_DIODE: diode_kernel<<<grid_for(t.n, 256), 256, 0, s>>>(t, o, f, io); break;
     case XG_DEV_MOS1: mos1_kernel<<<grid_for(t.n, 128), 128, 0, s>>>(t, o, f, io); break;
+    case XG_DEV_BSIM3: bsim3_kernel<<<grid_for(t.n, 128), 128, 0, s>>>(t, o, f, io); break;
     default: return XG_ERR_UNSUPPORTED;
   }
   return cudaGetLastError() == cudaSuccess ? XG_OK : XG_ERR_CUDA;

@@ -75,6 +75,8 @@ struct LoadIO {
   double *sta, *sto;        // next state / store (sto holds previous iterate on entry)
   double *terms;            // per-load stamp terms
   double *diode_vd;         // Diode Instance::Vd carried between loads
+  double *b3_mem;           // BSIM3 members carried between loads, [k*n + i]
+  double *sta_curr_w;       // current state, written on the first transient step
 };
 
 // Everything setup derives from a netlist (host side).
