@@ -236,6 +236,29 @@ int xg_load_dae_vectors(xg_circuit *c);
 int xg_load_dae_matrices(xg_circuit *c);
 int xg_load(xg_circuit *c, const xg_load_flags *flags);
 
+/* xg_load_noalloc — the same load as xg_load, for callers that cannot
+ * allocate device memory at the point where they load: code running while a
+ * stream is captured into a CUDA graph, runtimes that give the GPU a fixed
+ * memory budget up front, real-time loops that must not enter the allocator.
+ * It calls no cudaMalloc, cudaFree or allocating library routine.  No
+ * counterpart exists in the reference.
+ *   - The per-load stamp terms live in one fixed device array inside the
+ *     library, at most 2,097,152 terms (16 MiB); every GPU that loads the
+ *     library keeps it reserved until exit.  Circuits needing more terms
+ *     (xg_circuit_info.n_terms) are rejected with XG_ERR_ARG.
+ *   - Outputs go to dev_out (device memory, dev_out_len >= the circuit's
+ *     output count 4*(n_unknowns+1) + 2*nnz), laid out
+ *     [F | Q | dFdxdVp | dQdxdVp] (n_unknowns+1 each, ground last) then dF/dx
+ *     and dQ/dx values on the pattern of xg_circuit_get_pattern.  Next state
+ *     and store are written in the circuit as xg_load writes them.
+ *   - The first call on a device looks the array's device address up
+ *     (cudaGetSymbolAddress) with that device current; make that first call
+ *     before any stream capture.
+ *   - All calls share the array: calls whose work overlaps on the GPU race
+ *     and must be serialised by the caller. */
+int xg_load_noalloc(xg_circuit *c, const xg_load_flags *flags, double *dev_out,
+                    int64_t dev_out_len);
+
 #ifdef __cplusplus
 }
 #endif

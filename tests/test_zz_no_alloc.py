@@ -1,0 +1,75 @@
+"""xg_load_noalloc: the load for callers that cannot allocate device memory
+where they load (inside a CUDA graph capture, under a fixed memory budget, in
+a real-time loop).  Its stamp-term scratch is a fixed array inside the
+library instead of a per-circuit buffer, and its outputs go to a buffer the
+caller passes in.  Checked through the C ABI against xg_load on two calls in a
+row, and for its size limit.  Kept in a file collected last.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from xyce_gb300 import abi, engine, netlists
+
+pytestmark = pytest.mark.gpu
+
+
+def _noalloc(c, flags, out_ptr, out_len):
+    return engine.lib().xg_load_noalloc(c.h, C.byref(flags), C.c_void_p(out_ptr), C.c_int64(out_len))
+
+
+def test_noalloc_load_matches_regular_load_twice(engine_lib):
+    import torch
+    L = engine.lib()
+    L.xg_load_noalloc.argtypes = [C.c_void_p, C.POINTER(abi.XgLoadFlags), C.c_void_p, C.c_int64]
+    ctx = engine.Context(0, abi.device_options())
+    # level-1 inverters with load capacitors and sources: no member carried
+    # from one load to the next, so each load depends on its inputs alone
+    c = engine.Circuit(ctx, netlists.inverter_chain(2000))
+    n_out = 4 * (c.n_unknowns + 1) + 2 * c.nnz
+    assert c.info.n_terms <= 2 * 1024 * 1024
+    out = torch.full((n_out,), float("nan"), dtype=torch.float64, device="cuda:0")
+    for k in range(2):
+        ins = netlists.random_state(c.n_unknowns, c.n_state, c.n_store, seed=20 + k)
+        flags = abi.load_flags(transient=1, newton_iter=1 + k, time=0.4e-9 * (k + 1), pdt=1e11)
+        c.set_state(*ins)
+        c.load(flags)
+        want = c.outputs()
+        want_state = (c.download(abi.VEC_STA_NEXT), c.download(abi.VEC_STO_NEXT))
+        c.set_state(*ins)
+        assert _noalloc(c, flags, out.data_ptr(), n_out) == 0, L.xg_last_error()
+        ctx.synchronize()
+        got = out.cpu().numpy()
+        n1 = c.n_unknowns + 1
+        np.testing.assert_array_equal(got[0:c.n_unknowns], want["F"])
+        np.testing.assert_array_equal(got[n1:n1 + c.n_unknowns], want["Q"])
+        np.testing.assert_array_equal(got[2 * n1:2 * n1 + c.n_unknowns], want["dFdxdVp"])
+        np.testing.assert_array_equal(got[3 * n1:3 * n1 + c.n_unknowns], want["dQdxdVp"])
+        np.testing.assert_array_equal(got[4 * n1:4 * n1 + c.nnz], want["dFdx"])
+        np.testing.assert_array_equal(got[4 * n1 + c.nnz:4 * n1 + 2 * c.nnz], want["dQdx"])
+        np.testing.assert_array_equal(c.download(abi.VEC_STA_NEXT), want_state[0])
+        np.testing.assert_array_equal(c.download(abi.VEC_STO_NEXT), want_state[1])
+    c.close()
+    ctx.close()
+
+
+def test_noalloc_rejects_oversized_circuits_and_short_buffers(engine_lib):
+    import torch
+    L = engine.lib()
+    L.xg_load_noalloc.argtypes = [C.c_void_p, C.POINTER(abi.XgLoadFlags), C.c_void_p, C.c_int64]
+    ctx = engine.Context(0, abi.device_options())
+    big = engine.Circuit(ctx, netlists.random_mos_netlist(60_000, 20_000, seed=1))
+    assert big.info.n_terms > 2 * 1024 * 1024
+    out = torch.zeros(16, dtype=torch.float64, device="cuda:0")
+    flags = abi.load_flags()
+    assert _noalloc(big, flags, out.data_ptr(), 16) == -1
+    n_out = 4 * (big.n_unknowns + 1) + 2 * big.nnz
+    assert _noalloc(big, flags, out.data_ptr(), n_out) == -1
+    assert b"scratch" in L.xg_last_error()
+    big.close()
+    small = engine.Circuit(ctx, netlists.inverter_chain(10))
+    assert _noalloc(small, flags, out.data_ptr(), 16) == -1  # buffer too short
+    assert b"shorter" in L.xg_last_error()
+    small.close()
+    ctx.close()

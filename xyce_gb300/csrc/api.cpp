@@ -147,6 +147,26 @@ int set_device(const xg_ctx *ctx) {
 
 }  // namespace
 
+namespace xg {
+
+void set_error(const std::string &msg) { g_err = msg; }
+
+int circuit_view(xg_circuit *c, CircuitView *v) {
+  if (!c || !v) return XG_ERR_ARG;
+  v->plan = &c->plan;
+  v->device = c->ctx->device;
+  v->stream = (void *)c->ctx->stream;
+  v->fma = c->opt.fma;
+  v->opt = DevOptions{c->opt.gmin, c->opt.voltlim};
+  v->io = LoadIO{c->d_sol[0], c->d_sta[1], c->d_sto[1], c->d_sta[0], c->d_sto[0], c->d_terms,
+                 c->d_diode_vd, c->d_b3_mem, c->d_sta[1]};
+  v->red_ptr = c->d_red_ptr;
+  v->red_idx = c->d_red_idx;
+  return XG_OK;
+}
+
+}  // namespace xg
+
 extern "C" {
 
 int xg_abi_version(void) { return XG_ABI_VERSION; }

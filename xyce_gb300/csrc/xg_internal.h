@@ -103,6 +103,21 @@ struct Plan {
 int build_plan(const xg_netlist *nl, const xg_device_options *opt, Plan *plan, std::string *err,
                bool params_only = false);
 
+// Read-only view of a circuit's device data (api.cpp), for entry points
+// implemented in other translation units.
+struct CircuitView {
+  const Plan *plan;
+  int device;
+  void *stream;
+  int fma;
+  DevOptions opt;
+  LoadIO io;                   // terms = the circuit's own term buffer
+  const int64_t *red_ptr;
+  const uint32_t *red_idx;
+};
+int circuit_view(xg_circuit *c, CircuitView *v);
+void set_error(const std::string &msg);
+
 // load_kernels.cu (two builds: bit-exact and FMA-contracted)
 namespace exact {
 int launch_eval(int dev_type, const DevType &t, const DevOptions &o, const Flags &f,
