@@ -105,6 +105,30 @@ def eval_bytes(nl, n_unknowns, nparams):
     return b
 
 
+def ncu_counts(workload, kernel):
+    """Per-launch DRAM bytes and executed FP64 flops of `kernel` on `workload`
+    from the committed ncu summary (profiles/ncu_counts.json), or {}."""
+    p = os.path.join(HERE, "profiles", "ncu_counts.json")
+    if not os.path.exists(p):
+        return {}
+    with open(p) as f:
+        return json.load(f).get(workload, {}).get(kernel, {})
+
+
+def fp64_roofline(counts, kernel_ms, peak_flops, fma):
+    """The evaluation kernels are bound by the FP64 pipe: executed FP64 flops
+    (ncu count of the bit-exact build) per launch over the launch time, against
+    the DFMA throughput probed on this GPU in the same process."""
+    fl = counts.get("fp64_flops")
+    if not fl or not peak_flops or fma != (counts.get("build") == "fast"):
+        return {"achieved": None, "peak": peak_flops and peak_flops / 1e12, "unit": "TFLOP/s",
+                "frac": None, "note": "no ncu flop count for this kernel and build"}
+    ach = fl / (kernel_ms / 1e3)
+    return {"bound": "fp64", "achieved": ach / 1e12, "peak": peak_flops / 1e12, "unit": "TFLOP/s",
+            "frac": ach / peak_flops, "fp64_flops_per_launch": fl,
+            "peak_source": "xg_probe_fp64_rate (DFMA chains, this GPU, this run)"}
+
+
 def measured_peaks():
     p = os.path.join(HERE, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -365,6 +389,10 @@ def run_xg(args, world, rank, local, dist):
         return 0
 
     hbm, peak_kind = measured_peaks()
+    fp64_peak = C.c_double(0.0)
+    if L.xg_probe_fp64_rate(local, C.byref(fp64_peak)) != 0:
+        fp64_peak.value = 0.0
+    fp64_peak = fp64_peak.value
     ev_ms = float(np.mean(eval_ms))
     rd_ms = float(np.mean(red_ms))
     params = {t: c.params(t) for t in range(abi.NUM_DEV_TYPES) if nl.count(t)}
@@ -374,11 +402,8 @@ def run_xg(args, world, rank, local, dist):
     b_red = 4 * 8 * (c.n_unknowns + 1) + 2 * 8 * c.nnz
     dom = "eval" if ev_ms >= rd_ms else "reduce"
     ach = (b_eval / (ev_ms / 1e3) if dom == "eval" else b_red / (rd_ms / 1e3)) / 1e9
-    traffic = None
-    prof = os.path.join(HERE, "profiles", "traffic.json")
-    if os.path.exists(prof):
-        with open(prof) as f:
-            traffic = json.load(f).get(args.workload, {}).get(dom)
+    counts = ncu_counts(args.workload, dom)
+    traffic = counts.get("dram_bytes")
     c.close()
     cpu_v, cpu_n = cpu_baseline_sample(nl, params, opt, seconds=args.cpu_seconds)
     clk = clocks.summary()
@@ -396,6 +421,8 @@ def run_xg(args, world, rank, local, dist):
                      "unit": "GB/s", "frac": ach / hbm, "traffic": traffic,
                      "peak_source": peak_kind,
                      "algorithmic_bytes": b_eval if dom == "eval" else b_red},
+        "roofline_fp64": fp64_roofline(counts, ev_ms if dom == "eval" else rd_ms, fp64_peak,
+                                       bool(args.fma)),
         "roofline_load": {"achieved": b_load / step_s / 1e9, "unit": "GB/s",
                           "frac": b_load / step_s / 1e9 / hbm, "algorithmic_bytes": b_load},
         "e2e": {"value": world * n_inst / e2e_s, "unit": "instances/s", "h2d_bytes_per_step": h2d,

@@ -186,6 +186,12 @@ int  xg_abi_version(void);
 const char *xg_last_error(void);
 const char *xg_status_string(int status);
 
+/* Sustained FP64 fused-multiply-add throughput of a GPU [flop/s] (2 flops per
+ * DFMA), measured with a short DFMA-chain kernel: the roofline denominator of
+ * the device-evaluation kernels, which are bound by the FP64 pipe.  A
+ * measurement utility with no counterpart in the reference. */
+int xg_probe_fp64_rate(int cuda_device, double *flops_per_second);
+
 /* ---- context: one GPU, one stream (replaces the DeviceMgr singleton) -------- */
 int xg_ctx_create(int cuda_device, xg_ctx **out);
 int xg_ctx_destroy(xg_ctx *ctx);

@@ -58,6 +58,8 @@ def lib():
     L.xg_load_dae_vectors.argtypes = [vp]
     L.xg_load_dae_matrices.argtypes = [vp]
     L.xg_load.argtypes = [vp, C.POINTER(abi.XgLoadFlags)]
+    L.xg_load_noalloc.argtypes = [vp, C.POINTER(abi.XgLoadFlags), vp, C.c_int64]
+    L.xg_probe_fp64_rate.argtypes = [i, C.POINTER(C.c_double)]
     _lib = L
     return L
 
