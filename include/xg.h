@@ -242,6 +242,53 @@ int xg_load_dae_vectors(xg_circuit *c);
 int xg_load_dae_matrices(xg_circuit *c);
 int xg_load(xg_circuit *c, const xg_load_flags *flags);
 
+/* ---- sparse LU of the Newton solve -------------------------------------------
+ * Replaces the KLU solver behind N_LAS_AmesosSolver::solve
+ * (N_LAS_AmesosSolver.C:231-492): symbolic analysis once per pattern (:388),
+ * numeric factorisation per Newton iteration (:405), solve (:444).
+ * xg_lu_analyze   : host: approximate-minimum-degree column order, then a
+ *                   left-looking threshold-partial-pivot factorisation of the
+ *                   given values (KLU's tol 0.001, diagonal preferred) that
+ *                   fixes the pivot order and the L\U pattern; uploads them.
+ * xg_lu_refactor  : GPU numeric refactorisation of new values (device CSR
+ *                   values in the analysed pattern) with that pivot order.
+ *                   Asynchronous; a zero or non-finite pivot is reported by
+ *                   xg_lu_status (the reference repivots; here the caller
+ *                   analyses again).
+ * xg_lu_solve     : GPU forward/backward solves, x = A^-1 b (device buffers,
+ *                   length n, distinct).  With XG_LU_FP32 the factors and
+ *                   solves are FP32 and n_refine steps of FP64 iterative
+ *                   refinement follow (r = b - A x with the FP64 matrix).
+ * xg_lu_status    : synchronises; status bits 1 = zero/non-finite pivot (bad_row
+ *                   = first such row of B), 2 = a wait gave up, 4 = pattern error.
+ */
+enum xg_lu_precision { XG_LU_FP64 = 0, XG_LU_FP32 = 1 };
+typedef struct xg_lu xg_lu;
+typedef struct {
+  int n;
+  int64_t nnz_a, nnz_lu;      /* matrix and L\U non-zeros */
+  int precision;
+  int levels;                 /* longest row dependency chain of the refactor */
+  int n_dense;                /* dense rows ordered last */
+  double refactor_flops;      /* multiply-adds + divides of one refactor */
+  double solve_flops;         /* multiply-adds of one forward + backward solve */
+  double min_pivot, max_pivot;/* |U(k,k)| range of the analysed matrix */
+} xg_lu_info;
+int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const int *host_colidx,
+                  const double *host_values, int precision, xg_lu **out);
+int xg_lu_refactor(xg_lu *lu, const double *dev_values);
+int xg_lu_solve(xg_lu *lu, const double *dev_b, double *dev_x, int n_refine);
+int xg_lu_status(xg_lu *lu, int *status, int *bad_row);
+int xg_lu_get_info(const xg_lu *lu, xg_lu_info *info);
+/* host copies of the analysis: P, Q (n each), L\U row pointers (n+1), columns (nnz_lu) */
+int xg_lu_get_symbolic(const xg_lu *lu, int *P, int *Q, int *lu_rowptr, int *lu_colidx);
+int xg_lu_destroy(xg_lu *lu);
+/* host-only analysis pieces (no GPU): the AMD order alone, and the full
+ * analysis returning P, Q and the L\U non-zero count */
+int xg_lu_order(int n, const int *host_rowptr, const int *host_colidx, int *order, int *n_dense);
+int xg_lu_analyze_host(int n, const int *host_rowptr, const int *host_colidx,
+                       const double *host_values, int *P, int *Q, int64_t *nnz_lu);
+
 /* xg_load_noalloc — the same load as xg_load, for callers that cannot
  * allocate device memory at the point where they load: code running while a
  * stream is captured into a CUDA graph, runtimes that give the GPU a fixed

@@ -100,3 +100,22 @@ def _cmp(x, y):
     scale = RTOL * np.abs(y) + ATOL_FRAC * np.max(np.abs(y)) + 1e-300
     viol = float(np.max(np.abs(x - y) / scale))
     return (int(x.size), neq, viol)
+
+
+def circuit_jacobian(netlist, seed=0, pdt=1e11, options=None):
+    """The trapezoid-style Newton matrix dF/dx + pdt * dQ/dx of one transient
+    load of `netlist` at a seeded random state, from the oracle (CSR, scipy)."""
+    import scipy.sparse as sp
+
+    from oracle.oracle import OracleCircuit
+    from xyce_gb300 import engine, netlists
+    opt = options or abi.device_options()
+    params = {t: engine.setup_params(netlist, t, opt) for t in range(abi.NUM_DEV_TYPES)
+              if netlist.count(t)}
+    oc = OracleCircuit(netlist, params, opt)
+    ins = netlists.random_state(oc.n_unknowns, oc.n_state, oc.n_store, seed=seed)
+    out = oc.load(abi.load_flags(transient=1, newton_iter=1, pdt=pdt), *ins)
+    n = oc.n_unknowns
+    A = sp.csr_matrix((out["dFdx"] + pdt * out["dQdx"], (out["rows"], out["cols"])), shape=(n, n))
+    A.sort_indices()
+    return A

@@ -1,0 +1,117 @@
+"""GPU refactorisation and solves of the Newton-solve LU, through the C ABI.
+
+The host analysis fixes the pivot order on one matrix; the GPU refactors a
+second matrix of the same pattern (another load of the same circuit) with
+that order, then solves.  Checked against scipy's SuperLU in FP64 and by the
+backward error |b - A x| / (|A| |x| + |b|) (infinity norms), which a
+backward-stable FP64 solve keeps near 1e-16 whatever the conditioning:
+  * FP64 factors: backward error <= 1e-13;
+  * FP32 factors: ~1e-7 unrefined; <= 1e-13 after FP64 iterative refinement.
+"""
+import numpy as np
+import pytest
+import scipy.sparse.linalg as sla
+
+from helpers import circuit_jacobian
+from xyce_gb300 import abi, engine, netlists
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    "inverter_chain_1000": lambda: netlists.inverter_chain(1000),
+    "power_grid_60x60": lambda: netlists.power_grid(60, 60, 1200, seed=1),
+    "ring_oscillator_101": lambda: netlists.ring_oscillator(101, seed=2),
+    "random_mos_3000": lambda: netlists.random_mos_netlist(3000, 800, seed=3),
+    "random_bsim3_3000": lambda: netlists.random_mos_netlist(
+        3000, 700, dev_type=abi.DEV_BSIM3, seed=5,
+        models=(abi.Model(abi.DEV_BSIM3, 1), abi.Model(abi.DEV_BSIM3, -1))),
+}
+
+
+def _backward_error(A, x, b):
+    r = b - A @ x
+    return np.abs(r).max() / (abs(A).sum(axis=1).max() * np.abs(x).max() + np.abs(b).max())
+
+
+def _solve(ctx, A_analyse, A, b, precision, n_refine):
+    import torch
+    lu = engine.LU(ctx, A_analyse.indptr, A_analyse.indices, A_analyse.data, precision)
+    dev_vals = torch.from_numpy(A.data.copy()).cuda()
+    dev_b = torch.from_numpy(b).cuda()
+    dev_x = torch.zeros_like(dev_b)
+    lu.refactor(dev_vals.data_ptr())
+    lu.solve(dev_b.data_ptr(), dev_x.data_ptr(), n_refine)
+    status, _ = lu.status()
+    x = dev_x.cpu().numpy()
+    info = lu.info
+    lu.close()
+    return x, status, info
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_fp64_refactor_and_solve(case, gpu_ctx, oracle_lib):
+    nl = CASES[case]()
+    A0 = circuit_jacobian(nl, seed=4)
+    A = circuit_jacobian(nl, seed=5)
+    assert np.array_equal(A0.indices, A.indices)
+    b = np.random.default_rng(7).standard_normal(A.shape[0])
+    x, status, info = _solve(gpu_ctx, A0, A, b, abi.LU_FP64, 0)
+    assert status == 0
+    assert _backward_error(A, x, b) <= 1e-13
+    ref = sla.spsolve(A.tocsc(), b)
+    assert _backward_error(A, ref, b) <= 1e-13
+    if case in ("inverter_chain_1000", "power_grid_60x60", "ring_oscillator_101"):
+        assert np.abs(x - ref).max() <= 1e-9 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("case", ["inverter_chain_1000", "power_grid_60x60", "ring_oscillator_101"])
+def test_fp32_factors_with_fp64_refinement(case, gpu_ctx, oracle_lib):
+    nl = CASES[case]()
+    A0 = circuit_jacobian(nl, seed=4)
+    A = circuit_jacobian(nl, seed=5)
+    b = np.random.default_rng(8).standard_normal(A.shape[0])
+    x0, st0, _ = _solve(gpu_ctx, A0, A, b, abi.LU_FP32, 0)
+    x3, st3, _ = _solve(gpu_ctx, A0, A, b, abi.LU_FP32, 3)
+    assert st0 == 0 and st3 == 0
+    e0, e3 = _backward_error(A, x0, b), _backward_error(A, x3, b)
+    assert e0 <= 1e-5
+    assert e3 <= 1e-13, (e0, e3)
+
+
+def test_refactor_and_solve_are_deterministic(gpu_ctx, oracle_lib):
+    nl = CASES["power_grid_60x60"]()
+    A = circuit_jacobian(nl, seed=5)
+    b = np.random.default_rng(9).standard_normal(A.shape[0])
+    xs = [_solve(gpu_ctx, A, A, b, abi.LU_FP64, 0)[0] for _ in range(2)]
+    assert np.array_equal(xs[0], xs[1])
+
+
+def test_zero_pivot_is_reported(gpu_ctx, oracle_lib):
+    """All-zero values: the refactor meets a zero pivot, finishes, and says so."""
+    import torch
+    nl = CASES["inverter_chain_1000"]()
+    A = circuit_jacobian(nl, seed=5)
+    lu = engine.LU(gpu_ctx, A.indptr, A.indices, A.data, abi.LU_FP64)
+    zeros = torch.zeros(A.nnz, dtype=torch.float64, device="cuda:0")
+    lu.refactor(zeros.data_ptr())
+    status, bad_row = lu.status()
+    assert status & 1 and bad_row == 0
+    # a good matrix afterwards factors cleanly again
+    vals = torch.from_numpy(A.data.copy()).cuda()
+    lu.refactor(vals.data_ptr())
+    assert lu.status() == (0, -1)
+    lu.close()
+
+
+def test_full_size_power_grid_solve(gpu_ctx, oracle_lib):
+    """200x200 mesh with 40,000 MOSFET sinks (120,002 unknowns)."""
+    nl = netlists.power_grid(200, 200, 40000, seed=0)
+    A0 = circuit_jacobian(nl, seed=4)
+    A = circuit_jacobian(nl, seed=5)
+    b = np.random.default_rng(10).standard_normal(A.shape[0])
+    x, status, info = _solve(gpu_ctx, A0, A, b, abi.LU_FP64, 0)
+    assert status == 0 and info.n == 120002
+    assert _backward_error(A, x, b) <= 1e-13
+    x32, status, _ = _solve(gpu_ctx, A0, A, b, abi.LU_FP32, 3)
+    assert status == 0
+    assert _backward_error(A, x32, b) <= 1e-13

@@ -1,0 +1,115 @@
+"""Host side of the Newton-solve LU (no GPU): the approximate-minimum-degree
+order and the pivoting analysis that fixes the pivot order and the L\\U
+pattern the GPU refactorisation reuses."""
+import heapq
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from helpers import circuit_jacobian
+from xyce_gb300 import engine, netlists
+
+
+def _structural_fill(B):
+    """Non-zeros of the L\\U of B with diagonal pivots (row-wise symbolic)."""
+    n = B.shape[0]
+    upper = [None] * n
+    total = 0
+    for i in range(n):
+        S = set(B.indices[B.indptr[i]:B.indptr[i + 1]].tolist())
+        S.add(i)
+        h = [k for k in S if k < i]
+        heapq.heapify(h)
+        seen = set(h)
+        while h:
+            k = heapq.heappop(h)
+            for m in upper[k]:
+                if m not in S:
+                    S.add(m)
+                    if m < i and m not in seen:
+                        heapq.heappush(h, m)
+                        seen.add(m)
+        upper[i] = [m for m in S if m > i]
+        total += len(S)
+    return total
+
+
+def _grid_laplacian(k):
+    n = k * k
+    rows, cols = [], []
+    for i in range(k):
+        for j in range(k):
+            a = i * k + j
+            rows.append(a), cols.append(a)
+            for di, dj in ((1, 0), (0, 1)):
+                if i + di < k and j + dj < k:
+                    b = (i + di) * k + j + dj
+                    rows += [a, b]
+                    cols += [b, a]
+    vals = np.where(np.array(rows) == np.array(cols), 4.0, -1.0)
+    A = sp.csr_matrix((vals, (rows, cols)), shape=(n, n))
+    A.sort_indices()
+    return A
+
+
+@pytest.mark.parametrize("case", ["inverter_chain_24", "power_grid_20x20", "random_mos_3000"])
+def test_analysis_pattern_and_pivots(case, engine_lib, oracle_lib):
+    nl = {"inverter_chain_24": lambda: netlists.inverter_chain(24),
+          "power_grid_20x20": lambda: netlists.power_grid(20, 20, 60, seed=1),
+          "random_mos_3000": lambda: netlists.random_mos_netlist(3000, 800, seed=3)}[case]()
+    A = circuit_jacobian(nl, seed=4)
+    n = A.shape[0]
+    P, Q, nnz_lu = engine.lu_analyze_host(A.indptr, A.indices, A.data)
+    assert sorted(P.tolist()) == list(range(n)) and sorted(Q.tolist()) == list(range(n))
+    B = A[P][:, Q].tocsr()
+    B.sort_indices()
+    # the reported pattern is exactly the structural fill of B = A(P, Q)
+    assert nnz_lu == _structural_fill(B)
+    # the pivot order works without further pivoting: dense Doolittle on B
+    D = B.toarray()
+    for k in range(n):
+        assert D[k, k] != 0.0
+        D[k + 1:, k] /= D[k, k]
+        D[k + 1:, k + 1:] -= np.outer(D[k + 1:, k], D[k, k + 1:])
+    # and solves the system
+    L = np.tril(D, -1) + np.eye(n)
+    U = np.triu(D)
+    b = np.random.default_rng(1).standard_normal(n)
+    z = np.linalg.solve(U, np.linalg.solve(L, b[P]))
+    x = np.empty(n)
+    x[Q] = z
+    # backward error of the solution (the matrices are badly scaled: random
+    # node voltages forward-bias junctions, so entries span ~17 decades)
+    Ad = A.toarray()
+    r = b - Ad @ x
+    assert np.abs(r).max() <= 1e-13 * (np.abs(Ad).sum(1).max() * np.abs(x).max() + np.abs(b).max())
+
+
+def test_amd_reduces_fill_on_a_mesh(engine_lib):
+    A = _grid_laplacian(30)
+    order, n_dense = engine.amd_order(A.indptr, A.indices)
+    assert sorted(order.tolist()) == list(range(A.shape[0])) and n_dense == 0
+    natural = _structural_fill(A)
+    B = A[order][:, order].tocsr()
+    B.sort_indices()
+    amd = _structural_fill(B)
+    assert amd < 0.5 * natural, (amd, natural)
+
+
+def test_dense_rows_are_ordered_last(engine_lib):
+    # a star: node 0 touches every other node
+    n = 400
+    rows = list(range(n)) + [0] * (n - 1) + list(range(1, n))
+    cols = list(range(n)) + list(range(1, n)) + [0] * (n - 1)
+    A = sp.csr_matrix((np.ones(len(rows)), (rows, cols)), shape=(n, n))
+    A.sort_indices()
+    order, n_dense = engine.amd_order(A.indptr, A.indices)
+    assert n_dense == 1 and order[-1] == 0
+
+
+def test_singular_matrix_is_reported(engine_lib):
+    A = sp.csr_matrix(np.array([[1.0, 2.0], [2.0, 4.0]]))
+    with pytest.raises(engine.XgError) as e:
+        engine.lu_analyze_host(A.indptr, A.indices, A.data)
+    assert e.value.status == -4

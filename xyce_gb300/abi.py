@@ -75,6 +75,16 @@ class XgCircuitInfo(C.Structure):
                 ("n_instances", C.c_int * NUM_DEV_TYPES)]
 
 
+LU_FP64, LU_FP32 = 0, 1
+
+
+class XgLuInfo(C.Structure):
+    _fields_ = [("n", C.c_int), ("nnz_a", C.c_int64), ("nnz_lu", C.c_int64),
+                ("precision", C.c_int), ("levels", C.c_int), ("n_dense", C.c_int),
+                ("refactor_flops", C.c_double), ("solve_flops", C.c_double),
+                ("min_pivot", C.c_double), ("max_pivot", C.c_double)]
+
+
 def device_options(gmin=1e-12, temp=300.15, tnom=300.15, voltlim=1, newmeyer=0, fma=0):
     return XgDeviceOptions(gmin, temp, tnom, voltlim, newmeyer, fma)
 

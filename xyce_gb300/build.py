@@ -16,6 +16,7 @@ BUILD = os.path.join(PKG, "_build")
 LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libxg.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+FMA_SOURCES = {"lu_kernels.cu"}
 
 
 def _nvcc():
@@ -68,7 +69,9 @@ def build_engine(verbose=False):
         src = os.path.join(CSRC, f)
         if f.endswith(".cu") and f != "load_kernels.cu":
             obj = os.path.join(BUILD, f[:-3] + ".o")
-            jobs.append((obj, [src] + heads, cu_common + ["-fmad=false", "-c", src, "-o", obj]))
+            # the sparse LU has no bit-parity target: contract to FMA there
+            fmad = "true" if f in FMA_SOURCES else "false"
+            jobs.append((obj, [src] + heads, cu_common + [f"-fmad={fmad}", "-c", src, "-o", obj]))
         elif f.endswith(".cpp"):
             obj = os.path.join(BUILD, f[:-4] + ".o")
             cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall",

@@ -151,6 +151,13 @@ namespace xg {
 
 void set_error(const std::string &msg) { g_err = msg; }
 
+int ctx_info(xg_ctx *ctx, int *device, void **stream) {
+  if (!ctx) return XG_ERR_ARG;
+  *device = ctx->device;
+  *stream = ctx->stream;
+  return XG_OK;
+}
+
 int circuit_view(xg_circuit *c, CircuitView *v) {
   if (!c || !v) return XG_ERR_ARG;
   v->plan = &c->plan;

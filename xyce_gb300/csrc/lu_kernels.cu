@@ -1,0 +1,513 @@
+// lu_kernels.cu — GPU numeric refactorisation and triangular solves of the
+// Newton-solve LU, and the xg_lu_* C ABI.
+//
+// The reference refactors and solves with KLU on the host for every Newton
+// iteration (N_LAS_AmesosSolver.C:405 NumericFactorization, :444 Solve).
+// Here the pivot order and the filled L\U pattern come from the host analysis
+// (lu_symbolic.cpp) and the numeric work runs on the GPU:
+//
+//  * refactor: row-wise ("up-looking") elimination of B = A(P, Q).  One warp
+//    owns one row; rows are claimed in ascending order from a counter, and a
+//    row waits (bounded spin on a per-row epoch flag) only for the rows k of
+//    its L part, at the moment it reaches them.  Every row a warp waits for
+//    was claimed earlier by a running warp, so the schedule always advances.
+//    Rows far apart in the elimination order run concurrently; the row
+//    pipeline needs no level barriers.  Each entry of a row is updated by one
+//    lane in ascending k, so the result is the same on every run.
+//  * solves: the same claim/wait scheme by rows of L (forward) and of U
+//    (backward, rows claimed in descending order), a fixed lane-strided
+//    partial sum and a fixed shuffle tree per row.
+//  * precision: factors in FP64, or in FP32 with FP64 iterative refinement
+//    (r = b - A x with the FP64 matrix, solve, x += d).
+//
+// Epochs and claim counters live in device memory and are advanced by the
+// kernel that precedes each phase, so a captured sequence can be replayed.
+// Every spin has an iteration limit; a wait that gives up records bit 1 in the
+// status word and the row is finished anyway, so a launch always ends.
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+
+#include "xg.h"
+#include "xg_internal.h"
+#include "xg_lu.h"
+
+namespace xg {
+namespace {
+
+enum Ctrl : int {
+  C_EPOCH_F = 0, C_CLAIM_F, C_EPOCH_S, C_CLAIM_L, C_CLAIM_U, C_STATUS, C_BAD_ROW, C_N
+};
+enum Status : unsigned { ST_PIVOT = 1u, ST_TIMEOUT = 2u, ST_PATTERN = 4u };
+
+constexpr int kSpinLimit = 1 << 20;  // polls per wait (~0.1-0.5 s) before giving up
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(unsigned *p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Wait until flag == epoch; false (and the timeout bit set) if it never does.
+// Once any wait of the launch has given up, the others give up at their next
+// check, so a broken schedule ends in one wait time rather than one per row.
+__device__ bool wait_epoch(const unsigned *flag, unsigned epoch, unsigned *ctrl) {
+  int it = 0;
+  while (ld_acquire(flag) != epoch) {
+    ++it;
+    if (it > kSpinLimit ||
+        ((it & 1023) == 0 && (*(volatile unsigned *)&ctrl[C_STATUS] & ST_TIMEOUT))) {
+      atomicOr(&ctrl[C_STATUS], ST_TIMEOUT);
+      return false;
+    }
+    if (it > 32) __nanosleep(64);
+  }
+  return true;
+}
+
+struct LuDev {
+  int n;
+  const int *rp, *ci, *diag;  // L\U pattern of B
+  const int *lu2a;            // LU position -> A entry, -1 for fill
+  const int *P, *Q;
+  const int *arp, *aci;       // A pattern (CSR) for the residual
+  unsigned *ctrl;
+  unsigned *done_f, *done_l, *done_u;
+};
+
+// Scatter A into the L\U value array (fill entries zero), keep an FP64 copy of
+// A for the residual, and open a new factorisation epoch.
+template <class T>
+__global__ void lu_assemble(LuDev d, const double *__restrict__ a, double *__restrict__ a_copy,
+                            int64_t nnz_a, T *__restrict__ val, int64_t nnz_lu) {
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  const int64_t t0 = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t0 == 0) {
+    d.ctrl[C_EPOCH_F] += 1;
+    d.ctrl[C_CLAIM_F] = 0;
+    d.ctrl[C_STATUS] = 0;
+    d.ctrl[C_BAD_ROW] = 0xffffffffu;
+  }
+  for (int64_t p = t0; p < nnz_lu; p += stride) {
+    int s = d.lu2a[p];
+    val[p] = s >= 0 ? T(a[s]) : T(0);
+  }
+  if (a_copy != a)
+    for (int64_t p = t0; p < nnz_a; p += stride) a_copy[p] = a[p];
+}
+
+__device__ __forceinline__ int find_col(const int *__restrict__ ci, int lo, int end, int col) {
+  // the position in [lo, end) holding col, or -1
+  int hi = end;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    int c = __ldg(ci + mid);
+    if (c < col) lo = mid + 1; else hi = mid;
+  }
+  return (lo < end && __ldg(ci + lo) == col) ? lo : -1;
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) lu_factor(LuDev d, T *val) {
+  const int lane = threadIdx.x & 31;
+  const unsigned epoch = *(volatile unsigned *)&d.ctrl[C_EPOCH_F];
+  while (true) {
+    int row = 0;
+    if (lane == 0) row = int(atomicAdd(&d.ctrl[C_CLAIM_F], 1u));
+    row = __shfl_sync(0xffffffffu, row, 0);
+    if (row >= d.n) break;
+    const int s = __ldg(d.rp + row), dp = __ldg(d.diag + row), e = __ldg(d.rp + row + 1);
+    for (int p = s; p < dp; ++p) {
+      const int k = __ldg(d.ci + p);
+      if (lane == 0) wait_epoch(d.done_f + k, epoch, d.ctrl);
+      __syncwarp();
+      const int kd = __ldg(d.diag + k), ke = __ldg(d.rp + k + 1);
+      const T l = val[p] / __ldcg(val + kd);
+      __syncwarp();
+      if (lane == 0) val[p] = l;
+      for (int q = kd + 1 + lane; q < ke; q += 32) {
+        const int m = __ldg(d.ci + q);
+        const int pos = find_col(d.ci, p + 1, e, m);
+        if (pos >= 0) {
+          val[pos] -= l * __ldcg(val + q);
+        } else {
+          atomicOr(&d.ctrl[C_STATUS], ST_PATTERN);
+        }
+      }
+      __syncwarp();
+    }
+    if (lane == 0) {
+      const T u = val[dp];
+      if (!(fabs(double(u)) > 0.0) || !isfinite(double(u))) {
+        atomicOr(&d.ctrl[C_STATUS], ST_PIVOT);
+        atomicMin(&d.ctrl[C_BAD_ROW], unsigned(row));
+      }
+      __threadfence();
+      st_release(d.done_f + row, epoch);
+    }
+  }
+}
+
+__global__ void lu_solve_open(LuDev d) {
+  d.ctrl[C_EPOCH_S] += 1;
+  d.ctrl[C_CLAIM_L] = 0;
+  d.ctrl[C_CLAIM_U] = 0;
+}
+
+template <class T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// y = L \ b(P)   (unit lower triangular, rows ascending)
+template <class T>
+__global__ void __launch_bounds__(256) lu_lsolve(LuDev d, const T *__restrict__ val,
+                                                 const double *__restrict__ b, T *y) {
+  const int lane = threadIdx.x & 31;
+  const unsigned epoch = *(volatile unsigned *)&d.ctrl[C_EPOCH_S];
+  while (true) {
+    int row = 0;
+    if (lane == 0) row = int(atomicAdd(&d.ctrl[C_CLAIM_L], 1u));
+    row = __shfl_sync(0xffffffffu, row, 0);
+    if (row >= d.n) break;
+    const int s = __ldg(d.rp + row), dp = __ldg(d.diag + row);
+    T acc = T(0);
+    for (int p = s + lane; p < dp; p += 32) {
+      const int k = __ldg(d.ci + p);
+      wait_epoch(d.done_l + k, epoch, d.ctrl);
+      acc += __ldcg(val + p) * __ldcg(y + k);
+    }
+    acc = warp_sum(acc);
+    if (lane == 0) {
+      y[row] = T(b[__ldg(d.P + row)]) - acc;
+      __threadfence();
+      st_release(d.done_l + row, epoch);
+    }
+  }
+}
+
+// z = U \ y, x(Q) = z   (rows descending)
+template <class T>
+__global__ void __launch_bounds__(256) lu_usolve(LuDev d, const T *__restrict__ val,
+                                                 const T *__restrict__ y, T *z, double *x) {
+  const int lane = threadIdx.x & 31;
+  const unsigned epoch = *(volatile unsigned *)&d.ctrl[C_EPOCH_S];
+  while (true) {
+    int c = 0;
+    if (lane == 0) c = int(atomicAdd(&d.ctrl[C_CLAIM_U], 1u));
+    c = __shfl_sync(0xffffffffu, c, 0);
+    if (c >= d.n) break;
+    const int row = d.n - 1 - c;
+    const int dp = __ldg(d.diag + row), e = __ldg(d.rp + row + 1);
+    T acc = T(0);
+    for (int p = dp + 1 + lane; p < e; p += 32) {
+      const int k = __ldg(d.ci + p);
+      wait_epoch(d.done_u + k, epoch, d.ctrl);
+      acc += __ldcg(val + p) * __ldcg(z + k);
+    }
+    acc = warp_sum(acc);
+    if (lane == 0) {
+      const T zi = (__ldcg(y + row) - acc) / __ldcg(val + dp);
+      z[row] = zi;
+      x[__ldg(d.Q + row)] = double(zi);
+      __threadfence();
+      st_release(d.done_u + row, epoch);
+    }
+  }
+}
+
+// r = b - A x   (FP64, one thread per row, entries in CSR order)
+__global__ void lu_residual(LuDev d, const double *__restrict__ a, const double *__restrict__ x,
+                            const double *__restrict__ b, double *__restrict__ r) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n; i += gridDim.x * blockDim.x) {
+    const int p0 = __ldg(d.arp + i), p1 = __ldg(d.arp + i + 1);
+    double acc = b[i];
+    for (int p = p0; p < p1; ++p) acc -= a[p] * x[__ldg(d.aci + p)];
+    r[i] = acc;
+  }
+}
+
+__global__ void lu_axpy(int n, const double *__restrict__ dx, double *__restrict__ x) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    x[i] += dx[i];
+}
+
+}  // namespace
+}  // namespace xg
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+
+struct xg_lu {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int precision = XG_LU_FP64;
+  xg::LuSymbolic S;
+  int64_t nnz_lu = 0;
+  int *d_rp = nullptr, *d_ci = nullptr, *d_diag = nullptr, *d_lu2a = nullptr;
+  int *d_P = nullptr, *d_Q = nullptr, *d_arp = nullptr, *d_aci = nullptr;
+  unsigned *d_ctrl = nullptr, *d_done = nullptr;  // 3n flags
+  void *d_val = nullptr;                          // nnz_lu of T
+  void *d_y = nullptr, *d_z = nullptr;            // n of T
+  double *d_a = nullptr;                          // FP64 copy of A
+  double *d_r = nullptr, *d_dx = nullptr;         // refinement work
+  int grid_factor = 0, grid_solve = 0;
+  bool factored = false;
+  xg::LuDev dev() const {
+    return xg::LuDev{S.n, d_rp, d_ci, d_diag, d_lu2a, d_P, d_Q, d_arp, d_aci, d_ctrl,
+                     d_done, d_done + S.n, d_done + 2 * S.n};
+  }
+};
+
+namespace {
+
+int cuda_fail(cudaError_t e, const char *what) {
+  xg::set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return XG_ERR_CUDA;
+}
+
+#define XG_CU(call)                                      \
+  do {                                                   \
+    cudaError_t e_ = (call);                             \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call);  \
+  } while (0)
+
+template <class V>
+int upload(V **dst, const std::vector<V> &src) {
+  XG_CU(cudaMalloc((void **)dst, sizeof(V) * std::max<size_t>(src.size(), 1)));
+  if (!src.empty()) XG_CU(cudaMemcpy(*dst, src.data(), sizeof(V) * src.size(), cudaMemcpyHostToDevice));
+  return XG_OK;
+}
+
+void free_lu(xg_lu *lu) {
+  void *ptrs[] = {lu->d_rp, lu->d_ci, lu->d_diag, lu->d_lu2a, lu->d_P, lu->d_Q, lu->d_arp,
+                  lu->d_aci, lu->d_ctrl, lu->d_done, lu->d_val, lu->d_y, lu->d_z, lu->d_a,
+                  lu->d_r, lu->d_dx};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+}
+
+template <class T>
+int refactor_t(xg_lu *lu, const double *dev_values) {
+  xg::LuDev d = lu->dev();
+  xg::lu_assemble<T><<<lu->grid_solve, 256, 0, lu->stream>>>(
+      d, dev_values, lu->d_a, lu->S.nnz_a, (T *)lu->d_val, lu->nnz_lu);
+  xg::lu_factor<T><<<lu->grid_factor, 256, 0, lu->stream>>>(d, (T *)lu->d_val);
+  XG_CU(cudaGetLastError());
+  return XG_OK;
+}
+
+template <class T>
+int solve_once(xg_lu *lu, const double *b, double *x) {
+  xg::LuDev d = lu->dev();
+  xg::lu_solve_open<<<1, 1, 0, lu->stream>>>(d);
+  xg::lu_lsolve<T><<<lu->grid_factor, 256, 0, lu->stream>>>(d, (const T *)lu->d_val, b, (T *)lu->d_y);
+  xg::lu_usolve<T><<<lu->grid_factor, 256, 0, lu->stream>>>(d, (const T *)lu->d_val, (const T *)lu->d_y,
+                                                            (T *)lu->d_z, x);
+  XG_CU(cudaGetLastError());
+  return XG_OK;
+}
+
+template <class T>
+int solve_t(xg_lu *lu, const double *b, double *x, int n_refine) {
+  int rc = solve_once<T>(lu, b, x);
+  if (rc) return rc;
+  xg::LuDev d = lu->dev();
+  const int nb = std::min(1024, (lu->S.n + 255) / 256);
+  for (int it = 0; it < n_refine; ++it) {
+    xg::lu_residual<<<nb, 256, 0, lu->stream>>>(d, lu->d_a, x, b, lu->d_r);
+    rc = solve_once<T>(lu, lu->d_r, lu->d_dx);
+    if (rc) return rc;
+    xg::lu_axpy<<<nb, 256, 0, lu->stream>>>(lu->S.n, lu->d_dx, x);
+  }
+  XG_CU(cudaGetLastError());
+  return XG_OK;
+}
+
+}  // namespace
+
+extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const int *host_colidx,
+                             const double *host_values, int precision, xg_lu **out) {
+  if (!ctx || !out || n <= 0 || !host_rowptr || !host_colidx || !host_values ||
+      (precision != XG_LU_FP64 && precision != XG_LU_FP32)) {
+    xg::set_error("xg_lu_analyze: bad argument");
+    return XG_ERR_ARG;
+  }
+  *out = nullptr;
+  std::unique_ptr<xg_lu> lu(new xg_lu);
+  void *stream = nullptr;
+  xg::ctx_info(ctx, &lu->device, &stream);
+  lu->stream = (cudaStream_t)stream;
+  lu->precision = precision;
+  std::string err;
+  if (xg::lu_analyze(n, host_rowptr, host_colidx, host_values, 1e-3, &lu->S, &err)) {
+    xg::set_error(err);
+    return XG_ERR_SINGULAR;
+  }
+  XG_CU(cudaSetDevice(lu->device));
+  const xg::LuSymbolic &S = lu->S;
+  lu->nnz_lu = S.rp[n];
+  std::vector<int> arp(host_rowptr, host_rowptr + n + 1);
+  std::vector<int> aci(host_colidx, host_colidx + S.nnz_a);
+  int rc = 0;
+  auto fail = [&](int r) {
+    free_lu(lu.get());
+    return r;
+  };
+  if ((rc = upload(&lu->d_rp, S.rp)) || (rc = upload(&lu->d_ci, S.ci)) ||
+      (rc = upload(&lu->d_diag, S.diag)) || (rc = upload(&lu->d_lu2a, S.lu2a)) ||
+      (rc = upload(&lu->d_P, S.P)) || (rc = upload(&lu->d_Q, S.Q)) ||
+      (rc = upload(&lu->d_arp, arp)) || (rc = upload(&lu->d_aci, aci)))
+    return fail(rc);
+  const size_t tsz = precision == XG_LU_FP32 ? sizeof(float) : sizeof(double);
+  cudaError_t e = cudaSuccess;
+  if ((e = cudaMalloc((void **)&lu->d_ctrl, sizeof(unsigned) * xg::C_N)) ||
+      (e = cudaMalloc((void **)&lu->d_done, sizeof(unsigned) * 3 * size_t(n))) ||
+      (e = cudaMalloc(&lu->d_val, tsz * size_t(lu->nnz_lu))) ||
+      (e = cudaMalloc(&lu->d_y, tsz * size_t(n))) || (e = cudaMalloc(&lu->d_z, tsz * size_t(n))) ||
+      (e = cudaMalloc((void **)&lu->d_a, sizeof(double) * size_t(S.nnz_a))) ||
+      (e = cudaMalloc((void **)&lu->d_r, sizeof(double) * size_t(n))) ||
+      (e = cudaMalloc((void **)&lu->d_dx, sizeof(double) * size_t(n)))) {
+    free_lu(lu.get());
+    return e == cudaErrorMemoryAllocation ? (xg::set_error("xg_lu_analyze: out of device memory"),
+                                             XG_ERR_OOM)
+                                          : cuda_fail(e, "xg_lu_analyze");
+  }
+  // flags start at 0 and the first epoch is 1
+  if ((e = cudaMemset(lu->d_ctrl, 0, sizeof(unsigned) * xg::C_N)) ||
+      (e = cudaMemset(lu->d_done, 0, sizeof(unsigned) * 3 * size_t(n)))) {
+    free_lu(lu.get());
+    return cuda_fail(e, "xg_lu_analyze: cudaMemset");
+  }
+  int sms = 0, occ = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, lu->device);
+  if (precision == XG_LU_FP32)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, xg::lu_factor<float>, 256, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, xg::lu_factor<double>, 256, 0);
+  // one warp per row: never more warps than rows
+  lu->grid_factor = std::max(1, std::min(sms * std::max(occ, 1), (n + 7) / 8));
+  lu->grid_solve = std::max(1, std::min(sms * 4, int((lu->nnz_lu + 255) / 256)));
+  *out = lu.release();
+  return XG_OK;
+}
+
+extern "C" int xg_lu_refactor(xg_lu *lu, const double *dev_values) {
+  if (!lu || !dev_values) {
+    xg::set_error("xg_lu_refactor: bad argument");
+    return XG_ERR_ARG;
+  }
+  XG_CU(cudaSetDevice(lu->device));
+  int rc = lu->precision == XG_LU_FP32 ? refactor_t<float>(lu, dev_values)
+                                       : refactor_t<double>(lu, dev_values);
+  if (!rc) lu->factored = true;
+  return rc;
+}
+
+extern "C" int xg_lu_solve(xg_lu *lu, const double *dev_b, double *dev_x, int n_refine) {
+  if (!lu || !dev_b || !dev_x || n_refine < 0 || dev_b == dev_x) {
+    xg::set_error("xg_lu_solve: bad argument (b and x must be distinct device buffers)");
+    return XG_ERR_ARG;
+  }
+  if (!lu->factored) {
+    xg::set_error("xg_lu_solve: no factorisation yet (call xg_lu_refactor)");
+    return XG_ERR_STATE;
+  }
+  XG_CU(cudaSetDevice(lu->device));
+  return lu->precision == XG_LU_FP32 ? solve_t<float>(lu, dev_b, dev_x, n_refine)
+                                     : solve_t<double>(lu, dev_b, dev_x, n_refine);
+}
+
+extern "C" int xg_lu_status(xg_lu *lu, int *status, int *bad_row) {
+  if (!lu || !status) {
+    xg::set_error("xg_lu_status: bad argument");
+    return XG_ERR_ARG;
+  }
+  XG_CU(cudaSetDevice(lu->device));
+  unsigned h[xg::C_N];
+  XG_CU(cudaMemcpyAsync(h, lu->d_ctrl, sizeof(h), cudaMemcpyDeviceToHost, lu->stream));
+  XG_CU(cudaStreamSynchronize(lu->stream));
+  *status = int(h[xg::C_STATUS]);
+  if (bad_row) *bad_row = h[xg::C_BAD_ROW] == 0xffffffffu ? -1 : int(h[xg::C_BAD_ROW]);
+  return XG_OK;
+}
+
+extern "C" int xg_lu_get_info(const xg_lu *lu, xg_lu_info *info) {
+  if (!lu || !info) {
+    xg::set_error("xg_lu_get_info: bad argument");
+    return XG_ERR_ARG;
+  }
+  std::memset(info, 0, sizeof(*info));
+  info->n = lu->S.n;
+  info->nnz_a = lu->S.nnz_a;
+  info->nnz_lu = lu->nnz_lu;
+  info->precision = lu->precision;
+  info->levels = lu->S.levels;
+  info->n_dense = lu->S.n_dense;
+  info->refactor_flops = lu->S.refactor_flops;
+  info->solve_flops = lu->S.solve_flops;
+  info->min_pivot = lu->S.min_pivot;
+  info->max_pivot = lu->S.max_pivot;
+  return XG_OK;
+}
+
+extern "C" int xg_lu_get_symbolic(const xg_lu *lu, int *P, int *Q, int *lu_rowptr, int *lu_colidx) {
+  if (!lu) {
+    xg::set_error("xg_lu_get_symbolic: bad argument");
+    return XG_ERR_ARG;
+  }
+  const xg::LuSymbolic &S = lu->S;
+  if (P) std::memcpy(P, S.P.data(), sizeof(int) * S.n);
+  if (Q) std::memcpy(Q, S.Q.data(), sizeof(int) * S.n);
+  if (lu_rowptr) std::memcpy(lu_rowptr, S.rp.data(), sizeof(int) * (S.n + 1));
+  if (lu_colidx) std::memcpy(lu_colidx, S.ci.data(), sizeof(int) * S.ci.size());
+  return XG_OK;
+}
+
+extern "C" int xg_lu_destroy(xg_lu *lu) {
+  if (!lu) return XG_OK;
+  cudaSetDevice(lu->device);
+  cudaStreamSynchronize(lu->stream);
+  free_lu(lu);
+  delete lu;
+  return XG_OK;
+}
+
+extern "C" int xg_lu_order(int n, const int *host_rowptr, const int *host_colidx, int *order,
+                           int *n_dense) {
+  if (n <= 0 || !host_rowptr || !host_colidx || !order) {
+    xg::set_error("xg_lu_order: bad argument");
+    return XG_ERR_ARG;
+  }
+  std::vector<int> o = xg::amd_order(n, host_rowptr, host_colidx, n_dense);
+  std::memcpy(order, o.data(), sizeof(int) * n);
+  return XG_OK;
+}
+
+extern "C" int xg_lu_analyze_host(int n, const int *host_rowptr, const int *host_colidx,
+                                  const double *host_values, int *P, int *Q, int64_t *nnz_lu) {
+  if (n <= 0 || !host_rowptr || !host_colidx || !host_values) {
+    xg::set_error("xg_lu_analyze_host: bad argument");
+    return XG_ERR_ARG;
+  }
+  xg::LuSymbolic S;
+  std::string err;
+  if (xg::lu_analyze(n, host_rowptr, host_colidx, host_values, 1e-3, &S, &err)) {
+    xg::set_error(err);
+    return XG_ERR_SINGULAR;
+  }
+  if (P) std::memcpy(P, S.P.data(), sizeof(int) * n);
+  if (Q) std::memcpy(Q, S.Q.data(), sizeof(int) * n);
+  if (nnz_lu) *nnz_lu = S.rp[n];
+  return XG_OK;
+}

@@ -117,6 +117,8 @@ struct CircuitView {
 };
 int circuit_view(xg_circuit *c, CircuitView *v);
 void set_error(const std::string &msg);
+// The device and stream of a context (api.cpp).
+int ctx_info(xg_ctx *ctx, int *device, void **stream);
 
 // load_kernels.cu (two builds: bit-exact and FMA-contracted)
 namespace exact {

@@ -1,0 +1,48 @@
+// xg_lu.h — the sparse LU of the Newton solve: host symbolic analysis
+// (lu_symbolic.cpp) shared with the device refactor/solve (lu_kernels.cu).
+//
+// The reference factors the Jacobian with KLU through Amesos
+// (N_LAS_AmesosSolver.C:231-492): one symbolic analysis per matrix pattern,
+// a numeric factorisation with partial pivoting per Newton iteration, then
+// the triangular solves.  Here the analysis runs once on the host: an
+// approximate-minimum-degree column order, then a left-looking partial-pivot
+// factorisation of the first matrix that fixes the row (pivot) order and the
+// filled L\U pattern.  Every later factorisation reuses that pivot order and
+// pattern and runs on the GPU.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace xg {
+
+struct LuSymbolic {
+  int n = 0;
+  int64_t nnz_a = 0;
+  // B = A(P, Q): row k of B is row P[k] of A, column j of B is column Q[j].
+  std::vector<int> P, Q;
+  // Filled pattern of L\U of B, row-wise (CSR), columns ascending in each
+  // row; L strictly left of the diagonal (unit diagonal implied), U from the
+  // diagonal on.
+  std::vector<int> rp, ci, diag;
+  std::vector<int> lu2a;     // LU position -> CSR index of the A entry, or -1 (fill)
+  double refactor_flops = 0;  // multiply-adds + divides of one refactorisation
+  double solve_flops = 0;     // multiply-adds of one forward + backward solve
+  int levels = 0;             // longest row dependency chain of the factorisation
+  int n_dense = 0;            // rows/columns ordered last as dense
+  double min_pivot = 0, max_pivot = 0;  // |U(k,k)| range of the analysed matrix
+};
+
+// Approximate minimum degree order of the graph of A + A^T (diagonal
+// ignored).  Returns the elimination order: order[k] = the k-th unknown.
+std::vector<int> amd_order(int n, const int *rp, const int *ci, int *n_dense);
+
+// Ordering + pivoting factorisation of A (CSR, n x n) with threshold partial
+// pivoting (diagonal preferred when |a_diag| >= pivot_tol * max|column|).
+// Returns 0, or -1 with *err set when A is structurally or numerically
+// singular.
+int lu_analyze(int n, const int *rp, const int *ci, const double *val, double pivot_tol,
+               LuSymbolic *out, std::string *err);
+
+}  // namespace xg

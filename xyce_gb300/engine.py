@@ -60,6 +60,15 @@ def lib():
     L.xg_load.argtypes = [vp, C.POINTER(abi.XgLoadFlags)]
     L.xg_load_noalloc.argtypes = [vp, C.POINTER(abi.XgLoadFlags), vp, C.c_int64]
     L.xg_probe_fp64_rate.argtypes = [i, C.POINTER(C.c_double)]
+    L.xg_lu_analyze.argtypes = [vp, i, vp, vp, vp, i, C.POINTER(vp)]
+    L.xg_lu_refactor.argtypes = [vp, vp]
+    L.xg_lu_solve.argtypes = [vp, vp, vp, i]
+    L.xg_lu_status.argtypes = [vp, C.POINTER(i), C.POINTER(i)]
+    L.xg_lu_get_info.argtypes = [vp, C.POINTER(abi.XgLuInfo)]
+    L.xg_lu_get_symbolic.argtypes = [vp, vp, vp, vp, vp]
+    L.xg_lu_destroy.argtypes = [vp]
+    L.xg_lu_order.argtypes = [i, vp, vp, vp, C.POINTER(i)]
+    L.xg_lu_analyze_host.argtypes = [i, vp, vp, vp, vp, vp, i64p]
     _lib = L
     return L
 
@@ -219,3 +228,73 @@ class Circuit:
         out["rows"] = np.repeat(np.arange(n, dtype=np.int32), np.diff(self.rowptr))
         out["cols"] = self.colidx.copy()
         return out
+
+
+class LU:
+    """Sparse LU of an n x n CSR matrix (the Newton-solve factorisation):
+    host analysis at construction, GPU refactor and solve on device buffers
+    (raw device pointers as ints)."""
+
+    def __init__(self, ctx, rowptr, colidx, values, precision=abi.LU_FP64):
+        self.rowptr = np.ascontiguousarray(rowptr, dtype=np.int32)
+        self.colidx = np.ascontiguousarray(colidx, dtype=np.int32)
+        vals = np.ascontiguousarray(values, dtype=np.float64)
+        self.n = self.rowptr.size - 1
+        h = C.c_void_p()
+        check(lib().xg_lu_analyze(ctx.h, self.n, _ptr(self.rowptr), _ptr(self.colidx), _ptr(vals),
+                                  precision, C.byref(h)))
+        self.h = h
+        info = abi.XgLuInfo()
+        check(lib().xg_lu_get_info(h, C.byref(info)))
+        self.info = info
+
+    def refactor(self, dev_values):
+        check(lib().xg_lu_refactor(self.h, C.c_void_p(dev_values)))
+
+    def solve(self, dev_b, dev_x, n_refine=0):
+        check(lib().xg_lu_solve(self.h, C.c_void_p(dev_b), C.c_void_p(dev_x), n_refine))
+
+    def status(self):
+        st, row = C.c_int(), C.c_int()
+        check(lib().xg_lu_status(self.h, C.byref(st), C.byref(row)))
+        return st.value, row.value
+
+    def symbolic(self):
+        n, nnz = self.n, self.info.nnz_lu
+        P, Q = np.zeros(n, np.int32), np.zeros(n, np.int32)
+        rp, ci = np.zeros(n + 1, np.int32), np.zeros(nnz, np.int32)
+        check(lib().xg_lu_get_symbolic(self.h, _ptr(P), _ptr(Q), _ptr(rp), _ptr(ci)))
+        return P, Q, rp, ci
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().xg_lu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def lu_analyze_host(rowptr, colidx, values):
+    """Host-only analysis: (P, Q, nnz of L\\U) of the CSR matrix."""
+    rp = np.ascontiguousarray(rowptr, dtype=np.int32)
+    ci = np.ascontiguousarray(colidx, dtype=np.int32)
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    n = rp.size - 1
+    P, Q = np.zeros(n, np.int32), np.zeros(n, np.int32)
+    nnz = C.c_int64()
+    check(lib().xg_lu_analyze_host(n, _ptr(rp), _ptr(ci), _ptr(v), _ptr(P), _ptr(Q), C.byref(nnz)))
+    return P, Q, nnz.value
+
+
+def amd_order(rowptr, colidx):
+    rp = np.ascontiguousarray(rowptr, dtype=np.int32)
+    ci = np.ascontiguousarray(colidx, dtype=np.int32)
+    n = rp.size - 1
+    order = np.zeros(n, np.int32)
+    nd = C.c_int()
+    check(lib().xg_lu_order(n, _ptr(rp), _ptr(ci), _ptr(order), C.byref(nd)))
+    return order, nd.value
