@@ -289,6 +289,35 @@ int xg_lu_order(int n, const int *host_rowptr, const int *host_colidx, int *orde
 int xg_lu_analyze_host(int n, const int *host_rowptr, const int *host_colidx,
                        const double *host_values, int *P, int *Q, int64_t *nnz_lu);
 
+/* ---- transient analysis on the GPU -----------------------------------------
+ * DC operating point, then .TRAN TSTEP TSTOP with the trapezoid ("OneStep")
+ * integrator, every Newton iteration on the device: xg_load, the trapezoid
+ * combine of residual and Jacobian (N_TIA_OneStep.C:215-352), the sparse LU
+ * above, the damped-Newton convergence test (N_NLS_DampedNewton.C:1787-1919),
+ * the local error test and step/order control (N_TIA_OneStep.C:1355-2190,
+ * N_TIA_StepErrorControl.C:520-800) and breakpoints at PULSE corners.
+ * host_x0: the DC solve's starting guess (.NODESET; NULL = zeros), or with
+ * uic the initial condition itself (no DC solve).  Records t and x[out_idx]
+ * at t = 0 and every accepted step, up to max_points. */
+typedef struct {
+  double tstop, tstep;        /* TSTEP is also the first step's upper bound */
+  double maxstep;             /* <= 0: 0.1 * tstop */
+  double reltol, abstol;      /* local error test; <= 0: 1e-3, 1e-6 */
+  int lu_precision;           /* XG_LU_FP64 or XG_LU_FP32 (+ refinement) */
+  int n_refine;               /* refinement steps per solve (FP32 factors) */
+  int uic;
+} xg_tran_options;
+typedef struct {
+  int status;                 /* last failing Newton / step status, 0 if none */
+  int steps, steps_attempted, rejected;
+  int newton_iters, factorizations, loads;
+  int dcop_iters, dcop_solves, analyses;
+  double t_end;
+} xg_tran_stats;
+int xg_tran_run(xg_circuit *c, const xg_tran_options *o, const double *host_x0, int n_out,
+                const int *out_idx, int max_points, double *host_t, double *host_v,
+                int *n_points, xg_tran_stats *st);
+
 /* xg_load_noalloc — the same load as xg_load, for callers that cannot
  * allocate device memory at the point where they load: code running while a
  * stream is captured into a CUDA graph, runtimes that give the GPU a fixed

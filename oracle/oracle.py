@@ -32,8 +32,42 @@ def lib():
         L.xgo_load.argtypes = [vp, C.POINTER(abi.XgLoadFlags), vp] + [vp] * 8
         L.xgo_load_range.argtypes = [vp, C.POINTER(abi.XgLoadFlags), vp, C.c_int, C.c_int,
                                      C.c_int] + [vp] * 8
+        L.xgo_tran_run.argtypes = [vp, C.POINTER(TranOpts), vp, vp, C.POINTER(C.c_int),
+                                   C.POINTER(TranStats)]
+        L.xgo_sparse_solve.argtypes = [C.c_int, vp, vp, vp, vp, vp, vp]
         _lib = L
     return _lib
+
+
+class TranOpts(C.Structure):
+    _fields_ = [("tstop", C.c_double), ("tstep", C.c_double), ("maxstep", C.c_double),
+                ("reltol", C.c_double), ("abstol", C.c_double), ("n_out", C.c_int),
+                ("out_idx", C.c_void_p), ("max_points", C.c_int), ("col_order", C.c_void_p),
+                ("x0", C.c_void_p), ("uic", C.c_int)]
+
+
+class TranStats(C.Structure):
+    _fields_ = [("status", C.c_int), ("steps", C.c_int), ("steps_attempted", C.c_int),
+                ("rejected", C.c_int), ("newton_iters", C.c_int), ("factorizations", C.c_int),
+                ("loads", C.c_int), ("dcop_iters", C.c_int), ("dcop_solves", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def sparse_solve(rowptr, col, val, b, col_order=None):
+    """x = A^-1 b with the transient driver's partial-pivoting sparse LU."""
+    rp = np.ascontiguousarray(rowptr, np.int32)
+    ci = np.ascontiguousarray(col, np.int32)
+    v = np.ascontiguousarray(val, np.float64)
+    bb = np.ascontiguousarray(b, np.float64)
+    x = np.zeros_like(bb)
+    q = None if col_order is None else np.ascontiguousarray(col_order, np.int32)
+    rc = lib().xgo_sparse_solve(rp.size - 1, _ptr(rp), _ptr(ci), _ptr(v),
+                                None if q is None else _ptr(q), _ptr(bb), _ptr(x))
+    if rc != 0:
+        raise RuntimeError(f"xgo_sparse_solve failed: {rc}")
+    return x
 
 
 def _ptr(a):
@@ -121,3 +155,25 @@ class OracleCircuit:
         if rc != 0:
             raise RuntimeError(f"xgo_load_range failed: {rc}")
         return scratch
+
+
+def transient(oc, tstop, tstep, out_idx, col_order=None, max_points=200000, maxstep=0.0,
+              reltol=1e-3, abstol=1e-6, x0=None, uic=False):
+    """DC operating point (from the guess x0, or x0 itself with uic) then
+    .TRAN tstep tstop on an OracleCircuit; returns (t, V[len(t), len(out_idx)],
+    stats dict)."""
+    idx = np.ascontiguousarray(out_idx, np.int32)
+    q = None if col_order is None else np.ascontiguousarray(col_order, np.int32)
+    x0a = None if x0 is None else np.ascontiguousarray(x0, np.float64)
+    o = TranOpts(tstop, tstep, maxstep, reltol, abstol, idx.size, _ptr(idx).value, max_points,
+                 None if q is None else _ptr(q).value, None if x0a is None else _ptr(x0a).value,
+                 int(bool(uic)))
+    t = np.zeros(max_points)
+    v = np.zeros((max_points, max(1, idx.size)))
+    npts = C.c_int()
+    st = TranStats()
+    rc = lib().xgo_tran_run(oc.h, C.byref(o), _ptr(t), _ptr(v), C.byref(npts), C.byref(st))
+    if rc != 0:
+        raise RuntimeError(f"xgo_tran_run failed: {rc} {st.as_dict()}")
+    n = npts.value
+    return t[:n], v[:n, : idx.size], st.as_dict()

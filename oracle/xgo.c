@@ -34,14 +34,35 @@ int xgo_slot(const xgo_circuit *c, int r, int col) {
   return -2; /* not in pattern: a bug in the stamp enumeration */
 }
 
+static int cached_slot(xgo_circuit *c, int r, int col) {
+  if (c->recording) {
+    int s = xgo_slot(c, r, col);
+    if (c->n_slots == c->cap_slots) {
+      c->cap_slots = c->cap_slots ? 2 * c->cap_slots : 1024;
+      c->slot_rc = (int *)realloc(c->slot_rc, sizeof(int) * 3 * (size_t)c->cap_slots);
+    }
+    int *e = c->slot_rc + 3 * c->n_slots++;
+    e[0] = r; e[1] = col; e[2] = s;
+    return s;
+  }
+  if (c->slot_rc && c->cursor < c->n_slots) {
+    const int *e = c->slot_rc + 3 * c->cursor;
+    if (e[0] == r && e[1] == col) {
+      ++c->cursor;
+      return e[2];
+    }
+  }
+  return xgo_slot(c, r, col);
+}
+
 /* dFdx / dQdx `+=` (sign +1) or `-=` (sign -1) on one entry. */
 void xgo_madd(xgo_circuit *c, double *vals, int r, int col, double v) {
-  int s = xgo_slot(c, r, col);
+  int s = cached_slot(c, r, col);
   if (s >= 0) vals[s] += v;
   else if (s == -2) c->bad_slot = 1;
 }
 void xgo_msub(xgo_circuit *c, double *vals, int r, int col, double v) {
-  int s = xgo_slot(c, r, col);
+  int s = cached_slot(c, r, col);
   if (s >= 0) vals[s] -= v;
   else if (s == -2) c->bad_slot = 1;
 }
@@ -165,6 +186,50 @@ int xgo_build(const xg_netlist *nl, const xg_device_options *opt,
 
   c->diode_vd = (double *)calloc((size_t)c->T[XG_DEV_DIODE].n + 1, sizeof(double));
   c->b3_member = xgo_b3_members_alloc(c->T[XG_DEV_BSIM3].n);
+
+  /* record every instance's stamp positions: one matrix load of a transient
+   * Newton iteration on zero vectors (the values are discarded) */
+  {
+    const size_t nr = (size_t)c->n_unk + 1;
+    const size_t nz = nr + (size_t)c->n_sta + (size_t)c->n_sto + 3;
+    double *zv = (double *)calloc(nz, sizeof(double));
+    double *zs = (double *)calloc(nz, sizeof(double));
+    double *m0 = (double *)calloc((size_t)c->nnz + 1, sizeof(double));
+    double *m1 = (double *)calloc((size_t)c->nnz + 1, sizeof(double));
+    xg_load_flags fl;
+    memset(&fl, 0, sizeof fl);
+    fl.transient = 1;
+    fl.newton_iter = 1;
+    xgo_io io;
+    memset(&io, 0, sizeof io);
+    io.fl = &fl;
+    io.sol = io.sol_curr = io.sol_last = zv;
+    io.sta_curr = io.sta_last = io.sto_curr = io.sto_last = zv;
+    io.sta = io.sto = io.f = io.q = io.dfdxdvp = io.dqdxdvp = zs;
+    io.dfdx = m0;
+    io.dqdx = m1;
+    for (int k = 0; k < c->n_order; ++k)
+      if (c->T[c->order[k]].n) xgo_update_state(c, c->order[k], 0, c->T[c->order[k]].n, &io);
+    c->recording = 1;
+    for (int k = 0; k < c->n_order; ++k) {
+      int t = c->order[k];
+      int nt = c->T[t].n;
+      if (!nt) continue;
+      c->slot_off[t] = (int64_t *)malloc(sizeof(int64_t) * ((size_t)nt + 1));
+      for (int i = 0; i < nt; ++i) {
+        c->slot_off[t][i] = c->n_slots;
+        xgo_load_matrices(c, t, i, i + 1, &io);
+      }
+      c->slot_off[t][nt] = c->n_slots;
+    }
+    c->recording = 0;
+    c->bad_slot = 0;
+    xgo_reset_members(c);
+    free(zv);
+    free(zs);
+    free(m0);
+    free(m1);
+  }
   *out = c;
   return XG_OK;
 }
@@ -179,6 +244,8 @@ void xgo_free(xgo_circuit *c) {
   free(c->col);
   free(c->diode_vd);
   free(c->b3_member);
+  free(c->slot_rc);
+  for (int t = 0; t < XG_NUM_DEV_TYPES; ++t) free(c->slot_off[t]);
   free(c);
 }
 
@@ -224,12 +291,16 @@ static int run_load(xgo_circuit *c, const xg_load_flags *fl, const double *const
     int a = only_type >= 0 ? i0 : 0, b = only_type >= 0 ? i1 : c->T[t].n;
     xgo_load_vectors(c, t, a, b, io);
   }
-  /* Master::loadDAEMatrices (N_DEV_DeviceMgr.C:2385-2397). */
+  /* Master::loadDAEMatrices (N_DEV_DeviceMgr.C:2385-2397), one instance at
+   * a time so each starts at its cached stamp positions. */
   for (int k = 0; k < c->n_order; ++k) {
     int t = c->order[k];
     if (!c->T[t].n || (only_type >= 0 && t != only_type)) continue;
     int a = only_type >= 0 ? i0 : 0, b = only_type >= 0 ? i1 : c->T[t].n;
-    xgo_load_matrices(c, t, a, b, io);
+    for (int i = a; i < b; ++i) {
+      c->cursor = c->slot_off[t] ? c->slot_off[t][i] : c->n_slots;
+      xgo_load_matrices(c, t, i, i + 1, io);
+    }
   }
   return c->bad_slot ? XG_ERR_ARG : XG_OK;
 }

@@ -52,6 +52,35 @@ int xgo_load_range(xgo_circuit *c, const xg_load_flags *fl, const double *const 
                    double *dqdxdvp, double *sta_next, double *sto_next, double *dfdx,
                    double *dqdx);
 
+/* ---- transient analysis (xgo_tran.c) ---------------------------------------- */
+typedef struct {
+  double tstop, tstep;        /* .TRAN TSTEP TSTOP (TSTEP = starting step) */
+  double maxstep;             /* <= 0: 0.1 * tstop */
+  double reltol, abstol;      /* local error test: 1e-3, 1e-6 */
+  int n_out;                  /* unknowns recorded at every accepted point */
+  const int *out_idx;
+  int max_points;             /* capacity of t_out / v_out */
+  const int *col_order;       /* column order of the sparse LU, or NULL */
+  const double *x0;           /* initial guess of the DC operating point
+                                 (.NODESET), n_unknowns values, or NULL = 0 */
+  int uic;                    /* 1: no DC operating point, start from x0 (.TRAN UIC) */
+} xgo_tran_opts;
+
+typedef struct {
+  int status;                 /* 0, or the failing Newton / step status */
+  int steps, steps_attempted, rejected;
+  int newton_iters, factorizations, loads;
+  int dcop_iters, dcop_solves;
+} xgo_tran_stats;
+
+/* DC operating point, then the transient to tstop; records (t, x[out_idx])
+ * at t = 0 and at every accepted step. 0 on success. */
+int xgo_tran_run(xgo_circuit *c, const xgo_tran_opts *o, double *t_out, double *v_out,
+                 int *n_points, xgo_tran_stats *st);
+/* x = A^-1 b with the driver's sparse LU (CSR A, column order or NULL). */
+int xgo_sparse_solve(int n, const int *rowptr, const int *col, const double *val,
+                     const int *col_order, const double *b, double *x);
+
 #ifdef __cplusplus
 }
 #endif

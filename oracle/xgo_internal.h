@@ -23,6 +23,14 @@ struct xgo_circuit {
   int bad_slot;
   double *diode_vd;        /* Diode Instance::Vd carried between loads  */
   void *b3_member;         /* BSIM3 members carried between loads       */
+  /* Matrix positions of each instance's dFdx/dQdx stamps in call order,
+   * found once at build (the reference caches the same positions as
+   * pointers, registerJacLIDs/setupPointers); a call whose (row, col) does
+   * not match the cached entry falls back to a search. */
+  int *slot_rc;            /* [3 * k]: row, col, position */
+  int64_t *slot_off[XG_NUM_DEV_TYPES];
+  int64_t n_slots, cap_slots, cursor;
+  int recording;
 };
 
 typedef struct {

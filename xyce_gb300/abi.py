@@ -85,6 +85,22 @@ class XgLuInfo(C.Structure):
                 ("min_pivot", C.c_double), ("max_pivot", C.c_double)]
 
 
+class XgTranOptions(C.Structure):
+    _fields_ = [("tstop", C.c_double), ("tstep", C.c_double), ("maxstep", C.c_double),
+                ("reltol", C.c_double), ("abstol", C.c_double), ("lu_precision", C.c_int),
+                ("n_refine", C.c_int), ("uic", C.c_int)]
+
+
+class XgTranStats(C.Structure):
+    _fields_ = [("status", C.c_int), ("steps", C.c_int), ("steps_attempted", C.c_int),
+                ("rejected", C.c_int), ("newton_iters", C.c_int), ("factorizations", C.c_int),
+                ("loads", C.c_int), ("dcop_iters", C.c_int), ("dcop_solves", C.c_int),
+                ("analyses", C.c_int), ("t_end", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 def device_options(gmin=1e-12, temp=300.15, tnom=300.15, voltlim=1, newmeyer=0, fma=0):
     return XgDeviceOptions(gmin, temp, tnom, voltlim, newmeyer, fma)
 

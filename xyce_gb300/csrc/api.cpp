@@ -151,6 +151,18 @@ namespace xg {
 
 void set_error(const std::string &msg) { g_err = msg; }
 
+int circuit_reset_members(xg_circuit *c) {
+  if (!c) return XG_ERR_ARG;
+  const xg::Plan &P = c->plan;
+  cudaStream_t s = c->ctx->stream;
+  if (c->d_diode_vd && P.T[XG_DEV_DIODE].n)
+    CK(cudaMemsetAsync(c->d_diode_vd, 0, sizeof(double) * P.T[XG_DEV_DIODE].n, s));
+  if (c->d_b3_mem && P.T[XG_DEV_BSIM3].n)
+    CK(cudaMemsetAsync(c->d_b3_mem, 0, sizeof(double) * kB3MemPerInstance * P.T[XG_DEV_BSIM3].n, s));
+  c->state_done = false;
+  return XG_OK;
+}
+
 int ctx_info(xg_ctx *ctx, int *device, void **stream) {
   if (!ctx) return XG_ERR_ARG;
   *device = ctx->device;
@@ -160,6 +172,7 @@ int ctx_info(xg_ctx *ctx, int *device, void **stream) {
 
 int circuit_view(xg_circuit *c, CircuitView *v) {
   if (!c || !v) return XG_ERR_ARG;
+  v->ctx = c->ctx;
   v->plan = &c->plan;
   v->device = c->ctx->device;
   v->stream = (void *)c->ctx->stream;

@@ -106,6 +106,7 @@ int build_plan(const xg_netlist *nl, const xg_device_options *opt, Plan *plan, s
 // Read-only view of a circuit's device data (api.cpp), for entry points
 // implemented in other translation units.
 struct CircuitView {
+  xg_ctx *ctx;
   const Plan *plan;
   int device;
   void *stream;
@@ -117,6 +118,8 @@ struct CircuitView {
 };
 int circuit_view(xg_circuit *c, CircuitView *v);
 void set_error(const std::string &msg);
+// Zero the members carried between loads (diode Vd, BSIM3 charges/caps).
+int circuit_reset_members(xg_circuit *c);
 // The device and stream of a context (api.cpp).
 int ctx_info(xg_ctx *ctx, int *device, void **stream);
 

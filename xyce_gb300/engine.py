@@ -69,6 +69,8 @@ def lib():
     L.xg_lu_destroy.argtypes = [vp]
     L.xg_lu_order.argtypes = [i, vp, vp, vp, C.POINTER(i)]
     L.xg_lu_analyze_host.argtypes = [i, vp, vp, vp, vp, vp, i64p]
+    L.xg_tran_run.argtypes = [vp, C.POINTER(abi.XgTranOptions), vp, i, vp, i, vp, vp,
+                              C.POINTER(i), C.POINTER(abi.XgTranStats)]
     _lib = L
     return L
 
@@ -298,3 +300,21 @@ def amd_order(rowptr, colidx):
     nd = C.c_int()
     check(lib().xg_lu_order(n, _ptr(rp), _ptr(ci), _ptr(order), C.byref(nd)))
     return order, nd.value
+
+
+def transient(circuit, tstop, tstep, out_idx, x0=None, uic=False, precision=abi.LU_FP64,
+              n_refine=0, max_points=200000, maxstep=0.0, reltol=1e-3, abstol=1e-6):
+    """DC operating point (from the guess x0, or x0 itself with uic) then
+    .TRAN tstep tstop, all on the GPU; returns (t, V[len(t), len(out_idx)],
+    stats dict)."""
+    idx = np.ascontiguousarray(out_idx, np.int32)
+    o = abi.XgTranOptions(tstop, tstep, maxstep, reltol, abstol, precision, n_refine, int(bool(uic)))
+    x0a = None if x0 is None else np.ascontiguousarray(x0, np.float64)
+    t = np.zeros(max_points)
+    v = np.zeros((max_points, max(1, idx.size)))
+    npts = C.c_int()
+    st = abi.XgTranStats()
+    check(lib().xg_tran_run(circuit.h, C.byref(o), None if x0a is None else _ptr(x0a), idx.size,
+                            _ptr(idx), max_points, _ptr(t), _ptr(v), C.byref(npts), C.byref(st)))
+    n = npts.value
+    return t[:n], v[:n, : idx.size], st.as_dict()

@@ -46,6 +46,15 @@ def inverter_chain(stages=1000, cload=10e-15, vdd=1.8, tr=100e-12, per=2e-9):
     return nl
 
 
+def inverter_chain_nodeset(stages=1000, vdd=1.8):
+    """Node-voltage guess (.NODESET) of the chain's DC state with the input
+    low: supply high, input low, stage outputs alternating high/low."""
+    v = np.zeros(stages + 2)
+    v[0] = vdd
+    v[2::2] = vdd
+    return v
+
+
 def random_mos_netlist(n_dev, n_nodes, dev_type=abi.DEV_MOS1, seed=0, models=None):
     """n_dev MOSFETs whose terminals are drawn uniformly from n_nodes nodes
     (about 4*n_dev/n_nodes attachments per node), first half NMOS, second half
@@ -105,6 +114,11 @@ def power_grid(nx=200, ny=200, n_sinks=40000, seed=0, r_seg=0.1, c_node=1e-15, v
     return nl
 
 
+def power_grid_nodeset(nx=200, ny=200, n_sinks=40000, vdd=1.8):
+    """Mesh and supply pin at the supply voltage, sink gates low."""
+    return np.r_[np.full(nx * ny + 1, vdd), np.zeros(n_sinks)]
+
+
 def ring_oscillator(stages=5, seed=0, sigma=0.10 / 3, cload=10e-15, vdd=1.8):
     """Odd-stage CMOS ring; each stage's VTO and KP scaled by (1+d), d~N(0,
     sigma) truncated at +-10% (a Monte-Carlo variant per seed)."""
@@ -129,6 +143,15 @@ def ring_oscillator(stages=5, seed=0, sigma=0.10 / 3, cload=10e-15, vdd=1.8):
     nl.cap = dict(p=nodes, m=np.full(stages, -1), value=np.full(stages, cload))
     nl.vsrc = dict(p=[0], m=[-1], kind=[abi.SRC_DC], wave=[[vdd, 0, 0, 0, 0, 0, 0]])
     return nl
+
+
+def ring_oscillator_nodeset(stages=5, vdd=1.8):
+    """Initial condition that starts the ring: supply high, ring nodes
+    alternating high/low (the odd ring breaks the pattern at one stage)."""
+    v = np.zeros(stages + 1)
+    v[0] = vdd
+    v[1::2] = vdd
+    return v
 
 
 def random_state(n_unknowns, n_state, n_store, seed=0, vmax=1.8):
