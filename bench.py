@@ -63,8 +63,210 @@ WORKLOADS = {
     "single_load_mos1_100k": dict(kind="random", n_dev=100_000, n_nodes=25_000,
                                   dev_type=abi.DEV_MOS1),
     "power_grid_200x200": dict(kind="grid"),
+    # .TRAN 1ps 20ns of a 1,000-stage CMOS inverter chain (2,000 level-1
+    # MOSFETs, 10 fF per stage, PULSE input 0->1.8 V, 100 ps edges, 2 ns
+    # period); one step = one whole transient (DC point + time steps)
+    "tran_inverter_chain_1000": dict(kind="tran", circuit="chain", stages=1000, tstop=20e-9,
+                                     tstep=1e-12),
+    # 200x200 resistive mesh (0.1 ohm, 1 fF per node) with 40,000 diode-
+    # clamped level-1 sinks on seeded PULSE gates (delay U[0,5ns]), 120,002
+    # unknowns; one step = .TRAN 1ps 3ps (the first breakpoint-dense window)
+    "tran_power_grid_200x200": dict(kind="tran", circuit="grid", nx=200, sinks=40000, tstop=3e-12,
+                                    tstep=1e-12),
+    # 101-stage ring oscillator (level-1, VTO/KP +-10% Monte-Carlo), from an
+    # initial condition, .TRAN 1ps 5ns
+    "tran_ring_oscillator_101": dict(kind="tran", circuit="ring", stages=101, tstop=5e-9,
+                                     tstep=1e-12),
 }
 METRIC = "device-loads/sec"
+TRAN_METRIC = "newton-iters/sec"
+
+
+def build_tran(name):
+    """(netlist, starting guess over the node unknowns, tstop, tstep, uic, outputs)."""
+    w = WORKLOADS[name]
+    if w["circuit"] == "chain":
+        k = w["stages"]
+        nl = netlists.inverter_chain(k)
+        return nl, netlists.inverter_chain_nodeset(k), w["tstop"], w["tstep"], False, [1, 2, k + 1]
+    if w["circuit"] == "grid":
+        nx, ns = w["nx"], w["sinks"]
+        nl = netlists.power_grid(nx, nx, ns, seed=0)
+        return (nl, netlists.power_grid_nodeset(nx, nx, ns), w["tstop"], w["tstep"], False,
+                [0, nx * nx // 2, nx * nx - 1])
+    k = w["stages"]
+    nl = netlists.ring_oscillator(k, seed=3)
+    return nl, netlists.ring_oscillator_nodeset(k), w["tstop"], w["tstep"], True, [1, k // 2, k]
+
+
+def _x0(nl, guess):
+    n = nl.n_nodes + nl.count(abi.DEV_VSRC)
+    x0 = np.zeros(n)
+    x0[:len(guess)] = guess
+    return x0
+
+
+def tran_cpu_baseline(name, seconds=20.0):
+    """The oracle's transient driver on one core (the reference is single-
+    threaded per rank) over the same window, or the leading part of it that
+    fits the time budget."""
+    from oracle.oracle import OracleCircuit, transient
+    from xyce_gb300 import engine
+    nl, guess, tstop, tstep, uic, out = build_tran(name)
+    opt = abi.device_options()
+    params = {t: engine.setup_params(nl, t, opt) for t in range(abi.NUM_DEV_TYPES) if nl.count(t)}
+    oc = OracleCircuit(nl, params, opt)
+    order, _ = engine.amd_order(oc.rowptr, oc.col)
+    window = tstop / 16
+    while True:
+        t0 = time.perf_counter()
+        _, _, st = transient(oc, window, tstep, out, col_order=order, x0=_x0(nl, guess), uic=uic)
+        dt = time.perf_counter() - t0
+        if dt >= 0.25 * seconds or window >= tstop:
+            break
+        window = min(tstop, window * max(2.0, 0.5 * seconds / max(dt, 1e-3)))
+    oc.close()
+    iters = st["newton_iters"] + st["dcop_iters"]
+    return iters / dt, iters, window, st
+
+
+def lu_shape(ctx, c):
+    """The LU analysis of the circuit's pattern (sizes of the linear algebra
+    per Newton iteration): analysed on the matrix dF/dx + dQ/dx/tstep of a
+    load at zero, its diagonal kept away from zero."""
+    from xyce_gb300 import engine
+    c.set_state(*netlists.random_state(c.n_unknowns, c.n_state, c.n_store, seed=1))
+    c.load(abi.load_flags(transient=1, newton_iter=1, pdt=1e12))
+    vals = c.download(abi.VEC_DFDX) + 1e12 * c.download(abi.VEC_DQDX)
+    rows = np.repeat(np.arange(c.n_unknowns), np.diff(c.rowptr))
+    vals[rows == c.colidx] += 1.0
+    lu = engine.LU(ctx, c.rowptr, c.colidx, vals)
+    info = lu.info
+    lu.close()
+    return info
+
+
+def run_tran(args, world, rank, local, dist):
+    import ctypes as C
+
+    import torch
+
+    from xyce_gb300 import engine
+    torch.cuda.set_device(local)
+    nl, guess, tstop, tstep, uic, out = build_tran(args.workload)
+    prec = abi.LU_FP32 if args.fp32 else abi.LU_FP64
+    nref = 2 if args.fp32 else 0
+    ctx = engine.Context(local, abi.device_options())
+    c = engine.Circuit(ctx, nl)
+    x0 = _x0(nl, guess)
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=local)
+    L = engine.lib()
+    for _ in range(args.warmup):
+        engine.transient(c, tstop, tstep, out, x0=x0, uic=uic, precision=prec, n_refine=nref)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    iters, dev_ms, launches = 0, 0.0, 0
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            l0 = L.xg_launch_count()
+            e0.record(stream)
+            tt, vv, st = engine.transient(c, tstop, tstep, out, x0=x0, uic=uic, precision=prec,
+                                          n_refine=nref)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            launches += L.xg_launch_count() - l0
+            dev_ms += e0.elapsed_time(e1)
+            iters += st["newton_iters"] + st["dcop_iters"]
+        wall = time.perf_counter() - t0
+    step_s = dev_ms / 1e3 / args.steps
+    if dist:
+        tt_ = torch.tensor([step_s], device=f"cuda:{local}")
+        dist.all_reduce(tt_, op=dist.ReduceOp.MAX)
+        step_s = float(tt_.item())
+    per_step_iters = iters / args.steps
+    value = world * per_step_iters / step_s
+    if rank != 0:
+        c.close()
+        return 0
+    # the LU of this circuit (shape of the linear-algebra work per iteration)
+    info = lu_shape(ctx, c)
+    hbm, peak_kind = measured_peaks()
+    n_types = sum(1 for t in range(abi.NUM_DEV_TYPES) if nl.count(t))
+    params = {t: c.params(t) for t in range(abi.NUM_DEV_TYPES) if nl.count(t)}
+    nparams = {t: p.shape[0] for t, p in params.items()}
+    # algorithmic bytes of one Newton iteration: the load, the combine (two
+    # matrices read, one written), refactor (L\U values and pattern read and
+    # written) and solves (read)
+    b_iter = (load_bytes(nl, c.n_unknowns, c.nnz, nparams) + 3 * 8 * c.nnz
+              + 2 * 12 * info.nnz_lu + 12 * info.nnz_lu)
+    ach = b_iter * per_step_iters / step_s / 1e9
+    cpu_v, cpu_n, cpu_window, cpu_st = tran_cpu_baseline(args.workload, seconds=args.cpu_seconds)
+    c.close()
+    line = {
+        "metric": TRAN_METRIC, "value": value, "unit": "newton-iters/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded netlist, the reference's benchmark circuit shape)",
+        "config": {"workload": args.workload, "tstop": tstop, "tstep": tstep, "unknowns": c.n_unknowns,
+                   "nnz": c.nnz, "nnz_lu": info.nnz_lu, "lu_levels": info.levels,
+                   "lu_precision": "fp32+2 refinement" if args.fp32 else "fp64",
+                   "newton_iters_per_step": per_step_iters, "time_steps_per_step": st["steps"],
+                   "l2": "working set below L2; latency-bound"},
+        "roofline": {"kernel": "newton iteration", "bound": "hbm", "achieved": ach, "peak": hbm,
+                     "unit": "GB/s", "frac": ach / hbm, "traffic": None, "peak_source": peak_kind,
+                     "algorithmic_bytes_per_iter": b_iter},
+        "e2e": {"value": value * (dev_ms / 1e3) / wall, "unit": "newton-iters/s",
+                "h2d_bytes_per_step": 8 * len(x0),
+                "d2h_bytes_per_step": int(8 * (1 + len(out)) * (st["steps"] + 1))},
+        "gpu_launches": int(launches),
+        "clocks": clocks.summary(),
+        "cpu_baseline": {"value": cpu_v, "unit": "newton-iters/s", "cores": 1, "kind": "port",
+                         "sample": f".TRAN window {cpu_window:.3g} s: {cpu_n} Newton iterations on one core"},
+        "wall_s": wall,
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_tran_reference(args, world, rank):
+    """CPU arm for transient workloads: the oracle's transient driver, one
+    core per run (the reference's transient is single-threaded per rank)."""
+    if rank != 0:
+        return 0
+    from oracle.oracle import OracleCircuit, transient
+    from xyce_gb300 import engine
+    nl, guess, tstop, tstep, uic, out = build_tran(args.workload)
+    opt = abi.device_options()
+    params = {t: engine.setup_params(nl, t, opt) for t in range(abi.NUM_DEV_TYPES) if nl.count(t)}
+    oc = OracleCircuit(nl, params, opt)
+    order, _ = engine.amd_order(oc.rowptr, oc.col)
+    # bounded per step: the leading window of the transient that one core
+    # finishes in about the budget
+    _, _, window, _ = tran_cpu_baseline(args.workload, seconds=args.cpu_seconds)
+    times, iters = [], []
+    for k in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        _, _, st = transient(oc, window, tstep, out, col_order=order, x0=_x0(nl, guess), uic=uic)
+        if k >= args.warmup:
+            times.append(time.perf_counter() - t0)
+            iters.append(st["newton_iters"] + st["dcop_iters"])
+    oc.close()
+    t = float(np.mean(times))
+    value = float(np.mean(iters)) / t
+    line = {"metric": TRAN_METRIC, "value": value, "unit": "newton-iters/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)", "impl": "reference",
+            "config": {"workload": args.workload, "tstop": window},
+            "cpu_baseline": {"value": value, "unit": "newton-iters/s", "cores": 1, "kind": "port",
+                             "sample": f".TRAN window {window:.3g} s per step, one core"},
+            "e2e": {"value": value, "unit": "newton-iters/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
 
 
 def build_workload(name):
@@ -334,6 +536,7 @@ def run_xg(args, world, rank, local, dist):
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
+    L0 = engine.lib().xg_launch_count()
     with ClockSampler(local) as clocks:
         t0 = time.perf_counter()
         for k in range(args.steps):
@@ -345,6 +548,7 @@ def run_xg(args, world, rank, local, dist):
             ev[k][2].record(stream)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
+    launches = engine.lib().xg_launch_count() - L0
     eval_ms = [ev[k][0].elapsed_time(ev[k][1]) for k in range(args.steps)]
     red_ms = [ev[k][1].elapsed_time(ev[k][2]) for k in range(args.steps)]
     step_ms = float(np.mean([a + b for a, b in zip(eval_ms, red_ms)]))
@@ -427,7 +631,7 @@ def run_xg(args, world, rank, local, dist):
                           "frac": b_load / step_s / 1e9 / hbm, "algorithmic_bytes": b_load},
         "e2e": {"value": world * n_inst / e2e_s, "unit": "instances/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
-        "gpu_launches": args.steps * (n_types + 2),
+        "gpu_launches": int(launches),
         "clocks": clk,
         "cpu_baseline": {"value": cpu_v, "unit": "instances/s", "cores": 1, "kind": "port",
                          "sample": f"{cpu_n} instance loads in ~{args.cpu_seconds:.0f} s, one core"},
@@ -445,13 +649,15 @@ def main():
     ap.add_argument("--impl", default="xg", choices=["xg", "reference"])
     ap.add_argument("--workload", default="single_load_bsim3_1M", choices=sorted(WORKLOADS))
     ap.add_argument("--fma", action="store_true")
+    ap.add_argument("--fp32", action="store_true", help="transient: FP32 factors + FP64 refinement")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args()
     world, rank, local, dist = dist_setup(args)
+    tran = WORKLOADS[args.workload]["kind"] == "tran"
     if args.impl == "reference":
-        rc = run_reference(args, world, rank)
+        rc = (run_tran_reference if tran else run_reference)(args, world, rank)
     else:
-        rc = run_xg(args, world, rank, local, dist)
+        rc = (run_tran if tran else run_xg)(args, world, rank, local, dist)
     if dist:
         dist.destroy_process_group()
     return rc

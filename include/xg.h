@@ -185,6 +185,8 @@ typedef struct {
 int  xg_abi_version(void);
 const char *xg_last_error(void);
 const char *xg_status_string(int status);
+/* Kernels this library has launched since it was loaded (all contexts). */
+long long xg_launch_count(void);
 
 /* Sustained FP64 fused-multiply-add throughput of a GPU [flop/s] (2 flops per
  * DFMA), measured with a short DFMA-chain kernel: the roofline denominator of

@@ -115,3 +115,25 @@ def test_full_size_power_grid_solve(gpu_ctx, oracle_lib):
     x32, status, _ = _solve(gpu_ctx, A0, A, b, abi.LU_FP32, 3)
     assert status == 0
     assert _backward_error(A, x32, b) <= 1e-13
+
+
+@pytest.mark.parametrize("case", ["inverter_chain_1000", "ring_oscillator_101"])
+def test_sequential_cta_and_grid_paths_agree(case, gpu_ctx, oracle_lib, monkeypatch):
+    """Narrow factors are walked by one lane, small ones run in one CTA out of
+    shared memory, the rest grid-wide; forcing each path on the same matrix
+    gives the same solution."""
+    nl = CASES[case]()
+    A = circuit_jacobian(nl, seed=5)
+    b = np.random.default_rng(11).standard_normal(A.shape[0])
+    xs = []
+    for env in ({}, {"XG_LU_NO_SEQ": "1"}, {"XG_LU_NO_SEQ": "1", "XG_LU_NO_CTA": "1"}):
+        for k in ("XG_LU_NO_SEQ", "XG_LU_NO_CTA"):
+            monkeypatch.delenv(k, raising=False)
+        for k, v in env.items():
+            monkeypatch.setenv(k, v)
+        x, st, _ = _solve(gpu_ctx, A, A, b, abi.LU_FP64, 0)
+        assert st == 0
+        assert _backward_error(A, x, b) <= 1e-13
+        xs.append(x)
+    for x in xs[1:]:
+        assert np.abs(x - xs[0]).max() <= 1e-12 * np.abs(xs[0]).max()

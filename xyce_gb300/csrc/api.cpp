@@ -10,6 +10,9 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <atomic>
+
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -68,6 +71,7 @@ struct xg_circuit {
   double *d_terms = nullptr;     // per-load stamp terms
   int64_t *d_red_ptr = nullptr;
   uint32_t *d_red_idx = nullptr;
+  int64_t *d_long_out = nullptr; // outputs reduced by a warp each
   double *d_diode_vd = nullptr;  // Diode Instance::Vd carried between loads
   double *d_b3_mem = nullptr;    // BSIM3 members carried between loads
   bool state_done = false;
@@ -95,6 +99,7 @@ void free_circuit(xg_circuit *c) {
   cudaFree(c->d_out);
   cudaFree(c->d_terms);
   cudaFree(c->d_red_ptr);
+  cudaFree(c->d_long_out);
   cudaFree(c->d_red_idx);
   cudaFree(c->d_diode_vd);
   cudaFree(c->d_b3_mem);
@@ -163,6 +168,9 @@ int circuit_reset_members(xg_circuit *c) {
   return XG_OK;
 }
 
+static std::atomic<long long> g_launches{0};
+void count_launches(int k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+
 int ctx_info(xg_ctx *ctx, int *device, void **stream) {
   if (!ctx) return XG_ERR_ARG;
   *device = ctx->device;
@@ -182,7 +190,17 @@ int circuit_view(xg_circuit *c, CircuitView *v) {
                  c->d_diode_vd, c->d_b3_mem, c->d_sta[1]};
   v->red_ptr = c->d_red_ptr;
   v->red_idx = c->d_red_idx;
+  v->long_out = c->d_long_out;
   return XG_OK;
+}
+
+ReduceArgs reduce_args(const Plan &P, const double *terms, const int64_t *red_ptr,
+                       const uint32_t *red_idx, const int64_t *d_long_out, double *out, int64_t o0,
+                       int64_t o1) {
+  auto lo = std::lower_bound(P.long_out.begin(), P.long_out.end(), o0);
+  auto hi = std::lower_bound(P.long_out.begin(), P.long_out.end(), o1);
+  return ReduceArgs{terms, red_ptr, red_idx, d_long_out + (lo - P.long_out.begin()),
+                    (int64_t)(hi - lo), out, o0, o1};
 }
 
 }  // namespace xg
@@ -192,6 +210,8 @@ extern "C" {
 int xg_abi_version(void) { return XG_ABI_VERSION; }
 
 const char *xg_last_error(void) { return g_err.c_str(); }
+
+long long xg_launch_count(void) { return xg::g_launches.load(std::memory_order_relaxed); }
 
 const char *xg_status_string(int status) {
   switch (status) {
@@ -293,6 +313,10 @@ int xg_circuit_create(xg_ctx *ctx, const xg_netlist *nl, xg_circuit **out) {
   if (!rc) rc = dalloc(&c->d_terms, P.n_terms);
   if (!rc) rc = dalloc(&c->d_red_ptr, P.n_out + 1);
   if (!rc) rc = dalloc(&c->d_red_idx, (int64_t)P.red_idx.size());
+  if (!rc) rc = dalloc(&c->d_long_out, (int64_t)P.long_out.size());
+  if (!rc && !P.long_out.empty() &&
+      cudaMemcpy(c->d_long_out, P.long_out.data(), P.long_out.size() * sizeof(int64_t),
+                 cudaMemcpyHostToDevice) != cudaSuccess) rc = fail(XG_ERR_CUDA, "copy long_out");
   if (!rc) rc = dalloc(&c->d_diode_vd, P.T[XG_DEV_DIODE].n);
   if (!rc) rc = dalloc(&c->d_b3_mem, (int64_t)kB3MemPerInstance * P.T[XG_DEV_BSIM3].n);
   for (int t = 0; t < XG_NUM_DEV_TYPES && !rc; ++t) {
@@ -485,11 +509,10 @@ int xg_update_state(xg_circuit *c, const xg_load_flags *flags) {
 }
 
 static int reduce_range(xg_circuit *c, int64_t o0, int64_t o1) {
-  int rc = c->opt.fma
-               ? xg::fast::launch_reduce(c->d_terms, c->d_red_ptr, c->d_red_idx, c->d_out, o0, o1,
-                                         c->ctx->stream)
-               : xg::exact::launch_reduce(c->d_terms, c->d_red_ptr, c->d_red_idx, c->d_out, o0, o1,
-                                          c->ctx->stream);
+  const xg::ReduceArgs a = xg::reduce_args(c->plan, c->d_terms, c->d_red_ptr, c->d_red_idx,
+                                           c->d_long_out, c->d_out, o0, o1);
+  int rc = c->opt.fma ? xg::fast::launch_reduce(a, c->ctx->stream)
+                      : xg::exact::launch_reduce(a, c->ctx->stream);
   return rc ? fail(rc, "reduce kernel launch failed") : XG_OK;
 }
 

@@ -14,6 +14,8 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include <cstdint>
 
 #include "xg_internal.h"
@@ -647,16 +649,46 @@ __global__ void __launch_bounds__(128) mos1_kernel(DevType t, DevOptions o, Flag
 #include "bsim3_eval.cuh"
 
 // ---- fixed-order reduction ---------------------------------------------------
-__global__ void __launch_bounds__(256) reduce_kernel(const double *__restrict__ terms,
-                                                     const int64_t *__restrict__ red_ptr,
-                                                     const uint32_t *__restrict__ red_idx,
-                                                     double *__restrict__ out, int64_t o0, int64_t o1) {
-  for (int64_t o = o0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < o1;
-       o += (int64_t)gridDim.x * blockDim.x) {
-    int64_t b = __ldg(red_ptr + o), e = __ldg(red_ptr + o + 1);
+// Each output is the sum of its terms in the reference's statement order,
+// s = ((0 + t1) + t2) + ..., so the result is bit-identical to a serial load.
+// Short outputs take a thread each.  Outputs with more than kLongSegment
+// terms (a supply node collects a term from every device on it) take a warp
+// each: the warp gathers the terms, 256 at a time, into shared memory with
+// independent loads, and one lane adds them in order.  Blocks [0, long_blocks)
+// serve the long outputs, the rest the short ones.
+constexpr int kRedThreads = 256;
+constexpr int kRedWarps = kRedThreads / 32;
+constexpr int kRedChunk = 256;
+
+__global__ void __launch_bounds__(kRedThreads) reduce_kernel(ReduceArgs a, int long_blocks) {
+  if ((int)blockIdx.x < long_blocks) {
+    __shared__ double buf[kRedWarps][kRedChunk];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int64_t w = (int64_t)blockIdx.x * kRedWarps + wid; w < a.n_long;
+         w += (int64_t)long_blocks * kRedWarps) {
+      const int64_t o = a.long_out[w];
+      const int64_t b = __ldg(a.red_ptr + o), e = __ldg(a.red_ptr + o + 1);
+      double s = 0.0;
+      for (int64_t base = b; base < e; base += kRedChunk) {
+        const int cnt = (int)(e - base < kRedChunk ? e - base : kRedChunk);
+        for (int j = lane; j < cnt; j += 32) buf[wid][j] = __ldg(a.terms + __ldg(a.red_idx + base + j));
+        __syncwarp();
+        if (lane == 0)
+          for (int j = 0; j < cnt; ++j) s += buf[wid][j];
+        __syncwarp();
+      }
+      if (lane == 0) a.out[o] = s;
+    }
+    return;
+  }
+  const int64_t nb = (int64_t)gridDim.x - long_blocks;
+  for (int64_t o = a.o0 + ((int64_t)blockIdx.x - long_blocks) * blockDim.x + threadIdx.x; o < a.o1;
+       o += nb * blockDim.x) {
+    const int64_t b = __ldg(a.red_ptr + o), e = __ldg(a.red_ptr + o + 1);
+    if (e - b > kLongSegment) continue;  // a warp sums it
     double s = 0.0;
-    for (int64_t j = b; j < e; ++j) s += __ldg(terms + __ldg(red_idx + j));
-    out[o] = s;
+    for (int64_t j = b; j < e; ++j) s += __ldg(a.terms + __ldg(a.red_idx + j));
+    a.out[o] = s;
   }
 }
 
@@ -669,24 +701,24 @@ int launch_eval(int dev_type, const DevType &t, const DevOptions &o, const Flags
   if (t.n <= 0) return XG_OK;
   cudaStream_t s = (cudaStream_t)stream;
   switch (dev_type) {
-    case XG_DEV_RES: res_kernel<<<grid_for(t.n, 256), 256, 0, s>>>(t, io); break;
-    case XG_DEV_CAP: cap_kernel<<<grid_for(t.n, 256), 256, 0, s>>>(t, io); break;
-    case XG_DEV_VSRC: vsrc_kernel<<<grid_for(t.n, 256), 256, 0, s>>>(t, f, io); break;
-    case XG_DEV_DIODE: diode_kernel<<<grid_for(t.n, 256), 256, 0, s>>>(t, o, f, io); break;
-    case XG_DEV_MOS1: mos1_kernel<<<grid_for(t.n, 128), 128, 0, s>>>(t, o, f, io); break;
-    case XG_DEV_BSIM3: bsim3_kernel<<<grid_for(t.n, 128), 128, 0, s>>>(t, o, f, io); break;
+    case XG_DEV_RES: res_kernel<<<grid_for(t.n, 256), 256, 0, s>>>(t, io); xg::count_launches(1); break;
+    case XG_DEV_CAP: cap_kernel<<<grid_for(t.n, 256), 256, 0, s>>>(t, io); xg::count_launches(1); break;
+    case XG_DEV_VSRC: vsrc_kernel<<<grid_for(t.n, 256), 256, 0, s>>>(t, f, io); xg::count_launches(1); break;
+    case XG_DEV_DIODE: diode_kernel<<<grid_for(t.n, 256), 256, 0, s>>>(t, o, f, io); xg::count_launches(1); break;
+    case XG_DEV_MOS1: mos1_kernel<<<grid_for(t.n, 128), 128, 0, s>>>(t, o, f, io); xg::count_launches(1); break;
+    case XG_DEV_BSIM3: bsim3_kernel<<<grid_for(t.n, 128), 128, 0, s>>>(t, o, f, io); xg::count_launches(1); break;
     default: return XG_ERR_UNSUPPORTED;
   }
   return cudaGetLastError() == cudaSuccess ? XG_OK : XG_ERR_CUDA;
 }
 
-int launch_reduce(const double *terms, const int64_t *red_ptr, const uint32_t *red_idx,
-                  double *out, int64_t o0, int64_t o1, void *stream) {
-  if (o1 <= o0) return XG_OK;
-  int64_t n = o1 - o0;
-  int grid = (int)((n + 255) / 256);
+int launch_reduce(const ReduceArgs &a, void *stream) {
+  const int64_t n = a.o1 - a.o0;
+  if (n <= 0) return XG_OK;
+  int grid = (int)((n + kRedThreads - 1) / kRedThreads);
   if (grid > 152 * 32) grid = 152 * 32;
-  reduce_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(terms, red_ptr, red_idx, out, o0, o1);
+  const int long_blocks = (int)std::min<int64_t>((a.n_long + kRedWarps - 1) / kRedWarps, 152 * 8);
+  reduce_kernel<<<grid + long_blocks, kRedThreads, 0, (cudaStream_t)stream>>>(a, long_blocks); xg::count_launches(1);
   return cudaGetLastError() == cudaSuccess ? XG_OK : XG_ERR_CUDA;
 }
 

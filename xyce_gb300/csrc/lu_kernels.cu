@@ -28,6 +28,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -80,6 +81,7 @@ struct LuDev {
   const int *arp, *aci;       // A pattern (CSR) for the residual
   unsigned *ctrl;
   unsigned *done_f, *done_l, *done_u;
+  void *rdiag;                // 1 / U(k,k) per row, written by the refactor
 };
 
 // Scatter A into the L\U value array (fill entries zero), keep an FP64 copy of
@@ -124,12 +126,13 @@ __global__ void __launch_bounds__(256) lu_factor(LuDev d, T *val) {
     row = __shfl_sync(0xffffffffu, row, 0);
     if (row >= d.n) break;
     const int s = __ldg(d.rp + row), dp = __ldg(d.diag + row), e = __ldg(d.rp + row + 1);
+    T *rdiag = (T *)d.rdiag;
     for (int p = s; p < dp; ++p) {
       const int k = __ldg(d.ci + p);
+      const int kd = __ldg(d.diag + k), ke = __ldg(d.rp + k + 1);
       if (lane == 0) wait_epoch(d.done_f + k, epoch, d.ctrl);
       __syncwarp();
-      const int kd = __ldg(d.diag + k), ke = __ldg(d.rp + k + 1);
-      const T l = val[p] / __ldcg(val + kd);
+      const T l = val[p] * __ldcg(rdiag + k);
       __syncwarp();
       if (lane == 0) val[p] = l;
       for (int q = kd + 1 + lane; q < ke; q += 32) {
@@ -149,6 +152,7 @@ __global__ void __launch_bounds__(256) lu_factor(LuDev d, T *val) {
         atomicOr(&d.ctrl[C_STATUS], ST_PIVOT);
         atomicMin(&d.ctrl[C_BAD_ROW], unsigned(row));
       }
+      rdiag[row] = T(1) / u;
       __threadfence();
       st_release(d.done_f + row, epoch);
     }
@@ -180,15 +184,17 @@ __global__ void __launch_bounds__(256) lu_lsolve(LuDev d, const T *__restrict__ 
     row = __shfl_sync(0xffffffffu, row, 0);
     if (row >= d.n) break;
     const int s = __ldg(d.rp + row), dp = __ldg(d.diag + row);
+    const T bi = lane == 0 ? T(b[__ldg(d.P + row)]) : T(0);  // before any wait
     T acc = T(0);
     for (int p = s + lane; p < dp; p += 32) {
       const int k = __ldg(d.ci + p);
+      const T lv = __ldcg(val + p);
       wait_epoch(d.done_l + k, epoch, d.ctrl);
-      acc += __ldcg(val + p) * __ldcg(y + k);
+      acc += lv * __ldcg(y + k);
     }
     acc = warp_sum(acc);
     if (lane == 0) {
-      y[row] = T(b[__ldg(d.P + row)]) - acc;
+      y[row] = bi - acc;
       __threadfence();
       st_release(d.done_l + row, epoch);
     }
@@ -208,17 +214,21 @@ __global__ void __launch_bounds__(256) lu_usolve(LuDev d, const T *__restrict__ 
     if (c >= d.n) break;
     const int row = d.n - 1 - c;
     const int dp = __ldg(d.diag + row), e = __ldg(d.rp + row + 1);
+    const T yi = lane == 0 ? __ldcg(y + row) : T(0);
+    const T ri = lane == 0 ? __ldcg((const T *)d.rdiag + row) : T(0);
+    const int qi = lane == 0 ? __ldg(d.Q + row) : 0;
     T acc = T(0);
     for (int p = dp + 1 + lane; p < e; p += 32) {
       const int k = __ldg(d.ci + p);
+      const T uv = __ldcg(val + p);
       wait_epoch(d.done_u + k, epoch, d.ctrl);
-      acc += __ldcg(val + p) * __ldcg(z + k);
+      acc += uv * __ldcg(z + k);
     }
     acc = warp_sum(acc);
     if (lane == 0) {
-      const T zi = (__ldcg(y + row) - acc) / __ldcg(val + dp);
+      const T zi = (yi - acc) * ri;
       z[row] = zi;
-      x[__ldg(d.Q + row)] = double(zi);
+      x[qi] = double(zi);
       __threadfence();
       st_release(d.done_u + row, epoch);
     }
@@ -241,6 +251,341 @@ __global__ void lu_axpy(int n, const double *__restrict__ dx, double *__restrict
     x[i] += dx[i];
 }
 
+template <class T>
+struct SmemLU {
+  T *val;
+  volatile T *y;              // solve vector (forward result, then backward)
+  T *rd;                      // reciprocal pivots (one-lane solve)
+  int *ci, *rp, *diag;
+  volatile int *flag, *flag_u;
+};
+
+// Shared-memory layout, the same for factor and solve:
+// [val: T x nnz | y: T x n | rd: T x n | ci: nnz | rp: n+1 | diag: n | flag: n | flag_u: n]
+// with the T arrays each padded to 16 bytes.
+__host__ __device__ inline size_t smem_bytes(int n, int64_t nnz, size_t tsz) {
+  auto a16 = [](size_t v) { return (v + 15) & ~size_t(15); };
+  return a16(tsz * size_t(nnz)) + 2 * a16(tsz * size_t(n)) +
+         sizeof(int) * (size_t(nnz) + 4 * size_t(n) + 1);
+}
+// The one-lane factor also keeps a column -> position map of the current row.
+__host__ __device__ inline size_t smem_bytes_seq(int n, int64_t nnz, size_t tsz) {
+  return smem_bytes(n, nnz, tsz) + sizeof(int) * size_t(n);
+}
+
+template <class T>
+__device__ SmemLU<T> smem_layout(char *base, int n, int64_t nnz) {
+  auto a16 = [](size_t v) { return (v + 15) & ~size_t(15); };
+  SmemLU<T> L;
+  size_t off = 0;
+  L.val = (T *)(base + off);
+  off += a16(sizeof(T) * size_t(nnz));
+  L.y = (volatile T *)(base + off);
+  off += a16(sizeof(T) * size_t(n));
+  L.rd = (T *)(base + off);
+  off += a16(sizeof(T) * size_t(n));
+  L.ci = (int *)(base + off);
+  off += sizeof(int) * size_t(nnz);
+  L.rp = (int *)(base + off);
+  off += sizeof(int) * size_t(n + 1);
+  L.diag = (int *)(base + off);
+  off += sizeof(int) * size_t(n);
+  L.flag = (volatile int *)(base + off);
+  off += sizeof(int) * size_t(n);
+  L.flag_u = (volatile int *)(base + off);
+  return L;
+}
+
+// ---- narrow matrices: one lane walks the rows in order --------------------------
+// When the elimination has little row parallelism (a chain of inverters, a
+// ring: at most a few rows per level), handing rows between warps costs more
+// than the rows themselves.  One warp loads the factor into shared memory and
+// lane 0 factors, then solves, row after row with no flags at all.
+
+// 1/u by Newton-Raphson on the reciprocal (x <- x (2 - u x), each step
+// doubling the correct bits) from a single-precision seed; IEEE division
+// outside the range where the seed is representable.  Within 1 ulp of 1/u.
+template <class T>
+__device__ __forceinline__ T recip(T u) {
+  const double a = fabs(double(u));
+  if (!(a > 1e-30 && a < 1e30)) return T(1) / u;
+  double x = double(1.0f / float(u));
+  x = x * (2.0 - double(u) * x);
+  x = x * (2.0 - double(u) * x);
+  return T(x);
+}
+
+constexpr int kSeqThreads = 512;  // for the copies in and out; thread 0 does the walk
+
+template <class T>
+__global__ void __launch_bounds__(kSeqThreads) lu_factor_seq(LuDev d, const double *__restrict__ a,
+                                                    double *__restrict__ a_copy, int64_t nnz_a,
+                                                    T *__restrict__ val_out, int64_t nnz) {
+  extern __shared__ __align__(16) char smem[];
+  SmemLU<T> L = smem_layout<T>(smem, d.n, nnz);
+  const int n = d.n;
+  if (threadIdx.x == 0) {
+    d.ctrl[C_EPOCH_F] += 1;
+    d.ctrl[C_STATUS] = 0;
+    d.ctrl[C_BAD_ROW] = 0xffffffffu;
+  }
+  for (int64_t p = threadIdx.x; p < nnz; p += blockDim.x) {
+    const int s = d.lu2a[p];
+    L.val[p] = s >= 0 ? T(a[s]) : T(0);
+    L.ci[p] = d.ci[p];
+  }
+  for (int i = threadIdx.x; i <= n; i += blockDim.x) L.rp[i] = d.rp[i];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) L.diag[i] = d.diag[i];
+  if (a_copy != a)
+    for (int64_t p = threadIdx.x; p < nnz_a; p += blockDim.x) a_copy[p] = a[p];
+  __syncthreads();
+  // column -> position in the current row; every column a row update touches
+  // is in that row's pattern, so stale entries of earlier rows are never read
+  int *map = (int *)(L.flag_u + n);
+  if (threadIdx.x == 0) {
+    T *rd = (T *)L.y;
+    int bad = -1;
+    for (int row = 0; row < n; ++row) {
+      const int s = L.rp[row], dp = L.diag[row], e = L.rp[row + 1];
+      for (int p = s; p < e; ++p) map[L.ci[p]] = p;
+      for (int p = s; p < dp; ++p) {
+        const int k = L.ci[p];
+        const T l = L.val[p] * rd[k];
+        L.val[p] = l;
+        for (int q = L.diag[k] + 1; q < L.rp[k + 1]; ++q) {
+          const int pos = map[L.ci[q]];
+          if (pos > p && pos < e && L.ci[pos] == L.ci[q]) L.val[pos] -= l * L.val[q];
+          else bad = -2;
+        }
+      }
+      const T u = L.val[dp];
+      if (!(fabs(double(u)) > 0.0) || !isfinite(double(u))) {
+        if (bad == -1) bad = row;
+      }
+      rd[row] = recip(u);
+    }
+    if (bad == -2) atomicOr(&d.ctrl[C_STATUS], ST_PATTERN);
+    else if (bad >= 0) {
+      atomicOr(&d.ctrl[C_STATUS], ST_PIVOT);
+      d.ctrl[C_BAD_ROW] = unsigned(bad);
+    }
+  }
+  __syncthreads();
+  for (int64_t p = threadIdx.x; p < nnz; p += blockDim.x) val_out[p] = L.val[p];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) ((T *)d.rdiag)[i] = L.y[i];
+}
+
+template <class T>
+__global__ void __launch_bounds__(kSeqThreads) lu_solve_seq(LuDev d, const T *__restrict__ val, int64_t nnz,
+                                                   const double *__restrict__ b,
+                                                   double *__restrict__ x) {
+  extern __shared__ __align__(16) char smem[];
+  SmemLU<T> L = smem_layout<T>(smem, d.n, nnz);
+  const int n = d.n;
+  T *y = (T *)L.y;
+  for (int64_t p = threadIdx.x; p < nnz; p += blockDim.x) {
+    L.val[p] = val[p];
+    L.ci[p] = d.ci[p];
+  }
+  for (int i = threadIdx.x; i <= n; i += blockDim.x) L.rp[i] = d.rp[i];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    L.diag[i] = d.diag[i];
+    y[i] = T(b[d.P[i]]);
+    L.rd[i] = ((const T *)d.rdiag)[i];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int row = 0; row < n; ++row) {
+      T acc = y[row];
+      for (int p = L.rp[row]; p < L.diag[row]; ++p) acc -= L.val[p] * y[L.ci[p]];
+      y[row] = acc;
+    }
+    for (int row = n - 1; row >= 0; --row) {
+      T acc = y[row];
+      for (int p = L.diag[row] + 1; p < L.rp[row + 1]; ++p) acc -= L.val[p] * y[L.ci[p]];
+      y[row] = acc * L.rd[row];
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) x[d.Q[i]] = double(y[i]);
+}
+
+// ---- small matrices: the whole factorisation or solve in one CTA ---------------
+// When the L\U values, columns, row pointers and flags fit in shared memory,
+// one CTA of 32 warps runs the same row-claim schedule with its flags in shared
+// memory: a dependency costs a shared-memory poll instead of an L2 round trip
+// between SMs.  Chains of dependent rows (an inverter chain is one) are the
+// case this serves.
+
+constexpr int kCtaThreads = 1024;
+
+// Spin on a shared-memory flag; after a few polls back off with a short
+// sleep so waiting warps leave the issue slots to the warp they wait for.
+__device__ __forceinline__ bool wait_flag_smem(volatile int *flag, unsigned *ctrl) {
+  int it = 0;
+  while (*flag == 0) {
+    if (++it > kSpinLimit) {
+      atomicOr(&ctrl[C_STATUS], ST_TIMEOUT);
+      return false;
+    }
+    if (it > 4) __nanosleep(20);
+  }
+  __threadfence_block();
+  return true;
+}
+
+__device__ __forceinline__ int find_col_smem(const int *ci, int lo, int end, int col) {
+  int hi = end;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (ci[mid] < col) lo = mid + 1; else hi = mid;
+  }
+  return (lo < end && ci[lo] == col) ? lo : -1;
+}
+
+template <class T>
+__global__ void __launch_bounds__(kCtaThreads) lu_factor_cta(LuDev d, const double *__restrict__ a,
+                                                             double *__restrict__ a_copy, int64_t nnz_a,
+                                                             T *__restrict__ val_out, int64_t nnz) {
+  extern __shared__ __align__(16) char smem[];
+  __shared__ int claim;
+  SmemLU<T> L = smem_layout<T>(smem, d.n, nnz);
+  const int n = d.n;
+  if (threadIdx.x == 0) {
+    claim = 0;
+    d.ctrl[C_EPOCH_F] += 1;
+    d.ctrl[C_STATUS] = 0;
+    d.ctrl[C_BAD_ROW] = 0xffffffffu;
+  }
+  for (int64_t p = threadIdx.x; p < nnz; p += blockDim.x) {
+    const int s = d.lu2a[p];
+    L.val[p] = s >= 0 ? T(a[s]) : T(0);
+    L.ci[p] = d.ci[p];
+  }
+  for (int i = threadIdx.x; i <= n; i += blockDim.x) L.rp[i] = d.rp[i];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    L.diag[i] = d.diag[i];
+    L.flag[i] = 0;
+  }
+  if (a_copy != a)
+    for (int64_t p = threadIdx.x; p < nnz_a; p += blockDim.x) a_copy[p] = a[p];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  while (true) {
+    int row = 0;
+    if (lane == 0) row = atomicAdd(&claim, 1);
+    row = __shfl_sync(0xffffffffu, row, 0);
+    if (row >= n) break;
+    const int s = L.rp[row], dp = L.diag[row], e = L.rp[row + 1];
+    for (int p = s; p < dp; ++p) {
+      const int k = L.ci[p];
+      if (lane == 0) wait_flag_smem(L.flag + k, d.ctrl);
+      __syncwarp();
+      __threadfence_block();
+      const int ke = L.rp[k + 1];
+      const int kd = L.diag[k];
+      const T l = L.val[p] * L.y[k];
+      __syncwarp();
+      if (lane == 0) L.val[p] = l;
+      for (int q = kd + 1 + lane; q < ke; q += 32) {
+        const int pos = find_col_smem(L.ci, p + 1, e, L.ci[q]);
+        if (pos >= 0) L.val[pos] -= l * L.val[q];
+        else atomicOr(&d.ctrl[C_STATUS], ST_PATTERN);
+      }
+      __syncwarp();
+    }
+    if (lane == 0) {
+      const T u = L.val[dp];
+      if (!(fabs(double(u)) > 0.0) || !isfinite(double(u))) {
+        atomicOr(&d.ctrl[C_STATUS], ST_PIVOT);
+        atomicMin(&d.ctrl[C_BAD_ROW], unsigned(row));
+      }
+      L.y[row] = T(1) / u;  // the reciprocal pivot, used by later rows and the solves
+      __threadfence_block();
+      L.flag[row] = 1;
+    }
+  }
+  __syncthreads();
+  for (int64_t p = threadIdx.x; p < nnz; p += blockDim.x) val_out[p] = L.val[p];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) ((T *)d.rdiag)[i] = L.y[i];
+}
+
+// x(Q) = U \ (L \ b(P)) in one CTA; y and z share one shared-memory vector.
+template <class T>
+__global__ void __launch_bounds__(kCtaThreads) lu_solve_cta(LuDev d, const T *__restrict__ val,
+                                                            int64_t nnz, const double *__restrict__ b,
+                                                            double *__restrict__ x) {
+  extern __shared__ __align__(16) char smem[];
+  __shared__ int claim_l, claim_u;
+  SmemLU<T> L = smem_layout<T>(smem, d.n, nnz);
+  const int n = d.n;
+  volatile T *y = L.y;
+  volatile int *flag_u = L.flag_u;
+  if (threadIdx.x == 0) {
+    claim_l = 0;
+    claim_u = 0;
+  }
+  for (int64_t p = threadIdx.x; p < nnz; p += blockDim.x) {
+    L.val[p] = val[p];
+    L.ci[p] = d.ci[p];
+  }
+  for (int i = threadIdx.x; i <= n; i += blockDim.x) L.rp[i] = d.rp[i];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    L.diag[i] = d.diag[i];
+    L.flag[i] = 0;
+    flag_u[i] = 0;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  // forward: y = L \ b(P)
+  while (true) {
+    int row = 0;
+    if (lane == 0) row = atomicAdd(&claim_l, 1);
+    row = __shfl_sync(0xffffffffu, row, 0);
+    if (row >= n) break;
+    const int s = L.rp[row], dp = L.diag[row];
+    const T bi = lane == 0 ? T(b[d.P[row]]) : T(0);  // before any wait
+    T acc = T(0);
+    for (int p = s + lane; p < dp; p += 32) {
+      const int k = L.ci[p];
+      wait_flag_smem(L.flag + k, d.ctrl);
+      acc += L.val[p] * y[k];
+    }
+    acc = warp_sum(acc);
+    if (lane == 0) {
+      y[row] = bi - acc;
+      __threadfence_block();
+      L.flag[row] = 1;
+    }
+  }
+  __syncthreads();
+  // backward: z = U \ y (z overwrites y row by row: row i reads only z of rows > i)
+  while (true) {
+    int c = 0;
+    if (lane == 0) c = atomicAdd(&claim_u, 1);
+    c = __shfl_sync(0xffffffffu, c, 0);
+    if (c >= n) break;
+    const int row = n - 1 - c;
+    const int dp = L.diag[row], e = L.rp[row + 1];
+    const T ri = lane == 0 ? ((const T *)d.rdiag)[row] : T(0);
+    const int qi = lane == 0 ? d.Q[row] : 0;
+    T acc = T(0);
+    for (int p = dp + 1 + lane; p < e; p += 32) {
+      const int k = L.ci[p];
+      wait_flag_smem(flag_u + k, d.ctrl);
+      acc += L.val[p] * y[k];
+    }
+    acc = warp_sum(acc);
+    if (lane == 0) {
+      const T zi = (y[row] - acc) * ri;
+      y[row] = zi;
+      x[qi] = double(zi);
+      __threadfence_block();
+      flag_u[row] = 1;
+    }
+  }
+}
+
 }  // namespace
 }  // namespace xg
 
@@ -259,13 +604,17 @@ struct xg_lu {
   unsigned *d_ctrl = nullptr, *d_done = nullptr;  // 3n flags
   void *d_val = nullptr;                          // nnz_lu of T
   void *d_y = nullptr, *d_z = nullptr;            // n of T
+  void *d_rdiag = nullptr;                        // n of T: 1 / U(k,k)
   double *d_a = nullptr;                          // FP64 copy of A
   double *d_r = nullptr, *d_dx = nullptr;         // refinement work
   int grid_factor = 0, grid_solve = 0;
+  size_t smem_factor = 0, smem_solve = 0;  // > 0: the one-CTA path
+  int cta_threads = 0;                     // its block size (warps ~ level width)
+  bool narrow = false;                     // one lane walks the rows (<= 2 rows per level)
   bool factored = false;
   xg::LuDev dev() const {
     return xg::LuDev{S.n, d_rp, d_ci, d_diag, d_lu2a, d_P, d_Q, d_arp, d_aci, d_ctrl,
-                     d_done, d_done + S.n, d_done + 2 * S.n};
+                     d_done, d_done + S.n, d_done + 2 * S.n, d_rdiag};
   }
 };
 
@@ -291,7 +640,7 @@ int upload(V **dst, const std::vector<V> &src) {
 
 void free_lu(xg_lu *lu) {
   void *ptrs[] = {lu->d_rp, lu->d_ci, lu->d_diag, lu->d_lu2a, lu->d_P, lu->d_Q, lu->d_arp,
-                  lu->d_aci, lu->d_ctrl, lu->d_done, lu->d_val, lu->d_y, lu->d_z, lu->d_a,
+                  lu->d_aci, lu->d_ctrl, lu->d_done, lu->d_val, lu->d_y, lu->d_z, lu->d_rdiag, lu->d_a,
                   lu->d_r, lu->d_dx};
   for (void *p : ptrs)
     if (p) cudaFree(p);
@@ -300,9 +649,21 @@ void free_lu(xg_lu *lu) {
 template <class T>
 int refactor_t(xg_lu *lu, const double *dev_values) {
   xg::LuDev d = lu->dev();
+  if (lu->narrow) {
+    xg::lu_factor_seq<T><<<1, xg::kSeqThreads, lu->smem_factor, lu->stream>>>(
+        d, dev_values, lu->d_a, lu->S.nnz_a, (T *)lu->d_val, lu->nnz_lu); xg::count_launches(1);
+    XG_CU(cudaGetLastError());
+    return XG_OK;
+  }
+  if (lu->smem_factor) {
+    xg::lu_factor_cta<T><<<1, lu->cta_threads, lu->smem_factor, lu->stream>>>(
+        d, dev_values, lu->d_a, lu->S.nnz_a, (T *)lu->d_val, lu->nnz_lu); xg::count_launches(1);
+    XG_CU(cudaGetLastError());
+    return XG_OK;
+  }
   xg::lu_assemble<T><<<lu->grid_solve, 256, 0, lu->stream>>>(
-      d, dev_values, lu->d_a, lu->S.nnz_a, (T *)lu->d_val, lu->nnz_lu);
-  xg::lu_factor<T><<<lu->grid_factor, 256, 0, lu->stream>>>(d, (T *)lu->d_val);
+      d, dev_values, lu->d_a, lu->S.nnz_a, (T *)lu->d_val, lu->nnz_lu); xg::count_launches(1);
+  xg::lu_factor<T><<<lu->grid_factor, 256, 0, lu->stream>>>(d, (T *)lu->d_val); xg::count_launches(1);
   XG_CU(cudaGetLastError());
   return XG_OK;
 }
@@ -310,10 +671,22 @@ int refactor_t(xg_lu *lu, const double *dev_values) {
 template <class T>
 int solve_once(xg_lu *lu, const double *b, double *x) {
   xg::LuDev d = lu->dev();
-  xg::lu_solve_open<<<1, 1, 0, lu->stream>>>(d);
-  xg::lu_lsolve<T><<<lu->grid_factor, 256, 0, lu->stream>>>(d, (const T *)lu->d_val, b, (T *)lu->d_y);
+  if (lu->narrow) {
+    xg::lu_solve_seq<T><<<1, xg::kSeqThreads, lu->smem_solve, lu->stream>>>(d, (const T *)lu->d_val, lu->nnz_lu,
+                                                               b, x); xg::count_launches(1);
+    XG_CU(cudaGetLastError());
+    return XG_OK;
+  }
+  if (lu->smem_solve) {
+    xg::lu_solve_cta<T><<<1, lu->cta_threads, lu->smem_solve, lu->stream>>>(
+        d, (const T *)lu->d_val, lu->nnz_lu, b, x); xg::count_launches(1);
+    XG_CU(cudaGetLastError());
+    return XG_OK;
+  }
+  xg::lu_solve_open<<<1, 1, 0, lu->stream>>>(d); xg::count_launches(1);
+  xg::lu_lsolve<T><<<lu->grid_factor, 256, 0, lu->stream>>>(d, (const T *)lu->d_val, b, (T *)lu->d_y); xg::count_launches(1);
   xg::lu_usolve<T><<<lu->grid_factor, 256, 0, lu->stream>>>(d, (const T *)lu->d_val, (const T *)lu->d_y,
-                                                            (T *)lu->d_z, x);
+                                                            (T *)lu->d_z, x); xg::count_launches(1);
   XG_CU(cudaGetLastError());
   return XG_OK;
 }
@@ -325,10 +698,10 @@ int solve_t(xg_lu *lu, const double *b, double *x, int n_refine) {
   xg::LuDev d = lu->dev();
   const int nb = std::min(1024, (lu->S.n + 255) / 256);
   for (int it = 0; it < n_refine; ++it) {
-    xg::lu_residual<<<nb, 256, 0, lu->stream>>>(d, lu->d_a, x, b, lu->d_r);
+    xg::lu_residual<<<nb, 256, 0, lu->stream>>>(d, lu->d_a, x, b, lu->d_r); xg::count_launches(1);
     rc = solve_once<T>(lu, lu->d_r, lu->d_dx);
     if (rc) return rc;
-    xg::lu_axpy<<<nb, 256, 0, lu->stream>>>(lu->S.n, lu->d_dx, x);
+    xg::lu_axpy<<<nb, 256, 0, lu->stream>>>(lu->S.n, lu->d_dx, x); xg::count_launches(1);
   }
   XG_CU(cudaGetLastError());
   return XG_OK;
@@ -375,6 +748,7 @@ extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const i
       (e = cudaMalloc((void **)&lu->d_done, sizeof(unsigned) * 3 * size_t(n))) ||
       (e = cudaMalloc(&lu->d_val, tsz * size_t(lu->nnz_lu))) ||
       (e = cudaMalloc(&lu->d_y, tsz * size_t(n))) || (e = cudaMalloc(&lu->d_z, tsz * size_t(n))) ||
+      (e = cudaMalloc(&lu->d_rdiag, tsz * size_t(n))) ||
       (e = cudaMalloc((void **)&lu->d_a, sizeof(double) * size_t(S.nnz_a))) ||
       (e = cudaMalloc((void **)&lu->d_r, sizeof(double) * size_t(n))) ||
       (e = cudaMalloc((void **)&lu->d_dx, sizeof(double) * size_t(n)))) {
@@ -398,6 +772,40 @@ extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const i
   // one warp per row: never more warps than rows
   lu->grid_factor = std::max(1, std::min(sms * std::max(occ, 1), (n + 7) / 8));
   lu->grid_solve = std::max(1, std::min(sms * 4, int((lu->nnz_lu + 255) / 256)));
+  // one-CTA path when the factor (and the solve's extra vectors) fit in shared memory
+  {
+    const size_t factor_b = xg::smem_bytes_seq(n, lu->nnz_lu, tsz);
+    const size_t solve_b = factor_b;
+    int max_optin = 0;
+    cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, lu->device);
+    const size_t limit = size_t(max_optin) > 8192 ? size_t(max_optin) - 4096 : 0;
+    if (solve_b <= limit && factor_b <= limit && !std::getenv("XG_LU_NO_CTA")) {
+      cudaError_t e1, e2, e3, e4;
+      if (precision == XG_LU_FP32) {
+        e1 = cudaFuncSetAttribute(xg::lu_factor_cta<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(factor_b));
+        e2 = cudaFuncSetAttribute(xg::lu_solve_cta<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(solve_b));
+        e3 = cudaFuncSetAttribute(xg::lu_factor_seq<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(factor_b));
+        e4 = cudaFuncSetAttribute(xg::lu_solve_seq<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(solve_b));
+      } else {
+        e1 = cudaFuncSetAttribute(xg::lu_factor_cta<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(factor_b));
+        e2 = cudaFuncSetAttribute(xg::lu_solve_cta<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(solve_b));
+        e3 = cudaFuncSetAttribute(xg::lu_factor_seq<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(factor_b));
+        e4 = cudaFuncSetAttribute(xg::lu_solve_seq<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(solve_b));
+      }
+      if (e3 != cudaSuccess || e4 != cudaSuccess) e1 = e3 != cudaSuccess ? e3 : e4;
+      if (e1 == cudaSuccess && e2 == cudaSuccess) {
+        lu->smem_factor = factor_b;
+        lu->smem_solve = solve_b;
+        // as many warps as rows can be in flight, 2 to 32
+        const int warps = std::max(2, std::min(32, lu->S.max_width));
+        lu->cta_threads = 32 * warps;
+        // average rows per level: little parallelism -> the one-lane walk
+        lu->narrow = double(n) / std::max(1, lu->S.levels) < 3.0 && !std::getenv("XG_LU_NO_SEQ");
+      } else {
+        cudaGetLastError();
+      }
+    }
+  }
   *out = lu.release();
   return XG_OK;
 }
@@ -427,6 +835,10 @@ extern "C" int xg_lu_solve(xg_lu *lu, const double *dev_b, double *dev_x, int n_
   return lu->precision == XG_LU_FP32 ? solve_t<float>(lu, dev_b, dev_x, n_refine)
                                      : solve_t<double>(lu, dev_b, dev_x, n_refine);
 }
+
+namespace xg {
+const unsigned *lu_status_device(const xg_lu *lu) { return lu->d_ctrl + C_STATUS; }
+}  // namespace xg
 
 extern "C" int xg_lu_status(xg_lu *lu, int *status, int *bad_row) {
   if (!lu || !status) {

@@ -340,6 +340,9 @@ int lu_analyze(int n, const int *rp, const int *ci, const double *val, double pi
   }
   S.refactor_flops = fl;
   S.solve_flops = sfl;
+  // rows per level at the widest level: how many rows can be in flight
+  std::vector<int> width(S.levels + 1, 0);
+  for (int i = 0; i < n; ++i) S.max_width = std::max(S.max_width, ++width[level[i]]);
   return 0;
 }
 

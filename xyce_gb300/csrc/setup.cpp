@@ -782,6 +782,9 @@ int build_plan(const xg_netlist *nl, const xg_device_options *opt, Plan *plan, s
     std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
     for (size_t j = 0; j < out_of.size(); ++j) P.red_idx[(size_t)fill[(size_t)out_of[j]]++] = idx_of[j];
   }
+  P.long_out.clear();
+  for (int64_t o = 0; o < P.n_out; ++o)
+    if (P.red_ptr[(size_t)o + 1] - P.red_ptr[(size_t)o] > kLongSegment) P.long_out.push_back(o);
   return XG_OK;
 }
 

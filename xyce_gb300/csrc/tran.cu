@@ -29,6 +29,7 @@
 
 #include "xg.h"
 #include "xg_internal.h"
+#include "xg_lu.h"
 
 namespace xg {
 namespace {
@@ -213,14 +214,22 @@ struct Run {
     err = std::string(what) + ": " + cudaGetErrorString(e);
     return XG_ERR_CUDA;
   }
-  // read back the partials of the given kinds and reduce them in block order
-  int reduce(std::initializer_list<int> kinds, double *out) {
+  // read back the partials of the given kinds (and the LU status word when
+  // asked) with one synchronisation, and reduce them in block order
+  int reduce(std::initializer_list<int> kinds, double *out, unsigned *lu_status = nullptr) {
     for (int k : kinds) {
       cudaError_t e = cudaMemcpyAsync(h_part + k * kRedBlocks, partials + k * kRedBlocks,
                                       sizeof(double) * kRedBlocks, cudaMemcpyDeviceToHost, s);
       if (e != cudaSuccess) return fail_cuda(e, "partials");
     }
+    unsigned *h_status = reinterpret_cast<unsigned *>(h_part + P_N * kRedBlocks);
+    if (lu_status) {
+      cudaError_t e = cudaMemcpyAsync(h_status, lu_status_device(lu), sizeof(unsigned),
+                                      cudaMemcpyDeviceToHost, s);
+      if (e != cudaSuccess) return fail_cuda(e, "status");
+    }
     cudaError_t e = cudaStreamSynchronize(s);
+    if (lu_status) *lu_status = *h_status;
     if (e != cudaSuccess) return fail_cuda(e, "stream");
     for (int k : kinds) {
       const bool is_max = k == P_RHSMAX || k == P_LIMMAX || k == P_XMAX;
@@ -239,7 +248,7 @@ struct Run {
     return xg_load(c, &fl);
   }
 
-  int combine(bool transient, int order, double h, double out[P_N]) {
+  int combine(bool transient, int order, double h, double out[P_N], bool fetch = true) {
     CombineArgs a;
     a.n = n;
     a.n_nodes = n_nodes;
@@ -263,11 +272,14 @@ struct Run {
     a.rhs = rhs;
     a.jac = jac;
     a.partials = partials;
-    tran_combine<<<kRedBlocks, kThreads, 0, s>>>(a);
-    if (!transient && gshunt > 0.0) tran_shunt<<<grid, kThreads, 0, s>>>(n_nodes, diag, gshunt, jac);
+    tran_combine<<<kRedBlocks, kThreads, 0, s>>>(a); xg::count_launches(1);
+    if (!transient && gshunt > 0.0) {
+      tran_shunt<<<grid, kThreads, 0, s>>>(n_nodes, diag, gshunt, jac);
+      xg::count_launches(1);
+    }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail_cuda(e, "tran_combine");
-    return reduce({P_RHS2, P_RHSMAX, P_LIMMAX}, out);
+    return fetch ? reduce({P_RHS2, P_RHSMAX, P_LIMMAX}, out) : XG_OK;
   }
 
   // N_NLS_DampedNewton::converged_
@@ -326,7 +338,10 @@ struct Run {
     const double norm_init = norm_rhs;
     double norm_old = norm_rhs;
     double *x = vec(XG_VEC_SOL_NEXT), *xc = vec(XG_VEC_SOL_CURR);
-    if (transient) tran_weights<<<grid, kThreads, 0, s>>>(n, xc, x, rel_tol, abs_tol, w);
+    if (transient) {
+      tran_weights<<<grid, kThreads, 0, s>>>(n, xc, x, rel_tol, abs_tol, w);
+      xg::count_launches(1);
+    }
     int status = 0, step = 0;
     while (status == 0) {
       ++step;
@@ -334,19 +349,17 @@ struct Run {
       if ((*rc = xg_lu_refactor(lu, jac))) return 0;
       if ((*rc = xg_lu_solve(lu, rhs, dx, o->n_refine))) return 0;
       tran_update<<<kRedBlocks, kThreads, 0, s>>>(n, dx, x, xc, !transient, rel_tol, abs_tol, w,
-                                                  partials);
+                                                  partials); xg::count_launches(1);
       fl.newton_iter = step;
       fl.init_jct = 0;
       fl.init_fix = !transient && st->dcop_solves == 0 && any_limit;
       if ((*rc = load(fl))) return 0;
-      if ((*rc = combine(transient, order, h, r))) return 0;
+      if ((*rc = combine(transient, order, h, r, false))) return 0;
+      unsigned lu_status = 0;
+      if ((*rc = reduce({P_RHS2, P_RHSMAX, P_LIMMAX, P_DXW2}, r, &lu_status))) return 0;
       any_limit = r[P_LIMMAX] != 0.0;
-      double q[P_N];
-      if ((*rc = reduce({P_DXW2}, q))) return 0;
-      int lu_status = 0, bad = 0;
-      if ((*rc = xg_lu_status(lu, &lu_status, &bad))) return 0;
       if (lu_status) return -5;
-      const double upd = std::sqrt(q[P_DXW2] / n);
+      const double upd = std::sqrt(r[P_DXW2] / n);
       norm_rhs = std::sqrt(r[P_RHS2]);
       max_rhs = r[P_RHSMAX];
       const double rhs_rel = norm_rhs / norm_init, rate = norm_rhs / norm_old;
@@ -443,7 +456,7 @@ extern "C" int xg_tran_run(xg_circuit *c, const xg_tran_options *o, const double
   for (double **b : bufs) TRY_CUDA(cudaMalloc((void **)b, sizeof(double) * nr));
   TRY_CUDA(cudaMalloc((void **)&R.jac, sizeof(double) * std::max<int64_t>(R.nnz, 1)));
   TRY_CUDA(cudaMalloc((void **)&R.partials, sizeof(double) * P_N * kRedBlocks));
-  TRY_CUDA(cudaMallocHost((void **)&R.h_part, sizeof(double) * P_N * kRedBlocks));
+  TRY_CUDA(cudaMallocHost((void **)&R.h_part, sizeof(double) * (P_N * kRedBlocks + 1)));
   TRY_CUDA(cudaMalloc((void **)&R.diag, sizeof(int64_t) * nr));
   TRY_CUDA(cudaMalloc((void **)&d_rec, sizeof(double) * std::max(1, n_out) * (size_t)max_points));
   TRY_CUDA(cudaMalloc((void **)&d_idx, sizeof(int) * std::max(1, n_out)));
@@ -534,7 +547,7 @@ extern "C" int xg_tran_run(xg_circuit *c, const xg_tran_options *o, const double
     if (np >= max_points) return;
     host_t[np] = t;
     if (n_out)
-      tran_record<<<1, 128, 0, R.s>>>(n_out, d_idx, R.vec(XG_VEC_SOL_CURR), d_rec + (size_t)np * n_out);
+      tran_record<<<1, 128, 0, R.s>>>(n_out, d_idx, R.vec(XG_VEC_SOL_CURR), d_rec + (size_t)np * n_out); xg::count_launches(1);
     ++np;
   };
   auto copy_vec = [&](int dst, int src, int64_t len) -> int {
@@ -638,7 +651,7 @@ extern "C" int xg_tran_run(xg_circuit *c, const xg_tran_options *o, const double
       h_last = h;
       next_time = t + h;
       tran_init_hist<<<R.grid, kThreads, 0, R.s>>>(n, h, R.vec(XG_VEC_SOL_CURR), R.vec(XG_VEC_Q),
-                                                   R.vec(XG_VEC_F), R.xh0, R.xh1, R.qh0, R.qh1);
+                                                   R.vec(XG_VEC_F), R.xh0, R.xh1, R.qh0, R.qh1); xg::count_launches(1);
       n_steps = 0;
       order = 1;
       psi[0] = h;
@@ -657,7 +670,7 @@ extern "C" int xg_tran_run(xg_circuit *c, const xg_tran_options *o, const double
       ck = h / h_sum;
     }
     tran_predict<<<R.grid, kThreads, 0, R.s>>>(n, order, beta[1], beta[2], R.xh0, R.xh1, R.xh2,
-                                               R.xn0, R.vec(XG_VEC_SOL_NEXT));
+                                               R.xn0, R.vec(XG_VEC_SOL_NEXT)); xg::count_launches(1);
     if ((rc = copy_vec(XG_VEC_STA_NEXT, XG_VEC_STA_CURR, P.n_state)) ||
         (rc = copy_vec(XG_VEC_STO_NEXT, XG_VEC_STO_CURR, P.n_store))) {
       cleanup();
@@ -671,7 +684,7 @@ extern "C" int xg_tran_run(xg_circuit *c, const xg_tran_options *o, const double
     double est = 0.0;
     if (ok && st->steps >= 1 && !beginning) {
       tran_lte<<<kRedBlocks, kThreads, 0, R.s>>>(n, R.vec(XG_VEC_SOL_NEXT), R.xn0,
-                                                 R.vec(XG_VEC_SOL_CURR), R.partials);
+                                                 R.vec(XG_VEC_SOL_CURR), R.partials); xg::count_launches(1);
       double q[P_N];
       if ((rc = R.reduce({P_ERR2, P_XMAX}, q))) { cleanup(); return rc; }
       const double wt = reltol * q[P_XMAX] + abstol;
@@ -702,7 +715,7 @@ extern "C" int xg_tran_run(xg_circuit *c, const xg_tran_options *o, const double
       st->steps++;
       tran_history<<<R.grid, kThreads, 0, R.s>>>(n, order, R.vec(XG_VEC_SOL_NEXT), R.vec(XG_VEC_Q),
                                                  R.vec(XG_VEC_F), R.xh0, R.xh1, R.xh2, R.qh0,
-                                                 R.qh1, R.qh2);
+                                                 R.qh1, R.qh2); xg::count_launches(1);
       const double min_step = t * 10.0 * DBL_EPSILON;
       hn = std::max(hn, min_step);
       hn = std::min(hn, max_step);

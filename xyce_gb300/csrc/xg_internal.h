@@ -95,6 +95,21 @@ struct Plan {
   // summed, in reference order, into output o
   std::vector<int64_t> red_ptr;
   std::vector<uint32_t> red_idx;
+  // outputs summing more than kLongSegment terms (a supply node's row), in
+  // ascending order: reduced by a warp each instead of a thread
+  std::vector<int64_t> long_out;
+};
+constexpr int64_t kLongSegment = 64;
+
+// The reduction's device data and the long outputs inside [o0, o1).
+struct ReduceArgs {
+  const double *terms;
+  const int64_t *red_ptr;
+  const uint32_t *red_idx;
+  const int64_t *long_out;    // device, the sub-range of long outputs in [o0, o1)
+  int64_t n_long;
+  double *out;
+  int64_t o0, o1;
 };
 
 // setup.cpp
@@ -115,9 +130,17 @@ struct CircuitView {
   LoadIO io;                   // terms = the circuit's own term buffer
   const int64_t *red_ptr;
   const uint32_t *red_idx;
+  const int64_t *long_out;     // device copy of plan->long_out
 };
 int circuit_view(xg_circuit *c, CircuitView *v);
+// ReduceArgs for outputs [o0, o1) of a circuit's plan (long outputs located
+// on the host copy, addressed in the device copy).
+ReduceArgs reduce_args(const Plan &P, const double *terms, const int64_t *red_ptr,
+                       const uint32_t *red_idx, const int64_t *d_long_out, double *out, int64_t o0,
+                       int64_t o1);
 void set_error(const std::string &msg);
+// Kernel launches of this library, counted at every launch site (api.cpp).
+void count_launches(int k);
 // Zero the members carried between loads (diode Vd, BSIM3 charges/caps).
 int circuit_reset_members(xg_circuit *c);
 // The device and stream of a context (api.cpp).
@@ -127,14 +150,12 @@ int ctx_info(xg_ctx *ctx, int *device, void **stream);
 namespace exact {
 int launch_eval(int dev_type, const DevType &t, const DevOptions &o, const Flags &f,
                 const LoadIO &io, void *stream);
-int launch_reduce(const double *terms, const int64_t *red_ptr, const uint32_t *red_idx,
-                  double *out, int64_t o0, int64_t o1, void *stream);
+int launch_reduce(const ReduceArgs &a, void *stream);
 }  // namespace exact
 namespace fast {
 int launch_eval(int dev_type, const DevType &t, const DevOptions &o, const Flags &f,
                 const LoadIO &io, void *stream);
-int launch_reduce(const double *terms, const int64_t *red_ptr, const uint32_t *red_idx,
-                  double *out, int64_t o0, int64_t o1, void *stream);
+int launch_reduce(const ReduceArgs &a, void *stream);
 }  // namespace fast
 
 }  // namespace xg

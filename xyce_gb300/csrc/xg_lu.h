@@ -15,6 +15,8 @@
 #include <string>
 #include <vector>
 
+#include "xg.h"
+
 namespace xg {
 
 struct LuSymbolic {
@@ -30,6 +32,7 @@ struct LuSymbolic {
   double refactor_flops = 0;  // multiply-adds + divides of one refactorisation
   double solve_flops = 0;     // multiply-adds of one forward + backward solve
   int levels = 0;             // longest row dependency chain of the factorisation
+  int max_width = 0;          // rows in the widest level of that chain
   int n_dense = 0;            // rows/columns ordered last as dense
   double min_pivot = 0, max_pivot = 0;  // |U(k,k)| range of the analysed matrix
 };
@@ -44,5 +47,9 @@ std::vector<int> amd_order(int n, const int *rp, const int *ci, int *n_dense);
 // singular.
 int lu_analyze(int n, const int *rp, const int *ci, const double *val, double pivot_tol,
                LuSymbolic *out, std::string *err);
+
+// Device address of an LU's status word (bits as xg_lu_status reports), for
+// callers that read it back together with other results.
+const unsigned *lu_status_device(const xg_lu *lu);
 
 }  // namespace xg

@@ -33,6 +33,7 @@ def lib():
     L = C.CDLL(LIB_PATH)
     vp, i, i64p = C.c_void_p, C.c_int, C.POINTER(C.c_int64)
     L.xg_abi_version.restype = i
+    L.xg_launch_count.restype = C.c_longlong
     L.xg_last_error.restype = C.c_char_p
     L.xg_status_string.restype = C.c_char_p
     L.xg_status_string.argtypes = [i]
@@ -238,6 +239,7 @@ class LU:
     (raw device pointers as ints)."""
 
     def __init__(self, ctx, rowptr, colidx, values, precision=abi.LU_FP64):
+        self.ctx = ctx  # the context (its stream) must outlive the factorisation
         self.rowptr = np.ascontiguousarray(rowptr, dtype=np.int32)
         self.colidx = np.ascontiguousarray(colidx, dtype=np.int32)
         vals = np.ascontiguousarray(values, dtype=np.float64)
