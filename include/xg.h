@@ -320,6 +320,43 @@ int xg_tran_run(xg_circuit *c, const xg_tran_options *o, const double *host_x0, 
                 const int *out_idx, int max_points, double *host_t, double *host_v,
                 int *n_points, xg_tran_stats *st);
 
+/* ---- batched transients (serving) ---------------------------------------------
+ * Many independent requests (.STEP / Monte-Carlo variants, uneven sizes)
+ * stepped together on one GPU: the block-diagonal union of their netlists is
+ * loaded in one pass, and one warp per request refactors and solves its own
+ * sparse system (pivot order analysed per request at creation; FP32 factors
+ * with FP64 refinement or FP64), while a device-side state machine per request
+ * runs the damped-Newton test, local error test and step control of
+ * xg_tran_run.  One batch iteration (one Newton iteration of every request) is
+ * a fixed sequence of launches, captured into a CUDA graph on the batch's own
+ * stream; batches created while others run overlap on the device.
+ * Requests start from their initial condition (UIC); sources must be DC (no
+ * breakpoints).  x0[r] and out_idx[r] use request r's own unknown numbering
+ * (nodes, then its internal unknowns). */
+typedef struct xg_batch xg_batch;
+typedef struct {
+  double tstep;               /* first-step bound (.TRAN TSTEP) */
+  double maxstep;             /* <= 0: 0.1 * tstop of each request */
+  double reltol, abstol;      /* local error test; <= 0: 1e-3, 1e-6 */
+  int lu_precision;           /* XG_LU_FP64 or XG_LU_FP32 */
+  int n_refine;               /* FP64 refinement steps with FP32 factors */
+  int n_out;                  /* recorded unknowns per request */
+  int max_points;             /* recorded points per request */
+} xg_batch_options;
+int xg_batch_create(xg_ctx *ctx, int n_requests, const xg_netlist *const *netlists,
+                    const double *const *x0, const double *tstop, const int *const *out_idx,
+                    const xg_batch_options *o, xg_batch **out);
+/* enqueue `iterations` batch iterations (asynchronous, on the batch's stream) */
+int xg_batch_run(xg_batch *b, int iterations);
+/* wait = 0: *n_done = -1 while the batch's stream is busy; otherwise the
+ * number of finished requests (wait = 1 synchronises) */
+int xg_batch_poll(xg_batch *b, int wait, int *n_done);
+/* request i's recorded (t, x[out_idx]) and counters (after a poll) */
+int xg_batch_results(xg_batch *b, int i, double *host_t, double *host_v, int *n_points,
+                     xg_tran_stats *st);
+int xg_batch_info(const xg_batch *b, int *n_requests, int64_t *device_bytes);
+int xg_batch_destroy(xg_batch *b);
+
 /* xg_load_noalloc — the same load as xg_load, for callers that cannot
  * allocate device memory at the point where they load: code running while a
  * stream is captured into a CUDA graph, runtimes that give the GPU a fixed

@@ -1,0 +1,90 @@
+"""Batched transients (the serving path): each request gives the same result
+alone and inside a mix of uneven requests, to within the simulation's own
+tolerance (reltol 1e-3 of the 1.8 V swing); the mix matches the CPU
+transient driver; FP32 factors with FP64 refinement match FP64 factors; and
+batches repeat bit for bit."""
+import numpy as np
+import pytest
+
+from xyce_gb300 import abi, engine, netlists
+
+pytestmark = pytest.mark.gpu
+
+VTOL = 1e-3 * 1.8
+TSTOP = 1e-9
+
+
+def _ring(stages, seed):
+    nl = netlists.ring_oscillator(stages, seed=seed)
+    x0 = np.zeros(nl.n_nodes + nl.count(abi.DEV_VSRC))
+    x0[:nl.n_nodes] = netlists.ring_oscillator_nodeset(stages)
+    return nl, x0, [1, 2, stages // 2 + 1]
+
+
+MIX = [(5, 1), (11, 2), (51, 3), (101, 4), (31, 5)]
+
+
+def _batch(ctx, reqs, precision=abi.LU_FP64, n_refine=0, tstop=TSTOP):
+    nls, x0s, outs = zip(*reqs)
+    b = engine.Batch(ctx, list(nls), list(x0s), [tstop] * len(reqs), list(outs), precision=precision,
+                     n_refine=n_refine, max_points=8192)
+    engine.run_batch(b)
+    res = [b.results(i) for i in range(len(reqs))]
+    b.close()
+    return res
+
+
+def _agree(a, b):
+    (ta, va, sa), (tb, vb, sb) = a, b
+    assert sa["status"] == 0 and sb["status"] == 0
+    assert abs(len(ta) - len(tb)) <= 0.02 * len(tb) + 2, (len(ta), len(tb))
+    vi = np.stack([np.interp(tb, ta, va[:, k]) for k in range(va.shape[1])], 1)
+    err = np.abs(vi - vb).max()
+    assert err <= VTOL, err
+    return err
+
+
+def test_each_request_alone_and_in_the_mix(gpu_ctx):
+    gpu_ctx.set_options(abi.device_options())
+    reqs = [_ring(k, s) for k, s in MIX]
+    mixed = _batch(gpu_ctx, reqs)
+    for r, m in zip(reqs, mixed):
+        alone = _batch(gpu_ctx, [r])[0]
+        _agree(m, alone)
+        assert abs(m[0][-1] - TSTOP) < 1e-18
+
+
+def test_mix_matches_standalone_transient_and_oracle(gpu_ctx, oracle_lib):
+    from oracle.oracle import OracleCircuit, transient
+    gpu_ctx.set_options(abi.device_options())
+    reqs = [_ring(k, s) for k, s in MIX[:3]]
+    mixed = _batch(gpu_ctx, reqs)
+    for (nl, x0, out), m in zip(reqs, mixed):
+        c = engine.Circuit(gpu_ctx, nl)
+        single = engine.transient(c, TSTOP, 1e-12, out, x0=x0, uic=True)
+        c.close()
+        _agree(m, single)
+        opt = abi.device_options()
+        params = {t: engine.setup_params(nl, t, opt) for t in range(abi.NUM_DEV_TYPES) if nl.count(t)}
+        oc = OracleCircuit(nl, params, opt)
+        order, _ = engine.amd_order(oc.rowptr, oc.col)
+        cpu = transient(oc, TSTOP, 1e-12, out, col_order=order, x0=x0, uic=True)
+        _agree(m, cpu)
+
+
+def test_fp32_factors_with_refinement_match_fp64(gpu_ctx):
+    gpu_ctx.set_options(abi.device_options())
+    reqs = [_ring(k, s) for k, s in MIX]
+    a = _batch(gpu_ctx, reqs)
+    b = _batch(gpu_ctx, reqs, precision=abi.LU_FP32, n_refine=2)
+    for x, y in zip(a, b):
+        _agree(x, y)
+
+
+def test_batches_repeat_bit_for_bit(gpu_ctx):
+    gpu_ctx.set_options(abi.device_options())
+    reqs = [_ring(k, s) for k, s in MIX[:3]]
+    a = _batch(gpu_ctx, reqs)
+    b = _batch(gpu_ctx, reqs)
+    for x, y in zip(a, b):
+        assert np.array_equal(x[0], y[0]) and np.array_equal(x[1], y[1])

@@ -101,6 +101,12 @@ class XgTranStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class XgBatchOptions(C.Structure):
+    _fields_ = [("tstep", C.c_double), ("maxstep", C.c_double), ("reltol", C.c_double),
+                ("abstol", C.c_double), ("lu_precision", C.c_int), ("n_refine", C.c_int),
+                ("n_out", C.c_int), ("max_points", C.c_int)]
+
+
 def device_options(gmin=1e-12, temp=300.15, tnom=300.15, voltlim=1, newmeyer=0, fma=0):
     return XgDeviceOptions(gmin, temp, tnom, voltlim, newmeyer, fma)
 
@@ -109,6 +115,11 @@ def load_flags(dcop=0, tranop=0, acop=0, transient=1, init_jct=0, init_fix=0, ne
                inputop=0, pdt=0.0, time=0.0, init_tran=0):
     return XgLoadFlags(dcop, tranop, acop, transient, init_jct, init_fix, newton_iter, inputop,
                        pdt, time, init_tran)
+
+
+_NAME_ARRAYS = {}  # parameter-name tuple -> (C array of names, its address); lives with the module
+_MODEL_DTYPE = np.dtype([("type", "<i4"), ("polarity", "<i4"), ("n_params", "<i4"), ("pad", "<i4"),
+                         ("names", "<u8"), ("values", "<u8")])
 
 
 def _iarr(a):
@@ -199,15 +210,25 @@ class Netlist:
         keep = []
         nl = XgNetlist()
         nl.n_nodes = self.n_nodes
-        mods = (XgModelDesc * max(1, len(self.models)))()
+        # the model cards as one array laid out like xg_model_desc, one value
+        # buffer for every card, and name arrays shared by cards that give the
+        # same parameters (Monte-Carlo variants give many such cards)
+        nm = len(self.models)
+        allv = _darr([v for m in self.models for v in m.params.values()] or [0.0])
+        mods = np.zeros(max(1, nm), dtype=_MODEL_DTYPE)
+        off = 0
         for i, m in enumerate(self.models):
-            names = (C.c_char_p * max(1, len(m.params)))(*[k.encode() for k in m.params])
-            vals = _darr(list(m.params.values()) or [0.0])
-            keep += [names, vals]
-            mods[i] = XgModelDesc(m.type, m.polarity, len(m.params), names, _p(vals, _dp))
-        keep.append(mods)
-        nl.n_models = len(self.models)
-        nl.models = mods
+            key = tuple(m.params)
+            names = _NAME_ARRAYS.get(key)
+            if names is None:
+                names = (C.c_char_p * max(1, len(key)))(*[k.encode() for k in key])
+                _NAME_ARRAYS[key] = (names, C.addressof(names))
+                names = _NAME_ARRAYS[key]
+            mods[i] = (m.type, m.polarity, len(key), 0, names[1], allv.ctypes.data + 8 * off)
+            off += len(key)
+        keep += [allv, mods]
+        nl.n_models = nm
+        nl.models = C.cast(mods.ctypes.data, C.POINTER(XgModelDesc))
         if self.type_order is not None:
             to = _iarr(self.type_order)
             keep.append(to)

@@ -192,6 +192,7 @@ __device__ double pulse_value(const double *p, int n, int i, double t) {
 __global__ void __launch_bounds__(256) vsrc_kernel(DevType t, Flags f, LoadIO io) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= t.n) return;
+  if (t.cflags) f = t.cflags[t.cid[i]];
   const int n = t.n;
   int lp = ld(t.lid + i), ln = ld(t.lid + n + i), lb = ld(t.lid + 2 * n + i);
   double source;
@@ -216,6 +217,7 @@ __global__ void __launch_bounds__(256) vsrc_kernel(DevType t, Flags f, LoadIO io
 __global__ void __launch_bounds__(256) diode_kernel(DevType t, DevOptions o, Flags f, LoadIO io) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= t.n) return;
+  if (t.cflags) f = t.cflags[t.cid[i]];
   const int n = t.n;
   const double *p = t.p;
 #define PRM(k) ld(p + (k) * n + i)
@@ -336,6 +338,7 @@ __global__ void __launch_bounds__(256) diode_kernel(DevType t, DevOptions o, Fla
 __global__ void __launch_bounds__(128) mos1_kernel(DevType t, DevOptions o, Flags f, LoadIO io) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= t.n) return;
+  if (t.cflags) f = t.cflags[t.cid[i]];
   const int n = t.n;
   const double *p = t.p;
 #define PRM(k) ld(p + (k) * n + i)

@@ -1,0 +1,1295 @@
+// serve.cu — many independent transients stepped together on one GPU (the
+// serving path: .STEP / Monte-Carlo variants of a circuit, each a request).
+//
+// A batch is the block-diagonal union of its requests' netlists, set up once
+// as one circuit: one launch per device type evaluates every instance of every
+// request, and the fixed-order reduction stamps every request's matrices, with
+// each instance reading its own request's load flags (time, Newton iteration,
+// first step).  What the reference does per circuit on the host, the batch does
+// per request on the device, with no host round trip inside the time loop:
+//
+//   batch_solve    one warp per request: refactor its Jacobian with the pivot
+//                  order analysed for it at set-up, solve, FP64 refinement when
+//                  the factors are FP32, update x, weighted norm of the update;
+//   load           the union's evaluation kernels and reduction;
+//   batch_combine  one warp per request: trapezoid residual and Jacobian
+//                  (N_TIA_OneStep.C:215-352) and the norms the tests need;
+//   batch_control  one thread per request: damped-Newton convergence test
+//                  (N_NLS_DampedNewton.C:1787-1919), local error test, step and
+//                  order control (N_TIA_OneStep.C:1355-2190), finish;
+//   batch_vector   one warp per request: history update, state rotation,
+//                  waveform record, predictor of the next step.
+//
+// One batch iteration is these six launches; a run of them is captured once
+// into a CUDA graph on the batch's own stream and replayed, so batches admitted
+// at different times overlap on the device.  Requests start from their
+// initial condition (.TRAN ... UIC); their sources carry no breakpoints.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <cfloat>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "xg.h"
+#include "xg_internal.h"
+#include "xg_lu.h"
+
+namespace xg {
+namespace {
+
+enum Phase : int { PH_DONE = 0, PH_INIT = 1, PH_START = 2, PH_ITER = 3 };
+enum Action : int { A_INIT = 1, A_ACCEPT = 2, A_PREDICT = 4 };
+enum Part : int { Q_RHS2 = 0, Q_RHSMAX, Q_LIMMAX, Q_DXW2, Q_ERR2, Q_XMAX, Q_LUFAIL, Q_N };
+
+struct CState {
+  double t, h, h_last, h_sum, saved, next_time, tstop, tstep, max_step, reltol, abstol;
+  double psi[3], beta[3], ck;
+  double norm_init, norm_old, stall_rate;
+  int order, n_steps, nef, beginning, first_step;
+  int phase, nstep, stall_count, action, status, failed;
+  int steps, steps_attempted, rejected, newton_iters, loads, n_rec;
+};
+
+struct BatchDev {
+  int nc;
+  const int *uptr, *uidx;        // unknowns of request c (union ids, local order)
+  const int *sptr, *sidx;        // its state slots: ranges (start, length) sptr[c]..sptr[c+1]
+  const int *optr, *oidx;        // its store slots, the same way
+  const int *arp, *aci;          // union Jacobian pattern
+  const int *lrp_off;            // request c's local row pointers start here (n_c + 1)
+  const int64_t *lnz_off;        // its L\U entries start here
+  const int *lrp, *lci, *ldiag;  // local CSR of L\U (row pointers relative to lnz_off;
+                                 // diagonal positions per unknown, from uptr[c])
+  const int64_t *lu2a;           // L\U entry -> union Jacobian entry, -1 for fill
+  const int *lP, *lQ;            // local pivot order
+  void *lval, *lrd;              // L\U values and reciprocal pivots (FP64 or FP32)
+  double *y, *r, *dd;            // solve workspace per union unknown
+  int *map;                      // column -> position, per union unknown
+  double *x, *xc, *xl, *sta, *stac, *stal, *sto, *stoc, *stol;
+  const double *f, *q, *fvp, *qvp, *dfdx, *dqdx;
+  double *jac, *rhs, *dx, *w, *xh0, *xh1, *xh2, *qh0, *qh1, *qh2, *xn0;
+  double *part;                  // [nc][Q_N]
+  CState *cs;
+  Flags *flags;                  // per request load flags
+  const int *out_idx;            // [nc][n_out] union ids
+  int n_out, max_points;
+  double *rec_t, *rec_v;         // [nc][max_points], [nc][max_points][n_out]
+  int n_refine;
+};
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_max_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// ---- batch_solve: factor, solve, refine, update (one warp per request) -------
+template <class T>
+__global__ void __launch_bounds__(128) batch_solve(BatchDev b) {
+  const int c = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (c >= b.nc) return;
+  if (b.cs[c].phase != PH_ITER) return;
+  const int u0 = b.uptr[c], n = b.uptr[c + 1] - u0;
+  const int *rp = b.lrp + b.lrp_off[c];
+  const int64_t z0 = b.lnz_off[c];
+  const int *ci = b.lci + z0;
+  const int *diag = b.ldiag + u0;
+  T *val = (T *)b.lval + z0;
+  T *rd = (T *)b.lrd + u0;
+  int *map = b.map + u0;
+  const int *P = b.lP + u0, *Q = b.lQ + u0;
+  const int64_t nz = b.lnz_off[c + 1] - z0;
+  for (int64_t p = lane; p < nz; p += 32) {
+    const int64_t s = b.lu2a[z0 + p];
+    val[p] = s >= 0 ? T(b.jac[s]) : T(0);
+  }
+  __syncwarp();
+  int bad = 0;
+  if (lane == 0) {
+    for (int row = 0; row < n; ++row) {
+      const int s = rp[row], dp = diag[row], e = rp[row + 1];
+      for (int p = s; p < e; ++p) map[ci[p]] = p;
+      for (int p = s; p < dp; ++p) {
+        const int k = ci[p];
+        const T l = val[p] * rd[k];
+        val[p] = l;
+        for (int q = diag[k] + 1; q < rp[k + 1]; ++q) {
+          const int pos = map[ci[q]];
+          if (pos > p && pos < e && ci[pos] == ci[q]) val[pos] -= l * val[q];
+          else bad = 1;
+        }
+      }
+      const T u = val[dp];
+      if (!(fabs(double(u)) > 0.0) || !isfinite(double(u))) bad = 1;
+      rd[row] = T(1) / u;
+    }
+  }
+  __syncwarp();
+  // solve J dx = rhs, then refine against the FP64 Jacobian
+  double *y = b.y + u0;
+  for (int pass = 0; pass <= b.n_refine; ++pass) {
+    const double *src = pass == 0 ? b.rhs : b.r;
+    for (int k = lane; k < n; k += 32) y[k] = src[b.uidx[u0 + P[k]]];
+    __syncwarp();
+    if (lane == 0) {
+      for (int row = 0; row < n; ++row) {
+        T acc = T(y[row]);
+        for (int p = rp[row]; p < diag[row]; ++p) acc -= val[p] * T(y[ci[p]]);
+        y[row] = double(acc);
+      }
+      for (int row = n - 1; row >= 0; --row) {
+        T acc = T(y[row]);
+        for (int p = diag[row] + 1; p < rp[row + 1]; ++p) acc -= val[p] * T(y[ci[p]]);
+        y[row] = double(acc * rd[row]);
+      }
+    }
+    __syncwarp();
+    for (int k = lane; k < n; k += 32) {
+      const int g = b.uidx[u0 + Q[k]];
+      if (pass == 0) b.dx[g] = y[k];
+      else b.dx[g] += y[k];
+    }
+    __syncwarp();
+    if (pass < b.n_refine) {
+      // r = rhs - J dx over this request's rows (FP64)
+      for (int k = lane; k < n; k += 32) {
+        const int g = b.uidx[u0 + k];
+        double acc = b.rhs[g];
+        for (int p = b.arp[g]; p < b.arp[g + 1]; ++p) acc -= b.jac[p] * b.dx[b.aci[p]];
+        b.r[g] = acc;
+      }
+      __syncwarp();
+    }
+  }
+  // x += dx, weighted norm of the update
+  double s2 = 0.0;
+  for (int k = lane; k < n; k += 32) {
+    const int g = b.uidx[u0 + k];
+    b.x[g] += b.dx[g];
+    const double t = b.dx[g] / b.w[g];
+    s2 += t * t;
+  }
+  s2 = warp_sum_d(s2);
+  bad = __shfl_sync(0xffffffffu, bad, 0);
+  if (lane == 0) {
+    b.part[c * Q_N + Q_DXW2] = s2;
+    b.part[c * Q_N + Q_LUFAIL] = bad;
+  }
+}
+
+// Shared-memory variant: one warp per block stages its request's L\U values,
+// pattern, map and vectors in shared memory, so lane 0's walk costs shared-
+// memory latencies instead of L2 round trips.  Used when the largest
+// request's footprint fits (smem_bytes_request).
+__host__ __device__ inline size_t smem_bytes_request(int n, int64_t nz, size_t tsz) {
+  auto a16 = [](size_t v) { return (v + 15) & ~size_t(15); };
+  return a16(tsz * size_t(nz)) + a16(tsz * size_t(n)) + a16(sizeof(double) * size_t(n)) +
+         sizeof(int) * (size_t(nz) + 3 * size_t(n) + 1);
+}
+
+template <class T>
+__global__ void __launch_bounds__(32) batch_solve_smem(BatchDev b) {
+  extern __shared__ __align__(16) char sm[];
+  const int c = blockIdx.x, lane = threadIdx.x;
+  if (c >= b.nc) return;
+  if (b.cs[c].phase != PH_ITER) return;
+  const int u0 = b.uptr[c], n = b.uptr[c + 1] - u0;
+  const int64_t z0 = b.lnz_off[c];
+  const int nz = int(b.lnz_off[c + 1] - z0);
+  auto a16 = [](size_t v) { return (v + 15) & ~size_t(15); };
+  T *val = (T *)sm;
+  T *rd = (T *)(sm + a16(sizeof(T) * nz));
+  double *y = (double *)(sm + a16(sizeof(T) * nz) + a16(sizeof(T) * n));
+  int *ci = (int *)(sm + a16(sizeof(T) * nz) + a16(sizeof(T) * n) + a16(sizeof(double) * n));
+  int *rp = ci + nz, *diag = rp + n + 1, *map = diag + n;
+  const int *grp = b.lrp + b.lrp_off[c];
+  for (int p = lane; p < nz; p += 32) {
+    const int64_t s = b.lu2a[z0 + p];
+    val[p] = s >= 0 ? T(b.jac[s]) : T(0);
+    ci[p] = b.lci[z0 + p];
+  }
+  for (int i = lane; i <= n; i += 32) rp[i] = grp[i];
+  for (int i = lane; i < n; i += 32) diag[i] = b.ldiag[u0 + i];
+  __syncwarp();
+  int bad = 0;
+  if (lane == 0) {
+    for (int row = 0; row < n; ++row) {
+      const int s = rp[row], dp = diag[row], e = rp[row + 1];
+      for (int p = s; p < e; ++p) map[ci[p]] = p;
+      for (int p = s; p < dp; ++p) {
+        const int k = ci[p];
+        const T l = val[p] * rd[k];
+        val[p] = l;
+        for (int q = diag[k] + 1; q < rp[k + 1]; ++q) {
+          const int pos = map[ci[q]];
+          if (pos > p && pos < e && ci[pos] == ci[q]) val[pos] -= l * val[q];
+          else bad = 1;
+        }
+      }
+      const T u = val[dp];
+      if (!(fabs(double(u)) > 0.0) || !isfinite(double(u))) bad = 1;
+      rd[row] = T(1) / u;
+    }
+  }
+  __syncwarp();
+  const int *P = b.lP + u0, *Q = b.lQ + u0;
+  for (int pass = 0; pass <= b.n_refine; ++pass) {
+    const double *src = pass == 0 ? b.rhs : b.r;
+    for (int k = lane; k < n; k += 32) y[k] = src[b.uidx[u0 + P[k]]];
+    __syncwarp();
+    if (lane == 0) {
+      for (int row = 0; row < n; ++row) {
+        T acc = T(y[row]);
+        for (int p = rp[row]; p < diag[row]; ++p) acc -= val[p] * T(y[ci[p]]);
+        y[row] = double(acc);
+      }
+      for (int row = n - 1; row >= 0; --row) {
+        T acc = T(y[row]);
+        for (int p = diag[row] + 1; p < rp[row + 1]; ++p) acc -= val[p] * T(y[ci[p]]);
+        y[row] = double(acc * rd[row]);
+      }
+    }
+    __syncwarp();
+    for (int k = lane; k < n; k += 32) {
+      const int g = b.uidx[u0 + Q[k]];
+      if (pass == 0) b.dx[g] = y[k];
+      else b.dx[g] += y[k];
+    }
+    __syncwarp();
+    if (pass < b.n_refine) {
+      for (int k = lane; k < n; k += 32) {
+        const int g = b.uidx[u0 + k];
+        double acc = b.rhs[g];
+        for (int p = b.arp[g]; p < b.arp[g + 1]; ++p) acc -= b.jac[p] * b.dx[b.aci[p]];
+        b.r[g] = acc;
+      }
+      __syncwarp();
+    }
+  }
+  double s2 = 0.0;
+  for (int k = lane; k < n; k += 32) {
+    const int g = b.uidx[u0 + k];
+    b.x[g] += b.dx[g];
+    const double t = b.dx[g] / b.w[g];
+    s2 += t * t;
+  }
+  s2 = warp_sum_d(s2);
+  bad = __shfl_sync(0xffffffffu, bad, 0);
+  if (lane == 0) {
+    b.part[c * Q_N + Q_DXW2] = s2;
+    b.part[c * Q_N + Q_LUFAIL] = bad;
+  }
+}
+
+// ---- batch_combine: residual, Jacobian and norms (one warp per request) ------
+__global__ void __launch_bounds__(128) batch_combine(BatchDev b) {
+  const int c = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (c >= b.nc) return;
+  const CState &cs = b.cs[c];
+  if (cs.phase == PH_DONE || cs.phase == PH_INIT) return;
+  const int u0 = b.uptr[c], n = b.uptr[c + 1] - u0;
+  const int order = cs.order;
+  const double inv_h = 1.0 / cs.h, fs = order == 2 ? 0.5 : 1.0;
+  double s2 = 0.0, mx = 0.0, lim = 0.0, e2 = 0.0, xm = 0.0;
+  for (int k = lane; k < n; k += 32) {
+    const int g = b.uidx[u0 + k];
+    double r = (b.q[g] - b.qh0[g]) * inv_h;
+    r = order == 2 ? r + 0.5 * b.f[g] + 0.5 * b.qh2[g] : r + b.f[g];
+    r = -r;
+    r += b.qvp[g] * inv_h;
+    r += fs * b.fvp[g];
+    b.rhs[g] = r;
+    s2 += r * r;
+    mx = fmax(mx, fabs(r));
+    lim = fmax(lim, fmax(fabs(b.fvp[g]), fabs(b.qvp[g])));
+    const double e = b.x[g] - b.xn0[g];
+    e2 += e * e;
+    xm = fmax(xm, fabs(b.xc[g]));
+    for (int p = b.arp[g]; p < b.arp[g + 1]; ++p) b.jac[p] = inv_h * b.dqdx[p] + fs * b.dfdx[p];
+  }
+  s2 = warp_sum_d(s2);
+  e2 = warp_sum_d(e2);
+  mx = warp_max_d(mx);
+  lim = warp_max_d(lim);
+  xm = warp_max_d(xm);
+  if (lane == 0) {
+    double *pp = b.part + c * Q_N;
+    pp[Q_RHS2] = s2;
+    pp[Q_RHSMAX] = mx;
+    pp[Q_LIMMAX] = lim;
+    pp[Q_ERR2] = e2;
+    pp[Q_XMAX] = xm;
+  }
+}
+
+// ---- batch_control: Newton test and step control (one thread per request) ----
+__device__ int converged(CState &cs, int step, double max_rhs, double upd, double rhs_rel,
+                         double rate) {
+  const double eps = DBL_EPSILON, rate_max = 0.5 * DBL_MAX, min_red = 0.9, stag = 1e-3;
+  const int max_step = 20;
+  const double rhs_tol = 1e-2, dx_tol = 0.33, small_update = 1e-6;
+  if (max_rhs <= eps && max_rhs <= rhs_tol) return 1;
+  if (max_rhs <= rhs_tol && upd <= dx_tol) return 2;
+  if (step > max_step && rhs_rel <= min_red && rate <= 1.0) return 3;
+  if (upd <= small_update) return 4;
+  if (step > max_step) return -1;
+  if (rate > rate_max) return -2;
+  if (fabs(rate - 1.0) <= stag) {
+    if (cs.stall_count == 0 || rate < cs.stall_rate) cs.stall_rate = rate;
+    cs.stall_count++;
+  } else {
+    cs.stall_count = 0;
+  }
+  if (cs.stall_count == 5) {
+    cs.stall_count = 0;
+    return (rhs_rel < min_red && cs.stall_rate <= 1.0) ? 3 : -3;
+  }
+  return 0;
+}
+
+__device__ void update_coeffs(CState &cs) {
+  const double h = cs.h;
+  if (cs.order == 2) cs.psi[2] = cs.psi[1];
+  cs.psi[1] = cs.psi[0];
+  cs.psi[0] = h;
+  cs.beta[0] = 1.0;
+  if (cs.order == 2) {
+    const double rr = h / cs.psi[1];
+    cs.beta[1] = rr + rr * rr / 2;
+    cs.beta[2] = -1.0 * h * h / cs.psi[1] / cs.psi[2] / 2;
+    cs.ck = (h / cs.h_sum) / 3.0;
+  } else {
+    cs.beta[1] = h / cs.psi[1];
+    cs.beta[2] = 0.0;
+    cs.ck = h / cs.h_sum;
+  }
+}
+
+__device__ void start_step(CState &cs, Flags &fl) {
+  update_coeffs(cs);
+  cs.action |= A_PREDICT;
+  cs.phase = PH_START;
+  fl = Flags{};
+  fl.transient = 1;
+  fl.time = cs.next_time;
+  fl.pdt = 1.0 / cs.h;
+  fl.newton_iter = 0;
+  fl.init_tran = cs.first_step;
+  cs.loads++;
+}
+
+__global__ void batch_control(BatchDev b) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= b.nc) return;
+  CState &cs = b.cs[c];
+  Flags &fl = b.flags[c];
+  const double *pp = b.part + c * Q_N;
+  const int n = b.uptr[c + 1] - b.uptr[c];
+  cs.action = 0;
+  if (cs.phase == PH_DONE) return;
+  if (cs.phase == PH_INIT) {
+    // OneStep::initialize at t = 0 (no breakpoints: the stop time is tstop)
+    const double tts = cs.tstop - cs.t;
+    double hh = 0.005 * fabs(tts);
+    hh = fmin(cs.tstep, hh);
+    if (hh > cs.max_step) hh = cs.max_step;
+    cs.h = hh;
+    cs.h_sum = 2.0 * hh;
+    cs.h_last = hh;
+    cs.next_time = cs.t + hh;
+    cs.n_steps = 0;
+    cs.order = 1;
+    cs.psi[0] = hh;
+    cs.action = A_INIT;
+    start_step(cs, fl);
+    return;
+  }
+  int status = 0;
+  if (cs.phase == PH_START) {
+    const double norm = sqrt(pp[Q_RHS2]);
+    if (norm < DBL_EPSILON) {
+      status = 1;
+    } else {
+      cs.norm_init = cs.norm_old = norm;
+      cs.nstep = 0;
+      cs.phase = PH_ITER;
+      fl.newton_iter = 1;
+      cs.loads++;
+      return;
+    }
+  } else {  // PH_ITER
+    cs.nstep++;
+    cs.newton_iters++;
+    if (pp[Q_LUFAIL] != 0.0) {
+      status = -5;
+    } else {
+      const double upd = sqrt(pp[Q_DXW2] / n);
+      const double norm = sqrt(pp[Q_RHS2]), max_rhs = pp[Q_RHSMAX];
+      const double rel = norm / cs.norm_init, rate = norm / cs.norm_old;
+      cs.norm_old = norm;
+      status = converged(cs, cs.nstep, max_rhs, upd, rel, rate);
+      if (max_rhs != 0.0 && !(max_rhs < 0.0) && !(max_rhs > 0.0)) status = -6;
+      if (status == 0) {
+        fl.newton_iter = cs.nstep + 1;
+        cs.loads++;
+        return;
+      }
+    }
+  }
+  // the Newton solve of this step has ended: local error test, accept or reject
+  cs.steps_attempted++;
+  bool ok = status >= 0;
+  double est = 0.0;
+  if (ok && cs.steps >= 1 && !cs.beginning) {
+    const double wt = cs.reltol * pp[Q_XMAX] + cs.abstol;
+    est = cs.ck * sqrt(pp[Q_ERR2] / n) / wt;
+    ok = est <= 1.0;
+  }
+  const double tol_aim = 0.5, r_min = 0.25, r_max = 0.9;
+  if (ok) {
+    cs.first_step = 0;
+    cs.beginning = 0;
+    cs.n_steps++;
+    cs.nef = 0;
+    cs.t = cs.next_time;
+    double hn = cs.h;
+    cs.h_last = cs.h;
+    double rr = pow(tol_aim / (est + 0.0001), 1.0 / (cs.order + 1.0));
+    if (cs.n_steps >= 2 && cs.order == 1) {
+      cs.order = 2;
+      rr = pow(tol_aim / (est + 0.0001), 1.0 / (cs.order + 1.0));
+      if (rr <= 1.05) cs.order = 1;
+    }
+    if (rr >= 2.0) hn = 2.0 * cs.h;
+    else if (rr <= 1) hn = fmax(r_min, fmin(r_max, rr)) * cs.h;
+    cs.steps++;
+    cs.action |= A_ACCEPT;
+    const double min_step = cs.t * 10.0 * DBL_EPSILON;
+    hn = fmax(hn, min_step);
+    hn = fmin(hn, cs.max_step);
+    if (cs.tstop - cs.t >= min_step) {
+      if (cs.t + hn > cs.tstop) {
+        cs.saved = hn;
+        hn = cs.tstop - cs.t;
+      }
+      cs.next_time = cs.t + hn;
+      cs.h_sum = hn + cs.h_last;
+    }
+    cs.h = hn;
+    if (!(cs.t < cs.tstop) || fabs(cs.t - cs.tstop) <= 1e-18) {
+      cs.phase = PH_DONE;
+      return;
+    }
+  } else {
+    cs.rejected++;
+    cs.nef++;
+    for (int i = 1; i <= cs.order; ++i) cs.psi[i - 1] = cs.psi[i];
+    double hn;
+    if (status <= 0) hn = cs.h / 8;
+    else if (cs.nef == 1) hn = fmax(r_min, fmin(r_max, pow(tol_aim / (est + 0.0001), 1.0 / (cs.order + 1.0)))) * cs.h;
+    else hn = r_min * cs.h;
+    cs.order = 1;
+    hn = fmax(hn, cs.t * 10.0 * DBL_EPSILON);
+    hn = fmin(hn, cs.max_step);
+    if (cs.t + hn > cs.tstop) hn = cs.tstop - cs.t;
+    cs.next_time = cs.t + hn;
+    cs.h_sum = hn + cs.h_last;
+    cs.h = hn;
+    if (cs.nef >= 15 || cs.h < 1e-21) {
+      cs.failed = 1;
+      cs.status = status != 0 ? status : -7;
+      cs.phase = PH_DONE;
+      return;
+    }
+  }
+  start_step(cs, fl);
+}
+
+// ---- batch_vector: history, rotation, record, predictor (warp per request) ---
+__global__ void __launch_bounds__(128) batch_vector(BatchDev b) {
+  const int c = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (c >= b.nc) return;
+  CState &cs = b.cs[c];
+  const int act = cs.action;
+  if (!act) return;
+  const int u0 = b.uptr[c], n = b.uptr[c + 1] - u0;
+  if (act & A_INIT) {
+    for (int k = lane; k < n; k += 32) {
+      const int g = b.uidx[u0 + k];
+      b.xh0[g] = b.xc[g];
+      b.xh1[g] = 0.0;
+      b.qh0[g] = b.q[g];
+      b.qh1[g] = -cs.h_last * b.f[g];
+    }
+    // the initial point is the first recorded one
+    for (int j = lane; j < b.n_out; j += 32)
+      b.rec_v[(size_t)c * b.max_points * b.n_out + j] = b.xc[b.out_idx[c * b.n_out + j]];
+    if (lane == 0) {
+      b.rec_t[(size_t)c * b.max_points] = 0.0;
+      cs.n_rec = 1;
+    }
+    __syncwarp();
+  }
+  if (act & A_ACCEPT) {
+    const int order = cs.order;
+    for (int k = lane; k < n; k += 32) {
+      const int g = b.uidx[u0 + k];
+      if (order == 2) {
+        b.xh2[g] = b.xh1[g];
+        b.qh2[g] = b.f[g];
+      }
+      b.xh1[g] = b.x[g] - b.xh0[g];
+      b.qh1[g] = b.q[g] - b.qh0[g];
+      b.xh0[g] = b.x[g];
+      b.qh0[g] = b.q[g];
+      b.xl[g] = b.xc[g];
+      b.xc[g] = b.x[g];
+    }
+    // state / store of the accepted point become current (the load kernels
+    // read current and next, never last; they are ranges of slots)
+    for (int k = b.sptr[c]; k < b.sptr[c + 1]; ++k)
+      for (int s = b.sidx[2 * k] + lane; s < b.sidx[2 * k] + b.sidx[2 * k + 1]; s += 32)
+        b.stac[s] = b.sta[s];
+    for (int k = b.optr[c]; k < b.optr[c + 1]; ++k)
+      for (int s = b.oidx[2 * k] + lane; s < b.oidx[2 * k] + b.oidx[2 * k + 1]; s += 32)
+        b.stoc[s] = b.sto[s];
+    __syncwarp();
+    const int np = cs.n_rec;
+    if (np < b.max_points) {
+      for (int j = lane; j < b.n_out; j += 32)
+        b.rec_v[((size_t)c * b.max_points + np) * b.n_out + j] = b.xc[b.out_idx[c * b.n_out + j]];
+      if (lane == 0) {
+        b.rec_t[(size_t)c * b.max_points + np] = cs.t;
+        cs.n_rec = np + 1;
+      }
+    }
+  }
+  __syncwarp();
+  if ((act & A_PREDICT) && cs.phase != PH_DONE) {
+    const double b1 = cs.beta[1], b2 = cs.beta[2];
+    const int order = cs.order;
+    for (int k = lane; k < n; k += 32) {
+      const int g = b.uidx[u0 + k];
+      double v = b.xh0[g];
+      v = b1 * b.xh1[g] + v;
+      if (order == 2) v = b2 * b.xh2[g] + v;
+      b.xn0[g] = v;
+      b.x[g] = v;
+      b.w[g] = 1e-2 * fmax(fabs(b.xc[g]), fabs(v)) + 1e-6;
+    }
+    // the limiters read the previous iterate from next store: start from the
+    // current one (every state slot is rewritten by the next load)
+    for (int k = b.optr[c]; k < b.optr[c + 1]; ++k)
+      for (int s = b.oidx[2 * k] + lane; s < b.oidx[2 * k] + b.oidx[2 * k + 1]; s += 32)
+        b.sto[s] = b.stoc[s];
+  }
+}
+
+template <class V>
+int to_dev(V **d, const std::vector<V> &h) {
+  if (cudaMalloc((void **)d, sizeof(V) * std::max<size_t>(h.size(), 1)) != cudaSuccess) return XG_ERR_OOM;
+  if (!h.empty() && cudaMemcpy(*d, h.data(), sizeof(V) * h.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+    return XG_ERR_CUDA;
+  return XG_OK;
+}
+
+}  // namespace
+}  // namespace xg
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+
+struct xg_batch {
+  xg_ctx *ctx = nullptr;
+  xg_circuit *ckt = nullptr;
+  cudaStream_t stream = nullptr;
+  int nc = 0, n_out = 0, max_points = 0, precision = XG_LU_FP64;
+  xg::BatchDev dev{};
+  std::vector<void *> allocs;
+  std::vector<int> n_unk;              // unknowns per request
+  int *d_cid[XG_NUM_DEV_TYPES] = {};   // instance -> request, per type
+  cudaGraphExec_t graph = nullptr;
+  int graph_iters = 0;
+  int graph_launches_per_iter = 0;
+  size_t solve_smem = 0;               // > 0: batch_solve_smem with this much shared memory
+  int64_t bytes = 0;
+  // pinned host mirror of the request states
+  xg::CState *h_cs = nullptr;
+};
+
+namespace {
+
+// The union of the requests' netlists: nodes and models offset, instances
+// concatenated per device type (each request's instances stay in order).
+struct UnionNetlist {
+  xg_netlist nl{};
+  std::vector<xg_model_desc> models;
+  std::vector<std::vector<int>> ints;
+  std::vector<std::vector<double>> dbls;
+  std::vector<int> type_order;
+  int *iv(size_t n) { ints.emplace_back(n); return ints.back().data(); }
+  double *dv(size_t n) { dbls.emplace_back(n); return dbls.back().data(); }
+};
+
+int build_union(int n, const xg_netlist *const *nls, UnionNetlist *U,
+                std::vector<std::array<int, XG_NUM_DEV_TYPES>> *inst0, std::vector<int> *node0) {
+  for (int r = 1; r < n; ++r) {
+    const xg_netlist &a = *nls[0], &bb = *nls[r];
+    bool same = a.n_type_order == bb.n_type_order;
+    for (int k = 0; same && k < a.n_type_order; ++k) same = a.type_order[k] == bb.type_order[k];
+    if (!same) {
+      xg::set_error("xg_batch_create: requests differ in device-type load order");
+      return XG_ERR_ARG;
+    }
+  }
+  xg_netlist &u = U->nl;
+  std::memset(&u, 0, sizeof(u));
+  int nodes = 0, models = 0;
+  inst0->assign(n + 1, {});
+  node0->assign(n + 1, 0);
+  std::vector<int> model0(n + 1, 0);
+  for (int r = 0; r < n; ++r) {
+    (*node0)[r] = nodes;
+    model0[r] = models;
+    nodes += nls[r]->n_nodes;
+    models += nls[r]->n_models;
+    for (int m = 0; m < nls[r]->n_models; ++m) U->models.push_back(nls[r]->models[m]);
+  }
+  (*node0)[n] = nodes;
+  u.n_nodes = nodes;
+  u.n_models = models;
+  u.models = U->models.data();
+  if (nls[0]->type_order && nls[0]->n_type_order) {
+    U->type_order.assign(nls[0]->type_order, nls[0]->type_order + nls[0]->n_type_order);
+    u.n_type_order = nls[0]->n_type_order;
+    u.type_order = U->type_order.data();
+  }
+  auto node = [&](int r, int v) { return v < 0 ? -1 : v + (*node0)[r]; };
+  auto count = [&](int t, const xg_netlist &a) {
+    switch (t) {
+      case XG_DEV_RES: return a.res.n; case XG_DEV_CAP: return a.cap.n;
+      case XG_DEV_VSRC: return a.vsrc.n; case XG_DEV_ISRC: return a.isrc.n;
+      case XG_DEV_DIODE: return a.diode.n; case XG_DEV_MOS1: return a.mos1.n;
+      default: return a.bsim3.n;
+    }
+  };
+  for (int t = 0; t < XG_NUM_DEV_TYPES; ++t) {
+    int tot = 0;
+    for (int r = 0; r < n; ++r) {
+      (*inst0)[r][t] = tot;
+      tot += count(t, *nls[r]);
+    }
+    (*inst0)[n][t] = tot;
+  }
+  // two-terminal R, C
+  for (int which = 0; which < 2; ++which) {
+    const int t = which == 0 ? XG_DEV_RES : XG_DEV_CAP;
+    const int tot = (*inst0)[n][t];
+    if (!tot) continue;
+    int *p = U->iv(tot), *m = U->iv(tot);
+    double *val = U->dv(tot);
+    for (int r = 0; r < n; ++r) {
+      const xg_twoterm_desc &d = which == 0 ? nls[r]->res : nls[r]->cap;
+      for (int i = 0; i < d.n; ++i) {
+        const int k = (*inst0)[r][t] + i;
+        p[k] = node(r, d.p[i]);
+        m[k] = node(r, d.m[i]);
+        val[k] = d.value[i];
+      }
+    }
+    xg_twoterm_desc &o = which == 0 ? u.res : u.cap;
+    o.n = tot; o.p = p; o.m = m; o.value = val;
+  }
+  // sources
+  for (int which = 0; which < 2; ++which) {
+    const int t = which == 0 ? XG_DEV_VSRC : XG_DEV_ISRC;
+    const int tot = (*inst0)[n][t];
+    if (!tot) continue;
+    int *p = U->iv(tot), *m = U->iv(tot), *kind = U->iv(tot);
+    double *wave = U->dv((size_t)tot * 7);
+    for (int r = 0; r < n; ++r) {
+      const xg_src_desc &d = which == 0 ? nls[r]->vsrc : nls[r]->isrc;
+      for (int i = 0; i < d.n; ++i) {
+        const int k = (*inst0)[r][t] + i;
+        p[k] = node(r, d.p[i]);
+        m[k] = node(r, d.m[i]);
+        kind[k] = d.kind ? d.kind[i] : XG_SRC_DC;
+        for (int j = 0; j < 7; ++j) wave[(size_t)k * 7 + j] = d.wave[(size_t)i * 7 + j];
+        if (kind[k] == XG_SRC_PULSE) {
+          xg::set_error("xg_batch_create: PULSE sources (breakpoints) are not supported in a batch");
+          return XG_ERR_UNSUPPORTED;
+        }
+      }
+    }
+    xg_src_desc &o = which == 0 ? u.vsrc : u.isrc;
+    o.n = tot; o.p = p; o.m = m; o.kind = kind; o.wave = wave;
+  }
+  // diodes
+  if (int tot = (*inst0)[n][XG_DEV_DIODE]) {
+    int *a = U->iv(tot), *cc = U->iv(tot), *mod = U->iv(tot);
+    double *area = U->dv(tot);
+    for (int r = 0; r < n; ++r) {
+      const xg_diode_desc &d = nls[r]->diode;
+      for (int i = 0; i < d.n; ++i) {
+        const int k = (*inst0)[r][XG_DEV_DIODE] + i;
+        a[k] = node(r, d.a[i]);
+        cc[k] = node(r, d.c[i]);
+        mod[k] = d.model[i] + model0[r];
+        area[k] = d.area ? d.area[i] : 1.0;
+      }
+    }
+    u.diode.n = tot; u.diode.a = a; u.diode.c = cc; u.diode.model = mod; u.diode.area = area;
+  }
+  // MOSFETs: optional per-instance arrays stay NULL (the model default) only
+  // when no request gives them
+  for (int which = 0; which < 2; ++which) {
+    const int t = which == 0 ? XG_DEV_MOS1 : XG_DEV_BSIM3;
+    const int tot = (*inst0)[n][t];
+    if (!tot) continue;
+    int *dd = U->iv(tot), *g = U->iv(tot), *s = U->iv(tot), *bb = U->iv(tot), *mod = U->iv(tot);
+    double *geo[9];
+    for (int j = 0; j < 9; ++j) {
+      int given = 0, reqs = 0;
+      for (int r = 0; r < n; ++r) {
+        const xg_mos_desc &d = which == 0 ? nls[r]->mos1 : nls[r]->bsim3;
+        if (!d.n) continue;
+        const double *src[9] = {d.w, d.l, d.ad, d.as, d.pd, d.ps, d.nrd, d.nrs, d.m};
+        ++reqs;
+        given += src[j] != nullptr;
+      }
+      if (given && given != reqs) {
+        xg::set_error("xg_batch_create: requests differ in which MOSFET geometry arrays they give");
+        return XG_ERR_ARG;
+      }
+      geo[j] = given ? U->dv(tot) : nullptr;
+    }
+    for (int r = 0; r < n; ++r) {
+      const xg_mos_desc &d = which == 0 ? nls[r]->mos1 : nls[r]->bsim3;
+      const double *src[9] = {d.w, d.l, d.ad, d.as, d.pd, d.ps, d.nrd, d.nrs, d.m};
+      for (int i = 0; i < d.n; ++i) {
+        const int k = (*inst0)[r][t] + i;
+        dd[k] = node(r, d.d[i]);
+        g[k] = node(r, d.g[i]);
+        s[k] = node(r, d.s[i]);
+        bb[k] = node(r, d.b[i]);
+        mod[k] = d.model[i] + model0[r];
+        for (int j = 0; j < 9; ++j)
+          if (geo[j]) geo[j][k] = src[j][i];
+      }
+    }
+    xg_mos_desc &o = which == 0 ? u.mos1 : u.bsim3;
+    o.n = tot; o.d = dd; o.g = g; o.s = s; o.b = bb; o.model = mod;
+    o.w = geo[0]; o.l = geo[1]; o.ad = geo[2]; o.as = geo[3]; o.pd = geo[4]; o.ps = geo[5];
+    o.nrd = geo[6]; o.nrs = geo[7]; o.m = geo[8];
+  }
+  return XG_OK;
+}
+
+}  // namespace
+
+namespace {
+
+void free_batch(xg_batch *b) {
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  for (void *p : b->allocs) cudaFree(p);
+  for (int t = 0; t < XG_NUM_DEV_TYPES; ++t)
+    if (b->d_cid[t]) cudaFree(b->d_cid[t]);
+  if (b->h_cs) cudaFreeHost(b->h_cs);
+  if (b->ckt) xg_circuit_destroy(b->ckt);
+  if (b->stream) cudaStreamDestroy(b->stream);
+}
+
+template <class V>
+int dev_copy(xg_batch *b, V **d, const std::vector<V> &h) {
+  int rc = xg::to_dev(d, h);
+  if (*d) b->allocs.push_back((void *)*d);
+  b->bytes += int64_t(sizeof(V) * h.size());
+  return rc;
+}
+
+int dev_zero(xg_batch *b, double **d, size_t n) {
+  if (cudaMalloc((void **)d, sizeof(double) * std::max<size_t>(n, 1)) != cudaSuccess) return XG_ERR_OOM;
+  b->allocs.push_back(*d);
+  b->bytes += int64_t(sizeof(double) * n);
+  return cudaMemset(*d, 0, sizeof(double) * std::max<size_t>(n, 1)) == cudaSuccess ? XG_OK : XG_ERR_CUDA;
+}
+
+// One batch iteration: solve, load, combine, control, vector.
+int enqueue_iteration(xg_batch *b) {
+  using namespace xg;
+  CircuitView v;
+  circuit_view(b->ckt, &v);
+  const Plan &P = *v.plan;
+  cudaStream_t s = b->stream;
+  const int blocks4 = (b->nc + 3) / 4;
+  if (b->solve_smem) {
+    if (b->precision == XG_LU_FP32) batch_solve_smem<float><<<b->nc, 32, b->solve_smem, s>>>(b->dev);
+    else batch_solve_smem<double><<<b->nc, 32, b->solve_smem, s>>>(b->dev);
+  } else if (b->precision == XG_LU_FP32) {
+    batch_solve<float><<<blocks4, 128, 0, s>>>(b->dev);
+  } else {
+    batch_solve<double><<<blocks4, 128, 0, s>>>(b->dev);
+  }
+  count_launches(1);
+  Flags unused{};
+  for (int k = 0; k < P.n_order; ++k) {
+    const int t = P.order[k];
+    const TypeData &T = P.T[t];
+    if (!T.n) continue;
+    DevType dt{T.n, T.nterm, T.sta0, T.sto0, T.term0, T.d_params, T.d_lid, b->d_cid[t], b->dev.flags};
+    int rc = v.fma ? fast::launch_eval(t, dt, v.opt, unused, v.io, s)
+                   : exact::launch_eval(t, dt, v.opt, unused, v.io, s);
+    if (rc) return rc;
+  }
+  double *out = nullptr;
+  xg_vec_device_ptr(b->ckt, XG_VEC_F, &out);
+  const ReduceArgs ra = reduce_args(P, v.io.terms, v.red_ptr, v.red_idx, v.long_out, out, 0, P.n_out);
+  int rc = v.fma ? fast::launch_reduce(ra, s) : exact::launch_reduce(ra, s);
+  if (rc) return rc;
+  batch_combine<<<blocks4, 128, 0, s>>>(b->dev);
+  batch_control<<<(b->nc + 127) / 128, 128, 0, s>>>(b->dev);
+  batch_vector<<<blocks4, 128, 0, s>>>(b->dev);
+  count_launches(3);
+  return cudaGetLastError() == cudaSuccess ? XG_OK : XG_ERR_CUDA;
+}
+
+}  // namespace
+
+extern "C" int xg_batch_create(xg_ctx *ctx, int n, const xg_netlist *const *nls,
+                               const double *const *x0, const double *tstop, const int *const *out_idx,
+                               const xg_batch_options *o, xg_batch **out) {
+  using namespace xg;
+  if (!ctx || n <= 0 || !nls || !tstop || !o || !out || o->max_points <= 0 || o->n_out < 0 ||
+      (o->n_out && !out_idx) || (o->lu_precision != XG_LU_FP64 && o->lu_precision != XG_LU_FP32) ||
+      o->n_refine < 0) {
+    set_error("xg_batch_create: bad argument");
+    return XG_ERR_ARG;
+  }
+  *out = nullptr;
+  std::unique_ptr<xg_batch, void (*)(xg_batch *)> b(new xg_batch, [](xg_batch *p) {
+    free_batch(p);
+    delete p;
+  });
+  b->ctx = ctx;
+  b->nc = n;
+  b->n_out = o->n_out;
+  b->max_points = o->max_points;
+  b->precision = o->lu_precision;
+  UnionNetlist U;
+  std::vector<std::array<int, XG_NUM_DEV_TYPES>> inst0;
+  std::vector<int> node0;
+  int rc = build_union(n, nls, &U, &inst0, &node0);
+  if (rc) return rc;
+  if ((rc = xg_circuit_create(ctx, &U.nl, &b->ckt))) return rc;
+  CircuitView v;
+  circuit_view(b->ckt, &v);
+  const Plan &P = *v.plan;
+  const int NU = P.n_unknowns;
+  int device = 0;
+  void *ctx_stream = nullptr;
+  ctx_info(ctx, &device, &ctx_stream);
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    set_error("xg_batch_create: cudaStreamCreate failed");
+    return XG_ERR_CUDA;
+  }
+  // requests of instances, unknowns, state and store slots
+  std::vector<std::vector<int>> l2u(n), sl(n), ol(n);
+  std::vector<int> owner(NU, -1);
+  for (int r = 0; r < n; ++r)
+    for (int k = node0[r]; k < node0[r + 1]; ++k) {
+      l2u[r].push_back(k);
+      owner[k] = r;
+    }
+  for (int k = 0; k < P.n_order; ++k) {
+    const int t = P.order[k];
+    const TypeData &T = P.T[t];
+    if (!T.n) continue;
+    std::vector<int> cid(T.n);
+    for (int r = 0; r < n; ++r) {
+      const int i0 = inst0[r][t], i1 = inst0[r + 1][t];
+      for (int i = i0; i < i1; ++i) {
+        cid[i] = r;
+        for (int j = 0; j < T.nlid; ++j) {
+          const int g = T.lid[(size_t)j * T.n + i];
+          if (g < NU && owner[g] < 0) {
+            owner[g] = r;
+            l2u[r].push_back(g);
+          }
+        }
+      }
+      if (t != XG_DEV_DIODE)
+        for (int s = T.sta0 + i0 * T.nsta; s < T.sta0 + i1 * T.nsta; ++s) sl[r].push_back(s);
+      for (int s = T.sto0 + i0 * T.nsto; s < T.sto0 + i1 * T.nsto; ++s) ol[r].push_back(s);
+    }
+    if (to_dev(&b->d_cid[t], cid)) {
+      set_error("xg_batch_create: out of device memory");
+      return XG_ERR_OOM;
+    }
+  }
+  for (int g = 0; g < NU; ++g)
+    if (owner[g] < 0) {
+      set_error("xg_batch_create: an unknown belongs to no request");
+      return XG_ERR_ARG;
+    }
+  std::vector<int> uptr(n + 1, 0), uidx, sptr(n + 1, 0), sidx, optr(n + 1, 0), oidx;
+  // slot lists -> runs of consecutive slots (start, length)
+  auto runs = [](const std::vector<int> &v, std::vector<int> *out) {
+    int cnt = 0;
+    for (size_t k = 0; k < v.size();) {
+      size_t e = k + 1;
+      while (e < v.size() && v[e] == v[e - 1] + 1) ++e;
+      out->push_back(v[k]);
+      out->push_back(int(e - k));
+      ++cnt;
+      k = e;
+    }
+    return cnt;
+  };
+  for (int r = 0; r < n; ++r) {
+    uptr[r + 1] = uptr[r] + int(l2u[r].size());
+    uidx.insert(uidx.end(), l2u[r].begin(), l2u[r].end());
+    sptr[r + 1] = sptr[r] + runs(sl[r], &sidx);
+    optr[r + 1] = optr[r] + runs(ol[r], &oidx);
+    b->n_unk.push_back(int(l2u[r].size()));
+  }
+  // starting point and a first Jacobian (dF/dx + dQ/dx / tstep) for the
+  // per-request pivot analysis
+  std::vector<double> xu(NU + 1, 0.0);
+  for (int r = 0; r < n; ++r)
+    if (x0 && x0[r])
+      for (int k = 0; k < int(l2u[r].size()); ++k) xu[l2u[r][k]] = x0[r][k];
+  for (int id : {XG_VEC_SOL_NEXT, XG_VEC_SOL_CURR, XG_VEC_SOL_LAST})
+    if ((rc = xg_vec_upload(b->ckt, id, xu.data()))) return rc;
+  const double tstep = o->tstep > 0 ? o->tstep : 1e-12;
+  xg_load_flags fl{};
+  fl.transient = 1;
+  fl.pdt = 1.0 / tstep;
+  if ((rc = xg_load(b->ckt, &fl))) return rc;
+  std::vector<double> dfdx(P.nnz), dqdx(P.nnz);
+  if ((rc = xg_vec_download(b->ckt, XG_VEC_DFDX, dfdx.data())) ||
+      (rc = xg_vec_download(b->ckt, XG_VEC_DQDX, dqdx.data())))
+    return rc;
+  if ((rc = circuit_reset_members(b->ckt))) return rc;
+  std::vector<int> lrp_off(n + 1, 0), lrp, lci, ldiag, lP, lQ;
+  std::vector<int64_t> lnz_off(n + 1, 0), lu2a;
+  std::vector<int> g2l(NU, -1);
+  for (int r = 0; r < n; ++r) {
+    const int nr_ = int(l2u[r].size());
+    for (int k = 0; k < nr_; ++k) g2l[l2u[r][k]] = k;
+    std::vector<int> rp(nr_ + 1, 0), ci;
+    std::vector<int64_t> gpos;
+    std::vector<double> val;
+    for (int k = 0; k < nr_; ++k) {
+      const int g = l2u[r][k];
+      std::vector<std::pair<int, int64_t>> row;
+      for (int p = P.rowptr[g]; p < P.rowptr[g + 1]; ++p) row.push_back({g2l[P.colidx[p]], p});
+      std::sort(row.begin(), row.end());
+      for (auto &e : row) {
+        ci.push_back(e.first);
+        gpos.push_back(e.second);
+        double a = dfdx[e.second] + dqdx[e.second] / tstep;
+        if (e.first == k && a == 0.0) a = 1e-12;
+        val.push_back(a);
+      }
+      rp[k + 1] = int(ci.size());
+    }
+    LuSymbolic S;
+    std::string err;
+    if (lu_analyze(nr_, rp.data(), ci.data(), val.data(), 1e-3, &S, &err)) {
+      set_error("xg_batch_create: request " + std::to_string(r) + ": " + err);
+      return XG_ERR_SINGULAR;
+    }
+    lrp_off[r + 1] = lrp_off[r] + nr_ + 1;
+    lnz_off[r + 1] = lnz_off[r] + S.rp[nr_];
+    lrp.insert(lrp.end(), S.rp.begin(), S.rp.end());
+    lci.insert(lci.end(), S.ci.begin(), S.ci.end());
+    ldiag.insert(ldiag.end(), S.diag.begin(), S.diag.end());
+    for (int a : S.lu2a) lu2a.push_back(a >= 0 ? gpos[a] : -1);
+    lP.insert(lP.end(), S.P.begin(), S.P.end());
+    lQ.insert(lQ.end(), S.Q.begin(), S.Q.end());
+  }
+  std::vector<int> outs((size_t)n * std::max(1, o->n_out), 0);
+  for (int r = 0; r < n; ++r)
+    for (int j = 0; j < o->n_out; ++j) {
+      const int k = out_idx[r][j];
+      if (k < 0 || k >= int(l2u[r].size())) {
+        set_error("xg_batch_create: output index out of range");
+        return XG_ERR_ARG;
+      }
+      outs[(size_t)r * o->n_out + j] = l2u[r][k];
+    }
+  BatchDev &d = b->dev;
+  d.nc = n;
+  d.n_out = o->n_out;
+  d.max_points = o->max_points;
+  d.n_refine = o->lu_precision == XG_LU_FP32 ? o->n_refine : 0;
+  int *t_uptr, *t_uidx, *t_sptr, *t_sidx, *t_optr, *t_oidx, *t_lrp_off, *t_lrp, *t_lci, *t_ldiag,
+      *t_lP, *t_lQ, *t_out, *t_arp, *t_aci;
+  int64_t *t_lnz_off, *t_lu2a;
+  if (dev_copy(b.get(), &t_uptr, uptr) || dev_copy(b.get(), &t_uidx, uidx) ||
+      dev_copy(b.get(), &t_sptr, sptr) || dev_copy(b.get(), &t_sidx, sidx) ||
+      dev_copy(b.get(), &t_optr, optr) || dev_copy(b.get(), &t_oidx, oidx) ||
+      dev_copy(b.get(), &t_lrp_off, lrp_off) || dev_copy(b.get(), &t_lnz_off, lnz_off) ||
+      dev_copy(b.get(), &t_lrp, lrp) || dev_copy(b.get(), &t_lci, lci) ||
+      dev_copy(b.get(), &t_ldiag, ldiag) || dev_copy(b.get(), &t_lu2a, lu2a) ||
+      dev_copy(b.get(), &t_lP, lP) || dev_copy(b.get(), &t_lQ, lQ) ||
+      dev_copy(b.get(), &t_out, outs) || dev_copy(b.get(), &t_arp, P.rowptr) ||
+      dev_copy(b.get(), &t_aci, P.colidx)) {
+    set_error("xg_batch_create: out of device memory");
+    return XG_ERR_OOM;
+  }
+  d.uptr = t_uptr; d.uidx = t_uidx; d.sptr = t_sptr; d.sidx = t_sidx; d.optr = t_optr; d.oidx = t_oidx;
+  d.arp = t_arp; d.aci = t_aci; d.lrp_off = t_lrp_off; d.lnz_off = t_lnz_off; d.lrp = t_lrp;
+  d.lci = t_lci; d.ldiag = t_ldiag; d.lu2a = t_lu2a; d.lP = t_lP; d.lQ = t_lQ; d.out_idx = t_out;
+  const size_t tsz = o->lu_precision == XG_LU_FP32 ? sizeof(float) : sizeof(double);
+  {
+    size_t need = 0;
+    for (int r = 0; r < n; ++r)
+      need = std::max(need, smem_bytes_request(uptr[r + 1] - uptr[r], lnz_off[r + 1] - lnz_off[r], tsz));
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    if (need + 1024 <= size_t(optin) && !std::getenv("XG_BATCH_NO_SMEM")) {
+      cudaError_t e = o->lu_precision == XG_LU_FP32
+                          ? cudaFuncSetAttribute(batch_solve_smem<float>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(need))
+                          : cudaFuncSetAttribute(batch_solve_smem<double>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(need));
+      if (e == cudaSuccess) b->solve_smem = need;
+      else cudaGetLastError();
+    }
+  }
+  {
+    void *pv = nullptr, *pr = nullptr;
+    int *pm = nullptr;
+    if (cudaMalloc(&pv, tsz * std::max<int64_t>(lnz_off[n], 1)) != cudaSuccess ||
+        cudaMalloc(&pr, tsz * std::max(NU, 1)) != cudaSuccess ||
+        cudaMalloc((void **)&pm, sizeof(int) * std::max(NU, 1)) != cudaSuccess) {
+      if (pv) cudaFree(pv);
+      if (pr) cudaFree(pr);
+      set_error("xg_batch_create: out of device memory");
+      return XG_ERR_OOM;
+    }
+    b->allocs.push_back(pv);
+    b->allocs.push_back(pr);
+    b->allocs.push_back(pm);
+    b->bytes += int64_t(tsz * (lnz_off[n] + NU) + sizeof(int) * NU);
+    d.lval = pv;
+    d.lrd = pr;
+    d.map = pm;
+  }
+  double **vecs[] = {&d.y, &d.r, &d.dd, &d.jac, &d.rhs, &d.dx, &d.w, &d.xh0, &d.xh1, &d.xh2,
+                     &d.qh0, &d.qh1, &d.qh2, &d.xn0};
+  for (double **p : vecs) {
+    const size_t len = p == &d.jac ? size_t(std::max<int64_t>(P.nnz, 1)) : size_t(NU + 1);
+    if (dev_zero(b.get(), p, len)) {
+      set_error("xg_batch_create: out of device memory");
+      return XG_ERR_OOM;
+    }
+  }
+  if (dev_zero(b.get(), &d.part, size_t(n) * Q_N) ||
+      dev_zero(b.get(), &d.rec_t, size_t(n) * o->max_points) ||
+      dev_zero(b.get(), &d.rec_v, size_t(n) * o->max_points * std::max(1, o->n_out))) {
+    set_error("xg_batch_create: out of device memory");
+    return XG_ERR_OOM;
+  }
+  xg_vec_device_ptr(b->ckt, XG_VEC_SOL_NEXT, &d.x);
+  xg_vec_device_ptr(b->ckt, XG_VEC_SOL_CURR, &d.xc);
+  xg_vec_device_ptr(b->ckt, XG_VEC_SOL_LAST, &d.xl);
+  xg_vec_device_ptr(b->ckt, XG_VEC_STA_NEXT, &d.sta);
+  xg_vec_device_ptr(b->ckt, XG_VEC_STA_CURR, &d.stac);
+  xg_vec_device_ptr(b->ckt, XG_VEC_STA_LAST, &d.stal);
+  xg_vec_device_ptr(b->ckt, XG_VEC_STO_NEXT, &d.sto);
+  xg_vec_device_ptr(b->ckt, XG_VEC_STO_CURR, &d.stoc);
+  xg_vec_device_ptr(b->ckt, XG_VEC_STO_LAST, &d.stol);
+  double *pf, *pq, *pfv, *pqv, *pdf, *pdq;
+  xg_vec_device_ptr(b->ckt, XG_VEC_F, &pf);
+  xg_vec_device_ptr(b->ckt, XG_VEC_Q, &pq);
+  xg_vec_device_ptr(b->ckt, XG_VEC_DFDXDVP, &pfv);
+  xg_vec_device_ptr(b->ckt, XG_VEC_DQDXDVP, &pqv);
+  xg_vec_device_ptr(b->ckt, XG_VEC_DFDX, &pdf);
+  xg_vec_device_ptr(b->ckt, XG_VEC_DQDX, &pdq);
+  d.f = pf; d.q = pq; d.fvp = pfv; d.qvp = pqv; d.dfdx = pdf; d.dqdx = pdq;
+  // initial states: x0 everywhere, state and store zero, first load in DC mode
+  for (int id : {XG_VEC_SOL_NEXT, XG_VEC_SOL_CURR, XG_VEC_SOL_LAST})
+    if ((rc = xg_vec_upload(b->ckt, id, xu.data()))) return rc;
+  {
+    std::vector<double> z(std::max(P.n_state, P.n_store) + 1, 0.0);
+    for (int id : {XG_VEC_STA_NEXT, XG_VEC_STA_CURR, XG_VEC_STA_LAST})
+      if (P.n_state && (rc = xg_vec_upload(b->ckt, id, z.data()))) return rc;
+    for (int id : {XG_VEC_STO_NEXT, XG_VEC_STO_CURR, XG_VEC_STO_LAST})
+      if (P.n_store && (rc = xg_vec_upload(b->ckt, id, z.data()))) return rc;
+  }
+  std::vector<CState> cs(n);
+  std::vector<Flags> fls(n);
+  for (int r = 0; r < n; ++r) {
+    CState &c = cs[r];
+    std::memset(&c, 0, sizeof(c));
+    c.tstop = tstop[r];
+    c.tstep = tstep;
+    c.max_step = o->maxstep > 0 ? o->maxstep : 0.1 * tstop[r];
+    c.reltol = o->reltol > 0 ? o->reltol : 1e-3;
+    c.abstol = o->abstol > 0 ? o->abstol : 1e-6;
+    c.saved = 1e-10;
+    c.phase = PH_INIT;
+    c.first_step = 1;
+    c.beginning = 1;
+    c.order = 1;
+    c.loads = 1;
+    Flags f{};
+    f.dcop = 1;
+    f.tranop = 1;
+    fls[r] = f;
+  }
+  CState *t_cs;
+  Flags *t_fl;
+  if (dev_copy(b.get(), &t_cs, cs) || dev_copy(b.get(), &t_fl, fls)) {
+    set_error("xg_batch_create: out of device memory");
+    return XG_ERR_OOM;
+  }
+  d.cs = t_cs;
+  d.flags = t_fl;
+  if (cudaMallocHost((void **)&b->h_cs, sizeof(CState) * n) != cudaSuccess) {
+    set_error("xg_batch_create: out of pinned host memory");
+    return XG_ERR_OOM;
+  }
+  std::memcpy(b->h_cs, cs.data(), sizeof(CState) * n);
+  xg_circuit_info info;
+  xg_circuit_get_info(b->ckt, &info);
+  b->bytes += info.scratch_bytes;
+  for (int t = 0; t < XG_NUM_DEV_TYPES; ++t)
+    b->bytes += int64_t(P.T[t].params.size() * sizeof(double) + P.T[t].lid.size() * sizeof(int));
+  b->bytes += int64_t(9 * (NU + 1) + P.n_out) * int64_t(sizeof(double));
+  if (cudaDeviceSynchronize() != cudaSuccess) {
+    set_error("xg_batch_create: set-up failed");
+    return XG_ERR_CUDA;
+  }
+  *out = b.release();
+  return XG_OK;
+}
+
+extern "C" int xg_batch_run(xg_batch *b, int iterations) {
+  if (!b || iterations <= 0) {
+    xg::set_error("xg_batch_run: bad argument");
+    return XG_ERR_ARG;
+  }
+  if (!b->graph || b->graph_iters != iterations) {
+    if (b->graph) {
+      cudaStreamSynchronize(b->stream);
+      cudaGraphExecDestroy(b->graph);
+      b->graph = nullptr;
+    }
+    cudaGraph_t g;
+    if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      xg::set_error("xg_batch_run: stream capture failed");
+      return XG_ERR_CUDA;
+    }
+    const long long before = xg_launch_count();
+    int rc = XG_OK;
+    for (int k = 0; k < iterations && !rc; ++k) rc = enqueue_iteration(b);
+    // the captured launches run when the graph is launched, not here
+    const long long captured = xg_launch_count() - before;
+    b->graph_launches_per_iter = int(captured / iterations);
+    xg::count_launches(-int(captured));
+    cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+    if (rc || e != cudaSuccess) {
+      xg::set_error("xg_batch_run: capture of the batch iteration failed");
+      return XG_ERR_CUDA;
+    }
+    e = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      xg::set_error(std::string("xg_batch_run: cudaGraphInstantiate: ") + cudaGetErrorString(e));
+      return XG_ERR_CUDA;
+    }
+    b->graph_iters = iterations;
+  }
+  if (cudaGraphLaunch(b->graph, b->stream) != cudaSuccess) {
+    xg::set_error("xg_batch_run: cudaGraphLaunch failed");
+    return XG_ERR_CUDA;
+  }
+  xg::count_launches(iterations * b->graph_launches_per_iter);
+  return XG_OK;
+}
+
+extern "C" int xg_batch_poll(xg_batch *b, int wait, int *n_done) {
+  if (!b || !n_done) {
+    xg::set_error("xg_batch_poll: bad argument");
+    return XG_ERR_ARG;
+  }
+  if (!wait && cudaStreamQuery(b->stream) == cudaErrorNotReady) {
+    *n_done = -1;  // still running
+    return XG_OK;
+  }
+  if (cudaMemcpyAsync(b->h_cs, b->dev.cs, sizeof(xg::CState) * b->nc, cudaMemcpyDeviceToHost,
+                      b->stream) != cudaSuccess ||
+      cudaStreamSynchronize(b->stream) != cudaSuccess) {
+    xg::set_error("xg_batch_poll: copy failed");
+    return XG_ERR_CUDA;
+  }
+  int d = 0;
+  for (int i = 0; i < b->nc; ++i) d += b->h_cs[i].phase == xg::PH_DONE;
+  *n_done = d;
+  return XG_OK;
+}
+
+extern "C" int xg_batch_results(xg_batch *b, int i, double *t, double *v, int *n_points,
+                                xg_tran_stats *st) {
+  if (!b || i < 0 || i >= b->nc || !n_points) {
+    xg::set_error("xg_batch_results: bad argument");
+    return XG_ERR_ARG;
+  }
+  const xg::CState &c = b->h_cs[i];
+  const int np = std::min(c.n_rec, b->max_points);
+  *n_points = np;
+  if (np && t &&
+      cudaMemcpy(t, b->dev.rec_t + (size_t)i * b->max_points, sizeof(double) * np,
+                 cudaMemcpyDeviceToHost) != cudaSuccess)
+    return XG_ERR_CUDA;
+  if (np && v && b->n_out &&
+      cudaMemcpy(v, b->dev.rec_v + (size_t)i * b->max_points * b->n_out,
+                 sizeof(double) * np * b->n_out, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return XG_ERR_CUDA;
+  if (st) {
+    std::memset(st, 0, sizeof(*st));
+    st->status = c.failed ? c.status : 0;
+    st->steps = c.steps;
+    st->steps_attempted = c.steps_attempted;
+    st->rejected = c.rejected;
+    st->newton_iters = c.newton_iters;
+    st->factorizations = c.newton_iters;
+    st->loads = c.loads;
+    st->t_end = c.t;
+  }
+  return XG_OK;
+}
+
+extern "C" int xg_batch_info(const xg_batch *b, int *n_requests, int64_t *device_bytes) {
+  if (!b) {
+    xg::set_error("xg_batch_info: bad argument");
+    return XG_ERR_ARG;
+  }
+  if (n_requests) *n_requests = b->nc;
+  if (device_bytes) *device_bytes = b->bytes;
+  return XG_OK;
+}
+
+extern "C" int xg_batch_destroy(xg_batch *b) {
+  if (!b) return XG_OK;
+  free_batch(b);
+  delete b;
+  return XG_OK;
+}

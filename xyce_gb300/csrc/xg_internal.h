@@ -47,6 +47,8 @@ struct TypeData {
   int *d_lid = nullptr;
 };
 
+struct Flags;
+
 // Device-side view of one device type, passed to kernels by value.
 struct DevType {
   int n;
@@ -55,6 +57,10 @@ struct DevType {
   int64_t term0;
   const double *p;   // SoA params
   const int *lid;    // SoA LIDs
+  // Batched loads of independent circuits: the circuit of each instance and
+  // the per-circuit load flags (null: every instance uses the launch's flags)
+  const int *cid = nullptr;
+  const Flags *cflags = nullptr;
 };
 
 struct DevOptions {

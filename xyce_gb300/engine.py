@@ -72,6 +72,13 @@ def lib():
     L.xg_lu_analyze_host.argtypes = [i, vp, vp, vp, vp, vp, i64p]
     L.xg_tran_run.argtypes = [vp, C.POINTER(abi.XgTranOptions), vp, i, vp, i, vp, vp,
                               C.POINTER(i), C.POINTER(abi.XgTranStats)]
+    L.xg_batch_create.argtypes = [vp, i, vp, vp, vp, vp, C.POINTER(abi.XgBatchOptions),
+                                  C.POINTER(vp)]
+    L.xg_batch_run.argtypes = [vp, i]
+    L.xg_batch_poll.argtypes = [vp, i, C.POINTER(i)]
+    L.xg_batch_results.argtypes = [vp, i, vp, vp, C.POINTER(i), C.POINTER(abi.XgTranStats)]
+    L.xg_batch_info.argtypes = [vp, C.POINTER(i), i64p]
+    L.xg_batch_destroy.argtypes = [vp]
     _lib = L
     return L
 
@@ -320,3 +327,85 @@ def transient(circuit, tstop, tstep, out_idx, x0=None, uic=False, precision=abi.
                             _ptr(idx), max_points, _ptr(t), _ptr(v), C.byref(npts), C.byref(st)))
     n = npts.value
     return t[:n], v[:n, : idx.size], st.as_dict()
+
+
+class Batch:
+    """Independent transients stepped together on the GPU (xg_batch_*): each
+    request is a netlist, its initial condition x0 (its own unknown
+    numbering), tstop and the unknowns to record."""
+
+    def __init__(self, ctx, netlists, x0s, tstops, out_idx, tstep=1e-12, precision=abi.LU_FP64,
+                 n_refine=0, max_points=4096, maxstep=0.0, reltol=1e-3, abstol=1e-6):
+        self.ctx = ctx
+        n = len(netlists)
+        self._nl = [nl.to_c() for nl in netlists]
+        self._keep = list(netlists)
+        nl_arr = (C.c_void_p * n)(*[C.addressof(x) for x in self._nl])
+        self._x0 = [np.ascontiguousarray(x, np.float64) for x in x0s]
+        x0_arr = (C.c_void_p * n)(*[x.ctypes.data for x in self._x0])
+        self._ts = np.ascontiguousarray(tstops, np.float64)
+        self.n_out = len(out_idx[0])
+        self._out = [np.ascontiguousarray(o, np.int32) for o in out_idx]
+        out_arr = (C.c_void_p * n)(*[o.ctypes.data for o in self._out])
+        self.max_points = max_points
+        o = abi.XgBatchOptions(tstep, maxstep, reltol, abstol, precision, n_refine, self.n_out,
+                               max_points)
+        h = C.c_void_p()
+        check(lib().xg_batch_create(ctx.h, n, nl_arr, x0_arr, _ptr(self._ts), out_arr, C.byref(o),
+                                    C.byref(h)))
+        self.h = h
+        self.n = n
+
+    def run(self, iterations):
+        check(lib().xg_batch_run(self.h, iterations))
+
+    def poll(self, wait=True):
+        d = C.c_int()
+        check(lib().xg_batch_poll(self.h, int(bool(wait)), C.byref(d)))
+        return d.value
+
+    def results(self, i):
+        np_ = C.c_int()
+        t = np.zeros(self.max_points)
+        v = np.zeros((self.max_points, max(1, self.n_out)))
+        st = abi.XgTranStats()
+        check(lib().xg_batch_results(self.h, i, _ptr(t), _ptr(v), C.byref(np_), C.byref(st)))
+        k = np_.value
+        return t[:k], v[:k, : self.n_out], st.as_dict()
+
+    def stats(self, i):
+        """Request i's counters from the last poll; 'finished' once it is done."""
+        np_ = C.c_int()
+        st = abi.XgTranStats()
+        check(lib().xg_batch_results(self.h, i, None, None, C.byref(np_), C.byref(st)))
+        d = st.as_dict()
+        d["points"] = np_.value
+        d["finished"] = bool(st.status != 0 or st.t_end >= self._ts[i] * (1 - 1e-12))
+        return d
+
+    def device_bytes(self):
+        nb, b = C.c_int(), C.c_int64()
+        check(lib().xg_batch_info(self.h, C.byref(nb), C.byref(b)))
+        return b.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().xg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def run_batch(batch, chunk=64, max_iters=10**7):
+    """Step a batch until every request has finished; returns iterations run."""
+    it = 0
+    while it < max_iters:
+        batch.run(chunk)
+        it += chunk
+        if batch.poll(wait=True) == batch.n:
+            break
+    return it

@@ -1,0 +1,136 @@
+"""Continuous batching of transient requests on one GPU (the serving path).
+
+Requests (.STEP / Monte-Carlo variants of a circuit, of uneven sizes) arrive
+over time.  The server admits whatever has arrived into a new batch
+(xg_batch_*) as soon as the concurrency limit and the device-memory budget
+allow, so requests that arrive while others run start at once and their work
+overlaps with the running batches on the device (each batch has its own
+stream and replays its own CUDA graph).  Each batch is stepped in chunks of
+batch iterations; between chunks the server harvests finished requests, so a
+short request leaves as soon as it is done, not when its batch is.
+
+Latency = completion - arrival, reported as p50 / p99 beside throughput.
+"""
+import collections
+import time
+
+import numpy as np
+
+from . import abi, engine, netlists
+
+
+class Request:
+    __slots__ = ("netlist", "x0", "tstop", "out_idx", "arrival", "start", "done", "result")
+
+    def __init__(self, netlist, x0, tstop, out_idx):
+        self.netlist, self.x0, self.tstop, self.out_idx = netlist, x0, tstop, out_idx
+        self.arrival = self.start = self.done = None
+        self.result = None
+
+
+def ring_mc_requests(n, seed=0, stages=(5, 501), tstop=5e-9):
+    """n seeded Monte-Carlo ring oscillators: odd stage counts uniform in
+    [stages[0], stages[1]], VTO and KP of every stage scaled by (1 + d),
+    d ~ N(0, 0.1/3) truncated at +-10%; started from an alternating initial
+    condition; recorded at the first node and mid-ring."""
+    rng = np.random.default_rng(seed)
+    lo, hi = (stages[0] - 1) // 2, (stages[1] - 1) // 2
+    out = []
+    for k in range(n):
+        st = 2 * int(rng.integers(lo, hi + 1)) + 1
+        nl = netlists.ring_oscillator(st, seed=int(rng.integers(1 << 30)))
+        x0 = np.zeros(nl.n_nodes + nl.count(abi.DEV_VSRC))
+        x0[:nl.n_nodes] = netlists.ring_oscillator_nodeset(st)
+        out.append(Request(nl, x0, tstop, [1, st // 2 + 1]))
+    return out
+
+
+def poisson_arrivals(n, rate, seed=0):
+    rng = np.random.default_rng(seed)
+    return np.cumsum(rng.exponential(1.0 / rate, n))
+
+
+class Server:
+    def __init__(self, ctx, precision=abi.LU_FP64, n_refine=0, max_batch=512, max_concurrent=8,
+                 memory_budget=64 << 30, chunk=64, tstep=1e-12, max_points=8192):
+        self.ctx = ctx
+        self.precision, self.n_refine = precision, n_refine
+        self.max_batch, self.max_concurrent = max_batch, max_concurrent
+        self.memory_budget, self.chunk, self.tstep = memory_budget, chunk, tstep
+        self.max_points = max_points
+        self.bytes_per_unknown = None
+
+    def _footprint(self, reqs):
+        unk = sum(len(r.x0) for r in reqs)
+        return 0 if self.bytes_per_unknown is None else unk * self.bytes_per_unknown
+
+    def _start(self, reqs, now):
+        b = engine.Batch(self.ctx, [r.netlist for r in reqs], [r.x0 for r in reqs],
+                         [r.tstop for r in reqs], [r.out_idx for r in reqs], tstep=self.tstep,
+                         precision=self.precision, n_refine=self.n_refine,
+                         max_points=self.max_points)
+        nb = b.device_bytes()
+        unk = sum(len(r.x0) for r in reqs)
+        self.bytes_per_unknown = nb / max(1, unk)
+        for r in reqs:
+            r.start = now
+        b.run(self.chunk)
+        return [b, reqs, [False] * len(reqs), nb]
+
+    def run(self, requests, arrivals):
+        """Serve requests arriving at the given times (s); returns a summary."""
+        n = len(requests)
+        for r, a in zip(requests, arrivals):
+            r.arrival = float(a)
+        queue = collections.deque()
+        active = []
+        nxt = done = 0
+        in_use = 0
+        t0 = time.perf_counter()
+        while done < n:
+            now = time.perf_counter() - t0
+            while nxt < n and requests[nxt].arrival <= now:
+                queue.append(requests[nxt])
+                nxt += 1
+            busy = False
+            if queue and len(active) < self.max_concurrent:
+                take = [queue[k] for k in range(min(len(queue), self.max_batch))]
+                if in_use + self._footprint(take) <= self.memory_budget:
+                    for _ in take:
+                        queue.popleft()
+                    entry = self._start(take, now)
+                    in_use += entry[3]
+                    active.append(entry)
+                    busy = True
+            for entry in list(active):
+                b, reqs, fin, nb = entry
+                nd = b.poll(wait=False)
+                if nd < 0:
+                    continue
+                busy = True
+                t_now = time.perf_counter() - t0
+                for j, r in enumerate(reqs):
+                    if not fin[j]:
+                        st = b.stats(j)
+                        if st["finished"]:
+                            fin[j] = True
+                            r.done = t_now
+                            r.result = b.results(j)
+                            done += 1
+                if all(fin):
+                    b.close()
+                    in_use -= nb
+                    active.remove(entry)
+                else:
+                    b.run(self.chunk)
+            if not busy:
+                time.sleep(0.0002)
+        wall = time.perf_counter() - t0
+        lat = np.array([r.done - r.arrival for r in requests])
+        iters = sum(r.result[2]["newton_iters"] for r in requests)
+        failed = sum(1 for r in requests if r.result[2]["status"] != 0)
+        return {"requests": n, "wall_s": wall, "solves_per_s": n / wall,
+                "newton_iters_per_s": iters / wall,
+                "p50_ms": float(np.percentile(lat, 50) * 1e3),
+                "p99_ms": float(np.percentile(lat, 99) * 1e3),
+                "mean_ms": float(lat.mean() * 1e3), "failed": failed}
