@@ -73,6 +73,11 @@ WORKLOADS = {
     # unknowns; one step = .TRAN 1ps 3ps (the first breakpoint-dense window)
     "tran_power_grid_200x200": dict(kind="tran", circuit="grid", nx=200, sinks=40000, tstop=3e-12,
                                     tstep=1e-12),
+    # served batch: a Poisson stream (2,000 req/s) of 1,000 seeded Monte-Carlo
+    # ring oscillators, 5-501 stages (VTO, KP +-10%), .TRAN 1ps 5ns each from an
+    # initial condition; one step = serving the whole stream, FP32 factors with
+    # one FP64 refinement step (the FP64 form is measured beside it)
+    "serve_ring_mc": dict(kind="serve", n=1000, rate=2000.0, tstop=5e-9),
     # 101-stage ring oscillator (level-1, VTO/KP +-10% Monte-Carlo), from an
     # initial condition, .TRAN 1ps 5ns
     "tran_ring_oscillator_101": dict(kind="tran", circuit="ring", stages=101, tstop=5e-9,
@@ -227,6 +232,150 @@ def run_tran(args, world, rank, local, dist):
                          "sample": f".TRAN window {cpu_window:.3g} s: {cpu_n} Newton iterations on one core"},
         "wall_s": wall,
     }
+    print(json.dumps(line))
+    return 0
+
+
+SERVE_METRIC = "served solves/sec"
+
+
+def run_serve(args, world, rank, local, dist):
+    import torch
+
+    from xyce_gb300 import engine, serve
+    torch.cuda.set_device(local)
+    w = WORKLOADS[args.workload]
+    ctx = engine.Context(local, abi.device_options())
+    L = engine.lib()
+
+    def one(prec, nref):
+        reqs = serve.ring_mc_requests(w["n"], seed=1, tstop=w["tstop"])
+        arr = serve.poisson_arrivals(w["n"], w["rate"], seed=2)
+        srv = serve.Server(ctx, precision=prec, n_refine=nref, max_batch=1024, max_concurrent=8,
+                           chunk=64)
+        res = srv.run(reqs, arr)
+        return res, reqs
+
+    for _ in range(args.warmup):
+        one(abi.LU_FP32, 1)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    runs, fp64 = [], []
+    l0 = L.xg_launch_count()
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            res, reqs = one(abi.LU_FP32, 1)
+            runs.append((res, reqs))
+        wall = time.perf_counter() - t0
+    launches = L.xg_launch_count() - l0
+    for _ in range(max(1, args.steps // 2)):
+        fp64.append(one(abi.LU_FP64, 0))
+    if rank != 0:
+        return 0
+    # accuracy of the mixed-precision form against the FP64 form, request by request
+    err = 0.0
+    for (ta, va, _), (tb, vb, _) in zip((r.result for r in fp64[0][1]), (r.result for r in runs[0][1])):
+        vi = np.stack([np.interp(ta, tb, vb[:, k]) for k in range(vb.shape[1])], 1)
+        err = max(err, float(np.abs(vi - va).max()))
+    sps = [r[0]["solves_per_s"] for r in runs]
+    value = world * float(np.mean(sps))
+    step_s = float(np.mean([r[0]["wall_s"] for r in runs]))
+    f64 = fp64[0][0]
+    cpu_v, cpu_n = serve_cpu_baseline(args.cpu_seconds)
+    line = {
+        "metric": SERVE_METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded Monte-Carlo ring oscillators, Poisson arrivals)",
+        "config": {"workload": args.workload, "requests": w["n"], "rate_per_s": w["rate"],
+                   "stages": "5-501 odd", "tstop": w["tstop"], "lu": "fp32 + 1 fp64 refinement",
+                   "l2": "per-request working sets below L2"},
+        "p50_ms": float(np.mean([r[0]["p50_ms"] for r in runs])),
+        "p99_ms": float(np.mean([r[0]["p99_ms"] for r in runs])),
+        "fp64": {"solves_per_s": f64["solves_per_s"], "p50_ms": f64["p50_ms"], "p99_ms": f64["p99_ms"]},
+        "fp32_vs_fp64_max_waveform_diff_v": err,
+        "newton_iters_per_s": float(np.mean([r[0]["newton_iters_per_s"] for r in runs])),
+        "roofline": {"kernel": "batch iteration", "bound": "hbm", "achieved": None, "peak": measured_peaks()[0],
+                     "unit": "GB/s", "frac": None, "traffic": None,
+                     "note": "latency-bound: one warp walks each request's factor"},
+        "e2e": {"value": value, "unit": "solves/s",
+                "h2d_bytes_per_step": int(sum(8 * len(r.x0) for r in runs[0][1])),
+                "d2h_bytes_per_step": int(sum(r.result[1].nbytes + r.result[0].nbytes for r in runs[0][1]))},
+        "gpu_launches": int(launches),
+        "clocks": clocks.summary(),
+        "cpu_baseline": {"value": cpu_v, "unit": "solves/s", "cores": 1, "kind": "port",
+                         "sample": f"{cpu_n} requests of the same stream, one core"},
+        "wall_s": wall,
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def _serve_ref_worker(job):
+    """Reference arm for serving: requests solved one after another on one core."""
+    idx, n, tstop = job
+    from oracle.oracle import OracleCircuit, transient
+    from xyce_gb300 import engine, serve
+    reqs = serve.ring_mc_requests(n, seed=1, tstop=tstop)
+    opt = abi.device_options()
+    t0 = time.perf_counter()
+    done = 0
+    for k in idx:
+        r = reqs[k]
+        params = {t: engine.setup_params(r.netlist, t, opt) for t in range(abi.NUM_DEV_TYPES)
+                  if r.netlist.count(t)}
+        oc = OracleCircuit(r.netlist, params, opt)
+        order, _ = engine.amd_order(oc.rowptr, oc.col)
+        transient(oc, r.tstop, 1e-12, r.out_idx, col_order=order, x0=r.x0, uic=True)
+        oc.close()
+        done += 1
+    return done, time.perf_counter() - t0
+
+
+def serve_cpu_baseline(seconds=10.0):
+    """One core solving the stream's requests back to back for about `seconds`."""
+    w = WORKLOADS["serve_ring_mc"]
+    done, t = 0, 0.0
+    k = 0
+    while t < seconds and k < w["n"]:
+        d, dt = _serve_ref_worker(([k], w["n"], w["tstop"]))
+        done += d
+        t += dt
+        k += 1
+    return done / t, done
+
+
+def run_serve_reference(args, world, rank):
+    """CPU arm for serving: the request stream spread over every host core,
+    each request solved by the oracle's transient driver."""
+    if rank != 0:
+        return 0
+    import multiprocessing as mp
+    w = WORKLOADS[args.workload]
+    cores = os.cpu_count() or 1
+    sample = min(w["n"], 8 * cores)
+    jobs = [(list(range(c, sample, cores)), w["n"], w["tstop"]) for c in range(cores)]
+    ctx = mp.get_context("spawn")
+    times = []
+    with ctx.Pool(cores) as pool:
+        for k in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            pool.map(_serve_ref_worker, jobs)
+            if k >= args.warmup:
+                times.append(time.perf_counter() - t0)
+    t = float(np.mean(times))
+    value = sample / t
+    line = {"metric": SERVE_METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)", "impl": "reference",
+            "config": {"workload": args.workload, "sample_requests": sample},
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
+                             "sample": f"{sample} of {w['n']} requests per step over {cores} processes"},
+            "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
 
@@ -653,11 +802,13 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args()
     world, rank, local, dist = dist_setup(args)
-    tran = WORKLOADS[args.workload]["kind"] == "tran"
+    kind = WORKLOADS[args.workload]["kind"]
     if args.impl == "reference":
-        rc = (run_tran_reference if tran else run_reference)(args, world, rank)
+        ref = {"tran": run_tran_reference, "serve": run_serve_reference}.get(kind, run_reference)
+        rc = ref(args, world, rank)
     else:
-        rc = (run_tran if tran else run_xg)(args, world, rank, local, dist)
+        arm = {"tran": run_tran, "serve": run_serve}.get(kind, run_xg)
+        rc = arm(args, world, rank, local, dist)
     if dist:
         dist.destroy_process_group()
     return rc

@@ -84,6 +84,20 @@ struct BatchDev {
   int n_refine;
 };
 
+// 1/u by Newton-Raphson on the reciprocal from a single-precision seed (two
+// steps, each doubling the correct bits); IEEE division outside the range
+// where the seed is representable.
+template <class T>
+__device__ __forceinline__ T recip_nr(T u) {
+  const double a = fabs(double(u));
+  if (!(a > 1e-30 && a < 1e30)) return T(1) / u;
+  if (sizeof(T) == sizeof(float)) return T(1.0f / float(u));
+  double x = double(1.0f / float(u));
+  x = x * (2.0 - double(u) * x);
+  x = x * (2.0 - double(u) * x);
+  return T(x);
+}
+
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -133,7 +147,7 @@ __global__ void __launch_bounds__(128) batch_solve(BatchDev b) {
       }
       const T u = val[dp];
       if (!(fabs(double(u)) > 0.0) || !isfinite(double(u))) bad = 1;
-      rd[row] = T(1) / u;
+      rd[row] = recip_nr(u);
     }
   }
   __syncwarp();
@@ -240,7 +254,7 @@ __global__ void __launch_bounds__(32) batch_solve_smem(BatchDev b) {
       }
       const T u = val[dp];
       if (!(fabs(double(u)) > 0.0) || !isfinite(double(u))) bad = 1;
-      rd[row] = T(1) / u;
+      rd[row] = recip_nr(u);
     }
   }
   __syncwarp();
@@ -1173,7 +1187,8 @@ extern "C" int xg_batch_create(xg_ctx *ctx, int n, const xg_netlist *const *nls,
   for (int t = 0; t < XG_NUM_DEV_TYPES; ++t)
     b->bytes += int64_t(P.T[t].params.size() * sizeof(double) + P.T[t].lid.size() * sizeof(int));
   b->bytes += int64_t(9 * (NU + 1) + P.n_out) * int64_t(sizeof(double));
-  if (cudaDeviceSynchronize() != cudaSuccess) {
+  // the set-up loads ran on the context's stream; running batches keep going
+  if (cudaStreamSynchronize((cudaStream_t)ctx_stream) != cudaSuccess) {
     set_error("xg_batch_create: set-up failed");
     return XG_ERR_CUDA;
   }

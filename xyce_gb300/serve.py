@@ -51,6 +51,13 @@ def poisson_arrivals(n, rate, seed=0):
 
 
 class Server:
+    """Continuous batching.  Queued requests are grouped by size class
+    (unknowns within a factor of 2), so one batch's per-iteration time, set by
+    its largest request, is not imposed on much smaller ones; the oldest
+    waiting request picks the class admitted next.  Batches are set up on a
+    helper thread (the set-up call releases the interpreter lock) while the
+    running ones keep stepping."""
+
     def __init__(self, ctx, precision=abi.LU_FP64, n_refine=0, max_batch=512, max_concurrent=8,
                  memory_budget=64 << 30, chunk=64, tstep=1e-12, max_points=8192):
         self.ctx = ctx
@@ -60,32 +67,47 @@ class Server:
         self.max_points = max_points
         self.bytes_per_unknown = None
 
+    @staticmethod
+    def size_class(r):
+        return int(np.log2(max(2, len(r.x0))))
+
     def _footprint(self, reqs):
         unk = sum(len(r.x0) for r in reqs)
         return 0 if self.bytes_per_unknown is None else unk * self.bytes_per_unknown
 
-    def _start(self, reqs, now):
+    def _create(self, reqs):
         b = engine.Batch(self.ctx, [r.netlist for r in reqs], [r.x0 for r in reqs],
                          [r.tstop for r in reqs], [r.out_idx for r in reqs], tstep=self.tstep,
                          precision=self.precision, n_refine=self.n_refine,
                          max_points=self.max_points)
-        nb = b.device_bytes()
-        unk = sum(len(r.x0) for r in reqs)
-        self.bytes_per_unknown = nb / max(1, unk)
-        for r in reqs:
-            r.start = now
         b.run(self.chunk)
-        return [b, reqs, [False] * len(reqs), nb]
+        return b
+
+    def _take(self, queue):
+        """Up to max_batch queued requests of the oldest request's size class."""
+        cls = self.size_class(queue[0])
+        take, keep = [], collections.deque()
+        while queue:
+            r = queue.popleft()
+            if len(take) < self.max_batch and self.size_class(r) == cls:
+                take.append(r)
+            else:
+                keep.append(r)
+        queue.extend(keep)
+        return take
 
     def run(self, requests, arrivals):
         """Serve requests arriving at the given times (s); returns a summary."""
         n = len(requests)
         for r, a in zip(requests, arrivals):
             r.arrival = float(a)
+        import concurrent.futures as cf
         queue = collections.deque()
         active = []
+        pending = None                 # (future, requests, footprint) being set up
         nxt = done = 0
         in_use = 0
+        pool = cf.ThreadPoolExecutor(1)
         t0 = time.perf_counter()
         while done < n:
             now = time.perf_counter() - t0
@@ -93,15 +115,25 @@ class Server:
                 queue.append(requests[nxt])
                 nxt += 1
             busy = False
-            if queue and len(active) < self.max_concurrent:
-                take = [queue[k] for k in range(min(len(queue), self.max_batch))]
-                if in_use + self._footprint(take) <= self.memory_budget:
-                    for _ in take:
-                        queue.popleft()
-                    entry = self._start(take, now)
-                    in_use += entry[3]
-                    active.append(entry)
+            if pending is not None and pending[0].done():
+                b = pending[0].result()
+                nb = b.device_bytes()
+                self.bytes_per_unknown = nb / max(1, sum(len(r.x0) for r in pending[1]))
+                in_use += nb - pending[2]
+                active.append([b, pending[1], [False] * len(pending[1]), nb])
+                pending = None
+                busy = True
+            if pending is None and queue and len(active) < self.max_concurrent:
+                take = self._take(queue)
+                fp = self._footprint(take)
+                if in_use + fp <= self.memory_budget:
+                    for r in take:
+                        r.start = now
+                    pending = (pool.submit(self._create, take), take, fp)
+                    in_use += fp
                     busy = True
+                else:
+                    queue.extendleft(reversed(take))
             for entry in list(active):
                 b, reqs, fin, nb = entry
                 nd = b.poll(wait=False)
@@ -125,6 +157,7 @@ class Server:
                     b.run(self.chunk)
             if not busy:
                 time.sleep(0.0002)
+        pool.shutdown()
         wall = time.perf_counter() - t0
         lat = np.array([r.done - r.arrival for r in requests])
         iters = sum(r.result[2]["newton_iters"] for r in requests)
