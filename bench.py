@@ -73,6 +73,11 @@ WORKLOADS = {
     # unknowns; one step = .TRAN 1ps 3ps (the first breakpoint-dense window)
     "tran_power_grid_200x200": dict(kind="tran", circuit="grid", nx=200, sinks=40000, tstop=3e-12,
                                     tstep=1e-12),
+    # 500,000 BSIM3 MOSFETs in seeded random 2-input NAND/NOR/INV logic
+    # (fan-out 1-4, 5 fF wires, 200 PULSE inputs), ~250k nodes; one step =
+    # .TRAN 2ps 10ps from the logic state (a bounded window of the 10 ns run)
+    "tran_random_logic_500k": dict(kind="tran", circuit="logic", n_mos=500_000, tstop=10e-12,
+                                   tstep=2e-12),
     # served batch: a Poisson stream (2,000 req/s) of 1,000 seeded Monte-Carlo
     # ring oscillators, 5-501 stages (VTO, KP +-10%), .TRAN 1ps 5ns each from an
     # initial condition; one step = serving the whole stream, FP32 factors with
@@ -99,6 +104,14 @@ def build_tran(name):
         nl = netlists.power_grid(nx, nx, ns, seed=0)
         return (nl, netlists.power_grid_nodeset(nx, nx, ns), w["tstop"], w["tstep"], False,
                 [0, nx * nx // 2, nx * nx - 1])
+    if w["circuit"] == "logic":
+        nl = netlists.random_logic(w["n_mos"], seed=0)
+        o = nl.logic["out"]
+        # started from the logic state as an initial condition: the damped
+        # Newton DC solve of this many BSIM3 junctions converges linearly
+        # (one thermal voltage per iteration under pnjlim) within 200 steps
+        return (nl, netlists.random_logic_nodeset(nl), w["tstop"], w["tstep"], True,
+                [1, int(o[len(o) // 2]), int(o[-1])])
     k = w["stages"]
     nl = netlists.ring_oscillator(k, seed=3)
     return nl, netlists.ring_oscillator_nodeset(k), w["tstop"], w["tstep"], True, [1, k // 2, k]

@@ -85,3 +85,13 @@ def test_transient_is_deterministic(gpu_ctx):
         runs.append(engine.transient(c, 2e-9, 1e-12, [2, 20, 41], x0=np.r_[x0, 0.0, 0.0]))
         c.close()
     assert np.array_equal(runs[0][0], runs[1][0]) and np.array_equal(runs[0][1], runs[1][1])
+
+
+def test_random_logic_bsim3_waveforms(gpu_ctx, oracle_lib):
+    """2,000 BSIM3 MOSFETs of seeded random NAND/NOR/INV logic, from its
+    logic state, 20 ps: the BSIM3 load inside the time loop."""
+    nl = netlists.random_logic(2000, seed=0)
+    o = nl.logic["out"]
+    cpu, gpu = _both(gpu_ctx, nl, netlists.random_logic_nodeset(nl), 20e-12,
+                     [1, int(o[len(o) // 2]), int(o[-1])], uic=True)
+    _agree(cpu, gpu)
