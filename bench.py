@@ -83,6 +83,10 @@ WORKLOADS = {
     # initial condition; one step = serving the whole stream, FP32 factors with
     # one FP64 refinement step (the FP64 form is measured beside it)
     "serve_ring_mc": dict(kind="serve", n=1000, rate=2000.0, tstop=5e-9),
+    # a 60x60 mesh with 1,200 sinks (6,002 unknowns), .TRAN 1ps 20ps: the
+    # grid-wide LU path at a size a profiler captures quickly
+    "tran_power_grid_60x60": dict(kind="tran", circuit="grid", nx=60, sinks=1200, tstop=20e-12,
+                                  tstep=1e-12),
     # 101-stage ring oscillator (level-1, VTO/KP +-10% Monte-Carlo), from an
     # initial condition, .TRAN 1ps 5ns
     "tran_ring_oscillator_101": dict(kind="tran", circuit="ring", stages=101, tstop=5e-9,
@@ -101,7 +105,7 @@ def build_tran(name):
         return nl, netlists.inverter_chain_nodeset(k), w["tstop"], w["tstep"], False, [1, 2, k + 1]
     if w["circuit"] == "grid":
         nx, ns = w["nx"], w["sinks"]
-        nl = netlists.power_grid(nx, nx, ns, seed=0)
+        nl = netlists.power_grid(nx, nx, ns, seed=0 if nx == 200 else 1)
         return (nl, netlists.power_grid_nodeset(nx, nx, ns), w["tstop"], w["tstep"], False,
                 [0, nx * nx // 2, nx * nx - 1])
     if w["circuit"] == "logic":

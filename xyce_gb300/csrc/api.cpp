@@ -70,8 +70,10 @@ struct xg_circuit {
   double *d_out = nullptr;       // [F | Q | dFdxdVp | dQdxdVp | dFdx | dQdx]
   double *d_terms = nullptr;     // per-load stamp terms
   int64_t *d_red_ptr = nullptr;
-  uint32_t *d_red_idx = nullptr;
+  uint32_t *d_term_pos = nullptr;  // scatter layout: term -> position in reduction order
+  uint32_t *d_red_idx = nullptr;   // gather layout: reduction entry -> term
   int64_t *d_long_out = nullptr; // outputs reduced by a warp each
+  int64_t *d_short_order = nullptr; // the others, by term count
   double *d_diode_vd = nullptr;  // Diode Instance::Vd carried between loads
   double *d_b3_mem = nullptr;    // BSIM3 members carried between loads
   bool state_done = false;
@@ -100,6 +102,8 @@ void free_circuit(xg_circuit *c) {
   cudaFree(c->d_terms);
   cudaFree(c->d_red_ptr);
   cudaFree(c->d_long_out);
+  cudaFree(c->d_short_order);
+  cudaFree(c->d_term_pos);
   cudaFree(c->d_red_idx);
   cudaFree(c->d_diode_vd);
   cudaFree(c->d_b3_mem);
@@ -186,21 +190,27 @@ int circuit_view(xg_circuit *c, CircuitView *v) {
   v->stream = (void *)c->ctx->stream;
   v->fma = c->opt.fma;
   v->opt = DevOptions{c->opt.gmin, c->opt.voltlim};
-  v->io = LoadIO{c->d_sol[0], c->d_sta[1], c->d_sto[1], c->d_sta[0], c->d_sto[0], c->d_terms,
+  v->io = LoadIO{c->d_sol[0], c->d_sta[1], c->d_sto[1], c->d_sta[0], c->d_sto[0], c->d_terms, c->d_term_pos,
                  c->d_diode_vd, c->d_b3_mem, c->d_sta[1]};
   v->red_ptr = c->d_red_ptr;
   v->red_idx = c->d_red_idx;
   v->long_out = c->d_long_out;
+  v->short_order = c->d_short_order;
   return XG_OK;
 }
 
 ReduceArgs reduce_args(const Plan &P, const double *terms, const int64_t *red_ptr,
-                       const uint32_t *red_idx, const int64_t *d_long_out, double *out, int64_t o0,
-                       int64_t o1) {
+                       const uint32_t *d_red_idx, const int64_t *d_long_out,
+                       const int64_t *d_short_order, double *out, int64_t o0, int64_t o1) {
   auto lo = std::lower_bound(P.long_out.begin(), P.long_out.end(), o0);
   auto hi = std::lower_bound(P.long_out.begin(), P.long_out.end(), o1);
-  return ReduceArgs{terms, red_ptr, red_idx, d_long_out + (lo - P.long_out.begin()),
-                    (int64_t)(hi - lo), out, o0, o1};
+  // the short outputs of [o0, o1): the vector part, the matrix part or both
+  const int64_t n_short = (int64_t)P.short_order.size();
+  const int64_t s0 = o0 >= P.n_vec_out ? P.n_short_vec : 0;
+  const int64_t s1 = o1 <= P.n_vec_out ? P.n_short_vec : n_short;
+  return ReduceArgs{terms, red_ptr, P.scatter_terms ? nullptr : d_red_idx,
+                    d_long_out + (lo - P.long_out.begin()),
+                    (int64_t)(hi - lo), d_short_order + s0, s1 - s0, out, o0, o1};
 }
 
 }  // namespace xg
@@ -310,10 +320,18 @@ int xg_circuit_create(xg_ctx *ctx, const xg_netlist *nl, xg_circuit **out) {
     if (!rc) rc = dalloc(&c->d_sto[k], P.n_store);
   }
   if (!rc) rc = dalloc(&c->d_out, P.n_out);
-  if (!rc) rc = dalloc(&c->d_terms, P.n_terms);
+  if (!rc) rc = dalloc(&c->d_terms, P.n_terms + 1);  // + the discard slot
   if (!rc) rc = dalloc(&c->d_red_ptr, P.n_out + 1);
-  if (!rc) rc = dalloc(&c->d_red_idx, (int64_t)P.red_idx.size());
+  if (!rc && P.scatter_terms) rc = dalloc(&c->d_term_pos, (int64_t)P.term_pos.size());
+  if (!rc && !P.scatter_terms) rc = dalloc(&c->d_red_idx, (int64_t)P.red_idx.size());
+  if (!rc && !P.scatter_terms && !P.red_idx.empty() &&
+      cudaMemcpy(c->d_red_idx, P.red_idx.data(), P.red_idx.size() * sizeof(uint32_t),
+                 cudaMemcpyHostToDevice) != cudaSuccess) rc = fail(XG_ERR_CUDA, "copy red_idx");
   if (!rc) rc = dalloc(&c->d_long_out, (int64_t)P.long_out.size());
+  if (!rc) rc = dalloc(&c->d_short_order, (int64_t)P.short_order.size());
+  if (!rc && !P.short_order.empty() &&
+      cudaMemcpy(c->d_short_order, P.short_order.data(), P.short_order.size() * sizeof(int64_t),
+                 cudaMemcpyHostToDevice) != cudaSuccess) rc = fail(XG_ERR_CUDA, "copy short_order");
   if (!rc && !P.long_out.empty() &&
       cudaMemcpy(c->d_long_out, P.long_out.data(), P.long_out.size() * sizeof(int64_t),
                  cudaMemcpyHostToDevice) != cudaSuccess) rc = fail(XG_ERR_CUDA, "copy long_out");
@@ -331,9 +349,9 @@ int xg_circuit_create(xg_ctx *ctx, const xg_netlist *nl, xg_circuit **out) {
   }
   if (!rc && cudaMemcpy(c->d_red_ptr, P.red_ptr.data(), P.red_ptr.size() * sizeof(int64_t),
                         cudaMemcpyHostToDevice) != cudaSuccess) rc = fail(XG_ERR_CUDA, "copy red_ptr");
-  if (!rc && !P.red_idx.empty() &&
-      cudaMemcpy(c->d_red_idx, P.red_idx.data(), P.red_idx.size() * sizeof(uint32_t),
-                 cudaMemcpyHostToDevice) != cudaSuccess) rc = fail(XG_ERR_CUDA, "copy red_idx");
+  if (!rc && P.scatter_terms && !P.term_pos.empty() &&
+      cudaMemcpy(c->d_term_pos, P.term_pos.data(), P.term_pos.size() * sizeof(uint32_t),
+                 cudaMemcpyHostToDevice) != cudaSuccess) rc = fail(XG_ERR_CUDA, "copy term_pos");
   if (!rc) {
     cudaError_t e = cudaSuccess;
     for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
@@ -378,7 +396,7 @@ int xg_circuit_get_info(const xg_circuit *c, xg_circuit_info *info) {
   info->n_store = P.n_store;
   info->nnz = P.nnz;
   info->n_terms = P.n_terms;
-  info->scratch_bytes = P.n_terms * (int64_t)sizeof(double);
+  info->scratch_bytes = (P.n_terms + 1) * (int64_t)sizeof(double);
   for (int t = 0; t < XG_NUM_DEV_TYPES; ++t) info->n_instances[t] = P.T[t].n;
   return XG_OK;
 }
@@ -493,7 +511,7 @@ int xg_update_state(xg_circuit *c, const xg_load_flags *flags) {
   xg::Flags f{flags->dcop, flags->tranop, flags->acop, flags->transient, flags->init_jct,
               flags->init_fix, flags->newton_iter, flags->inputop, flags->pdt, flags->time,
               flags->init_tran};
-  xg::LoadIO io{c->d_sol[0], c->d_sta[1], c->d_sto[1], c->d_sta[0], c->d_sto[0], c->d_terms,
+  xg::LoadIO io{c->d_sol[0], c->d_sta[1], c->d_sto[1], c->d_sta[0], c->d_sto[0], c->d_terms, c->d_term_pos,
                 c->d_diode_vd, c->d_b3_mem, c->d_sta[1]};
   for (int k = 0; k < P.n_order; ++k) {
     int t = P.order[k];
@@ -510,7 +528,7 @@ int xg_update_state(xg_circuit *c, const xg_load_flags *flags) {
 
 static int reduce_range(xg_circuit *c, int64_t o0, int64_t o1) {
   const xg::ReduceArgs a = xg::reduce_args(c->plan, c->d_terms, c->d_red_ptr, c->d_red_idx,
-                                           c->d_long_out, c->d_out, o0, o1);
+                                           c->d_long_out, c->d_short_order, c->d_out, o0, o1);
   int rc = c->opt.fma ? xg::fast::launch_reduce(a, c->ctx->stream)
                       : xg::exact::launch_reduce(a, c->ctx->stream);
   return rc ? fail(rc, "reduce kernel launch failed") : XG_OK;

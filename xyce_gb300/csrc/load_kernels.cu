@@ -129,10 +129,17 @@ __device__ __forceinline__ void qmeyer(double vgs, double vgd, double von, doubl
 }
 
 // Term writer: term q of instance i.
+// A term goes either straight to its place in reduction order (scatter
+// layout: each output then sums a contiguous run of terms) or to [q][i]
+// (gather layout: the reduction gathers them).
 struct Terms {
   double *__restrict__ base;
+  const uint32_t *__restrict__ pos;
   int n;
-  __device__ __forceinline__ void put(int q, int i, double v) const { base[(int64_t)q * n + i] = v; }
+  __device__ __forceinline__ void put(int q, int i, double v) const {
+    const int64_t k = (int64_t)q * n + i;
+    base[pos ? (int64_t)__ldg(pos + k) : k] = v;
+  }
 };
 
 // ---- resistor (N_DEV_Resistor.C:1073-1135) ---------------------------------
@@ -143,7 +150,7 @@ __global__ void __launch_bounds__(256) res_kernel(DevType t, LoadIO io) {
   int lp = ld(t.lid + i), ln = ld(t.lid + n + i);
   double G = ld(t.p + i);
   double i0 = (ld(io.sol + lp) - ld(io.sol + ln)) * G;
-  Terms T{io.terms + t.term0, n};
+  Terms T{io.terms + (io.term_pos ? 0 : t.term0), io.term_pos ? io.term_pos + t.term0 : nullptr, n};
   T.put(0, i, i0);
   T.put(1, i, -i0);
   T.put(2, i, G);
@@ -162,7 +169,7 @@ __global__ void __launch_bounds__(256) cap_kernel(DevType t, LoadIO io) {
   double vcap = ld(io.sol + lp) - ld(io.sol + ln);
   double q0 = C * vcap;
   io.sta[t.sta0 + i] = q0;
-  Terms T{io.terms + t.term0, n};
+  Terms T{io.terms + (io.term_pos ? 0 : t.term0), io.term_pos ? io.term_pos + t.term0 : nullptr, n};
   T.put(0, i, q0);
   T.put(1, i, -q0);
   T.put(2, i, C);
@@ -202,7 +209,7 @@ __global__ void __launch_bounds__(256) vsrc_kernel(DevType t, Flags f, LoadIO io
     source = ld(t.p + XG_V_V1 * n + i);
   double srcCurrent = ld(io.sol + lb);
   double srcDrop = (ld(io.sol + lp) - ld(io.sol + ln));
-  Terms T{io.terms + t.term0, n};
+  Terms T{io.terms + (io.term_pos ? 0 : t.term0), io.term_pos ? io.term_pos + t.term0 : nullptr, n};
   T.put(0, i, srcCurrent);
   T.put(1, i, -srcCurrent);
   T.put(2, i, srcDrop);
@@ -305,7 +312,7 @@ __global__ void __launch_bounds__(256) diode_kernel(DevType t, DevOptions o, Fla
   const double Gspr = PRM(XG_D_GSPR);
 #undef PRM
   double Ir = Gspr * (Vp - Vpp);
-  Terms T{io.terms + t.term0, n};
+  Terms T{io.terms + (io.term_pos ? 0 : t.term0), io.term_pos ? io.term_pos + t.term0 : nullptr, n};
   T.put(0, i, -(-Ir));
   T.put(1, i, -Id);
   T.put(2, i, -(-Id + Ir));
@@ -580,7 +587,7 @@ __global__ void __launch_bounds__(128) mos1_kernel(DevType t, DevOptions o, Flag
   // Master::loadDAEVectors
   const double numberParallel = PRM(XG_M1_M);
 #undef PRM
-  Terms T{io.terms + t.term0, n};
+  Terms T{io.terms + (io.term_pos ? 0 : t.term0), io.term_pos ? io.term_pos + t.term0 : nullptr, n};
   const double ceqbs = dtype * (cbs), ceqbd = dtype * (cbd);
   const double ceqgb = 0.0, ceqgs = 0.0, ceqgd = 0.0;
   T.put(0, i, drainConductance != 0.0 ? Idrain * numberParallel : 0.0);
@@ -674,7 +681,8 @@ __global__ void __launch_bounds__(kRedThreads) reduce_kernel(ReduceArgs a, int l
       double s = 0.0;
       for (int64_t base = b; base < e; base += kRedChunk) {
         const int cnt = (int)(e - base < kRedChunk ? e - base : kRedChunk);
-        for (int j = lane; j < cnt; j += 32) buf[wid][j] = __ldg(a.terms + __ldg(a.red_idx + base + j));
+        for (int j = lane; j < cnt; j += 32)
+          buf[wid][j] = __ldg(a.terms + (a.red_idx ? (int64_t)__ldg(a.red_idx + base + j) : base + j));
         __syncwarp();
         if (lane == 0)
           for (int j = 0; j < cnt; ++j) s += buf[wid][j];
@@ -684,13 +692,18 @@ __global__ void __launch_bounds__(kRedThreads) reduce_kernel(ReduceArgs a, int l
     }
     return;
   }
+  // short outputs in order of term count: the lanes of a warp run loops of
+  // the same length
   const int64_t nb = (int64_t)gridDim.x - long_blocks;
-  for (int64_t o = a.o0 + ((int64_t)blockIdx.x - long_blocks) * blockDim.x + threadIdx.x; o < a.o1;
-       o += nb * blockDim.x) {
+  for (int64_t k = ((int64_t)blockIdx.x - long_blocks) * blockDim.x + threadIdx.x; k < a.n_short;
+       k += nb * blockDim.x) {
+    const int64_t o = __ldg(a.short_order + k);
     const int64_t b = __ldg(a.red_ptr + o), e = __ldg(a.red_ptr + o + 1);
-    if (e - b > kLongSegment) continue;  // a warp sums it
     double s = 0.0;
-    for (int64_t j = b; j < e; ++j) s += __ldg(a.terms + __ldg(a.red_idx + j));
+    if (a.red_idx)
+      for (int64_t j = b; j < e; ++j) s += __ldg(a.terms + __ldg(a.red_idx + j));
+    else
+      for (int64_t j = b; j < e; ++j) s += __ldg(a.terms + j);
     a.out[o] = s;
   }
 }
@@ -716,9 +729,9 @@ int launch_eval(int dev_type, const DevType &t, const DevOptions &o, const Flags
 }
 
 int launch_reduce(const ReduceArgs &a, void *stream) {
-  const int64_t n = a.o1 - a.o0;
-  if (n <= 0) return XG_OK;
-  int grid = (int)((n + kRedThreads - 1) / kRedThreads);
+  const int64_t n = a.n_short;
+  if (n <= 0 && a.n_long <= 0) return XG_OK;
+  int grid = (int)std::max<int64_t>(1, (n + kRedThreads - 1) / kRedThreads);
   if (grid > 152 * 32) grid = 152 * 32;
   const int long_blocks = (int)std::min<int64_t>((a.n_long + kRedWarps - 1) / kRedWarps, 152 * 8);
   reduce_kernel<<<grid + long_blocks, kRedThreads, 0, (cudaStream_t)stream>>>(a, long_blocks); xg::count_launches(1);

@@ -69,7 +69,7 @@ extern "C" int xg_load_noalloc(xg_circuit *c, const xg_load_flags *flags, double
     xg::set_error("xg_load_noalloc: output buffer shorter than the circuit's outputs");
     return XG_ERR_ARG;
   }
-  if (P.n_terms > kScratchTerms) {
+  if (P.n_terms + 1 > kScratchTerms) {  // the terms and their discard slot
     xg::set_error("xg_load_noalloc: circuit needs " + std::to_string(P.n_terms) +
                   " stamp terms; the fixed scratch array holds " +
                   std::to_string(kScratchTerms) + " (use xg_load)");
@@ -100,7 +100,7 @@ extern "C" int xg_load_noalloc(xg_circuit *c, const xg_load_flags *flags, double
       return rc;
     }
   }
-  const xg::ReduceArgs ra = xg::reduce_args(P, scratch, v.red_ptr, v.red_idx, v.long_out, dev_out, 0,
+  const xg::ReduceArgs ra = xg::reduce_args(P, scratch, v.red_ptr, v.red_idx, v.long_out, v.short_order, dev_out, 0,
                                             P.n_out);
   rc = v.fma ? xg::fast::launch_reduce(ra, v.stream) : xg::exact::launch_reduce(ra, v.stream);
   if (rc) xg::set_error("xg_load_noalloc: reduction kernel launch failed");

@@ -737,7 +737,7 @@ int build_plan(const xg_netlist *nl, const xg_device_options *opt, Plan *plan, s
     term += (int64_t)T.n * T.nterm;
   }
   P.n_terms = term;
-  if (P.n_terms >= ((int64_t)1 << 32)) { *err = "too many stamp terms"; return XG_ERR_ARG; }
+  if (P.n_terms + 1 >= ((int64_t)1 << 32)) { *err = "too many stamp terms"; return XG_ERR_ARG; }
 
   // Fixed-order reduction lists: a counting sort by output, stable in the
   // reference's (type, instance, statement) order.
@@ -782,9 +782,34 @@ int build_plan(const xg_netlist *nl, const xg_device_options *opt, Plan *plan, s
     std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
     for (size_t j = 0; j < out_of.size(); ++j) P.red_idx[(size_t)fill[(size_t)out_of[j]]++] = idx_of[j];
   }
+  // scatter layout unless BSIM3 terms make up half of all terms; terms with
+  // no output (a stamp on the ground row or column) then go to a discard slot
+  // after the last real one
+  const int64_t b3_terms = (int64_t)P.T[XG_DEV_BSIM3].n * P.T[XG_DEV_BSIM3].nterm;
+  P.scatter_terms = 2 * b3_terms < P.n_terms;
+  P.term_pos.clear();
+  if (P.scatter_terms) {
+    P.term_pos.assign((size_t)P.n_terms, (uint32_t)P.red_idx.size());
+    for (size_t j = 0; j < P.red_idx.size(); ++j) P.term_pos[P.red_idx[j]] = (uint32_t)j;
+  }
   P.long_out.clear();
-  for (int64_t o = 0; o < P.n_out; ++o)
-    if (P.red_ptr[(size_t)o + 1] - P.red_ptr[(size_t)o] > kLongSegment) P.long_out.push_back(o);
+  P.short_order.clear();
+  for (int64_t o = 0; o < P.n_out; ++o) {
+    const int64_t len = P.red_ptr[(size_t)o + 1] - P.red_ptr[(size_t)o];
+    if (len > kLongSegment) P.long_out.push_back(o);
+    else P.short_order.push_back(o);
+  }
+  auto mid = std::lower_bound(P.short_order.begin(), P.short_order.end(), P.n_vec_out);
+  P.n_short_vec = mid - P.short_order.begin();
+  // stable counting sort of each part by term count (0..kLongSegment)
+  auto bucket = [&](std::vector<int64_t>::iterator b, std::vector<int64_t>::iterator e) {
+    std::vector<int64_t> cnt(kLongSegment + 2, 0), tmp(b, e);
+    for (int64_t o : tmp) cnt[(size_t)(P.red_ptr[(size_t)o + 1] - P.red_ptr[(size_t)o]) + 1]++;
+    for (size_t k = 1; k < cnt.size(); ++k) cnt[k] += cnt[k - 1];
+    for (int64_t o : tmp) *(b + cnt[(size_t)(P.red_ptr[(size_t)o + 1] - P.red_ptr[(size_t)o])]++) = o;
+  };
+  bucket(P.short_order.begin(), mid);
+  bucket(mid, P.short_order.end());
   return XG_OK;
 }
 

@@ -80,6 +80,8 @@ struct LoadIO {
   const double *sta_curr, *sto_curr;
   double *sta, *sto;        // next state / store (sto holds previous iterate on entry)
   double *terms;            // per-load stamp terms
+  const uint32_t *term_pos; // scatter layout: where term q of instance i goes,
+                            // term_pos[term0 + q*n + i]; null: [q][i] layout
   double *diode_vd;         // Diode Instance::Vd carried between loads
   double *b3_mem;           // BSIM3 members carried between loads, [k*n + i]
   double *sta_curr_w;       // current state, written on the first transient step
@@ -101,9 +103,21 @@ struct Plan {
   // summed, in reference order, into output o
   std::vector<int64_t> red_ptr;
   std::vector<uint32_t> red_idx;
+  // Term layout.  scatter_terms: each term (term0 + q*n + i) is written at
+  // its position in reduction order (term_pos) and output o sums the
+  // contiguous terms [red_ptr[o], red_ptr[o+1]); otherwise terms are written
+  // in [q][i] order and output o gathers terms red_idx[red_ptr[o]..].  The
+  // scattered store is nearly free in the level-1/diode/linear kernels; the
+  // register-bound BSIM3 kernel absorbs it worse than the reduction gains.
+  bool scatter_terms = false;
+  std::vector<uint32_t> term_pos;
   // outputs summing more than kLongSegment terms (a supply node's row), in
   // ascending order: reduced by a warp each instead of a thread
   std::vector<int64_t> long_out;
+  // the other outputs, vector outputs first, then matrix outputs, each part
+  // sorted by term count: a warp then sums segments of one length
+  std::vector<int64_t> short_order;
+  int64_t n_short_vec = 0;    // short outputs in [0, n_vec_out)
 };
 constexpr int64_t kLongSegment = 64;
 
@@ -111,9 +125,11 @@ constexpr int64_t kLongSegment = 64;
 struct ReduceArgs {
   const double *terms;
   const int64_t *red_ptr;
-  const uint32_t *red_idx;
+  const uint32_t *red_idx;    // gather layout: term of each reduction entry; null: contiguous
   const int64_t *long_out;    // device, the sub-range of long outputs in [o0, o1)
   int64_t n_long;
+  const int64_t *short_order; // device, the short outputs of [o0, o1) by term count
+  int64_t n_short;
   double *out;
   int64_t o0, o1;
 };
@@ -135,15 +151,16 @@ struct CircuitView {
   DevOptions opt;
   LoadIO io;                   // terms = the circuit's own term buffer
   const int64_t *red_ptr;
-  const uint32_t *red_idx;
+  const uint32_t *red_idx;     // gather layout only (else null)
   const int64_t *long_out;     // device copy of plan->long_out
+  const int64_t *short_order;  // device copy of plan->short_order
 };
 int circuit_view(xg_circuit *c, CircuitView *v);
 // ReduceArgs for outputs [o0, o1) of a circuit's plan (long outputs located
 // on the host copy, addressed in the device copy).
 ReduceArgs reduce_args(const Plan &P, const double *terms, const int64_t *red_ptr,
-                       const uint32_t *red_idx, const int64_t *d_long_out, double *out, int64_t o0,
-                       int64_t o1);
+                       const uint32_t *d_red_idx, const int64_t *d_long_out,
+                       const int64_t *d_short_order, double *out, int64_t o0, int64_t o1);
 void set_error(const std::string &msg);
 // Kernel launches of this library, counted at every launch site (api.cpp).
 void count_launches(int k);
