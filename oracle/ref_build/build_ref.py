@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(os.path.dirname(HERE), "_ref")
 REPO = os.path.dirname(os.path.dirname(HERE))
 
-OPEN_MODELS = ["MOSFET1", "MOSFET_B3", "Diode", "Resistor", "Capacitor", "Vsrc"]
+OPEN_MODELS = ["MOSFET1", "MOSFET_B3", "Diode", "Resistor", "Capacitor", "Vsrc", "ISRC"]
 # Core files left out: the device manager itself (replaced by the harness) and
 # the reaction/TCAD machinery that needs Sacado.
 CORE_SKIP = {"N_DEV_DeviceMgr", "N_DEV_RxnSet", "N_DEV_SpecieSource", "N_DEV_Region",

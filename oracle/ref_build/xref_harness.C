@@ -41,6 +41,7 @@
 #include <N_DEV_DeviceMaster.h>
 #include <N_DEV_DeviceOptions.h>
 #include <N_DEV_Diode.h>
+#include <N_DEV_ISRC.h>
 #include <N_DEV_ExternData.h>
 #include <N_DEV_MOSFET1.h>
 #include <N_DEV_MOSFET_B3.h>
@@ -122,6 +123,7 @@ void register_once() {
   Resistor::registerDevice();
   Capacitor::registerDevice();
   Vsrc::registerDevice();
+  ISRC::registerDevice();
   Diode::registerDevice();
   MOSFET1::registerDevice();
   MOSFET_B3::registerDevice();
@@ -133,6 +135,7 @@ const char *letter_of(int type) {
     case XG_DEV_RES: return "R";
     case XG_DEV_CAP: return "C";
     case XG_DEV_VSRC: return "V";
+    case XG_DEV_ISRC: return "I";
     case XG_DEV_DIODE: return "D";
     default: return "M";
   }
@@ -198,6 +201,7 @@ int xref_build(const xg_netlist *nl, const xg_device_options *opt, XRef **out) {
       case XG_DEV_RES: count = nl->res.n; break;
       case XG_DEV_CAP: count = nl->cap.n; break;
       case XG_DEV_VSRC: count = nl->vsrc.n; break;
+      case XG_DEV_ISRC: count = nl->isrc.n; break;
       case XG_DEV_DIODE: count = nl->diode.n; break;
       case XG_DEV_MOS1: count = nl->mos1.n; break;
       case XG_DEV_BSIM3: count = nl->bsim3.n; break;
@@ -269,11 +273,13 @@ int xref_build(const xg_netlist *nl, const xg_device_options *opt, XRef **out) {
         }
         break;
       case XG_DEV_VSRC:
-        for (int i = 0; i < nl->vsrc.n; ++i) {
-          snprintf(nm, sizeof nm, "V%d", i);
-          const double *w = nl->vsrc.wave + 7 * i;
+      case XG_DEV_ISRC: {
+        const xg_src_desc &sd = e.type == XG_DEV_VSRC ? nl->vsrc : nl->isrc;
+        for (int i = 0; i < sd.n; ++i) {
+          snprintf(nm, sizeof nm, "%s%d", e.type == XG_DEV_VSRC ? "V" : "I", i);
+          const double *w = sd.wave + 7 * i;
           std::vector<Param> ps;
-          if (nl->vsrc.kind[i] == XG_SRC_PULSE) {
+          if (sd.kind[i] == XG_SRC_PULSE) {
             ps.push_back(Param("DCV0", w[0], true));
             ps.push_back(Param("DCSOURCETYPE", (int)_DC_DATA, true));
             ps.push_back(Param("TRANSIENTSOURCETYPE", (int)_PULSE_DATA, true));
@@ -284,9 +290,10 @@ int xref_build(const xg_netlist *nl, const xg_device_options *opt, XRef **out) {
             ps.push_back(Param("DCSOURCETYPE", (int)_DC_DATA, true));
           }
           add(e, nm, "", ps, 2);
-          en.push_back({nl->vsrc.p[i], nl->vsrc.m[i]});
+          en.push_back({sd.p[i], sd.m[i]});
         }
         break;
+      }
       case XG_DEV_DIODE:
         for (int i = 0; i < nl->diode.n; ++i) {
           snprintf(nm, sizeof nm, "D%d", i);
@@ -694,18 +701,26 @@ int xref_params(XRef *x, int type, double *out, int *n_params) {
         v[XG_B3_CKAPPA] = p.ckappa;
         v[XG_B3_CGDL] = p.cgdl;
         v[XG_B3_CGSL] = p.cgsl;
-      } else if (type == XG_DEV_VSRC) {
+      } else if (type == XG_DEV_VSRC || type == XG_DEV_ISRC) {
         // PulseData / ConstData parameters (N_DEV_SourceData.C:1033-1045, 2065-2070)
-        Vsrc::Instance &s = *static_cast<Vsrc::Instance *>(e.inst[i]);
+        SourceData *tran, *dc;
+        int tran_type;
+        if (type == XG_DEV_VSRC) {
+          Vsrc::Instance &s = *static_cast<Vsrc::Instance *>(e.inst[i]);
+          tran = s.Data_ptr; dc = s.dcData_ptr; tran_type = s.TRANSIENTSOURCETYPE;
+        } else {
+          ISRC::Instance &s = *static_cast<ISRC::Instance *>(e.inst[i]);
+          tran = s.Data_ptr; dc = s.dcData_ptr; tran_type = s.TRANSIENTSOURCETYPE;
+        }
         np = XG_V_NPARAMS;
         double w[16] = {0};
-        if (s.Data_ptr && s.TRANSIENTSOURCETYPE == _PULSE_DATA) {
+        if (tran && tran_type == _PULSE_DATA) {
           v[XG_V_KIND] = XG_SRC_PULSE;
-          s.Data_ptr->getParams(w);
+          tran->getParams(w);
           for (int k = 0; k < 7; ++k) v[XG_V_V1 + k] = w[k];
         } else {
           v[XG_V_KIND] = XG_SRC_DC;
-          if (s.dcData_ptr) s.dcData_ptr->getParams(w);
+          if (dc) dc->getParams(w);
           v[XG_V_V1] = w[0];
         }
       } else {

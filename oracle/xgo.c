@@ -84,7 +84,7 @@ static int nparams_of(int t) {
   switch (t) {
     case XG_DEV_RES: return XG_R_NPARAMS;
     case XG_DEV_CAP: return XG_C_NPARAMS;
-    case XG_DEV_VSRC: return XG_V_NPARAMS;
+    case XG_DEV_VSRC: case XG_DEV_ISRC: return XG_V_NPARAMS;
     case XG_DEV_DIODE: return XG_D_NPARAMS;
     case XG_DEV_MOS1: return XG_M1_NPARAMS;
     case XG_DEV_BSIM3: return xgo_b3_nparams();
@@ -112,9 +112,8 @@ int xgo_build(const xg_netlist *nl, const xg_device_options *opt,
     T->n = type_count(nl, t);
     T->np = nparams_of(t);
     T->p = params ? params[t] : NULL;
-    if (T->n > 0 && !T->p && t != XG_DEV_ISRC) { free(c); return XG_ERR_ARG; }
+    if (T->n > 0 && !T->p) { free(c); return XG_ERR_ARG; }
   }
-  if (c->T[XG_DEV_ISRC].n) { free(c); return XG_ERR_UNSUPPORTED; }
 
   /* LIDs: nodes, then internal unknowns by type order and instance. */
   int next = nl->n_nodes;

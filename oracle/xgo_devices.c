@@ -40,7 +40,7 @@ static void *members(xgo_circuit *c, int t, size_t sz) {
 
 int xgo_nlid(int t) {
   switch (t) {
-    case XG_DEV_RES: case XG_DEV_CAP: return 2;
+    case XG_DEV_RES: case XG_DEV_CAP: case XG_DEV_ISRC: return 2;
     case XG_DEV_VSRC: case XG_DEV_DIODE: return 3;
     case XG_DEV_MOS1: return 6;
     case XG_DEV_BSIM3: return xgo_b3_nlid();
@@ -58,6 +58,8 @@ void xgo_assign_lids(xgo_circuit *c, const xg_netlist *nl, int t, int i, int *ne
     case XG_DEV_CAP: L[0] = nl->cap.p[i]; L[1] = nl->cap.m[i]; break;
     case XG_DEV_VSRC: /* N_DEV_Vsrc.C registerLIDs: li_Bra = intLIDVec[0] */
       L[0] = nl->vsrc.p[i]; L[1] = nl->vsrc.m[i]; L[2] = (*next)++; break;
+    case XG_DEV_ISRC: /* N_DEV_ISRC.C:430-431: two external nodes, no internal */
+      L[0] = nl->isrc.p[i]; L[1] = nl->isrc.m[i]; break;
     case XG_DEV_DIODE: /* N_DEV_Diode.C:456-459: li_Pri internal iff RS != 0 */
       L[0] = nl->diode.a[i]; L[1] = nl->diode.c[i];
       L[2] = (P(T, XG_D_GSPR, i) != 0.0) ? (*next)++ : L[0];
@@ -781,6 +783,20 @@ void xgo_load_vectors(xgo_circuit *c, int t, int i0, int i1, xgo_io *io) {
         const int *L = T->lid + (int64_t)i * 2;
         io->q[L[0]] += m[i].q0;
         io->q[L[1]] += -m[i].q0;
+      }
+      break;
+    }
+    case XG_DEV_ISRC: { /* N_DEV_ISRC.C:774-800: F only, no matrix entries */
+      const xg_load_flags *fl = io->fl;
+      for (int i = i0; i < i1; ++i) {
+        const int *L = T->lid + (int64_t)i * 2;
+        double source;
+        if ((fl->tranop || fl->transient) && P(T, XG_V_KIND, i) == XG_SRC_PULSE)
+          source = pulse_value(T, i, fl->time);
+        else
+          source = P(T, XG_V_V1, i);
+        io->f[L[0]] += source;
+        io->f[L[1]] -= source;
       }
       break;
     }

@@ -371,24 +371,27 @@ static int cmp_double(const void *a, const void *b) {
   return x < y ? -1 : x > y;
 }
 
-/* PULSE corners up to tstop, sorted, without duplicates (PulseData::getBreakPoints). */
+/* PULSE corners of voltage and current sources up to tstop, sorted, without
+ * duplicates (PulseData::getBreakPoints). */
 static double *breakpoints(const xgo_circuit *c, double tstop, int *nbp) {
-  const xgo_type *V = &c->T[XG_DEV_VSRC];
   int cap = 64, nb = 0;
   double *bp = (double *)xmalloc(sizeof(double) * cap);
-  for (int i = 0; i < V->n; ++i) {
-    if (P(V, XG_V_KIND, i) != XG_SRC_PULSE) continue;
-    double td = P(V, XG_V_TD, i), tr = P(V, XG_V_TR, i), tf = P(V, XG_V_TF, i);
-    double pw = P(V, XG_V_PW, i), per = P(V, XG_V_PER, i);
-    for (int k = 0;; ++k) {
-      double base = per > 0 ? per * k : 0.0;
-      double pts[4] = {base + td, base + td + tr, base + td + tr + pw, base + td + tr + pw + tf};
-      for (int j = 0; j < 4; ++j) {
-        if (pts[j] <= 0.0 || pts[j] >= tstop) continue;
-        if (nb == cap) { cap *= 2; bp = (double *)realloc(bp, sizeof(double) * cap); }
-        bp[nb++] = pts[j];
+  for (int src = 0; src < 2; ++src) {
+    const xgo_type *V = &c->T[src == 0 ? XG_DEV_VSRC : XG_DEV_ISRC];
+    for (int i = 0; i < V->n; ++i) {
+      if (P(V, XG_V_KIND, i) != XG_SRC_PULSE) continue;
+      double td = P(V, XG_V_TD, i), tr = P(V, XG_V_TR, i), tf = P(V, XG_V_TF, i);
+      double pw = P(V, XG_V_PW, i), per = P(V, XG_V_PER, i);
+      for (int k = 0;; ++k) {
+        double base = per > 0 ? per * k : 0.0;
+        double pts[4] = {base + td, base + td + tr, base + td + tr + pw, base + td + tr + pw + tf};
+        for (int j = 0; j < 4; ++j) {
+          if (pts[j] <= 0.0 || pts[j] >= tstop) continue;
+          if (nb == cap) { cap *= 2; bp = (double *)realloc(bp, sizeof(double) * cap); }
+          bp[nb++] = pts[j];
+        }
+        if (per <= 0 || base + td >= tstop) break;
       }
-      if (per <= 0 || base + td >= tstop) break;
     }
   }
   if (nb == cap) bp = (double *)realloc(bp, sizeof(double) * (cap + 1));

@@ -1,7 +1,8 @@
 """Small seeded circuits for the golden fixtures and the parity tests.
 
 Each entry builds a Netlist and lists the load sequence (solver flags) that
-the fixture records.  The circuits cover every supported device, every
+the fixture records.  The circuits cover every supported device (current
+sources, DC and PULSE, in the mixed circuit), every
 per-instance branch the flags reach (limiting on/off, dcop/initJct/transient,
 newton_iter 0 / >0), internal nodes (RD, diode RS) and ground terminals.
 """
@@ -44,6 +45,10 @@ def mixed(seed=1):
     nl.vsrc = dict(p=[0, 1, 2], m=[-1, -1, 3], kind=[abi.SRC_DC, abi.SRC_PULSE, abi.SRC_PULSE],
                    wave=[[1.8, 0, 0, 0, 0, 0, 0], [0, 1.8, 1e-10, 1e-10, 1e-10, 9e-10, 2e-9],
                          [0.2, 1.2, 0, 5e-11, 2e-10, 3e-10, 1e-9]])
+    nl.isrc = dict(p=[4, -1, 7, 9], m=[-1, 5, 8, 4],
+                   kind=[abi.SRC_DC, abi.SRC_PULSE, abi.SRC_PULSE, abi.SRC_DC],
+                   wave=[[1e-4, 0, 0, 0, 0, 0, 0], [0, 2e-3, 5e-11, 1e-10, 2e-10, 4e-10, 1.5e-9],
+                         [-1e-3, 1e-3, 0, 3e-10, 1e-10, 2e-10, 0], [-5e-5, 0, 0, 0, 0, 0, 0]])
     nl.type_order = [abi.DEV_VSRC, abi.DEV_RES, abi.DEV_MOS1, abi.DEV_DIODE, abi.DEV_CAP,
                      abi.DEV_ISRC, abi.DEV_BSIM3]
     return nl

@@ -58,12 +58,16 @@ def test_setup_rejects_unknown_model_parameter(engine_lib):
     assert b"XYZZY" in engine.lib().xg_last_error()
 
 
-def test_setup_rejects_current_sources_and_newmeyer(engine_lib):
-    nl = netlists.inverter_chain(3)
-    nl.isrc = dict(p=[1], m=[-1], kind=[0], wave=[[1e-3, 0, 0, 0, 0, 0, 0]])
-    assert _status(nl) == -8
+def test_setup_rejects_newmeyer_and_bad_sources(engine_lib):
     nl = netlists.inverter_chain(3)
     assert _status(nl, opt=abi.device_options(newmeyer=1)) == -8
+    nl = netlists.inverter_chain(3)
+    nl.isrc = dict(p=[1], m=[-1], kind=[7], wave=[[1e-3, 0, 0, 0, 0, 0, 0]])
+    assert _status(nl) == -1  # XG_ERR_ARG: unknown waveform kind
+    nl.isrc = dict(p=[1], m=[99], kind=[0], wave=[[1e-3, 0, 0, 0, 0, 0, 0]])
+    assert _status(nl) != 0   # terminal outside the circuit
+    nl.isrc = dict(p=[1], m=[-1], kind=[0], wave=[[1e-3, 0, 0, 0, 0, 0, 0]])
+    assert _status(nl) == 0
 
 
 def test_setup_rejects_wrong_model_type(engine_lib):

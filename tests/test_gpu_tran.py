@@ -75,6 +75,15 @@ def test_rc_closed_form(gpu_ctx):
     assert np.abs(v[:, 1] - rc_exact(t)).max() < 1e-3
 
 
+def test_current_source_rc(gpu_ctx, oracle_lib):
+    """PULSE current source into an RC: closed form, and the oracle's steps."""
+    from test_tran_cpu import rc_current_driven, rc_exact
+    cpu, gpu = _both(gpu_ctx, rc_current_driven(), np.zeros(1), 5e-9, [0])
+    _agree(cpu, gpu)
+    t, v, _ = gpu
+    assert np.abs(v[:, 0] - rc_exact(t)).max() < 1e-3
+
+
 def test_transient_is_deterministic(gpu_ctx):
     nl = netlists.inverter_chain(40)
     x0 = netlists.inverter_chain_nodeset(40)

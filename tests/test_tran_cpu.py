@@ -44,6 +44,27 @@ def test_rc_step_response_matches_closed_form(oracle_lib):
     assert abs(v[-1, 1] - exact[-1]) < 1e-3
 
 
+def rc_current_driven(r=1e3, c=1e-12, td=0.1e-9, tr=1e-12, i2=1e-3):
+    """PULSE current from ground into node 0, R and C from node 0 to ground:
+    C dv/dt + v/R = I(t), the low-pass response to a step of I2*R volts."""
+    nl = abi.Netlist(1)
+    nl.res = dict(p=[0], m=[-1], value=[r])
+    nl.cap = dict(p=[0], m=[-1], value=[c])
+    nl.isrc = dict(p=[-1], m=[0], kind=[abi.SRC_PULSE], wave=[[0.0, i2, td, tr, tr, 50e-9, 0.0]])
+    return nl
+
+
+def test_current_source_rc_matches_closed_form(oracle_lib):
+    from oracle.oracle import transient
+    nl = rc_current_driven()
+    t, v, st = transient(_oracle(nl), 5e-9, 1e-12, [0])
+    assert st["status"] == 0 and st["steps"] > 20
+    assert np.abs(v[:, 0] - rc_exact(t)).max() < 1e-3
+    # the PULSE corners of a current source are breakpoints too
+    for bp in (0.1e-9, 0.1e-9 + 1e-12):
+        assert np.min(np.abs(t - bp)) < 1e-18
+
+
 def test_breakpoints_are_hit(oracle_lib):
     from oracle.oracle import transient
     nl = rc_lowpass(td=0.3e-9, tr=50e-12)

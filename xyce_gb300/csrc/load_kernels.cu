@@ -220,6 +220,23 @@ __global__ void __launch_bounds__(256) vsrc_kernel(DevType t, Flags f, LoadIO io
   T.put(7, i, -1.0);
 }
 
+// ---- independent current source (N_DEV_ISRC.C:774-800) ----------------------
+// The source value goes into F at both terminals; there are no matrix entries.
+__global__ void __launch_bounds__(256) isrc_kernel(DevType t, Flags f, LoadIO io) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= t.n) return;
+  if (t.cflags) f = t.cflags[t.cid[i]];
+  const int n = t.n;
+  double source;
+  if ((f.tranop || f.transient) && ld(t.p + XG_V_KIND * n + i) == XG_SRC_PULSE)
+    source = pulse_value(t.p, n, i, f.time);
+  else
+    source = ld(t.p + XG_V_V1 * n + i);
+  Terms T{io.terms + (io.term_pos ? 0 : t.term0), io.term_pos ? io.term_pos + t.term0 : nullptr, n};
+  T.put(0, i, source);
+  T.put(1, i, -source);
+}
+
 // ---- junction diode, level 1 (N_DEV_Diode.C:873-1331, 2007-2128) ------------
 __global__ void __launch_bounds__(256) diode_kernel(DevType t, DevOptions o, Flags f, LoadIO io) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -720,6 +737,7 @@ int launch_eval(int dev_type, const DevType &t, const DevOptions &o, const Flags
     case XG_DEV_RES: res_kernel<<<grid_for(t.n, 256), 256, 0, s>>>(t, io); xg::count_launches(1); break;
     case XG_DEV_CAP: cap_kernel<<<grid_for(t.n, 256), 256, 0, s>>>(t, io); xg::count_launches(1); break;
     case XG_DEV_VSRC: vsrc_kernel<<<grid_for(t.n, 256), 256, 0, s>>>(t, f, io); xg::count_launches(1); break;
+    case XG_DEV_ISRC: isrc_kernel<<<grid_for(t.n, 256), 256, 0, s>>>(t, f, io); xg::count_launches(1); break;
     case XG_DEV_DIODE: diode_kernel<<<grid_for(t.n, 256), 256, 0, s>>>(t, o, f, io); xg::count_launches(1); break;
     case XG_DEV_MOS1: mos1_kernel<<<grid_for(t.n, 128), 128, 0, s>>>(t, o, f, io); xg::count_launches(1); break;
     case XG_DEV_BSIM3: bsim3_kernel<<<grid_for(t.n, 128), 128, 0, s>>>(t, o, f, io); xg::count_launches(1); break;

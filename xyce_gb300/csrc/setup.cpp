@@ -48,6 +48,8 @@ static const TermDef kCapTerms[] = {
 static const TermDef kVsrcTerms[] = {
     {OUT_F, 0, 0}, {OUT_F, 1, 0}, {OUT_F, 2, 0}, {OUT_F, 2, 0},
     {OUT_DFDX, 0, 2}, {OUT_DFDX, 1, 2}, {OUT_DFDX, 2, 0}, {OUT_DFDX, 2, 1}};
+// ISRC: N_DEV_ISRC.C:774-800 (F only, an empty Jacobian stamp).  LID slots: 0 pos, 1 neg.
+static const TermDef kIsrcTerms[] = {{OUT_F, 0, 0}, {OUT_F, 1, 0}};
 // Diode: N_DEV_Diode.C:2034-2128.  LID slots: 0 pos, 1 neg, 2 pos'.
 static const TermDef kDiodeTerms[] = {
     {OUT_F, 0, 0}, {OUT_F, 1, 0}, {OUT_F, 2, 0},
@@ -78,7 +80,7 @@ const TypeLayout &type_layout(int t) {
       {2, NT(kResTerms), kResTerms, XG_R_NPARAMS, 0, 0},
       {2, NT(kCapTerms), kCapTerms, XG_C_NPARAMS, 1, 0},
       {3, NT(kVsrcTerms), kVsrcTerms, XG_V_NPARAMS, 0, 0},
-      {0, 0, nullptr, 0, 0, 0},  // ISRC: not supported
+      {2, NT(kIsrcTerms), kIsrcTerms, XG_V_NPARAMS, 0, 0},
       {3, NT(kDiodeTerms), kDiodeTerms, XG_D_NPARAMS, 0, 1},
       {6, NT(kMos1Terms), kMos1Terms, XG_M1_NPARAMS, 8, 5},
       {b3_nlid(), b3_nterm(), b3_terms(), XG_B3_NPARAMS, 12, 5},
@@ -512,7 +514,6 @@ int build_plan(const xg_netlist *nl, const xg_device_options *opt, Plan *plan, s
   Plan &P = *plan;
   if (!nl || !opt || nl->n_nodes < 0) { *err = "null netlist/options"; return XG_ERR_ARG; }
   if (opt->newmeyer) { *err = "newmeyer=1 is not supported"; return XG_ERR_UNSUPPORTED; }
-  if (nl->isrc.n) { *err = "independent current sources are not supported"; return XG_ERR_UNSUPPORTED; }
   P.n_nodes = nl->n_nodes;
   if (nl->type_order && nl->n_type_order > 0) {
     if (nl->n_type_order > XG_NUM_DEV_TYPES) { *err = "type_order too long"; return XG_ERR_ARG; }
@@ -578,10 +579,13 @@ int build_plan(const xg_netlist *nl, const xg_device_options *opt, Plan *plan, s
           if (!node_ok(nl->cap.p[i], P.n_nodes) || !node_ok(nl->cap.m[i], P.n_nodes)) goto badnode;
           tmp[XG_C_C] = nl->cap.value[i];
           break;
-        case XG_DEV_VSRC: {
-          if (!node_ok(nl->vsrc.p[i], P.n_nodes) || !node_ok(nl->vsrc.m[i], P.n_nodes)) goto badnode;
-          const double *w = nl->vsrc.wave + 7 * (size_t)i;
-          int kind = nl->vsrc.kind[i];
+        case XG_DEV_VSRC:
+        case XG_DEV_ISRC: {
+          // Same source data for both (N_DEV_SourceData.C): the DC value, or PULSE's seven.
+          const xg_src_desc &d = t == XG_DEV_VSRC ? nl->vsrc : nl->isrc;
+          if (!node_ok(d.p[i], P.n_nodes) || !node_ok(d.m[i], P.n_nodes)) goto badnode;
+          const double *w = d.wave + 7 * (size_t)i;
+          int kind = d.kind[i];
           if (kind != XG_SRC_DC && kind != XG_SRC_PULSE) { *err = "bad source kind"; return XG_ERR_ARG; }
           tmp[XG_V_KIND] = kind;
           for (int k = 0; k < 7; ++k) tmp[XG_V_V1 + k] = kind == XG_SRC_PULSE || k == 0 ? w[k] : 0.0;
@@ -639,6 +643,7 @@ int build_plan(const xg_netlist *nl, const xg_device_options *opt, Plan *plan, s
         case XG_DEV_RES: Ls[0] = nl->res.p[i]; Ls[1] = nl->res.m[i]; break;
         case XG_DEV_CAP: Ls[0] = nl->cap.p[i]; Ls[1] = nl->cap.m[i]; break;
         case XG_DEV_VSRC: Ls[0] = nl->vsrc.p[i]; Ls[1] = nl->vsrc.m[i]; Ls[2] = next++; break;
+        case XG_DEV_ISRC: Ls[0] = nl->isrc.p[i]; Ls[1] = nl->isrc.m[i]; break;
         case XG_DEV_DIODE:
           Ls[0] = nl->diode.a[i]; Ls[1] = nl->diode.c[i];
           Ls[2] = prm(XG_D_GSPR) != 0.0 ? next++ : Ls[0];

@@ -374,18 +374,20 @@ struct Run {
 
 std::vector<double> pulse_breakpoints(const Plan &P, double tstop) {
   std::vector<double> bp;
-  const TypeData &V = P.T[XG_DEV_VSRC];
-  for (int i = 0; i < V.n; ++i) {
-    auto p = [&](int k) { return V.params[(size_t)k * V.n + i]; };
-    if (p(XG_V_KIND) != XG_SRC_PULSE) continue;
-    const double td = p(XG_V_TD), tr = p(XG_V_TR), tf = p(XG_V_TF), pw = p(XG_V_PW),
-                 per = p(XG_V_PER);
-    for (int k = 0;; ++k) {
-      const double base = per > 0 ? per * k : 0.0;
-      const double pts[4] = {base + td, base + td + tr, base + td + tr + pw, base + td + tr + pw + tf};
-      for (double t : pts)
-        if (t > 0.0 && t < tstop) bp.push_back(t);
-      if (per <= 0 || base + td >= tstop) break;
+  for (int src : {XG_DEV_VSRC, XG_DEV_ISRC}) {
+    const TypeData &V = P.T[src];
+    for (int i = 0; i < V.n; ++i) {
+      auto p = [&](int k) { return V.params[(size_t)k * V.n + i]; };
+      if (p(XG_V_KIND) != XG_SRC_PULSE) continue;
+      const double td = p(XG_V_TD), tr = p(XG_V_TR), tf = p(XG_V_TF), pw = p(XG_V_PW),
+                   per = p(XG_V_PER);
+      for (int k = 0;; ++k) {
+        const double base = per > 0 ? per * k : 0.0;
+        const double pts[4] = {base + td, base + td + tr, base + td + tr + pw, base + td + tr + pw + tf};
+        for (double t : pts)
+          if (t > 0.0 && t < tstop) bp.push_back(t);
+        if (per <= 0 || base + td >= tstop) break;
+      }
     }
   }
   bp.push_back(tstop);
