@@ -248,7 +248,9 @@ int xg_load(xg_circuit *c, const xg_load_flags *flags);
  * Replaces the KLU solver behind N_LAS_AmesosSolver::solve
  * (N_LAS_AmesosSolver.C:231-492): symbolic analysis once per pattern (:388),
  * numeric factorisation per Newton iteration (:405), solve (:444).
- * xg_lu_analyze   : host: approximate-minimum-degree column order, then a
+ * xg_lu_analyze   : host: a column order (approximate minimum degree, or
+ *                   nested dissection when minimum degree leaves a long
+ *                   dependency chain and dissection models faster), then a
  *                   left-looking threshold-partial-pivot factorisation of the
  *                   given values (KLU's tol 0.001, diagonal preferred) that
  *                   fixes the pivot order and the L\U pattern; uploads them.
@@ -275,6 +277,7 @@ typedef struct {
   double refactor_flops;      /* multiply-adds + divides of one refactor */
   double solve_flops;         /* multiply-adds of one forward + backward solve */
   double min_pivot, max_pivot;/* |U(k,k)| range of the analysed matrix */
+  int ordering;               /* column order: 0 minimum degree, 1 nested dissection */
 } xg_lu_info;
 int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const int *host_colidx,
                   const double *host_values, int precision, xg_lu **out);
@@ -286,10 +289,12 @@ int xg_lu_get_info(const xg_lu *lu, xg_lu_info *info);
 int xg_lu_get_symbolic(const xg_lu *lu, int *P, int *Q, int *lu_rowptr, int *lu_colidx);
 int xg_lu_destroy(xg_lu *lu);
 /* host-only analysis pieces (no GPU): the AMD order alone, and the full
- * analysis returning P, Q and the L\U non-zero count */
+ * analysis returning P, Q, the L\U non-zero count and (info may be NULL) the
+ * statistics xg_lu_get_info reports */
 int xg_lu_order(int n, const int *host_rowptr, const int *host_colidx, int *order, int *n_dense);
 int xg_lu_analyze_host(int n, const int *host_rowptr, const int *host_colidx,
-                       const double *host_values, int *P, int *Q, int64_t *nnz_lu);
+                       const double *host_values, int *P, int *Q, int64_t *nnz_lu,
+                       xg_lu_info *info);
 
 /* ---- transient analysis on the GPU -----------------------------------------
  * DC operating point, then .TRAN TSTEP TSTOP with the trapezoid ("OneStep")

@@ -13,7 +13,10 @@
 //    was claimed earlier by a running warp, so the schedule always advances.
 //    Rows far apart in the elimination order run concurrently; the row
 //    pipeline needs no level barriers.  Each entry of a row is updated by one
-//    lane in ascending k, so the result is the same on every run.
+//    lane in ascending k, so the result is the same on every run.  The
+//    position in row i that each entry of U row k updates is precomputed on
+//    the host (the update schedule, lu_build_updates), so an update is one
+//    coalesced index load, one coalesced value load and one multiply-add.
 //  * solves: the same claim/wait scheme by rows of L (forward) and of U
 //    (backward, rows claimed in descending order), a fixed lane-strided
 //    partial sum and a fixed shuffle tree per row.
@@ -79,6 +82,8 @@ struct LuDev {
   const int *lu2a;            // LU position -> A entry, -1 for fill
   const int *P, *Q;
   const int *arp, *aci;       // A pattern (CSR) for the residual
+  const int64_t *urp;         // per row: start of its updates in upos
+  const int *upos;            // per update: the position in the row it updates
   unsigned *ctrl;
   unsigned *done_f, *done_l, *done_u;
   void *rdiag;                // 1 / U(k,k) per row, written by the refactor
@@ -105,17 +110,6 @@ __global__ void lu_assemble(LuDev d, const double *__restrict__ a, double *__res
     for (int64_t p = t0; p < nnz_a; p += stride) a_copy[p] = a[p];
 }
 
-__device__ __forceinline__ int find_col(const int *__restrict__ ci, int lo, int end, int col) {
-  // the position in [lo, end) holding col, or -1
-  int hi = end;
-  while (lo < hi) {
-    int mid = (lo + hi) >> 1;
-    int c = __ldg(ci + mid);
-    if (c < col) lo = mid + 1; else hi = mid;
-  }
-  return (lo < end && __ldg(ci + lo) == col) ? lo : -1;
-}
-
 template <class T>
 __global__ void __launch_bounds__(256) lu_factor(LuDev d, T *val) {
   const int lane = threadIdx.x & 31;
@@ -125,25 +119,19 @@ __global__ void __launch_bounds__(256) lu_factor(LuDev d, T *val) {
     if (lane == 0) row = int(atomicAdd(&d.ctrl[C_CLAIM_F], 1u));
     row = __shfl_sync(0xffffffffu, row, 0);
     if (row >= d.n) break;
-    const int s = __ldg(d.rp + row), dp = __ldg(d.diag + row), e = __ldg(d.rp + row + 1);
+    const int s = __ldg(d.rp + row), dp = __ldg(d.diag + row);
     T *rdiag = (T *)d.rdiag;
+    const int *up = d.upos + __ldg(d.urp + row);
     for (int p = s; p < dp; ++p) {
       const int k = __ldg(d.ci + p);
-      const int kd = __ldg(d.diag + k), ke = __ldg(d.rp + k + 1);
+      const int q0 = __ldg(d.diag + k) + 1, len = __ldg(d.rp + k + 1) - q0;
       if (lane == 0) wait_epoch(d.done_f + k, epoch, d.ctrl);
       __syncwarp();
       const T l = val[p] * __ldcg(rdiag + k);
       __syncwarp();
       if (lane == 0) val[p] = l;
-      for (int q = kd + 1 + lane; q < ke; q += 32) {
-        const int m = __ldg(d.ci + q);
-        const int pos = find_col(d.ci, p + 1, e, m);
-        if (pos >= 0) {
-          val[pos] -= l * __ldcg(val + q);
-        } else {
-          atomicOr(&d.ctrl[C_STATUS], ST_PATTERN);
-        }
-      }
+      for (int j = lane; j < len; j += 32) val[__ldg(up + j)] -= l * __ldcg(val + q0 + j);
+      up += len;
       __syncwarp();
     }
     if (lane == 0) {
@@ -268,11 +256,6 @@ __host__ __device__ inline size_t smem_bytes(int n, int64_t nnz, size_t tsz) {
   return a16(tsz * size_t(nnz)) + 2 * a16(tsz * size_t(n)) +
          sizeof(int) * (size_t(nnz) + 4 * size_t(n) + 1);
 }
-// The one-lane factor also keeps a column -> position map of the current row.
-__host__ __device__ inline size_t smem_bytes_seq(int n, int64_t nnz, size_t tsz) {
-  return smem_bytes(n, nnz, tsz) + sizeof(int) * size_t(n);
-}
-
 template <class T>
 __device__ SmemLU<T> smem_layout(char *base, int n, int64_t nnz) {
   auto a16 = [](size_t v) { return (v + 15) & ~size_t(15); };
@@ -339,24 +322,19 @@ __global__ void __launch_bounds__(kSeqThreads) lu_factor_seq(LuDev d, const doub
   if (a_copy != a)
     for (int64_t p = threadIdx.x; p < nnz_a; p += blockDim.x) a_copy[p] = a[p];
   __syncthreads();
-  // column -> position in the current row; every column a row update touches
-  // is in that row's pattern, so stale entries of earlier rows are never read
-  int *map = (int *)(L.flag_u + n);
   if (threadIdx.x == 0) {
     T *rd = (T *)L.y;
     int bad = -1;
+    const int *up = d.upos;
     for (int row = 0; row < n; ++row) {
-      const int s = L.rp[row], dp = L.diag[row], e = L.rp[row + 1];
-      for (int p = s; p < e; ++p) map[L.ci[p]] = p;
+      const int s = L.rp[row], dp = L.diag[row];
       for (int p = s; p < dp; ++p) {
         const int k = L.ci[p];
         const T l = L.val[p] * rd[k];
         L.val[p] = l;
-        for (int q = L.diag[k] + 1; q < L.rp[k + 1]; ++q) {
-          const int pos = map[L.ci[q]];
-          if (pos > p && pos < e && L.ci[pos] == L.ci[q]) L.val[pos] -= l * L.val[q];
-          else bad = -2;
-        }
+        const int q0 = L.diag[k] + 1, len = L.rp[k + 1] - q0;
+        for (int j = 0; j < len; ++j) L.val[__ldg(up + j)] -= l * L.val[q0 + j];
+        up += len;
       }
       const T u = L.val[dp];
       if (!(fabs(double(u)) > 0.0) || !isfinite(double(u))) {
@@ -364,8 +342,7 @@ __global__ void __launch_bounds__(kSeqThreads) lu_factor_seq(LuDev d, const doub
       }
       rd[row] = recip(u);
     }
-    if (bad == -2) atomicOr(&d.ctrl[C_STATUS], ST_PATTERN);
-    else if (bad >= 0) {
+    if (bad >= 0) {
       atomicOr(&d.ctrl[C_STATUS], ST_PIVOT);
       d.ctrl[C_BAD_ROW] = unsigned(bad);
     }
@@ -434,15 +411,6 @@ __device__ __forceinline__ bool wait_flag_smem(volatile int *flag, unsigned *ctr
   return true;
 }
 
-__device__ __forceinline__ int find_col_smem(const int *ci, int lo, int end, int col) {
-  int hi = end;
-  while (lo < hi) {
-    int mid = (lo + hi) >> 1;
-    if (ci[mid] < col) lo = mid + 1; else hi = mid;
-  }
-  return (lo < end && ci[lo] == col) ? lo : -1;
-}
-
 template <class T>
 __global__ void __launch_bounds__(kCtaThreads) lu_factor_cta(LuDev d, const double *__restrict__ a,
                                                              double *__restrict__ a_copy, int64_t nnz_a,
@@ -476,22 +444,19 @@ __global__ void __launch_bounds__(kCtaThreads) lu_factor_cta(LuDev d, const doub
     if (lane == 0) row = atomicAdd(&claim, 1);
     row = __shfl_sync(0xffffffffu, row, 0);
     if (row >= n) break;
-    const int s = L.rp[row], dp = L.diag[row], e = L.rp[row + 1];
+    const int s = L.rp[row], dp = L.diag[row];
+    const int *up = d.upos + __ldg(d.urp + row);
     for (int p = s; p < dp; ++p) {
       const int k = L.ci[p];
       if (lane == 0) wait_flag_smem(L.flag + k, d.ctrl);
       __syncwarp();
       __threadfence_block();
-      const int ke = L.rp[k + 1];
-      const int kd = L.diag[k];
+      const int q0 = L.diag[k] + 1, len = L.rp[k + 1] - q0;
       const T l = L.val[p] * L.y[k];
       __syncwarp();
       if (lane == 0) L.val[p] = l;
-      for (int q = kd + 1 + lane; q < ke; q += 32) {
-        const int pos = find_col_smem(L.ci, p + 1, e, L.ci[q]);
-        if (pos >= 0) L.val[pos] -= l * L.val[q];
-        else atomicOr(&d.ctrl[C_STATUS], ST_PATTERN);
-      }
+      for (int j = lane; j < len; j += 32) L.val[__ldg(up + j)] -= l * L.val[q0 + j];
+      up += len;
       __syncwarp();
     }
     if (lane == 0) {
@@ -601,6 +566,8 @@ struct xg_lu {
   int64_t nnz_lu = 0;
   int *d_rp = nullptr, *d_ci = nullptr, *d_diag = nullptr, *d_lu2a = nullptr;
   int *d_P = nullptr, *d_Q = nullptr, *d_arp = nullptr, *d_aci = nullptr;
+  int64_t *d_urp = nullptr;
+  int *d_upos = nullptr;
   unsigned *d_ctrl = nullptr, *d_done = nullptr;  // 3n flags
   void *d_val = nullptr;                          // nnz_lu of T
   void *d_y = nullptr, *d_z = nullptr;            // n of T
@@ -613,8 +580,8 @@ struct xg_lu {
   bool narrow = false;                     // one lane walks the rows (<= 2 rows per level)
   bool factored = false;
   xg::LuDev dev() const {
-    return xg::LuDev{S.n, d_rp, d_ci, d_diag, d_lu2a, d_P, d_Q, d_arp, d_aci, d_ctrl,
-                     d_done, d_done + S.n, d_done + 2 * S.n, d_rdiag};
+    return xg::LuDev{S.n, d_rp, d_ci, d_diag, d_lu2a, d_P, d_Q, d_arp, d_aci, d_urp, d_upos,
+                     d_ctrl, d_done, d_done + S.n, d_done + 2 * S.n, d_rdiag};
   }
 };
 
@@ -640,6 +607,7 @@ int upload(V **dst, const std::vector<V> &src) {
 
 void free_lu(xg_lu *lu) {
   void *ptrs[] = {lu->d_rp, lu->d_ci, lu->d_diag, lu->d_lu2a, lu->d_P, lu->d_Q, lu->d_arp,
+                  lu->d_urp, lu->d_upos,
                   lu->d_aci, lu->d_ctrl, lu->d_done, lu->d_val, lu->d_y, lu->d_z, lu->d_rdiag, lu->d_a,
                   lu->d_r, lu->d_dx};
   for (void *p : ptrs)
@@ -727,6 +695,10 @@ extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const i
     xg::set_error(err);
     return XG_ERR_SINGULAR;
   }
+  if (!xg::lu_build_updates(lu->S)) {
+    xg::set_error("xg_lu_analyze: internal error, an update falls outside the L\\U pattern");
+    return XG_ERR_ARG;
+  }
   XG_CU(cudaSetDevice(lu->device));
   const xg::LuSymbolic &S = lu->S;
   lu->nnz_lu = S.rp[n];
@@ -740,8 +712,15 @@ extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const i
   if ((rc = upload(&lu->d_rp, S.rp)) || (rc = upload(&lu->d_ci, S.ci)) ||
       (rc = upload(&lu->d_diag, S.diag)) || (rc = upload(&lu->d_lu2a, S.lu2a)) ||
       (rc = upload(&lu->d_P, S.P)) || (rc = upload(&lu->d_Q, S.Q)) ||
-      (rc = upload(&lu->d_arp, arp)) || (rc = upload(&lu->d_aci, aci)))
+      (rc = upload(&lu->d_arp, arp)) || (rc = upload(&lu->d_aci, aci)) ||
+      (rc = upload(&lu->d_urp, S.urp)) || (rc = upload(&lu->d_upos, S.upos)))
     return fail(rc);
+  const int64_t nup = S.urp[n];
+  std::vector<int> urp32;  // the row starts as int, for the level path
+  if (nup < (int64_t(1) << 31)) urp32.assign(S.urp.begin(), S.urp.end());
+  // the schedule lives on the device only
+  std::vector<int64_t>().swap(lu->S.urp);
+  std::vector<int>().swap(lu->S.upos);
   const size_t tsz = precision == XG_LU_FP32 ? sizeof(float) : sizeof(double);
   cudaError_t e = cudaSuccess;
   if ((e = cudaMalloc((void **)&lu->d_ctrl, sizeof(unsigned) * xg::C_N)) ||
@@ -774,7 +753,7 @@ extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const i
   lu->grid_solve = std::max(1, std::min(sms * 4, int((lu->nnz_lu + 255) / 256)));
   // one-CTA path when the factor (and the solve's extra vectors) fit in shared memory
   {
-    const size_t factor_b = xg::smem_bytes_seq(n, lu->nnz_lu, tsz);
+    const size_t factor_b = xg::smem_bytes(n, lu->nnz_lu, tsz);
     const size_t solve_b = factor_b;
     int max_optin = 0;
     cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, lu->device);
@@ -854,22 +833,27 @@ extern "C" int xg_lu_status(xg_lu *lu, int *status, int *bad_row) {
   return XG_OK;
 }
 
+static void fill_info(const xg::LuSymbolic &S, int precision, xg_lu_info *info) {
+  std::memset(info, 0, sizeof(*info));
+  info->n = S.n;
+  info->nnz_a = S.nnz_a;
+  info->nnz_lu = S.rp.empty() ? 0 : S.rp[S.n];
+  info->precision = precision;
+  info->levels = S.levels;
+  info->n_dense = S.n_dense;
+  info->refactor_flops = S.refactor_flops;
+  info->solve_flops = S.solve_flops;
+  info->min_pivot = S.min_pivot;
+  info->max_pivot = S.max_pivot;
+  info->ordering = S.ordering;
+}
+
 extern "C" int xg_lu_get_info(const xg_lu *lu, xg_lu_info *info) {
   if (!lu || !info) {
     xg::set_error("xg_lu_get_info: bad argument");
     return XG_ERR_ARG;
   }
-  std::memset(info, 0, sizeof(*info));
-  info->n = lu->S.n;
-  info->nnz_a = lu->S.nnz_a;
-  info->nnz_lu = lu->nnz_lu;
-  info->precision = lu->precision;
-  info->levels = lu->S.levels;
-  info->n_dense = lu->S.n_dense;
-  info->refactor_flops = lu->S.refactor_flops;
-  info->solve_flops = lu->S.solve_flops;
-  info->min_pivot = lu->S.min_pivot;
-  info->max_pivot = lu->S.max_pivot;
+  fill_info(lu->S, lu->precision, info);
   return XG_OK;
 }
 
@@ -907,7 +891,8 @@ extern "C" int xg_lu_order(int n, const int *host_rowptr, const int *host_colidx
 }
 
 extern "C" int xg_lu_analyze_host(int n, const int *host_rowptr, const int *host_colidx,
-                                  const double *host_values, int *P, int *Q, int64_t *nnz_lu) {
+                                  const double *host_values, int *P, int *Q, int64_t *nnz_lu,
+                                  xg_lu_info *info) {
   if (n <= 0 || !host_rowptr || !host_colidx || !host_values) {
     xg::set_error("xg_lu_analyze_host: bad argument");
     return XG_ERR_ARG;
@@ -921,5 +906,6 @@ extern "C" int xg_lu_analyze_host(int n, const int *host_rowptr, const int *host
   if (P) std::memcpy(P, S.P.data(), sizeof(int) * n);
   if (Q) std::memcpy(Q, S.Q.data(), sizeof(int) * n);
   if (nnz_lu) *nnz_lu = S.rp[n];
+  if (info) fill_info(S, XG_LU_FP64, info);
   return XG_OK;
 }

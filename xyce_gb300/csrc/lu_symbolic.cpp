@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <string>
 #include <vector>
 
@@ -168,14 +169,175 @@ std::vector<int> amd_order(int n, const int *rp, const int *ci, int *n_dense_out
   return order;
 }
 
-int lu_analyze(int n, const int *rp, const int *ci, const double *val, double pivot_tol,
-               LuSymbolic *out, std::string *err) {
+// Nested dissection by level-structure separators (A. George, "Nested
+// dissection of a regular finite element mesh", SIAM J. Numer. Anal. 10(2),
+// 1973; the automatic form of George and Liu, "Computer Solution of Large
+// Sparse Positive Definite Systems", 1981, ch. 8): a breadth-first level
+// structure from a pseudo-peripheral vertex, the smallest level near the
+// middle as separator (only its vertices with a neighbour in the next level),
+// the two sides ordered first, recursively, the separator after them.  Parts
+// of at most `leaf` vertices are ordered by minimum degree; disconnected
+// parts are split without a separator; dense vertices go last as in
+// amd_order.  The elimination tree is then about log2(n / leaf) separators
+// deep instead of following the long chains minimum degree leaves in
+// path-like circuits.
+std::vector<int> nd_order(int n, const int *rp, const int *ci, int leaf, int *n_dense_out) {
+  std::vector<int> ap(n + 1, 0), aj;
+  {
+    std::vector<std::vector<int>> adj(n);
+    for (int i = 0; i < n; ++i)
+      for (int p = rp[i]; p < rp[i + 1]; ++p) {
+        int j = ci[p];
+        if (j == i) continue;
+        adj[i].push_back(j);
+        adj[j].push_back(i);
+      }
+    for (int i = 0; i < n; ++i) {
+      auto &a = adj[i];
+      std::sort(a.begin(), a.end());
+      a.erase(std::unique(a.begin(), a.end()), a.end());
+      ap[i + 1] = ap[i] + int(a.size());
+    }
+    aj.reserve(ap[n]);
+    for (auto &a : adj) aj.insert(aj.end(), a.begin(), a.end());
+  }
+  const int dense = std::max(16, int(10.0 * std::sqrt(double(n))));
+  std::vector<char> is_dense(n, 0);
+  std::vector<int> dense_list, all;
+  for (int i = 0; i < n; ++i) {
+    if (ap[i + 1] - ap[i] > dense) { is_dense[i] = 1; dense_list.push_back(i); }
+    else all.push_back(i);
+  }
+  std::vector<int> order;
+  order.reserve(n);
+  std::vector<int> in_set(n, 0), level(n, -1), local(n, -1);
+  int stamp = 0;
+  // Work items: a vertex set to dissect, or a separator to emit.  Popping
+  // A's subtree before B's and the separator last gives a post-order.
+  struct Item { bool emit; std::vector<int> v; };
+  std::vector<Item> work;
+  work.push_back({false, std::move(all)});
+  std::vector<int> queue, counts;
+  auto bfs = [&](int root, int st, std::vector<int> &q) {
+    q.clear();
+    q.push_back(root);
+    level[root] = 0;
+    in_set[root] = -st;  // visited in this search
+    for (size_t h = 0; h < q.size(); ++h) {
+      int u = q[h];
+      for (int p = ap[u]; p < ap[u + 1]; ++p) {
+        int v = aj[p];
+        if (in_set[v] != st) continue;
+        in_set[v] = -st;
+        level[v] = level[u] + 1;
+        q.push_back(v);
+      }
+    }
+    for (int u : q) in_set[u] = st;  // restore membership
+  };
+  auto order_leaf = [&](const std::vector<int> &V) {
+    // minimum degree on the induced subgraph
+    const int m = int(V.size());
+    for (int k = 0; k < m; ++k) local[V[k]] = k;
+    std::vector<int> lp(m + 1, 0), lj;
+    for (int k = 0; k < m; ++k) {
+      int u = V[k];
+      for (int p = ap[u]; p < ap[u + 1]; ++p)
+        if (local[aj[p]] >= 0 && !is_dense[aj[p]]) lj.push_back(local[aj[p]]);
+      lp[k + 1] = int(lj.size());
+    }
+    std::vector<int> o = amd_order(m, lp.data(), lj.data(), nullptr);
+    for (int k : o) order.push_back(V[k]);
+    for (int u : V) local[u] = -1;
+  };
+  while (!work.empty()) {
+    Item it = std::move(work.back());
+    work.pop_back();
+    std::vector<int> &V = it.v;
+    if (it.emit) {
+      order.insert(order.end(), V.begin(), V.end());
+      continue;
+    }
+    if (int(V.size()) <= leaf) {
+      order_leaf(V);
+      continue;
+    }
+    const int st = ++stamp;
+    for (int u : V) in_set[u] = st;
+    // pseudo-peripheral root: restart from a least-degree vertex of the last
+    // level while the eccentricity grows
+    int root = V[0], ecc = -1;
+    for (int tries = 0; tries < 6; ++tries) {
+      bfs(root, st, queue);
+      int e = level[queue.back()];
+      if (e <= ecc) break;
+      ecc = e;
+      int best = queue.back(), bd = n + 1;
+      for (int k = int(queue.size()) - 1; k >= 0 && level[queue[k]] == e; --k) {
+        int d = ap[queue[k] + 1] - ap[queue[k]];
+        if (d < bd) { bd = d; best = queue[k]; }
+      }
+      if (tries < 5) root = best;
+    }
+    bfs(root, st, queue);
+    if (queue.size() < V.size()) {
+      // disconnected: this component and the rest are independent parts
+      std::vector<int> rest;
+      for (int u : V)
+        if (level[u] < 0) rest.push_back(u);
+      for (int u : V) level[u] = -1;
+      work.push_back({false, std::move(rest)});
+      work.push_back({false, queue});
+      continue;
+    }
+    const int h = level[queue.back()] + 1;
+    if (h < 3) {  // too shallow to split: a near-clique
+      for (int u : V) level[u] = -1;
+      order_leaf(V);
+      continue;
+    }
+    counts.assign(h, 0);
+    for (int u : V) counts[level[u]]++;
+    int mid = 0;
+    for (int c = 0, acc = 0; c < h; ++c) {
+      acc += counts[c];
+      if (2 * acc >= int(V.size())) { mid = c; break; }
+    }
+    int m = std::min(std::max(mid, 1), h - 2);
+    for (int c = std::max(1, mid - 2); c <= std::min(h - 2, mid + 2); ++c)
+      if (counts[c] < counts[m] || (counts[c] == counts[m] && std::abs(c - mid) < std::abs(m - mid)))
+        m = c;
+    std::vector<int> A, B, sep;
+    for (int u : V) {
+      int lu = level[u];
+      if (lu < m) { A.push_back(u); continue; }
+      if (lu > m) { B.push_back(u); continue; }
+      bool touches = false;
+      for (int p = ap[u]; p < ap[u + 1] && !touches; ++p)
+        touches = in_set[aj[p]] == st && level[aj[p]] == m + 1;
+      (touches ? sep : A).push_back(u);
+    }
+    for (int u : V) level[u] = -1;
+    work.push_back({true, std::move(sep)});
+    work.push_back({false, std::move(B)});
+    work.push_back({false, std::move(A)});
+  }
+  for (int i : dense_list) order.push_back(i);
+  if (n_dense_out) *n_dense_out = int(dense_list.size());
+  return order;
+}
+
+namespace {
+
+// The pivoting factorisation for a given column order.
+int analyze_ordered(int n, const int *rp, const int *ci, const double *val, double pivot_tol,
+                    std::vector<int> order, int n_dense, LuSymbolic *out, std::string *err) {
   LuSymbolic &S = *out;
   S = LuSymbolic();
   S.n = n;
   S.nnz_a = rp[n];
-  // column order
-  S.Q = amd_order(n, rp, ci, &S.n_dense);
+  S.Q = std::move(order);
+  S.n_dense = n_dense;
   std::vector<int> qinv(n);
   for (int j = 0; j < n; ++j) qinv[S.Q[j]] = j;
   // A by columns, remembering each entry's CSR index
@@ -344,6 +506,71 @@ int lu_analyze(int n, const int *rp, const int *ci, const double *val, double pi
   std::vector<int> width(S.levels + 1, 0);
   for (int i = 0; i < n; ++i) S.max_width = std::max(S.max_width, ++width[level[i]]);
   return 0;
+}
+
+}  // namespace
+
+int lu_analyze(int n, const int *rp, const int *ci, const double *val, double pivot_tol,
+               LuSymbolic *out, std::string *err, int ordering) {
+  const char *force = ordering >= 0 ? nullptr : std::getenv("XG_LU_ORDER");
+  const int forced = !force ? ordering
+                            : std::string(force) == "nd" ? 1 : std::string(force) == "amd" ? 0 : -1;
+  // (each order is computed before the call: its dense count is an argument)
+  auto with_nd = [&](LuSymbolic *dst, std::string *e) {
+    int nd_dense = 0;
+    std::vector<int> q = nd_order(n, rp, ci, kNdLeaf, &nd_dense);
+    if (analyze_ordered(n, rp, ci, val, pivot_tol, std::move(q), nd_dense, dst, e)) return -1;
+    dst->ordering = 1;
+    return 0;
+  };
+  if (forced == 1) return with_nd(out, err);
+  int amd_dense = 0;
+  std::vector<int> q = amd_order(n, rp, ci, &amd_dense);
+  if (analyze_ordered(n, rp, ci, val, pivot_tol, std::move(q), amd_dense, out, err)) return -1;
+  out->ordering = 0;
+  if (forced == 0 || out->levels <= kNdMinLevels) return 0;
+  // A long dependency chain: try nested dissection and keep it when the
+  // modelled refactorisation time is lower.
+  LuSymbolic nd;
+  std::string nd_err;
+  if (with_nd(&nd, &nd_err)) return 0;
+  if (lu_model_seconds(nd) < 0.8 * lu_model_seconds(*out)) *out = std::move(nd);
+  return 0;
+}
+
+bool lu_build_updates(LuSymbolic &S) {
+  const int n = S.n;
+  S.urp.assign(n + 1, 0);
+  for (int i = 0; i < n; ++i) {
+    int64_t c = 0;
+    for (int p = S.rp[i]; p < S.diag[i]; ++p) {
+      const int k = S.ci[p];
+      c += S.rp[k + 1] - S.diag[k] - 1;
+    }
+    S.urp[i + 1] = S.urp[i] + c;
+  }
+  S.upos.assign(size_t(S.urp[n]), 0);
+  std::vector<int> map(n, -1);
+  for (int i = 0; i < n; ++i) {
+    const int s = S.rp[i], e = S.rp[i + 1];
+    for (int p = s; p < e; ++p) map[S.ci[p]] = p;
+    int64_t u = S.urp[i];
+    for (int p = s; p < S.diag[i]; ++p) {
+      const int k = S.ci[p];
+      for (int q = S.diag[k] + 1; q < S.rp[k + 1]; ++q) {
+        const int pos = map[S.ci[q]];
+        if (pos <= p || pos >= e || S.ci[pos] != S.ci[q]) return false;
+        S.upos[size_t(u++)] = pos;
+      }
+    }
+    for (int p = s; p < e; ++p) map[S.ci[p]] = -1;
+  }
+  return true;
+}
+
+double lu_model_seconds(const LuSymbolic &S) {
+  // dependent steps cost a fixed latency each, independent work a rate
+  return S.levels * kLuLevelSeconds + S.refactor_flops * kLuFlopSeconds;
 }
 
 }  // namespace xg

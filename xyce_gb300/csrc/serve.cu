@@ -1023,7 +1023,9 @@ extern "C" int xg_batch_create(xg_ctx *ctx, int n, const xg_netlist *const *nls,
     }
     LuSymbolic S;
     std::string err;
-    if (lu_analyze(nr_, rp.data(), ci.data(), val.data(), 1e-3, &S, &err)) {
+    // one warp walks each request's rows in order: fewest operations wins,
+    // the dependency depth does not matter, so minimum degree
+    if (lu_analyze(nr_, rp.data(), ci.data(), val.data(), 1e-3, &S, &err, 0)) {
       set_error("xg_batch_create: request " + std::to_string(r) + ": " + err);
       return XG_ERR_SINGULAR;
     }

@@ -35,7 +35,28 @@ struct LuSymbolic {
   int max_width = 0;          // rows in the widest level of that chain
   int n_dense = 0;            // rows/columns ordered last as dense
   double min_pivot = 0, max_pivot = 0;  // |U(k,k)| range of the analysed matrix
+  int ordering = 0;           // column order: 0 minimum degree, 1 nested dissection
+  // Update schedule of the refactorisation (lu_build_updates): for row i, its
+  // L entries p in ascending column k, and for each the entries q of U row k
+  // right of the diagonal in ascending column, upos holds the position in
+  // row i that U(k, ci[q]) updates.  urp[i] is where row i's updates start.
+  std::vector<int64_t> urp;
+  std::vector<int> upos;
 };
+
+// Ordering choice: nested dissection is tried when minimum degree leaves a
+// dependency chain longer than kNdMinLevels rows; parts of at most kNdLeaf
+// vertices are ordered by minimum degree.  The refactorisation time model
+// charges kLuLevelSeconds per dependent level and kLuFlopSeconds per
+// multiply-add.
+constexpr int kNdMinLevels = 64;
+constexpr int kNdLeaf = 16;
+constexpr double kLuLevelSeconds = 2e-6;
+constexpr double kLuFlopSeconds = 2e-10;
+double lu_model_seconds(const LuSymbolic &S);
+
+// Nested-dissection order of the graph of A + A^T (diagonal ignored).
+std::vector<int> nd_order(int n, const int *rp, const int *ci, int leaf, int *n_dense);
 
 // Approximate minimum degree order of the graph of A + A^T (diagonal
 // ignored).  Returns the elimination order: order[k] = the k-th unknown.
@@ -43,10 +64,16 @@ std::vector<int> amd_order(int n, const int *rp, const int *ci, int *n_dense);
 
 // Ordering + pivoting factorisation of A (CSR, n x n) with threshold partial
 // pivoting (diagonal preferred when |a_diag| >= pivot_tol * max|column|).
+// ordering: 0 minimum degree, 1 nested dissection, -1 chooses (see
+// kNdMinLevels; XG_LU_ORDER=amd|nd in the environment overrides that choice).
 // Returns 0, or -1 with *err set when A is structurally or numerically
 // singular.
 int lu_analyze(int n, const int *rp, const int *ci, const double *val, double pivot_tol,
-               LuSymbolic *out, std::string *err);
+               LuSymbolic *out, std::string *err, int ordering = -1);
+
+// Fills S.urp and S.upos from the L\U pattern; false if an update falls
+// outside the pattern (cannot happen for a pattern lu_analyze made).
+bool lu_build_updates(LuSymbolic &S);
 
 // Device address of an LU's status word (bits as xg_lu_status reports), for
 // callers that read it back together with other results.

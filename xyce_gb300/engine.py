@@ -69,7 +69,7 @@ def lib():
     L.xg_lu_get_symbolic.argtypes = [vp, vp, vp, vp, vp]
     L.xg_lu_destroy.argtypes = [vp]
     L.xg_lu_order.argtypes = [i, vp, vp, vp, C.POINTER(i)]
-    L.xg_lu_analyze_host.argtypes = [i, vp, vp, vp, vp, vp, i64p]
+    L.xg_lu_analyze_host.argtypes = [i, vp, vp, vp, vp, vp, i64p, C.POINTER(abi.XgLuInfo)]
     L.xg_tran_run.argtypes = [vp, C.POINTER(abi.XgTranOptions), vp, i, vp, i, vp, vp,
                               C.POINTER(i), C.POINTER(abi.XgTranStats)]
     L.xg_batch_create.argtypes = [vp, i, vp, vp, vp, vp, C.POINTER(abi.XgBatchOptions),
@@ -289,16 +289,19 @@ class LU:
             pass
 
 
-def lu_analyze_host(rowptr, colidx, values):
-    """Host-only analysis: (P, Q, nnz of L\\U) of the CSR matrix."""
+def lu_analyze_host(rowptr, colidx, values, with_info=False):
+    """Host-only analysis: (P, Q, nnz of L\\U) of the CSR matrix, and its
+    XgLuInfo when with_info."""
     rp = np.ascontiguousarray(rowptr, dtype=np.int32)
     ci = np.ascontiguousarray(colidx, dtype=np.int32)
     v = np.ascontiguousarray(values, dtype=np.float64)
     n = rp.size - 1
     P, Q = np.zeros(n, np.int32), np.zeros(n, np.int32)
     nnz = C.c_int64()
-    check(lib().xg_lu_analyze_host(n, _ptr(rp), _ptr(ci), _ptr(v), _ptr(P), _ptr(Q), C.byref(nnz)))
-    return P, Q, nnz.value
+    info = abi.XgLuInfo()
+    check(lib().xg_lu_analyze_host(n, _ptr(rp), _ptr(ci), _ptr(v), _ptr(P), _ptr(Q), C.byref(nnz),
+                                   C.byref(info)))
+    return (P, Q, nnz.value, info) if with_info else (P, Q, nnz.value)
 
 
 def amd_order(rowptr, colidx):
