@@ -117,17 +117,22 @@ def test_full_size_power_grid_solve(gpu_ctx, oracle_lib):
     assert _backward_error(A, x32, b) <= 1e-13
 
 
-@pytest.mark.parametrize("case", ["inverter_chain_1000", "ring_oscillator_101"])
-def test_sequential_cta_and_grid_paths_agree(case, gpu_ctx, oracle_lib, monkeypatch):
-    """Narrow factors are walked by one lane, small ones run in one CTA out of
-    shared memory, the rest grid-wide; forcing each path on the same matrix
-    gives the same solution."""
+@pytest.mark.parametrize("order", ["amd", "nd"])
+@pytest.mark.parametrize("case", ["inverter_chain_1000", "ring_oscillator_101", "random_mos_3000"])
+def test_level_sequential_cta_and_grid_paths_agree(case, order, gpu_ctx, oracle_lib, monkeypatch):
+    """Small factors run level by level in one CTA (long trailing rows with
+    all threads); with that path off, narrow ones are walked by one lane,
+    other small ones run warp-per-row in one CTA, the rest grid-wide.
+    Forcing each path, under either column order, on the same matrix gives
+    the same solution."""
     nl = CASES[case]()
     A = circuit_jacobian(nl, seed=5)
     b = np.random.default_rng(11).standard_normal(A.shape[0])
     xs = []
-    for env in ({}, {"XG_LU_NO_SEQ": "1"}, {"XG_LU_NO_SEQ": "1", "XG_LU_NO_CTA": "1"}):
-        for k in ("XG_LU_NO_SEQ", "XG_LU_NO_CTA"):
+    monkeypatch.setenv("XG_LU_ORDER", order)
+    for env in ({}, {"XG_LU_NO_LVL": "1"}, {"XG_LU_NO_LVL": "1", "XG_LU_NO_SEQ": "1"},
+                {"XG_LU_NO_LVL": "1", "XG_LU_NO_SEQ": "1", "XG_LU_NO_CTA": "1"}):
+        for k in ("XG_LU_NO_LVL", "XG_LU_NO_SEQ", "XG_LU_NO_CTA"):
             monkeypatch.delenv(k, raising=False)
         for k, v in env.items():
             monkeypatch.setenv(k, v)

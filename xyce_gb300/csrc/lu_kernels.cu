@@ -551,6 +551,231 @@ __global__ void __launch_bounds__(kCtaThreads) lu_solve_cta(LuDev d, const T *__
   }
 }
 
+// ---- small matrices, level by level: one thread per row -------------------------
+// GB300 issues FP64 at two lanes per clock per SM, so an FP64 instruction
+// costs about the same whether one lane of the warp uses it or all 32.  The
+// warp-per-row kernels above leave most lanes idle on the short rows of
+// circuit matrices.  Here the rows of one dependency level (independent of
+// each other) go to different threads, the levels follow one another with a
+// block barrier, and everything the kernel reads sits in shared memory: the
+// values, the pattern, the update schedule and the level lists.  With a
+// nested-dissection order a chain of 1,000 inverters has ~22 levels.  The
+// trailing rows with long L parts (the tail, see LuSymbolic) are done after
+// the levels, one row at a time with all threads.
+
+struct LvlDev {
+  const int *lrow, *lptr, *urow, *uptr;  // rows by L level / by U level
+  const int *urp32;                      // update-schedule row starts (int)
+  const int *tail_rowg, *tail_gptr, *tail_pos, *tail_pp, *tail_pm, *tail_q;
+  int levels, ulevels, nup;
+  int tail0, ntail, ngroups, npos, npairs;
+};
+
+enum LvlOff { O_VAL, O_RD, O_Y, O_RED, O_CI, O_RP, O_DIAG, O_URP, O_UPOS, O_LROW, O_LPTR, O_UROW,
+              O_UPTR, O_TROWG, O_TGPTR, O_TPOS, O_TPP, O_TPM, O_TQ, O_END };
+
+// Shared-memory layout of the level kernels (the same function on host and
+// device).  The factor uses val, rd, the schedule and the tail; the solve
+// uses val, rd, y, the reduction scratch (one T per thread) and both level
+// lists.  The T arrays come first, each padded to 16 bytes.
+__host__ __device__ inline size_t lvl_layout(int n, int64_t nnz, const LvlDev &v, int threads,
+                                             size_t tsz, bool solve, size_t *off) {
+  auto a16 = [](size_t x) { return (x + 15) & ~size_t(15); };
+  const size_t I = sizeof(int);
+  size_t o = 0;
+  off[O_VAL] = o; o += a16(tsz * size_t(nnz));
+  off[O_RD] = o; o += a16(tsz * size_t(n));
+  off[O_Y] = o; o += solve ? a16(tsz * size_t(n)) : 0;
+  off[O_RED] = o; o += solve ? a16(tsz * size_t(threads)) : 0;
+  off[O_CI] = o; o += I * size_t(nnz);
+  off[O_RP] = o; o += I * size_t(n + 1);
+  off[O_DIAG] = o; o += I * size_t(n);
+  off[O_URP] = o; o += solve ? 0 : I * size_t(n + 1);
+  off[O_UPOS] = o; o += solve ? 0 : I * size_t(v.nup);
+  off[O_LROW] = o; o += I * size_t(v.tail0);
+  off[O_LPTR] = o; o += I * size_t(v.levels + 1);
+  off[O_UROW] = o; o += solve ? I * size_t(n) : 0;
+  off[O_UPTR] = o; o += solve ? I * size_t(v.ulevels + 1) : 0;
+  off[O_TROWG] = o; o += solve ? 0 : I * size_t(v.ntail + 1);
+  off[O_TGPTR] = o; o += solve ? 0 : I * size_t(v.ngroups + 1);
+  off[O_TPOS] = o; o += solve ? 0 : I * size_t(v.npos);
+  off[O_TPP] = o; o += solve ? 0 : I * size_t(v.npos + 1);
+  off[O_TPM] = o; o += solve ? 0 : I * size_t(v.npairs);
+  off[O_TQ] = o; o += solve ? 0 : I * size_t(v.npairs);
+  off[O_END] = o;
+  return o;
+}
+
+// A zero, infinite or NaN pivot, from the bits (no FP64 instruction).
+__device__ __forceinline__ bool bad_pivot(double u) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(u);
+  return (b << 1) == 0 || ((b >> 52) & 0x7ff) == 0x7ff;
+}
+__device__ __forceinline__ bool bad_pivot(float u) {
+  const unsigned b = __float_as_uint(u);
+  return (b << 1) == 0 || ((b >> 23) & 0xff) == 0xff;
+}
+
+__device__ __forceinline__ void stage_ints(int *dst, const int *src, int count) {
+  for (int i = threadIdx.x; i < count; i += blockDim.x) dst[i] = __ldg(src + i);
+}
+
+template <class T>
+__global__ void __launch_bounds__(1024) lu_factor_lvl(LuDev d, LvlDev v, const double *__restrict__ a,
+                                                      double *__restrict__ a_copy, int64_t nnz_a,
+                                                      T *__restrict__ val_out, int64_t nnz) {
+  extern __shared__ __align__(16) char smem[];
+  const int n = d.n;
+  size_t off[O_END + 1];
+  lvl_layout(n, nnz, v, blockDim.x, sizeof(T), false, off);
+  T *val = (T *)(smem + off[O_VAL]);
+  T *rd = (T *)(smem + off[O_RD]);
+  int *ci = (int *)(smem + off[O_CI]), *rp = (int *)(smem + off[O_RP]);
+  int *diag = (int *)(smem + off[O_DIAG]), *urp = (int *)(smem + off[O_URP]);
+  int *upos = (int *)(smem + off[O_UPOS]), *lrow = (int *)(smem + off[O_LROW]);
+  int *lptr = (int *)(smem + off[O_LPTR]);
+  int *trowg = (int *)(smem + off[O_TROWG]), *tgptr = (int *)(smem + off[O_TGPTR]);
+  int *tpos = (int *)(smem + off[O_TPOS]), *tpp = (int *)(smem + off[O_TPP]);
+  int *tpm = (int *)(smem + off[O_TPM]), *tq = (int *)(smem + off[O_TQ]);
+  if (threadIdx.x == 0) {
+    d.ctrl[C_EPOCH_F] += 1;
+    d.ctrl[C_STATUS] = 0;
+    d.ctrl[C_BAD_ROW] = 0xffffffffu;
+  }
+  for (int64_t p = threadIdx.x; p < nnz; p += blockDim.x) {
+    const int s = __ldg(d.lu2a + p);
+    val[p] = s >= 0 ? T(a[s]) : T(0);
+    ci[p] = __ldg(d.ci + p);
+  }
+  stage_ints(rp, d.rp, n + 1);
+  stage_ints(diag, d.diag, n);
+  stage_ints(urp, v.urp32, n + 1);
+  stage_ints(upos, d.upos, v.nup);
+  stage_ints(lrow, v.lrow, v.tail0);
+  stage_ints(lptr, v.lptr, v.levels + 1);
+  stage_ints(trowg, v.tail_rowg, v.ntail + 1);
+  stage_ints(tgptr, v.tail_gptr, v.ngroups + 1);
+  stage_ints(tpos, v.tail_pos, v.npos);
+  stage_ints(tpp, v.tail_pp, v.npos + 1);
+  stage_ints(tpm, v.tail_pm, v.npairs);
+  stage_ints(tq, v.tail_q, v.npairs);
+  if (a_copy != a)
+    for (int64_t p = threadIdx.x; p < nnz_a; p += blockDim.x) a_copy[p] = a[p];
+  __syncthreads();
+  unsigned bad = 0xffffffffu;
+  for (int lv = 0; lv < v.levels; ++lv) {
+    for (int t = lptr[lv] + threadIdx.x; t < lptr[lv + 1]; t += blockDim.x) {
+      const int i = lrow[t];
+      const int dp = diag[i];
+      int u = urp[i];
+      for (int p = rp[i]; p < dp; ++p) {
+        const int k = ci[p];
+        const T l = val[p] * rd[k];
+        val[p] = l;
+        const int q0 = diag[k] + 1, len = rp[k + 1] - q0;
+        for (int j = 0; j < len; ++j) val[upos[u + j]] -= l * val[q0 + j];
+        u += len;
+      }
+      const T piv = val[dp];
+      if (bad_pivot(piv)) bad = min(bad, unsigned(i));
+      rd[i] = recip(piv);
+    }
+    __syncthreads();
+  }
+  // the tail: each position pulls its updates, group after group
+  for (int r = 0; r < v.ntail; ++r) {
+    const int i = v.tail0 + r, dp = diag[i];
+    for (int g = trowg[r]; g < trowg[r + 1]; ++g) {
+      for (int t = tgptr[g] + threadIdx.x; t < tgptr[g + 1]; t += blockDim.x) {
+        const int p = tpos[t];
+        T acc = val[p];
+        for (int j = tpp[t]; j < tpp[t + 1]; ++j) acc -= val[tpm[j]] * val[tq[j]];
+        val[p] = p < dp ? acc * rd[ci[p]] : acc;
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      const T piv = val[dp];
+      if (bad_pivot(piv)) bad = min(bad, unsigned(i));
+      rd[i] = recip(piv);
+    }
+    __syncthreads();
+  }
+  if (bad != 0xffffffffu) {
+    atomicOr(&d.ctrl[C_STATUS], ST_PIVOT);
+    atomicMin(&d.ctrl[C_BAD_ROW], bad);
+  }
+  for (int64_t p = threadIdx.x; p < nnz; p += blockDim.x) val_out[p] = val[p];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) ((T *)d.rdiag)[i] = rd[i];
+}
+
+template <class T>
+__global__ void __launch_bounds__(1024) lu_solve_lvl(LuDev d, LvlDev v, const T *__restrict__ val_in,
+                                                     int64_t nnz, const double *__restrict__ b,
+                                                     double *__restrict__ x) {
+  extern __shared__ __align__(16) char smem[];
+  const int n = d.n;
+  size_t off[O_END + 1];
+  lvl_layout(n, nnz, v, blockDim.x, sizeof(T), true, off);
+  T *val = (T *)(smem + off[O_VAL]);
+  T *rd = (T *)(smem + off[O_RD]);
+  T *y = (T *)(smem + off[O_Y]);
+  T *red = (T *)(smem + off[O_RED]);
+  int *ci = (int *)(smem + off[O_CI]), *rp = (int *)(smem + off[O_RP]);
+  int *diag = (int *)(smem + off[O_DIAG]), *lrow = (int *)(smem + off[O_LROW]);
+  int *lptr = (int *)(smem + off[O_LPTR]), *urow = (int *)(smem + off[O_UROW]);
+  int *uptr = (int *)(smem + off[O_UPTR]);
+  for (int64_t p = threadIdx.x; p < nnz; p += blockDim.x) {
+    val[p] = val_in[p];
+    ci[p] = __ldg(d.ci + p);
+  }
+  stage_ints(rp, d.rp, n + 1);
+  stage_ints(diag, d.diag, n);
+  stage_ints(lrow, v.lrow, v.tail0);
+  stage_ints(lptr, v.lptr, v.levels + 1);
+  stage_ints(urow, v.urow, n);
+  stage_ints(uptr, v.uptr, v.ulevels + 1);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    rd[i] = ((const T *)d.rdiag)[i];
+    y[i] = T(b[__ldg(d.P + i)]);
+  }
+  __syncthreads();
+  // y = L \ b(P): the levels, then the tail rows as block-wide dot products
+  for (int lv = 0; lv < v.levels; ++lv) {
+    for (int t = lptr[lv] + threadIdx.x; t < lptr[lv + 1]; t += blockDim.x) {
+      const int i = lrow[t];
+      T acc = y[i];
+      for (int p = rp[i]; p < diag[i]; ++p) acc -= val[p] * y[ci[p]];
+      y[i] = acc;
+    }
+    __syncthreads();
+  }
+  for (int i = v.tail0; i < n; ++i) {
+    T part = T(0);
+    for (int p = rp[i] + threadIdx.x; p < diag[i]; p += blockDim.x) part += val[p] * y[ci[p]];
+    red[threadIdx.x] = part;
+    __syncthreads();
+    // fixed pairing: the same sum on every run (blockDim is a power of two)
+    for (int h = blockDim.x >> 1; h > 0; h >>= 1) {
+      if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) y[i] -= red[0];
+    __syncthreads();
+  }
+  // z = U \ y in place: a row reads only rows of lower U levels
+  for (int lv = 0; lv < v.ulevels; ++lv) {
+    for (int t = uptr[lv] + threadIdx.x; t < uptr[lv + 1]; t += blockDim.x) {
+      const int i = urow[t];
+      T acc = y[i];
+      for (int p = diag[i] + 1; p < rp[i + 1]; ++p) acc -= val[p] * y[ci[p]];
+      y[i] = acc * rd[i];
+    }
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < n; i += blockDim.x) x[__ldg(d.Q + i)] = double(y[i]);
+}
+
 }  // namespace
 }  // namespace xg
 
@@ -578,6 +803,11 @@ struct xg_lu {
   size_t smem_factor = 0, smem_solve = 0;  // > 0: the one-CTA path
   int cta_threads = 0;                     // its block size (warps ~ level width)
   bool narrow = false;                     // one lane walks the rows (<= 2 rows per level)
+  bool lvl = false;                        // level by level, one thread per row, in one CTA
+  size_t smem_lvl_factor = 0, smem_lvl_solve = 0;
+  int lvl_threads = 0;
+  int *d_lvl = nullptr;                    // level lists, row starts and tail, one buffer
+  xg::LvlDev lvl_dev{};
   bool factored = false;
   xg::LuDev dev() const {
     return xg::LuDev{S.n, d_rp, d_ci, d_diag, d_lu2a, d_P, d_Q, d_arp, d_aci, d_urp, d_upos,
@@ -607,7 +837,7 @@ int upload(V **dst, const std::vector<V> &src) {
 
 void free_lu(xg_lu *lu) {
   void *ptrs[] = {lu->d_rp, lu->d_ci, lu->d_diag, lu->d_lu2a, lu->d_P, lu->d_Q, lu->d_arp,
-                  lu->d_urp, lu->d_upos,
+                  lu->d_urp, lu->d_upos, lu->d_lvl,
                   lu->d_aci, lu->d_ctrl, lu->d_done, lu->d_val, lu->d_y, lu->d_z, lu->d_rdiag, lu->d_a,
                   lu->d_r, lu->d_dx};
   for (void *p : ptrs)
@@ -617,6 +847,13 @@ void free_lu(xg_lu *lu) {
 template <class T>
 int refactor_t(xg_lu *lu, const double *dev_values) {
   xg::LuDev d = lu->dev();
+  if (lu->lvl) {
+    xg::lu_factor_lvl<T><<<1, lu->lvl_threads, lu->smem_lvl_factor, lu->stream>>>(
+        d, lu->lvl_dev, dev_values, lu->d_a, lu->S.nnz_a, (T *)lu->d_val, lu->nnz_lu);
+    xg::count_launches(1);
+    XG_CU(cudaGetLastError());
+    return XG_OK;
+  }
   if (lu->narrow) {
     xg::lu_factor_seq<T><<<1, xg::kSeqThreads, lu->smem_factor, lu->stream>>>(
         d, dev_values, lu->d_a, lu->S.nnz_a, (T *)lu->d_val, lu->nnz_lu); xg::count_launches(1);
@@ -639,6 +876,13 @@ int refactor_t(xg_lu *lu, const double *dev_values) {
 template <class T>
 int solve_once(xg_lu *lu, const double *b, double *x) {
   xg::LuDev d = lu->dev();
+  if (lu->lvl) {
+    xg::lu_solve_lvl<T><<<1, lu->lvl_threads, lu->smem_lvl_solve, lu->stream>>>(
+        d, lu->lvl_dev, (const T *)lu->d_val, lu->nnz_lu, b, x);
+    xg::count_launches(1);
+    XG_CU(cudaGetLastError());
+    return XG_OK;
+  }
   if (lu->narrow) {
     xg::lu_solve_seq<T><<<1, xg::kSeqThreads, lu->smem_solve, lu->stream>>>(d, (const T *)lu->d_val, lu->nnz_lu,
                                                                b, x); xg::count_launches(1);
@@ -780,6 +1024,75 @@ extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const i
         lu->cta_threads = 32 * warps;
         // average rows per level: little parallelism -> the one-lane walk
         lu->narrow = double(n) / std::max(1, lu->S.levels) < 3.0 && !std::getenv("XG_LU_NO_SEQ");
+      } else {
+        cudaGetLastError();
+      }
+    }
+  }
+  // level-by-level path when its whole working set fits in shared memory and
+  // the levels hold several rows each (a chain of single rows is walked faster
+  // by the one lane of the narrow path)
+  if (!std::getenv("XG_LU_NO_LVL") && !lu->narrow && !urp32.empty() &&
+      lu->nnz_lu < (int64_t(1) << 31)) {
+    // lrow | lptr | urow | uptr | urp32 | tail_rowg | tail_gptr | tail_pos | tail_pp | tail_pm | tail_q
+    const std::vector<int> *parts[] = {&S.lrow, &S.lptr, &S.urow, &S.uptr, &urp32, &S.tail_rowg,
+                                       &S.tail_gptr, &S.tail_pos, &S.tail_pp, &S.tail_pm, &S.tail_q};
+    size_t start[11], total = 0;
+    for (int k = 0; k < 11; ++k) { start[k] = total; total += parts[k]->size(); }
+    xg::LvlDev v{};
+    v.levels = int(S.lptr.size()) - 1;
+    v.ulevels = int(S.uptr.size()) - 1;
+    v.nup = int(nup);
+    v.tail0 = S.tail0;
+    v.ntail = int(S.tail_rowg.size()) - 1;
+    v.ngroups = int(S.tail_gptr.size()) - 1;
+    v.npos = int(S.tail_pos.size());
+    v.npairs = int(S.tail_pm.size());
+    // threads: the widest level or tail group, in warps, 1 to 32
+    int maxw = 1;
+    for (int l = 0; l < v.levels; ++l) maxw = std::max(maxw, S.lptr[l + 1] - S.lptr[l]);
+    for (int l = 0; l < v.ulevels; ++l) maxw = std::max(maxw, S.uptr[l + 1] - S.uptr[l]);
+    for (int g = 0; g < v.ngroups; ++g) maxw = std::max(maxw, S.tail_gptr[g + 1] - S.tail_gptr[g]);
+    if (v.ntail > 0) maxw = std::max(maxw, 256);  // the tail's dot products
+    int threads = 32;
+    while (threads < maxw && threads < 1024) threads *= 2;  // a power of two: the reduction
+    size_t off[xg::O_END + 1];
+    const size_t fb = xg::lvl_layout(n, lu->nnz_lu, v, threads, tsz, false, off);
+    const size_t sb = xg::lvl_layout(n, lu->nnz_lu, v, threads, tsz, true, off);
+    int max_optin = 0;
+    cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, lu->device);
+    const size_t limit = size_t(max_optin) > 8192 ? size_t(max_optin) - 4096 : 0;
+    if (fb <= limit && sb <= limit) {
+      cudaError_t e1, e2;
+      if (precision == XG_LU_FP32) {
+        e1 = cudaFuncSetAttribute(xg::lu_factor_lvl<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(fb));
+        e2 = cudaFuncSetAttribute(xg::lu_solve_lvl<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sb));
+      } else {
+        e1 = cudaFuncSetAttribute(xg::lu_factor_lvl<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(fb));
+        e2 = cudaFuncSetAttribute(xg::lu_solve_lvl<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sb));
+      }
+      if (e1 == cudaSuccess && e2 == cudaSuccess) {
+        std::vector<int> buf;
+        buf.reserve(total);
+        for (auto *pv : parts) buf.insert(buf.end(), pv->begin(), pv->end());
+        if ((rc = upload(&lu->d_lvl, buf))) return fail(rc);
+        const int *b0 = lu->d_lvl;
+        v.lrow = b0 + start[0];
+        v.lptr = b0 + start[1];
+        v.urow = b0 + start[2];
+        v.uptr = b0 + start[3];
+        v.urp32 = b0 + start[4];
+        v.tail_rowg = b0 + start[5];
+        v.tail_gptr = b0 + start[6];
+        v.tail_pos = b0 + start[7];
+        v.tail_pp = b0 + start[8];
+        v.tail_pm = b0 + start[9];
+        v.tail_q = b0 + start[10];
+        lu->lvl_dev = v;
+        lu->lvl_threads = threads;
+        lu->smem_lvl_factor = fb;
+        lu->smem_lvl_solve = sb;
+        lu->lvl = true;
       } else {
         cudaGetLastError();
       }

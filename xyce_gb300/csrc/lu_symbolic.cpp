@@ -565,6 +565,79 @@ bool lu_build_updates(LuSymbolic &S) {
     }
     for (int p = s; p < e; ++p) map[S.ci[p]] = -1;
   }
+  // the tail: from the first row with a long L part among the last
+  // kTailMaxRows rows to the end
+  S.tail0 = n;
+  for (int i = std::max(0, n - kTailMaxRows); i < n; ++i)
+    if (S.diag[i] - S.rp[i] > kTailMinL) { S.tail0 = i; break; }
+  S.tail_rowg.assign(1, 0);
+  S.tail_gptr.assign(1, 0);
+  S.tail_pos.clear();
+  S.tail_pp.assign(1, 0);
+  S.tail_pm.clear();
+  S.tail_q.clear();
+  for (int i = S.tail0; i < n; ++i) {
+    const int s = S.rp[i], e = S.rp[i + 1], len = e - s;
+    std::vector<std::vector<std::pair<int, int>>> pulls(len);  // by target, pm ascending
+    int64_t u = S.urp[i];
+    for (int p = s; p < S.diag[i]; ++p) {
+      const int k = S.ci[p];
+      for (int q = S.diag[k] + 1; q < S.rp[k + 1]; ++q)
+        pulls[S.upos[size_t(u++)] - s].push_back({p, q});
+    }
+    std::vector<int> plev(len, 0);
+    int ng = 1;
+    for (int t = 0; t < len; ++t) {
+      int l = 0;
+      for (auto &pq : pulls[t]) l = std::max(l, plev[pq.first - s] + 1);
+      plev[t] = l;
+      ng = std::max(ng, l + 1);
+    }
+    std::vector<int> cnt(ng + 1, 0);
+    for (int t = 0; t < len; ++t) cnt[plev[t] + 1]++;
+    for (int g = 0; g < ng; ++g) cnt[g + 1] += cnt[g];
+    const int base = int(S.tail_pos.size());
+    S.tail_pos.resize(size_t(base + len));
+    std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+    for (int t = 0; t < len; ++t) S.tail_pos[size_t(base + fill[plev[t]]++)] = s + t;
+    for (int g = 0; g < ng; ++g) S.tail_gptr.push_back(base + cnt[g + 1]);
+    S.tail_rowg.push_back(int(S.tail_gptr.size()) - 1);
+    for (int t = base; t < base + len; ++t) {
+      for (auto &pq : pulls[S.tail_pos[size_t(t)] - s]) {
+        S.tail_pm.push_back(pq.first);
+        S.tail_q.push_back(pq.second);
+      }
+      S.tail_pp.push_back(int(S.tail_pm.size()));
+    }
+  }
+  // rows by level, ascending row within a level
+  auto group = [](const std::vector<int> &lev, int nlev, int nrows, std::vector<int> &rows,
+                  std::vector<int> &ptr) {
+    ptr.assign(nlev + 1, 0);
+    for (int i = 0; i < nrows; ++i) ptr[lev[i] + 1]++;
+    for (int l = 0; l < nlev; ++l) ptr[l + 1] += ptr[l];
+    rows.assign(nrows, 0);
+    std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+    for (int i = 0; i < nrows; ++i) rows[fill[lev[i]]++] = i;
+  };
+  std::vector<int> lev(n, 0);
+  int nlev = 0;
+  for (int i = 0; i < S.tail0; ++i) {
+    int l = 0;
+    for (int p = S.rp[i]; p < S.diag[i]; ++p) l = std::max(l, lev[S.ci[p]] + 1);
+    lev[i] = l;
+    nlev = std::max(nlev, l + 1);
+  }
+  group(lev, nlev, S.tail0, S.lrow, S.lptr);
+  // U levels, from the last row up: a row's U part names later rows only
+  nlev = 0;
+  for (int i = n - 1; i >= 0; --i) {
+    int l = 0;
+    for (int p = S.diag[i] + 1; p < S.rp[i + 1]; ++p) l = std::max(l, lev[S.ci[p]] + 1);
+    lev[i] = l;
+    nlev = std::max(nlev, l + 1);
+  }
+  group(lev, nlev, n, S.urow, S.uptr);
   return true;
 }
 

@@ -42,7 +42,28 @@ struct LuSymbolic {
   // row i that U(k, ci[q]) updates.  urp[i] is where row i's updates start.
   std::vector<int64_t> urp;
   std::vector<int> upos;
+  // Rows grouped by dependency level for the level-by-level kernels: lrow
+  // lists the rows of L level 0, 1, ... (a row's L level is one more than the
+  // highest of the rows its L part names), lptr[l] where level l starts;
+  // urow/uptr the same for the backward solve, by U level.
+  std::vector<int> lrow, lptr, urow, uptr;
+  // Trailing rows with long L parts (a supply rail ordered last has one L
+  // entry per device on it), and the rows after them, are left out of lrow:
+  // one thread would walk them serially.  They are factored one at a time after the levels, each with
+  // all threads: every position of the row pulls its updates (tail_pm[j] the
+  // row's own multiplier, tail_q[j] the U entry, in the order the row-wise
+  // elimination applies them), positions grouped so that a group reads only
+  // multipliers of earlier groups.  tail_pos lists the positions by group,
+  // tail_gptr[g] where group g starts, tail_rowg[r] the first group of row
+  // tail0 + r, tail_pp[t] where the pairs of tail_pos[t] start.
+  int tail0 = 0;
+  std::vector<int> tail_rowg, tail_gptr, tail_pos, tail_pp, tail_pm, tail_q;
 };
+
+// The tail starts at the first of the last kTailMaxRows rows with more than
+// kTailMinL L entries.
+constexpr int kTailMinL = 64;
+constexpr int kTailMaxRows = 16;
 
 // Ordering choice: nested dissection is tried when minimum degree leaves a
 // dependency chain longer than kNdMinLevels rows; parts of at most kNdLeaf
@@ -71,8 +92,9 @@ std::vector<int> amd_order(int n, const int *rp, const int *ci, int *n_dense);
 int lu_analyze(int n, const int *rp, const int *ci, const double *val, double pivot_tol,
                LuSymbolic *out, std::string *err, int ordering = -1);
 
-// Fills S.urp and S.upos from the L\U pattern; false if an update falls
-// outside the pattern (cannot happen for a pattern lu_analyze made).
+// Fills the update schedule (urp, upos), the level lists and the tail from
+// the L\U pattern; false if an update falls outside the pattern (cannot
+// happen for a pattern lu_analyze made).
 bool lu_build_updates(LuSymbolic &S);
 
 // Device address of an LU's status word (bits as xg_lu_status reports), for
