@@ -178,7 +178,10 @@ def run_tran(args, world, rank, local, dist):
     nl, guess, tstop, tstep, uic, out = build_tran(args.workload)
     prec = abi.LU_FP32 if args.fp32 else abi.LU_FP64
     nref = 2 if args.fp32 else 0
-    ctx = engine.Context(local, abi.device_options())
+    # the transient needs the load to the simulation's tolerance, not the
+    # reference's rounding: the FMA build (long sums split over a warp) unless
+    # --exact-load
+    ctx = engine.Context(local, abi.device_options(fma=0 if args.exact_load else 1))
     c = engine.Circuit(ctx, nl)
     x0 = _x0(nl, guess)
     stream = torch.cuda.ExternalStream(ctx.stream(), device=local)
@@ -235,6 +238,9 @@ def run_tran(args, world, rank, local, dist):
         "config": {"workload": args.workload, "tstop": tstop, "tstep": tstep, "unknowns": c.n_unknowns,
                    "nnz": c.nnz, "nnz_lu": info.nnz_lu, "lu_levels": info.levels,
                    "lu_precision": "fp32+2 refinement" if args.fp32 else "fp64",
+                   "lu_order": "nested dissection" if info.ordering == 1 else "minimum degree",
+                   "load_build": "exact (reference rounding)" if args.exact_load
+                   else "fma, long sums split over a warp",
                    "newton_iters_per_step": per_step_iters, "time_steps_per_step": st["steps"],
                    "l2": "working set below L2; latency-bound"},
         "roofline": {"kernel": "newton iteration", "bound": "hbm", "achieved": ach, "peak": hbm,
@@ -816,6 +822,8 @@ def main():
     ap.add_argument("--workload", default="single_load_bsim3_1M", choices=sorted(WORKLOADS))
     ap.add_argument("--fma", action="store_true")
     ap.add_argument("--fp32", action="store_true", help="transient: FP32 factors + FP64 refinement")
+    ap.add_argument("--exact-load", action="store_true",
+                    help="transient: the bit-exact load build instead of the FMA build")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args()
     world, rank, local, dist = dist_setup(args)

@@ -15,7 +15,7 @@ pytestmark = pytest.mark.gpu
 VTOL = 1e-3 * 1.8
 
 
-def _both(ctx, nl, x0, tstop, out, uic=False, precision=abi.LU_FP64, n_refine=0):
+def _both(ctx, nl, x0, tstop, out, uic=False, precision=abi.LU_FP64, n_refine=0, fma=0):
     from oracle.oracle import OracleCircuit, transient
     opt = abi.device_options()
     params = {t: engine.setup_params(nl, t, opt) for t in range(abi.NUM_DEV_TYPES) if nl.count(t)}
@@ -24,7 +24,7 @@ def _both(ctx, nl, x0, tstop, out, uic=False, precision=abi.LU_FP64, n_refine=0)
     xx = np.zeros(oc.n_unknowns)
     xx[:len(x0)] = x0
     tc, vc, sc = transient(oc, tstop, 1e-12, out, col_order=order, x0=xx, uic=uic)
-    ctx.set_options(opt)
+    ctx.set_options(abi.device_options(fma=fma))
     c = engine.Circuit(ctx, nl)
     tg, vg, sg = engine.transient(c, tstop, 1e-12, out, x0=xx, uic=uic, precision=precision,
                                   n_refine=n_refine)
@@ -42,11 +42,14 @@ def _agree(cpu, gpu):
     return err
 
 
-@pytest.mark.parametrize("precision,n_refine", [(abi.LU_FP64, 0), (abi.LU_FP32, 2)])
-def test_inverter_chain_waveforms(precision, n_refine, gpu_ctx, oracle_lib):
+@pytest.mark.parametrize("precision,n_refine,fma", [(abi.LU_FP64, 0, 0), (abi.LU_FP32, 2, 0),
+                                                    (abi.LU_FP64, 0, 1)])
+def test_inverter_chain_waveforms(precision, n_refine, fma, gpu_ctx, oracle_lib):
+    """fma=1: the FMA load build, whose supply-rail sums (one term per
+    device) are split over a warp."""
     stages = 100
     cpu, gpu = _both(gpu_ctx, netlists.inverter_chain(stages), netlists.inverter_chain_nodeset(stages),
-                     4e-9, [1, 2, 3, 50, stages + 1], precision=precision, n_refine=n_refine)
+                     4e-9, [1, 2, 3, 50, stages + 1], precision=precision, n_refine=n_refine, fma=fma)
     _agree(cpu, gpu)
     assert gpu[2]["newton_iters"] > 300
 

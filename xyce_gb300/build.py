@@ -64,7 +64,9 @@ def build_engine(verbose=False):
     for ns, fmad in (("exact", "false"), ("fast", "true")):
         src = os.path.join(CSRC, "load_kernels.cu")
         obj = os.path.join(BUILD, f"load_kernels_{ns}.o")
-        jobs.append((obj, [src] + heads, cu_common + [f"-DXG_NS={ns}", f"-fmad={fmad}", "-c", src, "-o", obj]))
+        split = "1" if ns == "fast" else "0"
+        jobs.append((obj, [src] + heads, cu_common + [f"-DXG_NS={ns}", f"-DXG_SPLIT_SUMS={split}",
+                                                      f"-fmad={fmad}", "-c", src, "-o", obj]))
     for f in sorted(os.listdir(CSRC)):
         src = os.path.join(CSRC, f)
         if f.endswith(".cu") and f != "load_kernels.cu":

@@ -11,6 +11,12 @@
 // This file is compiled twice: with -fmad=false into namespace xg::exact (each
 // product and sum rounded on its own, as the serial CPU load does) and with
 // -fmad=true into xg::fast (contracted to FMA).  XG_NS names the namespace.
+// The fast build also splits each long output (a supply rail collects a term
+// from every device on it) over the 32 lanes of a warp, each lane summing
+// every 32nd term in order, and adds the lane sums in a fixed butterfly: a
+// serial chain of dependent FP64 adds is the slowest thing a GB300 can be
+// asked to do.  The result is the same on every run, but not the reference's
+// rounding, which the exact build keeps.
 
 #include <cuda_runtime.h>
 
@@ -22,6 +28,9 @@
 
 #ifndef XG_NS
 #error "compile with -DXG_NS=exact or -DXG_NS=fast"
+#endif
+#ifndef XG_SPLIT_SUMS
+#define XG_SPLIT_SUMS 0
 #endif
 
 namespace xg {
@@ -695,6 +704,14 @@ __global__ void __launch_bounds__(kRedThreads) reduce_kernel(ReduceArgs a, int l
          w += (int64_t)long_blocks * kRedWarps) {
       const int64_t o = a.long_out[w];
       const int64_t b = __ldg(a.red_ptr + o), e = __ldg(a.red_ptr + o + 1);
+#if XG_SPLIT_SUMS
+      double s = 0.0;
+      for (int64_t j = b + lane; j < e; j += 32)
+        s += __ldg(a.terms + (a.red_idx ? (int64_t)__ldg(a.red_idx + j) : j));
+#pragma unroll
+      for (int m = 16; m > 0; m >>= 1) s += __shfl_xor_sync(0xffffffffu, s, m);
+      if (lane == 0) a.out[o] = s;
+#else
       double s = 0.0;
       for (int64_t base = b; base < e; base += kRedChunk) {
         const int cnt = (int)(e - base < kRedChunk ? e - base : kRedChunk);
@@ -706,6 +723,7 @@ __global__ void __launch_bounds__(kRedThreads) reduce_kernel(ReduceArgs a, int l
         __syncwarp();
       }
       if (lane == 0) a.out[o] = s;
+#endif
     }
     return;
   }

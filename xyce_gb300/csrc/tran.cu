@@ -106,11 +106,15 @@ __global__ void tran_weights(int n, const double *xc, const double *x, double re
 }
 
 // x += dx; optionally refresh the weights from the updated x (DC); partial
-// sums of (dx / w)^2.
+// sums of (dx / w)^2.  Also copies the LU status word behind the partials, so
+// one read brings both back.
 __global__ void __launch_bounds__(kThreads) tran_update(int n, const double *dx, double *x,
                                                         const double *xc, int reweight, double rel,
-                                                        double abs_tol, double *w, double *partials) {
+                                                        double abs_tol, double *w, double *partials,
+                                                        const unsigned *lu_status) {
   __shared__ double sh[kThreads];
+  if (blockIdx.x == 0 && threadIdx.x == 0)
+    *reinterpret_cast<unsigned *>(partials + P_N * kRedBlocks) = *lu_status;
   double s2 = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     double xi = x[i] + dx[i];
@@ -216,19 +220,20 @@ struct Run {
   }
   // read back the partials of the given kinds (and the LU status word when
   // asked) with one synchronisation, and reduce them in block order
+  // (the status word is the one tran_update copied behind the partials)
   int reduce(std::initializer_list<int> kinds, double *out, unsigned *lu_status = nullptr) {
+    int k0 = P_N, k1 = 0;
     for (int k : kinds) {
-      cudaError_t e = cudaMemcpyAsync(h_part + k * kRedBlocks, partials + k * kRedBlocks,
-                                      sizeof(double) * kRedBlocks, cudaMemcpyDeviceToHost, s);
-      if (e != cudaSuccess) return fail_cuda(e, "partials");
+      k0 = std::min(k0, k);
+      k1 = std::max(k1, k + 1);
     }
+    if (lu_status) k1 = P_N;
+    const size_t count = size_t(k1 - k0) * kRedBlocks + (lu_status ? 1 : 0);
+    cudaError_t e = cudaMemcpyAsync(h_part + k0 * kRedBlocks, partials + k0 * kRedBlocks,
+                                    sizeof(double) * count, cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) return fail_cuda(e, "partials");
     unsigned *h_status = reinterpret_cast<unsigned *>(h_part + P_N * kRedBlocks);
-    if (lu_status) {
-      cudaError_t e = cudaMemcpyAsync(h_status, lu_status_device(lu), sizeof(unsigned),
-                                      cudaMemcpyDeviceToHost, s);
-      if (e != cudaSuccess) return fail_cuda(e, "status");
-    }
-    cudaError_t e = cudaStreamSynchronize(s);
+    e = cudaStreamSynchronize(s);
     if (lu_status) *lu_status = *h_status;
     if (e != cudaSuccess) return fail_cuda(e, "stream");
     for (int k : kinds) {
@@ -349,7 +354,8 @@ struct Run {
       if ((*rc = xg_lu_refactor(lu, jac))) return 0;
       if ((*rc = xg_lu_solve(lu, rhs, dx, o->n_refine))) return 0;
       tran_update<<<kRedBlocks, kThreads, 0, s>>>(n, dx, x, xc, !transient, rel_tol, abs_tol, w,
-                                                  partials); xg::count_launches(1);
+                                                  partials, lu_status_device(lu));
+      xg::count_launches(1);
       fl.newton_iter = step;
       fl.init_jct = 0;
       fl.init_fix = !transient && st->dcop_solves == 0 && any_limit;
@@ -457,7 +463,7 @@ extern "C" int xg_tran_run(xg_circuit *c, const xg_tran_options *o, const double
   double **bufs[] = {&R.rhs, &R.dx, &R.w, &R.xh0, &R.xh1, &R.xh2, &R.qh0, &R.qh1, &R.qh2, &R.xn0};
   for (double **b : bufs) TRY_CUDA(cudaMalloc((void **)b, sizeof(double) * nr));
   TRY_CUDA(cudaMalloc((void **)&R.jac, sizeof(double) * std::max<int64_t>(R.nnz, 1)));
-  TRY_CUDA(cudaMalloc((void **)&R.partials, sizeof(double) * P_N * kRedBlocks));
+  TRY_CUDA(cudaMalloc((void **)&R.partials, sizeof(double) * (P_N * kRedBlocks + 1)));
   TRY_CUDA(cudaMallocHost((void **)&R.h_part, sizeof(double) * (P_N * kRedBlocks + 1)));
   TRY_CUDA(cudaMalloc((void **)&R.diag, sizeof(int64_t) * nr));
   TRY_CUDA(cudaMalloc((void **)&d_rec, sizeof(double) * std::max(1, n_out) * (size_t)max_points));
