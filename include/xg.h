@@ -283,6 +283,11 @@ int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const int *host_co
                   const double *host_values, int precision, xg_lu **out);
 int xg_lu_refactor(xg_lu *lu, const double *dev_values);
 int xg_lu_solve(xg_lu *lu, const double *dev_b, double *dev_x, int n_refine);
+/* xg_lu_refactor followed by xg_lu_solve, one Newton step's linear algebra
+ * (NumericFactorization then Solve, N_LAS_AmesosSolver.C:405-444); small
+ * factors do both in one launch from one staging of the factor. */
+int xg_lu_refactor_solve(xg_lu *lu, const double *dev_values, const double *dev_b, double *dev_x,
+                         int n_refine);
 int xg_lu_status(xg_lu *lu, int *status, int *bad_row);
 int xg_lu_get_info(const xg_lu *lu, xg_lu_info *info);
 /* host copies of the analysis: P, Q (n each), L\U row pointers (n+1), columns (nnz_lu) */

@@ -142,3 +142,29 @@ def test_level_sequential_cta_and_grid_paths_agree(case, order, gpu_ctx, oracle_
         xs.append(x)
     for x in xs[1:]:
         assert np.abs(x - xs[0]).max() <= 1e-12 * np.abs(xs[0]).max()
+
+
+@pytest.mark.parametrize("case", ["inverter_chain_1000", "ring_oscillator_101", "power_grid_60x60"])
+def test_fused_refactor_solve_matches_separate_calls(case, gpu_ctx, oracle_lib):
+    """xg_lu_refactor_solve (one launch for small factors) gives the same
+    factor and solution as xg_lu_refactor then xg_lu_solve."""
+    import torch
+    nl = CASES[case]()
+    A0 = circuit_jacobian(nl, seed=4)
+    A = circuit_jacobian(nl, seed=5)
+    b = torch.from_numpy(np.random.default_rng(12).standard_normal(A.shape[0])).cuda()
+    vals = torch.from_numpy(A.data.copy()).cuda()
+    xs = []
+    for fused in (False, True):
+        lu = engine.LU(gpu_ctx, A0.indptr, A0.indices, A0.data, abi.LU_FP64)
+        x = torch.zeros_like(b)
+        if fused:
+            lu.refactor_solve(vals.data_ptr(), b.data_ptr(), x.data_ptr())
+        else:
+            lu.refactor(vals.data_ptr())
+            lu.solve(b.data_ptr(), x.data_ptr(), 0)
+        assert lu.status() == (0, -1)
+        xs.append(x.cpu().numpy())
+        lu.close()
+    assert np.array_equal(xs[0], xs[1])
+    assert _backward_error(A, xs[1], b.cpu().numpy()) <= 1e-13

@@ -561,7 +561,9 @@ __global__ void __launch_bounds__(kCtaThreads) lu_solve_cta(LuDev d, const T *__
 // values, the pattern, the update schedule and the level lists.  With a
 // nested-dissection order a chain of 1,000 inverters has ~22 levels.  The
 // trailing rows with long L parts (the tail, see LuSymbolic) are done after
-// the levels, one row at a time with all threads.
+// the levels, one row at a time with all threads.  A Newton step refactors
+// and then solves: lu_factor_solve_lvl does both from one staging of the
+// shared-memory working set.
 
 struct LvlDev {
   const int *lrow, *lptr, *urow, *uptr;  // rows by L level / by U level
@@ -573,35 +575,37 @@ struct LvlDev {
 
 enum LvlOff { O_VAL, O_RD, O_Y, O_RED, O_CI, O_RP, O_DIAG, O_URP, O_UPOS, O_LROW, O_LPTR, O_UROW,
               O_UPTR, O_TROWG, O_TGPTR, O_TPOS, O_TPP, O_TPM, O_TQ, O_END };
+enum LvlMode { LVL_FACTOR = 1, LVL_SOLVE = 2, LVL_BOTH = 3 };
 
 // Shared-memory layout of the level kernels (the same function on host and
 // device).  The factor uses val, rd, the schedule and the tail; the solve
 // uses val, rd, y, the reduction scratch (one T per thread) and both level
 // lists.  The T arrays come first, each padded to 16 bytes.
 __host__ __device__ inline size_t lvl_layout(int n, int64_t nnz, const LvlDev &v, int threads,
-                                             size_t tsz, bool solve, size_t *off) {
+                                             size_t tsz, int mode, size_t *off) {
   auto a16 = [](size_t x) { return (x + 15) & ~size_t(15); };
   const size_t I = sizeof(int);
+  const bool f = mode & LVL_FACTOR, sv = mode & LVL_SOLVE;
   size_t o = 0;
   off[O_VAL] = o; o += a16(tsz * size_t(nnz));
   off[O_RD] = o; o += a16(tsz * size_t(n));
-  off[O_Y] = o; o += solve ? a16(tsz * size_t(n)) : 0;
-  off[O_RED] = o; o += solve ? a16(tsz * size_t(threads)) : 0;
+  off[O_Y] = o; o += sv ? a16(tsz * size_t(n)) : 0;
+  off[O_RED] = o; o += sv ? a16(tsz * size_t(threads)) : 0;
   off[O_CI] = o; o += I * size_t(nnz);
   off[O_RP] = o; o += I * size_t(n + 1);
   off[O_DIAG] = o; o += I * size_t(n);
-  off[O_URP] = o; o += solve ? 0 : I * size_t(n + 1);
-  off[O_UPOS] = o; o += solve ? 0 : I * size_t(v.nup);
+  off[O_URP] = o; o += f ? I * size_t(n + 1) : 0;
+  off[O_UPOS] = o; o += f ? I * size_t(v.nup) : 0;
   off[O_LROW] = o; o += I * size_t(v.tail0);
   off[O_LPTR] = o; o += I * size_t(v.levels + 1);
-  off[O_UROW] = o; o += solve ? I * size_t(n) : 0;
-  off[O_UPTR] = o; o += solve ? I * size_t(v.ulevels + 1) : 0;
-  off[O_TROWG] = o; o += solve ? 0 : I * size_t(v.ntail + 1);
-  off[O_TGPTR] = o; o += solve ? 0 : I * size_t(v.ngroups + 1);
-  off[O_TPOS] = o; o += solve ? 0 : I * size_t(v.npos);
-  off[O_TPP] = o; o += solve ? 0 : I * size_t(v.npos + 1);
-  off[O_TPM] = o; o += solve ? 0 : I * size_t(v.npairs);
-  off[O_TQ] = o; o += solve ? 0 : I * size_t(v.npairs);
+  off[O_UROW] = o; o += sv ? I * size_t(n) : 0;
+  off[O_UPTR] = o; o += sv ? I * size_t(v.ulevels + 1) : 0;
+  off[O_TROWG] = o; o += f ? I * size_t(v.ntail + 1) : 0;
+  off[O_TGPTR] = o; o += f ? I * size_t(v.ngroups + 1) : 0;
+  off[O_TPOS] = o; o += f ? I * size_t(v.npos) : 0;
+  off[O_TPP] = o; o += f ? I * size_t(v.npos + 1) : 0;
+  off[O_TPM] = o; o += f ? I * size_t(v.npairs) : 0;
+  off[O_TQ] = o; o += f ? I * size_t(v.npairs) : 0;
   off[O_END] = o;
   return o;
 }
@@ -616,56 +620,103 @@ __device__ __forceinline__ bool bad_pivot(float u) {
   return (b << 1) == 0 || ((b >> 23) & 0xff) == 0xff;
 }
 
-__device__ __forceinline__ void stage_ints(int *dst, const int *src, int count) {
-  for (int i = threadIdx.x; i < count; i += blockDim.x) dst[i] = __ldg(src + i);
+// Copies count ints into shared memory, four loads in flight per thread.
+__device__ __forceinline__ void stage_ints(int *dst, const int *__restrict__ src, int count) {
+  const int T = blockDim.x;
+  int i = threadIdx.x;
+  for (; i + 3 * T < count; i += 4 * T) {
+    const int a0 = __ldg(src + i), a1 = __ldg(src + i + T), a2 = __ldg(src + i + 2 * T),
+              a3 = __ldg(src + i + 3 * T);
+    dst[i] = a0;
+    dst[i + T] = a1;
+    dst[i + 2 * T] = a2;
+    dst[i + 3 * T] = a3;
+  }
+  for (; i < count; i += T) dst[i] = __ldg(src + i);
 }
 
 template <class T>
-__global__ void __launch_bounds__(1024) lu_factor_lvl(LuDev d, LvlDev v, const double *__restrict__ a,
-                                                      double *__restrict__ a_copy, int64_t nnz_a,
-                                                      T *__restrict__ val_out, int64_t nnz) {
-  extern __shared__ __align__(16) char smem[];
-  const int n = d.n;
+struct LvlSmem {
+  T *val, *rd, *y, *red;
+  int *ci, *rp, *diag, *urp, *upos, *lrow, *lptr, *urow, *uptr;
+  int *trowg, *tgptr, *tpos, *tpp, *tpm, *tq;
+};
+
+template <class T>
+__device__ LvlSmem<T> lvl_smem(char *smem, int n, int64_t nnz, const LvlDev &v, int mode) {
   size_t off[O_END + 1];
-  lvl_layout(n, nnz, v, blockDim.x, sizeof(T), false, off);
-  T *val = (T *)(smem + off[O_VAL]);
-  T *rd = (T *)(smem + off[O_RD]);
-  int *ci = (int *)(smem + off[O_CI]), *rp = (int *)(smem + off[O_RP]);
-  int *diag = (int *)(smem + off[O_DIAG]), *urp = (int *)(smem + off[O_URP]);
-  int *upos = (int *)(smem + off[O_UPOS]), *lrow = (int *)(smem + off[O_LROW]);
-  int *lptr = (int *)(smem + off[O_LPTR]);
-  int *trowg = (int *)(smem + off[O_TROWG]), *tgptr = (int *)(smem + off[O_TGPTR]);
-  int *tpos = (int *)(smem + off[O_TPOS]), *tpp = (int *)(smem + off[O_TPP]);
-  int *tpm = (int *)(smem + off[O_TPM]), *tq = (int *)(smem + off[O_TQ]);
-  if (threadIdx.x == 0) {
-    d.ctrl[C_EPOCH_F] += 1;
-    d.ctrl[C_STATUS] = 0;
-    d.ctrl[C_BAD_ROW] = 0xffffffffu;
+  lvl_layout(n, nnz, v, blockDim.x, sizeof(T), mode, off);
+  LvlSmem<T> m;
+  m.val = (T *)(smem + off[O_VAL]);
+  m.rd = (T *)(smem + off[O_RD]);
+  m.y = (T *)(smem + off[O_Y]);
+  m.red = (T *)(smem + off[O_RED]);
+  m.ci = (int *)(smem + off[O_CI]);
+  m.rp = (int *)(smem + off[O_RP]);
+  m.diag = (int *)(smem + off[O_DIAG]);
+  m.urp = (int *)(smem + off[O_URP]);
+  m.upos = (int *)(smem + off[O_UPOS]);
+  m.lrow = (int *)(smem + off[O_LROW]);
+  m.lptr = (int *)(smem + off[O_LPTR]);
+  m.urow = (int *)(smem + off[O_UROW]);
+  m.uptr = (int *)(smem + off[O_UPTR]);
+  m.trowg = (int *)(smem + off[O_TROWG]);
+  m.tgptr = (int *)(smem + off[O_TGPTR]);
+  m.tpos = (int *)(smem + off[O_TPOS]);
+  m.tpp = (int *)(smem + off[O_TPP]);
+  m.tpm = (int *)(smem + off[O_TPM]);
+  m.tq = (int *)(smem + off[O_TQ]);
+  return m;
+}
+
+// Stage what `mode` needs.  The factor scatters A into the L\U positions and
+// keeps the FP64 copy of A the refinement uses; the solve takes the factor's
+// values, or (LVL_BOTH) keeps them in place.
+template <class T>
+__device__ void lvl_stage(const LuDev &d, const LvlDev &v, const LvlSmem<T> &m, int mode,
+                          const double *__restrict__ a, double *__restrict__ a_copy, int64_t nnz_a,
+                          const T *__restrict__ val_in, int64_t nnz, const double *__restrict__ b) {
+  const int n = d.n;
+  if (mode & LVL_FACTOR) {
+    for (int64_t p = threadIdx.x; p < nnz; p += blockDim.x) {
+      const int s = __ldg(d.lu2a + p);
+      m.val[p] = s >= 0 ? T(a[s]) : T(0);
+    }
+    if (a_copy != a)
+      for (int64_t p = threadIdx.x; p < nnz_a; p += blockDim.x) a_copy[p] = a[p];
+    stage_ints(m.urp, v.urp32, n + 1);
+    stage_ints(m.upos, d.upos, v.nup);
+    stage_ints(m.trowg, v.tail_rowg, v.ntail + 1);
+    stage_ints(m.tgptr, v.tail_gptr, v.ngroups + 1);
+    stage_ints(m.tpos, v.tail_pos, v.npos);
+    stage_ints(m.tpp, v.tail_pp, v.npos + 1);
+    stage_ints(m.tpm, v.tail_pm, v.npairs);
+    stage_ints(m.tq, v.tail_q, v.npairs);
+  } else {
+    for (int64_t p = threadIdx.x; p < nnz; p += blockDim.x) m.val[p] = val_in[p];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) m.rd[i] = ((const T *)d.rdiag)[i];
   }
-  for (int64_t p = threadIdx.x; p < nnz; p += blockDim.x) {
-    const int s = __ldg(d.lu2a + p);
-    val[p] = s >= 0 ? T(a[s]) : T(0);
-    ci[p] = __ldg(d.ci + p);
+  stage_ints(m.ci, d.ci, int(nnz));
+  stage_ints(m.rp, d.rp, n + 1);
+  stage_ints(m.diag, d.diag, n);
+  stage_ints(m.lrow, v.lrow, v.tail0);
+  stage_ints(m.lptr, v.lptr, v.levels + 1);
+  if (mode & LVL_SOLVE) {
+    stage_ints(m.urow, v.urow, n);
+    stage_ints(m.uptr, v.uptr, v.ulevels + 1);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) m.y[i] = T(b[__ldg(d.P + i)]);
   }
-  stage_ints(rp, d.rp, n + 1);
-  stage_ints(diag, d.diag, n);
-  stage_ints(urp, v.urp32, n + 1);
-  stage_ints(upos, d.upos, v.nup);
-  stage_ints(lrow, v.lrow, v.tail0);
-  stage_ints(lptr, v.lptr, v.levels + 1);
-  stage_ints(trowg, v.tail_rowg, v.ntail + 1);
-  stage_ints(tgptr, v.tail_gptr, v.ngroups + 1);
-  stage_ints(tpos, v.tail_pos, v.npos);
-  stage_ints(tpp, v.tail_pp, v.npos + 1);
-  stage_ints(tpm, v.tail_pm, v.npairs);
-  stage_ints(tq, v.tail_q, v.npairs);
-  if (a_copy != a)
-    for (int64_t p = threadIdx.x; p < nnz_a; p += blockDim.x) a_copy[p] = a[p];
-  __syncthreads();
+}
+
+// The factorisation in shared memory; ends with a barrier.
+template <class T>
+__device__ void lvl_factor(const LuDev &d, const LvlDev &v, const LvlSmem<T> &m) {
+  T *val = m.val, *rd = m.rd;
+  const int *ci = m.ci, *rp = m.rp, *diag = m.diag, *urp = m.urp, *upos = m.upos;
   unsigned bad = 0xffffffffu;
   for (int lv = 0; lv < v.levels; ++lv) {
-    for (int t = lptr[lv] + threadIdx.x; t < lptr[lv + 1]; t += blockDim.x) {
-      const int i = lrow[t];
+    for (int t = m.lptr[lv] + threadIdx.x; t < m.lptr[lv + 1]; t += blockDim.x) {
+      const int i = m.lrow[t];
       const int dp = diag[i];
       int u = urp[i];
       for (int p = rp[i]; p < dp; ++p) {
@@ -685,11 +736,11 @@ __global__ void __launch_bounds__(1024) lu_factor_lvl(LuDev d, LvlDev v, const d
   // the tail: each position pulls its updates, group after group
   for (int r = 0; r < v.ntail; ++r) {
     const int i = v.tail0 + r, dp = diag[i];
-    for (int g = trowg[r]; g < trowg[r + 1]; ++g) {
-      for (int t = tgptr[g] + threadIdx.x; t < tgptr[g + 1]; t += blockDim.x) {
-        const int p = tpos[t];
+    for (int g = m.trowg[r]; g < m.trowg[r + 1]; ++g) {
+      for (int t = m.tgptr[g] + threadIdx.x; t < m.tgptr[g + 1]; t += blockDim.x) {
+        const int p = m.tpos[t];
         T acc = val[p];
-        for (int j = tpp[t]; j < tpp[t + 1]; ++j) acc -= val[tpm[j]] * val[tq[j]];
+        for (int j = m.tpp[t]; j < m.tpp[t + 1]; ++j) acc -= val[m.tpm[j]] * val[m.tq[j]];
         val[p] = p < dp ? acc * rd[ci[p]] : acc;
       }
       __syncthreads();
@@ -705,45 +756,20 @@ __global__ void __launch_bounds__(1024) lu_factor_lvl(LuDev d, LvlDev v, const d
     atomicOr(&d.ctrl[C_STATUS], ST_PIVOT);
     atomicMin(&d.ctrl[C_BAD_ROW], bad);
   }
-  for (int64_t p = threadIdx.x; p < nnz; p += blockDim.x) val_out[p] = val[p];
-  for (int i = threadIdx.x; i < n; i += blockDim.x) ((T *)d.rdiag)[i] = rd[i];
 }
 
+// x(Q) = U \ (L \ b(P)) in shared memory (y staged from b).
 template <class T>
-__global__ void __launch_bounds__(1024) lu_solve_lvl(LuDev d, LvlDev v, const T *__restrict__ val_in,
-                                                     int64_t nnz, const double *__restrict__ b,
-                                                     double *__restrict__ x) {
-  extern __shared__ __align__(16) char smem[];
+__device__ void lvl_solve(const LuDev &d, const LvlDev &v, const LvlSmem<T> &m,
+                          double *__restrict__ x) {
   const int n = d.n;
-  size_t off[O_END + 1];
-  lvl_layout(n, nnz, v, blockDim.x, sizeof(T), true, off);
-  T *val = (T *)(smem + off[O_VAL]);
-  T *rd = (T *)(smem + off[O_RD]);
-  T *y = (T *)(smem + off[O_Y]);
-  T *red = (T *)(smem + off[O_RED]);
-  int *ci = (int *)(smem + off[O_CI]), *rp = (int *)(smem + off[O_RP]);
-  int *diag = (int *)(smem + off[O_DIAG]), *lrow = (int *)(smem + off[O_LROW]);
-  int *lptr = (int *)(smem + off[O_LPTR]), *urow = (int *)(smem + off[O_UROW]);
-  int *uptr = (int *)(smem + off[O_UPTR]);
-  for (int64_t p = threadIdx.x; p < nnz; p += blockDim.x) {
-    val[p] = val_in[p];
-    ci[p] = __ldg(d.ci + p);
-  }
-  stage_ints(rp, d.rp, n + 1);
-  stage_ints(diag, d.diag, n);
-  stage_ints(lrow, v.lrow, v.tail0);
-  stage_ints(lptr, v.lptr, v.levels + 1);
-  stage_ints(urow, v.urow, n);
-  stage_ints(uptr, v.uptr, v.ulevels + 1);
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    rd[i] = ((const T *)d.rdiag)[i];
-    y[i] = T(b[__ldg(d.P + i)]);
-  }
-  __syncthreads();
+  const T *val = m.val, *rd = m.rd;
+  T *y = m.y, *red = m.red;
+  const int *ci = m.ci, *rp = m.rp, *diag = m.diag;
   // y = L \ b(P): the levels, then the tail rows as block-wide dot products
   for (int lv = 0; lv < v.levels; ++lv) {
-    for (int t = lptr[lv] + threadIdx.x; t < lptr[lv + 1]; t += blockDim.x) {
-      const int i = lrow[t];
+    for (int t = m.lptr[lv] + threadIdx.x; t < m.lptr[lv + 1]; t += blockDim.x) {
+      const int i = m.lrow[t];
       T acc = y[i];
       for (int p = rp[i]; p < diag[i]; ++p) acc -= val[p] * y[ci[p]];
       y[i] = acc;
@@ -765,8 +791,8 @@ __global__ void __launch_bounds__(1024) lu_solve_lvl(LuDev d, LvlDev v, const T 
   }
   // z = U \ y in place: a row reads only rows of lower U levels
   for (int lv = 0; lv < v.ulevels; ++lv) {
-    for (int t = uptr[lv] + threadIdx.x; t < uptr[lv + 1]; t += blockDim.x) {
-      const int i = urow[t];
+    for (int t = m.uptr[lv] + threadIdx.x; t < m.uptr[lv + 1]; t += blockDim.x) {
+      const int i = m.urow[t];
       T acc = y[i];
       for (int p = diag[i] + 1; p < rp[i + 1]; ++p) acc -= val[p] * y[ci[p]];
       y[i] = acc * rd[i];
@@ -774,6 +800,64 @@ __global__ void __launch_bounds__(1024) lu_solve_lvl(LuDev d, LvlDev v, const T 
     __syncthreads();
   }
   for (int i = threadIdx.x; i < n; i += blockDim.x) x[__ldg(d.Q + i)] = double(y[i]);
+}
+
+template <class T>
+__device__ void lvl_open(const LuDev &d) {
+  if (threadIdx.x == 0) {
+    d.ctrl[C_EPOCH_F] += 1;
+    d.ctrl[C_STATUS] = 0;
+    d.ctrl[C_BAD_ROW] = 0xffffffffu;
+  }
+}
+
+template <class T>
+__device__ void lvl_store_factor(const LuDev &d, const LvlSmem<T> &m, T *__restrict__ val_out,
+                                 int64_t nnz) {
+  for (int64_t p = threadIdx.x; p < nnz; p += blockDim.x) val_out[p] = m.val[p];
+  for (int i = threadIdx.x; i < d.n; i += blockDim.x) ((T *)d.rdiag)[i] = m.rd[i];
+}
+
+template <class T>
+__global__ void __launch_bounds__(1024) lu_factor_lvl(LuDev d, LvlDev v, const double *__restrict__ a,
+                                                      double *__restrict__ a_copy, int64_t nnz_a,
+                                                      T *__restrict__ val_out, int64_t nnz) {
+  extern __shared__ __align__(16) char smem[];
+  const LvlSmem<T> m = lvl_smem<T>(smem, d.n, nnz, v, LVL_FACTOR);
+  lvl_open<T>(d);
+  lvl_stage<T>(d, v, m, LVL_FACTOR, a, a_copy, nnz_a, nullptr, nnz, nullptr);
+  __syncthreads();
+  lvl_factor<T>(d, v, m);
+  lvl_store_factor<T>(d, m, val_out, nnz);
+}
+
+template <class T>
+__global__ void __launch_bounds__(1024) lu_solve_lvl(LuDev d, LvlDev v, const T *__restrict__ val_in,
+                                                     int64_t nnz, const double *__restrict__ b,
+                                                     double *__restrict__ x) {
+  extern __shared__ __align__(16) char smem[];
+  const LvlSmem<T> m = lvl_smem<T>(smem, d.n, nnz, v, LVL_SOLVE);
+  lvl_stage<T>(d, v, m, LVL_SOLVE, nullptr, nullptr, 0, val_in, nnz, b);
+  __syncthreads();
+  lvl_solve<T>(d, v, m, x);
+}
+
+// Refactor, keep the factor, then solve with it while it is in shared memory.
+template <class T>
+__global__ void __launch_bounds__(1024) lu_factor_solve_lvl(LuDev d, LvlDev v,
+                                                            const double *__restrict__ a,
+                                                            double *__restrict__ a_copy,
+                                                            int64_t nnz_a, T *__restrict__ val_out,
+                                                            int64_t nnz, const double *__restrict__ b,
+                                                            double *__restrict__ x) {
+  extern __shared__ __align__(16) char smem[];
+  const LvlSmem<T> m = lvl_smem<T>(smem, d.n, nnz, v, LVL_BOTH);
+  lvl_open<T>(d);
+  lvl_stage<T>(d, v, m, LVL_BOTH, a, a_copy, nnz_a, nullptr, nnz, b);
+  __syncthreads();
+  lvl_factor<T>(d, v, m);
+  lvl_store_factor<T>(d, m, val_out, nnz);
+  lvl_solve<T>(d, v, m, x);
 }
 
 }  // namespace
@@ -805,6 +889,7 @@ struct xg_lu {
   bool narrow = false;                     // one lane walks the rows (<= 2 rows per level)
   bool lvl = false;                        // level by level, one thread per row, in one CTA
   size_t smem_lvl_factor = 0, smem_lvl_solve = 0;
+  size_t smem_lvl_both = 0;                // > 0: the fused refactor + solve fits
   int lvl_threads = 0;
   int *d_lvl = nullptr;                    // level lists, row starts and tail, one buffer
   xg::LvlDev lvl_dev{};
@@ -903,6 +988,11 @@ int solve_once(xg_lu *lu, const double *b, double *x) {
   return XG_OK;
 }
 
+// Refactor and solve; one fused launch on the level path when it fits.
+template <class T>
+int refactor_solve_t(xg_lu *lu, const double *dev_values, const double *b, double *x,
+                     int n_refine);
+
 template <class T>
 int solve_t(xg_lu *lu, const double *b, double *x, int n_refine) {
   int rc = solve_once<T>(lu, b, x);
@@ -912,6 +1002,29 @@ int solve_t(xg_lu *lu, const double *b, double *x, int n_refine) {
   for (int it = 0; it < n_refine; ++it) {
     xg::lu_residual<<<nb, 256, 0, lu->stream>>>(d, lu->d_a, x, b, lu->d_r); xg::count_launches(1);
     rc = solve_once<T>(lu, lu->d_r, lu->d_dx);
+    if (rc) return rc;
+    xg::lu_axpy<<<nb, 256, 0, lu->stream>>>(lu->S.n, lu->d_dx, x); xg::count_launches(1);
+  }
+  XG_CU(cudaGetLastError());
+  return XG_OK;
+}
+
+template <class T>
+int refactor_solve_t(xg_lu *lu, const double *dev_values, const double *b, double *x,
+                     int n_refine) {
+  if (!lu->lvl || !lu->smem_lvl_both) {
+    int rc = refactor_t<T>(lu, dev_values);
+    return rc ? rc : solve_t<T>(lu, b, x, n_refine);
+  }
+  xg::LuDev d = lu->dev();
+  xg::lu_factor_solve_lvl<T><<<1, lu->lvl_threads, lu->smem_lvl_both, lu->stream>>>(
+      d, lu->lvl_dev, dev_values, lu->d_a, lu->S.nnz_a, (T *)lu->d_val, lu->nnz_lu, b, x);
+  xg::count_launches(1);
+  XG_CU(cudaGetLastError());
+  for (int it = 0; it < n_refine; ++it) {
+    const int nb = std::min(1024, (lu->S.n + 255) / 256);
+    xg::lu_residual<<<nb, 256, 0, lu->stream>>>(d, lu->d_a, x, b, lu->d_r); xg::count_launches(1);
+    int rc = solve_once<T>(lu, lu->d_r, lu->d_dx);
     if (rc) return rc;
     xg::lu_axpy<<<nb, 256, 0, lu->stream>>>(lu->S.n, lu->d_dx, x); xg::count_launches(1);
   }
@@ -1053,12 +1166,14 @@ extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const i
     for (int l = 0; l < v.levels; ++l) maxw = std::max(maxw, S.lptr[l + 1] - S.lptr[l]);
     for (int l = 0; l < v.ulevels; ++l) maxw = std::max(maxw, S.uptr[l + 1] - S.uptr[l]);
     for (int g = 0; g < v.ngroups; ++g) maxw = std::max(maxw, S.tail_gptr[g + 1] - S.tail_gptr[g]);
-    if (v.ntail > 0) maxw = std::max(maxw, 256);  // the tail's dot products
-    int threads = 32;
-    while (threads < maxw && threads < 1024) threads *= 2;  // a power of two: the reduction
+    // a power of two (the tail reduction), and at least 256 threads, so the
+    // staging keeps many loads in flight
+    int threads = 256;
+    while (threads < maxw && threads < 1024) threads *= 2;
     size_t off[xg::O_END + 1];
-    const size_t fb = xg::lvl_layout(n, lu->nnz_lu, v, threads, tsz, false, off);
-    const size_t sb = xg::lvl_layout(n, lu->nnz_lu, v, threads, tsz, true, off);
+    const size_t fb = xg::lvl_layout(n, lu->nnz_lu, v, threads, tsz, xg::LVL_FACTOR, off);
+    const size_t sb = xg::lvl_layout(n, lu->nnz_lu, v, threads, tsz, xg::LVL_SOLVE, off);
+    const size_t bb = xg::lvl_layout(n, lu->nnz_lu, v, threads, tsz, xg::LVL_BOTH, off);
     int max_optin = 0;
     cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, lu->device);
     const size_t limit = size_t(max_optin) > 8192 ? size_t(max_optin) - 4096 : 0;
@@ -1093,6 +1208,16 @@ extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const i
         lu->smem_lvl_factor = fb;
         lu->smem_lvl_solve = sb;
         lu->lvl = true;
+        // the fused refactor + solve when both working sets fit together
+        if (bb <= limit) {
+          cudaError_t e3 = precision == XG_LU_FP32
+              ? cudaFuncSetAttribute(xg::lu_factor_solve_lvl<float>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, int(bb))
+              : cudaFuncSetAttribute(xg::lu_factor_solve_lvl<double>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, int(bb));
+          if (e3 == cudaSuccess) lu->smem_lvl_both = bb;
+          else cudaGetLastError();
+        }
       } else {
         cudaGetLastError();
       }
@@ -1110,6 +1235,20 @@ extern "C" int xg_lu_refactor(xg_lu *lu, const double *dev_values) {
   XG_CU(cudaSetDevice(lu->device));
   int rc = lu->precision == XG_LU_FP32 ? refactor_t<float>(lu, dev_values)
                                        : refactor_t<double>(lu, dev_values);
+  if (!rc) lu->factored = true;
+  return rc;
+}
+
+extern "C" int xg_lu_refactor_solve(xg_lu *lu, const double *dev_values, const double *dev_b,
+                                    double *dev_x, int n_refine) {
+  if (!lu || !dev_values || !dev_b || !dev_x || n_refine < 0 || dev_b == dev_x) {
+    xg::set_error("xg_lu_refactor_solve: bad argument (b and x must be distinct device buffers)");
+    return XG_ERR_ARG;
+  }
+  XG_CU(cudaSetDevice(lu->device));
+  int rc = lu->precision == XG_LU_FP32
+               ? refactor_solve_t<float>(lu, dev_values, dev_b, dev_x, n_refine)
+               : refactor_solve_t<double>(lu, dev_values, dev_b, dev_x, n_refine);
   if (!rc) lu->factored = true;
   return rc;
 }

@@ -351,8 +351,7 @@ struct Run {
     while (status == 0) {
       ++step;
       st->factorizations++;
-      if ((*rc = xg_lu_refactor(lu, jac))) return 0;
-      if ((*rc = xg_lu_solve(lu, rhs, dx, o->n_refine))) return 0;
+      if ((*rc = xg_lu_refactor_solve(lu, jac, rhs, dx, o->n_refine))) return 0;
       tran_update<<<kRedBlocks, kThreads, 0, s>>>(n, dx, x, xc, !transient, rel_tol, abs_tol, w,
                                                   partials, lu_status_device(lu));
       xg::count_launches(1);

@@ -64,6 +64,7 @@ def lib():
     L.xg_lu_analyze.argtypes = [vp, i, vp, vp, vp, i, C.POINTER(vp)]
     L.xg_lu_refactor.argtypes = [vp, vp]
     L.xg_lu_solve.argtypes = [vp, vp, vp, i]
+    L.xg_lu_refactor_solve.argtypes = [vp, vp, vp, vp, i]
     L.xg_lu_status.argtypes = [vp, C.POINTER(i), C.POINTER(i)]
     L.xg_lu_get_info.argtypes = [vp, C.POINTER(abi.XgLuInfo)]
     L.xg_lu_get_symbolic.argtypes = [vp, vp, vp, vp, vp]
@@ -261,6 +262,10 @@ class LU:
 
     def refactor(self, dev_values):
         check(lib().xg_lu_refactor(self.h, C.c_void_p(dev_values)))
+
+    def refactor_solve(self, dev_values, dev_b, dev_x, n_refine=0):
+        check(lib().xg_lu_refactor_solve(self.h, C.c_void_p(dev_values), C.c_void_p(dev_b),
+                                         C.c_void_p(dev_x), n_refine))
 
     def solve(self, dev_b, dev_x, n_refine=0):
         check(lib().xg_lu_solve(self.h, C.c_void_p(dev_b), C.c_void_p(dev_x), n_refine))
