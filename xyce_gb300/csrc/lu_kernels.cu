@@ -567,14 +567,15 @@ __global__ void __launch_bounds__(kCtaThreads) lu_solve_cta(LuDev d, const T *__
 
 struct LvlDev {
   const int *lrow, *lptr, *urow, *uptr;  // rows by L level / by U level
+  const int *lheavy;                     // per L level: where its heavy rows start
   const int *urp32;                      // update-schedule row starts (int)
-  const int *tail_rowg, *tail_gptr, *tail_pos, *tail_pp, *tail_pm, *tail_q;
+  const int *tail_rowg, *tail_gptr, *tail_glong, *tail_pos, *tail_pp, *tail_pm, *tail_q;
   int levels, ulevels, nup;
   int tail0, ntail, ngroups, npos, npairs;
 };
 
 enum LvlOff { O_VAL, O_RD, O_Y, O_RED, O_CI, O_RP, O_DIAG, O_URP, O_UPOS, O_LROW, O_LPTR, O_UROW,
-              O_UPTR, O_TROWG, O_TGPTR, O_TPOS, O_TPP, O_TPM, O_TQ, O_END };
+              O_UPTR, O_TROWG, O_TGPTR, O_TGLONG, O_TPOS, O_TPP, O_TPM, O_TQ, O_LHEAVY, O_END };
 enum LvlMode { LVL_FACTOR = 1, LVL_SOLVE = 2, LVL_BOTH = 3 };
 
 // Shared-memory layout of the level kernels (the same function on host and
@@ -602,10 +603,12 @@ __host__ __device__ inline size_t lvl_layout(int n, int64_t nnz, const LvlDev &v
   off[O_UPTR] = o; o += sv ? I * size_t(v.ulevels + 1) : 0;
   off[O_TROWG] = o; o += f ? I * size_t(v.ntail + 1) : 0;
   off[O_TGPTR] = o; o += f ? I * size_t(v.ngroups + 1) : 0;
+  off[O_TGLONG] = o; o += f ? I * size_t(v.ngroups) : 0;
   off[O_TPOS] = o; o += f ? I * size_t(v.npos) : 0;
   off[O_TPP] = o; o += f ? I * size_t(v.npos + 1) : 0;
   off[O_TPM] = o; o += f ? I * size_t(v.npairs) : 0;
   off[O_TQ] = o; o += f ? I * size_t(v.npairs) : 0;
+  off[O_LHEAVY] = o; o += f ? I * size_t(v.levels) : 0;
   off[O_END] = o;
   return o;
 }
@@ -639,7 +642,7 @@ template <class T>
 struct LvlSmem {
   T *val, *rd, *y, *red;
   int *ci, *rp, *diag, *urp, *upos, *lrow, *lptr, *urow, *uptr;
-  int *trowg, *tgptr, *tpos, *tpp, *tpm, *tq;
+  int *trowg, *tgptr, *tglong, *tpos, *tpp, *tpm, *tq, *lheavy;
 };
 
 template <class T>
@@ -662,10 +665,12 @@ __device__ LvlSmem<T> lvl_smem(char *smem, int n, int64_t nnz, const LvlDev &v, 
   m.uptr = (int *)(smem + off[O_UPTR]);
   m.trowg = (int *)(smem + off[O_TROWG]);
   m.tgptr = (int *)(smem + off[O_TGPTR]);
+  m.tglong = (int *)(smem + off[O_TGLONG]);
   m.tpos = (int *)(smem + off[O_TPOS]);
   m.tpp = (int *)(smem + off[O_TPP]);
   m.tpm = (int *)(smem + off[O_TPM]);
   m.tq = (int *)(smem + off[O_TQ]);
+  m.lheavy = (int *)(smem + off[O_LHEAVY]);
   return m;
 }
 
@@ -688,10 +693,12 @@ __device__ void lvl_stage(const LuDev &d, const LvlDev &v, const LvlSmem<T> &m, 
     stage_ints(m.upos, d.upos, v.nup);
     stage_ints(m.trowg, v.tail_rowg, v.ntail + 1);
     stage_ints(m.tgptr, v.tail_gptr, v.ngroups + 1);
+    stage_ints(m.tglong, v.tail_glong, v.ngroups);
     stage_ints(m.tpos, v.tail_pos, v.npos);
     stage_ints(m.tpp, v.tail_pp, v.npos + 1);
     stage_ints(m.tpm, v.tail_pm, v.npairs);
     stage_ints(m.tq, v.tail_q, v.npairs);
+    stage_ints(m.lheavy, v.lheavy, v.levels);
   } else {
     for (int64_t p = threadIdx.x; p < nnz; p += blockDim.x) m.val[p] = val_in[p];
     for (int i = threadIdx.x; i < n; i += blockDim.x) m.rd[i] = ((const T *)d.rdiag)[i];
@@ -714,8 +721,31 @@ __device__ void lvl_factor(const LuDev &d, const LvlDev &v, const LvlSmem<T> &m)
   T *val = m.val, *rd = m.rd;
   const int *ci = m.ci, *rp = m.rp, *diag = m.diag, *urp = m.urp, *upos = m.upos;
   unsigned bad = 0xffffffffu;
+  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   for (int lv = 0; lv < v.levels; ++lv) {
-    for (int t = m.lptr[lv] + threadIdx.x; t < m.lptr[lv + 1]; t += blockDim.x) {
+    // heavy rows: a warp each, the updates of one L entry spread over the
+    // lanes, the L entries in order (the same sequence per entry as below)
+    for (int t = m.lheavy[lv] + (threadIdx.x >> 5); t < m.lptr[lv + 1]; t += nw) {
+      const int i = m.lrow[t];
+      const int dp = diag[i];
+      int u = urp[i];
+      for (int p = rp[i]; p < dp; ++p) {
+        const int k = ci[p];
+        const T l = val[p] * rd[k];
+        const int q0 = diag[k] + 1, len = rp[k + 1] - q0;
+        for (int j = lane; j < len; j += 32) val[upos[u + j]] -= l * val[q0 + j];
+        u += len;
+        __syncwarp();
+        if (lane == 0) val[p] = l;
+      }
+      __syncwarp();
+      if (lane == 0) {
+        const T piv = val[dp];
+        if (bad_pivot(piv)) bad = min(bad, unsigned(i));
+        rd[i] = recip(piv);
+      }
+    }
+    for (int t = m.lptr[lv] + threadIdx.x; t < m.lheavy[lv]; t += blockDim.x) {
       const int i = m.lrow[t];
       const int dp = diag[i];
       int u = urp[i];
@@ -724,7 +754,21 @@ __device__ void lvl_factor(const LuDev &d, const LvlDev &v, const LvlSmem<T> &m)
         const T l = val[p] * rd[k];
         val[p] = l;
         const int q0 = diag[k] + 1, len = rp[k + 1] - q0;
-        for (int j = 0; j < len; ++j) val[upos[u + j]] -= l * val[q0 + j];
+        // four updates at a time, all loads before the stores: the targets are
+        // distinct positions of row i, the sources lie in row k
+        int j = 0;
+        for (; j + 4 <= len; j += 4) {
+          const int t0 = upos[u + j], t1 = upos[u + j + 1], t2 = upos[u + j + 2],
+                    t3 = upos[u + j + 3];
+          const T s0 = val[q0 + j], s1 = val[q0 + j + 1], s2 = val[q0 + j + 2],
+                  s3 = val[q0 + j + 3];
+          const T v0 = val[t0], v1 = val[t1], v2 = val[t2], v3 = val[t3];
+          val[t0] = v0 - l * s0;
+          val[t1] = v1 - l * s1;
+          val[t2] = v2 - l * s2;
+          val[t3] = v3 - l * s3;
+        }
+        for (; j < len; ++j) val[upos[u + j]] -= l * val[q0 + j];
         u += len;
       }
       const T piv = val[dp];
@@ -737,11 +781,24 @@ __device__ void lvl_factor(const LuDev &d, const LvlDev &v, const LvlSmem<T> &m)
   for (int r = 0; r < v.ntail; ++r) {
     const int i = v.tail0 + r, dp = diag[i];
     for (int g = m.trowg[r]; g < m.trowg[r + 1]; ++g) {
-      for (int t = m.tgptr[g] + threadIdx.x; t < m.tgptr[g + 1]; t += blockDim.x) {
+      for (int t = m.tgptr[g] + threadIdx.x; t < m.tglong[g]; t += blockDim.x) {
         const int p = m.tpos[t];
         T acc = val[p];
         for (int j = m.tpp[t]; j < m.tpp[t + 1]; ++j) acc -= val[m.tpm[j]] * val[m.tq[j]];
         val[p] = p < dp ? acc * rd[ci[p]] : acc;
+      }
+      // long pulls: a warp each, lane-strided partial sums added in a fixed
+      // butterfly
+      for (int t = m.tglong[g] + (threadIdx.x >> 5); t < m.tgptr[g + 1]; t += nw) {
+        const int p = m.tpos[t];
+        T part = T(0);
+        for (int j = m.tpp[t] + lane; j < m.tpp[t + 1]; j += 32) part += val[m.tpm[j]] * val[m.tq[j]];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+        if (lane == 0) {
+          const T acc = val[p] - part;
+          val[p] = p < dp ? acc * rd[ci[p]] : acc;
+        }
       }
       __syncthreads();
     }
@@ -1147,11 +1204,13 @@ extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const i
   // by the one lane of the narrow path)
   if (!std::getenv("XG_LU_NO_LVL") && !lu->narrow && !urp32.empty() &&
       lu->nnz_lu < (int64_t(1) << 31)) {
-    // lrow | lptr | urow | uptr | urp32 | tail_rowg | tail_gptr | tail_pos | tail_pp | tail_pm | tail_q
+    // lrow | lptr | urow | uptr | urp32 | tail_rowg | tail_gptr | tail_pos | tail_pp | tail_pm |
+    // tail_q | tail_glong | lheavy
     const std::vector<int> *parts[] = {&S.lrow, &S.lptr, &S.urow, &S.uptr, &urp32, &S.tail_rowg,
-                                       &S.tail_gptr, &S.tail_pos, &S.tail_pp, &S.tail_pm, &S.tail_q};
-    size_t start[11], total = 0;
-    for (int k = 0; k < 11; ++k) { start[k] = total; total += parts[k]->size(); }
+                                       &S.tail_gptr, &S.tail_pos, &S.tail_pp, &S.tail_pm, &S.tail_q,
+                                       &S.tail_glong, &S.lheavy};
+    size_t start[13], total = 0;
+    for (int k = 0; k < 13; ++k) { start[k] = total; total += parts[k]->size(); }
     xg::LvlDev v{};
     v.levels = int(S.lptr.size()) - 1;
     v.ulevels = int(S.uptr.size()) - 1;
@@ -1166,9 +1225,12 @@ extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const i
     for (int l = 0; l < v.levels; ++l) maxw = std::max(maxw, S.lptr[l + 1] - S.lptr[l]);
     for (int l = 0; l < v.ulevels; ++l) maxw = std::max(maxw, S.uptr[l + 1] - S.uptr[l]);
     for (int g = 0; g < v.ngroups; ++g) maxw = std::max(maxw, S.tail_gptr[g + 1] - S.tail_gptr[g]);
-    // a power of two (the tail reduction), and at least 256 threads, so the
+    // a power of two (the tail reduction); 1,024 threads when there are heavy
+    // rows (a warp each) or the widest level needs them, else 256, so the
     // staging keeps many loads in flight
     int threads = 256;
+    for (int l = 0; l < v.levels; ++l)
+      if (S.lheavy[l] < S.lptr[l + 1]) maxw = std::max(maxw, 1024);
     while (threads < maxw && threads < 1024) threads *= 2;
     size_t off[xg::O_END + 1];
     const size_t fb = xg::lvl_layout(n, lu->nnz_lu, v, threads, tsz, xg::LVL_FACTOR, off);
@@ -1203,6 +1265,8 @@ extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const i
         v.tail_pp = b0 + start[8];
         v.tail_pm = b0 + start[9];
         v.tail_q = b0 + start[10];
+        v.tail_glong = b0 + start[11];
+        v.lheavy = b0 + start[12];
         lu->lvl_dev = v;
         lu->lvl_threads = threads;
         lu->smem_lvl_factor = fb;

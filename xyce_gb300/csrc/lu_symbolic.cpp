@@ -572,6 +572,7 @@ bool lu_build_updates(LuSymbolic &S) {
     if (S.diag[i] - S.rp[i] > kTailMinL) { S.tail0 = i; break; }
   S.tail_rowg.assign(1, 0);
   S.tail_gptr.assign(1, 0);
+  S.tail_glong.clear();
   S.tail_pos.clear();
   S.tail_pp.assign(1, 0);
   S.tail_pm.clear();
@@ -598,9 +599,22 @@ bool lu_build_updates(LuSymbolic &S) {
     for (int g = 0; g < ng; ++g) cnt[g + 1] += cnt[g];
     const int base = int(S.tail_pos.size());
     S.tail_pos.resize(size_t(base + len));
+    // within a group, positions with few pulls first, then the long ones
+    // (a warp each)
     std::vector<int> fill(cnt.begin(), cnt.end() - 1);
-    for (int t = 0; t < len; ++t) S.tail_pos[size_t(base + fill[plev[t]]++)] = s + t;
-    for (int g = 0; g < ng; ++g) S.tail_gptr.push_back(base + cnt[g + 1]);
+    std::vector<int> nshort(ng, 0);
+    for (int t = 0; t < len; ++t)
+      if (int(pulls[t].size()) <= kTailLongPulls) nshort[plev[t]]++;
+    std::vector<int> lfill(ng);
+    for (int g = 0; g < ng; ++g) lfill[g] = cnt[g] + nshort[g];
+    for (int t = 0; t < len; ++t) {
+      const bool lng = int(pulls[t].size()) > kTailLongPulls;
+      S.tail_pos[size_t(base + (lng ? lfill[plev[t]]++ : fill[plev[t]]++))] = s + t;
+    }
+    for (int g = 0; g < ng; ++g) {
+      S.tail_glong.push_back(base + cnt[g] + nshort[g]);
+      S.tail_gptr.push_back(base + cnt[g + 1]);
+    }
     S.tail_rowg.push_back(int(S.tail_gptr.size()) - 1);
     for (int t = base; t < base + len; ++t) {
       for (auto &pq : pulls[S.tail_pos[size_t(t)] - s]) {
@@ -629,6 +643,21 @@ bool lu_build_updates(LuSymbolic &S) {
     nlev = std::max(nlev, l + 1);
   }
   group(lev, nlev, S.tail0, S.lrow, S.lptr);
+  // within a level, the rows with many updates last, from lheavy[l] on
+  S.lheavy.assign(nlev, 0);
+  for (int l = 0; l < nlev; ++l) {
+    auto b = S.lrow.begin() + S.lptr[l], e = S.lrow.begin() + S.lptr[l + 1];
+    auto light = [&](int i) { return S.urp[i + 1] - S.urp[i] <= kHeavyRowUpdates; };
+    // a warp per row only while few rows need it: a warp's FP64 instruction
+    // costs the same with 4 lanes busy as with 32, so many heavy rows run
+    // better one per lane
+    if (e - b - std::count_if(b, e, light) > kMaxHeavyRows) {
+      S.lheavy[l] = S.lptr[l + 1];
+      continue;
+    }
+    auto mid = std::stable_partition(b, e, light);
+    S.lheavy[l] = int(mid - S.lrow.begin());
+  }
   // U levels, from the last row up: a row's U part names later rows only
   nlev = 0;
   for (int i = n - 1; i >= 0; --i) {

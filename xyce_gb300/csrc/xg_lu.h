@@ -47,6 +47,10 @@ struct LuSymbolic {
   // highest of the rows its L part names), lptr[l] where level l starts;
   // urow/uptr the same for the backward solve, by U level.
   std::vector<int> lrow, lptr, urow, uptr;
+  // Within level l the rows with more than kHeavyRowUpdates updates come
+  // last, from lheavy[l] on: a warp factors each of those (when the level
+  // has at most kMaxHeavyRows of them).
+  std::vector<int> lheavy;
   // Trailing rows with long L parts (a supply rail ordered last has one L
   // entry per device on it), and the rows after them, are left out of lrow:
   // one thread would walk them serially.  They are factored one at a time after the levels, each with
@@ -55,10 +59,17 @@ struct LuSymbolic {
   // elimination applies them), positions grouped so that a group reads only
   // multipliers of earlier groups.  tail_pos lists the positions by group,
   // tail_gptr[g] where group g starts, tail_rowg[r] the first group of row
-  // tail0 + r, tail_pp[t] where the pairs of tail_pos[t] start.
+  // tail0 + r, tail_pp[t] where the pairs of tail_pos[t] start.  Within a
+  // group the positions with more than kTailLongPulls pairs come last, from
+  // tail_glong[g] on: a warp sums each of those (the diagonal of a supply
+  // rail pulls one pair per device on the rail).
   int tail0 = 0;
-  std::vector<int> tail_rowg, tail_gptr, tail_pos, tail_pp, tail_pm, tail_q;
+  std::vector<int> tail_rowg, tail_gptr, tail_glong, tail_pos, tail_pp, tail_pm, tail_q;
 };
+
+constexpr int kTailLongPulls = 32;
+constexpr int kHeavyRowUpdates = 32;
+constexpr int kMaxHeavyRows = 8;
 
 // The tail starts at the first of the last kTailMaxRows rows with more than
 // kTailMinL L entries.
