@@ -19,7 +19,8 @@
 //    coalesced index load, one coalesced value load and one multiply-add.
 //  * solves: the same claim/wait scheme by rows of L (forward) and of U
 //    (backward, rows claimed in descending order), a fixed lane-strided
-//    partial sum and a fixed shuffle tree per row.
+//    partial sum and a fixed shuffle tree per row; a row waits on the values
+//    it needs themselves, which hold a pending pattern until written.
 //  * precision: factors in FP64, or in FP32 with FP64 iterative refinement
 //    (r = b - A x with the FP64 matrix, solve, x += d).
 //
@@ -147,10 +148,83 @@ __global__ void __launch_bounds__(256) lu_factor(LuDev d, T *val) {
   }
 }
 
-__global__ void lu_solve_open(LuDev d) {
-  d.ctrl[C_EPOCH_S] += 1;
-  d.ctrl[C_CLAIM_L] = 0;
-  d.ctrl[C_CLAIM_U] = 0;
+// The grid-wide solves carry readiness in the value itself: before a solve
+// every entry of y and z holds a signalling-NaN bit pattern, which no
+// arithmetic produces (an invalid operation gives a quiet NaN); a row's result
+// replaces it with one aligned store, and a row that needs it polls the value.
+// One L2 round trip per dependency, with no flag and no fence between them.
+template <class T> struct Pending;
+template <> struct Pending<double> {
+  using U = unsigned long long;
+  static constexpr U bits = 0x7FF4DEADBEEF0001ull;
+};
+template <> struct Pending<float> {
+  using U = unsigned;
+  static constexpr U bits = 0x7FA5DEADu;
+};
+
+__device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned ld_relaxed(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed(unsigned long long *p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void st_relaxed(unsigned *p, unsigned v) {
+  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ double from_bits(unsigned long long v) { return __longlong_as_double((long long)v); }
+__device__ __forceinline__ float from_bits(unsigned v) { return __uint_as_float(v); }
+__device__ __forceinline__ unsigned long long to_bits(double v) {
+  return (unsigned long long)__double_as_longlong(v);
+}
+__device__ __forceinline__ unsigned to_bits(float v) { return __float_as_uint(v); }
+
+// The value at p once it is no longer pending; zero (and the timeout bit) if
+// it never arrives.
+template <class T>
+__device__ T wait_value(const T *p, unsigned *ctrl) {
+  using U = typename Pending<T>::U;
+  const U *q = reinterpret_cast<const U *>(p);
+  int it = 0;
+  U v;
+  while ((v = ld_relaxed(q)) == Pending<T>::bits) {
+    ++it;
+    if (it > kSpinLimit ||
+        ((it & 1023) == 0 && (*(volatile unsigned *)&ctrl[C_STATUS] & ST_TIMEOUT))) {
+      atomicOr(&ctrl[C_STATUS], ST_TIMEOUT);
+      return T(0);
+    }
+    if (it > 32) __nanosleep(64);
+  }
+  return from_bits(v);
+}
+
+template <class T>
+__device__ __forceinline__ void publish(T *p, T v) {
+  st_relaxed(reinterpret_cast<typename Pending<T>::U *>(p), to_bits(v));
+}
+
+// Opens a solve: row claims restart, y and z become pending.
+template <class T>
+__global__ void lu_solve_open(LuDev d, T *y, T *z) {
+  const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t0 == 0) {
+    d.ctrl[C_EPOCH_S] += 1;
+    d.ctrl[C_CLAIM_L] = 0;
+    d.ctrl[C_CLAIM_U] = 0;
+  }
+  using U = typename Pending<T>::U;
+  for (int i = t0; i < d.n; i += gridDim.x * blockDim.x) {
+    reinterpret_cast<U *>(y)[i] = Pending<T>::bits;
+    reinterpret_cast<U *>(z)[i] = Pending<T>::bits;
+  }
 }
 
 template <class T>
@@ -165,7 +239,6 @@ template <class T>
 __global__ void __launch_bounds__(256) lu_lsolve(LuDev d, const T *__restrict__ val,
                                                  const double *__restrict__ b, T *y) {
   const int lane = threadIdx.x & 31;
-  const unsigned epoch = *(volatile unsigned *)&d.ctrl[C_EPOCH_S];
   while (true) {
     int row = 0;
     if (lane == 0) row = int(atomicAdd(&d.ctrl[C_CLAIM_L], 1u));
@@ -177,15 +250,10 @@ __global__ void __launch_bounds__(256) lu_lsolve(LuDev d, const T *__restrict__ 
     for (int p = s + lane; p < dp; p += 32) {
       const int k = __ldg(d.ci + p);
       const T lv = __ldcg(val + p);
-      wait_epoch(d.done_l + k, epoch, d.ctrl);
-      acc += lv * __ldcg(y + k);
+      acc += lv * wait_value(y + k, d.ctrl);
     }
     acc = warp_sum(acc);
-    if (lane == 0) {
-      y[row] = bi - acc;
-      __threadfence();
-      st_release(d.done_l + row, epoch);
-    }
+    if (lane == 0) publish(y + row, bi - acc);
   }
 }
 
@@ -194,7 +262,6 @@ template <class T>
 __global__ void __launch_bounds__(256) lu_usolve(LuDev d, const T *__restrict__ val,
                                                  const T *__restrict__ y, T *z, double *x) {
   const int lane = threadIdx.x & 31;
-  const unsigned epoch = *(volatile unsigned *)&d.ctrl[C_EPOCH_S];
   while (true) {
     int c = 0;
     if (lane == 0) c = int(atomicAdd(&d.ctrl[C_CLAIM_U], 1u));
@@ -209,16 +276,13 @@ __global__ void __launch_bounds__(256) lu_usolve(LuDev d, const T *__restrict__ 
     for (int p = dp + 1 + lane; p < e; p += 32) {
       const int k = __ldg(d.ci + p);
       const T uv = __ldcg(val + p);
-      wait_epoch(d.done_u + k, epoch, d.ctrl);
-      acc += uv * __ldcg(z + k);
+      acc += uv * wait_value(z + k, d.ctrl);
     }
     acc = warp_sum(acc);
     if (lane == 0) {
       const T zi = (yi - acc) * ri;
-      z[row] = zi;
+      publish(z + row, zi);
       x[qi] = double(zi);
-      __threadfence();
-      st_release(d.done_u + row, epoch);
     }
   }
 }
@@ -1037,7 +1101,9 @@ int solve_once(xg_lu *lu, const double *b, double *x) {
     XG_CU(cudaGetLastError());
     return XG_OK;
   }
-  xg::lu_solve_open<<<1, 1, 0, lu->stream>>>(d); xg::count_launches(1);
+  xg::lu_solve_open<T><<<std::min(1024, (lu->S.n + 255) / 256), 256, 0, lu->stream>>>(
+      d, (T *)lu->d_y, (T *)lu->d_z);
+  xg::count_launches(1);
   xg::lu_lsolve<T><<<lu->grid_factor, 256, 0, lu->stream>>>(d, (const T *)lu->d_val, b, (T *)lu->d_y); xg::count_launches(1);
   xg::lu_usolve<T><<<lu->grid_factor, 256, 0, lu->stream>>>(d, (const T *)lu->d_val, (const T *)lu->d_y,
                                                             (T *)lu->d_z, x); xg::count_launches(1);
