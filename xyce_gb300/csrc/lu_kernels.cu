@@ -90,69 +90,14 @@ struct LuDev {
   void *rdiag;                // 1 / U(k,k) per row, written by the refactor
 };
 
-// Scatter A into the L\U value array (fill entries zero), keep an FP64 copy of
-// A for the residual, and open a new factorisation epoch.
-template <class T>
-__global__ void lu_assemble(LuDev d, const double *__restrict__ a, double *__restrict__ a_copy,
-                            int64_t nnz_a, T *__restrict__ val, int64_t nnz_lu) {
-  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
-  const int64_t t0 = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (t0 == 0) {
-    d.ctrl[C_EPOCH_F] += 1;
-    d.ctrl[C_CLAIM_F] = 0;
-    d.ctrl[C_STATUS] = 0;
-    d.ctrl[C_BAD_ROW] = 0xffffffffu;
-  }
-  for (int64_t p = t0; p < nnz_lu; p += stride) {
-    int s = d.lu2a[p];
-    val[p] = s >= 0 ? T(a[s]) : T(0);
-  }
-  if (a_copy != a)
-    for (int64_t p = t0; p < nnz_a; p += stride) a_copy[p] = a[p];
-}
-
-template <class T>
-__global__ void __launch_bounds__(256) lu_factor(LuDev d, T *val) {
-  const int lane = threadIdx.x & 31;
-  const unsigned epoch = *(volatile unsigned *)&d.ctrl[C_EPOCH_F];
-  while (true) {
-    int row = 0;
-    if (lane == 0) row = int(atomicAdd(&d.ctrl[C_CLAIM_F], 1u));
-    row = __shfl_sync(0xffffffffu, row, 0);
-    if (row >= d.n) break;
-    const int s = __ldg(d.rp + row), dp = __ldg(d.diag + row);
-    T *rdiag = (T *)d.rdiag;
-    const int *up = d.upos + __ldg(d.urp + row);
-    for (int p = s; p < dp; ++p) {
-      const int k = __ldg(d.ci + p);
-      const int q0 = __ldg(d.diag + k) + 1, len = __ldg(d.rp + k + 1) - q0;
-      if (lane == 0) wait_epoch(d.done_f + k, epoch, d.ctrl);
-      __syncwarp();
-      const T l = val[p] * __ldcg(rdiag + k);
-      __syncwarp();
-      if (lane == 0) val[p] = l;
-      for (int j = lane; j < len; j += 32) val[__ldg(up + j)] -= l * __ldcg(val + q0 + j);
-      up += len;
-      __syncwarp();
-    }
-    if (lane == 0) {
-      const T u = val[dp];
-      if (!(fabs(double(u)) > 0.0) || !isfinite(double(u))) {
-        atomicOr(&d.ctrl[C_STATUS], ST_PIVOT);
-        atomicMin(&d.ctrl[C_BAD_ROW], unsigned(row));
-      }
-      rdiag[row] = T(1) / u;
-      __threadfence();
-      st_release(d.done_f + row, epoch);
-    }
-  }
-}
-
-// The grid-wide solves carry readiness in the value itself: before a solve
-// every entry of y and z holds a signalling-NaN bit pattern, which no
-// arithmetic produces (an invalid operation gives a quiet NaN); a row's result
-// replaces it with one aligned store, and a row that needs it polls the value.
-// One L2 round trip per dependency, with no flag and no fence between them.
+// The grid-wide kernels carry readiness in the value itself: before a
+// refactor every reciprocal pivot, before a solve every entry of y and z,
+// holds a signalling-NaN bit pattern, which no arithmetic produces (an
+// invalid operation gives a quiet NaN); a row's result replaces it with one
+// aligned store, and a row that needs it polls the value.  The solves need
+// nothing else from the row, so relaxed accesses do; the refactor also reads
+// the row's U part, so the pivot is stored with release after it and polled
+// with acquire.
 template <class T> struct Pending;
 template <> struct Pending<double> {
   using U = unsigned long long;
@@ -209,6 +154,120 @@ __device__ T wait_value(const T *p, unsigned *ctrl) {
 template <class T>
 __device__ __forceinline__ void publish(T *p, T v) {
   st_relaxed(reinterpret_cast<typename Pending<T>::U *>(p), to_bits(v));
+}
+
+__device__ __forceinline__ unsigned long long ld_acq(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned ld_acq(const unsigned *p) { return ld_acquire(p); }
+__device__ __forceinline__ void st_rel(unsigned long long *p, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void st_rel(unsigned *p, unsigned v) { st_release(p, v); }
+
+// wait_value with acquire: what the writer stored before its release is
+// visible after it.
+template <class T>
+__device__ T wait_value_acquire(const T *p, unsigned *ctrl) {
+  using U = typename Pending<T>::U;
+  const U *q = reinterpret_cast<const U *>(p);
+  int it = 0;
+  U v;
+  while ((v = ld_acq(q)) == Pending<T>::bits) {
+    ++it;
+    if (it > kSpinLimit ||
+        ((it & 1023) == 0 && (*(volatile unsigned *)&ctrl[C_STATUS] & ST_TIMEOUT))) {
+      atomicOr(&ctrl[C_STATUS], ST_TIMEOUT);
+      return T(0);
+    }
+    if (it > 32) __nanosleep(64);
+  }
+  return from_bits(v);
+}
+
+template <class T>
+__device__ __forceinline__ void publish_release(T *p, T v) {
+  st_rel(reinterpret_cast<typename Pending<T>::U *>(p), to_bits(v));
+}
+
+// Scatter A into the L\U value array (fill entries zero), keep an FP64 copy of
+// A for the residual, and open a new factorisation epoch.
+template <class T>
+__global__ void lu_assemble(LuDev d, const double *__restrict__ a, double *__restrict__ a_copy,
+                            int64_t nnz_a, T *__restrict__ val, int64_t nnz_lu) {
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  const int64_t t0 = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t0 == 0) {
+    d.ctrl[C_EPOCH_F] += 1;
+    d.ctrl[C_CLAIM_F] = 0;
+    d.ctrl[C_STATUS] = 0;
+    d.ctrl[C_BAD_ROW] = 0xffffffffu;
+  }
+  for (int64_t p = t0; p < nnz_lu; p += stride) {
+    int s = d.lu2a[p];
+    val[p] = s >= 0 ? T(a[s]) : T(0);
+  }
+  if (a_copy != a)
+    for (int64_t p = t0; p < nnz_a; p += stride) a_copy[p] = a[p];
+  using U = typename Pending<T>::U;
+  for (int64_t i = t0; i < d.n; i += stride) reinterpret_cast<U *>(d.rdiag)[i] = Pending<T>::bits;
+}
+
+// A warp's own row lives in shared memory while it is eliminated (rows up to
+// kRowStage entries; longer ones stay in global memory): the multiplier of
+// each L entry reads what the previous entries' updates wrote, and a
+// shared-memory round trip is ~30 cycles where an L2 one is ~1 us.
+constexpr int kRowStage = 512;
+
+template <class T>
+__global__ void __launch_bounds__(256) lu_factor(LuDev d, T *val) {
+  __shared__ T stage[8][kRowStage];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  T *rdiag = (T *)d.rdiag;
+  while (true) {
+    int row = 0;
+    if (lane == 0) row = int(atomicAdd(&d.ctrl[C_CLAIM_F], 1u));
+    row = __shfl_sync(0xffffffffu, row, 0);
+    if (row >= d.n) break;
+    const int s = __ldg(d.rp + row), dp = __ldg(d.diag + row), e = __ldg(d.rp + row + 1);
+    const int *up = d.upos + __ldg(d.urp + row);
+    const bool staged = e - s <= kRowStage;
+    // the row's values: in shared memory (position p at p - s) or in place
+    T *rb = staged ? stage[wid] : val;
+    const int ro = staged ? s : 0;
+    if (staged) {
+      for (int p = s + lane; p < e; p += 32) rb[p - ro] = val[p];
+      __syncwarp();
+    }
+    for (int p = s; p < dp; ++p) {
+      const int k = __ldg(d.ci + p);
+      const int q0 = __ldg(d.diag + k) + 1, len = __ldg(d.rp + k + 1) - q0;
+      T rk = T(0);
+      if (lane == 0) rk = wait_value_acquire(rdiag + k, d.ctrl);
+      rk = __shfl_sync(0xffffffffu, rk, 0);
+      const T l = rb[p - ro] * rk;
+      __syncwarp();
+      if (lane == 0) rb[p - ro] = l;
+      for (int j = lane; j < len; j += 32) rb[__ldg(up + j) - ro] -= l * __ldcg(val + q0 + j);
+      up += len;
+      __syncwarp();
+    }
+    if (staged) {
+      for (int p = s + lane; p < e; p += 32) val[p] = rb[p - ro];
+      __syncwarp();
+    }
+    if (lane == 0) {
+      const T u = rb[dp - ro];
+      if (!(fabs(double(u)) > 0.0) || !isfinite(double(u))) {
+        atomicOr(&d.ctrl[C_STATUS], ST_PIVOT);
+        atomicMin(&d.ctrl[C_BAD_ROW], unsigned(row));
+      }
+      __threadfence();
+      publish_release(rdiag + row, T(1) / u);
+    }
+  }
 }
 
 // Opens a solve: row claims restart, y and z become pending.
