@@ -82,20 +82,35 @@ struct BatchDev {
   int n_out, max_points;
   double *rec_t, *rec_v;         // [nc][max_points], [nc][max_points][n_out]
   int n_refine;
+  // level schedule per request (batch_solve_lvl): lvl[c] != 0 when request c
+  // uses it; its int blob (lvl_blob layout) starts at sched_off[c]
+  const int *lvl;
+  const int64_t *sched_off;
+  const int *sched;
 };
 
 // 1/u by Newton-Raphson on the reciprocal from a single-precision seed (two
 // steps, each doubling the correct bits); IEEE division outside the range
 // where the seed is representable.
-template <class T>
-__device__ __forceinline__ T recip_nr(T u) {
-  const double a = fabs(double(u));
-  if (!(a > 1e-30 && a < 1e30)) return T(1) / u;
-  if (sizeof(T) == sizeof(float)) return T(1.0f / float(u));
+__device__ __forceinline__ double recip_nr(double u) {
+  const double a = fabs(u);
+  if (!(a > 1e-30 && a < 1e30)) return 1.0 / u;
   double x = double(1.0f / float(u));
-  x = x * (2.0 - double(u) * x);
-  x = x * (2.0 - double(u) * x);
-  return T(x);
+  x = x * (2.0 - u * x);
+  x = x * (2.0 - u * x);
+  return x;
+}
+// FP32 factors: a single-precision reciprocal, no FP64 instruction
+__device__ __forceinline__ float recip_nr(float u) { return 1.0f / u; }
+
+// A zero, infinite or NaN pivot, from the bits (no FP64 instruction).
+__device__ __forceinline__ bool bad_pivot(double u) {
+  const unsigned long long v = (unsigned long long)__double_as_longlong(u);
+  return (v << 1) == 0 || ((v >> 52) & 0x7ff) == 0x7ff;
+}
+__device__ __forceinline__ bool bad_pivot(float u) {
+  const unsigned v = __float_as_uint(u);
+  return (v << 1) == 0 || ((v >> 23) & 0xff) == 0xff;
 }
 
 __device__ __forceinline__ double warp_sum_d(double v) {
@@ -114,7 +129,7 @@ template <class T>
 __global__ void __launch_bounds__(128) batch_solve(BatchDev b) {
   const int c = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (c >= b.nc) return;
-  if (b.cs[c].phase != PH_ITER) return;
+  if (b.cs[c].phase != PH_ITER || b.lvl[c]) return;
   const int u0 = b.uptr[c], n = b.uptr[c + 1] - u0;
   const int *rp = b.lrp + b.lrp_off[c];
   const int64_t z0 = b.lnz_off[c];
@@ -146,34 +161,35 @@ __global__ void __launch_bounds__(128) batch_solve(BatchDev b) {
         }
       }
       const T u = val[dp];
-      if (!(fabs(double(u)) > 0.0) || !isfinite(double(u))) bad = 1;
+      if (bad_pivot(u)) bad = 1;
       rd[row] = recip_nr(u);
     }
   }
   __syncwarp();
-  // solve J dx = rhs, then refine against the FP64 Jacobian
-  double *y = b.y + u0;
+  // solve J dx = rhs, then refine against the FP64 Jacobian; the work vector
+  // is in the factors' precision
+  T *y = reinterpret_cast<T *>(b.y + u0);
   for (int pass = 0; pass <= b.n_refine; ++pass) {
     const double *src = pass == 0 ? b.rhs : b.r;
-    for (int k = lane; k < n; k += 32) y[k] = src[b.uidx[u0 + P[k]]];
+    for (int k = lane; k < n; k += 32) y[k] = T(src[b.uidx[u0 + P[k]]]);
     __syncwarp();
     if (lane == 0) {
       for (int row = 0; row < n; ++row) {
-        T acc = T(y[row]);
-        for (int p = rp[row]; p < diag[row]; ++p) acc -= val[p] * T(y[ci[p]]);
-        y[row] = double(acc);
+        T acc = y[row];
+        for (int p = rp[row]; p < diag[row]; ++p) acc -= val[p] * y[ci[p]];
+        y[row] = acc;
       }
       for (int row = n - 1; row >= 0; --row) {
-        T acc = T(y[row]);
-        for (int p = diag[row] + 1; p < rp[row + 1]; ++p) acc -= val[p] * T(y[ci[p]]);
-        y[row] = double(acc * rd[row]);
+        T acc = y[row];
+        for (int p = diag[row] + 1; p < rp[row + 1]; ++p) acc -= val[p] * y[ci[p]];
+        y[row] = acc * rd[row];
       }
     }
     __syncwarp();
     for (int k = lane; k < n; k += 32) {
       const int g = b.uidx[u0 + Q[k]];
-      if (pass == 0) b.dx[g] = y[k];
-      else b.dx[g] += y[k];
+      if (pass == 0) b.dx[g] = double(y[k]);
+      else b.dx[g] += double(y[k]);
     }
     __syncwarp();
     if (pass < b.n_refine) {
@@ -209,7 +225,7 @@ __global__ void __launch_bounds__(128) batch_solve(BatchDev b) {
 // request's footprint fits (smem_bytes_request).
 __host__ __device__ inline size_t smem_bytes_request(int n, int64_t nz, size_t tsz) {
   auto a16 = [](size_t v) { return (v + 15) & ~size_t(15); };
-  return a16(tsz * size_t(nz)) + a16(tsz * size_t(n)) + a16(sizeof(double) * size_t(n)) +
+  return a16(tsz * size_t(nz)) + 2 * a16(tsz * size_t(n)) +
          sizeof(int) * (size_t(nz) + 3 * size_t(n) + 1);
 }
 
@@ -218,15 +234,15 @@ __global__ void __launch_bounds__(32) batch_solve_smem(BatchDev b) {
   extern __shared__ __align__(16) char sm[];
   const int c = blockIdx.x, lane = threadIdx.x;
   if (c >= b.nc) return;
-  if (b.cs[c].phase != PH_ITER) return;
+  if (b.cs[c].phase != PH_ITER || b.lvl[c]) return;
   const int u0 = b.uptr[c], n = b.uptr[c + 1] - u0;
   const int64_t z0 = b.lnz_off[c];
   const int nz = int(b.lnz_off[c + 1] - z0);
   auto a16 = [](size_t v) { return (v + 15) & ~size_t(15); };
   T *val = (T *)sm;
   T *rd = (T *)(sm + a16(sizeof(T) * nz));
-  double *y = (double *)(sm + a16(sizeof(T) * nz) + a16(sizeof(T) * n));
-  int *ci = (int *)(sm + a16(sizeof(T) * nz) + a16(sizeof(T) * n) + a16(sizeof(double) * n));
+  T *y = (T *)(sm + a16(sizeof(T) * nz) + a16(sizeof(T) * n));
+  int *ci = (int *)(sm + a16(sizeof(T) * nz) + 2 * a16(sizeof(T) * n));
   int *rp = ci + nz, *diag = rp + n + 1, *map = diag + n;
   const int *grp = b.lrp + b.lrp_off[c];
   for (int p = lane; p < nz; p += 32) {
@@ -253,7 +269,7 @@ __global__ void __launch_bounds__(32) batch_solve_smem(BatchDev b) {
         }
       }
       const T u = val[dp];
-      if (!(fabs(double(u)) > 0.0) || !isfinite(double(u))) bad = 1;
+      if (bad_pivot(u)) bad = 1;
       rd[row] = recip_nr(u);
     }
   }
@@ -261,25 +277,25 @@ __global__ void __launch_bounds__(32) batch_solve_smem(BatchDev b) {
   const int *P = b.lP + u0, *Q = b.lQ + u0;
   for (int pass = 0; pass <= b.n_refine; ++pass) {
     const double *src = pass == 0 ? b.rhs : b.r;
-    for (int k = lane; k < n; k += 32) y[k] = src[b.uidx[u0 + P[k]]];
+    for (int k = lane; k < n; k += 32) y[k] = T(src[b.uidx[u0 + P[k]]]);
     __syncwarp();
     if (lane == 0) {
       for (int row = 0; row < n; ++row) {
-        T acc = T(y[row]);
-        for (int p = rp[row]; p < diag[row]; ++p) acc -= val[p] * T(y[ci[p]]);
-        y[row] = double(acc);
+        T acc = y[row];
+        for (int p = rp[row]; p < diag[row]; ++p) acc -= val[p] * y[ci[p]];
+        y[row] = acc;
       }
       for (int row = n - 1; row >= 0; --row) {
-        T acc = T(y[row]);
-        for (int p = diag[row] + 1; p < rp[row + 1]; ++p) acc -= val[p] * T(y[ci[p]]);
-        y[row] = double(acc * rd[row]);
+        T acc = y[row];
+        for (int p = diag[row] + 1; p < rp[row + 1]; ++p) acc -= val[p] * y[ci[p]];
+        y[row] = acc * rd[row];
       }
     }
     __syncwarp();
     for (int k = lane; k < n; k += 32) {
       const int g = b.uidx[u0 + Q[k]];
-      if (pass == 0) b.dx[g] = y[k];
-      else b.dx[g] += y[k];
+      if (pass == 0) b.dx[g] = double(y[k]);
+      else b.dx[g] += double(y[k]);
     }
     __syncwarp();
     if (pass < b.n_refine) {
@@ -307,17 +323,217 @@ __global__ void __launch_bounds__(32) batch_solve_smem(BatchDev b) {
   }
 }
 
+// ---- batch_solve_lvl: the level schedule, one warp per request ----------------
+// The walk above runs one lane over every row, so the batch iteration takes as
+// long as the largest request's rows in sequence.  Here each request's factor
+// comes with its dependency levels (nested dissection makes a ring of 501
+// stages ~30 levels deep): the rows of a level go to the lanes, the trailing
+// supply-rail rows are pulled position by position, and everything sits in
+// shared memory.  Per request the sums are in a fixed order, so a request's
+// result does not depend on the batch around it.
+
+// The blob, all ints: a header, then the arrays in this order.
+enum LvlHdr { H_LEVELS, H_ULEVELS, H_TAIL0, H_NTAIL, H_NGROUPS, H_NPOS, H_NPAIRS, H_NUP, H_N };
+__host__ __device__ inline int64_t lvl_blob_len(int n, const int *h) {
+  return H_N + (n + 1) + h[H_NUP] + h[H_TAIL0] + (h[H_LEVELS] + 1) + n + (h[H_ULEVELS] + 1) +
+         (h[H_NTAIL] + 1) + (h[H_NGROUPS] + 1) + h[H_NPOS] + (h[H_NPOS] + 1) + 2 * int64_t(h[H_NPAIRS]);
+}
+__host__ __device__ inline size_t smem_bytes_lvl(int n, int64_t nz, int64_t blob, size_t tsz) {
+  auto a16 = [](size_t v) { return (v + 15) & ~size_t(15); };
+  return a16(tsz * size_t(nz)) + 2 * a16(tsz * size_t(n)) +
+         sizeof(int) * (size_t(nz) + 2 * size_t(n) + 1 + size_t(blob));
+}
+
+template <class T>
+__device__ __forceinline__ T warp_sum_t(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <class T>
+__global__ void __launch_bounds__(32) batch_solve_lvl(BatchDev b) {
+  extern __shared__ __align__(16) char sm[];
+  const int c = blockIdx.x, lane = threadIdx.x;
+  if (c >= b.nc) return;
+  if (b.cs[c].phase != PH_ITER || !b.lvl[c]) return;
+  const int u0 = b.uptr[c], n = b.uptr[c + 1] - u0;
+  const int64_t z0 = b.lnz_off[c];
+  const int nz = int(b.lnz_off[c + 1] - z0);
+  const int64_t s0 = b.sched_off[c];
+  const int blob = int(b.sched_off[c + 1] - s0);
+  auto a16 = [](size_t v) { return (v + 15) & ~size_t(15); };
+  T *val = (T *)sm;
+  T *rd = (T *)(sm + a16(sizeof(T) * nz));
+  T *y = (T *)(sm + a16(sizeof(T) * nz) + a16(sizeof(T) * n));
+  int *ci = (int *)(sm + a16(sizeof(T) * nz) + 2 * a16(sizeof(T) * n));
+  int *rp = ci + nz, *diag = rp + n + 1, *h = diag + n;
+  const int *grp = b.lrp + b.lrp_off[c];
+  for (int p = lane; p < nz; p += 32) {
+    const int64_t s = b.lu2a[z0 + p];
+    val[p] = s >= 0 ? T(b.jac[s]) : T(0);
+    ci[p] = b.lci[z0 + p];
+  }
+  for (int i = lane; i <= n; i += 32) rp[i] = grp[i];
+  for (int i = lane; i < n; i += 32) diag[i] = b.ldiag[u0 + i];
+  for (int i = lane; i < blob; i += 32) h[i] = b.sched[s0 + i];
+  __syncwarp();
+  const int levels = h[H_LEVELS], ulevels = h[H_ULEVELS], tail0 = h[H_TAIL0];
+  const int ntail = h[H_NTAIL], ngroups = h[H_NGROUPS], npos = h[H_NPOS], npairs = h[H_NPAIRS];
+  const int *urp = h + H_N, *upos = urp + (n + 1), *lrow = upos + h[H_NUP];
+  const int *lptr = lrow + tail0, *urow = lptr + (levels + 1), *uptr = urow + n;
+  const int *trowg = uptr + (ulevels + 1), *tgptr = trowg + (ntail + 1), *tpos = tgptr + (ngroups + 1);
+  const int *tpp = tpos + npos, *tpm = tpp + (npos + 1), *tq = tpm + npairs;
+  bool bad = false;
+  // factor: the levels, one row per lane
+  for (int lv = 0; lv < levels; ++lv) {
+    for (int t = lptr[lv] + lane; t < lptr[lv + 1]; t += 32) {
+      const int i = lrow[t];
+      const int dp = diag[i];
+      int u = urp[i];
+      for (int p = rp[i]; p < dp; ++p) {
+        const int k = ci[p];
+        const T l = val[p] * rd[k];
+        val[p] = l;
+        const int q0 = diag[k] + 1, len = rp[k + 1] - q0;
+        for (int j = 0; j < len; ++j) val[upos[u + j]] -= l * val[q0 + j];
+        u += len;
+      }
+      const T piv = val[dp];
+      bad |= bad_pivot(piv);
+      rd[i] = recip_nr(piv);
+    }
+    __syncwarp();
+  }
+  // the tail rows: positions pull their updates, group by group; a group of
+  // one position (the rail's diagonal) is summed by the whole warp
+  for (int r = 0; r < ntail; ++r) {
+    const int i = tail0 + r, dp = diag[i];
+    for (int g = trowg[r]; g < trowg[r + 1]; ++g) {
+      if (tgptr[g + 1] - tgptr[g] == 1) {
+        const int t = tgptr[g], p = tpos[t];
+        T part = T(0);
+        for (int j = tpp[t] + lane; j < tpp[t + 1]; j += 32) part += val[tpm[j]] * val[tq[j]];
+        part = warp_sum_t(part);
+        if (lane == 0) {
+          const T acc = val[p] - part;
+          val[p] = p < dp ? acc * rd[ci[p]] : acc;
+        }
+      } else {
+        for (int t = tgptr[g] + lane; t < tgptr[g + 1]; t += 32) {
+          const int p = tpos[t];
+          T acc = val[p];
+          for (int j = tpp[t]; j < tpp[t + 1]; ++j) acc -= val[tpm[j]] * val[tq[j]];
+          val[p] = p < dp ? acc * rd[ci[p]] : acc;
+        }
+      }
+      __syncwarp();
+    }
+    if (lane == 0) {
+      const T piv = val[dp];
+      bad |= bad_pivot(piv);
+      rd[i] = recip_nr(piv);
+    }
+    __syncwarp();
+  }
+  const int *P = b.lP + u0, *Q = b.lQ + u0;
+  for (int pass = 0; pass <= b.n_refine; ++pass) {
+    const double *src = pass == 0 ? b.rhs : b.r;
+    for (int k = lane; k < n; k += 32) y[k] = T(src[b.uidx[u0 + P[k]]]);
+    __syncwarp();
+    for (int lv = 0; lv < levels; ++lv) {
+      for (int t = lptr[lv] + lane; t < lptr[lv + 1]; t += 32) {
+        const int i = lrow[t];
+        T acc = y[i];
+        for (int p = rp[i]; p < diag[i]; ++p) acc -= val[p] * y[ci[p]];
+        y[i] = acc;
+      }
+      __syncwarp();
+    }
+    for (int i = tail0; i < n; ++i) {
+      T part = T(0);
+      for (int p = rp[i] + lane; p < diag[i]; p += 32) part += val[p] * y[ci[p]];
+      part = warp_sum_t(part);
+      if (lane == 0) y[i] -= part;
+      __syncwarp();
+    }
+    for (int lv = 0; lv < ulevels; ++lv) {
+      for (int t = uptr[lv] + lane; t < uptr[lv + 1]; t += 32) {
+        const int i = urow[t];
+        T acc = y[i];
+        for (int p = diag[i] + 1; p < rp[i + 1]; ++p) acc -= val[p] * y[ci[p]];
+        y[i] = acc * rd[i];
+      }
+      __syncwarp();
+    }
+    for (int k = lane; k < n; k += 32) {
+      const int g = b.uidx[u0 + Q[k]];
+      if (pass == 0) b.dx[g] = double(y[k]);
+      else b.dx[g] += double(y[k]);
+    }
+    __syncwarp();
+    if (pass < b.n_refine) {
+      for (int k = lane; k < n; k += 32) {
+        const int g = b.uidx[u0 + k];
+        double acc = b.rhs[g];
+        for (int p = b.arp[g]; p < b.arp[g + 1]; ++p) acc -= b.jac[p] * b.dx[b.aci[p]];
+        b.r[g] = acc;
+      }
+      __syncwarp();
+    }
+  }
+  double s2 = 0.0;
+  for (int k = lane; k < n; k += 32) {
+    const int g = b.uidx[u0 + k];
+    b.x[g] += b.dx[g];
+    const double t = b.dx[g] / b.w[g];
+    s2 += t * t;
+  }
+  s2 = warp_sum_d(s2);
+  const int any_bad = __any_sync(0xffffffffu, bad) ? 1 : 0;
+  if (lane == 0) {
+    b.part[c * Q_N + Q_DXW2] = s2;
+    b.part[c * Q_N + Q_LUFAIL] = any_bad;
+  }
+}
+
 // ---- batch_combine: residual, Jacobian and norms (one warp per request) ------
-__global__ void __launch_bounds__(128) batch_combine(BatchDev b) {
-  const int c = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+// One block of kBatchThreads per request (not a warp): a request of 500
+// stages has thousands of unknowns, state slots and Jacobian entries, and its
+// supply row alone has one entry per device on the rail.
+constexpr int kBatchThreads = 256;
+
+// Block-wide sum and max in a fixed order (lane butterfly, then warps in
+// order): the same result whatever the batch around the request.
+__device__ void block_sum_max(double *vals, int nsum, int nmax, double *sh) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int j = 0; j < nsum; ++j) vals[j] = warp_sum_d(vals[j]);
+  for (int j = nsum; j < nsum + nmax; ++j) vals[j] = warp_max_d(vals[j]);
+  const int m = nsum + nmax;
+  if (lane == 0)
+    for (int j = 0; j < m; ++j) sh[wid * m + j] = vals[j];
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int j = 0; j < m; ++j) {
+      double acc = sh[j];
+      for (int w = 1; w < nw; ++w) acc = j < nsum ? acc + sh[w * m + j] : fmax(acc, sh[w * m + j]);
+      vals[j] = acc;
+    }
+}
+
+// ---- batch_combine: residual, Jacobian and norms (one block per request) ------
+__global__ void __launch_bounds__(kBatchThreads) batch_combine(BatchDev b) {
+  __shared__ double sh[(kBatchThreads / 32) * 5];
+  const int c = blockIdx.x, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nw = blockDim.x >> 5;
   if (c >= b.nc) return;
   const CState &cs = b.cs[c];
   if (cs.phase == PH_DONE || cs.phase == PH_INIT) return;
   const int u0 = b.uptr[c], n = b.uptr[c + 1] - u0;
   const int order = cs.order;
   const double inv_h = 1.0 / cs.h, fs = order == 2 ? 0.5 : 1.0;
-  double s2 = 0.0, mx = 0.0, lim = 0.0, e2 = 0.0, xm = 0.0;
-  for (int k = lane; k < n; k += 32) {
+  double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};  // sums: rhs^2, err^2; maxima: rhs, limiter, x
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
     const int g = b.uidx[u0 + k];
     double r = (b.q[g] - b.qh0[g]) * inv_h;
     r = order == 2 ? r + 0.5 * b.f[g] + 0.5 * b.qh2[g] : r + b.f[g];
@@ -325,26 +541,27 @@ __global__ void __launch_bounds__(128) batch_combine(BatchDev b) {
     r += b.qvp[g] * inv_h;
     r += fs * b.fvp[g];
     b.rhs[g] = r;
-    s2 += r * r;
-    mx = fmax(mx, fabs(r));
-    lim = fmax(lim, fmax(fabs(b.fvp[g]), fabs(b.qvp[g])));
+    v[0] += r * r;
     const double e = b.x[g] - b.xn0[g];
-    e2 += e * e;
-    xm = fmax(xm, fabs(b.xc[g]));
-    for (int p = b.arp[g]; p < b.arp[g + 1]; ++p) b.jac[p] = inv_h * b.dqdx[p] + fs * b.dfdx[p];
+    v[1] += e * e;
+    v[2] = fmax(v[2], fabs(r));
+    v[3] = fmax(v[3], fmax(fabs(b.fvp[g]), fabs(b.qvp[g])));
+    v[4] = fmax(v[4], fabs(b.xc[g]));
   }
-  s2 = warp_sum_d(s2);
-  e2 = warp_sum_d(e2);
-  mx = warp_max_d(mx);
-  lim = warp_max_d(lim);
-  xm = warp_max_d(xm);
-  if (lane == 0) {
+  // the Jacobian rows: a warp per row, its lanes over the row's entries
+  for (int k = wid; k < n; k += nw) {
+    const int g = b.uidx[u0 + k];
+    for (int p = b.arp[g] + lane; p < b.arp[g + 1]; p += 32)
+      b.jac[p] = inv_h * b.dqdx[p] + fs * b.dfdx[p];
+  }
+  block_sum_max(v, 2, 3, sh);
+  if (threadIdx.x == 0) {
     double *pp = b.part + c * Q_N;
-    pp[Q_RHS2] = s2;
-    pp[Q_RHSMAX] = mx;
-    pp[Q_LIMMAX] = lim;
-    pp[Q_ERR2] = e2;
-    pp[Q_XMAX] = xm;
+    pp[Q_RHS2] = v[0];
+    pp[Q_ERR2] = v[1];
+    pp[Q_RHSMAX] = v[2];
+    pp[Q_LIMMAX] = v[3];
+    pp[Q_XMAX] = v[4];
   }
 }
 
@@ -532,15 +749,15 @@ __global__ void batch_control(BatchDev b) {
 }
 
 // ---- batch_vector: history, rotation, record, predictor (warp per request) ---
-__global__ void __launch_bounds__(128) batch_vector(BatchDev b) {
-  const int c = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+__global__ void __launch_bounds__(kBatchThreads) batch_vector(BatchDev b) {
+  const int c = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
   if (c >= b.nc) return;
   CState &cs = b.cs[c];
   const int act = cs.action;
   if (!act) return;
   const int u0 = b.uptr[c], n = b.uptr[c + 1] - u0;
   if (act & A_INIT) {
-    for (int k = lane; k < n; k += 32) {
+    for (int k = tid; k < n; k += nt) {
       const int g = b.uidx[u0 + k];
       b.xh0[g] = b.xc[g];
       b.xh1[g] = 0.0;
@@ -548,17 +765,17 @@ __global__ void __launch_bounds__(128) batch_vector(BatchDev b) {
       b.qh1[g] = -cs.h_last * b.f[g];
     }
     // the initial point is the first recorded one
-    for (int j = lane; j < b.n_out; j += 32)
+    for (int j = tid; j < b.n_out; j += nt)
       b.rec_v[(size_t)c * b.max_points * b.n_out + j] = b.xc[b.out_idx[c * b.n_out + j]];
-    if (lane == 0) {
+    if (tid == 0) {
       b.rec_t[(size_t)c * b.max_points] = 0.0;
       cs.n_rec = 1;
     }
-    __syncwarp();
+    __syncthreads();
   }
   if (act & A_ACCEPT) {
     const int order = cs.order;
-    for (int k = lane; k < n; k += 32) {
+    for (int k = tid; k < n; k += nt) {
       const int g = b.uidx[u0 + k];
       if (order == 2) {
         b.xh2[g] = b.xh1[g];
@@ -574,27 +791,27 @@ __global__ void __launch_bounds__(128) batch_vector(BatchDev b) {
     // state / store of the accepted point become current (the load kernels
     // read current and next, never last; they are ranges of slots)
     for (int k = b.sptr[c]; k < b.sptr[c + 1]; ++k)
-      for (int s = b.sidx[2 * k] + lane; s < b.sidx[2 * k] + b.sidx[2 * k + 1]; s += 32)
+      for (int s = b.sidx[2 * k] + tid; s < b.sidx[2 * k] + b.sidx[2 * k + 1]; s += nt)
         b.stac[s] = b.sta[s];
     for (int k = b.optr[c]; k < b.optr[c + 1]; ++k)
-      for (int s = b.oidx[2 * k] + lane; s < b.oidx[2 * k] + b.oidx[2 * k + 1]; s += 32)
+      for (int s = b.oidx[2 * k] + tid; s < b.oidx[2 * k] + b.oidx[2 * k + 1]; s += nt)
         b.stoc[s] = b.sto[s];
-    __syncwarp();
+    __syncthreads();
     const int np = cs.n_rec;
     if (np < b.max_points) {
-      for (int j = lane; j < b.n_out; j += 32)
+      for (int j = tid; j < b.n_out; j += nt)
         b.rec_v[((size_t)c * b.max_points + np) * b.n_out + j] = b.xc[b.out_idx[c * b.n_out + j]];
-      if (lane == 0) {
+      if (tid == 0) {
         b.rec_t[(size_t)c * b.max_points + np] = cs.t;
         cs.n_rec = np + 1;
       }
     }
   }
-  __syncwarp();
+  __syncthreads();
   if ((act & A_PREDICT) && cs.phase != PH_DONE) {
     const double b1 = cs.beta[1], b2 = cs.beta[2];
     const int order = cs.order;
-    for (int k = lane; k < n; k += 32) {
+    for (int k = tid; k < n; k += nt) {
       const int g = b.uidx[u0 + k];
       double v = b.xh0[g];
       v = b1 * b.xh1[g] + v;
@@ -606,7 +823,7 @@ __global__ void __launch_bounds__(128) batch_vector(BatchDev b) {
     // the limiters read the previous iterate from next store: start from the
     // current one (every state slot is rewritten by the next load)
     for (int k = b.optr[c]; k < b.optr[c + 1]; ++k)
-      for (int s = b.oidx[2 * k] + lane; s < b.oidx[2 * k] + b.oidx[2 * k + 1]; s += 32)
+      for (int s = b.oidx[2 * k] + tid; s < b.oidx[2 * k] + b.oidx[2 * k + 1]; s += nt)
         b.sto[s] = b.stoc[s];
   }
 }
@@ -639,6 +856,7 @@ struct xg_batch {
   int graph_iters = 0;
   int graph_launches_per_iter = 0;
   size_t solve_smem = 0;               // > 0: batch_solve_smem with this much shared memory
+  size_t solve_lvl = 0;                // > 0: batch_solve_lvl (for its requests) with this much
   int64_t bytes = 0;
   // pinned host mirror of the request states
   xg::CState *h_cs = nullptr;
@@ -859,6 +1077,11 @@ int enqueue_iteration(xg_batch *b) {
     batch_solve<double><<<blocks4, 128, 0, s>>>(b->dev);
   }
   count_launches(1);
+  if (b->solve_lvl) {
+    if (b->precision == XG_LU_FP32) batch_solve_lvl<float><<<b->nc, 32, b->solve_lvl, s>>>(b->dev);
+    else batch_solve_lvl<double><<<b->nc, 32, b->solve_lvl, s>>>(b->dev);
+    count_launches(1);
+  }
   Flags unused{};
   for (int k = 0; k < P.n_order; ++k) {
     const int t = P.order[k];
@@ -874,9 +1097,9 @@ int enqueue_iteration(xg_batch *b) {
   const ReduceArgs ra = reduce_args(P, v.io.terms, v.red_ptr, v.red_idx, v.long_out, v.short_order, out, 0, P.n_out);
   int rc = v.fma ? fast::launch_reduce(ra, s) : exact::launch_reduce(ra, s);
   if (rc) return rc;
-  batch_combine<<<blocks4, 128, 0, s>>>(b->dev);
+  batch_combine<<<b->nc, kBatchThreads, 0, s>>>(b->dev);
   batch_control<<<(b->nc + 127) / 128, 128, 0, s>>>(b->dev);
-  batch_vector<<<blocks4, 128, 0, s>>>(b->dev);
+  batch_vector<<<b->nc, kBatchThreads, 0, s>>>(b->dev);
   count_launches(3);
   return cudaGetLastError() == cudaSuccess ? XG_OK : XG_ERR_CUDA;
 }
@@ -998,8 +1221,8 @@ extern "C" int xg_batch_create(xg_ctx *ctx, int n, const xg_netlist *const *nls,
       (rc = xg_vec_download(b->ckt, XG_VEC_DQDX, dqdx.data())))
     return rc;
   if ((rc = circuit_reset_members(b->ckt))) return rc;
-  std::vector<int> lrp_off(n + 1, 0), lrp, lci, ldiag, lP, lQ;
-  std::vector<int64_t> lnz_off(n + 1, 0), lu2a;
+  std::vector<int> lrp_off(n + 1, 0), lrp, lci, ldiag, lP, lQ, sched, lvl_req(n, 0);
+  std::vector<int64_t> lnz_off(n + 1, 0), lu2a, sched_off(n + 1, 0);
   std::vector<int> g2l(NU, -1);
   for (int r = 0; r < n; ++r) {
     const int nr_ = int(l2u[r].size());
@@ -1023,11 +1246,31 @@ extern "C" int xg_batch_create(xg_ctx *ctx, int n, const xg_netlist *const *nls,
     }
     LuSymbolic S;
     std::string err;
-    // one warp walks each request's rows in order: fewest operations wins,
-    // the dependency depth does not matter, so minimum degree
-    if (lu_analyze(nr_, rp.data(), ci.data(), val.data(), 1e-3, &S, &err, 0)) {
+    // the level schedule runs each request's levels on the lanes of a warp,
+    // so the column order is chosen for depth as for a single circuit
+    if (lu_analyze(nr_, rp.data(), ci.data(), val.data(), 1e-3, &S, &err, -1)) {
       set_error("xg_batch_create: request " + std::to_string(r) + ": " + err);
       return XG_ERR_SINGULAR;
+    }
+    if (!lu_build_updates(S)) {
+      set_error("xg_batch_create: internal error, an update falls outside the L\\U pattern");
+      return XG_ERR_ARG;
+    }
+    {
+      const int hdr[H_N] = {int(S.lptr.size()) - 1, int(S.uptr.size()) - 1, S.tail0,
+                            int(S.tail_rowg.size()) - 1, int(S.tail_gptr.size()) - 1,
+                            int(S.tail_pos.size()), int(S.tail_pm.size()), int(S.upos.size())};
+      const size_t b0 = sched.size();
+      sched.insert(sched.end(), hdr, hdr + H_N);
+      for (int64_t v : S.urp) sched.push_back(int(v));
+      for (const std::vector<int> *a : {&S.upos, &S.lrow, &S.lptr, &S.urow, &S.uptr, &S.tail_rowg,
+                                        &S.tail_gptr, &S.tail_pos, &S.tail_pp, &S.tail_pm, &S.tail_q})
+        sched.insert(sched.end(), a->begin(), a->end());
+      sched_off[r + 1] = int64_t(sched.size());
+      if (int64_t(sched.size() - b0) != lvl_blob_len(nr_, hdr)) {
+        set_error("xg_batch_create: internal error in the level schedule");
+        return XG_ERR_ARG;
+      }
     }
     lrp_off[r + 1] = lrp_off[r] + nr_ + 1;
     lnz_off[r + 1] = lnz_off[r] + S.rp[nr_];
@@ -1055,7 +1298,8 @@ extern "C" int xg_batch_create(xg_ctx *ctx, int n, const xg_netlist *const *nls,
   d.n_refine = o->lu_precision == XG_LU_FP32 ? o->n_refine : 0;
   int *t_uptr, *t_uidx, *t_sptr, *t_sidx, *t_optr, *t_oidx, *t_lrp_off, *t_lrp, *t_lci, *t_ldiag,
       *t_lP, *t_lQ, *t_out, *t_arp, *t_aci;
-  int64_t *t_lnz_off, *t_lu2a;
+  int64_t *t_lnz_off, *t_lu2a, *t_sched_off;
+  int *t_sched, *t_lvl;
   if (dev_copy(b.get(), &t_uptr, uptr) || dev_copy(b.get(), &t_uidx, uidx) ||
       dev_copy(b.get(), &t_sptr, sptr) || dev_copy(b.get(), &t_sidx, sidx) ||
       dev_copy(b.get(), &t_optr, optr) || dev_copy(b.get(), &t_oidx, oidx) ||
@@ -1073,9 +1317,46 @@ extern "C" int xg_batch_create(xg_ctx *ctx, int n, const xg_netlist *const *nls,
   d.lci = t_lci; d.ldiag = t_ldiag; d.lu2a = t_lu2a; d.lP = t_lP; d.lQ = t_lQ; d.out_idx = t_out;
   const size_t tsz = o->lu_precision == XG_LU_FP32 ? sizeof(float) : sizeof(double);
   {
+    // requests whose level schedule fits in shared memory use it
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    size_t need_lvl = 0;
+    if (!std::getenv("XG_BATCH_NO_LVL"))
+      for (int r = 0; r < n; ++r) {
+        const size_t sb = smem_bytes_lvl(uptr[r + 1] - uptr[r], lnz_off[r + 1] - lnz_off[r],
+                                         sched_off[r + 1] - sched_off[r], tsz);
+        if (sb + 1024 <= size_t(optin)) {
+          lvl_req[r] = 1;
+          need_lvl = std::max(need_lvl, sb);
+        }
+      }
+    if (need_lvl) {
+      cudaError_t e = o->lu_precision == XG_LU_FP32
+                          ? cudaFuncSetAttribute(batch_solve_lvl<float>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(need_lvl))
+                          : cudaFuncSetAttribute(batch_solve_lvl<double>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(need_lvl));
+      if (e == cudaSuccess) {
+        b->solve_lvl = need_lvl;
+      } else {
+        cudaGetLastError();
+        std::fill(lvl_req.begin(), lvl_req.end(), 0);
+      }
+    }
+    if (dev_copy(b.get(), &t_sched_off, sched_off) || dev_copy(b.get(), &t_sched, sched) ||
+        dev_copy(b.get(), &t_lvl, lvl_req)) {
+      set_error("xg_batch_create: out of device memory");
+      return XG_ERR_OOM;
+    }
+    d.sched_off = t_sched_off;
+    d.sched = t_sched;
+    d.lvl = t_lvl;
+  }
+  {
     size_t need = 0;
     for (int r = 0; r < n; ++r)
-      need = std::max(need, smem_bytes_request(uptr[r + 1] - uptr[r], lnz_off[r + 1] - lnz_off[r], tsz));
+      if (!lvl_req[r])
+        need = std::max(need, smem_bytes_request(uptr[r + 1] - uptr[r], lnz_off[r + 1] - lnz_off[r], tsz));
     int optin = 0;
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
     if (need + 1024 <= size_t(optin) && !std::getenv("XG_BATCH_NO_SMEM")) {
