@@ -268,7 +268,9 @@ def run_serve(args, world, rank, local, dist):
     from xyce_gb300 import engine, serve
     torch.cuda.set_device(local)
     w = WORKLOADS[args.workload]
-    ctx = engine.Context(local, abi.device_options())
+    # as for the transients: the FMA load build (long sums split over a warp)
+    # unless --exact-load
+    ctx = engine.Context(local, abi.device_options(fma=0 if args.exact_load else 1))
     L = engine.lib()
 
     def one(prec, nref):
@@ -314,6 +316,8 @@ def run_serve(args, world, rank, local, dist):
         "data": "synthetic (seeded Monte-Carlo ring oscillators, Poisson arrivals)",
         "config": {"workload": args.workload, "requests": w["n"], "rate_per_s": w["rate"],
                    "stages": "5-501 odd", "tstop": w["tstop"], "lu": "fp32 + 1 fp64 refinement",
+                   "load_build": "exact (reference rounding)" if args.exact_load
+                   else "fma, long sums split over a warp",
                    "l2": "per-request working sets below L2"},
         "p50_ms": float(np.mean([r[0]["p50_ms"] for r in runs])),
         "p99_ms": float(np.mean([r[0]["p99_ms"] for r in runs])),
@@ -322,7 +326,7 @@ def run_serve(args, world, rank, local, dist):
         "newton_iters_per_s": float(np.mean([r[0]["newton_iters_per_s"] for r in runs])),
         "roofline": {"kernel": "batch iteration", "bound": "hbm", "achieved": None, "peak": measured_peaks()[0],
                      "unit": "GB/s", "frac": None, "traffic": None,
-                     "note": "latency-bound: one warp walks each request's factor"},
+                     "note": "latency-bound: each request's factor runs level by level on one warp"},
         "e2e": {"value": value, "unit": "solves/s",
                 "h2d_bytes_per_step": int(sum(8 * len(r.x0) for r in runs[0][1])),
                 "d2h_bytes_per_step": int(sum(r.result[1].nbytes + r.result[0].nbytes for r in runs[0][1]))},

@@ -29,12 +29,14 @@
 
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <cfloat>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "xg.h"
@@ -1223,12 +1225,21 @@ extern "C" int xg_batch_create(xg_ctx *ctx, int n, const xg_netlist *const *nls,
   if ((rc = circuit_reset_members(b->ckt))) return rc;
   std::vector<int> lrp_off(n + 1, 0), lrp, lci, ldiag, lP, lQ, sched, lvl_req(n, 0);
   std::vector<int64_t> lnz_off(n + 1, 0), lu2a, sched_off(n + 1, 0);
-  std::vector<int> g2l(NU, -1);
-  for (int r = 0; r < n; ++r) {
+  // Each request's analysis is independent: analyse them on the host's cores,
+  // then concatenate in request order.
+  struct ReqLU {
+    LuSymbolic S;
+    std::vector<int64_t> gpos;
+    std::vector<int> blob;
+    int rc = XG_OK;
+    std::string err;
+  };
+  std::vector<ReqLU> req(n);
+  auto analyse = [&](int r, std::vector<int> &g2l) {
+    ReqLU &R = req[r];
     const int nr_ = int(l2u[r].size());
     for (int k = 0; k < nr_; ++k) g2l[l2u[r][k]] = k;
     std::vector<int> rp(nr_ + 1, 0), ci;
-    std::vector<int64_t> gpos;
     std::vector<double> val;
     for (int k = 0; k < nr_; ++k) {
       const int g = l2u[r][k];
@@ -1237,50 +1248,73 @@ extern "C" int xg_batch_create(xg_ctx *ctx, int n, const xg_netlist *const *nls,
       std::sort(row.begin(), row.end());
       for (auto &e : row) {
         ci.push_back(e.first);
-        gpos.push_back(e.second);
+        R.gpos.push_back(e.second);
         double a = dfdx[e.second] + dqdx[e.second] / tstep;
         if (e.first == k && a == 0.0) a = 1e-12;
         val.push_back(a);
       }
       rp[k + 1] = int(ci.size());
     }
-    LuSymbolic S;
-    std::string err;
+    LuSymbolic &S = R.S;
     // the level schedule runs each request's levels on the lanes of a warp,
     // so the column order is chosen for depth as for a single circuit
-    if (lu_analyze(nr_, rp.data(), ci.data(), val.data(), 1e-3, &S, &err, -1)) {
-      set_error("xg_batch_create: request " + std::to_string(r) + ": " + err);
-      return XG_ERR_SINGULAR;
+    if (lu_analyze(nr_, rp.data(), ci.data(), val.data(), 1e-3, &S, &R.err, -1)) {
+      R.rc = XG_ERR_SINGULAR;
+      R.err = "xg_batch_create: request " + std::to_string(r) + ": " + R.err;
+      return;
     }
     if (!lu_build_updates(S)) {
-      set_error("xg_batch_create: internal error, an update falls outside the L\\U pattern");
-      return XG_ERR_ARG;
+      R.rc = XG_ERR_ARG;
+      R.err = "xg_batch_create: internal error, an update falls outside the L\\U pattern";
+      return;
     }
-    {
-      const int hdr[H_N] = {int(S.lptr.size()) - 1, int(S.uptr.size()) - 1, S.tail0,
-                            int(S.tail_rowg.size()) - 1, int(S.tail_gptr.size()) - 1,
-                            int(S.tail_pos.size()), int(S.tail_pm.size()), int(S.upos.size())};
-      const size_t b0 = sched.size();
-      sched.insert(sched.end(), hdr, hdr + H_N);
-      for (int64_t v : S.urp) sched.push_back(int(v));
-      for (const std::vector<int> *a : {&S.upos, &S.lrow, &S.lptr, &S.urow, &S.uptr, &S.tail_rowg,
-                                        &S.tail_gptr, &S.tail_pos, &S.tail_pp, &S.tail_pm, &S.tail_q})
-        sched.insert(sched.end(), a->begin(), a->end());
-      sched_off[r + 1] = int64_t(sched.size());
-      if (int64_t(sched.size() - b0) != lvl_blob_len(nr_, hdr)) {
-        set_error("xg_batch_create: internal error in the level schedule");
-        return XG_ERR_ARG;
-      }
+    const int hdr[H_N] = {int(S.lptr.size()) - 1, int(S.uptr.size()) - 1, S.tail0,
+                          int(S.tail_rowg.size()) - 1, int(S.tail_gptr.size()) - 1,
+                          int(S.tail_pos.size()), int(S.tail_pm.size()), int(S.upos.size())};
+    R.blob.assign(hdr, hdr + H_N);
+    for (int64_t v : S.urp) R.blob.push_back(int(v));
+    for (const std::vector<int> *a : {&S.upos, &S.lrow, &S.lptr, &S.urow, &S.uptr, &S.tail_rowg,
+                                      &S.tail_gptr, &S.tail_pos, &S.tail_pp, &S.tail_pm, &S.tail_q})
+      R.blob.insert(R.blob.end(), a->begin(), a->end());
+    if (int64_t(R.blob.size()) != lvl_blob_len(nr_, hdr)) {
+      R.rc = XG_ERR_ARG;
+      R.err = "xg_batch_create: internal error in the level schedule";
     }
+    std::vector<int64_t>().swap(S.urp);
+    std::vector<int>().swap(S.upos);
+  };
+  {
+    const int nthreads = std::max(1, std::min<int>(std::min(16, n), int(std::thread::hardware_concurrency())));
+    std::atomic<int> next{0};
+    auto worker = [&]() {
+      std::vector<int> g2l(NU, -1);
+      for (int r = next++; r < n; r = next++) analyse(r, g2l);
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nthreads; ++t) pool.emplace_back(worker);
+    worker();
+    for (auto &t : pool) t.join();
+  }
+  for (int r = 0; r < n; ++r) {
+    const ReqLU &R = req[r];
+    if (R.rc) {
+      set_error(R.err);
+      return R.rc;
+    }
+    const LuSymbolic &S = R.S;
+    const int nr_ = int(l2u[r].size());
+    sched.insert(sched.end(), R.blob.begin(), R.blob.end());
+    sched_off[r + 1] = int64_t(sched.size());
     lrp_off[r + 1] = lrp_off[r] + nr_ + 1;
     lnz_off[r + 1] = lnz_off[r] + S.rp[nr_];
     lrp.insert(lrp.end(), S.rp.begin(), S.rp.end());
     lci.insert(lci.end(), S.ci.begin(), S.ci.end());
     ldiag.insert(ldiag.end(), S.diag.begin(), S.diag.end());
-    for (int a : S.lu2a) lu2a.push_back(a >= 0 ? gpos[a] : -1);
+    for (int a : S.lu2a) lu2a.push_back(a >= 0 ? R.gpos[a] : -1);
     lP.insert(lP.end(), S.P.begin(), S.P.end());
     lQ.insert(lQ.end(), S.Q.begin(), S.Q.end());
   }
+  std::vector<ReqLU>().swap(req);
   std::vector<int> outs((size_t)n * std::max(1, o->n_out), 0);
   for (int r = 0; r < n; ++r)
     for (int j = 0; j < o->n_out; ++j) {
