@@ -216,16 +216,22 @@ class Netlist:
         nm = len(self.models)
         allv = _darr([v for m in self.models for v in m.params.values()] or [0.0])
         mods = np.zeros(max(1, nm), dtype=_MODEL_DTYPE)
-        off = 0
-        for i, m in enumerate(self.models):
-            key = tuple(m.params)
-            names = _NAME_ARRAYS.get(key)
-            if names is None:
-                names = (C.c_char_p * max(1, len(key)))(*[k.encode() for k in key])
-                _NAME_ARRAYS[key] = (names, C.addressof(names))
-                names = _NAME_ARRAYS[key]
-            mods[i] = (m.type, m.polarity, len(key), 0, names[1], allv.ctypes.data + 8 * off)
-            off += len(key)
+        if nm:
+            name_addr = np.empty(nm, np.uint64)
+            for i, m in enumerate(self.models):
+                key = tuple(m.params)
+                names = _NAME_ARRAYS.get(key)
+                if names is None:
+                    arr_ = (C.c_char_p * max(1, len(key)))(*[k.encode() for k in key])
+                    names = _NAME_ARRAYS[key] = (arr_, C.addressof(arr_))
+                name_addr[i] = names[1]
+            lens = np.fromiter((len(m.params) for m in self.models), np.int64, nm)
+            offs = np.concatenate(([0], np.cumsum(lens)[:-1]))
+            mods["type"][:nm] = np.fromiter((m.type for m in self.models), np.int32, nm)
+            mods["polarity"][:nm] = np.fromiter((m.polarity for m in self.models), np.int32, nm)
+            mods["n_params"][:nm] = lens
+            mods["names"][:nm] = name_addr
+            mods["values"][:nm] = np.uint64(allv.ctypes.data) + (8 * offs).astype(np.uint64)
         keep += [allv, mods]
         nl.n_models = nm
         nl.models = C.cast(mods.ctypes.data, C.POINTER(XgModelDesc))

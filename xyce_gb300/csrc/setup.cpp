@@ -14,12 +14,14 @@
 // reference computes it.
 
 #include <algorithm>
+#include <atomic>
 #include <cctype>
 #include <cmath>
 #include <cstring>
 #include <map>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "xg_internal.h"
@@ -86,6 +88,42 @@ const TypeLayout &type_layout(int t) {
       {b3_nlid(), b3_nterm(), b3_terms(), XG_B3_NPARAMS, 12, 5},
   };
   return L[t];
+}
+
+// Runs f(i, scratch, err) for i in [0, n) on the host's cores, in fixed
+// chunks of 1,024, each worker with its own scratch of np doubles.  Returns
+// the error of the lowest failing i, as the serial loop would.  Set-up of a
+// batch union or a million-device netlist is per model and per instance.
+template <class F>
+int parallel_rows(int n, int np, F f, std::string *err) {
+  constexpr int kChunk = 1024;
+  const int nchunks = (n + kChunk - 1) / kChunk;
+  const int hw = int(std::thread::hardware_concurrency());
+  const int nt = std::max(1, std::min(std::min(nchunks, 16), hw > 0 ? hw : 1));
+  std::vector<int> rc(size_t(std::max(nchunks, 1)), 0);
+  std::vector<std::string> msg(size_t(std::max(nchunks, 1)));
+  std::atomic<int> next{0};
+  auto work = [&]() {
+    std::vector<double> tmp(size_t(std::max(np, 1)));
+    for (int c = next++; c < nchunks; c = next++)
+      for (int i = c * kChunk; i < std::min(n, (c + 1) * kChunk); ++i) {
+        const int r = f(i, tmp.data(), &msg[size_t(c)]);
+        if (r) {
+          rc[size_t(c)] = r;
+          break;
+        }
+      }
+  };
+  std::vector<std::thread> pool;
+  for (int k = 1; k < nt; ++k) pool.emplace_back(work);
+  work();
+  for (auto &th : pool) th.join();
+  for (int c = 0; c < nchunks; ++c)
+    if (rc[size_t(c)]) {
+      *err = msg[size_t(c)];
+      return rc[size_t(c)];
+    }
+  return XG_OK;
 }
 
 // ---- model cards -----------------------------------------------------------
@@ -537,15 +575,18 @@ int build_plan(const xg_netlist *nl, const xg_device_options *opt, Plan *plan, s
   std::vector<DiodeModel> diode_models(nl->n_models);
   std::vector<B3Model> b3_models(nl->n_models);
   std::vector<int> model_ok(nl->n_models, 0);
-  for (int mi = 0; mi < nl->n_models; ++mi) {
-    const xg_model_desc &md = nl->models[mi];
-    int rc = XG_OK;
-    if (md.type == XG_DEV_MOS1) rc = make_mos1_model(md, *opt, &mos1_models[mi], err);
-    else if (md.type == XG_DEV_DIODE) rc = make_diode_model(md, *opt, &diode_models[mi], err);
-    else if (md.type == XG_DEV_BSIM3) rc = b3_make_model(md, *opt, &b3_models[mi], err);
-    else { *err = "model of unsupported device type"; rc = XG_ERR_UNSUPPORTED; }
+  {
+    int rc = parallel_rows(nl->n_models, 0, [&](int mi, double *, std::string *e) {
+      const xg_model_desc &md = nl->models[mi];
+      int r = XG_OK;
+      if (md.type == XG_DEV_MOS1) r = make_mos1_model(md, *opt, &mos1_models[mi], e);
+      else if (md.type == XG_DEV_DIODE) r = make_diode_model(md, *opt, &diode_models[mi], e);
+      else if (md.type == XG_DEV_BSIM3) r = b3_make_model(md, *opt, &b3_models[mi], e);
+      else { *e = "model of unsupported device type"; r = XG_ERR_UNSUPPORTED; }
+      if (!r) model_ok[mi] = md.type;
+      return r;
+    }, err);
     if (rc) return rc;
-    model_ok[mi] = md.type;
   }
   auto check_model = [&](int mi, int type) {
     return mi >= 0 && mi < nl->n_models && model_ok[mi] == type;
@@ -563,67 +604,66 @@ int build_plan(const xg_netlist *nl, const xg_device_options *opt, Plan *plan, s
     T.nsto = L.nsto;
     if (!T.n) continue;
     T.params.assign((size_t)T.np * T.n, 0.0);
-    std::vector<double> tmp(T.np);
-    auto put = [&](int i) {
-      for (int k = 0; k < T.np; ++k) T.params[(size_t)k * T.n + i] = tmp[k];
-    };
-    for (int i = 0; i < T.n; ++i) {
+    auto row = [&](int i, double *tmp, std::string *e) -> int {
+      auto bad_node = [&]() {
+        *e = "node index out of range";
+        return XG_ERR_ARG;
+      };
       switch (t) {
         case XG_DEV_RES: {
-          if (!node_ok(nl->res.p[i], P.n_nodes) || !node_ok(nl->res.m[i], P.n_nodes)) goto badnode;
+          if (!node_ok(nl->res.p[i], P.n_nodes) || !node_ok(nl->res.m[i], P.n_nodes)) return bad_node();
           double R = nl->res.value[i], factor = 1.0;  // N_DEV_Resistor.C:852-860
           tmp[XG_R_G] = (R * factor != 0.0) ? 1.0 / (R * factor) : 0.0;
           break;
         }
         case XG_DEV_CAP:
-          if (!node_ok(nl->cap.p[i], P.n_nodes) || !node_ok(nl->cap.m[i], P.n_nodes)) goto badnode;
+          if (!node_ok(nl->cap.p[i], P.n_nodes) || !node_ok(nl->cap.m[i], P.n_nodes)) return bad_node();
           tmp[XG_C_C] = nl->cap.value[i];
           break;
         case XG_DEV_VSRC:
         case XG_DEV_ISRC: {
           // Same source data for both (N_DEV_SourceData.C): the DC value, or PULSE's seven.
           const xg_src_desc &d = t == XG_DEV_VSRC ? nl->vsrc : nl->isrc;
-          if (!node_ok(d.p[i], P.n_nodes) || !node_ok(d.m[i], P.n_nodes)) goto badnode;
+          if (!node_ok(d.p[i], P.n_nodes) || !node_ok(d.m[i], P.n_nodes)) return bad_node();
           const double *w = d.wave + 7 * (size_t)i;
           int kind = d.kind[i];
-          if (kind != XG_SRC_DC && kind != XG_SRC_PULSE) { *err = "bad source kind"; return XG_ERR_ARG; }
+          if (kind != XG_SRC_DC && kind != XG_SRC_PULSE) { *e = "bad source kind"; return XG_ERR_ARG; }
           tmp[XG_V_KIND] = kind;
           for (int k = 0; k < 7; ++k) tmp[XG_V_V1 + k] = kind == XG_SRC_PULSE || k == 0 ? w[k] : 0.0;
           break;
         }
         case XG_DEV_DIODE: {
-          if (!node_ok(nl->diode.a[i], P.n_nodes) || !node_ok(nl->diode.c[i], P.n_nodes)) goto badnode;
+          if (!node_ok(nl->diode.a[i], P.n_nodes) || !node_ok(nl->diode.c[i], P.n_nodes)) return bad_node();
           int mi = nl->diode.model[i];
-          if (!check_model(mi, XG_DEV_DIODE)) { *err = "diode references a non-diode model"; return XG_ERR_ARG; }
-          diode_instance_params(diode_models[mi], nl->diode, i, *opt, tmp.data());
+          if (!check_model(mi, XG_DEV_DIODE)) { *e = "diode references a non-diode model"; return XG_ERR_ARG; }
+          diode_instance_params(diode_models[mi], nl->diode, i, *opt, tmp);
           break;
         }
         case XG_DEV_MOS1: {
           const xg_mos_desc &d = nl->mos1;
           if (!node_ok(d.d[i], P.n_nodes) || !node_ok(d.g[i], P.n_nodes) ||
-              !node_ok(d.s[i], P.n_nodes) || !node_ok(d.b[i], P.n_nodes)) goto badnode;
+              !node_ok(d.s[i], P.n_nodes) || !node_ok(d.b[i], P.n_nodes)) return bad_node();
           int mi = d.model[i];
-          if (!check_model(mi, XG_DEV_MOS1)) { *err = "MOSFET references a non-level-1 model"; return XG_ERR_ARG; }
-          mos1_instance_params(mos1_models[mi], d, i, *opt, tmp.data());
+          if (!check_model(mi, XG_DEV_MOS1)) { *e = "MOSFET references a non-level-1 model"; return XG_ERR_ARG; }
+          mos1_instance_params(mos1_models[mi], d, i, *opt, tmp);
           break;
         }
         case XG_DEV_BSIM3: {
           const xg_mos_desc &d = nl->bsim3;
           if (!node_ok(d.d[i], P.n_nodes) || !node_ok(d.g[i], P.n_nodes) ||
-              !node_ok(d.s[i], P.n_nodes) || !node_ok(d.b[i], P.n_nodes)) goto badnode;
+              !node_ok(d.s[i], P.n_nodes) || !node_ok(d.b[i], P.n_nodes)) return bad_node();
           int mi = d.model[i];
-          if (!check_model(mi, XG_DEV_BSIM3)) { *err = "MOSFET references a non-BSIM3 model"; return XG_ERR_ARG; }
-          int rc = b3_instance_params(b3_models[mi], d, i, *opt, tmp.data(), err);
+          if (!check_model(mi, XG_DEV_BSIM3)) { *e = "MOSFET references a non-BSIM3 model"; return XG_ERR_ARG; }
+          int rc = b3_instance_params(b3_models[mi], d, i, *opt, tmp, e);
           if (rc) return rc;
           break;
         }
       }
-      put(i);
-    }
-    continue;
-  badnode:
-    *err = "node index out of range";
-    return XG_ERR_ARG;
+      for (int k = 0; k < T.np; ++k) T.params[(size_t)k * T.n + i] = tmp[k];
+      return XG_OK;
+    };
+    const int rc = parallel_rows(T.n, T.np, row, err);
+    if (rc) return rc;
   }
   if (params_only) return XG_OK;
 
