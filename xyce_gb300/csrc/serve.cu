@@ -353,10 +353,12 @@ __device__ __forceinline__ T warp_sum_t(T v) {
   return v;
 }
 
+constexpr int kLvlThreads = 128;  // threads per request in batch_solve_lvl
+
 template <class T>
-__global__ void __launch_bounds__(32) batch_solve_lvl(BatchDev b) {
+__global__ void __launch_bounds__(kLvlThreads) batch_solve_lvl(BatchDev b) {
   extern __shared__ __align__(16) char sm[];
-  const int c = blockIdx.x, lane = threadIdx.x;
+  const int c = blockIdx.x, lane = threadIdx.x & 31, tid = threadIdx.x, nt = blockDim.x;
   if (c >= b.nc) return;
   if (b.cs[c].phase != PH_ITER || !b.lvl[c]) return;
   const int u0 = b.uptr[c], n = b.uptr[c + 1] - u0;
@@ -371,15 +373,15 @@ __global__ void __launch_bounds__(32) batch_solve_lvl(BatchDev b) {
   int *ci = (int *)(sm + a16(sizeof(T) * nz) + 2 * a16(sizeof(T) * n));
   int *rp = ci + nz, *diag = rp + n + 1, *h = diag + n;
   const int *grp = b.lrp + b.lrp_off[c];
-  for (int p = lane; p < nz; p += 32) {
+  for (int p = tid; p < nz; p += nt) {
     const int64_t s = b.lu2a[z0 + p];
     val[p] = s >= 0 ? T(b.jac[s]) : T(0);
     ci[p] = b.lci[z0 + p];
   }
-  for (int i = lane; i <= n; i += 32) rp[i] = grp[i];
-  for (int i = lane; i < n; i += 32) diag[i] = b.ldiag[u0 + i];
-  for (int i = lane; i < blob; i += 32) h[i] = b.sched[s0 + i];
-  __syncwarp();
+  for (int i = tid; i <= n; i += nt) rp[i] = grp[i];
+  for (int i = tid; i < n; i += nt) diag[i] = b.ldiag[u0 + i];
+  for (int i = tid; i < blob; i += nt) h[i] = b.sched[s0 + i];
+  __syncthreads();
   const int levels = h[H_LEVELS], ulevels = h[H_ULEVELS], tail0 = h[H_TAIL0];
   const int ntail = h[H_NTAIL], ngroups = h[H_NGROUPS], npos = h[H_NPOS], npairs = h[H_NPAIRS];
   const int *urp = h + H_N, *upos = urp + (n + 1), *lrow = upos + h[H_NUP];
@@ -389,7 +391,7 @@ __global__ void __launch_bounds__(32) batch_solve_lvl(BatchDev b) {
   bool bad = false;
   // factor: the levels, one row per lane
   for (int lv = 0; lv < levels; ++lv) {
-    for (int t = lptr[lv] + lane; t < lptr[lv + 1]; t += 32) {
+    for (int t = lptr[lv] + tid; t < lptr[lv + 1]; t += nt) {
       const int i = lrow[t];
       const int dp = diag[i];
       int u = urp[i];
@@ -405,7 +407,7 @@ __global__ void __launch_bounds__(32) batch_solve_lvl(BatchDev b) {
       bad |= bad_pivot(piv);
       rd[i] = recip_nr(piv);
     }
-    __syncwarp();
+    __syncthreads();
   }
   // the tail rows: positions pull their updates, group by group; a group of
   // one position (the rail's diagonal) is summed by the whole warp
@@ -413,88 +415,96 @@ __global__ void __launch_bounds__(32) batch_solve_lvl(BatchDev b) {
     const int i = tail0 + r, dp = diag[i];
     for (int g = trowg[r]; g < trowg[r + 1]; ++g) {
       if (tgptr[g + 1] - tgptr[g] == 1) {
-        const int t = tgptr[g], p = tpos[t];
-        T part = T(0);
-        for (int j = tpp[t] + lane; j < tpp[t + 1]; j += 32) part += val[tpm[j]] * val[tq[j]];
-        part = warp_sum_t(part);
-        if (lane == 0) {
-          const T acc = val[p] - part;
-          val[p] = p < dp ? acc * rd[ci[p]] : acc;
+        if (tid < 32) {
+          const int t = tgptr[g], p = tpos[t];
+          T part = T(0);
+          for (int j = tpp[t] + lane; j < tpp[t + 1]; j += 32) part += val[tpm[j]] * val[tq[j]];
+          part = warp_sum_t(part);
+          if (lane == 0) {
+            const T acc = val[p] - part;
+            val[p] = p < dp ? acc * rd[ci[p]] : acc;
+          }
         }
       } else {
-        for (int t = tgptr[g] + lane; t < tgptr[g + 1]; t += 32) {
+        for (int t = tgptr[g] + tid; t < tgptr[g + 1]; t += nt) {
           const int p = tpos[t];
           T acc = val[p];
           for (int j = tpp[t]; j < tpp[t + 1]; ++j) acc -= val[tpm[j]] * val[tq[j]];
           val[p] = p < dp ? acc * rd[ci[p]] : acc;
         }
       }
-      __syncwarp();
+      __syncthreads();
     }
-    if (lane == 0) {
+    if (tid == 0) {
       const T piv = val[dp];
       bad |= bad_pivot(piv);
       rd[i] = recip_nr(piv);
     }
-    __syncwarp();
+    __syncthreads();
   }
   const int *P = b.lP + u0, *Q = b.lQ + u0;
   for (int pass = 0; pass <= b.n_refine; ++pass) {
     const double *src = pass == 0 ? b.rhs : b.r;
-    for (int k = lane; k < n; k += 32) y[k] = T(src[b.uidx[u0 + P[k]]]);
-    __syncwarp();
+    for (int k = tid; k < n; k += nt) y[k] = T(src[b.uidx[u0 + P[k]]]);
+    __syncthreads();
     for (int lv = 0; lv < levels; ++lv) {
-      for (int t = lptr[lv] + lane; t < lptr[lv + 1]; t += 32) {
+      for (int t = lptr[lv] + tid; t < lptr[lv + 1]; t += nt) {
         const int i = lrow[t];
         T acc = y[i];
         for (int p = rp[i]; p < diag[i]; ++p) acc -= val[p] * y[ci[p]];
         y[i] = acc;
       }
-      __syncwarp();
+      __syncthreads();
     }
-    for (int i = tail0; i < n; ++i) {
-      T part = T(0);
-      for (int p = rp[i] + lane; p < diag[i]; p += 32) part += val[p] * y[ci[p]];
-      part = warp_sum_t(part);
-      if (lane == 0) y[i] -= part;
-      __syncwarp();
-    }
+    if (tid < 32)
+      for (int i = tail0; i < n; ++i) {
+        T part = T(0);
+        for (int p = rp[i] + lane; p < diag[i]; p += 32) part += val[p] * y[ci[p]];
+        part = warp_sum_t(part);
+        if (lane == 0) y[i] -= part;
+        __syncwarp();
+      }
+    __syncthreads();
     for (int lv = 0; lv < ulevels; ++lv) {
-      for (int t = uptr[lv] + lane; t < uptr[lv + 1]; t += 32) {
+      for (int t = uptr[lv] + tid; t < uptr[lv + 1]; t += nt) {
         const int i = urow[t];
         T acc = y[i];
         for (int p = diag[i] + 1; p < rp[i + 1]; ++p) acc -= val[p] * y[ci[p]];
         y[i] = acc * rd[i];
       }
-      __syncwarp();
+      __syncthreads();
     }
-    for (int k = lane; k < n; k += 32) {
+    for (int k = tid; k < n; k += nt) {
       const int g = b.uidx[u0 + Q[k]];
       if (pass == 0) b.dx[g] = double(y[k]);
       else b.dx[g] += double(y[k]);
     }
-    __syncwarp();
+    __syncthreads();
     if (pass < b.n_refine) {
-      for (int k = lane; k < n; k += 32) {
+      for (int k = tid; k < n; k += nt) {
         const int g = b.uidx[u0 + k];
         double acc = b.rhs[g];
         for (int p = b.arp[g]; p < b.arp[g + 1]; ++p) acc -= b.jac[p] * b.dx[b.aci[p]];
         b.r[g] = acc;
       }
-      __syncwarp();
+      __syncthreads();
     }
   }
+  __shared__ double sh[kLvlThreads / 32];
   double s2 = 0.0;
-  for (int k = lane; k < n; k += 32) {
+  for (int k = tid; k < n; k += nt) {
     const int g = b.uidx[u0 + k];
     b.x[g] += b.dx[g];
     const double t = b.dx[g] / b.w[g];
     s2 += t * t;
   }
   s2 = warp_sum_d(s2);
-  const int any_bad = __any_sync(0xffffffffu, bad) ? 1 : 0;
-  if (lane == 0) {
-    b.part[c * Q_N + Q_DXW2] = s2;
+  if (lane == 0) sh[tid >> 5] = s2;
+  const int any_bad = __syncthreads_or(bad ? 1 : 0) ? 1 : 0;
+  if (tid == 0) {
+    double acc = sh[0];
+    for (int w = 1; w < nt / 32; ++w) acc += sh[w];
+    b.part[c * Q_N + Q_DXW2] = acc;
     b.part[c * Q_N + Q_LUFAIL] = any_bad;
   }
 }
@@ -1080,8 +1090,10 @@ int enqueue_iteration(xg_batch *b) {
   }
   count_launches(1);
   if (b->solve_lvl) {
-    if (b->precision == XG_LU_FP32) batch_solve_lvl<float><<<b->nc, 32, b->solve_lvl, s>>>(b->dev);
-    else batch_solve_lvl<double><<<b->nc, 32, b->solve_lvl, s>>>(b->dev);
+    if (b->precision == XG_LU_FP32)
+      batch_solve_lvl<float><<<b->nc, kLvlThreads, b->solve_lvl, s>>>(b->dev);
+    else
+      batch_solve_lvl<double><<<b->nc, kLvlThreads, b->solve_lvl, s>>>(b->dev);
     count_launches(1);
   }
   Flags unused{};
