@@ -167,3 +167,71 @@ class Server:
                 "p50_ms": float(np.percentile(lat, 50) * 1e3),
                 "p99_ms": float(np.percentile(lat, 99) * 1e3),
                 "mean_ms": float(lat.mean() * 1e3), "failed": failed}
+
+
+class Autotuner:
+    """Picks the server's batch schedule (requests per batch, batch iterations
+    per launch chunk, batches in flight) by measuring it: one parameter at a
+    time, each candidate serving the same probe stream, keeping the value
+    with the most solves/s.  `serve` is called as serve(params, requests,
+    arrivals) and returns Server.run's summary; the probe's requests are
+    rebuilt for every trial by `make_requests`.  Results can be kept in a
+    JSON file keyed by the device and the workload, so a server starts from
+    the last tuned schedule."""
+
+    GRID = {"max_batch": (128, 256, 512, 1024), "chunk": (16, 64, 256), "max_concurrent": (2, 4, 8)}
+    START = {"max_batch": 512, "chunk": 64, "max_concurrent": 8}
+
+    def __init__(self, serve, make_requests, grid=None, start=None, cache_path=None, key=None):
+        self.serve, self.make_requests = serve, make_requests
+        self.grid = dict(grid or self.GRID)
+        self.best = dict(start or self.START)
+        self.cache_path, self.key = cache_path, key
+        self.trials = []
+
+    def _cached(self):
+        import json
+        import os
+        if not self.cache_path or not self.key or not os.path.exists(self.cache_path):
+            return None
+        with open(self.cache_path) as f:
+            return json.load(f).get(self.key)
+
+    def _store(self):
+        import json
+        import os
+        if not self.cache_path or not self.key:
+            return
+        data = {}
+        if os.path.exists(self.cache_path):
+            with open(self.cache_path) as f:
+                data = json.load(f)
+        data[self.key] = self.best
+        with open(self.cache_path, "w") as f:
+            json.dump(data, f, indent=1, sort_keys=True)
+
+    def _score(self, params):
+        key = tuple(sorted(params.items()))
+        for p, sc in self.trials:
+            if tuple(sorted(p.items())) == key:
+                return sc
+        reqs, arr = self.make_requests()
+        res = self.serve(params, reqs, arr)
+        self.trials.append((dict(params), res["solves_per_s"]))
+        return res["solves_per_s"]
+
+    def tune(self):
+        hit = self._cached()
+        if hit is not None:
+            self.best = dict(hit)
+            return self.best
+        best_score = self._score(self.best)
+        for name, values in self.grid.items():
+            base = dict(self.best)
+            for v in values:
+                trial = dict(base, **{name: v})
+                sc = self._score(trial)
+                if sc > best_score:
+                    best_score, self.best = sc, trial
+        self._store()
+        return self.best
