@@ -177,7 +177,7 @@ def run_tran(args, world, rank, local, dist):
     torch.cuda.set_device(local)
     nl, guess, tstop, tstep, uic, out = build_tran(args.workload)
     prec = abi.LU_FP32 if args.fp32 else abi.LU_FP64
-    nref = 2 if args.fp32 else 0
+    nref = args.refine if args.fp32 else 0
     # the transient needs the load to the simulation's tolerance, not the
     # reference's rounding: the FMA build (long sums split over a warp) unless
     # --exact-load
@@ -237,7 +237,7 @@ def run_tran(args, world, rank, local, dist):
         "data": "synthetic (seeded netlist, the reference's benchmark circuit shape)",
         "config": {"workload": args.workload, "tstop": tstop, "tstep": tstep, "unknowns": c.n_unknowns,
                    "nnz": c.nnz, "nnz_lu": info.nnz_lu, "lu_levels": info.levels,
-                   "lu_precision": "fp32+2 refinement" if args.fp32 else "fp64",
+                   "lu_precision": f"fp32+{nref} fp64 refinement" if args.fp32 else "fp64",
                    "lu_order": "nested dissection" if info.ordering == 1 else "minimum degree",
                    "load_build": "exact (reference rounding)" if args.exact_load
                    else "fma, long sums split over a warp",
@@ -850,6 +850,8 @@ def main():
     ap.add_argument("--workload", default="single_load_bsim3_1M", choices=sorted(WORKLOADS))
     ap.add_argument("--fma", action="store_true")
     ap.add_argument("--fp32", action="store_true", help="transient: FP32 factors + FP64 refinement")
+    ap.add_argument("--refine", type=int, default=2,
+                    help="transient with --fp32: FP64 refinement steps per solve")
     ap.add_argument("--exact-load", action="store_true",
                     help="transient: the bit-exact load build instead of the FMA build")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
