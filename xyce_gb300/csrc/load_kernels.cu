@@ -12,10 +12,10 @@
 // product and sum rounded on its own, as the serial CPU load does) and with
 // -fmad=true into xg::fast (contracted to FMA).  XG_NS names the namespace.
 // The fast build also splits each long output (a supply rail collects a term
-// from every device on it) over the 32 lanes of a warp, each lane summing
-// every 32nd term in order, and adds the lane sums in a fixed butterfly: a
-// serial chain of dependent FP64 adds is the slowest thing a GB300 can be
-// asked to do.  The result is the same on every run, but not the reference's
+// from every device on it) over the 256 threads of a block, each thread
+// summing every 256th term in order, and adds the thread sums in a fixed
+// butterfly and warp order: a serial chain of dependent FP64 adds (and
+// gathers) is the slowest thing a GB300 can be asked to do.  The result is the same on every run, but not the reference's
 // rounding, which the exact build keeps.
 
 #include <cuda_runtime.h>
@@ -698,20 +698,37 @@ constexpr int kRedChunk = 256;
 
 __global__ void __launch_bounds__(kRedThreads) reduce_kernel(ReduceArgs a, int long_blocks) {
   if ((int)blockIdx.x < long_blocks) {
+#if XG_SPLIT_SUMS
+    // a block per long output: every thread sums a strided share of its terms,
+    // then a fixed butterfly per warp and the warps in order
+    __shared__ double part[kRedWarps];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int64_t w = blockIdx.x; w < a.n_long; w += long_blocks) {
+      const int64_t o = a.long_out[w];
+      const int64_t b = __ldg(a.red_ptr + o), e = __ldg(a.red_ptr + o + 1);
+      double s = 0.0;
+#pragma unroll 4
+      for (int64_t j = b + threadIdx.x; j < e; j += blockDim.x)
+        s += __ldg(a.terms + (a.red_idx ? (int64_t)__ldg(a.red_idx + j) : j));
+#pragma unroll
+      for (int m = 16; m > 0; m >>= 1) s += __shfl_xor_sync(0xffffffffu, s, m);
+      if (lane == 0) part[wid] = s;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double t = part[0];
+        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) t += part[k];
+        a.out[o] = t;
+      }
+      __syncthreads();
+    }
+    return;
+#else
     __shared__ double buf[kRedWarps][kRedChunk];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int64_t w = (int64_t)blockIdx.x * kRedWarps + wid; w < a.n_long;
          w += (int64_t)long_blocks * kRedWarps) {
       const int64_t o = a.long_out[w];
       const int64_t b = __ldg(a.red_ptr + o), e = __ldg(a.red_ptr + o + 1);
-#if XG_SPLIT_SUMS
-      double s = 0.0;
-      for (int64_t j = b + lane; j < e; j += 32)
-        s += __ldg(a.terms + (a.red_idx ? (int64_t)__ldg(a.red_idx + j) : j));
-#pragma unroll
-      for (int m = 16; m > 0; m >>= 1) s += __shfl_xor_sync(0xffffffffu, s, m);
-      if (lane == 0) a.out[o] = s;
-#else
       double s = 0.0;
       for (int64_t base = b; base < e; base += kRedChunk) {
         const int cnt = (int)(e - base < kRedChunk ? e - base : kRedChunk);
@@ -723,9 +740,9 @@ __global__ void __launch_bounds__(kRedThreads) reduce_kernel(ReduceArgs a, int l
         __syncwarp();
       }
       if (lane == 0) a.out[o] = s;
-#endif
     }
     return;
+#endif
   }
   // short outputs in order of term count: the lanes of a warp run loops of
   // the same length
@@ -769,7 +786,11 @@ int launch_reduce(const ReduceArgs &a, void *stream) {
   if (n <= 0 && a.n_long <= 0) return XG_OK;
   int grid = (int)std::max<int64_t>(1, (n + kRedThreads - 1) / kRedThreads);
   if (grid > 152 * 32) grid = 152 * 32;
+#if XG_SPLIT_SUMS
+  const int long_blocks = (int)std::min<int64_t>(a.n_long, 152 * 8);  // a block per long output
+#else
   const int long_blocks = (int)std::min<int64_t>((a.n_long + kRedWarps - 1) / kRedWarps, 152 * 8);
+#endif
   reduce_kernel<<<grid + long_blocks, kRedThreads, 0, (cudaStream_t)stream>>>(a, long_blocks); xg::count_launches(1);
   return cudaGetLastError() == cudaSuccess ? XG_OK : XG_ERR_CUDA;
 }
