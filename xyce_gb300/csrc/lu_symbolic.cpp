@@ -528,7 +528,11 @@ int lu_analyze(int n, const int *rp, const int *ci, const double *val, double pi
   std::vector<int> q = amd_order(n, rp, ci, &amd_dense);
   if (analyze_ordered(n, rp, ci, val, pivot_tol, std::move(q), amd_dense, out, err)) return -1;
   out->ordering = 0;
-  if (forced == 0 || out->levels <= kNdMinLevels) return 0;
+  // nested dissection pays where minimum degree leaves chains (few rows per
+  // level); on wide matrices it only adds fill, and its analysis costs more
+  // than the minimum-degree one
+  if (forced == 0 || out->levels <= kNdMinLevels || double(n) / out->levels >= kNdMaxRowsPerLevel)
+    return 0;
   // A long dependency chain: try nested dissection and keep it when the
   // modelled refactorisation time is lower.
   LuSymbolic nd;

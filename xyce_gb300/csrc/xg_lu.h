@@ -77,11 +77,13 @@ constexpr int kTailMinL = 64;
 constexpr int kTailMaxRows = 16;
 
 // Ordering choice: nested dissection is tried when minimum degree leaves a
-// dependency chain longer than kNdMinLevels rows; parts of at most kNdLeaf
+// dependency chain longer than kNdMinLevels rows with fewer than
+// kNdMaxRowsPerLevel rows per level on average; parts of at most kNdLeaf
 // vertices are ordered by minimum degree.  The refactorisation time model
 // charges kLuLevelSeconds per dependent level and kLuFlopSeconds per
 // multiply-add.
 constexpr int kNdMinLevels = 64;
+constexpr double kNdMaxRowsPerLevel = 8.0;  // and minimum degree averages fewer rows per level
 constexpr int kNdLeaf = 16;
 constexpr double kLuLevelSeconds = 2e-6;
 constexpr double kLuFlopSeconds = 2e-10;
