@@ -239,6 +239,8 @@ def run_tran(args, world, rank, local, dist):
                    "nnz": c.nnz, "nnz_lu": info.nnz_lu, "lu_levels": info.levels,
                    "lu_precision": f"fp32+{nref} fp64 refinement" if args.fp32 else "fp64",
                    "lu_order": "nested dissection" if info.ordering == 1 else "minimum degree",
+                   "lu_analysis": "done by the first (warm-up) run of the circuit, reused by the "
+                                  "timed runs (same first Newton matrix)",
                    "load_build": "exact (reference rounding)" if args.exact_load
                    else "fma, long sums split over a warp",
                    "newton_iters_per_step": per_step_iters, "time_steps_per_step": st["steps"],

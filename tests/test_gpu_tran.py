@@ -107,3 +107,19 @@ def test_random_logic_bsim3_waveforms(gpu_ctx, oracle_lib):
     cpu, gpu = _both(gpu_ctx, nl, netlists.random_logic_nodeset(nl), 20e-12,
                      [1, int(o[len(o) // 2]), int(o[-1])], uic=True)
     _agree(cpu, gpu)
+
+
+def test_second_transient_on_a_circuit_reuses_the_lu_analysis(gpu_ctx):
+    """The first transient leaves its LU analysis with the circuit; a second
+    one from the same start takes it back (no analysis) and gives the same
+    bits; a different start analyses afresh."""
+    nl = netlists.inverter_chain(40)
+    x0 = np.r_[netlists.inverter_chain_nodeset(40), 0.0, 0.0]
+    gpu_ctx.set_options(abi.device_options())
+    c = engine.Circuit(gpu_ctx, nl)
+    a = engine.transient(c, 1e-9, 1e-12, [2, 20, 41], x0=x0)
+    b = engine.transient(c, 1e-9, 1e-12, [2, 20, 41], x0=x0)
+    d = engine.transient(c, 1e-9, 1e-12, [2, 20, 41], x0=x0 * 0.5)
+    c.close()
+    assert a[2]["analyses"] >= 1 and b[2]["analyses"] == 0 and d[2]["analyses"] >= 1
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])

@@ -64,6 +64,10 @@ struct xg_circuit {
   xg_ctx *ctx = nullptr;
   xg_device_options opt;
   xg::Plan plan;
+  // the LU analysis of the last transient's first Newton matrix, kept for the
+  // next transient on this circuit (see circuit_lu_take)
+  xg_lu *lu_cache = nullptr;
+  uint64_t lu_cache_key = 0;
   double *d_sol[3] = {nullptr, nullptr, nullptr};
   double *d_sta[3] = {nullptr, nullptr, nullptr};
   double *d_sto[3] = {nullptr, nullptr, nullptr};
@@ -93,6 +97,8 @@ int dalloc(T **p, int64_t count) {
 }
 
 void free_circuit(xg_circuit *c) {
+  if (c->lu_cache) xg_lu_destroy(c->lu_cache);
+  c->lu_cache = nullptr;
   for (int k = 0; k < 3; ++k) {
     cudaFree(c->d_sol[k]);
     cudaFree(c->d_sta[k]);
@@ -159,6 +165,20 @@ int set_device(const xg_ctx *ctx) {
 namespace xg {
 
 void set_error(const std::string &msg) { g_err = msg; }
+
+xg_lu *circuit_lu_take(xg_circuit *c, uint64_t key) {
+  xg_lu *lu = c->lu_cache;
+  c->lu_cache = nullptr;
+  if (lu && c->lu_cache_key == key) return lu;
+  if (lu) xg_lu_destroy(lu);
+  return nullptr;
+}
+
+void circuit_lu_keep(xg_circuit *c, xg_lu *lu, uint64_t key) {
+  if (c->lu_cache && c->lu_cache != lu) xg_lu_destroy(c->lu_cache);
+  c->lu_cache = lu;
+  c->lu_cache_key = key;
+}
 
 int circuit_reset_members(xg_circuit *c) {
   if (!c) return XG_ERR_ARG;

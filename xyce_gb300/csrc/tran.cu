@@ -441,6 +441,8 @@ extern "C" int xg_tran_run(xg_circuit *c, const xg_tran_options *o, const double
   int rc = XG_OK;
   double *d_rec = nullptr;
   int *d_idx = nullptr;
+  bool reanalysed = false, reused = false;
+  uint64_t lu_key = 0;
   auto cleanup = [&]() {
     void *ptrs[] = {R.rhs, R.jac, R.dx, R.w, R.partials, R.xh0, R.xh1, R.xh2, R.qh0, R.qh1,
                     R.qh2, R.xn0, R.diag, d_rec, d_idx};
@@ -448,7 +450,9 @@ extern "C" int xg_tran_run(xg_circuit *c, const xg_tran_options *o, const double
     for (void *p : ptrs)
       if (p) cudaFree(p);
     if (R.h_part) cudaFreeHost(R.h_part);
-    if (R.lu) xg_lu_destroy(R.lu);
+    // the first analysis stays with the circuit for the next transient
+    if (R.lu && !reanalysed && lu_key) circuit_lu_keep(c, R.lu, lu_key);
+    else if (R.lu) xg_lu_destroy(R.lu);
   };
 #define TRY_CUDA(call)                                          \
   do {                                                          \
@@ -493,6 +497,7 @@ extern "C" int xg_tran_run(xg_circuit *c, const xg_tran_options *o, const double
   // first trapezoid step of length tstep at the starting point (static and
   // capacitive parts both present); zero diagonals get a 1e-12 placeholder
   double r[P_N];
+  bool first_analysis = true;
   auto analyse = [&](bool transient_matrix, double h) -> int {
     xg_load_flags fl;
     std::memset(&fl, 0, sizeof(fl));
@@ -510,12 +515,27 @@ extern "C" int xg_tran_run(xg_circuit *c, const xg_tran_options *o, const double
         if (P.colidx[p] == i && hj[p] == 0.0) hj[p] = 1e-12;
     if (R.lu) xg_lu_destroy(R.lu);
     R.lu = nullptr;
+    if (first_analysis) {
+      // FNV-1a over the matrix values and the precision
+      uint64_t hsh = 1469598103934665603ull;
+      const unsigned char *bytes = reinterpret_cast<const unsigned char *>(hj.data());
+      for (size_t k = 0; k < sizeof(double) * size_t(R.nnz); ++k) hsh = (hsh ^ bytes[k]) * 1099511628211ull;
+      hsh = (hsh ^ uint64_t(o->lu_precision + 1)) * 1099511628211ull;
+      lu_key = hsh ? hsh : 1;
+      first_analysis = false;
+      if ((R.lu = circuit_lu_take(c, lu_key))) {
+        reused = true;
+        return XG_OK;
+      }
+    } else {
+      reanalysed = true;
+    }
     return xg_lu_analyze(R.v.ctx, n, P.rowptr.data(), P.colidx.data(), hj.data(), o->lu_precision,
                          &R.lu);
   };
   const double tstep = o->tstep > 0 ? o->tstep : 1e-10;
   if ((rc = analyse(true, tstep))) { cleanup(); return rc; }
-  st->analyses = 1;
+  st->analyses = reused ? 0 : 1;
   // Newton with one re-analysis (new pivot order) when the refactor meets a
   // zero pivot, as the reference's KLU repivots
   auto newton = [&](bool transient, double h, int order, double time, int init_tran) -> int {

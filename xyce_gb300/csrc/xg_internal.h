@@ -166,6 +166,13 @@ void set_error(const std::string &msg);
 void count_launches(int k);
 // Zero the members carried between loads (diode Vd, BSIM3 charges/caps).
 int circuit_reset_members(xg_circuit *c);
+// A transient keeps its LU analysis in the circuit when it ends; the next
+// transient on the circuit takes it back when its first Newton matrix is the
+// same (key: a hash of the values and the precision), the case in which a
+// fresh analysis would find the same pivot order.  Otherwise the kept one is
+// destroyed and nullptr returned.
+xg_lu *circuit_lu_take(xg_circuit *c, uint64_t key);
+void circuit_lu_keep(xg_circuit *c, xg_lu *lu, uint64_t key);
 // The device and stream of a context (api.cpp).
 int ctx_info(xg_ctx *ctx, int *device, void **stream);
 
