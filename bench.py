@@ -179,7 +179,7 @@ def run_tran(args, world, rank, local, dist):
     prec = abi.LU_FP32 if args.fp32 else abi.LU_FP64
     nref = args.refine if args.fp32 else 0
     # the transient needs the load to the simulation's tolerance, not the
-    # reference's rounding: the FMA build (long sums split over a warp) unless
+    # reference's rounding: the FMA build (long sums split over a block) unless
     # --exact-load
     ctx = engine.Context(local, abi.device_options(fma=0 if args.exact_load else 1))
     c = engine.Circuit(ctx, nl)
@@ -242,7 +242,7 @@ def run_tran(args, world, rank, local, dist):
                    "lu_analysis": "done by the first (warm-up) run of the circuit, reused by the "
                                   "timed runs (same first Newton matrix)",
                    "load_build": "exact (reference rounding)" if args.exact_load
-                   else "fma, long sums split over a warp",
+                   else "fma, long sums split over a block",
                    "newton_iters_per_step": per_step_iters, "time_steps_per_step": st["steps"],
                    "l2": "working set below L2; latency-bound"},
         "roofline": {"kernel": "newton iteration", "bound": "hbm", "achieved": ach, "peak": hbm,
@@ -270,7 +270,7 @@ def run_serve(args, world, rank, local, dist):
     from xyce_gb300 import engine, serve
     torch.cuda.set_device(local)
     w = WORKLOADS[args.workload]
-    # as for the transients: the FMA load build (long sums split over a warp)
+    # as for the transients: the FMA load build (long sums split over a block)
     # unless --exact-load
     ctx = engine.Context(local, abi.device_options(fma=0 if args.exact_load else 1))
     L = engine.lib()
@@ -339,7 +339,7 @@ def run_serve(args, world, rank, local, dist):
                    "stages": "5-501 odd", "tstop": w["tstop"],
                    "lu": "fp32 factors and solves, corrected by Newton against the fp64 residual",
                    "load_build": "exact (reference rounding)" if args.exact_load
-                   else "fma, long sums split over a warp",
+                   else "fma, long sums split over a block",
                    "schedule": sched, "autotuner_trials": len(tuner.trials),
                    "l2": "per-request working sets below L2"},
         "p50_ms": float(np.mean([r[0]["p50_ms"] for r in runs])),
