@@ -35,6 +35,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -1530,6 +1531,12 @@ extern "C" int xg_batch_run(xg_batch *b, int iterations) {
     xg::set_error("xg_batch_run: bad argument");
     return XG_ERR_ARG;
   }
+  // One capture or graph launch at a time across threads: a server sets up
+  // and first runs a batch on a helper thread while its main thread keeps
+  // launching the others, and the launch counter's capture bookkeeping below
+  // assumes no other launch lands in between.
+  static std::mutex run_mutex;
+  std::lock_guard<std::mutex> lock(run_mutex);
   if (!b->graph || b->graph_iters != iterations) {
     if (b->graph) {
       cudaStreamSynchronize(b->stream);
