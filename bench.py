@@ -83,6 +83,10 @@ WORKLOADS = {
     # initial condition; one step = serving the whole stream, FP32 factors with
     # one FP64 refinement step (the FP64 form is measured beside it)
     "serve_ring_mc": dict(kind="serve", n=1000, rate=2000.0, tstop=5e-9),
+    # one batch: 256 requests of the same Monte-Carlo ring stream, all at
+    # once; one step = set up and run the batch to completion (FP32 factors
+    # corrected by Newton; the batched kernels without the server's threads)
+    "batch_ring_mc_256": dict(kind="batch", n=256, tstop=5e-9),
     # a 60x60 mesh with 1,200 sinks (6,002 unknowns), .TRAN 1ps 20ps: the
     # grid-wide LU path at a size a profiler captures quickly
     "tran_power_grid_60x60": dict(kind="tran", circuit="grid", nx=60, sinks=1200, tstop=20e-12,
@@ -366,6 +370,77 @@ def run_serve(args, world, rank, local, dist):
     return 0
 
 
+def run_batch(args, world, rank, local, dist):
+    import torch
+
+    from xyce_gb300 import engine, serve
+    torch.cuda.set_device(local)
+    w = WORKLOADS[args.workload]
+    ctx = engine.Context(local, abi.device_options(fma=0 if args.exact_load else 1))
+    L = engine.lib()
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=local)
+    reqs = serve.ring_mc_requests(w["n"], seed=1, tstop=w["tstop"])
+    prec, nref = (abi.LU_FP64, 0) if not args.fp32_batch else (abi.LU_FP32, 0)
+
+    def one():
+        b = engine.Batch(ctx, [r.netlist for r in reqs], [r.x0 for r in reqs],
+                         [r.tstop for r in reqs], [r.out_idx for r in reqs], tstep=1e-12,
+                         precision=prec, n_refine=nref, max_points=8192)
+        it = 0
+        while True:
+            b.run(64)
+            it += 64
+            if b.poll(wait=True) == len(reqs):
+                break
+        newton = sum(b.stats(i)["newton_iters"] for i in range(len(reqs)))
+        b.close()
+        return it, newton
+
+    for _ in range(args.warmup):
+        one()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    l0 = L.xg_launch_count()
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        res = [one() for _ in range(args.steps)]
+        wall = time.perf_counter() - t0
+    launches = L.xg_launch_count() - l0
+    if rank != 0:
+        return 0
+    step_s = wall / args.steps
+    batch_iters = res[0][0]
+    newton = float(np.mean([r[1] for r in res]))
+    value = world * len(reqs) / step_s
+    cpu_v, cpu_n = serve_cpu_baseline(args.cpu_seconds)
+    line = {
+        "metric": "solves/sec", "value": value, "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded Monte-Carlo ring oscillators, 5-501 stages)",
+        "config": {"workload": args.workload, "requests": len(reqs), "tstop": w["tstop"],
+                   "lu": "fp32, corrected by Newton" if args.fp32_batch else "fp64",
+                   "batch_iterations": batch_iters, "newton_iters_per_step": newton,
+                   "step": "set-up included (host analysis of every request)",
+                   "l2": "per-request working sets below L2"},
+        "newton_iters_per_s": newton / step_s,
+        "roofline": {"kernel": "batch iteration", "bound": "hbm", "achieved": None,
+                     "peak": measured_peaks()[0], "unit": "GB/s", "frac": None, "traffic": None,
+                     "note": "latency-bound: each request's factor runs level by level in one block"},
+        "e2e": {"value": value, "unit": "solves/s",
+                "h2d_bytes_per_step": int(sum(8 * len(r.x0) for r in reqs)),
+                "d2h_bytes_per_step": 0},
+        "gpu_launches": int(launches),
+        "clocks": clocks.summary(),
+        "cpu_baseline": {"value": cpu_v, "unit": "solves/s", "cores": 1, "kind": "port",
+                         "sample": f"{cpu_n} requests of the same stream, one core"},
+        "wall_s": wall,
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def _serve_ref_worker(job):
     """Reference arm for serving: requests solved one after another on one core."""
     idx, n, tstop = job
@@ -420,7 +495,8 @@ def run_serve_reference(args, world, rank):
                 times.append(time.perf_counter() - t0)
     t = float(np.mean(times))
     value = sample / t
-    line = {"metric": SERVE_METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus,
+    line = {"metric": SERVE_METRIC if w["kind"] == "serve" else "solves/sec", "value": value,
+            "unit": "solves/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded)", "impl": "reference",
@@ -854,6 +930,8 @@ def main():
     ap.add_argument("--fp32", action="store_true", help="transient: FP32 factors + FP64 refinement")
     ap.add_argument("--refine", type=int, default=2,
                     help="transient with --fp32: FP64 refinement steps per solve")
+    ap.add_argument("--fp32-batch", action="store_true",
+                    help="batch workload: FP32 factors (Newton-corrected)")
     ap.add_argument("--exact-load", action="store_true",
                     help="transient: the bit-exact load build instead of the FMA build")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
@@ -861,10 +939,11 @@ def main():
     world, rank, local, dist = dist_setup(args)
     kind = WORKLOADS[args.workload]["kind"]
     if args.impl == "reference":
-        ref = {"tran": run_tran_reference, "serve": run_serve_reference}.get(kind, run_reference)
+        ref = {"tran": run_tran_reference, "serve": run_serve_reference,
+               "batch": run_serve_reference}.get(kind, run_reference)
         rc = ref(args, world, rank)
     else:
-        arm = {"tran": run_tran, "serve": run_serve}.get(kind, run_xg)
+        arm = {"tran": run_tran, "serve": run_serve, "batch": run_batch}.get(kind, run_xg)
         rc = arm(args, world, rank, local, dist)
     if dist:
         dist.destroy_process_group()
