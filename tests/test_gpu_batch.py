@@ -2,7 +2,9 @@
 alone and inside a mix of uneven requests, to within the simulation's own
 tolerance (reltol 1e-3 of the 1.8 V swing); the mix matches the CPU
 transient driver; FP32 factors with FP64 refinement match FP64 factors; and
-batches repeat bit for bit."""
+batches repeat bit for bit.  Requests whose level schedule fits in shared
+memory use it (one block per request, level by level); the others are
+walked row by row by one lane; both give the same waveforms."""
 import numpy as np
 import pytest
 
@@ -88,3 +90,19 @@ def test_batches_repeat_bit_for_bit(gpu_ctx):
     b = _batch(gpu_ctx, reqs)
     for x, y in zip(a, b):
         assert np.array_equal(x[0], y[0]) and np.array_equal(x[1], y[1])
+
+
+def test_level_schedule_and_row_walk_agree(gpu_ctx, monkeypatch):
+    """XG_BATCH_NO_LVL sends every request to the row walk; the level-by-level
+    kernel (nested-dissection order, a 128-thread block per request) gives the
+    same waveforms; FP32 factors corrected by Newton alone agree too."""
+    gpu_ctx.set_options(abi.device_options(fma=1))
+    reqs = [_ring(k, s) for k, s in MIX]
+    lvl = _batch(gpu_ctx, reqs)
+    monkeypatch.setenv("XG_BATCH_NO_LVL", "1")
+    walk = _batch(gpu_ctx, reqs)
+    monkeypatch.delenv("XG_BATCH_NO_LVL")
+    f32 = _batch(gpu_ctx, reqs, precision=abi.LU_FP32, n_refine=0)
+    for a, b, c in zip(lvl, walk, f32):
+        _agree(a, b)
+        _agree(c, a)

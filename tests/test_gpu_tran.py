@@ -43,10 +43,11 @@ def _agree(cpu, gpu):
 
 
 @pytest.mark.parametrize("precision,n_refine,fma", [(abi.LU_FP64, 0, 0), (abi.LU_FP32, 2, 0),
-                                                    (abi.LU_FP64, 0, 1)])
+                                                    (abi.LU_FP64, 0, 1), (abi.LU_FP32, 0, 1)])
 def test_inverter_chain_waveforms(precision, n_refine, fma, gpu_ctx, oracle_lib):
     """fma=1: the FMA load build, whose supply-rail sums (one term per
-    device) are split over a warp."""
+    device) are split over a block; FP32 factors with no extra refinement
+    rely on Newton's FP64 residual alone."""
     stages = 100
     cpu, gpu = _both(gpu_ctx, netlists.inverter_chain(stages), netlists.inverter_chain_nodeset(stages),
                      4e-9, [1, 2, 3, 50, stages + 1], precision=precision, n_refine=n_refine, fma=fma)
