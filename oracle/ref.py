@@ -100,3 +100,61 @@ class RefCircuit:
         for k in ("F", "Q", "dFdxdVp", "dQdxdVp"):
             out[k] = out[k][: self.n_unknowns]
         return out
+
+
+KSPARSE_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_ref", "libksparse.so")
+_ks = None
+
+
+def ksparse_available():
+    return os.path.exists(KSPARSE_PATH)
+
+
+def ksparse_solve(rowptr, col, val, b, rel_threshold=1e-3, abs_threshold=1e-13, diag_pivoting=1):
+    """x = A \\ b with the reference's Kundert sparse solver, driven as its
+    Epetra_CrsKundertSparse wrapper does (ksparse/src/Epetra_CrsKundertSparse.C:
+    spGetElement per entry with 1-based indices, spOrderAndFactor with the
+    wrapper's default thresholds, spSolve on 1-based vectors).  The library
+    keeps state between matrices inside one process (a second matrix of
+    another size does not finish), so every solve runs in a fresh process."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    args = (np.asarray(rowptr), np.asarray(col), np.asarray(val, np.float64), np.asarray(b, np.float64),
+            rel_threshold, abs_threshold, diag_pivoting)
+    with cf.ProcessPoolExecutor(1, mp_context=mp.get_context("spawn")) as ex:
+        return ex.submit(_ksparse_solve_here, *args).result(timeout=300)
+
+
+def _ksparse_solve_here(rowptr, col, val, b, rel_threshold, abs_threshold, diag_pivoting):
+    global _ks
+    if _ks is None:
+        _ks = C.CDLL(KSPARSE_PATH)
+        _ks.spCreate.restype = C.c_void_p
+        _ks.spCreate.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int)]
+        _ks.spGetElement.restype = C.POINTER(C.c_double)
+        _ks.spGetElement.argtypes = [C.c_void_p, C.c_int, C.c_int]
+        _ks.spOrderAndFactor.restype = C.c_int
+        _ks.spOrderAndFactor.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int]
+        _ks.spSolve.restype = C.c_int
+        _ks.spSolve.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        _ks.spDestroy.argtypes = [C.c_void_p]
+    n = len(rowptr) - 1
+    err = C.c_int(0)
+    m = _ks.spCreate(n, 0, C.byref(err))
+    if not m or err.value != 0:
+        raise RuntimeError(f"spCreate failed: {err.value}")
+    try:
+        for i in range(n):
+            for p in range(rowptr[i], rowptr[i + 1]):
+                e = _ks.spGetElement(m, i + 1, int(col[p]) + 1)
+                e[0] += float(val[p])
+        rhs = np.zeros(n + 1)
+        rhs[1:] = b
+        x = np.zeros(n + 1)
+        st = _ks.spOrderAndFactor(m, _ptr(rhs), rel_threshold, abs_threshold, diag_pivoting)
+        if st != 0:
+            raise RuntimeError(f"spOrderAndFactor failed: {st}")
+        _ks.spSolve(m, _ptr(rhs), _ptr(x), None, None)
+        return x[1:]
+    finally:
+        _ks.spDestroy(m)

@@ -1,5 +1,6 @@
 """Build recipe for oracle/_ref/libxyceref.so: the reference Xyce device code,
-compiled from its own unmodified sources, plus the harness in this folder.
+compiled from its own unmodified sources, plus the harness in this folder;
+and oracle/_ref/libksparse.so, the reference's bundled sparse direct solver.
 
 Test infrastructure only.  Runs where the reference source tree is present
 (it is not copied into this repository); writes only under oracle/_ref/.
@@ -82,7 +83,41 @@ def main(argv=None):
     if r.returncode:
         raise RuntimeError("link failed\n" + r.stderr[-6000:])
     print(lib)
+    print(build_ksparse(a.ref, a.j))
     return 0
+
+
+def build_ksparse(ref, jobs):
+    """oracle/_ref/libksparse.so: the reference's bundled Kundert sparse
+    direct solver (src/LinearAlgebraServicesPKG/ksparse, the KSparse option
+    of its linear-solver factory), compiled from its C sources with a
+    two-line Xyce_config.h.  A reference-side FP64 direct solve for the LU
+    tests."""
+    src = os.path.join(ref, "src", "LinearAlgebraServicesPKG", "ksparse")
+    objdir = os.path.join(OUT, "ksparse_obj")
+    os.makedirs(objdir, exist_ok=True)
+    with open(os.path.join(objdir, "Xyce_config.h"), "w") as f:
+        f.write("#include <limits.h>\n#include <float.h>\n")
+    cflags = ["gcc", "-O2", "-fPIC", "-w", "-ffp-contract=off", "-I" + objdir,
+              "-I" + os.path.join(src, "include")]
+    cs = sorted(f for f in os.listdir(os.path.join(src, "src")) if f.endswith(".c"))
+
+    def one(f):
+        obj = os.path.join(objdir, f[:-2] + ".o")
+        r = subprocess.run(cflags + ["-c", os.path.join(src, "src", f), "-o", obj],
+                           capture_output=True, text=True)
+        if r.returncode:
+            raise RuntimeError(f"compile failed: {f}\n{r.stderr[-3000:]}")
+        return obj
+
+    with cf.ThreadPoolExecutor(jobs) as ex:
+        objs = list(ex.map(one, cs))
+    lib = os.path.join(OUT, "libksparse.so")
+    r = subprocess.run(["gcc", "-shared", "-o", lib] + objs + ["-Wl,--no-undefined", "-lm"],
+                       capture_output=True, text=True)
+    if r.returncode:
+        raise RuntimeError("ksparse link failed\n" + r.stderr[-4000:])
+    return lib
 
 
 if __name__ == "__main__":

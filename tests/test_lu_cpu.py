@@ -113,3 +113,30 @@ def test_singular_matrix_is_reported(engine_lib):
     with pytest.raises(engine.XgError) as e:
         engine.lu_analyze_host(A.indptr, A.indices, A.data)
     assert e.value.status == -4
+
+
+@pytest.mark.parametrize("case", ["inverter_chain_200", "power_grid_20x20", "ring_oscillator_51",
+                                  "random_logic_2000"])
+def test_oracle_solve_matches_the_reference_sparse_solver(case, oracle_lib):
+    """The oracle's sparse direct solve (minimum-degree order, threshold
+    partial pivoting) against the reference's own bundled Kundert sparse
+    solver (its KSparse linear-solver option) on circuit Jacobians: the same
+    solution to 1e-10 relative, and both backward-stable."""
+    from oracle import ref
+    from oracle.oracle import sparse_solve
+    if not ref.ksparse_available():
+        pytest.skip("oracle/_ref/libksparse.so is built only where the reference sources are")
+    nl = {"inverter_chain_200": lambda: netlists.inverter_chain(200),
+          "power_grid_20x20": lambda: netlists.power_grid(20, 20, 60, seed=1),
+          "ring_oscillator_51": lambda: netlists.ring_oscillator(51, seed=2),
+          "random_logic_2000": lambda: netlists.random_logic(2000, seed=1)}[case]()
+    A = circuit_jacobian(nl, seed=6)
+    b = np.random.default_rng(13).standard_normal(A.shape[0])
+    xk = ref.ksparse_solve(A.indptr, A.indices, A.data, b)
+    order, _ = engine.amd_order(A.indptr, A.indices)
+    xo = sparse_solve(A.indptr, A.indices, A.data, b, col_order=order)
+    scale = np.abs(xk).max()
+    assert np.abs(xo - xk).max() <= 1e-10 * scale, np.abs(xo - xk).max() / scale
+    for x in (xk, xo):
+        r = b - A @ x
+        assert np.abs(r).max() / (abs(A).sum(axis=1).max() * np.abs(x).max() + np.abs(b).max()) <= 1e-13
