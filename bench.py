@@ -606,6 +606,7 @@ def fp64_roofline(counts, kernel_ms, peak_flops, fma):
     ach = fl / (kernel_ms / 1e3)
     return {"bound": "fp64", "achieved": ach / 1e12, "peak": peak_flops / 1e12, "unit": "TFLOP/s",
             "frac": ach / peak_flops, "fp64_flops_per_launch": fl,
+            "fp64_pipe_active_ncu": counts.get("fp64_pipe_active"),
             "peak_source": "xg_probe_fp64_rate (DFMA chains, this GPU, this run)"}
 
 
