@@ -318,6 +318,20 @@ def run_serve(args, world, rank, local, dist):
     for _ in range(max(1, args.steps // 2)):
         fp64.append(one(abi.LU_FP64, 0))
         refined.append(one(abi.LU_FP32, 1))
+    # latency against offered load: the same kind of stream at other rates,
+    # about two seconds of arrivals each (at most the workload's request count)
+    sweep = []
+    if not args.no_sweep:
+        for rate in (100.0, 500.0, 2000.0, 5000.0):
+            n = int(min(w["n"], max(100, 2 * rate)))
+            row = {"rate_per_s": rate, "requests": n}
+            for name, prec in (("mixed", abi.LU_FP32), ("fp64", abi.LU_FP64)):
+                reqs = serve.ring_mc_requests(n, seed=3, tstop=w["tstop"])
+                arr = serve.poisson_arrivals(n, rate, seed=4)
+                r = serve.Server(ctx, precision=prec, n_refine=0, **sched).run(reqs, arr)
+                row[name] = {"solves_per_s": r["solves_per_s"], "p50_ms": r["p50_ms"],
+                             "p99_ms": r["p99_ms"]}
+            sweep.append(row)
     if rank != 0:
         return 0
     # accuracy of the mixed-precision forms against the FP64 form, request by request
@@ -353,6 +367,7 @@ def run_serve(args, world, rank, local, dist):
             "solves_per_s": refined[0][0]["solves_per_s"], "p50_ms": refined[0][0]["p50_ms"],
             "p99_ms": refined[0][0]["p99_ms"], "max_waveform_diff_vs_fp64_v": err_ref},
         "fp32_vs_fp64_max_waveform_diff_v": err,
+        "rate_sweep": sweep,
         "newton_iters_per_s": float(np.mean([r[0]["newton_iters_per_s"] for r in runs])),
         "roofline": {"kernel": "batch iteration", "bound": "hbm", "achieved": None, "peak": measured_peaks()[0],
                      "unit": "GB/s", "frac": None, "traffic": None,
@@ -931,6 +946,7 @@ def main():
     ap.add_argument("--fp32", action="store_true", help="transient: FP32 factors + FP64 refinement")
     ap.add_argument("--refine", type=int, default=2,
                     help="transient with --fp32: FP64 refinement steps per solve")
+    ap.add_argument("--no-sweep", action="store_true", help="serving: skip the arrival-rate sweep")
     ap.add_argument("--fp32-batch", action="store_true",
                     help="batch workload: FP32 factors (Newton-corrected)")
     ap.add_argument("--exact-load", action="store_true",
