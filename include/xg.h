@@ -340,9 +340,10 @@ int xg_tran_run(xg_circuit *c, const xg_tran_options *o, const double *host_x0, 
  * xg_tran_run.  One batch iteration (one Newton iteration of every request) is
  * a fixed sequence of launches, captured into a CUDA graph on the batch's own
  * stream; batches created while others run overlap on the device.
- * Requests start from their initial condition (UIC); sources must be DC (no
- * breakpoints).  x0[r] and out_idx[r] use request r's own unknown numbering
- * (nodes, then its internal unknowns). */
+ * Requests start from their initial condition (UIC).  Each request steps to
+ * the breakpoints of its own PULSE sources and restarts at first order there,
+ * as xg_tran_run does.  x0[r] and out_idx[r] use request r's own unknown
+ * numbering (nodes, then its internal unknowns). */
 typedef struct xg_batch xg_batch;
 typedef struct {
   double tstep;               /* first-step bound (.TRAN TSTEP) */

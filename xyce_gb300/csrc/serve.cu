@@ -48,16 +48,19 @@ namespace xg {
 namespace {
 
 enum Phase : int { PH_DONE = 0, PH_INIT = 1, PH_START = 2, PH_ITER = 3 };
-enum Action : int { A_INIT = 1, A_ACCEPT = 2, A_PREDICT = 4 };
+enum Action : int { A_INIT = 1, A_ACCEPT = 2, A_PREDICT = 4, A_RESTART = 8 };
 enum Part : int { Q_RHS2 = 0, Q_RHSMAX, Q_LIMMAX, Q_DXW2, Q_ERR2, Q_XMAX, Q_LUFAIL, Q_N };
 
 struct CState {
   double t, h, h_last, h_sum, saved, next_time, tstop, tstep, max_step, reltol, abstol;
+  double stop_time;              // the next breakpoint (or tstop)
   double psi[3], beta[3], ck;
   double norm_init, norm_old, stall_rate;
   int order, n_steps, nef, beginning, first_step;
   int phase, nstep, stall_count, action, status, failed;
   int steps, steps_attempted, rejected, newton_iters, loads, n_rec;
+  int bpi;                       // index of stop_time in the request's breakpoints
+  int hist_order;                // order of the history update of an accepted step
 };
 
 struct BatchDev {
@@ -90,6 +93,10 @@ struct BatchDev {
   const int *lvl;
   const int64_t *sched_off;
   const int *sched;
+  // breakpoints of request c (its PULSE corners, then its tstop):
+  // bp[bp_ptr[c]] .. bp[bp_ptr[c + 1] - 1], sorted
+  const int *bp_ptr;
+  const double *bp;
 };
 
 // 1/u by Newton-Raphson on the reciprocal from a single-precision seed (two
@@ -634,6 +641,17 @@ __device__ void start_step(CState &cs, Flags &fl) {
   cs.loads++;
 }
 
+constexpr double kBpTol = 1e-18;
+
+// The first breakpoint after t (the breakpoint list ends with tstop).
+__device__ void next_breakpoint(const BatchDev &b, int c, CState &cs) {
+  const int e = b.bp_ptr[c + 1];
+  int k = b.bp_ptr[c] + cs.bpi;
+  while (k < e && b.bp[k] <= cs.t + kBpTol) ++k;
+  cs.bpi = k - b.bp_ptr[c];
+  cs.stop_time = k < e ? b.bp[k] : cs.tstop;
+}
+
 __global__ void batch_control(BatchDev b) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= b.nc) return;
@@ -644,8 +662,9 @@ __global__ void batch_control(BatchDev b) {
   cs.action = 0;
   if (cs.phase == PH_DONE) return;
   if (cs.phase == PH_INIT) {
-    // OneStep::initialize at t = 0 (no breakpoints: the stop time is tstop)
-    const double tts = cs.tstop - cs.t;
+    // OneStep::initialize at t = 0, towards the first breakpoint
+    next_breakpoint(b, c, cs);
+    const double tts = cs.stop_time - cs.t;
     double hh = 0.005 * fabs(tts);
     hh = fmin(cs.tstep, hh);
     if (hh > cs.max_step) hh = cs.max_step;
@@ -723,18 +742,36 @@ __global__ void batch_control(BatchDev b) {
     const double min_step = cs.t * 10.0 * DBL_EPSILON;
     hn = fmax(hn, min_step);
     hn = fmin(hn, cs.max_step);
-    if (cs.tstop - cs.t >= min_step) {
-      if (cs.t + hn > cs.tstop) {
+    if (cs.stop_time - cs.t >= min_step) {
+      if (cs.t + hn > cs.stop_time) {
         cs.saved = hn;
-        hn = cs.tstop - cs.t;
+        hn = cs.stop_time - cs.t;
       }
       cs.next_time = cs.t + hn;
       cs.h_sum = hn + cs.h_last;
     }
     cs.h = hn;
-    if (!(cs.t < cs.tstop) || fabs(cs.t - cs.tstop) <= 1e-18) {
+    cs.hist_order = cs.order;
+    if (!(cs.t < cs.tstop) || fabs(cs.t - cs.tstop) <= kBpTol) {
       cs.phase = PH_DONE;
       return;
+    }
+    cs.beginning = fabs(cs.t - cs.stop_time) <= kBpTol && fabs(cs.t - cs.tstop) > kBpTol;
+    next_breakpoint(b, c, cs);
+    if (cs.beginning) {
+      // OneStep::initialize at a breakpoint: a first-order restart with a
+      // step of at most a tenth of the one cut short there
+      const double tts = cs.stop_time - cs.t;
+      double hh = 0.1 * fmin(cs.saved, fabs(tts));
+      if (hh > cs.max_step) hh = cs.max_step;
+      cs.h = fmin(cs.h, hh);
+      cs.h_sum = 2.0 * cs.h;
+      cs.h_last = cs.h;
+      cs.next_time = cs.t + cs.h;
+      cs.n_steps = 0;
+      cs.order = 1;
+      cs.psi[0] = cs.h;
+      cs.action |= A_RESTART;
     }
   } else {
     cs.rejected++;
@@ -747,7 +784,7 @@ __global__ void batch_control(BatchDev b) {
     cs.order = 1;
     hn = fmax(hn, cs.t * 10.0 * DBL_EPSILON);
     hn = fmin(hn, cs.max_step);
-    if (cs.t + hn > cs.tstop) hn = cs.tstop - cs.t;
+    if (cs.t + hn > cs.stop_time) hn = cs.stop_time - cs.t;
     cs.next_time = cs.t + hn;
     cs.h_sum = hn + cs.h_last;
     cs.h = hn;
@@ -787,7 +824,7 @@ __global__ void __launch_bounds__(kBatchThreads) batch_vector(BatchDev b) {
     __syncthreads();
   }
   if (act & A_ACCEPT) {
-    const int order = cs.order;
+    const int order = cs.hist_order;
     for (int k = tid; k < n; k += nt) {
       const int g = b.uidx[u0 + k];
       if (order == 2) {
@@ -821,6 +858,17 @@ __global__ void __launch_bounds__(kBatchThreads) batch_vector(BatchDev b) {
     }
   }
   __syncthreads();
+  if (act & A_RESTART) {
+    // the accepted point at a breakpoint starts a new first-order history
+    for (int k = tid; k < n; k += nt) {
+      const int g = b.uidx[u0 + k];
+      b.xh0[g] = b.xc[g];
+      b.xh1[g] = 0.0;
+      b.qh0[g] = b.q[g];
+      b.qh1[g] = -cs.h_last * b.f[g];
+    }
+    __syncthreads();
+  }
   if ((act & A_PREDICT) && cs.phase != PH_DONE) {
     const double b1 = cs.beta[1], b2 = cs.beta[2];
     const int order = cs.order;
@@ -973,10 +1021,6 @@ int build_union(int n, const xg_netlist *const *nls, UnionNetlist *U,
         m[k] = node(r, d.m[i]);
         kind[k] = d.kind ? d.kind[i] : XG_SRC_DC;
         for (int j = 0; j < 7; ++j) wave[(size_t)k * 7 + j] = d.wave[(size_t)i * 7 + j];
-        if (kind[k] == XG_SRC_PULSE) {
-          xg::set_error("xg_batch_create: PULSE sources (breakpoints) are not supported in a batch");
-          return XG_ERR_UNSUPPORTED;
-        }
       }
     }
     xg_src_desc &o = which == 0 ? u.vsrc : u.isrc;
@@ -1338,7 +1382,27 @@ extern "C" int xg_batch_create(xg_ctx *ctx, int n, const xg_netlist *const *nls,
       }
       outs[(size_t)r * o->n_out + j] = l2u[r][k];
     }
+  // breakpoints per request, from its own PULSE sources and tstop
+  std::vector<int> bp_ptr(n + 1, 0);
+  std::vector<double> bpv;
+  for (int r = 0; r < n; ++r) {
+    const int lo[2] = {inst0[r][XG_DEV_VSRC], inst0[r][XG_DEV_ISRC]};
+    const int hi[2] = {inst0[r + 1][XG_DEV_VSRC], inst0[r + 1][XG_DEV_ISRC]};
+    const std::vector<double> bp = pulse_breakpoints(P, tstop[r], lo, hi);
+    bpv.insert(bpv.end(), bp.begin(), bp.end());
+    bp_ptr[r + 1] = (int)bpv.size();
+  }
   BatchDev &d = b->dev;
+  {
+    int *t_bp_ptr;
+    double *t_bp;
+    if (dev_copy(b.get(), &t_bp_ptr, bp_ptr) || dev_copy(b.get(), &t_bp, bpv)) {
+      set_error("xg_batch_create: out of device memory");
+      return XG_ERR_OOM;
+    }
+    d.bp_ptr = t_bp_ptr;
+    d.bp = t_bp;
+  }
   d.nc = n;
   d.n_out = o->n_out;
   d.max_points = o->max_points;

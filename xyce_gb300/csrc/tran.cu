@@ -377,11 +377,15 @@ struct Run {
   }
 };
 
-std::vector<double> pulse_breakpoints(const Plan &P, double tstop) {
+}  // namespace
+
+std::vector<double> pulse_breakpoints(const Plan &P, double tstop, const int *lo,
+                                      const int *hi) {
   std::vector<double> bp;
-  for (int src : {XG_DEV_VSRC, XG_DEV_ISRC}) {
-    const TypeData &V = P.T[src];
-    for (int i = 0; i < V.n; ++i) {
+  for (int which = 0; which < 2; ++which) {
+    const TypeData &V = P.T[which == 0 ? XG_DEV_VSRC : XG_DEV_ISRC];
+    const int i0 = lo ? lo[which] : 0, i1 = hi ? hi[which] : V.n;
+    for (int i = i0; i < i1; ++i) {
       auto p = [&](int k) { return V.params[(size_t)k * V.n + i]; };
       if (p(XG_V_KIND) != XG_SRC_PULSE) continue;
       const double td = p(XG_V_TD), tr = p(XG_V_TR), tf = p(XG_V_TF), pw = p(XG_V_PW),
@@ -401,7 +405,6 @@ std::vector<double> pulse_breakpoints(const Plan &P, double tstop) {
   return bp;
 }
 
-}  // namespace
 }  // namespace xg
 
 extern "C" int xg_tran_run(xg_circuit *c, const xg_tran_options *o, const double *host_x0,

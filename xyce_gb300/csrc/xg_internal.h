@@ -175,6 +175,12 @@ xg_lu *circuit_lu_take(xg_circuit *c, uint64_t key);
 void circuit_lu_keep(xg_circuit *c, xg_lu *lu, uint64_t key);
 // The device and stream of a context (api.cpp).
 int ctx_info(xg_ctx *ctx, int *device, void **stream);
+// Breakpoints of the PULSE sources (both corners of each edge, every period,
+// up to tstop) and tstop itself, sorted and unique (tran.cu).  lo/hi, when
+// given, restrict the sources to instances [lo[0], hi[0]) of VSRC and
+// [lo[1], hi[1]) of ISRC: one request of a batch.
+std::vector<double> pulse_breakpoints(const Plan &P, double tstop, const int *lo = nullptr,
+                                      const int *hi = nullptr);
 
 // load_kernels.cu (two builds: bit-exact and FMA-contracted)
 namespace exact {
