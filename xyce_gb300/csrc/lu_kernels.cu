@@ -31,9 +31,11 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <memory>
 #include <string>
 
@@ -216,15 +218,79 @@ __global__ void lu_assemble(LuDev d, const double *__restrict__ a, double *__res
 }
 
 // A warp's own row lives in shared memory while it is eliminated (rows up to
-// kRowStage entries; longer ones stay in global memory): the multiplier of
-// each L entry reads what the previous entries' updates wrote, and a
-// shared-memory round trip is ~30 cycles where an L2 one is ~1 us.
-constexpr int kRowStage = 512;
+// `cap` entries, the matrix's longest row up to kStageBytes; longer ones stay
+// in global memory): the multiplier of each L entry reads what the previous
+// entries' updates wrote, and a shared-memory round trip is ~30 cycles where
+// an L2 one is ~1 us.
+constexpr int kStageBytes = 24 * 1024;
+constexpr int kMinStageBytes = 4 * 1024;
+constexpr int kUnstagedRows = 32;
+constexpr int kFactorWarps = 8;
+
+// row -= l * (U row of the pivot): the pivot row's values and target
+// positions of a chunk of 8 per lane are loaded before any of them is
+// applied, so a long U row costs one L2 round trip per 256 entries (the
+// target row and the pivot row are different rows: nothing aliases).
+template <class T>
+__device__ __forceinline__ void row_update(T *rb, int ro, const int *__restrict__ up,
+                                           const T *__restrict__ u, int len, T l, int lane) {
+  constexpr int kU = 8;
+  int j0 = 0;
+  for (; j0 + 32 * kU <= len; j0 += 32 * kU) {
+    T v[kU];
+    int q[kU];
+#pragma unroll
+    for (int r = 0; r < kU; ++r) {
+      v[r] = __ldcg(u + j0 + 32 * r + lane);
+      q[r] = __ldg(up + j0 + 32 * r + lane);
+    }
+#pragma unroll
+    for (int r = 0; r < kU; ++r) rb[q[r] - ro] -= l * v[r];
+  }
+  if (j0 < len) {
+    // the last chunk: steps past the row's end are skipped by the whole warp
+    // (an FP64 instruction costs its issue slot however few lanes it has)
+    T v[kU];
+    int q[kU];
+#pragma unroll
+    for (int r = 0; r < kU; ++r) {
+      const int j = j0 + 32 * r + lane;
+      v[r] = j < len ? __ldcg(u + j) : T(0);
+      q[r] = j < len ? __ldg(up + j) : -1;
+    }
+#pragma unroll
+    for (int r = 0; r < kU; ++r) {
+      if (j0 + 32 * r >= len) break;
+      if (q[r] >= 0) rb[q[r] - ro] -= l * v[r];
+    }
+  }
+}
+
+// Eliminate row `row` in rb (row entry p at rb[p - ro]).
+template <class T>
+__device__ __forceinline__ void eliminate(const LuDev &d, const T *val, T *rb, int ro, int s,
+                                          int dp, const int *up, int lane) {
+  const T *rdiag = (const T *)d.rdiag;
+  for (int p = s; p < dp; ++p) {
+    const int k = __ldg(d.ci + p);
+    const int q0 = __ldg(d.diag + k) + 1, len = __ldg(d.rp + k + 1) - q0;
+    T rk = T(0);
+    if (lane == 0) rk = wait_value_acquire(rdiag + k, d.ctrl);
+    rk = __shfl_sync(0xffffffffu, rk, 0);
+    const T l = rb[p - ro] * rk;
+    __syncwarp();
+    if (lane == 0) rb[p - ro] = l;
+    row_update(rb, ro, up, val + q0, len, l, lane);
+    up += len;
+    __syncwarp();
+  }
+}
 
 template <class T>
-__global__ void __launch_bounds__(256) lu_factor(LuDev d, T *val) {
-  __shared__ T stage[8][kRowStage];
+__global__ void __launch_bounds__(32 * kFactorWarps) lu_factor(LuDev d, T *val, int cap) {
+  extern __shared__ __align__(16) unsigned char stage_raw[];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  T *stage = reinterpret_cast<T *>(stage_raw) + size_t(wid) * cap;
   T *rdiag = (T *)d.rdiag;
   while (true) {
     int row = 0;
@@ -233,33 +299,19 @@ __global__ void __launch_bounds__(256) lu_factor(LuDev d, T *val) {
     if (row >= d.n) break;
     const int s = __ldg(d.rp + row), dp = __ldg(d.diag + row), e = __ldg(d.rp + row + 1);
     const int *up = d.upos + __ldg(d.urp + row);
-    const bool staged = e - s <= kRowStage;
-    // the row's values: in shared memory (position p at p - s) or in place
-    T *rb = staged ? stage[wid] : val;
-    const int ro = staged ? s : 0;
-    if (staged) {
-      for (int p = s + lane; p < e; p += 32) rb[p - ro] = val[p];
+    T u;
+    if (e - s <= cap) {
+      for (int p = s + lane; p < e; p += 32) stage[p - s] = val[p];
       __syncwarp();
-    }
-    for (int p = s; p < dp; ++p) {
-      const int k = __ldg(d.ci + p);
-      const int q0 = __ldg(d.diag + k) + 1, len = __ldg(d.rp + k + 1) - q0;
-      T rk = T(0);
-      if (lane == 0) rk = wait_value_acquire(rdiag + k, d.ctrl);
-      rk = __shfl_sync(0xffffffffu, rk, 0);
-      const T l = rb[p - ro] * rk;
+      eliminate(d, val, stage, s, s, dp, up, lane);
+      for (int p = s + lane; p < e; p += 32) val[p] = stage[p - s];
       __syncwarp();
-      if (lane == 0) rb[p - ro] = l;
-      for (int j = lane; j < len; j += 32) rb[__ldg(up + j) - ro] -= l * __ldcg(val + q0 + j);
-      up += len;
-      __syncwarp();
-    }
-    if (staged) {
-      for (int p = s + lane; p < e; p += 32) val[p] = rb[p - ro];
-      __syncwarp();
+      u = stage[dp - s];
+    } else {
+      eliminate(d, val, val, 0, s, dp, up, lane);
+      u = val[dp];
     }
     if (lane == 0) {
-      const T u = rb[dp - ro];
       if (!(fabs(double(u)) > 0.0) || !isfinite(double(u))) {
         atomicOr(&d.ctrl[C_STATUS], ST_PIVOT);
         atomicMin(&d.ctrl[C_BAD_ROW], unsigned(row));
@@ -1064,6 +1116,9 @@ struct xg_lu {
   double *d_a = nullptr;                          // FP64 copy of A
   double *d_r = nullptr, *d_dx = nullptr;         // refinement work
   int grid_factor = 0, grid_solve = 0;
+  int stage_cap = 0;                       // grid refactor: staged row entries per warp
+  size_t smem_grid = 0;                    // its dynamic shared memory
+  int grid_tri = 0;                        // grid solves: blocks
   size_t smem_factor = 0, smem_solve = 0;  // > 0: the one-CTA path
   int cta_threads = 0;                     // its block size (warps ~ level width)
   bool narrow = false;                     // one lane walks the rows (<= 2 rows per level)
@@ -1133,7 +1188,8 @@ int refactor_t(xg_lu *lu, const double *dev_values) {
   }
   xg::lu_assemble<T><<<lu->grid_solve, 256, 0, lu->stream>>>(
       d, dev_values, lu->d_a, lu->S.nnz_a, (T *)lu->d_val, lu->nnz_lu); xg::count_launches(1);
-  xg::lu_factor<T><<<lu->grid_factor, 256, 0, lu->stream>>>(d, (T *)lu->d_val); xg::count_launches(1);
+  xg::lu_factor<T><<<lu->grid_factor, 32 * xg::kFactorWarps, lu->smem_grid, lu->stream>>>(
+      d, (T *)lu->d_val, lu->stage_cap); xg::count_launches(1);
   XG_CU(cudaGetLastError());
   return XG_OK;
 }
@@ -1163,9 +1219,9 @@ int solve_once(xg_lu *lu, const double *b, double *x) {
   xg::lu_solve_open<T><<<std::min(1024, (lu->S.n + 255) / 256), 256, 0, lu->stream>>>(
       d, (T *)lu->d_y, (T *)lu->d_z);
   xg::count_launches(1);
-  xg::lu_lsolve<T><<<lu->grid_factor, 256, 0, lu->stream>>>(d, (const T *)lu->d_val, b, (T *)lu->d_y); xg::count_launches(1);
-  xg::lu_usolve<T><<<lu->grid_factor, 256, 0, lu->stream>>>(d, (const T *)lu->d_val, (const T *)lu->d_y,
-                                                            (T *)lu->d_z, x); xg::count_launches(1);
+  xg::lu_lsolve<T><<<lu->grid_tri, 256, 0, lu->stream>>>(d, (const T *)lu->d_val, b, (T *)lu->d_y); xg::count_launches(1);
+  xg::lu_usolve<T><<<lu->grid_tri, 256, 0, lu->stream>>>(d, (const T *)lu->d_val, (const T *)lu->d_y,
+                                                         (T *)lu->d_z, x); xg::count_launches(1);
   XG_CU(cudaGetLastError());
   return XG_OK;
 }
@@ -1283,13 +1339,50 @@ extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const i
   }
   int sms = 0, occ = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, lu->device);
-  if (precision == XG_LU_FP32)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, xg::lu_factor<float>, 256, 0);
-  else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, xg::lu_factor<double>, 256, 0);
+  {
+    // Stage every row when the longest fits kStageBytes per warp (the long
+    // rows of a dense trailing block are the critical path).  Otherwise (a
+    // supply node's row) all but the kUnstagedRows longest, with at least
+    // kMinStageBytes (a stage that small costs no occupancy: registers bound
+    // it first): the longest rows stay in global memory rather than cut the
+    // number of resident warps.
+    std::vector<int> len(n);
+    for (int i = 0; i < n; ++i) len[i] = S.rp[i + 1] - S.rp[i];
+    const int max_row = *std::max_element(len.begin(), len.end());
+    const int cap_max = xg::kStageBytes / int(tsz);
+    int cap = max_row;
+    if (max_row > cap_max) {
+      const int k = std::min(n - 1, xg::kUnstagedRows);
+      std::nth_element(len.begin(), len.begin() + k, len.end(), std::greater<int>());
+      cap = std::min(cap_max, std::max(len[k], xg::kMinStageBytes / int(tsz)));
+    }
+    lu->stage_cap = (cap + 31) / 32 * 32;
+    lu->smem_grid = size_t(xg::kFactorWarps) * size_t(lu->stage_cap) * tsz;
+    const void *fn = precision == XG_LU_FP32 ? (const void *)xg::lu_factor<float>
+                                             : (const void *)xg::lu_factor<double>;
+    if ((e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  int(lu->smem_grid)))) {
+      free_lu(lu.get());
+      return cuda_fail(e, "xg_lu_analyze: cudaFuncSetAttribute");
+    }
+    if (precision == XG_LU_FP32)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, xg::lu_factor<float>, 32 * xg::kFactorWarps,
+                                                    lu->smem_grid);
+    else
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, xg::lu_factor<double>, 32 * xg::kFactorWarps,
+                                                    lu->smem_grid);
+  }
   // one warp per row: never more warps than rows
-  lu->grid_factor = std::max(1, std::min(sms * std::max(occ, 1), (n + 7) / 8));
+  lu->grid_factor = std::max(1, std::min(sms * std::max(occ, 1), (n + xg::kFactorWarps - 1) / xg::kFactorWarps));
   lu->grid_solve = std::max(1, std::min(sms * 4, int((lu->nnz_lu + 255) / 256)));
+  {
+    int occ_tri = 0;
+    if (precision == XG_LU_FP32)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_tri, xg::lu_lsolve<float>, 256, 0);
+    else
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_tri, xg::lu_lsolve<double>, 256, 0);
+    lu->grid_tri = std::max(1, std::min(sms * std::max(occ_tri, 1), (n + 7) / 8));
+  }
   // one-CTA path when the factor (and the solve's extra vectors) fit in shared memory
   {
     const size_t factor_b = xg::smem_bytes(n, lu->nnz_lu, tsz);
