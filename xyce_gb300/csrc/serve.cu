@@ -568,11 +568,11 @@ __global__ void __launch_bounds__(kBatchThreads) batch_combine(BatchDev b) {
     v[3] = fmax(v[3], fmax(fabs(b.fvp[g]), fabs(b.qvp[g])));
     v[4] = fmax(v[4], fabs(b.xc[g]));
   }
-  // the Jacobian rows: a warp per row, its lanes over the row's entries
-  for (int k = wid; k < n; k += nw) {
+  // the Jacobian rows: a thread per row (circuit rows hold a few entries; a
+  // warp per row would issue each FP64 instruction for a handful of lanes)
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
     const int g = b.uidx[u0 + k];
-    for (int p = b.arp[g] + lane; p < b.arp[g + 1]; p += 32)
-      b.jac[p] = inv_h * b.dqdx[p] + fs * b.dfdx[p];
+    for (int p = b.arp[g]; p < b.arp[g + 1]; ++p) b.jac[p] = inv_h * b.dqdx[p] + fs * b.dfdx[p];
   }
   block_sum_max(v, 2, 3, sh);
   if (threadIdx.x == 0) {
@@ -1157,7 +1157,9 @@ int enqueue_iteration(xg_batch *b) {
   int rc = v.fma ? fast::launch_reduce(ra, s) : exact::launch_reduce(ra, s);
   if (rc) return rc;
   batch_combine<<<b->nc, kBatchThreads, 0, s>>>(b->dev);
-  batch_control<<<(b->nc + 127) / 128, 128, 0, s>>>(b->dev);
+  // one warp per 32 requests: the step control is FP64-heavy (pow, sqrt,
+  // divisions), and spread over as many SMs as there are warps
+  batch_control<<<(b->nc + 31) / 32, 32, 0, s>>>(b->dev);
   batch_vector<<<b->nc, kBatchThreads, 0, s>>>(b->dev);
   count_launches(3);
   return cudaGetLastError() == cudaSuccess ? XG_OK : XG_ERR_CUDA;

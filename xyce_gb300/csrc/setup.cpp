@@ -735,40 +735,55 @@ int build_plan(const xg_netlist *nl, const xg_device_options *opt, Plan *plan, s
   P.n_state = sta;
   P.n_store = sto;
 
-  // Jacobian pattern from every matrix term (ground excluded).
   const int64_t W = (int64_t)P.n_unknowns + 1;
-  std::vector<int64_t> keys;
+  // Jacobian pattern from every matrix term (ground excluded): the terms'
+  // columns bucketed by row (a counting sort), then each row's few columns
+  // sorted and made unique, rows in parallel.
   {
-    int64_t cap = 0;
-    for (int t = 0; t < XG_NUM_DEV_TYPES; ++t) cap += (int64_t)P.T[t].n * P.T[t].nterm;
-    keys.reserve((size_t)cap);
-  }
-  for (int k = 0; k < P.n_order; ++k) {
-    int t = P.order[k];
-    const TypeData &T = P.T[t];
-    if (!T.n) continue;
-    const TypeLayout &L = type_layout(t);
-    for (int i = 0; i < T.n; ++i)
-      for (int q = 0; q < L.nterm; ++q) {
-        const TermDef &td = L.terms[q];
-        if (td.kind != OUT_DFDX && td.kind != OUT_DQDX) continue;
-        int r = T.lid[(size_t)td.row * T.n + i], c = T.lid[(size_t)td.col * T.n + i];
-        if (r == gnd || c == gnd) continue;
-        keys.push_back(r * W + c);
+    std::vector<int64_t> rcount((size_t)P.n_unknowns + 1, 0);
+    auto each_matrix_term = [&](auto &&fn) {
+      for (int k = 0; k < P.n_order; ++k) {
+        const int t = P.order[k];
+        const TypeData &T = P.T[t];
+        if (!T.n) continue;
+        const TypeLayout &L = type_layout(t);
+        for (int i = 0; i < T.n; ++i)
+          for (int q = 0; q < L.nterm; ++q) {
+            const TermDef &td = L.terms[q];
+            if (td.kind != OUT_DFDX && td.kind != OUT_DQDX) continue;
+            const int r = T.lid[(size_t)td.row * T.n + i], c = T.lid[(size_t)td.col * T.n + i];
+            if (r == gnd || c == gnd) continue;
+            fn(r, c);
+          }
       }
+    };
+    each_matrix_term([&](int r, int) { rcount[(size_t)r + 1]++; });
+    for (int r = 0; r < P.n_unknowns; ++r) rcount[(size_t)r + 1] += rcount[(size_t)r];
+    std::vector<int> cols((size_t)rcount[(size_t)P.n_unknowns]);
+    {
+      std::vector<int64_t> fill(rcount.begin(), rcount.end() - 1);
+      each_matrix_term([&](int r, int c) { cols[(size_t)fill[(size_t)r]++] = c; });
+    }
+    std::vector<int> ulen((size_t)P.n_unknowns, 0);
+    int rc = parallel_rows(P.n_unknowns, 0, [&](int r, double *, std::string *) {
+      int *b = cols.data() + rcount[(size_t)r], *e = cols.data() + rcount[(size_t)r + 1];
+      std::sort(b, e);
+      ulen[(size_t)r] = int(std::unique(b, e) - b);
+      return 0;
+    }, err);
+    if (rc) return rc;
+    P.nnz = 0;
+    for (int r = 0; r < P.n_unknowns; ++r) P.nnz += ulen[(size_t)r];
+    if (P.nnz >= (int64_t)1 << 31) { *err = "pattern too large"; return XG_ERR_ARG; }
+    P.rowptr.assign((size_t)P.n_unknowns + 1, 0);
+    for (int r = 0; r < P.n_unknowns; ++r) P.rowptr[(size_t)r + 1] = P.rowptr[(size_t)r] + ulen[(size_t)r];
+    P.colidx.resize((size_t)P.nnz);
+    rc = parallel_rows(P.n_unknowns, 0, [&](int r, double *, std::string *) {
+      std::copy_n(cols.data() + rcount[(size_t)r], ulen[(size_t)r], P.colidx.data() + P.rowptr[(size_t)r]);
+      return 0;
+    }, err);
+    if (rc) return rc;
   }
-  std::sort(keys.begin(), keys.end());
-  keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
-  P.nnz = (int64_t)keys.size();
-  if (P.nnz >= (int64_t)1 << 31) { *err = "pattern too large"; return XG_ERR_ARG; }
-  P.rowptr.assign((size_t)P.n_unknowns + 1, 0);
-  P.colidx.resize((size_t)P.nnz);
-  for (int64_t j = 0; j < P.nnz; ++j) {
-    P.rowptr[(size_t)(keys[j] / W) + 1]++;
-    P.colidx[(size_t)j] = (int)(keys[j] % W);
-  }
-  for (int r = 0; r < P.n_unknowns; ++r) P.rowptr[r + 1] += P.rowptr[r];
-  std::vector<int64_t>().swap(keys);
 
   // Term plan.
   P.n_vec_out = 4 * W;
@@ -792,40 +807,59 @@ int build_plan(const xg_netlist *nl, const xg_device_options *opt, Plan *plan, s
     const int *it = std::lower_bound(b, e, c);
     return (int64_t)(it - P.colidx.data());
   };
-  std::vector<int64_t> &cnt = P.red_ptr;
-  cnt.assign((size_t)P.n_out + 1, 0);
-  std::vector<int64_t> out_of;  // per kept term: output index
-  std::vector<uint32_t> idx_of;
-  out_of.reserve((size_t)P.n_terms);
-  idx_of.reserve((size_t)P.n_terms);
+  // The output of every term (-1: none), instances in parallel; kept per
+  // instance in statement order so the counting passes read it in sequence.
+  std::vector<int64_t> out_of((size_t)P.n_terms);
   for (int k = 0; k < P.n_order; ++k) {
-    int t = P.order[k];
+    const int t = P.order[k];
     const TypeData &T = P.T[t];
     if (!T.n) continue;
     const TypeLayout &L = type_layout(t);
-    for (int i = 0; i < T.n; ++i)
+    int rc = parallel_rows(T.n, 0, [&](int i, double *, std::string *) {
+      int64_t *o_i = out_of.data() + T.term0 + (int64_t)i * L.nterm;
       for (int q = 0; q < L.nterm; ++q) {
         const TermDef &td = L.terms[q];
-        int r = T.lid[(size_t)td.row * T.n + i];
-        if (r == gnd) continue;
-        int64_t o;
-        if (td.kind <= OUT_DQDXDVP) {
-          o = (int64_t)td.kind * W + r;
-        } else {
-          int c = T.lid[(size_t)td.col * T.n + i];
-          if (c == gnd) continue;
-          o = P.n_vec_out + (td.kind == OUT_DQDX ? P.nnz : 0) + slot_of(r, c);
+        int64_t o = -1;
+        const int r = T.lid[(size_t)td.row * T.n + i];
+        if (r != gnd) {
+          if (td.kind <= OUT_DQDXDVP) {
+            o = (int64_t)td.kind * W + r;
+          } else {
+            const int c = T.lid[(size_t)td.col * T.n + i];
+            if (c != gnd) o = P.n_vec_out + (td.kind == OUT_DQDX ? P.nnz : 0) + slot_of(r, c);
+          }
         }
-        out_of.push_back(o);
-        idx_of.push_back((uint32_t)(T.term0 + (int64_t)q * T.n + i));
-        cnt[(size_t)o + 1]++;
+        o_i[q] = o;
       }
+      return 0;
+    }, err);
+    if (rc) return rc;
   }
+  std::vector<int64_t> &cnt = P.red_ptr;
+  cnt.assign((size_t)P.n_out + 1, 0);
+  int64_t kept = 0;
+  for (int64_t j = 0; j < P.n_terms; ++j)
+    if (out_of[(size_t)j] >= 0) {
+      cnt[(size_t)out_of[(size_t)j] + 1]++;
+      ++kept;
+    }
   for (int64_t o = 0; o < P.n_out; ++o) cnt[(size_t)o + 1] += cnt[(size_t)o];
-  P.red_idx.resize(out_of.size());
+  P.red_idx.resize((size_t)kept);
   {
+    // the (type, instance, statement) order of the reference's loads
     std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
-    for (size_t j = 0; j < out_of.size(); ++j) P.red_idx[(size_t)fill[(size_t)out_of[j]]++] = idx_of[j];
+    for (int k = 0; k < P.n_order; ++k) {
+      const int t = P.order[k];
+      const TypeData &T = P.T[t];
+      if (!T.n) continue;
+      const int nterm = type_layout(t).nterm;
+      for (int i = 0; i < T.n; ++i) {
+        const int64_t *o_i = out_of.data() + T.term0 + (int64_t)i * nterm;
+        for (int q = 0; q < nterm; ++q)
+          if (o_i[q] >= 0)
+            P.red_idx[(size_t)fill[(size_t)o_i[q]]++] = (uint32_t)(T.term0 + (int64_t)q * T.n + i);
+      }
+    }
   }
   // scatter layout unless BSIM3 terms make up half of all terms; terms with
   // no output (a stamp on the ground row or column) then go to a discard slot
