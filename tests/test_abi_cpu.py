@@ -100,3 +100,19 @@ def test_context_without_gpu_fails_cleanly(engine_lib):
     h = C.c_void_p()
     rc = engine.lib().xg_ctx_create(0, C.byref(h))
     assert rc in (-1, -2) and not h.value
+
+
+def test_model_set_matches_separate_cards(engine_lib):
+    """A ModelSet (Monte-Carlo cards as arrays) gives the same set-up as the
+    same cards added one Model at a time, and the same flat arrays."""
+    nl = netlists.ring_oscillator(9, seed=4)
+    assert isinstance(nl.models[0], abi.ModelSet) and nl.n_models == 18
+    per_card = netlists.ring_oscillator(9, seed=4)
+    per_card.models = list(nl.cards())
+    assert all(isinstance(m, abi.Model) for m in per_card.models)
+    opt = abi.device_options()
+    for t in range(abi.NUM_DEV_TYPES):
+        if nl.count(t):
+            assert np.array_equal(engine.setup_params(nl, t, opt), engine.setup_params(per_card, t, opt))
+    a, b = nl.to_arrays(), per_card.to_arrays()
+    assert a.keys() == b.keys() and all(np.array_equal(a[k], b[k]) for k in a)

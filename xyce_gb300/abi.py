@@ -143,6 +143,32 @@ class Model:
         self.params = {k.upper(): float(v) for k, v in params.items()}
 
 
+class ModelSet:
+    """Many .MODEL cards of one device type that give the same parameters
+    (Monte-Carlo variants): polarity per card and a values[card, param]
+    array.  A netlist keeps it as one entry that stands for len(self) cards
+    with consecutive indices, and hands them to the C ABI without a Python
+    loop over the cards."""
+
+    def __init__(self, type_, polarity, **params):
+        self.type = type_
+        self.names = tuple(k.upper() for k in params)
+        cols = [np.asarray(v, np.float64).reshape(-1) for v in params.values()]
+        n = len(cols[0]) if cols else len(np.atleast_1d(polarity))
+        self.values = np.ascontiguousarray(np.column_stack(cols) if cols else np.zeros((n, 0)))
+        self.polarity = np.broadcast_to(np.asarray(polarity, np.int32), (n,)).copy()
+
+    def __len__(self):
+        return len(self.polarity)
+
+    def cards(self):
+        """The cards as Model objects."""
+        for i in range(len(self)):
+            m = Model(self.type, int(self.polarity[i]))
+            m.params = dict(zip(self.names, (float(v) for v in self.values[i])))
+            yield m
+
+
 class Netlist:
     """Device arrays per type; node -1 is ground."""
 
@@ -159,8 +185,25 @@ class Netlist:
         self.bsim3 = None
 
     def add_model(self, model):
+        """Add a Model (returns its index) or a ModelSet (returns the indices
+        of its cards)."""
+        first = self.n_models
         self.models.append(model)
-        return len(self.models) - 1
+        if isinstance(model, ModelSet):
+            return np.arange(first, first + len(model))
+        return first
+
+    @property
+    def n_models(self):
+        return sum(len(m) if isinstance(m, ModelSet) else 1 for m in self.models)
+
+    def cards(self):
+        """Every model card as a Model, in index order."""
+        for m in self.models:
+            if isinstance(m, ModelSet):
+                yield from m.cards()
+            else:
+                yield m
 
     _GROUPS = ("res", "cap", "vsrc", "isrc", "diode", "mos1", "bsim3")
 
@@ -169,7 +212,7 @@ class Netlist:
         out = {"n_nodes": np.array(self.n_nodes)}
         if self.type_order is not None:
             out["type_order"] = np.asarray(self.type_order, np.int32)
-        for mi, m in enumerate(self.models):
+        for mi, m in enumerate(self.cards()):
             out[f"model{mi}.meta"] = np.array([m.type, m.polarity])
             out[f"model{mi}.names"] = np.array(list(m.params.keys()), dtype="U16")
             out[f"model{mi}.values"] = np.array(list(m.params.values()), np.float64)
@@ -213,24 +256,42 @@ class Netlist:
         # the model cards as one array laid out like xg_model_desc, one value
         # buffer for every card, and name arrays shared by cards that give the
         # same parameters (Monte-Carlo variants give many such cards)
-        nm = len(self.models)
-        allv = _darr([v for m in self.models for v in m.params.values()] or [0.0])
+        nm = self.n_models
         mods = np.zeros(max(1, nm), dtype=_MODEL_DTYPE)
+        allv = np.zeros(1)
         if nm:
-            name_addr = np.empty(nm, np.uint64)
-            for i, m in enumerate(self.models):
-                key = tuple(m.params)
+            def names_addr(key):
                 names = _NAME_ARRAYS.get(key)
                 if names is None:
                     arr_ = (C.c_char_p * max(1, len(key)))(*[k.encode() for k in key])
                     names = _NAME_ARRAYS[key] = (arr_, C.addressof(arr_))
-                name_addr[i] = names[1]
-            lens = np.fromiter((len(m.params) for m in self.models), np.int64, nm)
-            offs = np.concatenate(([0], np.cumsum(lens)[:-1]))
-            mods["type"][:nm] = np.fromiter((m.type for m in self.models), np.int32, nm)
-            mods["polarity"][:nm] = np.fromiter((m.polarity for m in self.models), np.int32, nm)
-            mods["n_params"][:nm] = lens
-            mods["names"][:nm] = name_addr
+                return names[1]
+            # per entry (a card or a set of cards): count, type, polarities,
+            # parameter names and values
+            cnt, typ, pol, lens, addr, vals = [], [], [], [], [], []
+            for m in self.models:
+                if isinstance(m, ModelSet):
+                    n, k = len(m), len(m.names)
+                    pol.append(m.polarity)
+                    vals.append(m.values.reshape(-1))
+                    key = m.names
+                else:
+                    n, k = 1, len(m.params)
+                    pol.append(np.array([m.polarity], np.int32))
+                    vals.append(np.fromiter(m.params.values(), np.float64, k))
+                    key = tuple(m.params)
+                cnt.append(n)
+                typ.append(m.type)
+                lens.append(k)
+                addr.append(names_addr(key))
+            cnt = np.asarray(cnt, np.int64)
+            per_card = np.repeat(np.asarray(lens, np.int64), cnt)
+            allv = _darr(np.concatenate(vals) if sum(len(v) for v in vals) else np.zeros(1))
+            offs = np.concatenate(([0], np.cumsum(per_card)[:-1]))
+            mods["type"][:nm] = np.repeat(np.asarray(typ, np.int32), cnt)
+            mods["polarity"][:nm] = np.concatenate(pol)
+            mods["n_params"][:nm] = per_card
+            mods["names"][:nm] = np.repeat(np.asarray(addr, np.uint64), cnt)
             mods["values"][:nm] = np.uint64(allv.ctypes.data) + (8 * offs).astype(np.uint64)
         keep += [allv, mods]
         nl.n_models = nm

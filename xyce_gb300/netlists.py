@@ -129,16 +129,14 @@ def ring_oscillator(stages=5, seed=0, sigma=0.10 / 3, cload=10e-15, vdd=1.8):
     nxt = np.roll(nodes, -1)
     dv = np.clip(rng.normal(0, sigma, (2, stages)), -0.1, 0.1)
     dk = np.clip(rng.normal(0, sigma, (2, stages)), -0.1, 0.1)
-    mods = []
-    for k in range(stages):
-        mods.append(nl.add_model(abi.Model(abi.DEV_MOS1, 1, VTO=0.7 * (1 + dv[0, k]),
-                                           KP=110e-6 * (1 + dk[0, k]))))
-        mods.append(nl.add_model(abi.Model(abi.DEV_MOS1, -1, VTO=-0.7 * (1 + dv[1, k]),
-                                           KP=50e-6 * (1 + dk[1, k]))))
+    # the cards per stage: NMOS then PMOS, each its own variant
+    vto = np.ravel(np.column_stack([0.7 * (1 + dv[0]), -0.7 * (1 + dv[1])]))
+    kp = np.ravel(np.column_stack([110e-6 * (1 + dk[0]), 50e-6 * (1 + dk[1])]))
+    mods = nl.add_model(abi.ModelSet(abi.DEV_MOS1, np.tile([1, -1], stages), VTO=vto, KP=kp))
     d = np.repeat(nxt, 2)
     g = np.repeat(nodes, 2)
     s = np.ravel(np.column_stack([np.full(stages, -1), np.zeros(stages, int)]))
-    nl.mos1 = dict(d=d, g=g, s=s, b=s.copy(), model=np.array(mods),
+    nl.mos1 = dict(d=d, g=g, s=s, b=s.copy(), model=mods,
                    w=np.tile([2e-6, 4e-6], stages), l=np.full(2 * stages, 1e-6))
     nl.cap = dict(p=nodes, m=np.full(stages, -1), value=np.full(stages, cload))
     nl.vsrc = dict(p=[0], m=[-1], kind=[abi.SRC_DC], wave=[[vdd, 0, 0, 0, 0, 0, 0]])
