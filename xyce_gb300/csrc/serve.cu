@@ -68,6 +68,7 @@ struct BatchDev {
   const int *uptr, *uidx;        // unknowns of request c (union ids, local order)
   const int *sptr, *sidx;        // its state slots: ranges (start, length) sptr[c]..sptr[c+1]
   const int *optr, *oidx;        // its store slots, the same way
+  const int *jptr, *jidx;        // its Jacobian entries (its rows), the same way
   const int *arp, *aci;          // union Jacobian pattern
   const int *lrp_off;            // request c's local row pointers start here (n_c + 1)
   const int64_t *lnz_off;        // its L\U entries start here
@@ -533,12 +534,16 @@ __device__ void block_sum_max(double *vals, int nsum, int nmax, double *sh) {
   if (lane == 0)
     for (int j = 0; j < m; ++j) sh[wid * m + j] = vals[j];
   __syncthreads();
-  if (threadIdx.x == 0)
-    for (int j = 0; j < m; ++j) {
-      double acc = sh[j];
-      for (int w = 1; w < nw; ++w) acc = j < nsum ? acc + sh[w * m + j] : fmax(acc, sh[w * m + j]);
-      vals[j] = acc;
+  // lane j of warp 0 combines value j over the warps, in warp order; the
+  // results reach every lane of warp 0 (thread 0 reads them)
+  if (wid == 0) {
+    double acc = 0.0;
+    if (lane < m) {
+      acc = sh[lane];
+      for (int w = 1; w < nw; ++w) acc = lane < nsum ? acc + sh[w * m + lane] : fmax(acc, sh[w * m + lane]);
     }
+    for (int j = 0; j < m; ++j) vals[j] = __shfl_sync(0xffffffffu, acc, j);
+  }
 }
 
 // ---- batch_combine: residual, Jacobian and norms (one block per request) ------
@@ -568,11 +573,11 @@ __global__ void __launch_bounds__(kBatchThreads) batch_combine(BatchDev b) {
     v[3] = fmax(v[3], fmax(fabs(b.fvp[g]), fabs(b.qvp[g])));
     v[4] = fmax(v[4], fabs(b.xc[g]));
   }
-  // the Jacobian rows: a thread per row (circuit rows hold a few entries; a
-  // warp per row would issue each FP64 instruction for a handful of lanes)
-  for (int k = threadIdx.x; k < n; k += blockDim.x) {
-    const int g = b.uidx[u0 + k];
-    for (int p = b.arp[g]; p < b.arp[g + 1]; ++p) b.jac[p] = inv_h * b.dqdx[p] + fs * b.dfdx[p];
+  // the Jacobian entries of the request's rows, as runs of consecutive
+  // entries spread over the block (a supply row's hundreds of entries too)
+  for (int k = b.jptr[c]; k < b.jptr[c + 1]; ++k) {
+    const int p0 = b.jidx[2 * k], p1 = p0 + b.jidx[2 * k + 1];
+    for (int p = p0 + threadIdx.x; p < p1; p += blockDim.x) b.jac[p] = inv_h * b.dqdx[p] + fs * b.dfdx[p];
   }
   block_sum_max(v, 2, 3, sh);
   if (threadIdx.x == 0) {
@@ -917,6 +922,7 @@ struct xg_batch {
   int graph_iters = 0;
   int graph_launches_per_iter = 0;
   size_t solve_smem = 0;               // > 0: batch_solve_smem with this much shared memory
+  int n_walk = 0;                      // requests walked row by row (not on the level path)
   size_t solve_lvl = 0;                // > 0: batch_solve_lvl (for its requests) with this much
   int64_t bytes = 0;
   // pinned host mirror of the request states
@@ -1125,15 +1131,17 @@ int enqueue_iteration(xg_batch *b) {
   const Plan &P = *v.plan;
   cudaStream_t s = b->stream;
   const int blocks4 = (b->nc + 3) / 4;
-  if (b->solve_smem) {
+  if (!b->n_walk) {
+    // every request is on the level path
+  } else if (b->solve_smem) {
     if (b->precision == XG_LU_FP32) batch_solve_smem<float><<<b->nc, 32, b->solve_smem, s>>>(b->dev);
     else batch_solve_smem<double><<<b->nc, 32, b->solve_smem, s>>>(b->dev);
-  } else if (b->precision == XG_LU_FP32) {
-    batch_solve<float><<<blocks4, 128, 0, s>>>(b->dev);
+    count_launches(1);
   } else {
-    batch_solve<double><<<blocks4, 128, 0, s>>>(b->dev);
+    if (b->precision == XG_LU_FP32) batch_solve<float><<<blocks4, 128, 0, s>>>(b->dev);
+    else batch_solve<double><<<blocks4, 128, 0, s>>>(b->dev);
+    count_launches(1);
   }
-  count_launches(1);
   if (b->solve_lvl) {
     if (b->precision == XG_LU_FP32)
       batch_solve_lvl<float><<<b->nc, kLvlThreads, b->solve_lvl, s>>>(b->dev);
@@ -1243,7 +1251,8 @@ extern "C" int xg_batch_create(xg_ctx *ctx, int n, const xg_netlist *const *nls,
       set_error("xg_batch_create: an unknown belongs to no request");
       return XG_ERR_ARG;
     }
-  std::vector<int> uptr(n + 1, 0), uidx, sptr(n + 1, 0), sidx, optr(n + 1, 0), oidx;
+  std::vector<int> uptr(n + 1, 0), uidx, sptr(n + 1, 0), sidx, optr(n + 1, 0), oidx, jptr(n + 1, 0),
+      jidx;
   // slot lists -> runs of consecutive slots (start, length)
   auto runs = [](const std::vector<int> &v, std::vector<int> *out) {
     int cnt = 0;
@@ -1263,6 +1272,22 @@ extern "C" int xg_batch_create(xg_ctx *ctx, int n, const xg_netlist *const *nls,
     sptr[r + 1] = sptr[r] + runs(sl[r], &sidx);
     optr[r + 1] = optr[r] + runs(ol[r], &oidx);
     b->n_unk.push_back(int(l2u[r].size()));
+    // Jacobian entries of the request's rows: consecutive rows merge
+    std::vector<int> rows(l2u[r]);
+    std::sort(rows.begin(), rows.end());
+    int nj = 0;
+    for (size_t k = 0; k < rows.size();) {
+      size_t e = k + 1;
+      while (e < rows.size() && rows[e] == rows[e - 1] + 1) ++e;
+      const int p0 = P.rowptr[rows[k]], p1 = P.rowptr[rows[e - 1] + 1];
+      if (p1 > p0) {
+        jidx.push_back(p0);
+        jidx.push_back(p1 - p0);
+        ++nj;
+      }
+      k = e;
+    }
+    jptr[r + 1] = jptr[r] + nj;
   }
   // starting point and a first Jacobian (dF/dx + dQ/dx / tstep) for the
   // per-request pivot analysis
@@ -1410,12 +1435,13 @@ extern "C" int xg_batch_create(xg_ctx *ctx, int n, const xg_netlist *const *nls,
   d.max_points = o->max_points;
   d.n_refine = o->lu_precision == XG_LU_FP32 ? o->n_refine : 0;
   int *t_uptr, *t_uidx, *t_sptr, *t_sidx, *t_optr, *t_oidx, *t_lrp_off, *t_lrp, *t_lci, *t_ldiag,
-      *t_lP, *t_lQ, *t_out, *t_arp, *t_aci;
+      *t_lP, *t_lQ, *t_out, *t_arp, *t_aci, *t_jptr, *t_jidx;
   int64_t *t_lnz_off, *t_lu2a, *t_sched_off;
   int *t_sched, *t_lvl;
   if (dev_copy(b.get(), &t_uptr, uptr) || dev_copy(b.get(), &t_uidx, uidx) ||
       dev_copy(b.get(), &t_sptr, sptr) || dev_copy(b.get(), &t_sidx, sidx) ||
       dev_copy(b.get(), &t_optr, optr) || dev_copy(b.get(), &t_oidx, oidx) ||
+      dev_copy(b.get(), &t_jptr, jptr) || dev_copy(b.get(), &t_jidx, jidx) ||
       dev_copy(b.get(), &t_lrp_off, lrp_off) || dev_copy(b.get(), &t_lnz_off, lnz_off) ||
       dev_copy(b.get(), &t_lrp, lrp) || dev_copy(b.get(), &t_lci, lci) ||
       dev_copy(b.get(), &t_ldiag, ldiag) || dev_copy(b.get(), &t_lu2a, lu2a) ||
@@ -1426,6 +1452,7 @@ extern "C" int xg_batch_create(xg_ctx *ctx, int n, const xg_netlist *const *nls,
     return XG_ERR_OOM;
   }
   d.uptr = t_uptr; d.uidx = t_uidx; d.sptr = t_sptr; d.sidx = t_sidx; d.optr = t_optr; d.oidx = t_oidx;
+  d.jptr = t_jptr; d.jidx = t_jidx;
   d.arp = t_arp; d.aci = t_aci; d.lrp_off = t_lrp_off; d.lnz_off = t_lnz_off; d.lrp = t_lrp;
   d.lci = t_lci; d.ldiag = t_ldiag; d.lu2a = t_lu2a; d.lP = t_lP; d.lQ = t_lQ; d.out_idx = t_out;
   const size_t tsz = o->lu_precision == XG_LU_FP32 ? sizeof(float) : sizeof(double);
@@ -1464,6 +1491,7 @@ extern "C" int xg_batch_create(xg_ctx *ctx, int n, const xg_netlist *const *nls,
     d.sched_off = t_sched_off;
     d.sched = t_sched;
     d.lvl = t_lvl;
+    b->n_walk = n - int(std::count(lvl_req.begin(), lvl_req.end(), 1));
   }
   {
     size_t need = 0;

@@ -6,8 +6,10 @@ Masters of one netlist, `update_state` / `load_dae_vectors` /
 loadDAEMatrices, and `load` runs all three.  Every call goes to the CUDA
 engine; there is no CPU fallback — a missing library or GPU raises.
 """
+import atexit
 import ctypes as C
 import os
+import weakref
 
 import numpy as np
 
@@ -15,6 +17,22 @@ from . import abi
 
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libxg.so")
 _lib = None
+
+# Handles still open at interpreter exit are closed while the library and the
+# CUDA runtime are intact, batches, factorisations and circuits before the
+# contexts whose streams they use (finalisation would otherwise free them in
+# no fixed order).
+_OPEN = {k: weakref.WeakSet() for k in ("batch", "lu", "circuit", "context")}
+
+
+@atexit.register
+def _close_open_handles():
+    for kind in ("batch", "lu", "circuit", "context"):
+        for obj in list(_OPEN[kind]):
+            try:
+                obj.close()
+            except Exception:
+                pass
 
 
 class XgError(RuntimeError):
@@ -115,6 +133,7 @@ class Context:
         h = C.c_void_p()
         check(lib().xg_ctx_create(device, C.byref(h)))
         self.h = h
+        _OPEN["context"].add(self)
         if options is not None:
             self.set_options(options)
 
@@ -150,6 +169,7 @@ class Circuit:
         h = C.c_void_p()
         check(lib().xg_circuit_create(ctx.h, C.byref(self._nl), C.byref(h)))
         self.h = h
+        _OPEN["circuit"].add(self)
         info = abi.XgCircuitInfo()
         check(lib().xg_circuit_get_info(h, C.byref(info)))
         self.info = info
@@ -256,6 +276,7 @@ class LU:
         check(lib().xg_lu_analyze(ctx.h, self.n, _ptr(self.rowptr), _ptr(self.colidx), _ptr(vals),
                                   precision, C.byref(h)))
         self.h = h
+        _OPEN["lu"].add(self)
         info = abi.XgLuInfo()
         check(lib().xg_lu_get_info(h, C.byref(info)))
         self.info = info
@@ -362,6 +383,7 @@ class Batch:
         check(lib().xg_batch_create(ctx.h, n, nl_arr, x0_arr, _ptr(self._ts), out_arr, C.byref(o),
                                     C.byref(h)))
         self.h = h
+        _OPEN["batch"].add(self)
         self.n = n
 
     def run(self, iterations):
