@@ -168,3 +168,25 @@ def test_fused_refactor_solve_matches_separate_calls(case, gpu_ctx, oracle_lib):
         lu.close()
     assert np.array_equal(xs[0], xs[1])
     assert _backward_error(A, xs[1], b.cpu().numpy()) <= 1e-13
+
+
+@pytest.mark.parametrize("precision,n_refine", [(abi.LU_FP64, 0), (abi.LU_FP32, 3)])
+def test_grid_refactor_of_a_row_too_long_to_stage(precision, n_refine, gpu_ctx):
+    """An arrowhead (a supply node coupled to 20,000 others): the last row of
+    the factor is longer than any shared-memory stage, so the grid refactor
+    eliminates it in global memory while the short rows are staged."""
+    import scipy.sparse as sp
+    n = 20001
+    rng = np.random.default_rng(14)
+    k = np.arange(n - 1)
+    rows = np.r_[np.arange(n), k, np.full(n - 1, n - 1)]
+    cols = np.r_[np.arange(n), np.full(n - 1, n - 1), k]
+    vals = np.r_[rng.uniform(4.0, 5.0, n - 1), float(n), rng.uniform(-1, 1, n - 1), rng.uniform(-1, 1, n - 1)]
+    A = sp.csr_matrix((vals, (rows, cols)), shape=(n, n))
+    A.sort_indices()
+    b = rng.standard_normal(n)
+    x, st, info = _solve(gpu_ctx, A, A, b, precision, n_refine)
+    assert st == 0 and info.nnz_lu >= 3 * (n - 1)
+    assert _backward_error(A, x, b) <= 1e-13
+    ref = sla.spsolve(A.tocsc(), b)
+    assert np.abs(x - ref).max() <= 1e-9 * np.abs(ref).max()

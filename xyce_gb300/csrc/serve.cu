@@ -523,6 +523,10 @@ __global__ void __launch_bounds__(kLvlThreads) batch_solve_lvl(BatchDev b) {
 // stages has thousands of unknowns, state slots and Jacobian entries, and its
 // supply row alone has one entry per device on the rail.
 constexpr int kBatchThreads = 256;
+// batch_vector's phases are chains of dependent gathers (request -> union
+// id -> history): a thread per unknown for requests up to 512 unknowns
+// keeps each phase one round trip deep
+constexpr int kVectorThreads = 512;
 
 // Block-wide sum and max in a fixed order (lane butterfly, then warps in
 // order): the same result whatever the batch around the request.
@@ -804,7 +808,7 @@ __global__ void batch_control(BatchDev b) {
 }
 
 // ---- batch_vector: history, rotation, record, predictor (warp per request) ---
-__global__ void __launch_bounds__(kBatchThreads) batch_vector(BatchDev b) {
+__global__ void __launch_bounds__(kVectorThreads) batch_vector(BatchDev b) {
   const int c = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
   if (c >= b.nc) return;
   CState &cs = b.cs[c];
@@ -1168,7 +1172,7 @@ int enqueue_iteration(xg_batch *b) {
   // one warp per 32 requests: the step control is FP64-heavy (pow, sqrt,
   // divisions), and spread over as many SMs as there are warps
   batch_control<<<(b->nc + 31) / 32, 32, 0, s>>>(b->dev);
-  batch_vector<<<b->nc, kBatchThreads, 0, s>>>(b->dev);
+  batch_vector<<<b->nc, kVectorThreads, 0, s>>>(b->dev);
   count_launches(3);
   return cudaGetLastError() == cudaSuccess ? XG_OK : XG_ERR_CUDA;
 }
