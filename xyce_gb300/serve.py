@@ -12,6 +12,7 @@ short request leaves as soon as it is done, not when its batch is.
 Latency = completion - arrival, reported as p50 / p99 beside throughput.
 """
 import collections
+import gc
 import time
 
 import numpy as np
@@ -97,7 +98,18 @@ class Server:
         return take
 
     def run(self, requests, arrivals):
-        """Serve requests arriving at the given times (s); returns a summary."""
+        """Serve requests arriving at the given times (s); returns a summary.
+        No cyclic garbage collection runs meanwhile: a full collection over
+        the requests' netlists would stall the loop that keeps the GPU fed."""
+        was = gc.isenabled()
+        gc.disable()
+        try:
+            return self._run(requests, arrivals)
+        finally:
+            if was:
+                gc.enable()
+
+    def _run(self, requests, arrivals):
         n = len(requests)
         for r, a in zip(requests, arrivals):
             r.arrival = float(a)
@@ -120,7 +132,7 @@ class Server:
                 nb = b.device_bytes()
                 self.bytes_per_unknown = nb / max(1, sum(len(r.x0) for r in pending[1]))
                 in_use += nb - pending[2]
-                active.append([b, pending[1], [False] * len(pending[1]), nb])
+                active.append([b, pending[1], [False] * len(pending[1]), nb, 0])
                 pending = None
                 busy = True
             if pending is None and queue and len(active) < self.max_concurrent:
@@ -135,20 +147,23 @@ class Server:
                 else:
                     queue.extendleft(reversed(take))
             for entry in list(active):
-                b, reqs, fin, nb = entry
+                b, reqs, fin, nb, seen = entry
                 nd = b.poll(wait=False)
                 if nd < 0:
                     continue
                 busy = True
                 t_now = time.perf_counter() - t0
-                for j, r in enumerate(reqs):
-                    if not fin[j]:
-                        st = b.stats(j)
-                        if st["finished"]:
-                            fin[j] = True
-                            r.done = t_now
-                            r.result = b.results(j)
-                            done += 1
+                if nd > seen:
+                    # some requests finished since the last look: find them
+                    entry[4] = nd
+                    for j, r in enumerate(reqs):
+                        if not fin[j]:
+                            st = b.stats(j)
+                            if st["finished"]:
+                                fin[j] = True
+                                r.done = t_now
+                                r.result = b.results(j)
+                                done += 1
                 if all(fin):
                     b.close()
                     in_use -= nb
