@@ -8,8 +8,9 @@
 //
 //  * refactor: row-wise ("up-looking") elimination of B = A(P, Q).  One warp
 //    owns one row; rows are claimed in ascending order from a counter, and a
-//    row waits (bounded spin on a per-row epoch flag) only for the rows k of
-//    its L part, at the moment it reaches them.  Every row a warp waits for
+//    row waits (bounded spin on row k's reciprocal pivot, which holds a
+//    pending pattern until row k is done) only for the rows k of its L part,
+//    at the moment it reaches them.  Every row a warp waits for
 //    was claimed earlier by a running warp, so the schedule always advances.
 //    Rows far apart in the elimination order run concurrently; the row
 //    pipeline needs no level barriers.  Each entry of a row is updated by one
@@ -24,8 +25,8 @@
 //  * precision: factors in FP64, or in FP32 with FP64 iterative refinement
 //    (r = b - A x with the FP64 matrix, solve, x += d).
 //
-// Epochs and claim counters live in device memory and are advanced by the
-// kernel that precedes each phase, so a captured sequence can be replayed.
+// Claim counters and pending patterns live in device memory and are reset by
+// the kernel that precedes each phase, so a captured sequence can be replayed.
 // Every spin has an iteration limit; a wait that gives up records bit 1 in the
 // status word and the row is finished anyway, so a launch always ends.
 
@@ -47,7 +48,7 @@ namespace xg {
 namespace {
 
 enum Ctrl : int {
-  C_EPOCH_F = 0, C_CLAIM_F, C_EPOCH_S, C_CLAIM_L, C_CLAIM_U, C_STATUS, C_BAD_ROW, C_N
+  C_CLAIM_F = 0, C_CLAIM_L, C_CLAIM_U, C_STATUS, C_BAD_ROW, C_N
 };
 enum Status : unsigned { ST_PIVOT = 1u, ST_TIMEOUT = 2u, ST_PATTERN = 4u };
 
@@ -62,23 +63,6 @@ __device__ __forceinline__ void st_release(unsigned *p, unsigned v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// Wait until flag == epoch; false (and the timeout bit set) if it never does.
-// Once any wait of the launch has given up, the others give up at their next
-// check, so a broken schedule ends in one wait time rather than one per row.
-__device__ bool wait_epoch(const unsigned *flag, unsigned epoch, unsigned *ctrl) {
-  int it = 0;
-  while (ld_acquire(flag) != epoch) {
-    ++it;
-    if (it > kSpinLimit ||
-        ((it & 1023) == 0 && (*(volatile unsigned *)&ctrl[C_STATUS] & ST_TIMEOUT))) {
-      atomicOr(&ctrl[C_STATUS], ST_TIMEOUT);
-      return false;
-    }
-    if (it > 32) __nanosleep(64);
-  }
-  return true;
-}
-
 struct LuDev {
   int n;
   const int *rp, *ci, *diag;  // L\U pattern of B
@@ -88,7 +72,6 @@ struct LuDev {
   const int64_t *urp;         // per row: start of its updates in upos
   const int *upos;            // per update: the position in the row it updates
   unsigned *ctrl;
-  unsigned *done_f, *done_l, *done_u;
   void *rdiag;                // 1 / U(k,k) per row, written by the refactor
 };
 
@@ -195,14 +178,14 @@ __device__ __forceinline__ void publish_release(T *p, T v) {
 }
 
 // Scatter A into the L\U value array (fill entries zero), keep an FP64 copy of
-// A for the residual, and open a new factorisation epoch.
+// A for the residual, reset the claim counter and status, and mark every
+// reciprocal pivot pending.
 template <class T>
 __global__ void lu_assemble(LuDev d, const double *__restrict__ a, double *__restrict__ a_copy,
                             int64_t nnz_a, T *__restrict__ val, int64_t nnz_lu) {
   const int64_t stride = int64_t(gridDim.x) * blockDim.x;
   const int64_t t0 = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (t0 == 0) {
-    d.ctrl[C_EPOCH_F] += 1;
     d.ctrl[C_CLAIM_F] = 0;
     d.ctrl[C_STATUS] = 0;
     d.ctrl[C_BAD_ROW] = 0xffffffffu;
@@ -327,7 +310,6 @@ template <class T>
 __global__ void lu_solve_open(LuDev d, T *y, T *z) {
   const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
   if (t0 == 0) {
-    d.ctrl[C_EPOCH_S] += 1;
     d.ctrl[C_CLAIM_L] = 0;
     d.ctrl[C_CLAIM_U] = 0;
   }
@@ -483,7 +465,6 @@ __global__ void __launch_bounds__(kSeqThreads) lu_factor_seq(LuDev d, const doub
   SmemLU<T> L = smem_layout<T>(smem, d.n, nnz);
   const int n = d.n;
   if (threadIdx.x == 0) {
-    d.ctrl[C_EPOCH_F] += 1;
     d.ctrl[C_STATUS] = 0;
     d.ctrl[C_BAD_ROW] = 0xffffffffu;
   }
@@ -596,7 +577,6 @@ __global__ void __launch_bounds__(kCtaThreads) lu_factor_cta(LuDev d, const doub
   const int n = d.n;
   if (threadIdx.x == 0) {
     claim = 0;
-    d.ctrl[C_EPOCH_F] += 1;
     d.ctrl[C_STATUS] = 0;
     d.ctrl[C_BAD_ROW] = 0xffffffffu;
   }
@@ -1037,7 +1017,6 @@ __device__ void lvl_solve(const LuDev &d, const LvlDev &v, const LvlSmem<T> &m,
 template <class T>
 __device__ void lvl_open(const LuDev &d) {
   if (threadIdx.x == 0) {
-    d.ctrl[C_EPOCH_F] += 1;
     d.ctrl[C_STATUS] = 0;
     d.ctrl[C_BAD_ROW] = 0xffffffffu;
   }
@@ -1109,7 +1088,7 @@ struct xg_lu {
   int *d_P = nullptr, *d_Q = nullptr, *d_arp = nullptr, *d_aci = nullptr;
   int64_t *d_urp = nullptr;
   int *d_upos = nullptr;
-  unsigned *d_ctrl = nullptr, *d_done = nullptr;  // 3n flags
+  unsigned *d_ctrl = nullptr;                     // claim counters, status, bad row
   void *d_val = nullptr;                          // nnz_lu of T
   void *d_y = nullptr, *d_z = nullptr;            // n of T
   void *d_rdiag = nullptr;                        // n of T: 1 / U(k,k)
@@ -1131,7 +1110,7 @@ struct xg_lu {
   bool factored = false;
   xg::LuDev dev() const {
     return xg::LuDev{S.n, d_rp, d_ci, d_diag, d_lu2a, d_P, d_Q, d_arp, d_aci, d_urp, d_upos,
-                     d_ctrl, d_done, d_done + S.n, d_done + 2 * S.n, d_rdiag};
+                     d_ctrl, d_rdiag};
   }
 };
 
@@ -1158,7 +1137,7 @@ int upload(V **dst, const std::vector<V> &src) {
 void free_lu(xg_lu *lu) {
   void *ptrs[] = {lu->d_rp, lu->d_ci, lu->d_diag, lu->d_lu2a, lu->d_P, lu->d_Q, lu->d_arp,
                   lu->d_urp, lu->d_upos, lu->d_lvl,
-                  lu->d_aci, lu->d_ctrl, lu->d_done, lu->d_val, lu->d_y, lu->d_z, lu->d_rdiag, lu->d_a,
+                  lu->d_aci, lu->d_ctrl, lu->d_val, lu->d_y, lu->d_z, lu->d_rdiag, lu->d_a,
                   lu->d_r, lu->d_dx};
   for (void *p : ptrs)
     if (p) cudaFree(p);
@@ -1319,7 +1298,6 @@ extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const i
   const size_t tsz = precision == XG_LU_FP32 ? sizeof(float) : sizeof(double);
   cudaError_t e = cudaSuccess;
   if ((e = cudaMalloc((void **)&lu->d_ctrl, sizeof(unsigned) * xg::C_N)) ||
-      (e = cudaMalloc((void **)&lu->d_done, sizeof(unsigned) * 3 * size_t(n))) ||
       (e = cudaMalloc(&lu->d_val, tsz * size_t(lu->nnz_lu))) ||
       (e = cudaMalloc(&lu->d_y, tsz * size_t(n))) || (e = cudaMalloc(&lu->d_z, tsz * size_t(n))) ||
       (e = cudaMalloc(&lu->d_rdiag, tsz * size_t(n))) ||
@@ -1331,9 +1309,7 @@ extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const i
                                              XG_ERR_OOM)
                                           : cuda_fail(e, "xg_lu_analyze");
   }
-  // flags start at 0 and the first epoch is 1
-  if ((e = cudaMemset(lu->d_ctrl, 0, sizeof(unsigned) * xg::C_N)) ||
-      (e = cudaMemset(lu->d_done, 0, sizeof(unsigned) * 3 * size_t(n)))) {
+  if ((e = cudaMemset(lu->d_ctrl, 0, sizeof(unsigned) * xg::C_N))) {
     free_lu(lu.get());
     return cuda_fail(e, "xg_lu_analyze: cudaMemset");
   }

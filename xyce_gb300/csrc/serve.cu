@@ -553,8 +553,7 @@ __device__ void block_sum_max(double *vals, int nsum, int nmax, double *sh) {
 // ---- batch_combine: residual, Jacobian and norms (one block per request) ------
 __global__ void __launch_bounds__(kBatchThreads) batch_combine(BatchDev b) {
   __shared__ double sh[(kBatchThreads / 32) * 5];
-  const int c = blockIdx.x, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int nw = blockDim.x >> 5;
+  const int c = blockIdx.x;
   if (c >= b.nc) return;
   const CState &cs = b.cs[c];
   if (cs.phase == PH_DONE || cs.phase == PH_INIT) return;
