@@ -190,3 +190,19 @@ def test_grid_refactor_of_a_row_too_long_to_stage(precision, n_refine, gpu_ctx):
     assert _backward_error(A, x, b) <= 1e-13
     ref = sla.spsolve(A.tocsc(), b)
     assert np.abs(x - ref).max() <= 1e-9 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("precision", [abi.LU_FP64, abi.LU_FP32])
+def test_chain_tail_matches_grid_solves(precision, gpu_ctx, oracle_lib, monkeypatch):
+    """The trailing rows of one row per level (the 60x60 grid's dense block)
+    are solved in order by one warp; its sums continue the grid solves'
+    own, so the solution is the same bit for bit as with every row solved
+    grid-wide (XG_LU_NO_CHAIN)."""
+    A = circuit_jacobian(CASES["power_grid_60x60"](), seed=5)
+    b = np.random.default_rng(15).standard_normal(A.shape[0])
+    x, st, _ = _solve(gpu_ctx, A, A, b, precision, 0)
+    monkeypatch.setenv("XG_LU_NO_CHAIN", "1")
+    x_grid, st_grid, _ = _solve(gpu_ctx, A, A, b, precision, 0)
+    assert st == 0 and st_grid == 0
+    assert np.array_equal(x, x_grid)
+    assert _backward_error(A, x, b) <= (1e-13 if precision == abi.LU_FP64 else 1e-5)

@@ -73,6 +73,12 @@ struct LuDev {
   const int *upos;            // per update: the position in the row it updates
   unsigned *ctrl;
   void *rdiag;                // 1 / U(k,k) per row, written by the refactor
+  // grid solves: rows >= tail0 (a chain of one-row levels) are solved by one
+  // warp in order (tail0 = n: none); per tail row {start, first entry in a
+  // column >= tail0, diagonal, P}, and its 32 lane sums over columns < tail0
+  int tail0;
+  const int4 *tdesc;
+  void *hpart;
 };
 
 // The grid-wide kernels carry readiness in the value itself: before a
@@ -338,6 +344,19 @@ __global__ void __launch_bounds__(256) lu_lsolve(LuDev d, const T *__restrict__ 
     row = __shfl_sync(0xffffffffu, row, 0);
     if (row >= d.n) break;
     const int s = __ldg(d.rp + row), dp = __ldg(d.diag + row);
+    if (row >= d.tail0) {
+      // a row of the chain: each lane's sum over its entries in columns below
+      // tail0 (columns ascend); the chain kernel continues it
+      const int sp = d.tdesc[row - d.tail0].y;
+      T acc = T(0);
+      for (int p = s + lane; p < sp; p += 32) {
+        const int k = __ldg(d.ci + p);
+        const T lv = __ldcg(val + p);
+        acc += lv * wait_value(y + k, d.ctrl);
+      }
+      reinterpret_cast<T *>(d.hpart)[size_t(row - d.tail0) * 32 + lane] = acc;
+      continue;
+    }
     const T bi = lane == 0 ? T(b[__ldg(d.P + row)]) : T(0);  // before any wait
     T acc = T(0);
     for (int p = s + lane; p < dp; p += 32) {
@@ -359,8 +378,8 @@ __global__ void __launch_bounds__(256) lu_usolve(LuDev d, const T *__restrict__ 
     int c = 0;
     if (lane == 0) c = int(atomicAdd(&d.ctrl[C_CLAIM_U], 1u));
     c = __shfl_sync(0xffffffffu, c, 0);
-    if (c >= d.n) break;
-    const int row = d.n - 1 - c;
+    if (c >= d.tail0) break;
+    const int row = d.tail0 - 1 - c;  // rows from tail0 on are solved already
     const int dp = __ldg(d.diag + row), e = __ldg(d.rp + row + 1);
     const T yi = lane == 0 ? __ldcg(y + row) : T(0);
     const T ri = lane == 0 ? __ldcg((const T *)d.rdiag + row) : T(0);
@@ -376,6 +395,133 @@ __global__ void __launch_bounds__(256) lu_usolve(LuDev d, const T *__restrict__ 
       const T zi = (yi - acc) * ri;
       publish(z + row, zi);
       x[qi] = double(zi);
+    }
+  }
+}
+
+// The chain at the end of a factor whose last rows each form their own
+// level (a supply node and what hangs on it): grid-wide, every row would
+// cost an L2 round trip for its one dependency; here one warp takes the rows
+// in order, keeps y and z of the chain in shared memory and loads the
+// entries of the next rows while it sums the current one.  Its sums are the
+// grid solves' own (lane-strided in column order, continued from the grid's
+// per-lane sums over earlier columns, then the butterfly), so the results
+// are the same bit for bit.  No waits: every input is final when it is read.
+constexpr int kChainR = 4;  // entries per lane held for a row (128 per row)
+
+template <class T>
+struct ChainRow {
+  int dp, p;        // the row's end and this lane's next entry
+  int k[kChainR];   // columns (-1: none)
+  T a[kChainR];     // values
+  T base;           // lower solve: the grid's lane sum; upper: 0
+  T head;           // lane 0: b(P(row)) or y(row); others 0
+  T rd;             // upper solve: 1 / U(row, row)
+};
+
+// row -> ChainRow: lower (mode 0) entries from the split point up to the
+// diagonal, upper (mode 1) entries after the diagonal
+template <class T>
+__device__ __forceinline__ void chain_fetch(const LuDev &d, const T *__restrict__ val,
+                                            const double *__restrict__ b, const T *ys, int row,
+                                            int mode, int lane, ChainRow<T> &q) {
+  const int4 ds = d.tdesc[row - d.tail0];  // {s, sp, dp, P}
+  int p;
+  if (mode == 0) {
+    p = ds.x + lane;
+    if (p < ds.y) p += (ds.y - p + 31) / 32 * 32;
+    q.dp = ds.z;
+    q.base = __ldcg(reinterpret_cast<const T *>(d.hpart) + size_t(row - d.tail0) * 32 + lane);
+    q.head = lane == 0 ? T(b[ds.w]) : T(0);
+    q.rd = T(0);
+  } else {
+    p = ds.z + 1 + lane;
+    q.dp = __ldg(d.rp + row + 1);
+    q.base = T(0);
+    q.head = lane == 0 ? ys[row - d.tail0] : T(0);
+    q.rd = lane == 0 ? __ldcg((const T *)d.rdiag + row) : T(0);
+  }
+#pragma unroll
+  for (int r = 0; r < kChainR; ++r) {
+    const int pp = p + 32 * r;
+    q.k[r] = pp < q.dp ? __ldg(d.ci + pp) : -1;
+    q.a[r] = pp < q.dp ? __ldcg(val + pp) : T(0);
+  }
+  q.p = p + 32 * kChainR;
+}
+
+// the row's sum: the held entries, then any beyond them (rows longer than
+// 128 entries past the split, loaded 128 at a time), in the same lane order;
+// a step no lane has is skipped by the warp (an FP64 instruction costs its
+// issue slot however few lanes it has)
+template <class T>
+__device__ __forceinline__ T chain_sum(const LuDev &d, const T *__restrict__ val,
+                                       const ChainRow<T> &q, const T *v) {
+  T acc = q.base;
+#pragma unroll
+  for (int r = 0; r < kChainR; ++r) {
+    if (!__any_sync(0xffffffffu, q.k[r] >= 0)) break;
+    if (q.k[r] >= 0) acc += q.a[r] * v[q.k[r] - d.tail0];
+  }
+  for (int p = q.p; __any_sync(0xffffffffu, p < q.dp); p += 32 * kChainR) {
+    int k[kChainR];
+    T a[kChainR];
+#pragma unroll
+    for (int r = 0; r < kChainR; ++r) {
+      const int pp = p + 32 * r;
+      k[r] = pp < q.dp ? __ldg(d.ci + pp) : -1;
+      a[r] = pp < q.dp ? __ldcg(val + pp) : T(0);
+    }
+#pragma unroll
+    for (int r = 0; r < kChainR; ++r)
+      if (k[r] >= 0) acc += a[r] * v[k[r] - d.tail0];
+  }
+  return warp_sum(acc);
+}
+
+template <class T>
+__global__ void __launch_bounds__(32) lu_solve_chain(LuDev d, const T *__restrict__ val,
+                                                     const double *__restrict__ b, T *y, T *z,
+                                                     double *x) {
+  extern __shared__ __align__(16) unsigned char chain_raw[];
+  const int lane = threadIdx.x, t0 = d.tail0, nt = d.n - t0;
+  T *ys = reinterpret_cast<T *>(chain_raw);
+  T *zs = ys + nt;
+  // y = L \ b(P) on the chain, rows ascending, the next two rows in flight
+  {
+    ChainRow<T> q0, q1, q2;
+    chain_fetch(d, val, b, ys, t0, 0, lane, q0);
+    if (t0 + 1 < d.n) chain_fetch(d, val, b, ys, t0 + 1, 0, lane, q1);
+    for (int row = t0; row < d.n; ++row) {
+      if (row + 2 < d.n) chain_fetch(d, val, b, ys, row + 2, 0, lane, q2);
+      const T acc = chain_sum(d, val, q0, ys);
+      if (lane == 0) {
+        const T v = q0.head - acc;
+        ys[row - t0] = v;
+        y[row] = v;
+      }
+      __syncwarp();
+      q0 = q1;
+      q1 = q2;
+    }
+  }
+  // z = U \ y, x(Q) = z on the chain, rows descending
+  {
+    ChainRow<T> q0, q1, q2;
+    chain_fetch(d, val, b, ys, d.n - 1, 1, lane, q0);
+    if (d.n - 2 >= t0) chain_fetch(d, val, b, ys, d.n - 2, 1, lane, q1);
+    for (int row = d.n - 1; row >= t0; --row) {
+      if (row - 2 >= t0) chain_fetch(d, val, b, ys, row - 2, 1, lane, q2);
+      const T acc = chain_sum(d, val, q0, zs);
+      if (lane == 0) {
+        const T zi = (q0.head - acc) * q0.rd;
+        zs[row - t0] = zi;
+        z[row] = zi;
+        x[__ldg(d.Q + row)] = double(zi);
+      }
+      __syncwarp();
+      q0 = q1;
+      q1 = q2;
     }
   }
 }
@@ -1071,6 +1217,65 @@ __global__ void __launch_bounds__(1024) lu_factor_solve_lvl(LuDev d, LvlDev v,
   lvl_solve<T>(d, v, m, x);
 }
 
+// Where the grid solves hand the trailing rows to the one-warp chain.  A
+// level of the grid solves costs an L2 round trip and a publish (~2.5 us,
+// measured); in the chain a row costs its FP64 sum and butterfly on one warp
+// (~0.35 us), an entry ~1 ns, and each 128 entries past the first 128 of a
+// row an L2 round trip (~0.7 us: they are not loaded ahead).  Candidates are
+// the last 256, 512, ... rows (y and z of the chain in shared memory); the
+// tail that saves the most modelled time over both solves wins, none when
+// nothing is saved, so only runs of nearly one row per level are taken.
+constexpr double kGridLevelSeconds = 2.5e-6;
+constexpr double kChainRowSeconds = 0.35e-6;
+constexpr double kChainEntrySeconds = 1e-9;
+constexpr double kChainReloadSeconds = 0.7e-6;
+constexpr size_t kChainBytes = 192 * 1024;
+
+int chain_start(const LuSymbolic &S, size_t tsz) {
+  const int n = S.n;
+  if (n < 4096) return n;
+  const int max_rows = int(kChainBytes / (2 * tsz));
+  // L level of each row, the levels of the rows before r, and per column the
+  // L entries below the diagonal (a tail from r holds those of columns >= r)
+  std::vector<int> lev(n), head(n + 1, 0), col_ptr(n + 1, 0);
+  for (int i = 0; i < n; ++i) {
+    int m = -1;
+    for (int p = S.rp[i]; p < S.diag[i]; ++p) {
+      m = std::max(m, lev[S.ci[p]]);
+      ++col_ptr[S.ci[p] + 1];
+    }
+    lev[i] = m + 1;
+    head[i + 1] = std::max(head[i], lev[i] + 1);
+  }
+  // the rows of each column's L entries (a tail from r gains, in each row
+  // below, its entry in column r)
+  for (int c = 0; c < n; ++c) col_ptr[c + 1] += col_ptr[c];
+  std::vector<int> col_row((size_t)col_ptr[n]), fill(col_ptr.begin(), col_ptr.end() - 1);
+  for (int i = 0; i < n; ++i)
+    for (int p = S.rp[i]; p < S.diag[i]; ++p) col_row[(size_t)fill[S.ci[p]]++] = i;
+  const int total = head[n];
+  int best = n;
+  double best_gain = 0.0;
+  int64_t entries = 0, reloads = 0;
+  std::vector<int> in_tail(n, 0);  // per row: its L entries in columns >= r
+  for (int r = n - 1; r >= std::max(1, n - max_rows); --r) {
+    for (int j = col_ptr[r]; j < col_ptr[r + 1]; ++j)
+      if (++in_tail[col_row[(size_t)j]] % 128 == 1 && in_tail[col_row[(size_t)j]] > 128) ++reloads;
+    const int u = S.rp[r + 1] - S.diag[r] - 1;
+    entries += (col_ptr[r + 1] - col_ptr[r]) + u;
+    reloads += std::max(0, (u + 127) / 128 - 1);
+    if ((n - r) % 256) continue;
+    const double saved = 2.0 * (total - head[r]) * kGridLevelSeconds;
+    const double cost = 2.0 * (n - r) * kChainRowSeconds + entries * kChainEntrySeconds +
+                        reloads * kChainReloadSeconds;
+    if (saved - cost > best_gain) {
+      best_gain = saved - cost;
+      best = r;
+    }
+  }
+  return best;
+}
+
 }  // namespace
 }  // namespace xg
 
@@ -1098,6 +1303,10 @@ struct xg_lu {
   int stage_cap = 0;                       // grid refactor: staged row entries per warp
   size_t smem_grid = 0;                    // its dynamic shared memory
   int grid_tri = 0;                        // grid solves: blocks
+  int solve_tail0 = 0;                     // grid solves: first row of the one-warp chain (n: none)
+  int4 *d_tdesc = nullptr;                 // its row descriptors
+  void *d_hpart = nullptr;                 // its rows' lane sums over earlier columns (T)
+  size_t smem_chain = 0;                   // its y and z in shared memory
   size_t smem_factor = 0, smem_solve = 0;  // > 0: the one-CTA path
   int cta_threads = 0;                     // its block size (warps ~ level width)
   bool narrow = false;                     // one lane walks the rows (<= 2 rows per level)
@@ -1110,7 +1319,7 @@ struct xg_lu {
   bool factored = false;
   xg::LuDev dev() const {
     return xg::LuDev{S.n, d_rp, d_ci, d_diag, d_lu2a, d_P, d_Q, d_arp, d_aci, d_urp, d_upos,
-                     d_ctrl, d_rdiag};
+                     d_ctrl, d_rdiag, solve_tail0, d_tdesc, d_hpart};
   }
 };
 
@@ -1137,7 +1346,7 @@ int upload(V **dst, const std::vector<V> &src) {
 void free_lu(xg_lu *lu) {
   void *ptrs[] = {lu->d_rp, lu->d_ci, lu->d_diag, lu->d_lu2a, lu->d_P, lu->d_Q, lu->d_arp,
                   lu->d_urp, lu->d_upos, lu->d_lvl,
-                  lu->d_aci, lu->d_ctrl, lu->d_val, lu->d_y, lu->d_z, lu->d_rdiag, lu->d_a,
+                  lu->d_aci, lu->d_ctrl, lu->d_tdesc, lu->d_hpart, lu->d_val, lu->d_y, lu->d_z, lu->d_rdiag, lu->d_a,
                   lu->d_r, lu->d_dx};
   for (void *p : ptrs)
     if (p) cudaFree(p);
@@ -1199,6 +1408,11 @@ int solve_once(xg_lu *lu, const double *b, double *x) {
       d, (T *)lu->d_y, (T *)lu->d_z);
   xg::count_launches(1);
   xg::lu_lsolve<T><<<lu->grid_tri, 256, 0, lu->stream>>>(d, (const T *)lu->d_val, b, (T *)lu->d_y); xg::count_launches(1);
+  if (lu->solve_tail0 < lu->S.n) {
+    xg::lu_solve_chain<T><<<1, 32, lu->smem_chain, lu->stream>>>(d, (const T *)lu->d_val, b, (T *)lu->d_y,
+                                                                (T *)lu->d_z, x);
+    xg::count_launches(1);
+  }
   xg::lu_usolve<T><<<lu->grid_tri, 256, 0, lu->stream>>>(d, (const T *)lu->d_val, (const T *)lu->d_y,
                                                          (T *)lu->d_z, x); xg::count_launches(1);
   XG_CU(cudaGetLastError());
@@ -1358,6 +1572,27 @@ extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const i
     else
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_tri, xg::lu_lsolve<double>, 256, 0);
     lu->grid_tri = std::max(1, std::min(sms * std::max(occ_tri, 1), (n + 7) / 8));
+    lu->solve_tail0 = std::getenv("XG_LU_NO_CHAIN") ? n : xg::chain_start(S, tsz);
+    const int t0 = lu->solve_tail0, nt = n - t0;
+    if (nt > 0) {
+      // per chain row {start, first entry in a column >= t0, diagonal, P}
+      std::vector<int4> desc(nt);
+      for (int r = t0; r < n; ++r) {
+        const int *c0 = S.ci.data() + S.rp[r], *c1 = S.ci.data() + S.diag[r];
+        desc[r - t0] = make_int4(S.rp[r], S.rp[r] + int(std::lower_bound(c0, c1, t0) - c0), S.diag[r],
+                                 S.P[r]);
+      }
+      lu->smem_chain = 2 * size_t(nt) * tsz;
+      const void *fn = precision == XG_LU_FP32 ? (const void *)xg::lu_solve_chain<float>
+                                               : (const void *)xg::lu_solve_chain<double>;
+      if ((rc = upload(&lu->d_tdesc, desc)) ||
+          (e = cudaMalloc(&lu->d_hpart, 32 * size_t(nt) * tsz)) ||
+          (e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    int(lu->smem_chain)))) {
+        free_lu(lu.get());
+        return rc ? rc : cuda_fail(e, "xg_lu_analyze");
+      }
+    }
   }
   // one-CTA path when the factor (and the solve's extra vectors) fit in shared memory
   {
