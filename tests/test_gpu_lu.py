@@ -200,9 +200,10 @@ def test_chain_tail_matches_grid_solves(precision, gpu_ctx, oracle_lib, monkeypa
     grid-wide (XG_LU_NO_CHAIN)."""
     A = circuit_jacobian(CASES["power_grid_60x60"](), seed=5)
     b = np.random.default_rng(15).standard_normal(A.shape[0])
-    x, st, _ = _solve(gpu_ctx, A, A, b, precision, 0)
+    x, st, info = _solve(gpu_ctx, A, A, b, precision, 0)
     monkeypatch.setenv("XG_LU_NO_CHAIN", "1")
-    x_grid, st_grid, _ = _solve(gpu_ctx, A, A, b, precision, 0)
+    x_grid, st_grid, info_grid = _solve(gpu_ctx, A, A, b, precision, 0)
     assert st == 0 and st_grid == 0
+    assert info.solve_chain == 256 and info_grid.solve_chain == 0
     assert np.array_equal(x, x_grid)
     assert _backward_error(A, x, b) <= (1e-13 if precision == abi.LU_FP64 else 1e-5)

@@ -82,7 +82,8 @@ class XgLuInfo(C.Structure):
     _fields_ = [("n", C.c_int), ("nnz_a", C.c_int64), ("nnz_lu", C.c_int64),
                 ("precision", C.c_int), ("levels", C.c_int), ("n_dense", C.c_int),
                 ("refactor_flops", C.c_double), ("solve_flops", C.c_double),
-                ("min_pivot", C.c_double), ("max_pivot", C.c_double), ("ordering", C.c_int)]
+                ("min_pivot", C.c_double), ("max_pivot", C.c_double), ("ordering", C.c_int),
+                ("solve_chain", C.c_int)]
 
 
 class XgTranOptions(C.Structure):

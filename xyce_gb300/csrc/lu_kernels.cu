@@ -1778,7 +1778,9 @@ extern "C" int xg_lu_status(xg_lu *lu, int *status, int *bad_row) {
   return XG_OK;
 }
 
-static void fill_info(const xg::LuSymbolic &S, int precision, xg_lu_info *info) {
+// with_chain: model the chain of the grid solves (the host-only analysis;
+// an analysed xg_lu reports the one it chose)
+static void fill_info(const xg::LuSymbolic &S, int precision, xg_lu_info *info, bool with_chain) {
   std::memset(info, 0, sizeof(*info));
   info->n = S.n;
   info->nnz_a = S.nnz_a;
@@ -1791,6 +1793,8 @@ static void fill_info(const xg::LuSymbolic &S, int precision, xg_lu_info *info) 
   info->min_pivot = S.min_pivot;
   info->max_pivot = S.max_pivot;
   info->ordering = S.ordering;
+  const size_t tsz = precision == XG_LU_FP32 ? sizeof(float) : sizeof(double);
+  info->solve_chain = with_chain && !S.rp.empty() ? S.n - xg::chain_start(S, tsz) : 0;
 }
 
 extern "C" int xg_lu_get_info(const xg_lu *lu, xg_lu_info *info) {
@@ -1798,7 +1802,9 @@ extern "C" int xg_lu_get_info(const xg_lu *lu, xg_lu_info *info) {
     xg::set_error("xg_lu_get_info: bad argument");
     return XG_ERR_ARG;
   }
-  fill_info(lu->S, lu->precision, info);
+  fill_info(lu->S, lu->precision, info, false);
+  const bool grid = !lu->lvl && !lu->narrow && !lu->smem_solve;
+  info->solve_chain = grid ? lu->S.n - lu->solve_tail0 : 0;
   return XG_OK;
 }
 
@@ -1851,6 +1857,6 @@ extern "C" int xg_lu_analyze_host(int n, const int *host_rowptr, const int *host
   if (P) std::memcpy(P, S.P.data(), sizeof(int) * n);
   if (Q) std::memcpy(Q, S.Q.data(), sizeof(int) * n);
   if (nnz_lu) *nnz_lu = S.rp[n];
-  if (info) fill_info(S, XG_LU_FP64, info);
+  if (info) fill_info(S, XG_LU_FP64, info, true);
   return XG_OK;
 }
