@@ -291,6 +291,13 @@ int xg_lu_solve(xg_lu *lu, const double *dev_b, double *dev_x, int n_refine);
 int xg_lu_refactor_solve(xg_lu *lu, const double *dev_values, const double *dev_b, double *dev_x,
                          int n_refine);
 int xg_lu_status(xg_lu *lu, int *status, int *bad_row);
+/* Polls a device wait of this factorisation's refactor and solves makes
+ * before it gives up, sets status bit 2 and returns (default 1,048,576, about
+ * 0.1-0.5 s).  Every launch ends even when a wait gives up; its results are
+ * then not valid.  Lowering it makes the waits run out, which is how the
+ * timeout path is tested.  No counterpart in the reference, whose host KLU
+ * has no device waits.  Synchronises the stream first. */
+int xg_lu_set_wait_limit(xg_lu *lu, int polls);
 int xg_lu_get_info(const xg_lu *lu, xg_lu_info *info);
 /* host copies of the analysis: P, Q (n each), L\U row pointers (n+1), columns (nnz_lu) */
 int xg_lu_get_symbolic(const xg_lu *lu, int *P, int *Q, int *lu_rowptr, int *lu_colidx);
@@ -371,9 +378,9 @@ int xg_batch_info(const xg_batch *b, int *n_requests, int64_t *device_bytes);
 int xg_batch_destroy(xg_batch *b);
 
 /* xg_load_noalloc — the same load as xg_load, for callers that cannot
- * allocate device memory at the point where they load: code running while a
- * stream is captured into a CUDA graph, runtimes that give the GPU a fixed
- * memory budget up front, real-time loops that must not enter the allocator.
+ * allocate device memory at the point where they load: host simulators that
+ * give the GPU a fixed memory budget up front and own every later byte
+ * themselves, and real-time loops that must never block in the allocator.
  * It calls no cudaMalloc, cudaFree or allocating library routine.  No
  * counterpart exists in the reference.
  *   - The per-load stamp terms live in one fixed device array inside the
@@ -386,8 +393,10 @@ int xg_batch_destroy(xg_batch *b);
  *     and dQ/dx values on the pattern of xg_circuit_get_pattern.  Next state
  *     and store are written in the circuit as xg_load writes them.
  *   - The first call on a device looks the array's device address up
- *     (cudaGetSymbolAddress) with that device current; make that first call
- *     before any stream capture.
+ *     (cudaGetSymbolAddress) with that device current and keeps it for the
+ *     life of the process; make that first call before any stream capture.
+ *     A cudaDeviceReset invalidates the kept address: reload the library
+ *     after one.
  *   - All calls share the array: calls whose work overlaps on the GPU race
  *     and must be serialised by the caller. */
 int xg_load_noalloc(xg_circuit *c, const xg_load_flags *flags, double *dev_out,

@@ -35,6 +35,8 @@ def lib():
         L.xgo_tran_run.argtypes = [vp, C.POINTER(TranOpts), vp, vp, C.POINTER(C.c_int),
                                    C.POINTER(TranStats)]
         L.xgo_sparse_solve.argtypes = [C.c_int, vp, vp, vp, vp, vp, vp]
+        L.xgo_setup_params.argtypes = [C.POINTER(abi.XgNetlist), C.POINTER(abi.XgDeviceOptions),
+                                       C.c_int, vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
         _lib = L
     return _lib
 
@@ -53,6 +55,30 @@ class TranStats(C.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def setup_params(netlist, dev_type, options=None):
+    """The (n_params, n_instances) parameter block of one device type from the
+    oracle's own restatement of the reference's set-up."""
+    cnl = netlist.to_c()
+    opt = options or abi.device_options()
+    npar, ninst = C.c_int(), C.c_int()
+    rc = lib().xgo_setup_params(C.byref(cnl), C.byref(opt), dev_type, None, C.byref(npar),
+                                C.byref(ninst))
+    if rc != 0:
+        raise RuntimeError(f"xgo_setup_params failed: {rc}")
+    out = np.zeros((npar.value, ninst.value))
+    if ninst.value:
+        rc = lib().xgo_setup_params(C.byref(cnl), C.byref(opt), dev_type, _ptr(out), None, None)
+        if rc != 0:
+            raise RuntimeError(f"xgo_setup_params failed: {rc}")
+    return out
+
+
+def all_params(netlist, options=None):
+    """Parameter blocks of every device type present, from the oracle's set-up."""
+    return {t: setup_params(netlist, t, options) for t in range(abi.NUM_DEV_TYPES)
+            if netlist.count(t)}
 
 
 def sparse_solve(rowptr, col, val, b, col_order=None):

@@ -15,6 +15,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(os.path.dirname(HERE), "_ref")
 REPO = os.path.dirname(os.path.dirname(HERE))
+# Where the build container mounts the reference source tree (read-only).
+DEFAULT_REF = "/root/reference"
 
 OPEN_MODELS = ["MOSFET1", "MOSFET_B3", "Diode", "Resistor", "Capacitor", "Vsrc", "ISRC"]
 # Core files left out: the device manager itself (replaced by the harness) and
@@ -50,7 +52,9 @@ def include_dirs(ref):
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default=os.environ.get("XYCE_REFERENCE", "/root/reference"))
+    ap.add_argument("--ref", default=os.environ.get("XYCE_REFERENCE") or DEFAULT_REF,
+                    help="reference source tree (default: $XYCE_REFERENCE, else the tree "
+                         "this recipe was written against)")
     ap.add_argument("-j", type=int, default=os.cpu_count() or 4)
     a = ap.parse_args(argv)
     if not os.path.isdir(os.path.join(a.ref, "src", "DeviceModelPKG")):

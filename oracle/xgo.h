@@ -6,8 +6,8 @@
  * never links, imports or calls anything in this folder.
  *
  * Inputs are the netlist of include/xg.h plus the per-instance parameter
- * blocks of include/xg_params.h (derived on the host by circuit setup); the
- * oracle restates only the load path.  Parity of this restatement with the
+ * blocks of include/xg_params.h, which the oracle derives with its own
+ * restatement of the reference's set-up (xgo_setup_params).  Parity of this restatement with the
  * reference itself is pinned by the tests against oracle/_ref (the reference's
  * own device sources compiled here) and the golden fixtures generated from it.
  *
@@ -27,6 +27,12 @@ extern "C" {
 #endif
 
 typedef struct xgo_circuit xgo_circuit;
+
+/* The parameter block of device type t (xg_params.h layout, column k of
+ * instance i at out[k*n + i]) derived by the oracle's own set-up
+ * (xgo_setup.c, xgo_b3setup.c).  out may be NULL to query the sizes. */
+int xgo_setup_params(const xg_netlist *nl, const xg_device_options *opt, int dev_type,
+                     double *out, int *n_params, int *n_instances);
 
 /* params[t] = SoA block of device type t (xg_params.h), or NULL if none. */
 int xgo_build(const xg_netlist *nl, const xg_device_options *opt,

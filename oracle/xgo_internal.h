@@ -65,6 +65,10 @@ double xgo_fetlim(double vnew, double vold, double vto);
 void xgo_qmeyer(double vgs, double vgd, double vgb, double von, double vdsat,
                 double *capgs, double *capgd, double *capgb, double phi, double cox);
 
+/* set-up (xgo_setup.c, xgo_b3setup.c) */
+int xgo_card_eq(const char *a, const char *b);
+int xgo_b3_setup(const xg_netlist *nl, const xg_device_options *opt, double *out);
+
 /* BSIM3 (xgo_bsim3.c) */
 int xgo_b3_nparams(void);
 void *xgo_b3_members_alloc(int n);

@@ -93,6 +93,39 @@ def compare(a, b, exact=True):
     return rep, bad
 
 
+def max_rel_above_floor(a, b):
+    """Largest |a-b|/|b| over the entries of every output whose reference
+    value is above the absolute floor ATOL_FRAC * max|b| of that output (the
+    entries the relative bound governs on its own)."""
+    worst = 0.0
+    same_pattern = (len(a["rows"]) == len(b["rows"]) and np.array_equal(a["rows"], b["rows"])
+                    and np.array_equal(a["cols"], b["cols"]))
+    for k in VEC_KEYS + MAT_KEYS:
+        if k in MAT_KEYS and not same_pattern:
+            A, B = mat_dict(a, k), mat_dict(b, k)
+            keys = sorted(set(A) | set(B))
+            x = np.array([A.get(q, 0.0) for q in keys])
+            y = np.array([B.get(q, 0.0) for q in keys])
+        else:
+            x, y = np.asarray(a[k], float), np.asarray(b[k], float)
+        if y.size == 0:
+            continue
+        m = np.abs(y) > ATOL_FRAC * np.max(np.abs(y))
+        if m.any():
+            worst = max(worst, float(np.max(np.abs(x[m] - y[m]) / np.abs(y[m]))))
+    return worst
+
+
+def report(rec):
+    """Append one JSON record to the file XG_PARITY_REPORT names, if set: the
+    measured parity figures (largest errors, identical-entry counts)."""
+    import json
+    path = os.environ.get("XG_PARITY_REPORT")
+    if path:
+        with open(path, "a") as f:
+            f.write(json.dumps(rec) + "\n")
+
+
 def _cmp(x, y):
     if x.size == 0:
         return (0, 0, 0.0)
@@ -119,3 +152,25 @@ def circuit_jacobian(netlist, seed=0, pdt=1e11, options=None):
     A = sp.csr_matrix((out["dFdx"] + pdt * out["dQdx"], (out["rows"], out["cols"])), shape=(n, n))
     A.sort_indices()
     return A
+
+
+def oracle_transient_workload(name):
+    """The oracle's CPU transient of one of bench.py's transient workloads
+    (same netlist, start, window and recorded unknowns); returns (t, V,
+    stats).  Runs in a spawned worker process."""
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    if root not in sys.path:
+        sys.path.insert(0, root)
+    import bench
+    from oracle.oracle import OracleCircuit, transient
+    from xyce_gb300 import engine
+    nl, guess, tstop, tstep, uic, out = bench.build_tran(name)
+    opt = abi.device_options()
+    params = {t: engine.setup_params(nl, t, opt) for t in range(abi.NUM_DEV_TYPES) if nl.count(t)}
+    oc = OracleCircuit(nl, params, opt)
+    order, _ = engine.amd_order(oc.rowptr, oc.col)
+    try:
+        return transient(oc, tstop, tstep, out, col_order=order, x0=bench._x0(nl, guess), uic=uic)
+    finally:
+        oc.close()

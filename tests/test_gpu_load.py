@@ -9,7 +9,7 @@
 import numpy as np
 import pytest
 
-from helpers import Golden, compare, golden_files
+from helpers import Golden, compare, golden_files, max_rel_above_floor, report
 from xyce_gb300 import abi, engine, netlists
 
 pytestmark = pytest.mark.gpu
@@ -37,13 +37,22 @@ def test_gpu_matches_reference_golden(path, gpu_ctx):
     loads = [(g.flags(k), g.inputs(k)) for k in range(g.n_loads)]
     outs = _gpu_run(gpu_ctx, g.netlist, g.options, loads)
     total = ident = 0
+    worst = 0.0
     for k, got in enumerate(outs):
-        rep, bad = compare(got, g.outputs(k), exact=False)
+        want = g.outputs(k)
+        rep, bad = compare(got, want, exact=False)
         assert not bad, f"load {k}: {bad}"
         total += sum(v[0] for v in rep.values())
         ident += sum(v[0] - v[1] for v in rep.values())
-    # the rest differ by CUDA's vs glibc's last-ulp exp/log/pow rounding
-    assert ident / total > 0.9, f"only {ident}/{total} entries bit-identical"
+        worst = max(worst, max_rel_above_floor(got, want))
+    report({"test": "golden", "fixture": g.name, "entries": total, "bit_identical": ident,
+            "max_rel_err_above_floor": worst})
+    # the rest differ by CUDA's vs glibc's last-ulp exp/log/pow rounding;
+    # measured at least 98.4% identical on every fixture
+    assert ident / total > 0.98, f"only {ident}/{total} entries bit-identical"
+    # entries above the absolute floor (no cancellation to near zero) are
+    # within a few ulp: measured at most 3.7e-15 relative over the fixtures
+    assert worst <= 1e-14, worst
 
 
 def _oracle(netlist, options, ctx_params):

@@ -207,3 +207,37 @@ def test_chain_tail_matches_grid_solves(precision, gpu_ctx, oracle_lib, monkeypa
     assert info.solve_chain == 256 and info_grid.solve_chain == 0
     assert np.array_equal(x, x_grid)
     assert _backward_error(A, x, b) <= (1e-13 if precision == abi.LU_FP64 else 1e-5)
+
+
+def test_wait_that_runs_out_reports_timeout(gpu_ctx, oracle_lib):
+    """The grid refactor's rows wait, bounded, for the pivots of the rows
+    their L part names.  With the limit lowered to one poll those waits give
+    up: the launch still ends, xg_lu_status reports bit 2 (a wait gave up),
+    and the context stays usable, as the next refactor at the default limit
+    shows."""
+    import torch
+    A = circuit_jacobian(CASES["power_grid_60x60"](), seed=5)
+    b = np.random.default_rng(16).standard_normal(A.shape[0])
+    lu = engine.LU(gpu_ctx, A.indptr, A.indices, A.data, abi.LU_FP64)
+    try:
+        vals = torch.from_numpy(A.data.copy()).cuda()
+        db = torch.from_numpy(b).cuda()
+        dx = torch.zeros_like(db)
+        lu.set_wait_limit(1)
+        lu.refactor(vals.data_ptr())
+        lu.solve(db.data_ptr(), dx.data_ptr(), 0)
+        status, _ = lu.status()
+        assert status & 2, status
+        lu.set_wait_limit(1 << 20)
+        lu.refactor(vals.data_ptr())
+        lu.solve(db.data_ptr(), dx.data_ptr(), 0)
+        assert lu.status() == (0, -1)
+        assert _backward_error(A, dx.cpu().numpy(), b) <= 1e-13
+    finally:
+        lu.close()
+    with pytest.raises(engine.XgError):
+        lu2 = engine.LU(gpu_ctx, A.indptr, A.indices, A.data, abi.LU_FP64)
+        try:
+            lu2.set_wait_limit(0)
+        finally:
+            lu2.close()

@@ -35,6 +35,48 @@ def test_setup_params_match_reference(path, engine_lib):
         assert np.all((got == want) | (rel <= 4.5e-16)), (t, np.argwhere(got != want)[:5])
 
 
+@pytest.mark.parametrize("path", golden_files(), ids=lambda p: p.split("/")[-1][:-4])
+def test_oracle_setup_matches_reference(path, oracle_lib):
+    """The oracle's own set-up reproduces the reference's derived instance
+    parameters bit for bit."""
+    from oracle import oracle
+    g = Golden(path)
+    for t, want in g.params.items():
+        got = oracle.setup_params(g.netlist, t, g.options)
+        if t == abi.DEV_BSIM3:  # the fixture holds the raw columns only
+            got = got[: want.shape[0]]
+        assert got.shape == want.shape
+        assert np.array_equal(got, want), (t, np.argwhere(got != want)[:5])
+
+
+def _bsim3_cards(seed, n, variant):
+    from golden import circuits
+    cards = circuits.bsim3(variant, seed=seed)
+    nl = netlists.random_mos_netlist(n, n // 4, dev_type=abi.DEV_BSIM3, seed=seed,
+                                     models=tuple(cards.models))
+    rng = np.random.default_rng(seed)
+    for k, hi in (("ad", 2e-12), ("as", 2e-12), ("pd", 8e-6), ("ps", 8e-6)):
+        nl.bsim3[k] = rng.uniform(0, hi, n)
+    nl.bsim3["m"] = rng.integers(1, 3, n).astype(float)
+    return nl
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2])
+def test_oracle_setup_matches_engine_setup(variant, oracle_lib, engine_lib):
+    """Oracle and engine set-up, two restatements of the reference's, give
+    the same full parameter blocks (hoisted BSIM3 columns included) on random
+    geometries of every device type."""
+    from oracle import oracle
+    nl = _random_mixed(40 + variant, 600, 150)
+    b3 = _bsim3_cards(50 + variant, 800, variant)
+    for net in (nl, b3):
+        for t in range(abi.NUM_DEV_TYPES):
+            if net.count(t):
+                a = oracle.setup_params(net, t)
+                b = engine.setup_params(net, t, abi.device_options())
+                assert np.array_equal(a, b), (variant, t, np.argwhere(a != b)[:5])
+
+
 def test_netlist_arrays_roundtrip():
     nl = netlists.power_grid(4, 4, 5, seed=1)
     back = abi.Netlist.from_arrays(nl.to_arrays())
@@ -74,9 +116,11 @@ def test_oracle_matches_live_reference_random(oracle_lib, engine_lib):
         nl = _random_mixed(seed, 400, 120)
         opt = abi.device_options()
         rc = ref.RefCircuit(nl, opt)
-        params = {t: engine.setup_params(nl, t, opt) for t in range(abi.NUM_DEV_TYPES) if nl.count(t)}
+        from oracle import oracle
+        params = oracle.all_params(nl, opt)
         for t in (abi.DEV_MOS1, abi.DEV_DIODE, abi.DEV_RES, abi.DEV_CAP):
             assert np.array_equal(params[t], rc.params(t)), t
+            assert np.array_equal(engine.setup_params(nl, t, opt), rc.params(t)), t
         oc = OracleCircuit(nl, params, opt)
         for k, fl in enumerate(circuits.FLAG_SEQUENCE):
             flags = abi.load_flags(**{**dict(transient=0), **fl})

@@ -1,9 +1,12 @@
 """xg_load_noalloc: the load for callers that cannot allocate device memory
-where they load (inside a CUDA graph capture, under a fixed memory budget, in
-a real-time loop).  Its stamp-term scratch is a fixed array inside the
-library instead of a per-circuit buffer, and its outputs go to a buffer the
-caller passes in.  Checked through the C ABI against xg_load on two calls in a
-row, and for its size limit.  Kept in a file collected last.
+where they load (a host simulator that gives the GPU a fixed memory budget up
+front, a real-time loop that must never enter the allocator).  Its stamp-term
+scratch is a fixed array inside the library instead of a per-circuit buffer,
+and its outputs go to a buffer the caller passes in.  Checked through the C
+ABI against xg_load on two calls in a row, on a level-1 circuit (terms
+scattered into reduction order) and on a BSIM3 circuit (terms in instance
+order, gathered by the reduction), and for its size limit.  Kept in a file
+collected last.
 """
 import ctypes as C
 
@@ -72,4 +75,45 @@ def test_noalloc_rejects_oversized_circuits_and_short_buffers(engine_lib):
     assert _noalloc(small, flags, out.data_ptr(), 16) == -1  # buffer too short
     assert b"shorter" in L.xg_last_error()
     small.close()
+    ctx.close()
+
+
+def _split(got, c):
+    n1, n = c.n_unknowns + 1, c.n_unknowns
+    return {"F": got[0:n], "Q": got[n1:n1 + n], "dFdxdVp": got[2 * n1:2 * n1 + n],
+            "dQdxdVp": got[3 * n1:3 * n1 + n], "dFdx": got[4 * n1:4 * n1 + c.nnz],
+            "dQdx": got[4 * n1 + c.nnz:4 * n1 + 2 * c.nnz]}
+
+
+def test_noalloc_load_matches_regular_load_bsim3(engine_lib):
+    """BSIM3 keeps capacitances and charges from one load to the next, so the
+    two entry points each run on a circuit of their own, fed the same inputs
+    in the same order; both calls of each must agree bit for bit."""
+    import torch
+    L = engine.lib()
+    L.xg_load_noalloc.argtypes = [C.c_void_p, C.POINTER(abi.XgLoadFlags), C.c_void_p, C.c_int64]
+    ctx = engine.Context(0, abi.device_options())
+    nl = netlists.random_mos_netlist(3000, 700, dev_type=abi.DEV_BSIM3, seed=41,
+                                     models=(abi.Model(abi.DEV_BSIM3, 1), abi.Model(abi.DEV_BSIM3, -1)))
+    ref = engine.Circuit(ctx, nl)
+    na = engine.Circuit(ctx, nl)
+    n_out = 4 * (na.n_unknowns + 1) + 2 * na.nnz
+    assert na.info.n_terms <= 2 * 1024 * 1024
+    out = torch.full((n_out,), float("nan"), dtype=torch.float64, device="cuda:0")
+    for k in range(2):
+        ins = netlists.random_state(ref.n_unknowns, ref.n_state, ref.n_store, seed=30 + k)
+        flags = abi.load_flags(transient=1, newton_iter=1 + k, time=0.4e-9 * (k + 1), pdt=1e11)
+        ref.set_state(*ins)
+        ref.load(flags)
+        want = ref.outputs()
+        na.set_state(*ins)
+        assert _noalloc(na, flags, out.data_ptr(), n_out) == 0, L.xg_last_error()
+        ctx.synchronize()
+        got = _split(out.cpu().numpy(), na)
+        for key, v in got.items():
+            np.testing.assert_array_equal(v, want[key], err_msg=f"call {k}: {key}")
+        np.testing.assert_array_equal(na.download(abi.VEC_STA_NEXT), want["sta_next"])
+        np.testing.assert_array_equal(na.download(abi.VEC_STO_NEXT), want["sto_next"])
+    ref.close()
+    na.close()
     ctx.close()

@@ -195,6 +195,17 @@ int circuit_reset_members(xg_circuit *c) {
 static std::atomic<long long> g_launches{0};
 void count_launches(int k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
 
+int sm_count() {
+  static std::atomic<int> cache[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
+  int v = cache[dev].load(std::memory_order_relaxed);
+  if (v > 0) return v;
+  if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v < 1) v = 1;
+  cache[dev].store(v, std::memory_order_relaxed);
+  return v;
+}
+
 int ctx_info(xg_ctx *ctx, int *device, void **stream) {
   if (!ctx) return XG_ERR_ARG;
   *device = ctx->device;

@@ -784,12 +784,13 @@ int launch_eval(int dev_type, const DevType &t, const DevOptions &o, const Flags
 int launch_reduce(const ReduceArgs &a, void *stream) {
   const int64_t n = a.n_short;
   if (n <= 0 && a.n_long <= 0) return XG_OK;
+  const int sms = sm_count();
   int grid = (int)std::max<int64_t>(1, (n + kRedThreads - 1) / kRedThreads);
-  if (grid > 152 * 32) grid = 152 * 32;
+  if (grid > sms * 32) grid = sms * 32;
 #if XG_SPLIT_SUMS
-  const int long_blocks = (int)std::min<int64_t>(a.n_long, 152 * 8);  // a block per long output
+  const int long_blocks = (int)std::min<int64_t>(a.n_long, sms * 8);  // a block per long output
 #else
-  const int long_blocks = (int)std::min<int64_t>((a.n_long + kRedWarps - 1) / kRedWarps, 152 * 8);
+  const int long_blocks = (int)std::min<int64_t>((a.n_long + kRedWarps - 1) / kRedWarps, sms * 8);
 #endif
   reduce_kernel<<<grid + long_blocks, kRedThreads, 0, (cudaStream_t)stream>>>(a, long_blocks); xg::count_launches(1);
   return cudaGetLastError() == cudaSuccess ? XG_OK : XG_ERR_CUDA;

@@ -48,11 +48,15 @@ namespace xg {
 namespace {
 
 enum Ctrl : int {
-  C_CLAIM_F = 0, C_CLAIM_L, C_CLAIM_U, C_STATUS, C_BAD_ROW, C_N
+  C_CLAIM_F = 0, C_CLAIM_L, C_CLAIM_U, C_STATUS, C_BAD_ROW,
+  // polls per wait before it gives up (kSpinLimit unless a caller lowers it);
+  // 128 bytes past the counters, so their atomics do not evict it from L1
+  C_SPIN = 32,
+  C_N
 };
 enum Status : unsigned { ST_PIVOT = 1u, ST_TIMEOUT = 2u, ST_PATTERN = 4u };
 
-constexpr int kSpinLimit = 1 << 20;  // polls per wait (~0.1-0.5 s) before giving up
+constexpr int kSpinLimit = 1 << 20;  // default polls per wait (~0.1-0.5 s) before giving up
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
   unsigned v;
@@ -129,10 +133,11 @@ __device__ T wait_value(const T *p, unsigned *ctrl) {
   using U = typename Pending<T>::U;
   const U *q = reinterpret_cast<const U *>(p);
   int it = 0;
+  const int limit = int(__ldg(&ctrl[C_SPIN]));
   U v;
   while ((v = ld_relaxed(q)) == Pending<T>::bits) {
     ++it;
-    if (it > kSpinLimit ||
+    if (it > limit ||
         ((it & 1023) == 0 && (*(volatile unsigned *)&ctrl[C_STATUS] & ST_TIMEOUT))) {
       atomicOr(&ctrl[C_STATUS], ST_TIMEOUT);
       return T(0);
@@ -165,10 +170,11 @@ __device__ T wait_value_acquire(const T *p, unsigned *ctrl) {
   using U = typename Pending<T>::U;
   const U *q = reinterpret_cast<const U *>(p);
   int it = 0;
+  const int limit = int(__ldg(&ctrl[C_SPIN]));
   U v;
   while ((v = ld_acq(q)) == Pending<T>::bits) {
     ++it;
-    if (it > kSpinLimit ||
+    if (it > limit ||
         ((it & 1023) == 0 && (*(volatile unsigned *)&ctrl[C_STATUS] & ST_TIMEOUT))) {
       atomicOr(&ctrl[C_STATUS], ST_TIMEOUT);
       return T(0);
@@ -702,8 +708,9 @@ constexpr int kCtaThreads = 1024;
 // sleep so waiting warps leave the issue slots to the warp they wait for.
 __device__ __forceinline__ bool wait_flag_smem(volatile int *flag, unsigned *ctrl) {
   int it = 0;
+  const int limit = int(__ldg(&ctrl[C_SPIN]));
   while (*flag == 0) {
-    if (++it > kSpinLimit) {
+    if (++it > limit) {
       atomicOr(&ctrl[C_STATUS], ST_TIMEOUT);
       return false;
     }
@@ -1490,6 +1497,7 @@ extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const i
   XG_CU(cudaSetDevice(lu->device));
   const xg::LuSymbolic &S = lu->S;
   lu->nnz_lu = S.rp[n];
+  lu->solve_tail0 = n;  // no one-warp chain unless the grid path below picks one
   std::vector<int> arp(host_rowptr, host_rowptr + n + 1);
   std::vector<int> aci(host_colidx, host_colidx + S.nnz_a);
   int rc = 0;
@@ -1523,9 +1531,13 @@ extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const i
                                              XG_ERR_OOM)
                                           : cuda_fail(e, "xg_lu_analyze");
   }
-  if ((e = cudaMemset(lu->d_ctrl, 0, sizeof(unsigned) * xg::C_N))) {
-    free_lu(lu.get());
-    return cuda_fail(e, "xg_lu_analyze: cudaMemset");
+  {
+    unsigned init[xg::C_N] = {};
+    init[xg::C_SPIN] = unsigned(xg::kSpinLimit);
+    if ((e = cudaMemcpy(lu->d_ctrl, init, sizeof(init), cudaMemcpyHostToDevice))) {
+      free_lu(lu.get());
+      return cuda_fail(e, "xg_lu_analyze: cudaMemcpy");
+    }
   }
   int sms = 0, occ = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, lu->device);
@@ -1775,6 +1787,19 @@ extern "C" int xg_lu_status(xg_lu *lu, int *status, int *bad_row) {
   XG_CU(cudaStreamSynchronize(lu->stream));
   *status = int(h[xg::C_STATUS]);
   if (bad_row) *bad_row = h[xg::C_BAD_ROW] == 0xffffffffu ? -1 : int(h[xg::C_BAD_ROW]);
+  return XG_OK;
+}
+
+extern "C" int xg_lu_set_wait_limit(xg_lu *lu, int polls) {
+  if (!lu || polls < 1) {
+    xg::set_error("xg_lu_set_wait_limit: bad argument");
+    return XG_ERR_ARG;
+  }
+  XG_CU(cudaSetDevice(lu->device));
+  // after the work already queued, so a launch in flight keeps the limit it began with
+  XG_CU(cudaStreamSynchronize(lu->stream));
+  const unsigned v = unsigned(polls);
+  XG_CU(cudaMemcpy(lu->d_ctrl + xg::C_SPIN, &v, sizeof(v), cudaMemcpyHostToDevice));
   return XG_OK;
 }
 

@@ -3,10 +3,9 @@
 //
 // The regular load (xg_load) keeps its per-load stamp terms in a buffer the
 // circuit allocated at set-up.  Some callers cannot allocate device memory at
-// the point where they load: code that runs while a CUDA stream is being
-// captured into a graph (cudaMalloc is not allowed there), host runtimes that
-// hand the GPU a fixed memory budget up front and forbid allocation
-// afterwards, and real-time loops that must never block in the allocator.
+// the point where they load: host simulators that hand the GPU a fixed memory
+// budget up front and forbid allocation afterwards, and real-time loops that
+// must never block in the allocator.
 // This entry point runs the same evaluation and fixed-order reduction kernels,
 // but the stamp terms live in one fixed device array defined in this file, and
 // the results are written to a buffer the caller passes in.
@@ -37,8 +36,10 @@ std::mutex g_mu;
 double *g_scratch_addr[kMaxDevices] = {};
 
 // Device address of the scratch array on `device`, looked up once per device
-// with that device current.  In host code the array's name only stands in for
-// the symbol; the kernels must be given this address.
+// with that device current and kept for the life of the process (a
+// cudaDeviceReset invalidates it; the library must be reloaded after one).
+// In host code the array's name only stands in for the symbol; the kernels
+// must be given this address.
 int scratch_on(int device, double **out) {
   if (device < 0 || device >= kMaxDevices) return XG_ERR_ARG;
   std::lock_guard<std::mutex> lock(g_mu);

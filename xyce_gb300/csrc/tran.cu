@@ -440,7 +440,7 @@ extern "C" int xg_tran_run(xg_circuit *c, const xg_tran_options *o, const double
       return XG_ERR_ARG;
     }
   if (cudaSetDevice(R.v.device) != cudaSuccess) return XG_ERR_CUDA;
-  R.grid = std::max(1, std::min(4 * 152, (n + kThreads - 1) / kThreads));
+  R.grid = std::max(1, std::min(4 * sm_count(), (n + kThreads - 1) / kThreads));
   int rc = XG_OK;
   double *d_rec = nullptr;
   int *d_idx = nullptr;

@@ -164,6 +164,9 @@ ReduceArgs reduce_args(const Plan &P, const double *terms, const int64_t *red_pt
 void set_error(const std::string &msg);
 // Kernel launches of this library, counted at every launch site (api.cpp).
 void count_launches(int k);
+// Streaming multiprocessors of the current CUDA device (queried once per
+// device); grids are sized in multiples of it.
+int sm_count();
 // Zero the members carried between loads (diode Vd, BSIM3 charges/caps).
 int circuit_reset_members(xg_circuit *c);
 // A transient keeps its LU analysis in the circuit when it ends; the next

@@ -84,6 +84,7 @@ def lib():
     L.xg_lu_solve.argtypes = [vp, vp, vp, i]
     L.xg_lu_refactor_solve.argtypes = [vp, vp, vp, vp, i]
     L.xg_lu_status.argtypes = [vp, C.POINTER(i), C.POINTER(i)]
+    L.xg_lu_set_wait_limit.argtypes = [vp, i]
     L.xg_lu_get_info.argtypes = [vp, C.POINTER(abi.XgLuInfo)]
     L.xg_lu_get_symbolic.argtypes = [vp, vp, vp, vp, vp]
     L.xg_lu_destroy.argtypes = [vp]
@@ -295,6 +296,10 @@ class LU:
         st, row = C.c_int(), C.c_int()
         check(lib().xg_lu_status(self.h, C.byref(st), C.byref(row)))
         return st.value, row.value
+
+    def set_wait_limit(self, polls):
+        """Polls a device wait makes before it gives up (status bit 2)."""
+        check(lib().xg_lu_set_wait_limit(self.h, int(polls)))
 
     def symbolic(self):
         n, nnz = self.n, self.info.nnz_lu
