@@ -83,6 +83,8 @@ WORKLOADS = {
     # initial condition; one step = serving the whole stream, FP32 factors with
     # one FP64 refinement step (the FP64 form is measured beside it)
     "serve_ring_mc": dict(kind="serve", n=1000, rate=2000.0, tstop=5e-9),
+    # the same stream at its full length of 10,000 requests
+    "serve_ring_mc_10k": dict(kind="serve", n=10000, rate=2000.0, tstop=5e-9),
     # one batch: 256 requests of the same Monte-Carlo ring stream, all at
     # once; one step = set up and run the batch to completion (FP32 factors
     # corrected by Newton; the batched kernels without the server's threads)
@@ -98,6 +100,44 @@ WORKLOADS = {
 }
 METRIC = "device-loads/sec"
 TRAN_METRIC = "newton-iters/sec"
+
+
+def _emit(line, emit):
+    """Print the JSON line (emit) or hand it to the caller (a sub-record)."""
+    if emit:
+        print(json.dumps(line))
+        return 0
+    return line
+
+
+def _mapped_libs():
+    """This repository's shared libraries mapped into the calling process."""
+    try:
+        with open("/proc/self/maps") as f:
+            paths = {ln.split()[-1] for ln in f if ln.rstrip().endswith(".so")}
+    except OSError:
+        return []
+    return sorted(os.path.relpath(q, HERE) for q in paths if q.startswith(HERE + os.sep))
+
+
+def workload_config(name):
+    """The `config` of a workload's line: what the workload is (both arms
+    print the same dict); how an arm runs it goes in its `details`."""
+    w = WORKLOADS[name]
+    k = w["kind"]
+    if k == "random":
+        return {"workload": name, "instances": w["n_dev"], "nodes": w["n_nodes"],
+                "l2": "inputs larger than L2 (parameter blocks alone exceed 129 MB)"}
+    if k == "tran":
+        return {"workload": name, "tstop": w["tstop"], "tstep": w["tstep"],
+                "l2": "working set below L2; latency-bound"}
+    if k in ("serve", "batch"):
+        c = {"workload": name, "requests": w["n"], "stages": "5-501 odd", "tstop": w["tstop"],
+             "l2": "per-request working sets below L2"}
+        if k == "serve":
+            c["rate_per_s"] = w["rate"]
+        return c
+    return {"workload": name}
 
 
 def build_tran(name):
@@ -136,13 +176,11 @@ def tran_cpu_baseline(name, seconds=20.0):
     """The oracle's transient driver on one core (the reference is single-
     threaded per rank) over the same window, or the leading part of it that
     fits the time budget."""
-    from oracle.oracle import OracleCircuit, transient
-    from xyce_gb300 import engine
+    from oracle.oracle import OracleCircuit, all_params, min_degree_order, transient
     nl, guess, tstop, tstep, uic, out = build_tran(name)
     opt = abi.device_options()
-    params = {t: engine.setup_params(nl, t, opt) for t in range(abi.NUM_DEV_TYPES) if nl.count(t)}
-    oc = OracleCircuit(nl, params, opt)
-    order, _ = engine.amd_order(oc.rowptr, oc.col)
+    oc = OracleCircuit(nl, all_params(nl, opt), opt)
+    order = min_degree_order(oc.rowptr, oc.col)
     window = tstop / 16
     while True:
         t0 = time.perf_counter()
@@ -172,7 +210,7 @@ def lu_shape(ctx, c):
     return info
 
 
-def run_tran(args, world, rank, local, dist):
+def run_tran(args, world, rank, local, dist, emit=True):
     import ctypes as C
 
     import torch
@@ -239,16 +277,15 @@ def run_tran(args, world, rank, local, dist):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded netlist, the reference's benchmark circuit shape)",
-        "config": {"workload": args.workload, "tstop": tstop, "tstep": tstep, "unknowns": c.n_unknowns,
-                   "nnz": c.nnz, "nnz_lu": info.nnz_lu, "lu_levels": info.levels,
+        "config": workload_config(args.workload),
+        "details": {"unknowns": c.n_unknowns, "nnz": c.nnz, "nnz_lu": info.nnz_lu, "lu_levels": info.levels,
                    "lu_precision": f"fp32+{nref} fp64 refinement" if args.fp32 else "fp64",
                    "lu_order": "nested dissection" if info.ordering == 1 else "minimum degree",
                    "lu_analysis": "done by the first (warm-up) run of the circuit, reused by the "
                                   "timed runs (same first Newton matrix)",
                    "load_build": "exact (reference rounding)" if args.exact_load
                    else "fma, long sums split over a block",
-                   "newton_iters_per_step": per_step_iters, "time_steps_per_step": st["steps"],
-                   "l2": "working set below L2; latency-bound"},
+                   "newton_iters_per_step": per_step_iters, "time_steps_per_step": st["steps"]},
         "roofline": {"kernel": "newton iteration", "bound": "hbm", "achieved": ach, "peak": hbm,
                      "unit": "GB/s", "frac": ach / hbm, "traffic": None, "peak_source": peak_kind,
                      "algorithmic_bytes_per_iter": b_iter},
@@ -261,14 +298,13 @@ def run_tran(args, world, rank, local, dist):
                          "sample": f".TRAN window {cpu_window:.3g} s: {cpu_n} Newton iterations on one core"},
         "wall_s": wall,
     }
-    print(json.dumps(line))
-    return 0
+    return _emit(line, emit)
 
 
 SERVE_METRIC = "served solves/sec"
 
 
-def run_serve(args, world, rank, local, dist):
+def run_serve(args, world, rank, local, dist, emit=True):
     import torch
 
     from xyce_gb300 import engine, serve
@@ -291,9 +327,10 @@ def run_serve(args, world, rank, local, dist):
     tuner = serve.Autotuner(serve_with, probe)
     sched = tuner.tune()
 
-    def one(prec, nref):
-        reqs = serve.ring_mc_requests(w["n"], seed=1, tstop=w["tstop"])
-        arr = serve.poisson_arrivals(w["n"], w["rate"], seed=2)
+    def one(prec, nref, n=None):
+        n = n or w["n"]
+        reqs = serve.ring_mc_requests(n, seed=1, tstop=w["tstop"])
+        arr = serve.poisson_arrivals(n, w["rate"], seed=2)
         srv = serve.Server(ctx, precision=prec, n_refine=nref, **sched)
         res = srv.run(reqs, arr)
         return res, reqs
@@ -301,8 +338,9 @@ def run_serve(args, world, rank, local, dist):
     # the mixed-precision form: FP32 factors and solves; every Newton step
     # computes the FP64 residual F(x) and solves for its correction, so the
     # Newton iteration refines the FP32 solve against the FP64 residual
+    # (warm-up streams: the first 1,000 requests of the stream at most)
     for _ in range(args.warmup):
-        one(abi.LU_FP32, 0)
+        one(abi.LU_FP32, 0, min(w["n"], 1000))
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -322,7 +360,7 @@ def run_serve(args, world, rank, local, dist):
     # about two seconds of arrivals each (at most the workload's request count)
     sweep = []
     if not args.no_sweep:
-        for rate in (100.0, 500.0, 2000.0, 5000.0):
+        for rate in [float(r) for r in args.sweep_rates.split(",") if r]:
             n = int(min(w["n"], max(100, 2 * rate)))
             row = {"rate_per_s": rate, "requests": n}
             for name, prec in (("mixed", abi.LU_FP32), ("fp64", abi.LU_FP64)):
@@ -353,13 +391,11 @@ def run_serve(args, world, rank, local, dist):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded Monte-Carlo ring oscillators, Poisson arrivals)",
-        "config": {"workload": args.workload, "requests": w["n"], "rate_per_s": w["rate"],
-                   "stages": "5-501 odd", "tstop": w["tstop"],
-                   "lu": "fp32 factors and solves, corrected by Newton against the fp64 residual",
+        "config": workload_config(args.workload),
+        "details": {"lu": "fp32 factors and solves, corrected by Newton against the fp64 residual",
                    "load_build": "exact (reference rounding)" if args.exact_load
                    else "fma, long sums split over a block",
-                   "schedule": sched, "autotuner_trials": len(tuner.trials),
-                   "l2": "per-request working sets below L2"},
+                   "schedule": sched, "autotuner_trials": len(tuner.trials)},
         "p50_ms": float(np.mean([r[0]["p50_ms"] for r in runs])),
         "p99_ms": float(np.mean([r[0]["p99_ms"] for r in runs])),
         "fp64": {"solves_per_s": f64["solves_per_s"], "p50_ms": f64["p50_ms"], "p99_ms": f64["p99_ms"]},
@@ -381,8 +417,7 @@ def run_serve(args, world, rank, local, dist):
                          "sample": f"{cpu_n} requests of the same stream, one core"},
         "wall_s": wall,
     }
-    print(json.dumps(line))
-    return 0
+    return _emit(line, emit)
 
 
 def run_batch(args, world, rank, local, dist):
@@ -434,11 +469,10 @@ def run_batch(args, world, rank, local, dist):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded Monte-Carlo ring oscillators, 5-501 stages)",
-        "config": {"workload": args.workload, "requests": len(reqs), "tstop": w["tstop"],
-                   "lu": "fp32, corrected by Newton" if args.fp32_batch else "fp64",
+        "config": workload_config(args.workload),
+        "details": {"lu": "fp32, corrected by Newton" if args.fp32_batch else "fp64",
                    "batch_iterations": batch_iters, "newton_iters_per_step": newton,
-                   "step": "set-up included (host analysis of every request)",
-                   "l2": "per-request working sets below L2"},
+                   "step": "set-up included (host analysis of every request)"},
         "newton_iters_per_s": newton / step_s,
         "roofline": {"kernel": "batch iteration", "bound": "hbm", "achieved": None,
                      "peak": measured_peaks()[0], "unit": "GB/s", "frac": None, "traffic": None,
@@ -459,22 +493,20 @@ def run_batch(args, world, rank, local, dist):
 def _serve_ref_worker(job):
     """Reference arm for serving: requests solved one after another on one core."""
     idx, n, tstop = job
-    from oracle.oracle import OracleCircuit, transient
-    from xyce_gb300 import engine, serve
+    from oracle.oracle import OracleCircuit, all_params, min_degree_order, transient
+    from xyce_gb300 import serve
     reqs = serve.ring_mc_requests(n, seed=1, tstop=tstop)
     opt = abi.device_options()
     t0 = time.perf_counter()
     done = 0
     for k in idx:
         r = reqs[k]
-        params = {t: engine.setup_params(r.netlist, t, opt) for t in range(abi.NUM_DEV_TYPES)
-                  if r.netlist.count(t)}
-        oc = OracleCircuit(r.netlist, params, opt)
-        order, _ = engine.amd_order(oc.rowptr, oc.col)
+        oc = OracleCircuit(r.netlist, all_params(r.netlist, opt), opt)
+        order = min_degree_order(oc.rowptr, oc.col)
         transient(oc, r.tstop, 1e-12, r.out_idx, col_order=order, x0=r.x0, uic=True)
         oc.close()
         done += 1
-    return done, time.perf_counter() - t0
+    return done, time.perf_counter() - t0, _mapped_libs()
 
 
 def serve_cpu_baseline(seconds=10.0):
@@ -483,14 +515,14 @@ def serve_cpu_baseline(seconds=10.0):
     done, t = 0, 0.0
     k = 0
     while t < seconds and k < w["n"]:
-        d, dt = _serve_ref_worker(([k], w["n"], w["tstop"]))
+        d, dt, _ = _serve_ref_worker(([k], w["n"], w["tstop"]))
         done += d
         t += dt
         k += 1
     return done / t, done
 
 
-def run_serve_reference(args, world, rank):
+def run_serve_reference(args, world, rank, emit=True):
     """CPU arm for serving: the request stream spread over every host core,
     each request solved by the oracle's transient driver."""
     if rank != 0:
@@ -501,13 +533,14 @@ def run_serve_reference(args, world, rank):
     sample = min(w["n"], 8 * cores)
     jobs = [(list(range(c, sample, cores)), w["n"], w["tstop"]) for c in range(cores)]
     ctx = mp.get_context("spawn")
-    times = []
+    times, libs = [], set(_mapped_libs())
     with ctx.Pool(cores) as pool:
         for k in range(args.warmup + args.steps):
             t0 = time.perf_counter()
-            pool.map(_serve_ref_worker, jobs)
+            out = pool.map(_serve_ref_worker, jobs)
             if k >= args.warmup:
                 times.append(time.perf_counter() - t0)
+            libs |= {q for r in out for q in r[2]}
     t = float(np.mean(times))
     value = sample / t
     line = {"metric": SERVE_METRIC if w["kind"] == "serve" else "solves/sec", "value": value,
@@ -515,27 +548,25 @@ def run_serve_reference(args, world, rank):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded)", "impl": "reference",
-            "config": {"workload": args.workload, "sample_requests": sample},
+            "config": workload_config(args.workload),
             "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
-                             "sample": f"{sample} of {w['n']} requests per step over {cores} processes"},
+                             "sample": f"{sample} of {w['n']} requests per step over {cores} processes",
+                             "libraries": sorted(libs)},
             "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
-    print(json.dumps(line))
-    return 0
+    return _emit(line, emit)
 
 
-def run_tran_reference(args, world, rank):
+def run_tran_reference(args, world, rank, emit=True):
     """CPU arm for transient workloads: the oracle's transient driver, one
     core per run (the reference's transient is single-threaded per rank)."""
     if rank != 0:
         return 0
-    from oracle.oracle import OracleCircuit, transient
-    from xyce_gb300 import engine
+    from oracle.oracle import OracleCircuit, all_params, min_degree_order, transient
     nl, guess, tstop, tstep, uic, out = build_tran(args.workload)
     opt = abi.device_options()
-    params = {t: engine.setup_params(nl, t, opt) for t in range(abi.NUM_DEV_TYPES) if nl.count(t)}
-    oc = OracleCircuit(nl, params, opt)
-    order, _ = engine.amd_order(oc.rowptr, oc.col)
+    oc = OracleCircuit(nl, all_params(nl, opt), opt)
+    order = min_degree_order(oc.rowptr, oc.col)
     # bounded per step: the leading window of the transient that one core
     # finishes in about the budget
     _, _, window, _ = tran_cpu_baseline(args.workload, seconds=args.cpu_seconds)
@@ -553,13 +584,14 @@ def run_tran_reference(args, world, rank):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded)", "impl": "reference",
-            "config": {"workload": args.workload, "tstop": window},
+            "config": workload_config(args.workload),
             "cpu_baseline": {"value": value, "unit": "newton-iters/s", "cores": 1, "kind": "port",
-                             "sample": f".TRAN window {window:.3g} s per step, one core"},
+                             "sample": f".TRAN window {window:.3g} s per step, one core (the "
+                                       "reference's transient runs on one thread)",
+                             "libraries": _mapped_libs()},
             "e2e": {"value": value, "unit": "newton-iters/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
-    print(json.dumps(line))
-    return 0
+    return _emit(line, emit)
 
 
 def build_workload(name):
@@ -610,19 +642,43 @@ def ncu_counts(workload, kernel):
         return json.load(f).get(workload, {}).get(kernel, {})
 
 
-def fp64_roofline(counts, kernel_ms, peak_flops, fma):
-    """The evaluation kernels are bound by the FP64 pipe: executed FP64 flops
-    (ncu count of the bit-exact build) per launch over the launch time, against
-    the DFMA throughput probed on this GPU in the same process."""
-    fl = counts.get("fp64_flops")
-    if not fl or not peak_flops or fma != (counts.get("build") == "fast"):
-        return {"achieved": None, "peak": peak_flops and peak_flops / 1e12, "unit": "TFLOP/s",
-                "frac": None, "note": "no ncu flop count for this kernel and build"}
-    ach = fl / (kernel_ms / 1e3)
-    return {"bound": "fp64", "achieved": ach / 1e12, "peak": peak_flops / 1e12, "unit": "TFLOP/s",
-            "frac": ach / peak_flops, "fp64_flops_per_launch": fl,
-            "fp64_pipe_active_ncu": counts.get("fp64_pipe_active"),
-            "peak_source": "xg_probe_fp64_rate (DFMA chains, this GPU, this run)"}
+def flop_counts(workload):
+    """Algorithmic FP64 operations of one load per instance (committed counts
+    of the oracle compiled over a counting scalar, oracle/count/), or {}."""
+    p = os.path.join(HERE, "profiles", "flop_counts.json")
+    if not os.path.exists(p):
+        return {}
+    with open(p) as f:
+        return json.load(f).get(workload, {})
+
+
+def fp64_roofline(workload, counts, n_inst, kernel_ms, peak_flops, fma, traffic):
+    """The evaluation kernels are bound by the FP64 pipe.  achieved =
+    algorithmic FP64 operations of the launch (the reference equations'
+    adds, multiplies, divides, square roots, exponentials and logarithms,
+    each counted once) over the launch time; peak = the DFMA throughput
+    probed on this GPU in the same process (GB300 nominal FP64: 1.25
+    TFLOP/s).  Executed FP64 flops (ncu, the exact build: a divide or
+    transcendental costs many instructions) are reported beside it."""
+    fc = flop_counts(workload)
+    alg = fc.get("eval_per_instance", 0.0) * n_inst
+    secs = kernel_ms / 1e3
+    out = {"kernel": "eval", "bound": "fp64", "unit": "TFLOP/s",
+           "peak": peak_flops / 1e12 if peak_flops else None, "traffic": traffic,
+           "peak_source": "xg_probe_fp64_rate (DFMA chains, this GPU, this run)",
+           "algorithmic_flops_per_launch": alg or None}
+    if alg and peak_flops:
+        out["achieved"] = alg / secs / 1e12
+        out["frac"] = alg / secs / peak_flops
+    else:
+        out["achieved"] = out["frac"] = None
+    ex = counts.get("fp64_flops")
+    if ex and peak_flops and fma == (counts.get("build") == "fast"):
+        out["executed_flops_per_launch"] = ex
+        out["executed_achieved"] = ex / secs / 1e12
+        out["frac_executed"] = ex / secs / peak_flops
+        out["fp64_pipe_active_ncu"] = counts.get("fp64_pipe_active")
+    return out
 
 
 def measured_peaks():
@@ -715,10 +771,10 @@ def slice_netlist(nl, params, t, i0, i1):
 
 def cpu_baseline_sample(nl, params, opt, seconds=10.0, max_instances=200_000):
     """The oracle on one core over a bounded sample of the workload."""
-    from oracle.oracle import OracleCircuit
+    from oracle.oracle import OracleCircuit, setup_params
     t = [k for k in range(abi.NUM_DEV_TYPES) if nl.count(k)][0]
-    nl, params = slice_netlist(nl, params, t, 0, min(nl.count(t), max_instances))
-    oc = OracleCircuit(nl, params, opt)
+    nl, _ = slice_netlist(nl, {t: np.zeros((1, nl.count(t)))}, t, 0, min(nl.count(t), max_instances))
+    oc = OracleCircuit(nl, {t: setup_params(nl, t, opt)}, opt)
     sol, sta, sto = netlists.random_state(oc.n_unknowns, oc.n_state, oc.n_store, seed=9)
     flags = abi.load_flags(transient=1, newton_iter=1, pdt=1e11)
     done = 0
@@ -741,13 +797,12 @@ def cpu_baseline_sample(nl, params, opt, seconds=10.0, max_instances=200_000):
 def _ref_worker(args):
     """One host process of the reference arm: loads instances [i0, i1)."""
     name, i0, i1, steps, warmup = args
-    from xyce_gb300 import engine
-    from oracle.oracle import OracleCircuit
+    from oracle.oracle import OracleCircuit, setup_params
     nl = build_workload(name)
     opt = abi.device_options()
     t = [t for t in range(abi.NUM_DEV_TYPES) if nl.count(t)][0]
     sub = slice_netlist(nl, {t: np.zeros((1, nl.count(t)))}, t, i0, i1)[0]
-    params = {t: engine.setup_params(sub, t, opt)}
+    params = {t: setup_params(sub, t, opt)}
     oc = OracleCircuit(sub, params, opt)
     sol, sta, sto = netlists.random_state(oc.n_unknowns, oc.n_state, oc.n_store, seed=9)
     flags = abi.load_flags(transient=1, newton_iter=1, pdt=1e11)
@@ -759,10 +814,10 @@ def _ref_worker(args):
         scratch = oc.load_range_timed(flags, sol, sta, sto, t, i0, i1, scratch)
         if k >= warmup:
             times.append(time.perf_counter() - t0)
-    return times
+    return times, _mapped_libs()
 
 
-def run_reference(args, world, rank):
+def run_reference(args, world, rank, emit=True):
     """CPU arm: the oracle port on all host cores (rank 0 only)."""
     if rank != 0:
         return 0
@@ -781,7 +836,9 @@ def run_reference(args, world, rank):
             for k in range(cores) if bounds[k + 1] > bounds[k]]
     ctx = mp.get_context("spawn")
     with ctx.Pool(len(jobs)) as pool:
-        res = pool.map(_ref_worker, jobs)
+        out = pool.map(_ref_worker, jobs)
+    res = [r[0] for r in out]
+    libs = sorted({q for r in out for q in r[1]} | set(_mapped_libs()))
     per_step = np.max(np.array(res), axis=0)       # slowest process per step
     t = float(np.mean(per_step))
     value = sample / t
@@ -789,17 +846,17 @@ def run_reference(args, world, rank):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3 * n / sample,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded)", "impl": "reference",
-            "config": {"workload": args.workload, "instances": n, "sample_instances": sample},
+            "config": workload_config(args.workload),
             "cpu_baseline": {"value": value, "unit": "instances/s", "cores": len(jobs),
                              "kind": "port",
-                             "sample": f"{sample} of {n} instances per step, {len(jobs)} processes"},
+                             "sample": f"{sample} of {n} instances per step, {len(jobs)} processes",
+                             "libraries": libs},
             "e2e": {"value": value, "unit": "instances/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
-    print(json.dumps(line))
-    return 0
+    return _emit(line, emit)
 
 
-def run_xg(args, world, rank, local, dist):
+def run_xg(args, world, rank, local, dist, emit=True):
     import ctypes as C
 
     import torch
@@ -903,24 +960,23 @@ def run_xg(args, world, rank, local, dist):
     counts = ncu_counts(args.workload, dom)
     traffic = counts.get("dram_bytes")
     c.close()
-    cpu_v, cpu_n = cpu_baseline_sample(nl, params, opt, seconds=args.cpu_seconds)
+    cpu_v, cpu_n = cpu_baseline_sample(nl, None, opt, seconds=args.cpu_seconds)
     clk = clocks.summary()
     line = {
         "metric": METRIC, "value": value, "unit": "instances/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded random netlist and node voltages)",
-        "config": {"workload": args.workload, "instances": n_inst, "unknowns": c.n_unknowns,
-                   "nnz": c.nnz, "fma": bool(args.fma),
-                   "l2": "inputs larger than L2 (parameter blocks alone exceed 129 MB)",
-                   "setup_s": round(t_setup, 3)},
+        "config": workload_config(args.workload),
+        "details": {"unknowns": c.n_unknowns, "nnz": c.nnz, "fma": bool(args.fma),
+                    "setup_s": round(t_setup, 3)},
         "kernels_ms": {"eval": ev_ms, "reduce": rd_ms},
-        "roofline": {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": hbm,
-                     "unit": "GB/s", "frac": ach / hbm, "traffic": traffic,
-                     "peak_source": peak_kind,
-                     "algorithmic_bytes": b_eval if dom == "eval" else b_red},
-        "roofline_fp64": fp64_roofline(counts, ev_ms if dom == "eval" else rd_ms, fp64_peak,
-                                       bool(args.fma)),
+        "roofline": fp64_roofline(args.workload, counts, n_inst, ev_ms, fp64_peak, bool(args.fma),
+                                  traffic) if dom == "eval" else None,
+        "roofline_hbm": {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": hbm,
+                         "unit": "GB/s", "frac": ach / hbm, "traffic": traffic,
+                         "peak_source": peak_kind,
+                         "algorithmic_bytes": b_eval if dom == "eval" else b_red},
         "roofline_load": {"achieved": b_load / step_s / 1e9, "unit": "GB/s",
                           "frac": b_load / step_s / 1e9 / hbm, "algorithmic_bytes": b_load},
         "e2e": {"value": world * n_inst / e2e_s, "unit": "instances/s", "h2d_bytes_per_step": h2d,
@@ -931,8 +987,48 @@ def run_xg(args, world, rank, local, dist):
                          "sample": f"{cpu_n} instance loads in ~{args.cpu_seconds:.0f} s, one core"},
         "wall_s": wall,
     }
-    print(json.dumps(line))
-    return 0
+    return _emit(line, emit)
+
+
+DEFAULT_WORKLOAD = "single_load_bsim3_1M"
+# The default run's sub-records: the other two metrics of the headline
+# benchmark, each on its own workload (Newton iterations per second of the
+# 1,000-stage inverter chain's whole .TRAN 1ps 20ns; served solves per second
+# and latency of the 10,000-request Monte-Carlo ring stream).
+SUB_NEWTON = dict(workload="tran_inverter_chain_1000", steps=3, warmup=1, fp32=False)
+SUB_SERVE = dict(workload="serve_ring_mc_10k", steps=1, warmup=1, sweep_rates="100,2000",
+                 no_sweep=False)
+
+
+def _sub_args(args, over):
+    a = argparse.Namespace(**vars(args))
+    for k, v in over.items():
+        setattr(a, k, v)
+    a.cpu_seconds = min(args.cpu_seconds, 5.0)
+    return a
+
+
+def run_default(args, world, rank, local, dist):
+    """The single load (headline line) with the Newton and serving metrics
+    as sub-records of the same line."""
+    line = run_xg(args, world, rank, local, dist, emit=False)
+    newton = run_tran(_sub_args(args, SUB_NEWTON), world, rank, local, dist, emit=False)
+    serving = run_serve(_sub_args(args, SUB_SERVE), world, rank, local, dist, emit=False)
+    if rank != 0:
+        return 0
+    line["newton"] = newton
+    line["serving"] = serving
+    line["gpu_launches_sub"] = {"newton": newton["gpu_launches"], "serving": serving["gpu_launches"]}
+    return _emit(line, True)
+
+
+def run_default_reference(args, world, rank):
+    if rank != 0:
+        return 0
+    line = run_reference(args, world, rank, emit=False)
+    line["newton"] = run_tran_reference(_sub_args(args, SUB_NEWTON), world, rank, emit=False)
+    line["serving"] = run_serve_reference(_sub_args(args, SUB_SERVE), world, rank, emit=False)
+    return _emit(line, True)
 
 
 def main():
@@ -941,12 +1037,17 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="xg", choices=["xg", "reference"])
-    ap.add_argument("--workload", default="single_load_bsim3_1M", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--fma", action="store_true")
     ap.add_argument("--fp32", action="store_true", help="transient: FP32 factors + FP64 refinement")
     ap.add_argument("--refine", type=int, default=2,
                     help="transient with --fp32: FP64 refinement steps per solve")
     ap.add_argument("--no-sweep", action="store_true", help="serving: skip the arrival-rate sweep")
+    ap.add_argument("--sweep-rates", default="100,500,2000,5000",
+                    help="serving: arrival rates [req/s] of the latency sweep")
+    ap.add_argument("--no-sub", action="store_true",
+                    help="default workload: the single load alone, without the Newton and "
+                         "serving sub-records")
     ap.add_argument("--fp32-batch", action="store_true",
                     help="batch workload: FP32 factors (Newton-corrected)")
     ap.add_argument("--exact-load", action="store_true",
@@ -955,13 +1056,15 @@ def main():
     args = ap.parse_args()
     world, rank, local, dist = dist_setup(args)
     kind = WORKLOADS[args.workload]["kind"]
+    composite = args.workload == DEFAULT_WORKLOAD and not args.no_sub
     if args.impl == "reference":
         ref = {"tran": run_tran_reference, "serve": run_serve_reference,
                "batch": run_serve_reference}.get(kind, run_reference)
-        rc = ref(args, world, rank)
+        rc = run_default_reference(args, world, rank) if composite else ref(args, world, rank)
     else:
         arm = {"tran": run_tran, "serve": run_serve, "batch": run_batch}.get(kind, run_xg)
-        rc = arm(args, world, rank, local, dist)
+        rc = (run_default(args, world, rank, local, dist) if composite
+              else arm(args, world, rank, local, dist))
     if dist:
         dist.destroy_process_group()
     return rc

@@ -35,6 +35,7 @@ def lib():
         L.xgo_tran_run.argtypes = [vp, C.POINTER(TranOpts), vp, vp, C.POINTER(C.c_int),
                                    C.POINTER(TranStats)]
         L.xgo_sparse_solve.argtypes = [C.c_int, vp, vp, vp, vp, vp, vp]
+        L.xgo_min_degree.argtypes = [C.c_int, vp, vp, vp]
         L.xgo_setup_params.argtypes = [C.POINTER(abi.XgNetlist), C.POINTER(abi.XgDeviceOptions),
                                        C.c_int, vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
         _lib = L
@@ -79,6 +80,18 @@ def all_params(netlist, options=None):
     """Parameter blocks of every device type present, from the oracle's set-up."""
     return {t: setup_params(netlist, t, options) for t in range(abi.NUM_DEV_TYPES)
             if netlist.count(t)}
+
+
+def min_degree_order(rowptr, col):
+    """Minimum-degree column order (dense rows last) of a CSR pattern for the
+    transient driver's sparse LU."""
+    rp = np.ascontiguousarray(rowptr, np.int32)
+    ci = np.ascontiguousarray(col, np.int32)
+    order = np.zeros(rp.size - 1, np.int32)
+    rc = lib().xgo_min_degree(rp.size - 1, _ptr(rp), _ptr(ci), _ptr(order))
+    if rc != 0:
+        raise RuntimeError(f"xgo_min_degree failed: {rc}")
+    return order
 
 
 def sparse_solve(rowptr, col, val, b, col_order=None):

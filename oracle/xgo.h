@@ -83,6 +83,9 @@ typedef struct {
  * at t = 0 and at every accepted step. 0 on success. */
 int xgo_tran_run(xgo_circuit *c, const xgo_tran_opts *o, double *t_out, double *v_out,
                  int *n_points, xgo_tran_stats *st);
+/* Minimum-degree column order of the n x n CSR pattern (xgo_order.c):
+ * order[k] = the k-th pivot column. */
+int xgo_min_degree(int n, const int *rowptr, const int *col, int *order);
 /* x = A^-1 b with the driver's sparse LU (CSR A, column order or NULL). */
 int xgo_sparse_solve(int n, const int *rowptr, const int *col, const double *val,
                      const int *col_order, const double *b, double *x);
