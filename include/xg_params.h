@@ -106,6 +106,54 @@ enum xg_b3_param {
   XG_B3_DSAT,               /* DrainSatCurrent                         */
   XG_B3_NVTM,               /* vtm * NJ                                */
   XG_B3_CZBD, XG_B3_CZBS, XG_B3_CZBDSW, XG_B3_CZBDSWG, XG_B3_CZBSSW, XG_B3_CZBSSWG,
+  /* Instance-constant subexpressions of updateIntermediateVars, each formed
+   * with the same operations in the same order as the evaluation would
+   * (so the results keep their bits):                                     */
+  XG_B3_XDEP0_SQRTPHI,      /* Xdep0 / sqrtPhi                          */
+  XG_B3_V0,                 /* vbi - phi                                */
+  XG_B3_DVT1_LEFF,          /* -0.5 * dvt1 * Leff                       */
+  XG_B3_DVT1W_WL,           /* -0.5 * dvt1w * weff * Leff               */
+  XG_B3_TRATIO,             /* temp / tnom - 1                          */
+  XG_B3_K1OX_NLX,           /* k1ox * (sqrt(1 + nlx / Leff) - 1) * sqrtPhi */
+  XG_B3_KT1_L,              /* kt1 + kt1l / Leff                        */
+  XG_B3_TOXPHI_W,           /* tox * phi / (weff + w0)                  */
+  XG_B3_VTH_BASE,           /* dtype * vth0 - k1 * sqrtPhi              */
+  XG_B3_K3B_TOXPHI,         /* k3b * (tox * phi / (weff + w0))          */
+  XG_B3_KT2_TRATIO,         /* kt2 * (temp / tnom - 1)                  */
+  XG_B3_NFACTOR_EPSSI,      /* nfactor * EPSSI                          */
+  XG_B3_VFB_PHI,            /* vfb + phi                                */
+  XG_B3_VTMCDEP_COX,        /* vtm * cdep0 / cox                        */
+  XG_B3_MCOX_VTMCDEP,       /* -cox / (vtm * cdep0)                     */
+  XG_B3_B0_W,               /* b0 / (weff + b1)                         */
+  XG_B3_AGS_A0,             /* ags * a0                                 */
+  XG_B3_VSAT2,              /* 2 * vsattemp                             */
+  XG_B3_ISUB_A,             /* alpha0 + alpha1 * Leff                   */
+  XG_B3_ISUB_T2,            /* (alpha0 + alpha1 * Leff) / Leff          */
+  XG_B3_BETA0_ET,           /* beta0 / EXP_THRESHOLD                    */
+  XG_B3_PSCBE1_LITL,        /* pscbe1 * litl                            */
+  XG_B3_PSCBE1_LITL_ET,     /* pscbe1 * litl / EXP_THRESHOLD            */
+  XG_B3_COXWL,              /* cox * weffCV * leffCV                    */
+  XG_B3_D3_VFBZB,           /* 4 * DELTA_3 * vfbzb                      */
+  XG_B3_TOX8,               /* 1e8 * tox                                */
+  XG_B3_LINK,               /* 1e-3 * tox                               */
+  XG_B3_LINK4_LDEB,         /* 4 * LINK * ldeb                          */
+  XG_B3_DPHI_DENOMI,        /* moin vtm k1ox^2 (k1ox > 0), else 0.25 moin vtm */
+  XG_B3_DPHI_T0,            /* k1ox sqrtPhi (k1ox > 0), else 0.5 sqrtPhi */
+  XG_B3_VTM2,               /* 2 * vtm                                  */
+  XG_B3_QBS0, XG_B3_QBSSW0, XG_B3_QBSSWG0,   /* PhiB*Temp * czbs, czbssw, czbsswg */
+  XG_B3_QBD0, XG_B3_QBDSW0, XG_B3_QBDSWG0,   /* ... * czbd, czbdsw, czbdswg      */
+  XG_B3_OMMJ, XG_B3_OMMJSW, XG_B3_OMMJSWG,   /* 1 - MJ, 1 - MJSW, 1 - MJSWG      */
+  XG_B3_CBS_F, XG_B3_CBSSW_F, XG_B3_CBSSWG_F,/* czbs * MJ / PhiBTemp, ...       */
+  XG_B3_CBD_F, XG_B3_CBDSW_F, XG_B3_CBDSWG_F,/* czbd * MJ / PhiBTemp, ...       */
+  XG_B3_CGDL_W, XG_B3_CGSL_W,                /* weffCV * cgdl, weffCV * cgsl    */
+  XG_B3_CGDO_T, XG_B3_CGSO_T,                /* cgdo + weffCV cgdl, cgso + ...  */
+  XG_B3_HALF_CKAPPA,                         /* 0.5 * ckappa                    */
+  /* Reciprocals of per-instance divisors, read only by the FMA build of the
+   * kernel, which multiplies by them instead of dividing:                 */
+  XG_B3_R_NVTM, XG_B3_R_SQRTPHI, XG_B3_R_PHIS3, XG_B3_R_COX, XG_B3_R_TOX,
+  XG_B3_R_LEFF, XG_B3_R_THETAROUT, XG_B3_R_TOX8, XG_B3_R_PSCBE2,
+  XG_B3_R_DPHI_DENOMI, XG_B3_R_CKAPPA, XG_B3_R_PHIB, XG_B3_R_PHIBSW,
+  XG_B3_R_PHIBSWG, XG_B3_R_OMMJ, XG_B3_R_OMMJSW, XG_B3_R_OMMJSWG,
   XG_B3_NPARAMS
 };
 

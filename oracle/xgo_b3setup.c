@@ -18,6 +18,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include "xg_b3_hoist.h"
 #include "xgo_internal.h"
 
 #define K_Q 1.6021918e-19
@@ -500,6 +501,7 @@ static int b3_instance(const b3card_t *M, const xg_mos_desc *d, int i, double te
   o[XG_B3_CZBDSWG] = czbdswg;
   o[XG_B3_CZBSSW] = czbssw;
   o[XG_B3_CZBSSWG] = czbsswg;
+  xg_b3_hoist(o);
   return XG_OK;
 }
 

@@ -66,6 +66,7 @@ def build_engine(verbose=False):
         obj = os.path.join(BUILD, f"load_kernels_{ns}.o")
         split = "1" if ns == "fast" else "0"
         jobs.append((obj, [src] + heads, cu_common + [f"-DXG_NS={ns}", f"-DXG_SPLIT_SUMS={split}",
+                                                      f"-DXG_FAST_DIV={split}",
                                                       f"-fmad={fmad}", "-c", src, "-o", obj]))
     for f in sorted(os.listdir(CSRC)):
         src = os.path.join(CSRC, f)
@@ -109,6 +110,34 @@ def build_oracle():
         _run(["gcc", "-std=c11", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wextra",
               "-I" + os.path.join(REPO, "include"), "-shared", "-o", ORACLE_LIB] + srcs + ["-lm"])
     return ORACLE_LIB
+
+
+ORACLE_COUNT_LIB = os.path.join(ORACLE_DIR, "_build", "liboracle_count.so")
+
+
+def build_oracle_count():
+    """The oracle's load compiled over a counting scalar (test
+    infrastructure: algorithmic operation counts, oracle/count/)."""
+    cdir = os.path.join(ORACLE_DIR, "count")
+    units = ["xgo.c", "xgo_support.c", "xgo_devices.c", "xgo_bsim3.c"]
+    deps = [os.path.join(ORACLE_DIR, f) for f in units] + [
+        os.path.join(cdir, f) for f in os.listdir(cdir) if f.endswith((".cpp", ".hpp"))]
+    deps += [os.path.join(REPO, "include", f) for f in os.listdir(os.path.join(REPO, "include"))]
+    if not _stale(ORACLE_COUNT_LIB, deps):
+        return ORACLE_COUNT_LIB
+    os.makedirs(os.path.dirname(ORACLE_COUNT_LIB), exist_ok=True)
+    objs = []
+    base = ["g++", "-std=c++17", "-fpermissive", "-w", "-O2", "-fPIC", "-I" + os.path.join(REPO, "include"),
+            "-I" + ORACLE_DIR]
+    for u in units:
+        o = os.path.join(os.path.dirname(ORACLE_COUNT_LIB), "count_" + u[:-2] + ".o")
+        _run(base + [f'-DXGO_UNIT="../{u}"', "-c", os.path.join(cdir, "xgo_count_unit.cpp"), "-o", o])
+        objs.append(o)
+    o = os.path.join(os.path.dirname(ORACLE_COUNT_LIB), "count_main.o")
+    _run(base + ["-c", os.path.join(cdir, "xgo_count.cpp"), "-o", o])
+    objs.append(o)
+    _run(["g++", "-shared", "-o", ORACLE_COUNT_LIB] + objs + ["-lm", "-Wl,--no-undefined"])
+    return ORACLE_COUNT_LIB
 
 
 if __name__ == "__main__":

@@ -28,6 +28,32 @@ constexpr double KQ = 1.6021918e-19;            // CONSTQ
 constexpr double KBOLTZ = 1.3806226e-23;        // CONSTboltz
 constexpr double CTOK = 273.15;                 // CONSTCtoK
 
+// Quotients.  The bit-exact build divides wherever the reference divides.
+// The FMA build (XG_FAST_DIV) forms the reciprocal of a denominator once
+// where several quotients share it, or reads it from the parameter block
+// where it is an instance constant, and multiplies: one divide (or none)
+// plus a multiply per quotient, ~1 ulp from the quotient, within the
+// tolerance that build is held to.  A literal divisor becomes a multiply by
+// its reciprocal, folded at compile time.
+//   B3_RCOL(name, k)   declares a reciprocal read from parameter column k
+//   B3_RCP(name, x)    declares the reciprocal of x (FMA build only)
+//   B3_DIV(a, b, rb)   a / b, or a * rb
+//   B3_DIVK(a, k)      a / k for a literal k, or a * (1 / k)
+//   B3_RSQRT(x)        1 / sqrt(x), or CUDA's rsqrt (within 1 ulp)
+#if XG_FAST_DIV
+#define B3_RCOL(name, k) const double name = PRM(k)
+#define B3_RCP(name, x) const double name = 1.0 / (x)
+#define B3_DIV(a, b, rb) ((a) * (rb))
+#define B3_DIVK(a, k) ((a) * (1.0 / (k)))
+#define B3_RSQRT(x) rsqrt(x)
+#else
+#define B3_RCOL(name, k) (void)0
+#define B3_RCP(name, x) (void)0
+#define B3_DIV(a, b, rb) ((a) / (b))
+#define B3_DIVK(a, k) ((a) / (k))
+#define B3_RSQRT(x) (1.0 / sqrt(x))
+#endif
+
 enum B3Mem {
   B3M_CAPCGGB = 0, B3M_CAPCGDB, B3M_CAPCGSB, B3M_CAPCDGB, B3M_CAPCDDB, B3M_CAPCDSB,
   B3M_CAPCSGB, B3M_CAPCSDB, B3M_CAPCSSB, B3M_CAPCBGB, B3M_CAPCBDB, B3M_CAPCBSB,
@@ -188,45 +214,41 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
   vgb = vgs - vbs;
 
   const double vtm = PRM(XG_B3_VTM);
-  Nvtm = vtm * PRM(XG_B3_NJ);
-  const double sourceArea = PRM(XG_B3_AS), sourcePerimeter = PRM(XG_B3_PS);
-  const double drainArea = PRM(XG_B3_AD), drainPerimeter = PRM(XG_B3_PD);
-  const double jctTempSatCurDensity = PRM(XG_B3_JSTEMP);
-  const double jctSidewallTempSatCurDensity = PRM(XG_B3_JSWTEMP);
+  Nvtm = PRM(XG_B3_NVTM);  // vtm * NJ
+  B3_RCOL(rNvtm, XG_B3_R_NVTM);
   const double ijth = PRM(XG_B3_IJTH);
-  if ((sourceArea <= 0.0) && (sourcePerimeter <= 0.0)) SourceSatCurrent = 1.0e-14;
-  else SourceSatCurrent = sourceArea * jctTempSatCurDensity + sourcePerimeter * jctSidewallTempSatCurDensity;
+  // area * Js + perimeter * Jsw, or 1e-14 with neither (set-up, :4475-4511)
+  SourceSatCurrent = PRM(XG_B3_SSAT);
   if (SourceSatCurrent <= 0.0) {
     gbs = gmin;
     cbs = gbs * vbs;
   } else if (ijth == 0.0) {
-    evbs = exp(vbs / Nvtm);
-    gbs = SourceSatCurrent * evbs / Nvtm + gmin;
+    evbs = exp(B3_DIV(vbs, Nvtm, rNvtm));
+    gbs = B3_DIV(SourceSatCurrent * evbs, Nvtm, rNvtm) + gmin;
     cbs = SourceSatCurrent * (evbs - 1.0) + gmin * vbs;
   } else if (vbs < PRM(XG_B3_VJSM)) {
-    evbs = exp(vbs / Nvtm);
-    gbs = SourceSatCurrent * evbs / Nvtm + gmin;
+    evbs = exp(B3_DIV(vbs, Nvtm, rNvtm));
+    gbs = B3_DIV(SourceSatCurrent * evbs, Nvtm, rNvtm) + gmin;
     cbs = SourceSatCurrent * (evbs - 1.0) + gmin * vbs;
   } else {
-    T0 = PRM(XG_B3_ISEVJSM) / Nvtm;
+    T0 = B3_DIV(PRM(XG_B3_ISEVJSM), Nvtm, rNvtm);
     gbs = T0 + gmin;
     cbs = PRM(XG_B3_ISEVJSM) - SourceSatCurrent + T0 * (vbs - PRM(XG_B3_VJSM)) + gmin * vbs;
   }
-  if ((drainArea <= 0.0) && (drainPerimeter <= 0.0)) DrainSatCurrent = 1.0e-14;
-  else DrainSatCurrent = drainArea * jctTempSatCurDensity + drainPerimeter * jctSidewallTempSatCurDensity;
+  DrainSatCurrent = PRM(XG_B3_DSAT);
   if (DrainSatCurrent <= 0.0) {
     gbd = gmin;
     cbd = gbd * vbd;
   } else if (ijth == 0.0) {
-    evbd = exp(vbd / Nvtm);
-    gbd = DrainSatCurrent * evbd / Nvtm + gmin;
+    evbd = exp(B3_DIV(vbd, Nvtm, rNvtm));
+    gbd = B3_DIV(DrainSatCurrent * evbd, Nvtm, rNvtm) + gmin;
     cbd = DrainSatCurrent * (evbd - 1.0) + gmin * vbd;
   } else if (vbd < PRM(XG_B3_VJDM)) {
-    evbd = exp(vbd / Nvtm);
-    gbd = DrainSatCurrent * evbd / Nvtm + gmin;
+    evbd = exp(B3_DIV(vbd, Nvtm, rNvtm));
+    gbd = B3_DIV(DrainSatCurrent * evbd, Nvtm, rNvtm) + gmin;
     cbd = DrainSatCurrent * (evbd - 1.0) + gmin * vbd;
   } else {
-    T0 = PRM(XG_B3_ISEVJDM) / Nvtm;
+    T0 = B3_DIV(PRM(XG_B3_ISEVJDM), Nvtm, rNvtm);
     gbd = T0 + gmin;
     cbd = PRM(XG_B3_ISEVJDM) - DrainSatCurrent + T0 * (vbd - PRM(XG_B3_VJDM)) + gmin * vbd;
   }
@@ -239,6 +261,8 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
 
   const double vbsc = PRM(XG_B3_VBSC), phi = PRM(XG_B3_PHI), phis3 = PRM(XG_B3_PHIS3);
   const double sqrtPhi = PRM(XG_B3_SQRTPHI), Xdep0 = PRM(XG_B3_XDEP0);
+  B3_RCOL(rPhis3, XG_B3_R_PHIS3);
+  B3_RCOL(rSqrtPhi, XG_B3_R_SQRTPHI);
   T0 = Vbs - vbsc - 0.001;
   double T1global = sqrt(T0 * T0 - 0.004 * vbsc);
   Vbseff = vbsc + 0.5 * (T0 + T1global);
@@ -249,19 +273,20 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
     Phis = phi * T0;
     dPhis_dVb = -T0 * T0;
     sqrtPhis = phis3 / (phi + 0.5 * Vbseff);
-    dsqrtPhis_dVb = -0.5 * sqrtPhis * sqrtPhis / phis3;
+    dsqrtPhis_dVb = B3_DIV(-0.5 * sqrtPhis * sqrtPhis, phis3, rPhis3);
   } else {
     Phis = phi - Vbseff;
     dPhis_dVb = -1.0;
     sqrtPhis = sqrt(Phis);
     dsqrtPhis_dVb = -0.5 / sqrtPhis;
   }
-  Xdep = Xdep0 * sqrtPhis / sqrtPhi;
-  dXdep_dVb = (Xdep0 / sqrtPhi) * dsqrtPhis_dVb;
+  Xdep = B3_DIV(Xdep0 * sqrtPhis, sqrtPhi, rSqrtPhi);
+  dXdep_dVb = PRM(XG_B3_XDEP0_SQRTPHI) * dsqrtPhis_dVb;
   Leff = PRM(XG_B3_LEFF);
   Vtm = vtm;
   T3 = sqrt(Xdep);
-  V0 = PRM(XG_B3_VBI) - phi;
+  B3_RCP(rSqXdep, T3);
+  V0 = PRM(XG_B3_V0);
   const double dvt2 = PRM(XG_B3_DVT2), dvt2w = PRM(XG_B3_DVT2W);
   T0 = dvt2 * Vbseff;
   if (T0 >= -0.5) {
@@ -273,7 +298,7 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
     T2 = dvt2 * T4 * T4;
   }
   lt1 = factor1 * T3 * T1;
-  dlt1_dVb = factor1 * (0.5 / T3 * T1 * dXdep_dVb + T3 * T2);
+  dlt1_dVb = factor1 * (B3_DIV(0.5, T3, rSqXdep) * T1 * dXdep_dVb + T3 * T2);
   T0 = dvt2w * Vbseff;
   if (T0 >= -0.5) {
     T1 = 1.0 + T0;
@@ -284,12 +309,13 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
     T2 = dvt2w * T4 * T4;
   }
   ltw = factor1 * T3 * T1;
-  dltw_dVb = factor1 * (0.5 / T3 * T1 * dXdep_dVb + T3 * T2);
-  T0 = -0.5 * PRM(XG_B3_DVT1) * Leff / lt1;
+  dltw_dVb = factor1 * (B3_DIV(0.5, T3, rSqXdep) * T1 * dXdep_dVb + T3 * T2);
+  B3_RCP(rlt1, lt1);
+  T0 = B3_DIV(PRM(XG_B3_DVT1_LEFF), lt1, rlt1);
   if (T0 > -EXP_THRESHOLD) {
     T1 = exp(T0);
     Theta0 = T1 * (1.0 + 2.0 * T1);
-    dT1_dVb = -T0 / lt1 * T1 * dlt1_dVb;
+    dT1_dVb = B3_DIV(-T0, lt1, rlt1) * T1 * dlt1_dVb;
     dTheta0_dVb = (1.0 + 4.0 * T1) * dT1_dVb;
   } else {
     T1 = MIN_EXP;
@@ -300,11 +326,12 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
   Delt_vth = thetavth * V0;
   dDelt_vth_dVb = PRM(XG_B3_DVT0) * dTheta0_dVb * V0;
   const double weff = PRM(XG_B3_WEFF);
-  T0 = -0.5 * PRM(XG_B3_DVT1W) * weff * Leff / ltw;
+  B3_RCP(rltw, ltw);
+  T0 = B3_DIV(PRM(XG_B3_DVT1W_WL), ltw, rltw);
   if (T0 > -EXP_THRESHOLD) {
     T1 = exp(T0);
     T2 = T1 * (1.0 + 2.0 * T1);
-    dT1_dVb = -T0 / ltw * T1 * dltw_dVb;
+    dT1_dVb = B3_DIV(-T0, ltw, rltw) * T1 * dltw_dVb;
     dT2_dVb = (1.0 + 4.0 * T1) * dT1_dVb;
   } else {
     T1 = MIN_EXP;
@@ -314,11 +341,10 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
   T0 = PRM(XG_B3_DVT0W) * T2;
   T2 = T0 * V0;
   dT2_dVb = PRM(XG_B3_DVT0W) * dT2_dVb * V0;
-  TempRatio = PRM(XG_B3_TEMP) / PRM(XG_B3_TNOM) - 1.0;
+  TempRatio = PRM(XG_B3_TRATIO);
   const double k1ox = PRM(XG_B3_K1OX), kt2 = PRM(XG_B3_KT2);
-  T0 = sqrt(1.0 + PRM(XG_B3_NLX) / Leff);
-  T1 = k1ox * (T0 - 1.0) * sqrtPhi + (PRM(XG_B3_KT1) + PRM(XG_B3_KT1L) / Leff + kt2 * Vbseff) * TempRatio;
-  tmp2 = tox * phi / (weff + PRM(XG_B3_W0));
+  T1 = PRM(XG_B3_K1OX_NLX) + (PRM(XG_B3_KT1_L) + kt2 * Vbseff) * TempRatio;
+  tmp2 = PRM(XG_B3_TOXPHI_W);
   const double etab = PRM(XG_B3_ETAB), theta0vb0 = PRM(XG_B3_THETA0VB0);
   T3 = PRM(XG_B3_ETA0) + etab * Vbseff;
   if (T3 < 1.0e-4) {
@@ -331,30 +357,32 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
   dDIBL_Sft_dVd = T3 * theta0vb0;
   DIBL_Sft = dDIBL_Sft_dVd * Vds;
   const double k2ox = PRM(XG_B3_K2OX), k3b = PRM(XG_B3_K3B);
-  Vth = dtype * PRM(XG_B3_VTH0) - PRM(XG_B3_K1) * sqrtPhi + k1ox * sqrtPhis - k2ox * Vbseff - Delt_vth -
+  Vth = PRM(XG_B3_VTH_BASE) + k1ox * sqrtPhis - k2ox * Vbseff - Delt_vth -
         T2 + (PRM(XG_B3_K3) + k3b * Vbseff) * tmp2 + T1 - DIBL_Sft;
   double von = Vth;
-  dVth_dVb = k1ox * dsqrtPhis_dVb - k2ox - dDelt_vth_dVb - dT2_dVb + k3b * tmp2 -
-             etab * Vds * theta0vb0 * T4 + kt2 * TempRatio;
+  dVth_dVb = k1ox * dsqrtPhis_dVb - k2ox - dDelt_vth_dVb - dT2_dVb + PRM(XG_B3_K3B_TOXPHI) -
+             etab * Vds * theta0vb0 * T4 + PRM(XG_B3_KT2_TRATIO);
   dVth_dVd = -dDIBL_Sft_dVd;
 
   const double cdscb = PRM(XG_B3_CDSCB), cdscd = PRM(XG_B3_CDSCD);
-  tmp2 = PRM(XG_B3_NFACTOR) * EPSSI / Xdep;
+  B3_RCP(rXdep, Xdep);
+  B3_RCOL(rcox, XG_B3_R_COX);
+  tmp2 = B3_DIV(PRM(XG_B3_NFACTOR_EPSSI), Xdep, rXdep);
   tmp3 = PRM(XG_B3_CDSC) + cdscb * Vbseff + cdscd * Vds;
-  tmp4 = (tmp2 + tmp3 * Theta0 + PRM(XG_B3_CIT)) / cox;
+  tmp4 = B3_DIV(tmp2 + tmp3 * Theta0 + PRM(XG_B3_CIT), cox, rcox);
   if (tmp4 >= -0.5) {
     n = 1.0 + tmp4;
-    dn_dVb = (-tmp2 / Xdep * dXdep_dVb + tmp3 * dTheta0_dVb + cdscb * Theta0) / cox;
-    dn_dVd = cdscd * Theta0 / cox;
+    dn_dVb = B3_DIV(B3_DIV(-tmp2, Xdep, rXdep) * dXdep_dVb + tmp3 * dTheta0_dVb + cdscb * Theta0, cox, rcox);
+    dn_dVd = B3_DIV(cdscd * Theta0, cox, rcox);
   } else {
     T0 = 1.0 / (3.0 + 8.0 * tmp4);
     n = (1.0 + 3.0 * tmp4) * T0;
     T0 *= T0;
-    dn_dVb = (-tmp2 / Xdep * dXdep_dVb + tmp3 * dTheta0_dVb + cdscb * Theta0) / cox * T0;
-    dn_dVd = cdscd * Theta0 / cox * T0;
+    dn_dVb = B3_DIV(B3_DIV(-tmp2, Xdep, rXdep) * dXdep_dVb + tmp3 * dTheta0_dVb + cdscb * Theta0, cox, rcox) * T0;
+    dn_dVd = B3_DIV(cdscd * Theta0, cox, rcox) * T0;
   }
 
-  T0 = PRM(XG_B3_VFB) + phi;
+  T0 = PRM(XG_B3_VFB_PHI);
   const double ngate = PRM(XG_B3_NGATE);
   if ((ngate > 1.e18) && (ngate < 1.e25) && (Vgs > T0)) {
     T1 = 1.0e6 * KQ * EPSSI * ngate / (cox * cox);
@@ -374,8 +402,9 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
 
   const double voff = PRM(XG_B3_VOFF), cdep0 = PRM(XG_B3_CDEP0);
   T10 = 2.0 * n * Vtm;
-  VgstNVt = Vgst / T10;
-  ExpArg = (2.0 * voff - Vgst) / T10;
+  B3_RCP(rT10, T10);
+  VgstNVt = B3_DIV(Vgst, T10, rT10);
+  ExpArg = B3_DIV(2.0 * voff - Vgst, T10, rT10);
   if (VgstNVt > EXP_THRESHOLD) {
     Vgsteff = Vgst;
     dVgsteff_dVg = dVgs_eff_dVg;
@@ -384,7 +413,7 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
   } else if (ExpArg > EXP_THRESHOLD) {
     T0 = (Vgst - voff) / (n * Vtm);
     ExpVgst = exp(T0);
-    Vgsteff = Vtm * cdep0 / cox * ExpVgst;
+    Vgsteff = PRM(XG_B3_VTMCDEP_COX) * ExpVgst;
     dVgsteff_dVg = Vgsteff / (n * Vtm);
     dVgsteff_dVd = -dVgsteff_dVg * (dVth_dVd + T0 * Vtm * dn_dVd);
     dVgsteff_dVb = -dVgsteff_dVg * (dVth_dVb + T0 * Vtm * dn_dVb);
@@ -393,17 +422,19 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
     ExpVgst = exp(VgstNVt);
     T1 = T10 * log(1.0 + ExpVgst);
     dT1_dVg = ExpVgst / (1.0 + ExpVgst);
-    dT1_dVb = -dT1_dVg * (dVth_dVb + Vgst / n * dn_dVb) + T1 / n * dn_dVb;
-    dT1_dVd = -dT1_dVg * (dVth_dVd + Vgst / n * dn_dVd) + T1 / n * dn_dVd;
-    dT2_dVg = -cox / (Vtm * cdep0) * exp(ExpArg);
+    B3_RCP(rn, n);
+    dT1_dVb = -dT1_dVg * (dVth_dVb + B3_DIV(Vgst, n, rn) * dn_dVb) + B3_DIV(T1, n, rn) * dn_dVb;
+    dT1_dVd = -dT1_dVg * (dVth_dVd + B3_DIV(Vgst, n, rn) * dn_dVd) + B3_DIV(T1, n, rn) * dn_dVd;
+    dT2_dVg = PRM(XG_B3_MCOX_VTMCDEP) * exp(ExpArg);
     T2 = 1.0 - T10 * dT2_dVg;
-    dT2_dVd = -dT2_dVg * (dVth_dVd - 2.0 * Vtm * ExpArg * dn_dVd) + (T2 - 1.0) / n * dn_dVd;
-    dT2_dVb = -dT2_dVg * (dVth_dVb - 2.0 * Vtm * ExpArg * dn_dVb) + (T2 - 1.0) / n * dn_dVb;
+    dT2_dVd = -dT2_dVg * (dVth_dVd - 2.0 * Vtm * ExpArg * dn_dVd) + B3_DIV(T2 - 1.0, n, rn) * dn_dVd;
+    dT2_dVb = -dT2_dVg * (dVth_dVb - 2.0 * Vtm * ExpArg * dn_dVb) + B3_DIV(T2 - 1.0, n, rn) * dn_dVb;
     Vgsteff = T1 / T2;
     T3 = T2 * T2;
-    dVgsteff_dVg = (T2 * dT1_dVg - T1 * dT2_dVg) / T3 * dVgs_eff_dVg;
-    dVgsteff_dVd = (T2 * dT1_dVd - T1 * dT2_dVd) / T3;
-    dVgsteff_dVb = (T2 * dT1_dVb - T1 * dT2_dVb) / T3;
+    B3_RCP(rT3, T3);
+    dVgsteff_dVg = B3_DIV(T2 * dT1_dVg - T1 * dT2_dVg, T3, rT3) * dVgs_eff_dVg;
+    dVgsteff_dVd = B3_DIV(T2 * dT1_dVd - T1 * dT2_dVd, T3, rT3);
+    dVgsteff_dVb = B3_DIV(T2 * dT1_dVb - T1 * dT2_dVb, T3, rT3);
   }
 
   const double dwg = PRM(XG_B3_DWG), dwb = PRM(XG_B3_DWB);
@@ -432,22 +463,23 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
     dRds_dVb = rds0 * prwb * dsqrtPhis_dVb * T1;
   }
 
-  T1 = 0.5 * k1ox / sqrtPhis;
-  dT1_dVb = -T1 / sqrtPhis * dsqrtPhis_dVb;
+  B3_RCP(rSqrtPhis, sqrtPhis);
+  T1 = B3_DIV(0.5 * k1ox, sqrtPhis, rSqrtPhis);
+  dT1_dVb = B3_DIV(-T1, sqrtPhis, rSqrtPhis) * dsqrtPhis_dVb;
   T9 = sqrt(PRM(XG_B3_XJ) * Xdep);
   tmp1 = Leff + 2.0 * T9;
-  T5 = Leff / tmp1;
+  B3_RCP(rtmp1, tmp1);
+  T5 = B3_DIV(Leff, tmp1, rtmp1);
   const double a0 = PRM(XG_B3_A0);
   tmp2 = a0 * T5;
-  tmp3 = weff + PRM(XG_B3_B1);
-  tmp4 = PRM(XG_B3_B0) / tmp3;
+  tmp4 = PRM(XG_B3_B0_W);  // b0 / (weff + b1)
   T2 = tmp2 + tmp4;
-  dT2_dVb = -T9 / tmp1 / Xdep * dXdep_dVb;
+  dT2_dVb = B3_DIV(B3_DIV(-T9, tmp1, rtmp1), Xdep, rXdep) * dXdep_dVb;
   T6 = T5 * T5;
   T7 = T5 * T6;
   Abulk0 = 1.0 + T1 * T2;
   dAbulk0_dVb = T1 * tmp2 * dT2_dVb + T2 * dT1_dVb;
-  T8 = PRM(XG_B3_AGS) * a0 * T7;
+  T8 = PRM(XG_B3_AGS_A0) * T7;
   dAbulk_dVg = -T1 * T8;
   Abulk = Abulk0 + dAbulk_dVg * Vgsteff;
   dAbulk_dVb = dAbulk0_dVb - T8 * Vgsteff * (dT1_dVb + 3.0 * T1 * dT2_dVb);
@@ -480,26 +512,27 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
   Abulk0 *= T0;
 
   const double ua = PRM(XG_B3_UA), ub = PRM(XG_B3_UB), uc = PRM(XG_B3_UC);
+  B3_RCOL(rtox, XG_B3_R_TOX);
   if (mobMod == 1) {
     T0 = Vgsteff + Vth + Vth;
     T2 = ua + uc * Vbseff;
-    T3 = T0 / tox;
+    T3 = B3_DIV(T0, tox, rtox);
     T5 = T3 * (T2 + ub * T3);
-    dDenomi_dVg = (T2 + 2.0 * ub * T3) / tox;
+    dDenomi_dVg = B3_DIV(T2 + 2.0 * ub * T3, tox, rtox);
     dDenomi_dVd = dDenomi_dVg * 2.0 * dVth_dVd;
     dDenomi_dVb = dDenomi_dVg * 2.0 * dVth_dVb + uc * T3;
   } else if (mobMod == 2) {
-    T5 = Vgsteff / tox * (ua + uc * Vbseff + ub * Vgsteff / tox);
-    dDenomi_dVg = (ua + uc * Vbseff + 2.0 * ub * Vgsteff / tox) / tox;
+    T5 = B3_DIV(Vgsteff, tox, rtox) * (ua + uc * Vbseff + B3_DIV(ub * Vgsteff, tox, rtox));
+    dDenomi_dVg = B3_DIV(ua + uc * Vbseff + B3_DIV(2.0 * ub * Vgsteff, tox, rtox), tox, rtox);
     dDenomi_dVd = 0.0;
-    dDenomi_dVb = Vgsteff * uc / tox;
+    dDenomi_dVb = B3_DIV(Vgsteff * uc, tox, rtox);
   } else {
     T0 = Vgsteff + Vth + Vth;
     T2 = 1.0 + uc * Vbseff;
-    T3 = T0 / tox;
+    T3 = B3_DIV(T0, tox, rtox);
     T4 = T3 * (ua + ub * T3);
     T5 = T4 * T2;
-    dDenomi_dVg = (ua + 2.0 * ub * T3) * T2 / tox;
+    dDenomi_dVg = B3_DIV((ua + 2.0 * ub * T3) * T2, tox, rtox);
     dDenomi_dVd = dDenomi_dVg * 2.0 * dVth_dVd;
     dDenomi_dVb = dDenomi_dVg * 2.0 * dVth_dVb + uc * T4;
   }
@@ -513,8 +546,9 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
     dDenomi_dVd *= T9;
     dDenomi_dVb *= T9;
   }
-  ueff = PRM(XG_B3_U0TEMP) / Denomi;
-  T9 = -ueff / Denomi;
+  B3_RCP(rDenomi, Denomi);
+  ueff = B3_DIV(PRM(XG_B3_U0TEMP), Denomi, rDenomi);
+  T9 = B3_DIV(-ueff, Denomi, rDenomi);
   dueff_dVg = T9 * dDenomi_dVg;
   dueff_dVd = T9 * dDenomi_dVd;
   dueff_dVb = T9 * dDenomi_dVb;
@@ -522,9 +556,11 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
   const double vsattemp = PRM(XG_B3_VSATTEMP);
   WVCox = Weff * vsattemp * cox;
   WVCoxRds = WVCox * Rds;
-  Esat = 2.0 * vsattemp / ueff;
+  B3_RCP(rueff, ueff);
+  Esat = B3_DIV(PRM(XG_B3_VSAT2), ueff, rueff);
   EsatL = Esat * Leff;
-  T0 = -EsatL / ueff;
+  B3_RCP(rEsatL, EsatL);
+  T0 = B3_DIV(-EsatL, ueff, rueff);
   dEsatL_dVg = T0 * dueff_dVg;
   dEsatL_dVd = T0 * dueff_dVd;
   dEsatL_dVb = T0 * dueff_dVb;
@@ -546,13 +582,16 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
     Lambda = 0.5 * (T1 + T2);
     dLambda_dVg = 0.5 * a1 * (1.0 + T1 / T2);
   }
-  Vgst2Vtm = Vgsteff + 2.0 * Vtm;
+  Vgst2Vtm = Vgsteff + PRM(XG_B3_VTM2);
+  B3_RCP(rVgst2Vtm, Vgst2Vtm);
+  B3_RCP(rWeff, Weff);
   if (Rds > 0) {
-    tmp2 = dRds_dVg / Rds + dWeff_dVg / Weff;
-    tmp3 = dRds_dVb / Rds + dWeff_dVb / Weff;
+    B3_RCP(rRds, Rds);
+    tmp2 = B3_DIV(dRds_dVg, Rds, rRds) + B3_DIV(dWeff_dVg, Weff, rWeff);
+    tmp3 = B3_DIV(dRds_dVb, Rds, rRds) + B3_DIV(dWeff_dVb, Weff, rWeff);
   } else {
-    tmp2 = dWeff_dVg / Weff;
-    tmp3 = dWeff_dVb / Weff;
+    tmp2 = B3_DIV(dWeff_dVg, Weff, rWeff);
+    tmp3 = B3_DIV(dWeff_dVb, Weff, rWeff);
   }
   if ((Rds == 0.0) && (Lambda == 1.0)) {
     T0 = 1.0 / (Abulk * EsatL + Vgst2Vtm);
@@ -587,14 +626,16 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
     dT2_dVb = Vgst2Vtm * (dEsatL_dVb + 2.0 * T6 * tmp3);
     dT2_dVd = Vgst2Vtm * dEsatL_dVd;
     T3 = sqrt(T1 * T1 - 2.0 * T0 * T2);
-    Vdsat = (T1 - T3) / T0;
+    B3_RCP(rT0v, T0);
+    B3_RCP(rT3v, T3);
+    Vdsat = B3_DIV(T1 - T3, T0, rT0v);
     dT3_dVg = (T1 * dT1_dVg - 2.0 * (T0 * dT2_dVg + T2 * dT0_dVg)) / T3;
     dT3_dVd = (T1 * dT1_dVd - 2.0 * (T0 * dT2_dVd + T2 * dT0_dVd)) / T3;
     dT3_dVb = (T1 * dT1_dVb - 2.0 * (T0 * dT2_dVb + T2 * dT0_dVb)) / T3;
     (void)dT3_dVg; (void)dT3_dVd; (void)dT3_dVb;
-    dVdsat_dVg = (dT1_dVg - (T1 * dT1_dVg - dT0_dVg * T2 - T0 * dT2_dVg) / T3 - Vdsat * dT0_dVg) / T0;
-    dVdsat_dVb = (dT1_dVb - (T1 * dT1_dVb - dT0_dVb * T2 - T0 * dT2_dVb) / T3 - Vdsat * dT0_dVb) / T0;
-    dVdsat_dVd = (dT1_dVd - (T1 * dT1_dVd - T0 * dT2_dVd) / T3) / T0;
+    dVdsat_dVg = B3_DIV(dT1_dVg - B3_DIV(T1 * dT1_dVg - dT0_dVg * T2 - T0 * dT2_dVg, T3, rT3v) - Vdsat * dT0_dVg, T0, rT0v);
+    dVdsat_dVb = B3_DIV(dT1_dVb - B3_DIV(T1 * dT1_dVb - dT0_dVb * T2 - T0 * dT2_dVb, T3, rT3v) - Vdsat * dT0_dVb, T0, rT0v);
+    dVdsat_dVd = B3_DIV(dT1_dVd - B3_DIV(T1 * dT1_dVd - T0 * dT2_dVd, T3, rT3v), T0, rT0v);
   }
 
   const double delta = PRM(XG_B3_DELTA);
@@ -603,8 +644,9 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
   dT1_dVd = dVdsat_dVd - 1.0;
   dT1_dVb = dVdsat_dVb;
   T2 = sqrt(T1 * T1 + 4.0 * delta * Vdsat);
-  T0 = T1 / T2;
-  T3 = 2.0 * delta / T2;
+  B3_RCP(rT2d, T2);
+  T0 = B3_DIV(T1, T2, rT2d);
+  T3 = B3_DIV(2.0 * delta, T2, rT2d);
   dT2_dVg = T0 * dT1_dVg + T3 * dVdsat_dVg;
   dT2_dVd = T0 * dT1_dVd + T3 * dVdsat_dVd;
   dT2_dVb = T0 * dT1_dVb + T3 * dVdsat_dVb;
@@ -618,35 +660,37 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
     dVdseff_dVb = 0.0;
   }
 
-  tmp4 = 1.0 - 0.5 * Abulk * Vdsat / Vgst2Vtm;
+  tmp4 = 1.0 - B3_DIV(0.5 * Abulk * Vdsat, Vgst2Vtm, rVgst2Vtm);
   T9 = WVCoxRds * Vgsteff;
-  T8 = T9 / Vgst2Vtm;
+  T8 = B3_DIV(T9, Vgst2Vtm, rVgst2Vtm);
   T0 = EsatL + Vdsat + 2.0 * T9 * tmp4;
   T7 = 2.0 * WVCoxRds * tmp4;
   dT0_dVg = dEsatL_dVg + dVdsat_dVg + T7 * (1.0 + tmp2 * Vgsteff) -
-            T8 * (Abulk * dVdsat_dVg - Abulk * Vdsat / Vgst2Vtm + Vdsat * dAbulk_dVg);
+            T8 * (Abulk * dVdsat_dVg - B3_DIV(Abulk * Vdsat, Vgst2Vtm, rVgst2Vtm) + Vdsat * dAbulk_dVg);
   dT0_dVb = dEsatL_dVb + dVdsat_dVb + T7 * tmp3 * Vgsteff - T8 * (dAbulk_dVb * Vdsat + Abulk * dVdsat_dVb);
   dT0_dVd = dEsatL_dVd + dVdsat_dVd - T8 * Abulk * dVdsat_dVd;
   T9 = WVCoxRds * Abulk;
   T1 = 2.0 / Lambda - 1.0 + T9;
   dT1_dVg = -2.0 * tmp1 + WVCoxRds * (Abulk * tmp2 + dAbulk_dVg);
   dT1_dVb = dAbulk_dVb * WVCoxRds + T9 * tmp3;
-  Vasat = T0 / T1;
-  dVasat_dVg = (dT0_dVg - Vasat * dT1_dVg) / T1;
-  dVasat_dVb = (dT0_dVb - Vasat * dT1_dVb) / T1;
-  dVasat_dVd = dT0_dVd / T1;
+  B3_RCP(rT1a, T1);
+  Vasat = B3_DIV(T0, T1, rT1a);
+  dVasat_dVg = B3_DIV(dT0_dVg - Vasat * dT1_dVg, T1, rT1a);
+  dVasat_dVb = B3_DIV(dT0_dVb - Vasat * dT1_dVb, T1, rT1a);
+  dVasat_dVd = B3_DIV(dT0_dVd, T1, rT1a);
   if (Vdseff > Vds) Vdseff = Vds;
   diffVds = Vds - Vdseff;
 
   const double pclm = PRM(XG_B3_PCLM), litl = PRM(XG_B3_LITL);
   if ((pclm > 0.0) && (diffVds > 1.0e-10)) {
     T0 = 1.0 / (pclm * Abulk * litl);
-    dT0_dVb = -T0 / Abulk * dAbulk_dVb;
-    dT0_dVg = -T0 / Abulk * dAbulk_dVg;
-    T2 = Vgsteff / EsatL;
+    B3_RCP(rAbulk, Abulk);
+    dT0_dVb = B3_DIV(-T0, Abulk, rAbulk) * dAbulk_dVb;
+    dT0_dVg = B3_DIV(-T0, Abulk, rAbulk) * dAbulk_dVg;
+    T2 = B3_DIV(Vgsteff, EsatL, rEsatL);
     T1 = Leff * (Abulk + T2);
-    dT1_dVg = Leff * ((1.0 - T2 * dEsatL_dVg) / EsatL + dAbulk_dVg);
-    dT1_dVb = Leff * (dAbulk_dVb - T2 * dEsatL_dVb / EsatL);
+    dT1_dVg = Leff * (B3_DIV(1.0 - T2 * dEsatL_dVg, EsatL, rEsatL) + dAbulk_dVg);
+    dT1_dVb = Leff * (dAbulk_dVb - B3_DIV(T2 * dEsatL_dVb, EsatL, rEsatL));
     dT1_dVd = -T2 * dEsatL_dVd / Esat;
     T9 = T0 * T1;
     VACLM = T9 * diffVds;
@@ -670,10 +714,13 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
     dT1_dVd = Abulk * dVdsat_dVd;
     T9 = T1 * T1;
     T2 = thetaRout;
-    VADIBL = (Vgst2Vtm - T0 / T1) / T2;
-    dVADIBL_dVg = (1.0 - dT0_dVg / T1 + T0 * dT1_dVg / T9) / T2;
-    dVADIBL_dVb = (-dT0_dVb / T1 + T0 * dT1_dVb / T9) / T2;
-    dVADIBL_dVd = (-dT0_dVd / T1 + T0 * dT1_dVd / T9) / T2;
+    B3_RCP(rT1r, T1);
+    B3_RCP(rT9r, T9);
+    B3_RCOL(rthetaRout, XG_B3_R_THETAROUT);
+    VADIBL = B3_DIV(Vgst2Vtm - B3_DIV(T0, T1, rT1r), T2, rthetaRout);
+    dVADIBL_dVg = B3_DIV(1.0 - B3_DIV(dT0_dVg, T1, rT1r) + B3_DIV(T0 * dT1_dVg, T9, rT9r), T2, rthetaRout);
+    dVADIBL_dVb = B3_DIV(B3_DIV(-dT0_dVb, T1, rT1r) + B3_DIV(T0 * dT1_dVb, T9, rT9r), T2, rthetaRout);
+    dVADIBL_dVd = B3_DIV(B3_DIV(-dT0_dVd, T1, rT1r) + B3_DIV(T0 * dT1_dVd, T9, rT9r), T2, rthetaRout);
     T7 = pdiblb * Vbseff;
     if (T7 >= -0.9) {
       T3 = 1.0 / (1.0 + T7);
@@ -693,19 +740,19 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
     VADIBL = MAX_EXP;
     dVADIBL_dVd = dVADIBL_dVg = dVADIBL_dVb = 0.0;
   }
-  T8 = PRM(XG_B3_PVAG) / EsatL;
+  T8 = B3_DIV(PRM(XG_B3_PVAG), EsatL, rEsatL);
   T9 = T8 * Vgsteff;
   if (T9 > -0.9) {
     T0 = 1.0 + T9;
-    dT0_dVg = T8 * (1.0 - Vgsteff * dEsatL_dVg / EsatL);
-    dT0_dVb = -T9 * dEsatL_dVb / EsatL;
-    dT0_dVd = -T9 * dEsatL_dVd / EsatL;
+    dT0_dVg = T8 * (1.0 - B3_DIV(Vgsteff * dEsatL_dVg, EsatL, rEsatL));
+    dT0_dVb = B3_DIV(-T9 * dEsatL_dVb, EsatL, rEsatL);
+    dT0_dVd = B3_DIV(-T9 * dEsatL_dVd, EsatL, rEsatL);
   } else {
     T1 = 1.0 / (17.0 + 20.0 * T9);
     T0 = (0.8 + T9) * T1;
     T1 *= T1;
-    dT0_dVg = T8 * (1.0 - Vgsteff * dEsatL_dVg / EsatL) * T1;
-    T9 *= T1 / EsatL;
+    dT0_dVg = T8 * (1.0 - B3_DIV(Vgsteff * dEsatL_dVg, EsatL, rEsatL)) * T1;
+    T9 *= B3_DIV(T1, EsatL, rEsatL);
     dT0_dVb = -T9 * dEsatL_dVb;
     dT0_dVd = -T9 * dEsatL_dVd;
   }
@@ -714,9 +761,10 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
   tmp3 = VACLM + VADIBL;
   T1 = VACLM * VADIBL / tmp3;
   tmp3 *= tmp3;
-  dT1_dVg = (tmp1 * dVADIBL_dVg + tmp2 * dVACLM_dVg) / tmp3;
-  dT1_dVd = (tmp1 * dVADIBL_dVd + tmp2 * dVACLM_dVd) / tmp3;
-  dT1_dVb = (tmp1 * dVADIBL_dVb + tmp2 * dVACLM_dVb) / tmp3;
+  B3_RCP(rtmp3, tmp3);
+  dT1_dVg = B3_DIV(tmp1 * dVADIBL_dVg + tmp2 * dVACLM_dVg, tmp3, rtmp3);
+  dT1_dVd = B3_DIV(tmp1 * dVADIBL_dVd + tmp2 * dVACLM_dVd, tmp3, rtmp3);
+  dT1_dVb = B3_DIV(tmp1 * dVADIBL_dVb + tmp2 * dVACLM_dVb, tmp3, rtmp3);
   Va = Vasat + T0 * T1;
   dVa_dVg = dVasat_dVg + T1 * dT0_dVg + T0 * dT1_dVg;
   dVa_dVd = dVasat_dVd + T1 * dT0_dVd + T0 * dT1_dVd;
@@ -724,10 +772,11 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
 
   const double pscbe1 = PRM(XG_B3_PSCBE1), pscbe2 = PRM(XG_B3_PSCBE2);
   if (pscbe2 > 0.0) {
-    if (diffVds > pscbe1 * litl / EXP_THRESHOLD) {
-      T0 = pscbe1 * litl / diffVds;
-      VASCBE = Leff * exp(T0) / pscbe2;
-      T1 = T0 * VASCBE / diffVds;
+    if (diffVds > PRM(XG_B3_PSCBE1_LITL_ET)) {
+      B3_RCP(rdiff, diffVds);
+      T0 = B3_DIV(PRM(XG_B3_PSCBE1_LITL), diffVds, rdiff);
+      VASCBE = B3_DIV(Leff * exp(T0), pscbe2, PRM(XG_B3_R_PSCBE2));
+      T1 = B3_DIV(T0 * VASCBE, diffVds, rdiff);
       dVASCBE_dVg = T1 * dVdseff_dVg;
       dVASCBE_dVd = -T1 * (1.0 - dVdseff_dVd);
       dVASCBE_dVb = T1 * dVdseff_dVb;
@@ -740,61 +789,67 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
     dVASCBE_dVg = dVASCBE_dVd = dVASCBE_dVb = 0.0;
   }
 
-  CoxWovL = cox * Weff / Leff;
+  CoxWovL = B3_DIV(cox * Weff, Leff, PRM(XG_B3_R_LEFF));
   beta = ueff * CoxWovL;
-  dbeta_dVg = CoxWovL * dueff_dVg + beta * dWeff_dVg / Weff;
+  dbeta_dVg = CoxWovL * dueff_dVg + B3_DIV(beta * dWeff_dVg, Weff, rWeff);
   dbeta_dVd = CoxWovL * dueff_dVd;
-  dbeta_dVb = CoxWovL * dueff_dVb + beta * dWeff_dVb / Weff;
-  T0 = 1.0 - 0.5 * Abulk * Vdseff / Vgst2Vtm;
-  dT0_dVg = -0.5 * (Abulk * dVdseff_dVg - Abulk * Vdseff / Vgst2Vtm + Vdseff * dAbulk_dVg) / Vgst2Vtm;
-  dT0_dVd = -0.5 * Abulk * dVdseff_dVd / Vgst2Vtm;
-  dT0_dVb = -0.5 * (Abulk * dVdseff_dVb + dAbulk_dVb * Vdseff) / Vgst2Vtm;
+  dbeta_dVb = CoxWovL * dueff_dVb + B3_DIV(beta * dWeff_dVb, Weff, rWeff);
+  T0 = 1.0 - B3_DIV(0.5 * Abulk * Vdseff, Vgst2Vtm, rVgst2Vtm);
+  dT0_dVg = B3_DIV(-0.5 * (Abulk * dVdseff_dVg - B3_DIV(Abulk * Vdseff, Vgst2Vtm, rVgst2Vtm) + Vdseff * dAbulk_dVg),
+                   Vgst2Vtm, rVgst2Vtm);
+  dT0_dVd = B3_DIV(-0.5 * Abulk * dVdseff_dVd, Vgst2Vtm, rVgst2Vtm);
+  dT0_dVb = B3_DIV(-0.5 * (Abulk * dVdseff_dVb + dAbulk_dVb * Vdseff), Vgst2Vtm, rVgst2Vtm);
   fgche1 = Vgsteff * T0;
   dfgche1_dVg = Vgsteff * dT0_dVg + T0;
   dfgche1_dVd = Vgsteff * dT0_dVd;
   dfgche1_dVb = Vgsteff * dT0_dVb;
-  T9 = Vdseff / EsatL;
+  T9 = B3_DIV(Vdseff, EsatL, rEsatL);
   fgche2 = 1.0 + T9;
-  dfgche2_dVg = (dVdseff_dVg - T9 * dEsatL_dVg) / EsatL;
-  dfgche2_dVd = (dVdseff_dVd - T9 * dEsatL_dVd) / EsatL;
-  dfgche2_dVb = (dVdseff_dVb - T9 * dEsatL_dVb) / EsatL;
-  gche = beta * fgche1 / fgche2;
-  dgche_dVg = (beta * dfgche1_dVg + fgche1 * dbeta_dVg - gche * dfgche2_dVg) / fgche2;
-  dgche_dVd = (beta * dfgche1_dVd + fgche1 * dbeta_dVd - gche * dfgche2_dVd) / fgche2;
-  dgche_dVb = (beta * dfgche1_dVb + fgche1 * dbeta_dVb - gche * dfgche2_dVb) / fgche2;
+  dfgche2_dVg = B3_DIV(dVdseff_dVg - T9 * dEsatL_dVg, EsatL, rEsatL);
+  dfgche2_dVd = B3_DIV(dVdseff_dVd - T9 * dEsatL_dVd, EsatL, rEsatL);
+  dfgche2_dVb = B3_DIV(dVdseff_dVb - T9 * dEsatL_dVb, EsatL, rEsatL);
+  B3_RCP(rfgche2, fgche2);
+  gche = B3_DIV(beta * fgche1, fgche2, rfgche2);
+  dgche_dVg = B3_DIV(beta * dfgche1_dVg + fgche1 * dbeta_dVg - gche * dfgche2_dVg, fgche2, rfgche2);
+  dgche_dVd = B3_DIV(beta * dfgche1_dVd + fgche1 * dbeta_dVd - gche * dfgche2_dVd, fgche2, rfgche2);
+  dgche_dVb = B3_DIV(beta * dfgche1_dVb + fgche1 * dbeta_dVb - gche * dfgche2_dVb, fgche2, rfgche2);
   T0 = 1.0 + gche * Rds;
-  T9 = Vdseff / T0;
+  B3_RCP(rT0i, T0);
+  T9 = B3_DIV(Vdseff, T0, rT0i);
   Idl = gche * T9;
-  dIdl_dVg = (gche * dVdseff_dVg + T9 * dgche_dVg) / T0 - Idl * gche / T0 * dRds_dVg;
-  dIdl_dVd = (gche * dVdseff_dVd + T9 * dgche_dVd) / T0;
-  dIdl_dVb = (gche * dVdseff_dVb + T9 * dgche_dVb - Idl * dRds_dVb * gche) / T0;
-  T9 = diffVds / Va;
+  dIdl_dVg = B3_DIV(gche * dVdseff_dVg + T9 * dgche_dVg, T0, rT0i) - B3_DIV(Idl * gche, T0, rT0i) * dRds_dVg;
+  dIdl_dVd = B3_DIV(gche * dVdseff_dVd + T9 * dgche_dVd, T0, rT0i);
+  dIdl_dVb = B3_DIV(gche * dVdseff_dVb + T9 * dgche_dVb - Idl * dRds_dVb * gche, T0, rT0i);
+  B3_RCP(rVa, Va);
+  T9 = B3_DIV(diffVds, Va, rVa);
   T0 = 1.0 + T9;
   Idsa = Idl * T0;
-  dIdsa_dVg = T0 * dIdl_dVg - Idl * (dVdseff_dVg + T9 * dVa_dVg) / Va;
-  dIdsa_dVd = T0 * dIdl_dVd + Idl * (1.0 - dVdseff_dVd - T9 * dVa_dVd) / Va;
-  dIdsa_dVb = T0 * dIdl_dVb - Idl * (dVdseff_dVb + T9 * dVa_dVb) / Va;
-  T9 = diffVds / VASCBE;
+  dIdsa_dVg = T0 * dIdl_dVg - B3_DIV(Idl * (dVdseff_dVg + T9 * dVa_dVg), Va, rVa);
+  dIdsa_dVd = T0 * dIdl_dVd + B3_DIV(Idl * (1.0 - dVdseff_dVd - T9 * dVa_dVd), Va, rVa);
+  dIdsa_dVb = T0 * dIdl_dVb - B3_DIV(Idl * (dVdseff_dVb + T9 * dVa_dVb), Va, rVa);
+  B3_RCP(rVASCBE, VASCBE);
+  T9 = B3_DIV(diffVds, VASCBE, rVASCBE);
   T0 = 1.0 + T9;
   Ids = Idsa * T0;
-  Gm = T0 * dIdsa_dVg - Idsa * (dVdseff_dVg + T9 * dVASCBE_dVg) / VASCBE;
-  Gds = T0 * dIdsa_dVd + Idsa * (1.0 - dVdseff_dVd - T9 * dVASCBE_dVd) / VASCBE;
-  Gmb = T0 * dIdsa_dVb - Idsa * (dVdseff_dVb + T9 * dVASCBE_dVb) / VASCBE;
+  Gm = T0 * dIdsa_dVg - B3_DIV(Idsa * (dVdseff_dVg + T9 * dVASCBE_dVg), VASCBE, rVASCBE);
+  Gds = T0 * dIdsa_dVd + B3_DIV(Idsa * (1.0 - dVdseff_dVd - T9 * dVASCBE_dVd), VASCBE, rVASCBE);
+  Gmb = T0 * dIdsa_dVb - B3_DIV(Idsa * (dVdseff_dVb + T9 * dVASCBE_dVb), VASCBE, rVASCBE);
   Gds += Gm * dVgsteff_dVd;
   Gmb += Gm * dVgsteff_dVb;
   Gm *= dVgsteff_dVg;
   Gmb *= dVbseff_dVb;
 
-  const double alpha0 = PRM(XG_B3_ALPHA0), alpha1 = PRM(XG_B3_ALPHA1), beta0 = PRM(XG_B3_BETA0);
-  tmp = alpha0 + alpha1 * Leff;
+  const double beta0 = PRM(XG_B3_BETA0);
+  tmp = PRM(XG_B3_ISUB_A);  // alpha0 + alpha1 * Leff
   if ((tmp <= 0.0) || (beta0 <= 0.0)) {
     Isub = Gbd = Gbb = Gbg = 0.0;
   } else {
-    T2 = tmp / Leff;
-    if (diffVds > beta0 / EXP_THRESHOLD) {
-      T0 = -beta0 / diffVds;
+    T2 = PRM(XG_B3_ISUB_T2);
+    if (diffVds > PRM(XG_B3_BETA0_ET)) {
+      B3_RCP(rdiffI, diffVds);
+      T0 = B3_DIV(-beta0, diffVds, rdiffI);
       T1 = T2 * diffVds * exp(T0);
-      T3 = T1 / diffVds * (T0 - 1.0);
+      T3 = B3_DIV(T1, diffVds, rdiffI) * (T0 - 1.0);
       dT1_dVg = T3 * dVdseff_dVg;
       dT1_dVd = T3 * (dVdseff_dVd - 1.0);
       dT1_dVb = T3 * dVdseff_dVb;
@@ -847,7 +902,7 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
     dVgst_dVb = -dVth_dVb;
     dVgst_dVg = dVgs_eff_dVg;
     (void)dVgst_dVb; (void)dVgst_dVg;
-    CoxWL = cox * weffCV * leffCV;
+    CoxWL = PRM(XG_B3_COXWL);
     Arg1 = Vgs_eff - Vbseff - Vfb;
     if (Arg1 <= 0.0) {
       qgate = CoxWL * Arg1;
@@ -1060,7 +1115,7 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
       VbseffCV = phi - Phis;
       dVbseffCV_dVb = -dPhis_dVb;
     }
-    CoxWL = cox * weffCV * leffCV;
+    CoxWL = PRM(XG_B3_COXWL);
     noff = n * PRM(XG_B3_NOFF);
     dnoff_dVd = PRM(XG_B3_NOFF) * dn_dVd;
     dnoff_dVb = PRM(XG_B3_NOFF) * dn_dVb;
@@ -1082,10 +1137,11 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
       ExpVgst = exp(VgstNVt);
       Vgsteff = T0 * log(1.0 + ExpVgst);
       dVgsteff_dVg = ExpVgst / (1.0 + ExpVgst);
-      dVgsteff_dVd = -dVgsteff_dVg * (dVth_dVd + (Vgst - voffcv) / noff * dnoff_dVd) +
-                     Vgsteff / noff * dnoff_dVd;
-      dVgsteff_dVb = -dVgsteff_dVg * (dVth_dVb + (Vgst - voffcv) / noff * dnoff_dVb) +
-                     Vgsteff / noff * dnoff_dVb;
+      B3_RCP(rnoff, noff);
+      dVgsteff_dVd = -dVgsteff_dVg * (dVth_dVd + B3_DIV(Vgst - voffcv, noff, rnoff) * dnoff_dVd) +
+                     B3_DIV(Vgsteff, noff, rnoff) * dnoff_dVd;
+      dVgsteff_dVb = -dVgsteff_dVg * (dVth_dVb + B3_DIV(Vgst - voffcv, noff, rnoff) * dnoff_dVb) +
+                     B3_DIV(Vgsteff, noff, rnoff) * dnoff_dVb;
       dVgsteff_dVg *= dVgs_eff_dVg;
     }
     if (capMod == 1) {
@@ -1217,10 +1273,10 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
       Vfb = PRM(XG_B3_VFBZB);
       V3 = Vfb - Vgs_eff + VbseffCV - DELTA_3;
       if (Vfb <= 0.0) {
-        T0 = sqrt(V3 * V3 - 4.0 * DELTA_3 * Vfb);
+        T0 = sqrt(V3 * V3 - PRM(XG_B3_D3_VFBZB));  // 4 DELTA_3 Vfb, Vfb = vfbzb
         T2 = -DELTA_3 / T0;
       } else {
-        T0 = sqrt(V3 * V3 + 4.0 * DELTA_3 * Vfb);
+        T0 = sqrt(V3 * V3 + PRM(XG_B3_D3_VFBZB));
         T2 = DELTA_3 / T0;
       }
       T1 = 0.5 * (1.0 + V3 / T0);
@@ -1341,21 +1397,22 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
       const double vfbzb = PRM(XG_B3_VFBZB), acde = PRM(XG_B3_ACDE), ldeb = PRM(XG_B3_LDEB);
       V3 = vfbzb - Vgs_eff + VbseffCV - DELTA_3;
       if (vfbzb <= 0.0) {
-        T0 = sqrt(V3 * V3 - 4.0 * DELTA_3 * vfbzb);
-        T2 = -DELTA_3 / T0;
+        T0 = sqrt(V3 * V3 - PRM(XG_B3_D3_VFBZB));
       } else {
-        T0 = sqrt(V3 * V3 + 4.0 * DELTA_3 * vfbzb);
-        T2 = DELTA_3 / T0;
+        T0 = sqrt(V3 * V3 + PRM(XG_B3_D3_VFBZB));
       }
-      T1 = 0.5 * (1.0 + V3 / T0);
+      B3_RCP(rT0f, T0);
+      T2 = B3_DIV(vfbzb <= 0.0 ? -DELTA_3 : DELTA_3, T0, rT0f);
+      T1 = 0.5 * (1.0 + B3_DIV(V3, T0, rT0f));
       Vfbeff = vfbzb - 0.5 * (V3 + T0);
       dVfbeff_dVg = T1 * dVgs_eff_dVg;
       dVfbeff_dVb = -T1 * dVbseffCV_dVb;
       Cox = cox;
-      Tox = 1.0e8 * tox;
-      T0 = (Vgs_eff - VbseffCV - vfbzb) / Tox;
-      dT0_dVg = dVgs_eff_dVg / Tox;
-      dT0_dVb = -dVbseffCV_dVb / Tox;
+      Tox = PRM(XG_B3_TOX8);
+      B3_RCOL(rTox, XG_B3_R_TOX8);
+      T0 = B3_DIV(Vgs_eff - VbseffCV - vfbzb, Tox, rTox);
+      dT0_dVg = B3_DIV(dVgs_eff_dVg, Tox, rTox);
+      dT0_dVb = B3_DIV(-dVbseffCV_dVb, Tox, rTox);
       tmp = T0 * acde;
       if ((-EXP_THRESHOLD < tmp) && (tmp < EXP_THRESHOLD)) {
         Tcen = ldeb * exp(tmp);
@@ -1369,23 +1426,25 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
         Tcen = ldeb * MAX_EXP;
         dTcen_dVg = dTcen_dVb = 0.0;
       }
-      LINK = 1.0e-3 * tox;
+      LINK = PRM(XG_B3_LINK);
       V3 = ldeb - Tcen - LINK;
-      V4 = sqrt(V3 * V3 + 4.0 * LINK * ldeb);
+      V4 = sqrt(V3 * V3 + PRM(XG_B3_LINK4_LDEB));
       Tcen = ldeb - 0.5 * (V3 + V4);
       T1 = 0.5 * (1.0 + V3 / V4);
       dTcen_dVg *= T1;
       dTcen_dVb *= T1;
-      Ccen = EPSSI / Tcen;
+      B3_RCP(rTcen, Tcen);
+      Ccen = B3_DIV(EPSSI, Tcen, rTcen);
       T2 = Cox / (Cox + Ccen);
       Coxeff = T2 * Ccen;
-      T3 = -Ccen / Tcen;
+      T3 = B3_DIV(-Ccen, Tcen, rTcen);
       dCoxeff_dVg = T2 * T2 * T3;
       dCoxeff_dVb = dCoxeff_dVg * dTcen_dVb;
       dCoxeff_dVg *= dTcen_dVg;
-      CoxWLcen = CoxWL * Coxeff / Cox;
+      CoxWLcen = B3_DIV(CoxWL * Coxeff, Cox, rcox);
       Qac0 = CoxWLcen * (Vfbeff - vfbzb);
-      QovCox = Qac0 / Coxeff;
+      B3_RCP(rCoxeff, Coxeff);
+      QovCox = B3_DIV(Qac0, Coxeff, rCoxeff);
       dQac0_dVg = CoxWLcen * dVfbeff_dVg + QovCox * dCoxeff_dVg;
       dQac0_dVb = CoxWLcen * dVfbeff_dVb + QovCox * dCoxeff_dVb;
       T0 = 0.5 * k1ox;
@@ -1401,62 +1460,62 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
         T2 = CoxWLcen * T0 / T1;
       }
       Qsub0 = CoxWLcen * k1ox * (T1 - T0);
-      QovCox = Qsub0 / Coxeff;
+      QovCox = B3_DIV(Qsub0, Coxeff, rCoxeff);
       dQsub0_dVg = T2 * (dVgs_eff_dVg - dVfbeff_dVg - dVgsteff_dVg) + QovCox * dCoxeff_dVg;
       dQsub0_dVd = -T2 * dVgsteff_dVd;
       dQsub0_dVb = -T2 * (dVfbeff_dVb + dVbseffCV_dVb + dVgsteff_dVb) + QovCox * dCoxeff_dVb;
-      const double moin = PRM(XG_B3_MOIN);
-      if (k1ox <= 0.0) {
-        Denomi = 0.25 * moin * Vtm;
-        T0 = 0.5 * sqrtPhi;
-      } else {
-        Denomi = moin * Vtm * k1ox * k1ox;
-        T0 = k1ox * sqrtPhi;
-      }
+      Denomi = PRM(XG_B3_DPHI_DENOMI);  // moin Vtm k1ox^2, or 0.25 moin Vtm
+      T0 = PRM(XG_B3_DPHI_T0);          // k1ox sqrtPhi, or 0.5 sqrtPhi
       T1 = 2.0 * T0 + Vgsteff;
-      DeltaPhi = Vtm * log(1.0 + T1 * Vgsteff / Denomi);
-      dDeltaPhi_dVg = 2.0 * Vtm * (T1 - T0) / (Denomi + T1 * Vgsteff);
+      DeltaPhi = Vtm * log(1.0 + B3_DIV(T1 * Vgsteff, Denomi, PRM(XG_B3_R_DPHI_DENOMI)));
+      dDeltaPhi_dVg = PRM(XG_B3_VTM2) * (T1 - T0) / (Denomi + T1 * Vgsteff);
       dDeltaPhi_dVd = dDeltaPhi_dVg * dVgsteff_dVd;
       dDeltaPhi_dVb = dDeltaPhi_dVg * dVgsteff_dVb;
       (void)dDeltaPhi_dVd; (void)dDeltaPhi_dVb;
       T3 = 4.0 * (Vth - vfbzb - phi);
       Tox += Tox;
+      // the doubled Tox's reciprocal is 0.5 / Tox exactly
       if (T3 >= 0.0) {
-        T0 = (Vgsteff + T3) / Tox;
-        dT0_dVd = (dVgsteff_dVd + 4.0 * dVth_dVd) / Tox;
-        dT0_dVb = (dVgsteff_dVb + 4.0 * dVth_dVb) / Tox;
+        T0 = B3_DIV(Vgsteff + T3, Tox, 0.5 * rTox);
+        dT0_dVd = B3_DIV(dVgsteff_dVd + 4.0 * dVth_dVd, Tox, 0.5 * rTox);
+        dT0_dVb = B3_DIV(dVgsteff_dVb + 4.0 * dVth_dVb, Tox, 0.5 * rTox);
       } else {
-        T0 = (Vgsteff + 1.0e-20) / Tox;
-        dT0_dVd = dVgsteff_dVd / Tox;
-        dT0_dVb = dVgsteff_dVb / Tox;
+        T0 = B3_DIV(Vgsteff + 1.0e-20, Tox, 0.5 * rTox);
+        dT0_dVd = B3_DIV(dVgsteff_dVd, Tox, 0.5 * rTox);
+        dT0_dVb = B3_DIV(dVgsteff_dVb, Tox, 0.5 * rTox);
       }
       tmp = exp(0.7 * log(T0));
       T1 = 1.0 + tmp;
       T2 = 0.7 * tmp / (T0 * Tox);
-      Tcen = 1.9e-9 / T1;
-      dTcen_dVg = -1.9e-9 * T2 / T1 / T1;
+      B3_RCP(rT1c, T1);
+      Tcen = B3_DIV(1.9e-9, T1, rT1c);
+      dTcen_dVg = B3_DIV(B3_DIV(-1.9e-9 * T2, T1, rT1c), T1, rT1c);
       dTcen_dVd = Tox * dTcen_dVg;
       dTcen_dVb = dTcen_dVd * dT0_dVb;
       dTcen_dVd *= dT0_dVd;
       dTcen_dVg *= dVgsteff_dVg;
-      Ccen = EPSSI / Tcen;
+      B3_RCP(rTcen2, Tcen);
+      Ccen = B3_DIV(EPSSI, Tcen, rTcen2);
       T0 = Cox / (Cox + Ccen);
       Coxeff = T0 * Ccen;
-      T1 = -Ccen / Tcen;
+      T1 = B3_DIV(-Ccen, Tcen, rTcen2);
       dCoxeff_dVg = T0 * T0 * T1;
       dCoxeff_dVd = dCoxeff_dVg * dTcen_dVd;
       dCoxeff_dVb = dCoxeff_dVg * dTcen_dVb;
       dCoxeff_dVg *= dTcen_dVg;
-      CoxWLcen = CoxWL * Coxeff / Cox;
+      CoxWLcen = B3_DIV(CoxWL * Coxeff, Cox, rcox);
       AbulkCV = Abulk0 * abulkCVfactor;
       dAbulkCV_dVb = abulkCVfactor * dAbulk0_dVb;
-      VdsatCV = (Vgsteff - DeltaPhi) / AbulkCV;
+      B3_RCP(rAbulkCV, AbulkCV);
+      B3_RCP(rCoxeff2, Coxeff);
+      VdsatCV = B3_DIV(Vgsteff - DeltaPhi, AbulkCV, rAbulkCV);
       V4 = VdsatCV - Vds - DELTA_4;
       T0 = sqrt(V4 * V4 + 4.0 * DELTA_4 * VdsatCV);
       VdseffCV = VdsatCV - 0.5 * (V4 + T0);
-      T1 = 0.5 * (1.0 + V4 / T0);
-      T2 = DELTA_4 / T0;
-      T3 = (1.0 - T1 - T2) / AbulkCV;
+      B3_RCP(rT0g, T0);
+      T1 = 0.5 * (1.0 + B3_DIV(V4, T0, rT0g));
+      T2 = B3_DIV(DELTA_4, T0, rT0g);
+      T3 = B3_DIV(1.0 - T1 - T2, AbulkCV, rAbulkCV);
       T4 = T3 * (1.0 - dDeltaPhi_dVg);
       dVdseffCV_dVg = T4;
       dVdseffCV_dVd = T1;
@@ -1469,31 +1528,32 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
       T0 = AbulkCV * VdseffCV;
       T1 = Vgsteff - DeltaPhi;
       T2 = 12.0 * (T1 - 0.5 * T0 + 1.0e-20);
-      T3 = T0 / T2;
+      B3_RCP(rT2h, T2);
+      T3 = B3_DIV(T0, T2, rT2h);
       T4 = 1.0 - 12.0 * T3 * T3;
-      T5 = AbulkCV * (6.0 * T0 * (4.0 * T1 - T0) / (T2 * T2) - 0.5);
-      T6 = T5 * VdseffCV / AbulkCV;
+      T5 = AbulkCV * (B3_DIV(6.0 * T0 * (4.0 * T1 - T0), T2 * T2, rT2h * rT2h) - 0.5);
+      T6 = B3_DIV(T5 * VdseffCV, AbulkCV, rAbulkCV);
       qgate = qinoi = CoxWLcen * (T1 - T0 * (0.5 - T3));
-      QovCox = qgate / Coxeff;
+      QovCox = B3_DIV(qgate, Coxeff, rCoxeff2);
       Cgg1 = CoxWLcen * (T4 * (1.0 - dDeltaPhi_dVg) + T5 * dVdseffCV_dVg);
       Cgd1 = CoxWLcen * T5 * dVdseffCV_dVd + Cgg1 * dVgsteff_dVd + QovCox * dCoxeff_dVd;
       Cgb1 = CoxWLcen * (T5 * dVdseffCV_dVb + T6 * dAbulkCV_dVb) + Cgg1 * dVgsteff_dVb + QovCox * dCoxeff_dVb;
       Cgg1 = Cgg1 * dVgsteff_dVg + QovCox * dCoxeff_dVg;
       T7 = 1.0 - AbulkCV;
       T8 = T2 * T2;
-      T9 = 12.0 * T7 * T0 * T0 / (T8 * AbulkCV);
+      T9 = B3_DIV(12.0 * T7 * T0 * T0, T8 * AbulkCV, rT2h * rT2h * rAbulkCV);
       T10 = T9 * (1.0 - dDeltaPhi_dVg);
-      T11 = -T7 * T5 / AbulkCV;
-      T12 = -(T9 * T1 / AbulkCV + VdseffCV * (0.5 - T0 / T2));
-      qbulk = CoxWLcen * T7 * (0.5 * VdseffCV - T0 * VdseffCV / T2);
-      QovCox = qbulk / Coxeff;
+      T11 = B3_DIV(-T7 * T5, AbulkCV, rAbulkCV);
+      T12 = -(B3_DIV(T9 * T1, AbulkCV, rAbulkCV) + VdseffCV * (0.5 - B3_DIV(T0, T2, rT2h)));
+      qbulk = CoxWLcen * T7 * (0.5 * VdseffCV - B3_DIV(T0 * VdseffCV, T2, rT2h));
+      QovCox = B3_DIV(qbulk, Coxeff, rCoxeff2);
       Cbg1 = CoxWLcen * (T10 + T11 * dVdseffCV_dVg);
       Cbd1 = CoxWLcen * T11 * dVdseffCV_dVd + Cbg1 * dVgsteff_dVd + QovCox * dCoxeff_dVd;
       Cbb1 = CoxWLcen * (T11 * dVdseffCV_dVb + T12 * dAbulkCV_dVb) + Cbg1 * dVgsteff_dVb + QovCox * dCoxeff_dVb;
       Cbg1 = Cbg1 * dVgsteff_dVg + QovCox * dCoxeff_dVg;
       if (xpart > 0.5) {
-        qsrc = -CoxWLcen * (T1 / 2.0 + T0 / 4.0 - 0.5 * T0 * T0 / T2);
-        QovCox = qsrc / Coxeff;
+        qsrc = -CoxWLcen * (T1 / 2.0 + T0 / 4.0 - B3_DIV(0.5 * T0 * T0, T2, rT2h));
+        QovCox = B3_DIV(qsrc, Coxeff, rCoxeff2);
         T2 += T2;
         T3 = T2 * T2;
         T7 = -(0.25 - 12.0 * T0 * (4.0 * T1 - T0) / T3);
@@ -1505,15 +1565,18 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
         Csb = CoxWLcen * (T5 * dVdseffCV_dVb + T6 * dAbulkCV_dVb) + Csg * dVgsteff_dVb + QovCox * dCoxeff_dVb;
         Csg = Csg * dVgsteff_dVg + QovCox * dCoxeff_dVg;
       } else if (xpart < 0.5) {
-        T2 = T2 / 12.0;
-        T3 = 0.5 * CoxWLcen / (T2 * T2);
-        T4 = T1 * (2.0 * T0 * T0 / 3.0 + T1 * (T1 - 4.0 * T0 / 3.0)) - 2.0 * T0 * T0 * T0 / 15.0;
+        T2 = B3_DIVK(T2, 12.0);
+        B3_RCP(rT2x, T2);
+        T3 = B3_DIV(0.5 * CoxWLcen, T2 * T2, rT2x * rT2x);
+        T4 = T1 * (B3_DIVK(2.0 * T0 * T0, 3.0) + T1 * (T1 - B3_DIVK(4.0 * T0, 3.0))) -
+             B3_DIVK(2.0 * T0 * T0 * T0, 15.0);
         qsrc = -T3 * T4;
-        QovCox = qsrc / Coxeff;
+        QovCox = B3_DIV(qsrc, Coxeff, rCoxeff2);
         T8 = 4.0 / 3.0 * T1 * (T1 - T0) + 0.4 * T0 * T0;
-        T5 = -2.0 * qsrc / T2 - T3 * (T1 * (3.0 * T1 - 8.0 * T0 / 3.0) + 2.0 * T0 * T0 / 3.0);
-        T6 = AbulkCV * (qsrc / T2 + T3 * T8);
-        T7 = T6 * VdseffCV / AbulkCV;
+        T5 = B3_DIV(-2.0 * qsrc, T2, rT2x) -
+             T3 * (T1 * (3.0 * T1 - B3_DIVK(8.0 * T0, 3.0)) + B3_DIVK(2.0 * T0 * T0, 3.0));
+        T6 = AbulkCV * (B3_DIV(qsrc, T2, rT2x) + T3 * T8);
+        T7 = B3_DIV(T6 * VdseffCV, AbulkCV, rAbulkCV);
         Csg = T5 * (1.0 - dDeltaPhi_dVg) + T6 * dVdseffCV_dVg;
         Csd = Csg * dVgsteff_dVd + T6 * dVdseffCV_dVd + QovCox * dCoxeff_dVd;
         Csb = Csg * dVgsteff_dVb + T6 * dVdseffCV_dVb + T7 * dAbulkCV_dVb + QovCox * dCoxeff_dVb;
@@ -1553,22 +1616,13 @@ finished:
   m.cd = cdrain;
   capbs = capbd = qbs = qbd = 0.0;
   if (ChargeComputationNeeded) {
-    czbd = PRM(XG_B3_CJTEMP) * drainArea;
-    czbs = PRM(XG_B3_CJTEMP) * sourceArea;
-    if (drainPerimeter < weff) {
-      czbdswg = PRM(XG_B3_CJSWGTEMP) * drainPerimeter;
-      czbdsw = 0.0;
-    } else {
-      czbdsw = PRM(XG_B3_CJSWTEMP) * (drainPerimeter - weff);
-      czbdswg = PRM(XG_B3_CJSWGTEMP) * weff;
-    }
-    if (sourcePerimeter < weff) {
-      czbssw = 0.0;
-      czbsswg = PRM(XG_B3_CJSWGTEMP) * sourcePerimeter;
-    } else {
-      czbssw = PRM(XG_B3_CJSWTEMP) * (sourcePerimeter - weff);
-      czbsswg = PRM(XG_B3_CJSWGTEMP) * weff;
-    }
+    // bottom and sidewall junction capacitances (:6983-7007), from set-up
+    czbd = PRM(XG_B3_CZBD);
+    czbs = PRM(XG_B3_CZBS);
+    czbdsw = PRM(XG_B3_CZBDSW);
+    czbdswg = PRM(XG_B3_CZBDSWG);
+    czbssw = PRM(XG_B3_CZBSSW);
+    czbsswg = PRM(XG_B3_CZBSSWG);
     MJ = PRM(XG_B3_MJ);
     MJSW = PRM(XG_B3_MJSW);
     MJSWG = PRM(XG_B3_MJSWG);
@@ -1579,32 +1633,32 @@ finished:
       capbs = czbs + czbssw + czbsswg;
     } else if (vbs < 0.0) {
       if (czbs > 0.0) {
-        arg = 1.0 - vbs / PhiBTemp;
-        if (MJ == 0.5) sarg = 1.0 / sqrt(arg);
+        arg = 1.0 - B3_DIV(vbs, PhiBTemp, PRM(XG_B3_R_PHIB));
+        if (MJ == 0.5) sarg = B3_RSQRT(arg);
         else sarg = exp(-MJ * log(arg));
-        qbs = PhiBTemp * czbs * (1.0 - arg * sarg) / (1.0 - MJ);
+        qbs = B3_DIV(PRM(XG_B3_QBS0) * (1.0 - arg * sarg), PRM(XG_B3_OMMJ), PRM(XG_B3_R_OMMJ));
         capbs = czbs * sarg;
       } else {
         qbs = 0.0;
         capbs = 0.0;
       }
       if (czbssw > 0.0) {
-        arg = 1.0 - vbs / PhiBSWTemp;
-        if (MJSW == 0.5) sarg = 1.0 / sqrt(arg);
+        arg = 1.0 - B3_DIV(vbs, PhiBSWTemp, PRM(XG_B3_R_PHIBSW));
+        if (MJSW == 0.5) sarg = B3_RSQRT(arg);
         else sarg = exp(-MJSW * log(arg));
-        qbs += PhiBSWTemp * czbssw * (1.0 - arg * sarg) / (1.0 - MJSW);
+        qbs += B3_DIV(PRM(XG_B3_QBSSW0) * (1.0 - arg * sarg), PRM(XG_B3_OMMJSW), PRM(XG_B3_R_OMMJSW));
         capbs += czbssw * sarg;
       }
       if (czbsswg > 0.0) {
-        arg = 1.0 - vbs / PhiBSWGTemp;
-        if (MJSWG == 0.5) sarg = 1.0 / sqrt(arg);
+        arg = 1.0 - B3_DIV(vbs, PhiBSWGTemp, PRM(XG_B3_R_PHIBSWG));
+        if (MJSWG == 0.5) sarg = B3_RSQRT(arg);
         else sarg = exp(-MJSWG * log(arg));
-        qbs += PhiBSWGTemp * czbsswg * (1.0 - arg * sarg) / (1.0 - MJSWG);
+        qbs += B3_DIV(PRM(XG_B3_QBSSWG0) * (1.0 - arg * sarg), PRM(XG_B3_OMMJSWG), PRM(XG_B3_R_OMMJSWG));
         capbs += czbsswg * sarg;
       }
     } else {
       T0 = czbs + czbssw + czbsswg;
-      T1 = vbs * (czbs * MJ / PhiBTemp + czbssw * MJSW / PhiBSWTemp + czbsswg * MJSWG / PhiBSWGTemp);
+      T1 = vbs * (PRM(XG_B3_CBS_F) + PRM(XG_B3_CBSSW_F) + PRM(XG_B3_CBSSWG_F));
       qbs = vbs * (T0 + 0.5 * T1);
       capbs = T0 + T1;
     }
@@ -1613,32 +1667,32 @@ finished:
       capbd = czbd + czbdsw + czbdswg;
     } else if (vbd < 0.0) {
       if (czbd > 0.0) {
-        arg = 1.0 - vbd / PhiBTemp;
-        if (MJ == 0.5) sarg = 1.0 / sqrt(arg);
+        arg = 1.0 - B3_DIV(vbd, PhiBTemp, PRM(XG_B3_R_PHIB));
+        if (MJ == 0.5) sarg = B3_RSQRT(arg);
         else sarg = exp(-MJ * log(arg));
-        qbd = PhiBTemp * czbd * (1.0 - arg * sarg) / (1.0 - MJ);
+        qbd = B3_DIV(PRM(XG_B3_QBD0) * (1.0 - arg * sarg), PRM(XG_B3_OMMJ), PRM(XG_B3_R_OMMJ));
         capbd = czbd * sarg;
       } else {
         qbd = 0.0;
         capbd = 0.0;
       }
       if (czbdsw > 0.0) {
-        arg = 1.0 - vbd / PhiBSWTemp;
-        if (MJSW == 0.5) sarg = 1.0 / sqrt(arg);
+        arg = 1.0 - B3_DIV(vbd, PhiBSWTemp, PRM(XG_B3_R_PHIBSW));
+        if (MJSW == 0.5) sarg = B3_RSQRT(arg);
         else sarg = exp(-MJSW * log(arg));
-        qbd += PhiBSWTemp * czbdsw * (1.0 - arg * sarg) / (1.0 - MJSW);
+        qbd += B3_DIV(PRM(XG_B3_QBDSW0) * (1.0 - arg * sarg), PRM(XG_B3_OMMJSW), PRM(XG_B3_R_OMMJSW));
         capbd += czbdsw * sarg;
       }
       if (czbdswg > 0.0) {
-        arg = 1.0 - vbd / PhiBSWGTemp;
-        if (MJSWG == 0.5) sarg = 1.0 / sqrt(arg);
+        arg = 1.0 - B3_DIV(vbd, PhiBSWGTemp, PRM(XG_B3_R_PHIBSWG));
+        if (MJSWG == 0.5) sarg = B3_RSQRT(arg);
         else sarg = exp(-MJSWG * log(arg));
-        qbd += PhiBSWGTemp * czbdswg * (1.0 - arg * sarg) / (1.0 - MJSWG);
+        qbd += B3_DIV(PRM(XG_B3_QBDSWG0) * (1.0 - arg * sarg), PRM(XG_B3_OMMJSWG), PRM(XG_B3_R_OMMJSWG));
         capbd += czbdswg * sarg;
       }
     } else {
       T0 = czbd + czbdsw + czbdswg;
-      T1 = vbd * (czbd * MJ / PhiBTemp + czbdsw * MJSW / PhiBSWTemp + czbdswg * MJSWG / PhiBSWGTemp);
+      T1 = vbd * (PRM(XG_B3_CBD_F) + PRM(XG_B3_CBDSW_F) + PRM(XG_B3_CBDSWG_F));
       qbd = vbd * (T0 + 0.5 * T1);
       capbd = T0 + T1;
     }
@@ -1673,17 +1727,17 @@ finished:
       T0 = vgd + DELTA_1;
       T1 = sqrt(T0 * T0 + 4.0 * DELTA_1);
       T2 = 0.5 * (T0 - T1);
-      T3 = weffCV * cgdl;
-      T4 = sqrt(1.0 - 4.0 * T2 / ckappa);
-      cgdo = PRM(XG_B3_CGDO) + T3 - T3 * (1.0 - 1.0 / T4) * (0.5 - 0.5 * T0 / T1);
-      qgdo = (PRM(XG_B3_CGDO) + T3) * vgd - T3 * (T2 + 0.5 * ckappa * (T4 - 1.0));
+      T3 = PRM(XG_B3_CGDL_W);  // weffCV * cgdl
+      T4 = sqrt(1.0 - B3_DIV(4.0 * T2, ckappa, PRM(XG_B3_R_CKAPPA)));
+      cgdo = PRM(XG_B3_CGDO_T) - T3 * (1.0 - 1.0 / T4) * (0.5 - 0.5 * T0 / T1);
+      qgdo = PRM(XG_B3_CGDO_T) * vgd - T3 * (T2 + PRM(XG_B3_HALF_CKAPPA) * (T4 - 1.0));
       T0 = vgs + DELTA_1;
       T1 = sqrt(T0 * T0 + 4.0 * DELTA_1);
       T2 = 0.5 * (T0 - T1);
-      T3 = weffCV * cgsl;
-      T4 = sqrt(1.0 - 4.0 * T2 / ckappa);
-      cgso = PRM(XG_B3_CGSO) + T3 - T3 * (1.0 - 1.0 / T4) * (0.5 - 0.5 * T0 / T1);
-      qgso = (PRM(XG_B3_CGSO) + T3) * vgs - T3 * (T2 + 0.5 * ckappa * (T4 - 1.0));
+      T3 = PRM(XG_B3_CGSL_W);  // weffCV * cgsl
+      T4 = sqrt(1.0 - B3_DIV(4.0 * T2, ckappa, PRM(XG_B3_R_CKAPPA)));
+      cgso = PRM(XG_B3_CGSO_T) - T3 * (1.0 - 1.0 / T4) * (0.5 - 0.5 * T0 / T1);
+      qgso = PRM(XG_B3_CGSO_T) * vgs - T3 * (T2 + PRM(XG_B3_HALF_CKAPPA) * (T4 - 1.0));
     }
     /* setupCapacitors_oldDAE: charge sums and partition (:7640-7898), nqsMod 0 */
     const double cgbo = PRM(XG_B3_CGBO);

@@ -18,6 +18,7 @@
 #include <string>
 #include <vector>
 
+#include "xg_b3_hoist.h"
 #include "xg_bsim3_setup.h"
 
 namespace xg {
@@ -563,6 +564,7 @@ int b3_instance_params(const B3Model &M, const xg_mos_desc &d, int i,
   o[XG_B3_CZBDSWG] = czbdswg;
   o[XG_B3_CZBSSW] = czbssw;
   o[XG_B3_CZBSSWG] = czbsswg;
+  xg_b3_hoist(o);
   return XG_OK;
 }
 
