@@ -291,6 +291,16 @@ int xg_lu_solve(xg_lu *lu, const double *dev_b, double *dev_x, int n_refine);
 int xg_lu_refactor_solve(xg_lu *lu, const double *dev_values, const double *dev_b, double *dev_x,
                          int n_refine);
 int xg_lu_status(xg_lu *lu, int *status, int *bad_row);
+/* xg_lu_solve_host — the same refactor (skipped with reuse_factors) and
+ * solve for a caller whose matrix and vectors live in host memory, as the
+ * reference's solvers receive them from Epetra (N_LAS_AmesosSolver::solve,
+ * N_LAS_AmesosSolver.C:231-444, values in the analysed CSR pattern).  The
+ * values and b go up, x comes back; synchronous.  *status gets the bits of
+ * xg_lu_status (1: zero or non-finite pivot; the caller repivots by
+ * analysing again).  Device staging for the three arrays is allocated on the
+ * first call. */
+int xg_lu_solve_host(xg_lu *lu, const double *host_values, const double *host_b, double *host_x,
+                     int n_refine, int reuse_factors, int *status);
 /* Polls a device wait of this factorisation's refactor and solves makes
  * before it gives up, sets status bit 2 and returns (default 1,048,576, about
  * 0.1-0.5 s).  Every launch ends even when a wait gives up; its results are

@@ -1306,6 +1306,7 @@ struct xg_lu {
   void *d_rdiag = nullptr;                        // n of T: 1 / U(k,k)
   double *d_a = nullptr;                          // FP64 copy of A
   double *d_r = nullptr, *d_dx = nullptr;         // refinement work
+  double *d_hv = nullptr, *d_hb = nullptr, *d_hx = nullptr;  // xg_lu_solve_host staging
   int grid_factor = 0, grid_solve = 0;
   int stage_cap = 0;                       // grid refactor: staged row entries per warp
   size_t smem_grid = 0;                    // its dynamic shared memory
@@ -1354,7 +1355,7 @@ void free_lu(xg_lu *lu) {
   void *ptrs[] = {lu->d_rp, lu->d_ci, lu->d_diag, lu->d_lu2a, lu->d_P, lu->d_Q, lu->d_arp,
                   lu->d_urp, lu->d_upos, lu->d_lvl,
                   lu->d_aci, lu->d_ctrl, lu->d_tdesc, lu->d_hpart, lu->d_val, lu->d_y, lu->d_z, lu->d_rdiag, lu->d_a,
-                  lu->d_r, lu->d_dx};
+                  lu->d_r, lu->d_dx, lu->d_hv, lu->d_hb, lu->d_hx};
   for (void *p : ptrs)
     if (p) cudaFree(p);
 }
@@ -1770,6 +1771,43 @@ extern "C" int xg_lu_solve(xg_lu *lu, const double *dev_b, double *dev_x, int n_
   XG_CU(cudaSetDevice(lu->device));
   return lu->precision == XG_LU_FP32 ? solve_t<float>(lu, dev_b, dev_x, n_refine)
                                      : solve_t<double>(lu, dev_b, dev_x, n_refine);
+}
+
+extern "C" int xg_lu_solve_host(xg_lu *lu, const double *host_values, const double *host_b,
+                                double *host_x, int n_refine, int reuse_factors, int *status) {
+  if (!lu || !host_b || !host_x || !status || n_refine < 0 || (!reuse_factors && !host_values)) {
+    xg::set_error("xg_lu_solve_host: bad argument");
+    return XG_ERR_ARG;
+  }
+  if (reuse_factors && !lu->factored) {
+    xg::set_error("xg_lu_solve_host: no factorisation to reuse");
+    return XG_ERR_STATE;
+  }
+  XG_CU(cudaSetDevice(lu->device));
+  const size_t n = size_t(lu->S.n), nnz = size_t(lu->S.nnz_a);
+  if (!lu->d_hv) {  // staging for host callers, made on first use
+    cudaError_t e;
+    if ((e = cudaMalloc((void **)&lu->d_hv, sizeof(double) * nnz)) ||
+        (e = cudaMalloc((void **)&lu->d_hb, sizeof(double) * n)) ||
+        (e = cudaMalloc((void **)&lu->d_hx, sizeof(double) * n))) {
+      cudaFree(lu->d_hv);
+      cudaFree(lu->d_hb);
+      lu->d_hv = lu->d_hb = lu->d_hx = nullptr;
+      return e == cudaErrorMemoryAllocation
+                 ? (xg::set_error("xg_lu_solve_host: out of device memory"), XG_ERR_OOM)
+                 : cuda_fail(e, "xg_lu_solve_host");
+    }
+  }
+  if (!reuse_factors)
+    XG_CU(cudaMemcpyAsync(lu->d_hv, host_values, sizeof(double) * nnz, cudaMemcpyHostToDevice,
+                          lu->stream));
+  XG_CU(cudaMemcpyAsync(lu->d_hb, host_b, sizeof(double) * n, cudaMemcpyHostToDevice, lu->stream));
+  const int rc = reuse_factors ? xg_lu_solve(lu, lu->d_hb, lu->d_hx, n_refine)
+                               : xg_lu_refactor_solve(lu, lu->d_hv, lu->d_hb, lu->d_hx, n_refine);
+  if (rc) return rc;
+  XG_CU(cudaMemcpyAsync(host_x, lu->d_hx, sizeof(double) * n, cudaMemcpyDeviceToHost, lu->stream));
+  int bad = -1;
+  return xg_lu_status(lu, status, &bad);  // synchronises the stream
 }
 
 namespace xg {
