@@ -216,3 +216,99 @@ def transient(oc, tstop, tstep, out_idx, col_order=None, max_points=200000, maxs
         raise RuntimeError(f"xgo_tran_run failed: {rc} {st.as_dict()}")
     n = npts.value
     return t[:n], v[:n, : idx.size], st.as_dict()
+
+
+# ---- the integrator's formulas (xgo_tran.c), one call each -----------------
+
+def _d(a):
+    return np.ascontiguousarray(a, np.float64)
+
+
+def _tia_lib(L):
+    vp, i, d = C.c_void_p, C.c_int, C.c_double
+    if getattr(L, "_tia_ready", False):
+        return L
+    names = {"update_coeffs": "xgo_tia_update_coeffs", "predictor": "xgo_tia_predictor",
+             "residual": "xgo_tia_residual", "jacobian": "xgo_tia_jacobian",
+             "error_estimate": "xgo_tia_error_estimate", "converged": "xgo_nls_converged"}
+    if not hasattr(L, names["update_coeffs"]):  # the reference's harness uses xref_ names
+        names = {k: v.replace("xgo_tia", "xref_tia").replace("xgo_nls", "xref_nls")
+                 for k, v in names.items()}
+    L._tia = {k: getattr(L, v) for k, v in names.items()}
+    L._tia["update_coeffs"].argtypes = [i, d, d, vp, vp, vp, vp]
+    L._tia["predictor"].argtypes = [i, i, vp, vp, vp, vp, vp, vp, vp]
+    L._tia["residual"].argtypes = [i, i, d, d, i, vp, vp, vp, vp, vp, vp, vp]
+    L._tia["jacobian"].argtypes = [C.c_int64, i, d, d, vp, vp, vp]
+    L._tia_ready = True
+    return L
+
+
+class Integrator:
+    """The integrator's formulas of one library: the oracle's (default) or,
+    given oracle.ref's TIA library, the reference's own compiled code, with
+    the same calls."""
+
+    def __init__(self, L=None):
+        self.L = _tia_lib(L or lib())
+        self.ref = hasattr(self.L, "xref_tia_update_coeffs")
+        t = self.L._tia
+        if self.ref:
+            t["error_estimate"].argtypes = [C.c_int, C.c_double, C.c_int] + [C.c_void_p] * 8
+            t["converged"].argtypes = [C.c_int, C.c_int, C.c_int] + [C.c_double] * 8 + [
+                C.POINTER(C.c_int), C.POINTER(C.c_double)]
+        else:
+            t["error_estimate"].argtypes = [C.c_int, C.c_double, C.c_void_p, C.c_void_p, C.c_double,
+                                            C.c_double]
+            t["converged"].argtypes = [C.c_int, C.c_int, C.c_int] + [C.c_double] * 7 + [
+                C.POINTER(C.c_int), C.POINTER(C.c_double)]
+        t["error_estimate"].restype = C.c_double
+        t["converged"].restype = C.c_int
+
+    def update_coeffs(self, order, h, h_sum, psi):
+        psi = _d(psi).copy()
+        beta = np.zeros(3)
+        a, ck = C.c_double(), C.c_double()
+        self.L._tia["update_coeffs"](order, h, h_sum, _ptr(psi), _ptr(beta), C.byref(a), C.byref(ck))
+        return psi, beta, a.value, ck.value
+
+    def predictor(self, order, beta, xh0, xh1, xh2, qh0):
+        n = len(xh0)
+        ins = [_d(v).copy() for v in (beta, xh0, xh1, xh2, qh0)]
+        xn0, qn0 = np.zeros(n), np.zeros(n)
+        self.L._tia["predictor"](n, order, *[_ptr(v) for v in ins], _ptr(xn0), _ptr(qn0))
+        return xn0, qn0
+
+    def residual(self, order, h, alphas, limiter, Q, qn0, F, qh2, fvp, qvp):
+        n = len(Q)
+        ins = [_d(v).copy() for v in (Q, qn0, F, qh2, fvp, qvp)]
+        rhs = np.zeros(n)
+        self.L._tia["residual"](n, order, h, alphas, int(limiter), *[_ptr(v) for v in ins], _ptr(rhs))
+        return rhs
+
+    def jacobian(self, order, h, alphas, dqdx, dfdx):
+        ins = [_d(v).copy() for v in (dqdx, dfdx)]
+        jac = np.zeros(len(dqdx))
+        self.L._tia["jacobian"](len(dqdx), order, h, alphas, *[_ptr(v) for v in ins], _ptr(jac))
+        return jac
+
+    def error_estimate(self, ck, x_curr, corr, reltol, abstol):
+        n = len(x_curr)
+        if self.ref:
+            ins = [_d(v).copy() for v in (x_curr, corr, np.zeros(n), np.zeros(n),
+                                          np.full(n, reltol), np.full(n, abstol))]
+            wt, qwt = np.zeros(n), np.zeros(n)
+            return self.L._tia["error_estimate"](n, ck, 1, *[_ptr(v) for v in ins], _ptr(wt), _ptr(qwt))
+        a, b = _d(x_curr), _d(corr)
+        return self.L._tia["error_estimate"](n, ck, _ptr(a), _ptr(b), reltol, abstol)
+
+    def converged(self, transient, step, max_step, rhs_tol, dx_tol, small_update, max_rhs, upd,
+                  rhs_rel, rate, count=0, stall_rate=0.0):
+        """(status, count, stall_rate) after one Newton step."""
+        c, r = C.c_int(count), C.c_double(stall_rate)
+        if self.ref:  # wtNormDX / stepLength with a full step
+            s = self.L._tia["converged"](int(transient), step, max_step, rhs_tol, dx_tol, small_update,
+                                         max_rhs, upd, 1.0, rhs_rel, rate, C.byref(c), C.byref(r))
+        else:
+            s = self.L._tia["converged"](int(transient), step, max_step, rhs_tol, dx_tol, small_update,
+                                         max_rhs, upd, rhs_rel, rate, C.byref(c), C.byref(r))
+        return s, c.value, r.value

@@ -13,8 +13,26 @@ LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_ref", "lib
 _lib = None
 
 
+TIA_LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_ref", "libxyceref_tia.so")
+_tia = None
+
+
 def available():
     return os.path.exists(LIB_PATH)
+
+
+def tia_available():
+    return os.path.exists(TIA_LIB_PATH)
+
+
+def integrator():
+    """The reference's own OneStep / DataStore / DampedNewton code
+    (libxyceref_tia.so, xref_tia.C) behind oracle.oracle.Integrator's calls."""
+    global _tia
+    from oracle.oracle import Integrator
+    if _tia is None:
+        _tia = Integrator(C.CDLL(TIA_LIB_PATH))
+    return _tia
 
 
 def lib():

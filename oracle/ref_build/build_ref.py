@@ -87,8 +87,51 @@ def main(argv=None):
     if r.returncode:
         raise RuntimeError("link failed\n" + r.stderr[-6000:])
     print(lib)
+    print(build_tia(a.ref, a.j, incs, flags))
     print(build_ksparse(a.ref, a.j))
     return 0
+
+
+# The reference's time-integration and Newton-convergence sources the
+# transient pin runs (xref_tia.C), and what their objects need to link.
+TIA_SOURCES = ["TimeIntegrationPKG/src/N_TIA_OneStep.C", "TimeIntegrationPKG/src/N_TIA_DataStore.C",
+               "TimeIntegrationPKG/src/N_TIA_StepErrorControl.C",
+               "TimeIntegrationPKG/src/N_TIA_TimeIntegrationMethods.C",
+               "NonlinearSolverPKG/src/N_NLS_DampedNewton.C", "NonlinearSolverPKG/src/N_NLS_NLParams.C",
+               "LoaderServicesPKG/src/N_LOA_Loader.C"]
+
+
+def build_tia(ref, jobs, incs, flags):
+    """oracle/_ref/libxyceref_tia.so: the reference's OneStep integrator, its
+    data store's error norm and DampedNewton's convergence test, driven on
+    plain arrays by xref_tia.C.  The sources are compiled with their symbols
+    hidden and unused sections dropped at the link, so that only what the
+    harness's entry points reach (and the vtables of the objects it builds)
+    has to resolve; the device library supplies the utility and error
+    packages."""
+    objdir = os.path.join(OUT, "tia_obj")
+    os.makedirs(objdir, exist_ok=True)
+    tflags = flags + ["-ffunction-sections", "-fdata-sections", "-fvisibility=hidden"]
+
+    def one(path):
+        obj = os.path.join(objdir, os.path.basename(path)[:-2] + ".o")
+        if os.path.exists(obj) and os.path.getmtime(obj) >= os.path.getmtime(path):
+            return obj
+        r = subprocess.run(tflags + incs + ["-c", path, "-o", obj], capture_output=True, text=True)
+        if r.returncode:
+            raise RuntimeError(f"compile failed: {path}\n{r.stderr[-3000:]}")
+        return obj
+
+    srcs = [os.path.join(ref, "src", s) for s in TIA_SOURCES] + [os.path.join(HERE, "xref_tia.C")]
+    with cf.ThreadPoolExecutor(jobs) as ex:
+        objs = list(ex.map(one, srcs))
+    lib = os.path.join(OUT, "libxyceref_tia.so")
+    r = subprocess.run(["g++", "-shared", "-o", lib] + objs +
+                       ["-L" + OUT, "-lxyceref", "-Wl,-rpath,$ORIGIN", "-Wl,--gc-sections",
+                        "-Wl,--no-undefined", "-ldl"], capture_output=True, text=True)
+    if r.returncode:
+        raise RuntimeError("TIA link failed\n" + r.stderr[-6000:])
+    return lib
 
 
 def build_ksparse(ref, jobs):

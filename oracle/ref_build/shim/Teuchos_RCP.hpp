@@ -8,6 +8,8 @@ template <class T> class RCP {
  public:
   RCP() {}
   RCP(T* p) : p_(p) {}
+  template <class U> RCP(const RCP<U>& o) : p_(o.shared()) {}
+  const std::shared_ptr<T>& shared() const { return p_; }
   T* get() const { return p_.get(); }
   T* operator->() const { return p_.get(); }
   T& operator*() const { return *p_; }

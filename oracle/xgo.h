@@ -86,6 +86,22 @@ int xgo_tran_run(xgo_circuit *c, const xgo_tran_opts *o, double *t_out, double *
 /* Minimum-degree column order of the n x n CSR pattern (xgo_order.c):
  * order[k] = the k-th pivot column. */
 int xgo_min_degree(int n, const int *rowptr, const int *col, int *order);
+/* The integrator's formulas the transient driver applies (xgo_tran.c; each
+ * held by the tests to the reference's own compiled code). */
+void xgo_tia_update_coeffs(int order, double h, double h_sum, double *psi, double *beta,
+                           double *alphas, double *ck);
+void xgo_tia_predictor(int n, int order, const double *beta, const double *xh0, const double *xh1,
+                       const double *xh2, const double *qh0, double *xn0, double *qn0);
+void xgo_tia_residual(int n, int order, double h, double alphas, int limiter, const double *Q,
+                      const double *qn0, const double *F, const double *qh2, const double *fvp,
+                      const double *qvp, double *rhs);
+void xgo_tia_jacobian(int64_t nnz, int order, double h, double alphas, const double *dqdx,
+                      const double *dfdx, double *jac);
+double xgo_tia_error_estimate(int n, double ck, const double *x_curr, const double *corr,
+                              double reltol, double abstol);
+int xgo_nls_converged(int transient, int step, int max_step, double rhs_tol, double dx_tol,
+                      double small_update, double max_rhs, double upd, double rhs_rel, double rate,
+                      int *count, double *stall_rate);
 /* x = A^-1 b with the driver's sparse LU (CSR A, column order or NULL). */
 int xgo_sparse_solve(int n, const int *rowptr, const int *col, const double *val,
                      const int *col_order, const double *b, double *x);

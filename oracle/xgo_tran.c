@@ -241,6 +241,120 @@ static double wrms(const double *v, const double *w, int n) {
   return sqrt(s / n);
 }
 
+/* ---- the integrator's formulas, one function each, exported so that the
+ * tests hold them to the reference's own compiled code ------------------ */
+
+/* OneStep::updateCoeffs (N_TIA_OneStep.C:1355-1480): the step history psi,
+ * the predictor coefficients beta, the leading coefficient alphas and the
+ * error constant ck of a trapezoid (order 2) or backward-Euler step. */
+void xgo_tia_update_coeffs(int order, double h, double h_sum, double *psi, double *beta,
+                           double *alphas, double *ck) {
+  if (order == 2) psi[2] = psi[1];
+  psi[1] = psi[0];
+  psi[0] = h;
+  beta[0] = 1.0;
+  *alphas = -1.0;
+  if (order == 2) {
+    double r = h / psi[1];
+    beta[1] = r + r * r / 2;
+    beta[2] = -1.0 * h * h / psi[1] / psi[2] / 2;
+    *ck = (h / h_sum) / 3.0;
+  } else {
+    beta[1] = h / psi[1];
+    *ck = h / h_sum;
+  }
+}
+
+/* OneStep::obtainPredictor (N_TIA_OneStep.C:115-205): xn0 = xh0 +
+ * beta_1 xh1 (+ beta_2 xh2 at order 2), qn0 = qh0. */
+void xgo_tia_predictor(int n, int order, const double *beta, const double *xh0, const double *xh1,
+                       const double *xh2, const double *qh0, double *xn0, double *qn0) {
+  for (int i = 0; i < n; ++i) {
+    double x = xh0[i];
+    x = beta[1] * xh1[i] + x;
+    if (order == 2) x = beta[2] * xh2[i] + x;
+    xn0[i] = x;
+    qn0[i] = qh0[i];
+  }
+}
+
+/* OneStep::obtainResidual (N_TIA_OneStep.C:215-290): the Newton right-hand
+ * side -[(Q - qn0)/h + f F + f qh2] + (-alphas/h) dQdxdVp + f dFdxdVp, with
+ * f = 1/2 at order 2 (the qh2 term then) and 1 at order 1; the limiter terms
+ * only when limiting changed a junction voltage.  alphas = -1. */
+void xgo_tia_residual(int n, int order, double h, double alphas, int limiter, const double *Q,
+                      const double *qn0, const double *F, const double *qh2, const double *fvp,
+                      const double *qvp, double *rhs) {
+  const double fs = order == 2 ? 0.5 : 1.0, qs = -alphas / h;
+  for (int i = 0; i < n; ++i) {
+    double r = 1.0 * Q[i] + -1.0 * qn0[i];
+    r = order == 2 ? (1.0 / h) * r + 0.5 * F[i] : (1.0 / h) * r + 1.0 * F[i];
+    if (order == 2) r = 1.0 * r + 0.5 * qh2[i];
+    r = -1.0 * r;
+    if (limiter) {
+      r = 1.0 * r + 1.0 * (qs * qvp[i]);
+      r = 1.0 * r + fs * fvp[i];
+    }
+    rhs[i] = r;
+  }
+}
+
+/* OneStep::obtainJacobian (N_TIA_OneStep.C:297-352): J = (-alphas/h) dQdx +
+ * f dFdx over the matrix values. */
+void xgo_tia_jacobian(int64_t nnz, int order, double h, double alphas, const double *dqdx,
+                      const double *dfdx, double *jac) {
+  const double qs = -alphas / h, fs = order == 2 ? 0.5 : 1.0;
+  for (int64_t p = 0; p < nnz; ++p) jac[p] = qs * dqdx[p] + fs * dfdx[p];
+}
+
+/* computeErrorEstimate = ck * WRMS_errorNorm (N_TIA_OneStep.h:97), with the
+ * weights of DataStore::setErrorWtVector (N_TIA_DataStore.C:1200-1370;
+ * newLte, every unknown treated as a voltage): reltol |x_curr|_inf + abstol,
+ * and the norm sqrt(sum((corr_i / w)^2) / n) of the Newton correction
+ * corr = x - predictor (N_TIA_DataStore.C:1380-1400). */
+double xgo_tia_error_estimate(int n, double ck, const double *x_curr, const double *corr,
+                              double reltol, double abstol) {
+  double xmax = 0.0;
+  for (int i = 0; i < n; ++i) xmax = fabs(x_curr[i]) > xmax ? fabs(x_curr[i]) : xmax;
+  const double wt = reltol * xmax + abstol;
+  double s2 = 0.0;
+  for (int i = 0; i < n; ++i) {
+    const double e = corr[i] / wt;
+    s2 += e * e;
+  }
+  return ck * sqrt(s2 / n);
+}
+
+/* Damped Newton convergence test, N_NLS_DampedNewton.C:1787-1919: the
+ * status of a Newton step (1, 2, 3, 4: converged; -1, -2, -3: failed; 0:
+ * go on) from the residual's max norm, the weighted norm of the update, the
+ * residual's reduction and its rate.  *count / *stall_rate carry the stall
+ * counter from one step to the next.  small_update: the solver's
+ * smallUpdateTol (1e-6). */
+int xgo_nls_converged(int transient, int step, int max_step, double rhs_tol, double dx_tol,
+                      double small_update, double max_rhs, double upd, double rhs_rel, double rate,
+                      int *count, double *stall_rate) {
+  const double eps = DBL_EPSILON, rate_max = 0.5 * DBL_MAX, min_red = 0.9, stag = 1e-3;
+  if (max_rhs <= eps && max_rhs <= rhs_tol) return 1;
+  if (max_rhs <= rhs_tol && upd <= dx_tol) return 2;
+  if (step > max_step && transient)
+    if (rhs_rel <= min_red && rate <= 1.0) return 3;
+  if (upd <= small_update) return 4;
+  if (step > max_step) return -1;
+  else if (rate > rate_max) return -2;
+  if (transient && fabs(rate - 1.0) <= stag) {
+    if (*count == 0 || rate < *stall_rate) *stall_rate = rate;
+    (*count)++;
+  } else {
+    *count = 0;
+  }
+  if (transient && *count == 5) {
+    *count = 0;
+    return (rhs_rel < min_red && *stall_rate <= 1.0) ? 3 : -3;
+  }
+  return 0;
+}
+
 static int do_load(tctx *T, const xg_load_flags *fl) {
   const double *in[9] = {T->sol[0], T->sol[1], T->sol[2], T->sta[0], T->sta[1], T->sta[2],
                          T->sto[0], T->sto[1], T->sto[2]};
@@ -256,29 +370,10 @@ static int do_load(tctx *T, const xg_load_flags *fl) {
   return rc;
 }
 
-/* Damped Newton convergence test, N_NLS_DampedNewton.C:1787-1919. */
 static int converged(tctx *T, int transient, int step, int max_step, double rhs_tol, double dx_tol,
                      double max_rhs, double upd, double rhs_rel, double rate) {
-  const double eps = DBL_EPSILON, rate_max = 0.5 * DBL_MAX, min_red = 0.9, stag = 1e-3;
-  const double small_update = 1e-6;
-  if (max_rhs <= eps && max_rhs <= rhs_tol) return 1;
-  if (max_rhs <= rhs_tol && upd <= dx_tol) return 2;
-  if (step > max_step && transient)
-    if (rhs_rel <= min_red && rate <= 1.0) return 3;
-  if (upd <= small_update) return 4;
-  if (step > max_step) return -1;
-  else if (rate > rate_max) return -2;
-  if (transient && fabs(rate - 1.0) <= stag) {
-    if (T->stall_count == 0 || rate < T->stall_rate) T->stall_rate = rate;
-    T->stall_count++;
-  } else {
-    T->stall_count = 0;
-  }
-  if (transient && T->stall_count == 5) {
-    T->stall_count = 0;
-    return (rhs_rel < min_red && T->stall_rate <= 1.0) ? 3 : -3;
-  }
-  return 0;
+  return xgo_nls_converged(transient, step, max_step, rhs_tol, dx_tol, 1e-6, max_rhs, upd, rhs_rel,
+                           rate, &T->stall_count, &T->stall_rate);
 }
 
 /* One Newton solve.  transient: trapezoid/BE residual with step h and order;
@@ -303,14 +398,8 @@ static int newton(tctx *T, int transient, double h, int order, double time, int 
 #define RESIDUAL()                                                                        \
   do {                                                                                    \
     if (transient) {                                                                      \
-      for (int i = 0; i < n; ++i) {                                                       \
-        double r = (T->q[i] - T->qn0[i]) * (1.0 / h);                                     \
-        r = order == 2 ? r + 0.5 * T->f[i] + 0.5 * T->qh2[i] : r + T->f[i];               \
-        r = -r;                                                                           \
-        r += T->qvp[i] * (1.0 / h);                                                       \
-        r += fs * T->fvp[i];                                                              \
-        T->rhs[i] = r;                                                                    \
-      }                                                                                   \
+      xgo_tia_residual(n, order, h, -1.0, 1, T->q, T->qn0, T->f, T->qh2, T->fvp, T->qvp,  \
+                       T->rhs);                                                           \
     } else {                                                                              \
       for (int i = 0; i < n; ++i) T->rhs[i] = -T->f[i] + T->fvp[i];                       \
       if (T->gshunt > 0)                                                                  \
@@ -333,8 +422,11 @@ static int newton(tctx *T, int transient, double h, int order, double time, int 
   int status = 0, step = 0;
   while (status == 0) {
     ++step;
-    const double qs = transient ? 1.0 / h : 1.0e-20;
-    for (int64_t p = 0; p < T->nnz; ++p) T->jac[p] = qs * T->dqdx[p] + fs * T->dfdx[p];
+    if (transient) {
+      xgo_tia_jacobian(T->nnz, order, h, -1.0, T->dqdx, T->dfdx, T->jac);
+    } else {
+      for (int64_t p = 0; p < T->nnz; ++p) T->jac[p] = 1.0e-20 * T->dqdx[p] + fs * T->dfdx[p];
+    }
     if (!transient && T->gshunt > 0)
       for (int i = 0; i < T->c->n_nodes; ++i)
         if (T->diag[i] >= 0) T->jac[T->diag[i]] += T->gshunt;
@@ -528,28 +620,9 @@ int xgo_tran_run(xgo_circuit *c, const xgo_tran_opts *o, double *t_out, double *
         order = 1;
         psi[0] = h;
       }
-      /* updateCoeffs */
-      if (order == 2) psi[2] = psi[1];
-      psi[1] = psi[0];
-      psi[0] = h;
-      beta[0] = 1.0;
-      if (order == 2) {
-        double r = h / psi[1];
-        beta[1] = r + r * r / 2;
-        beta[2] = -1.0 * h * h / psi[1] / psi[2] / 2;
-        ck = (h / h_sum) / 3.0;
-      } else {
-        beta[1] = h / psi[1];
-        ck = h / h_sum;
-      }
-      /* predictor */
-      for (int i = 0; i < n; ++i) {
-        double x = T.xh0[i];
-        x = beta[1] * T.xh1[i] + x;
-        if (order == 2) x = beta[2] * T.xh2[i] + x;
-        T.xn0[i] = x;
-        T.qn0[i] = T.qh0[i];
-      }
+      double alphas;
+      xgo_tia_update_coeffs(order, h, h_sum, psi, beta, &alphas, &ck);
+      xgo_tia_predictor(n, order, beta, T.xh0, T.xh1, T.xh2, T.qh0, T.xn0, T.qn0);
       memcpy(T.sol[0], T.xn0, sizeof(double) * n);
       memcpy(T.sta[0], T.sta[1], sizeof(double) * T.nsta);
       memcpy(T.sto[0], T.sto[1], sizeof(double) * T.nsto);
@@ -562,10 +635,8 @@ int xgo_tran_run(xgo_circuit *c, const xgo_tran_opts *o, double *t_out, double *
       int ok = ns >= 0;
       double est = 0.0;
       if (ok && st->steps >= 1 && !beginning) {
-        double xmax = inf_norm(T.sol[1], n);
-        double wt = reltol * xmax + abstol, s2 = 0;
-        for (int i = 0; i < n; ++i) { double e = (T.sol[0][i] - T.xn0[i]) / wt; s2 += e * e; }
-        est = ck * sqrt(s2 / n);
+        for (int i = 0; i < n; ++i) T.dx[i] = T.sol[0][i] - T.xn0[i];  /* the Newton correction */
+        est = xgo_tia_error_estimate(n, ck, T.sol[1], T.dx, reltol, abstol);
         ok = est <= 1.0;
         if (debug) fprintf(stderr, "   est=%.3e ck=%.3e\n", est, ck);
       }
