@@ -239,6 +239,11 @@ def _tia_lib(L):
     L._tia["predictor"].argtypes = [i, i, vp, vp, vp, vp, vp, vp, vp]
     L._tia["residual"].argtypes = [i, i, d, d, i, vp, vp, vp, vp, vp, vp, vp]
     L._tia["jacobian"].argtypes = [C.c_int64, i, d, d, vp, vp, vp]
+    pre = "xref_tia_" if hasattr(L, "xref_tia_update_coeffs") else "xgo_tia_"
+    L._tia["complete_step"] = getattr(L, pre + "complete_step")
+    L._tia["complete_step"].argtypes = [i, vp, vp, vp, vp, vp, vp]
+    L._tia["reject_step"] = getattr(L, pre + "reject_step")
+    L._tia["reject_step"].argtypes = [vp, vp]
     L._tia_ready = True
     return L
 
@@ -312,3 +317,24 @@ class Integrator:
             s = self.L._tia["converged"](int(transient), step, max_step, rhs_tol, dx_tol, small_update,
                                          max_rhs, upd, rhs_rel, rate, C.byref(c), C.byref(r))
         return s, c.value, r.value
+
+    # step control: state = [order, steps, failures, estOverTol, h, t, t_next,
+    # stop time, min step, max step, last step, h_sum, psi0, psi1, psi2,
+    # Newton status, saved step]; result = [order, steps, failures, h, t,
+    # t_next, last step, h_sum, saved step, psi0, psi1, psi2]
+    def complete_step(self, state, hist, x_next, Q, F):
+        """OneStep::completeStep: the result, and the six history vectors
+        (solution 0..2, charge 0..2) rotated."""
+        st = _d(state).copy()
+        hs = [_d(v).copy() for v in hist]
+        arr = (C.c_void_p * 6)(*[v.ctypes.data for v in hs])
+        ins = [_d(v).copy() for v in (x_next, Q, F)]
+        out = np.zeros(12)
+        self.L._tia["complete_step"](len(x_next), _ptr(st), arr, *[_ptr(v) for v in ins], _ptr(out))
+        return out, hs
+
+    def reject_step(self, state):
+        st = _d(state).copy()
+        out = np.zeros(12)
+        self.L._tia["reject_step"](_ptr(st), _ptr(out))
+        return out

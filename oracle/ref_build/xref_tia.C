@@ -425,3 +425,111 @@ XREF_API int xref_nls_converged(int transient, int step, int max_step, double rh
   *tmp_rate = s.tmpConvRate;
   return r;
 }
+
+namespace {
+// History vectors of one integrator, bound to caller arrays: hist[0..2] the
+// solution history, hist[3..5] the charge history; the state and store
+// histories the reference also rotates are bound to scratch.
+struct History {
+  Vec x[3], q[3], sto[3], stoqc[3], s0, scratch[4];
+  std::vector<double> tmp;
+  void bind(N_TIA_DataStore &ds, int n, double *const *hist) {
+    tmp.assign(12 * (size_t(n) + 1), 0.0);
+    double *t = tmp.data();
+    ds.xHistory = {x[0].bind(hist[0], n), x[1].bind(hist[1], n), x[2].bind(hist[2], n)};
+    ds.qHistory = {q[0].bind(hist[3], n), q[1].bind(hist[4], n), q[2].bind(hist[5], n)};
+    for (int k = 0; k < 3; ++k) {
+      sto[k].bind(t + (2 * k) * (n + 1), n);
+      stoqc[k].bind(t + (2 * k + 1) * (n + 1), n);
+    }
+    ds.stoHistory = {sto[0].obj.get(), sto[1].obj.get(), sto[2].obj.get()};
+    ds.stoLeadCurrQCompHistory = {stoqc[0].obj.get(), stoqc[1].obj.get(), stoqc[2].obj.get()};
+    ds.sHistory = {s0.bind(t + 6 * (n + 1), n)};
+    for (int k = 0; k < 4; ++k) scratch[k].bind(t + (7 + k) * (n + 1), n);
+    ds.nextStorePtr = scratch[0].obj.get();
+    ds.nextStoreLeadCurrQCompPtr = scratch[1].obj.get();
+    ds.nextStatePtr = scratch[2].obj.get();
+  }
+};
+
+void step_control_setup(Integrator &I, const double *in) {
+  N_TIA_TIAParams &tp = *I.params.get();
+  N_TIA_StepErrorControl &sec = *I.sec.get();
+  tp.errorAnalysisOption = 0;
+  tp.constantStepSize = false;
+  sec.tolAimFac_ = 0.5;
+  sec.r_factor_ = 1.0;  // the build without Xyce_USE_Q_NORM (N_TIA_StepErrorControl.C:164-168)
+  sec.r_safety_ = 2.0;
+  sec.r_fudge_ = 0.0001;
+  sec.r_min_ = 0.25;
+  sec.r_max_ = 0.9;
+  sec.r_hincr_test_ = 2.0;
+  sec.r_hincr_ = 2.0;
+  sec.max_LET_fail_ = 15;
+  sec.newOrder_ = 1;
+  sec.currentOrder_ = int(in[0]);
+  sec.usedOrder_ = int(in[0]);
+  sec.numberOfSteps_ = int(in[1]);
+  sec.nef_ = int(in[2]);
+  sec.estOverTol_ = in[3];
+  sec.currentTimeStep = in[4];
+  sec.currentTime = in[5];
+  sec.nextTime = in[6];
+  sec.stopTime = in[7];
+  sec.minTimeStep = in[8];
+  sec.maxTimeStep = in[9];
+  sec.lastTimeStep = in[10];
+  sec.currentTimeStepSum = in[11];
+  for (int k = 0; k < 3; ++k) sec.psi_[k] = in[12 + k];
+  sec.newtonConvergenceStatus = int(in[15]);
+  sec.savedTimeStep = in[16];
+}
+
+void step_control_result(Integrator &I, double *out) {
+  const N_TIA_StepErrorControl &sec = *I.sec.get();
+  out[0] = sec.currentOrder_;
+  out[1] = sec.numberOfSteps_;
+  out[2] = sec.nef_;
+  out[3] = sec.currentTimeStep;
+  out[4] = sec.currentTime;
+  out[5] = sec.nextTime;
+  out[6] = sec.lastTimeStep;
+  out[7] = sec.currentTimeStepSum;
+  out[8] = sec.savedTimeStep;
+  for (int k = 0; k < 3; ++k) out[9 + k] = sec.psi_[k];
+}
+}  // namespace
+
+// OneStep::completeStep (N_TIA_OneStep.C:1945-2190) after an accepted step:
+// the next order and step, the time advanced and the solution and charge
+// histories rotated (updateHistory, :1209-1300).  in[17]: order,
+// steps taken, error-test failures, estOverTol, h, t, t_next, stop time,
+// min step, max step, last step, h_sum, psi[3], Newton status, saved step.
+// hist[6]: x history 0..2 then Q history 0..2 (n each, updated in place);
+// x_next, Q, F: the accepted point.  out[12]: order, steps, failures, h,
+// t, t_next, last step, h_sum, saved step, psi[3].
+XREF_API void xref_tia_complete_step(int n, const double *in, double *const *hist, double *x_next,
+                                     double *Q, double *F, double *out) {
+  Integrator I;
+  N_TIA_DataStore &ds = *I.ds.get();
+  step_control_setup(I, in);
+  History H;
+  H.bind(ds, n, hist);
+  Vec vx, vq, vf;
+  ds.nextSolutionPtr = vx.bind(x_next, n);
+  ds.daeQVectorPtr = vq.bind(Q, n);
+  ds.daeFVectorPtr = vf.bind(F, n);
+  I.method->N_TIA_OneStep::completeStep();
+  step_control_result(I, out);
+}
+
+// OneStep::rejectStep (N_TIA_OneStep.C:1695-1930) after a failed step (a
+// Newton failure when the Newton status is <= 0, else the local error
+// test): the retry's order and step.  in / out as xref_tia_complete_step.
+XREF_API void xref_tia_reject_step(const double *in, double *out) {
+  Integrator I;
+  step_control_setup(I, in);
+  I.sec.get()->stepAttemptStatus = false;
+  I.method->N_TIA_OneStep::rejectStep();
+  step_control_result(I, out);
+}

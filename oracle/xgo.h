@@ -102,6 +102,9 @@ double xgo_tia_error_estimate(int n, double ck, const double *x_curr, const doub
 int xgo_nls_converged(int transient, int step, int max_step, double rhs_tol, double dx_tol,
                       double small_update, double max_rhs, double upd, double rhs_rel, double rate,
                       int *count, double *stall_rate);
+void xgo_tia_complete_step(int n, const double *in, double *const *hist, const double *x_next,
+                           const double *Q, const double *F, double *out);
+void xgo_tia_reject_step(const double *in, double *out);
 /* x = A^-1 b with the driver's sparse LU (CSR A, column order or NULL). */
 int xgo_sparse_solve(int n, const int *rowptr, const int *col, const double *val,
                      const int *col_order, const double *b, double *x);

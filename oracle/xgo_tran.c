@@ -355,6 +355,118 @@ int xgo_nls_converged(int transient, int step, int max_step, double rhs_tol, dou
   return 0;
 }
 
+/* Step control after an accepted step: OneStep::completeStep
+ * (N_TIA_OneStep.C:1945-2190) with the history update (updateHistory,
+ * :1209-1300).  in[17]: order, steps taken, error-test failures, estOverTol,
+ * h, t, t_next, stop time, min step, max step, last step, h_sum, psi[3],
+ * Newton status, saved step.  hist: the solution history 0..2 then the
+ * charge history 0..2 (n each, rotated in place); x_next, Q, F: the accepted
+ * point.  out[12]: order, steps, failures, h, t, t_next, last step, h_sum,
+ * saved step, psi[3]. */
+void xgo_tia_complete_step(int n, const double *in, double *const *hist, const double *x_next,
+                           const double *Q, const double *F, double *out) {
+  const double tol_aim = 0.5, r_min = 0.25, r_max = 0.9, r_hincr_test = 2.0, r_hincr = 2.0;
+  int order = (int)in[0], n_steps = (int)in[1] + 1;
+  const double est = in[3], h = in[4], t = in[6], stop_time = in[7], min_step = in[8];
+  const double max_step = in[9];
+  double next_time = in[6], h_sum = in[11], saved = in[16];
+  double hn = h, rr = pow(tol_aim / (est + 0.0001), 1.0 / (order + 1.0));
+  if (n_steps >= 2 && order == 1) {
+    order = 2;
+    rr = pow(tol_aim / (est + 0.0001), 1.0 / (order + 1.0));
+    if (rr <= 1.05) order = 1;
+  }
+  if (rr >= r_hincr_test) {
+    rr = r_hincr;
+    hn = rr * h;
+  } else if (rr <= 1) {
+    rr = fmax(r_min, fmin(r_max, rr));
+    hn = rr * h;
+  }
+  /* updateHistory, with the order chosen for the next step: a trapezoid
+   * step keeps F of the accepted point */
+  double *xh0 = hist[0], *xh1 = hist[1], *xh2 = hist[2], *qh0 = hist[3], *qh1 = hist[4], *qh2 = hist[5];
+  if (order == 2) {
+    memcpy(xh2, xh1, sizeof(double) * n);
+    memcpy(qh2, F, sizeof(double) * n);
+  }
+  for (int i = 0; i < n; ++i) {
+    xh1[i] = 1.0 * x_next[i] + -1.0 * xh0[i];
+    qh1[i] = 1.0 * Q[i] + -1.0 * qh0[i];
+  }
+  memcpy(xh0, x_next, sizeof(double) * n);
+  memcpy(qh0, Q, sizeof(double) * n);
+  hn = fmax(hn, min_step);
+  hn = fmin(hn, max_step);
+  if (stop_time - t >= min_step) {
+    double next_pt = t + hn;
+    if (next_pt > stop_time) {
+      saved = hn;
+      next_pt = stop_time;
+      hn = stop_time - t;
+    }
+    next_time = next_pt;
+    h_sum = hn + h;
+  }
+  out[0] = order;
+  out[1] = n_steps;
+  out[2] = 0;
+  out[3] = hn;
+  out[4] = t;
+  out[5] = next_time;
+  out[6] = h;
+  out[7] = h_sum;
+  out[8] = saved;
+  for (int k = 0; k < 3; ++k) out[9 + k] = in[12 + k];
+}
+
+/* Step control after a failed step: OneStep::rejectStep
+ * (N_TIA_OneStep.C:1695-1930), in the reference's default build (no
+ * Xyce_USE_Q_NORM: r_factor 1, r_safety 2, r_fudge 1e-4, and newOrder 1,
+ * which the one-step method never changes, N_TIA_StepErrorControl.C:155-176).
+ * A Newton failure retries an eighth of the step, a first local-error
+ * failure r = (2 (est + 1e-4))^(-1/2) clamped to [0.25, 0.9], a later one a
+ * quarter; each at order 1.  in / out as xgo_tia_complete_step. */
+void xgo_tia_reject_step(const double *in, double *out) {
+  const double r_min = 0.25, r_max = 0.9, r_factor = 1.0, r_safety = 2.0, r_fudge = 0.0001;
+  const int new_order = 1;
+  int order = (int)in[0], nef = (int)in[2] + 1;
+  const double est = in[3], h = in[4], t = in[5], stop_time = in[7], min_step = in[8];
+  const double max_step = in[9], h_last = in[10];
+  double psi[3] = {in[12], in[13], in[14]};
+  for (int i = 1; i <= order; ++i) psi[i - 1] = psi[i]; /* restoreHistory */
+  double hn = h;
+  if (in[15] <= 0) {
+    hn = h / 8;
+    order = 1;
+  } else if (nef == 1) {
+    double rr = r_factor * pow(r_safety * (est + r_fudge), -1.0 / (new_order + 1.0));
+    rr = fmax(r_min, fmin(r_max, rr));
+    hn = rr * h;
+    order = 1;
+  } else {
+    hn = r_min * h;
+    order = 1;
+  }
+  hn = fmax(hn, min_step);
+  hn = fmin(hn, max_step);
+  double next_pt = t + hn;
+  if (next_pt > stop_time) {
+    next_pt = stop_time;
+    hn = stop_time - t;
+  }
+  out[0] = order;
+  out[1] = in[1];
+  out[2] = nef;
+  out[3] = hn;
+  out[4] = t;
+  out[5] = next_pt;
+  out[6] = h_last;
+  out[7] = hn + h_last;
+  out[8] = in[16];
+  for (int k = 0; k < 3; ++k) out[9 + k] = psi[k];
+}
+
 static int do_load(tctx *T, const xg_load_flags *fl) {
   const double *in[9] = {T->sol[0], T->sol[1], T->sol[2], T->sta[0], T->sta[1], T->sta[2],
                          T->sto[0], T->sto[1], T->sto[2]};
@@ -588,7 +700,6 @@ int xgo_tran_run(xgo_circuit *c, const xgo_tran_opts *o, double *t_out, double *
   {
     const double tstop = o->tstop, reltol = o->reltol, abstol = o->abstol;
     const double max_step = o->maxstep > 0 ? o->maxstep : 0.1 * tstop;
-    const double tol_aim = 0.5, r_min = 0.25, r_max = 0.9, r_hincr_test = 2.0, r_hincr = 2.0;
     const double h0_max_factor = 0.005;
     const double starting = o->tstep > 0 ? o->tstep : 1e-10;
     double t = 0.0, h = starting, h_last = starting, h_sum = 2 * starting, saved = 1e-10;
@@ -641,47 +752,25 @@ int xgo_tran_run(xgo_circuit *c, const xgo_tran_opts *o, double *t_out, double *
         if (debug) fprintf(stderr, "   est=%.3e ck=%.3e\n", est, ck);
       }
       if (ok) {
-        /* completeStep */
+        /* completeStep, with the minimum step from machine precision at the
+         * new time (StepErrorControl::updateMinTimeStep) */
         first_step = 0;
-        n_steps++;
-        nef = 0;
-        t = next_time;
-        double hn = h, rr = 1.0;
-        h_last = h;
-        rr = pow(tol_aim / (est + 0.0001), 1.0 / (order + 1.0));
-        if (n_steps >= 2 && order == 1) {
-          order = 2;
-          rr = pow(tol_aim / (est + 0.0001), 1.0 / (order + 1.0));
-          if (rr <= 1.05) order = 1;
-        }
-        if (rr >= r_hincr_test) { rr = r_hincr; hn = rr * h; }
-        else if (rr <= 1) { rr = fmax(r_min, fmin(r_max, rr)); hn = rr * h; }
-        /* updateHistory, with the order chosen for the next step: a
-         * trapezoid step keeps F of the accepted point */
         st->steps++;
-        if (order == 2) {
-          memcpy(T.xh2, T.xh1, sizeof(double) * n);
-          memcpy(T.qh2, T.f, sizeof(double) * n);
-        }
-        for (int i = 0; i < n; ++i) {
-          T.xh1[i] = T.sol[0][i] - T.xh0[i];
-          T.qh1[i] = T.q[i] - T.qh0[i];
-        }
-        memcpy(T.xh0, T.sol[0], sizeof(double) * n);
-        memcpy(T.qh0, T.q, sizeof(double) * n);
-        /* minimum step from machine precision (StepErrorControl::updateMinTimeStep) */
-        const double min_step = t * 10.0 * DBL_EPSILON;
-        hn = fmax(hn, min_step);
-        hn = fmin(hn, max_step);
-        if (stop_time - t >= min_step) {
-          if (t + hn > stop_time) {
-            saved = hn;
-            hn = stop_time - t;
-          }
-          next_time = t + hn;
-          h_sum = hn + h_last;
-        }
-        h = hn;
+        double in[17] = {order, n_steps, nef, est, h, t, next_time, stop_time,
+                         next_time * 10.0 * DBL_EPSILON, max_step, h_last, h_sum, psi[0], psi[1],
+                         psi[2], ns, saved};
+        double out[12];
+        double *hist[6] = {T.xh0, T.xh1, T.xh2, T.qh0, T.qh1, T.qh2};
+        xgo_tia_complete_step(n, in, hist, T.sol[0], T.q, T.f, out);
+        order = (int)out[0];
+        n_steps = (int)out[1];
+        nef = (int)out[2];
+        h = out[3];
+        t = out[4];
+        next_time = out[5];
+        h_last = out[6];
+        h_sum = out[7];
+        saved = out[8];
         /* rotate the accepted point into current / last */
         memcpy(T.sol[2], T.sol[1], sizeof(double) * nr);
         memcpy(T.sol[1], T.sol[0], sizeof(double) * nr);
@@ -696,28 +785,18 @@ int xgo_tran_run(xgo_circuit *c, const xgo_tran_opts *o, double *t_out, double *
         /* rejectStep */
         st->rejected++;
         accepted_last = 0;
-        nef++;
-        for (int i = 1; i <= order; ++i) psi[i - 1] = psi[i];
-        if (nef >= 15) { rc = -2; st->status = -7; goto done; }
-        double hn;
-        if (ns <= 0) {
-          hn = h / 8;
-          order = 1;
-        } else if (nef == 1) {
-          double rr = pow(tol_aim / (est + 0.0001), 1.0 / (order + 1.0));
-          rr = fmax(r_min, fmin(r_max, rr));
-          hn = rr * h;
-          order = 1;
-        } else {
-          hn = r_min * h;
-          order = 1;
-        }
-        hn = fmax(hn, t * 10.0 * DBL_EPSILON);
-        hn = fmin(hn, max_step);
-        if (t + hn > stop_time) hn = stop_time - t;
-        next_time = t + hn;
-        h_sum = hn + h_last;
-        h = hn;
+        if (nef + 1 >= 15) { rc = -2; st->status = -7; goto done; }
+        double in[17] = {order, n_steps, nef, est, h, t, next_time, stop_time,
+                         t * 10.0 * DBL_EPSILON, max_step, h_last, h_sum, psi[0], psi[1], psi[2],
+                         ns, saved};
+        double out[12];
+        xgo_tia_reject_step(in, out);
+        order = (int)out[0];
+        nef = (int)out[2];
+        h = out[3];
+        next_time = out[5];
+        h_sum = out[7];
+        for (int k = 0; k < 3; ++k) psi[k] = out[9 + k];
         if (h < 1e-21) { rc = -3; st->status = -8; goto done; }
       }
     }

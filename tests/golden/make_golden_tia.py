@@ -10,7 +10,8 @@ are those of the circuit's transient loads in the device fixtures
 (inverter_chain_24.npz, ring_7.npz, made by the reference's own device code).
 Per step it stores the inputs and the reference's updateCoeffs, predictor,
 residual, Jacobian and error estimate; then a table of Newton convergence
-decisions over every branch of DampedNewton::converged_.  Needs the
+decisions over every branch of DampedNewton::converged_, and one of the step
+control after accepted and failed steps (completeStep, rejectStep).  Needs the
 reference source tree; the tests only read the .npz.
 
     python tests/golden/make_golden_tia.py
@@ -103,6 +104,42 @@ def convergence_table(rng):
     return {"conv.inputs": np.array(rows, float), "conv.outputs": np.array(res, float)}
 
 
+def step_control_table(rng):
+    """completeStep / rejectStep over accepted and failed steps: estimates
+    around the acceptance bound, first and later failures, Newton failures,
+    orders 1 and 2, steps clipped at a breakpoint and bounded by the min and
+    max step; the histories of the accepted ones are random vectors."""
+    R = ref.integrator()
+    out = {}
+    acc_in, acc_out, rej_in, rej_out = [], [], [], []
+    n = 5
+    for k in range(120):
+        order = int(rng.integers(1, 3))
+        steps = int(rng.integers(0, 6))
+        h = 10 ** rng.uniform(-13, -10)
+        t = rng.uniform(0, 5e-9)
+        stop = t + h * (rng.choice([0.5, 1.0, 3.0, 50.0]) + rng.uniform(0, 1))
+        state = [order, steps, int(rng.integers(0, 3)), 10 ** rng.uniform(-4, 1), h, t, t + h,
+                 stop, t * 10 * 2.220446049250313e-16, rng.choice([1e-12, 1e-10, 1e-9]),
+                 h * rng.uniform(0.3, 3), h * rng.uniform(1.5, 4),
+                 h, h * rng.uniform(0.5, 2), h * rng.uniform(0.5, 2), int(rng.choice([-1, 0, 2])),
+                 h * 2]
+        hist = [rng.standard_normal(n) for _ in range(6)]
+        x, q, f = rng.standard_normal(n), rng.standard_normal(n), rng.standard_normal(n)
+        res, hs = R.complete_step(state, hist, x, q, f)
+        out[f"acc{k}.state"] = np.array(state, float)
+        out[f"acc{k}.hist"] = np.array(hist)
+        out[f"acc{k}.xqf"] = np.array([x, q, f])
+        out[f"acc{k}.out"] = res
+        out[f"acc{k}.hist_out"] = np.array(hs)
+        rej_in.append(state)
+        rej_out.append(R.reject_step(state))
+    out["rej.inputs"] = np.array(rej_in, float)
+    out["rej.outputs"] = np.array(rej_out, float)
+    out["acc.n"] = np.array([120])
+    return out
+
+
 def main():
     if not ref.tia_available():
         print("oracle/_ref/libxyceref_tia.so not built (needs the reference source tree)")
@@ -112,6 +149,7 @@ def main():
     for name in ("inverter_chain_24", "ring_7"):
         out.update(steps_of(name, rng))
     out.update(convergence_table(rng))
+    out.update(step_control_table(rng))
     path = os.path.join(HERE, "tia", "steps.npz")
     np.savez_compressed(path, **out)
     print(path, len(out), "arrays")

@@ -112,13 +112,19 @@ def test_direct_solver_solves_reuses_and_refactors(fp32, drive, oracle_lib):
 def test_direct_solver_repivots_and_reports_singular(drive):
     import scipy.sparse as sp
     drive.drive_direct_reset(0)
-    # the first matrix fixes a diagonal pivot order ...
+    # the first matrix fixes a pivot order ...
     A = sp.csr_matrix(np.array([[4.0, 1.0, 0.0], [1.0, 4.0, 1.0], [0.0, 1.0, 4.0]]))
     b = np.array([1.0, 2.0, 3.0])
     rc, x, sing, refac, an = _solve(drive, A, b)
     assert rc == 0 and an == 1 and np.allclose(A @ x, b, rtol=0, atol=1e-14)
-    # ... which meets a zero pivot on the next values: analysed again
-    B = sp.csr_matrix((np.array([0.0, 1.0, 1.0, 4.0, 1.0, 1.0, 4.0]), A.indices, A.indptr), shape=(3, 3))
+    # ... which meets a zero pivot on the next values: A with its first pivot
+    # in that order (A[P[0], Q[0]], which no update reaches) set to zero,
+    # nonsingular all the same; analysed again
+    P, Q, _ = engine.lu_analyze_host(A.indptr, A.indices, A.data)
+    Bd = A.toarray()
+    Bd[P[0], Q[0]] = 0.0
+    assert abs(np.linalg.det(Bd)) > 1.0
+    B = sp.csr_matrix((Bd[A.nonzero()], A.indices, A.indptr), shape=(3, 3))
     rc, x, sing, refac, an = _solve(drive, B, b)
     assert (rc, sing, an) == (0, 0, 2) and np.allclose(B @ x, b, rtol=0, atol=1e-13)
     # a singular matrix: a zero solution and status 0 (the nonlinear solver decides)

@@ -3,8 +3,9 @@ reference's own compiled time-integration and Newton code.
 
 tests/golden/tia/steps.npz was written by the reference's N_TIA_OneStep
 (updateCoeffs, obtainPredictor, obtainResidual, obtainJacobian), its
-N_TIA_DataStore error weights and WRMS norm, and N_NLS_DampedNewton::
-converged_ (oracle/_ref/libxyceref_tia.so, made by
+N_TIA_DataStore error weights and WRMS norm, N_NLS_DampedNewton::
+converged_, and the step control of OneStep::completeStep and rejectStep
+(oracle/_ref/libxyceref_tia.so, made by
 tests/golden/make_golden_tia.py) over trapezoid steps of the 24-stage
 inverter chain and the 7-stage ring oscillator, on the F, Q, limiter
 vectors and matrices of their transient loads in the device fixtures.  The
@@ -67,6 +68,29 @@ def test_newton_convergence_decisions_match_reference(fx, integ):
         seen.add(got[0])
     # every verdict of the test was exercised
     assert seen >= {1, 2, 3, 4, -1, -2, -3, 0}, seen
+
+
+def test_step_control_matches_reference(fx, integ):
+    """Accepted steps: the next order and step, the breakpoint clip, the
+    saved step, the rotated histories; failed steps: Newton failure, first
+    and later local-error failures.  Every case bit for bit."""
+    branches = set()
+    for k in range(int(fx["acc.n"][0])):
+        st = fx[f"acc{k}.state"]
+        out, hs = integ.complete_step(st, list(fx[f"acc{k}.hist"]), *fx[f"acc{k}.xqf"])
+        assert np.array_equal(out, fx[f"acc{k}.out"]), (k, out, fx[f"acc{k}.out"])
+        assert np.array_equal(np.array(hs), fx[f"acc{k}.hist_out"]), k
+        ratio = out[3] / st[4]
+        branches.add("clip" if out[5] == st[7] else "grow" if ratio == 2.0 else
+                     "shrink" if ratio < 1.0 else "keep" if ratio == 1.0 else "bounded")
+        branches.add(f"order{int(out[0])}")
+    assert branches >= {"clip", "grow", "shrink", "keep", "order1", "order2"}, branches
+    seen = set()
+    for st, want in zip(fx["rej.inputs"], fx["rej.outputs"]):
+        got = integ.reject_step(st)
+        assert np.array_equal(got, want), (st, got, want)
+        seen.add("newton" if st[15] <= 0 else "first" if st[2] == 0 else "later")
+    assert seen == {"newton", "first", "later"}, seen
 
 
 def test_integrator_matches_live_reference_random(integ):

@@ -751,11 +751,12 @@ __global__ void batch_control(BatchDev b) {
     hn = fmax(hn, min_step);
     hn = fmin(hn, cs.max_step);
     if (cs.stop_time - cs.t >= min_step) {
-      if (cs.t + hn > cs.stop_time) {
+      cs.next_time = cs.t + hn;
+      if (cs.next_time > cs.stop_time) {
         cs.saved = hn;
+        cs.next_time = cs.stop_time;  // the breakpoint itself, not t + (stop - t)
         hn = cs.stop_time - cs.t;
       }
-      cs.next_time = cs.t + hn;
       cs.h_sum = hn + cs.h_last;
     }
     cs.h = hn;
@@ -787,13 +788,18 @@ __global__ void batch_control(BatchDev b) {
     for (int i = 1; i <= cs.order; ++i) cs.psi[i - 1] = cs.psi[i];
     double hn;
     if (status <= 0) hn = cs.h / 8;
-    else if (cs.nef == 1) hn = fmax(r_min, fmin(r_max, pow(tol_aim / (est + 0.0001), 1.0 / (cs.order + 1.0)))) * cs.h;
+    // first local-error failure: the default build's rejectStep (no Q-norm):
+    // r_factor 1, r_safety 2, r_fudge 1e-4, the one-step method's new order 1
+    else if (cs.nef == 1) hn = fmax(r_min, fmin(r_max, 1.0 * pow(2.0 * (est + 0.0001), -1.0 / (1 + 1.0)))) * cs.h;
     else hn = r_min * cs.h;
     cs.order = 1;
     hn = fmax(hn, cs.t * 10.0 * DBL_EPSILON);
     hn = fmin(hn, cs.max_step);
-    if (cs.t + hn > cs.stop_time) hn = cs.stop_time - cs.t;
     cs.next_time = cs.t + hn;
+    if (cs.next_time > cs.stop_time) {
+      cs.next_time = cs.stop_time;
+      hn = cs.stop_time - cs.t;
+    }
     cs.h_sum = hn + cs.h_last;
     cs.h = hn;
     if (cs.nef >= 15 || cs.h < 1e-21) {

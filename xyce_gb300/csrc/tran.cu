@@ -750,11 +750,12 @@ extern "C" int xg_tran_run(xg_circuit *c, const xg_tran_options *o, const double
       hn = std::max(hn, min_step);
       hn = std::min(hn, max_step);
       if (stop_time - t >= min_step) {
-        if (t + hn > stop_time) {
+        next_time = t + hn;
+        if (next_time > stop_time) {
           saved = hn;
+          next_time = stop_time;  // the breakpoint itself, not t + (stop - t)
           hn = stop_time - t;
         }
-        next_time = t + hn;
         h_sum = hn + h_last;
       }
       h = hn;
@@ -778,7 +779,9 @@ extern "C" int xg_tran_run(xg_circuit *c, const xg_tran_options *o, const double
       if (ns <= 0) {
         hn = h / 8;
       } else if (nef == 1) {
-        double rr = std::pow(tol_aim / (est + 0.0001), 1.0 / (order + 1.0));
+        // the default build's rejectStep (no Q-norm): r_factor 1, r_safety 2,
+        // r_fudge 1e-4 and the one-step method's new order 1
+        double rr = 1.0 * std::pow(2.0 * (est + 0.0001), -1.0 / (1 + 1.0));
         rr = std::max(r_min, std::min(r_max, rr));
         hn = rr * h;
       } else {
@@ -787,8 +790,11 @@ extern "C" int xg_tran_run(xg_circuit *c, const xg_tran_options *o, const double
       order = 1;
       hn = std::max(hn, t * 10.0 * DBL_EPSILON);
       hn = std::min(hn, max_step);
-      if (t + hn > stop_time) hn = stop_time - t;
       next_time = t + hn;
+      if (next_time > stop_time) {
+        next_time = stop_time;
+        hn = stop_time - t;
+      }
       h_sum = hn + h_last;
       h = hn;
       if (h < 1e-21) {
