@@ -387,6 +387,56 @@ int xg_batch_results(xg_batch *b, int i, double *host_t, double *host_v, int *n_
 int xg_batch_info(const xg_batch *b, int *n_requests, int64_t *device_bytes);
 int xg_batch_destroy(xg_batch *b);
 
+/* ---- slotted batches (continuous batching at request granularity) ------------
+ * A slotted batch is created empty with a fixed number of slots of one shape
+ * (a size class: the largest request a slot holds).  Requests are submitted
+ * into free slots while the batch runs; a finished request's results are read
+ * and its slot released for the next one, so a short request never waits for
+ * a long one, and a request arriving mid-run starts at the next batch
+ * iteration instead of waiting for a new batch.  Each request's arithmetic is
+ * the same as in a batch of its own (its load, reduction order, pivot order,
+ * Newton test and step control depend on it alone), so its results do not
+ * depend on which other requests share the batch.
+ *   - Device memory for every slot is allocated at creation
+ *     (xg_slot_bytes per slot): submitting allocates nothing on the device.
+ *   - xg_batch_submit sets the requests up on the host (device parameters,
+ *     pattern, reduction lists), evaluates their first Jacobian on the device
+ *     with a load restricted to their slots (on a stream of its own, beside
+ *     the running iterations), analyses each one's pivot order, and activates
+ *     them at the next batch iteration.  It returns when that activation is
+ *     enqueued; it may run on another thread than xg_batch_run/poll.
+ *   - xg_batch_run, xg_batch_poll and xg_batch_results work as for any batch,
+ *     with slot numbers for request numbers; a free slot counts as done. */
+typedef struct {
+  int max_unknowns;                       /* nodes + internal unknowns */
+  int max_instances[XG_NUM_DEV_TYPES];    /* per device type */
+  int64_t max_nnz;                        /* Jacobian entries */
+  int64_t max_lu_nnz;                     /* L\U entries after the pivot analysis */
+  int64_t max_schedule;                   /* level-schedule ints (0: no level path) */
+  int max_breakpoints;                    /* PULSE corners up to tstop, and tstop */
+} xg_slot_shape;
+/* The shape of one request: its set-up, first Jacobian (at x0, step tstep)
+ * and pivot analysis, exactly as xg_batch_submit does them. */
+int xg_slot_need(xg_ctx *ctx, const xg_netlist *nl, const double *x0, double tstop, double tstep,
+                 xg_slot_shape *need);
+/* Device bytes of one slot of this shape under these options (host
+ * arithmetic only: no device needed). */
+int xg_slot_bytes(const xg_slot_shape *shape, const xg_batch_options *o, int64_t *bytes);
+int xg_batch_create_slots(xg_ctx *ctx, int n_slots, const xg_slot_shape *shape,
+                          const xg_batch_options *o, xg_batch **out);
+/* Submit n requests.  slots[i] receives request i's slot, or -1 when no slot
+ * was free (the request was not taken).  A request larger than the shape, or
+ * whose set-up fails, is refused with an error and nothing of the call is
+ * admitted. */
+int xg_batch_submit(xg_batch *b, int n, const xg_netlist *const *netlists, const double *const *x0,
+                    const double *tstop, const int *const *out_idx, int *slots);
+/* Free a finished slot for the next request (its results are gone then). */
+int xg_batch_release(xg_batch *b, int slot);
+/* Free slots, and slots whose request is still running. */
+int xg_batch_slots(const xg_batch *b, int *n_free, int *n_running);
+/* Free and total device memory of the context's device (cudaMemGetInfo). */
+int xg_mem_info(xg_ctx *ctx, int64_t *free_bytes, int64_t *total_bytes);
+
 /* xg_load_noalloc — the same load as xg_load, for callers that cannot
  * allocate device memory at the point where they load: host simulators that
  * give the GPU a fixed memory budget up front and own every later byte

@@ -108,6 +108,28 @@ class XgBatchOptions(C.Structure):
                 ("n_out", C.c_int), ("max_points", C.c_int)]
 
 
+class XgSlotShape(C.Structure):
+    """The largest request one slot of a slotted batch holds."""
+    _fields_ = [("max_unknowns", C.c_int), ("max_instances", C.c_int * NUM_DEV_TYPES),
+                ("max_nnz", C.c_int64), ("max_lu_nnz", C.c_int64), ("max_schedule", C.c_int64),
+                ("max_breakpoints", C.c_int)]
+
+    def as_dict(self):
+        return {"max_unknowns": self.max_unknowns, "max_instances": list(self.max_instances),
+                "max_nnz": self.max_nnz, "max_lu_nnz": self.max_lu_nnz,
+                "max_schedule": self.max_schedule, "max_breakpoints": self.max_breakpoints}
+
+    @classmethod
+    def from_dict(cls, d):
+        s = cls()
+        s.max_unknowns = int(d["max_unknowns"])
+        for t, v in enumerate(d["max_instances"]):
+            s.max_instances[t] = int(v)
+        s.max_nnz, s.max_lu_nnz = int(d["max_nnz"]), int(d["max_lu_nnz"])
+        s.max_schedule, s.max_breakpoints = int(d["max_schedule"]), int(d["max_breakpoints"])
+        return s
+
+
 def device_options(gmin=1e-12, temp=300.15, tnom=300.15, voltlim=1, newmeyer=0, fma=0):
     return XgDeviceOptions(gmin, temp, tnom, voltlim, newmeyer, fma)
 

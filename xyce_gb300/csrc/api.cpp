@@ -213,6 +213,12 @@ int ctx_info(xg_ctx *ctx, int *device, void **stream) {
   return XG_OK;
 }
 
+int ctx_options(xg_ctx *ctx, xg_device_options *o) {
+  if (!ctx || !o) return XG_ERR_ARG;
+  *o = ctx->opt;
+  return XG_OK;
+}
+
 int circuit_view(xg_circuit *c, CircuitView *v) {
   if (!c || !v) return XG_ERR_ARG;
   v->ctx = c->ctx;

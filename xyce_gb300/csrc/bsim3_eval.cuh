@@ -71,8 +71,7 @@ struct B3Local {
 
 __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Flags f, LoadIO io) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= t.n) return;
-  if (t.cflags) f = t.cflags[t.cid[i]];
+  if (i >= t.n || !instance_flags(t, i, f)) return;
   const int nI = t.n;  // instances ("n" is the subthreshold swing below)
   const double *__restrict__ p = t.p;
 #define PRM(k) __ldg(p + (int64_t)(k) * nI + i)

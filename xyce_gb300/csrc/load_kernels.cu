@@ -151,10 +151,26 @@ struct Terms {
   }
 };
 
+// Batched loads: take instance i's circuit flags; false when the instance is
+// not evaluated (no circuit: an unused place in a slot; or a finished one).
+__device__ __forceinline__ bool instance_flags(const DevType &t, int i, Flags &f) {
+  if (!t.cid) return true;
+  const int c = __ldg(t.cid + i);
+  if (c < 0) return false;
+  if (!t.cflags) return true;
+  f = t.cflags[c];
+  return !f.skip;
+}
+__device__ __forceinline__ bool instance_live(const DevType &t, int i) {
+  if (!t.cid) return true;
+  const int c = __ldg(t.cid + i);
+  return c >= 0 && !(t.cflags && t.cflags[c].skip);
+}
+
 // ---- resistor (N_DEV_Resistor.C:1073-1135) ---------------------------------
 __global__ void __launch_bounds__(256) res_kernel(DevType t, LoadIO io) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= t.n) return;
+  if (i >= t.n || !instance_live(t, i)) return;
   const int n = t.n;
   int lp = ld(t.lid + i), ln = ld(t.lid + n + i);
   double G = ld(t.p + i);
@@ -171,7 +187,7 @@ __global__ void __launch_bounds__(256) res_kernel(DevType t, LoadIO io) {
 // ---- capacitor, constant C, no IC (N_DEV_Capacitor.C:1821-2040) -------------
 __global__ void __launch_bounds__(256) cap_kernel(DevType t, LoadIO io) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= t.n) return;
+  if (i >= t.n || !instance_live(t, i)) return;
   const int n = t.n;
   int lp = ld(t.lid + i), ln = ld(t.lid + n + i);
   double C = ld(t.p + i);
@@ -207,8 +223,7 @@ __device__ double pulse_value(const double *p, int n, int i, double t) {
 // ---- independent voltage source (N_DEV_Vsrc.C:941-1045) ---------------------
 __global__ void __launch_bounds__(256) vsrc_kernel(DevType t, Flags f, LoadIO io) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= t.n) return;
-  if (t.cflags) f = t.cflags[t.cid[i]];
+  if (i >= t.n || !instance_flags(t, i, f)) return;
   const int n = t.n;
   int lp = ld(t.lid + i), ln = ld(t.lid + n + i), lb = ld(t.lid + 2 * n + i);
   double source;
@@ -233,8 +248,7 @@ __global__ void __launch_bounds__(256) vsrc_kernel(DevType t, Flags f, LoadIO io
 // The source value goes into F at both terminals; there are no matrix entries.
 __global__ void __launch_bounds__(256) isrc_kernel(DevType t, Flags f, LoadIO io) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= t.n) return;
-  if (t.cflags) f = t.cflags[t.cid[i]];
+  if (i >= t.n || !instance_flags(t, i, f)) return;
   const int n = t.n;
   double source;
   if ((f.tranop || f.transient) && ld(t.p + XG_V_KIND * n + i) == XG_SRC_PULSE)
@@ -249,8 +263,7 @@ __global__ void __launch_bounds__(256) isrc_kernel(DevType t, Flags f, LoadIO io
 // ---- junction diode, level 1 (N_DEV_Diode.C:873-1331, 2007-2128) ------------
 __global__ void __launch_bounds__(256) diode_kernel(DevType t, DevOptions o, Flags f, LoadIO io) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= t.n) return;
-  if (t.cflags) f = t.cflags[t.cid[i]];
+  if (i >= t.n || !instance_flags(t, i, f)) return;
   const int n = t.n;
   const double *p = t.p;
 #define PRM(k) ld(p + (k) * n + i)
@@ -370,8 +383,7 @@ __global__ void __launch_bounds__(256) diode_kernel(DevType t, DevOptions o, Fla
 // ---- MOSFET level 1 (N_DEV_MOSFET1.C:2618-3427, 4103-4722), newMeyer off ----
 __global__ void __launch_bounds__(128) mos1_kernel(DevType t, DevOptions o, Flags f, LoadIO io) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= t.n) return;
-  if (t.cflags) f = t.cflags[t.cid[i]];
+  if (i >= t.n || !instance_flags(t, i, f)) return;
   const int n = t.n;
   const double *p = t.p;
 #define PRM(k) ld(p + (k) * n + i)

@@ -61,10 +61,17 @@ struct CState {
   int steps, steps_attempted, rejected, newton_iters, loads, n_rec;
   int bpi;                       // index of stop_time in the request's breakpoints
   int hist_order;                // order of the history update of an accepted step
+  int gen;                       // slotted batches: which request of the slot this is
 };
 
 struct BatchDev {
   int nc;
+  // Request c's ranges below run from xptr[c] to xend[c]: in a batch made
+  // from a fixed set of requests xend = xptr + 1 (the ranges are packed); in
+  // a slotted batch each slot owns a fixed region and xend marks how much of
+  // it the request in the slot uses.
+  const int *uend, *send, *oend, *jend, *bp_end;
+  const int64_t *lnz_end, *sched_end;
   const int *uptr, *uidx;        // unknowns of request c (union ids, local order)
   const int *sptr, *sidx;        // its state slots: ranges (start, length) sptr[c]..sptr[c+1]
   const int *optr, *oidx;        // its store slots, the same way
@@ -141,7 +148,7 @@ __global__ void __launch_bounds__(128) batch_solve(BatchDev b) {
   const int c = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (c >= b.nc) return;
   if (b.cs[c].phase != PH_ITER || b.lvl[c]) return;
-  const int u0 = b.uptr[c], n = b.uptr[c + 1] - u0;
+  const int u0 = b.uptr[c], n = b.uend[c] - u0;
   const int *rp = b.lrp + b.lrp_off[c];
   const int64_t z0 = b.lnz_off[c];
   const int *ci = b.lci + z0;
@@ -150,7 +157,7 @@ __global__ void __launch_bounds__(128) batch_solve(BatchDev b) {
   T *rd = (T *)b.lrd + u0;
   int *map = b.map + u0;
   const int *P = b.lP + u0, *Q = b.lQ + u0;
-  const int64_t nz = b.lnz_off[c + 1] - z0;
+  const int64_t nz = b.lnz_end[c] - z0;
   for (int64_t p = lane; p < nz; p += 32) {
     const int64_t s = b.lu2a[z0 + p];
     val[p] = s >= 0 ? T(b.jac[s]) : T(0);
@@ -246,9 +253,9 @@ __global__ void __launch_bounds__(32) batch_solve_smem(BatchDev b) {
   const int c = blockIdx.x, lane = threadIdx.x;
   if (c >= b.nc) return;
   if (b.cs[c].phase != PH_ITER || b.lvl[c]) return;
-  const int u0 = b.uptr[c], n = b.uptr[c + 1] - u0;
+  const int u0 = b.uptr[c], n = b.uend[c] - u0;
   const int64_t z0 = b.lnz_off[c];
-  const int nz = int(b.lnz_off[c + 1] - z0);
+  const int nz = int(b.lnz_end[c] - z0);
   auto a16 = [](size_t v) { return (v + 15) & ~size_t(15); };
   T *val = (T *)sm;
   T *rd = (T *)(sm + a16(sizeof(T) * nz));
@@ -370,11 +377,11 @@ __global__ void __launch_bounds__(kLvlThreads) batch_solve_lvl(BatchDev b) {
   const int c = blockIdx.x, lane = threadIdx.x & 31, tid = threadIdx.x, nt = blockDim.x;
   if (c >= b.nc) return;
   if (b.cs[c].phase != PH_ITER || !b.lvl[c]) return;
-  const int u0 = b.uptr[c], n = b.uptr[c + 1] - u0;
+  const int u0 = b.uptr[c], n = b.uend[c] - u0;
   const int64_t z0 = b.lnz_off[c];
-  const int nz = int(b.lnz_off[c + 1] - z0);
+  const int nz = int(b.lnz_end[c] - z0);
   const int64_t s0 = b.sched_off[c];
-  const int blob = int(b.sched_off[c + 1] - s0);
+  const int blob = int(b.sched_end[c] - s0);
   auto a16 = [](size_t v) { return (v + 15) & ~size_t(15); };
   T *val = (T *)sm;
   T *rd = (T *)(sm + a16(sizeof(T) * nz));
@@ -557,7 +564,7 @@ __global__ void __launch_bounds__(kBatchThreads) batch_combine(BatchDev b) {
   if (c >= b.nc) return;
   const CState &cs = b.cs[c];
   if (cs.phase == PH_DONE || cs.phase == PH_INIT) return;
-  const int u0 = b.uptr[c], n = b.uptr[c + 1] - u0;
+  const int u0 = b.uptr[c], n = b.uend[c] - u0;
   const int order = cs.order;
   const double inv_h = 1.0 / cs.h, fs = order == 2 ? 0.5 : 1.0;
   double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};  // sums: rhs^2, err^2; maxima: rhs, limiter, x
@@ -578,7 +585,7 @@ __global__ void __launch_bounds__(kBatchThreads) batch_combine(BatchDev b) {
   }
   // the Jacobian entries of the request's rows, as runs of consecutive
   // entries spread over the block (a supply row's hundreds of entries too)
-  for (int k = b.jptr[c]; k < b.jptr[c + 1]; ++k) {
+  for (int k = b.jptr[c]; k < b.jend[c]; ++k) {
     const int p0 = b.jidx[2 * k], p1 = p0 + b.jidx[2 * k + 1];
     for (int p = p0 + threadIdx.x; p < p1; p += blockDim.x) b.jac[p] = inv_h * b.dqdx[p] + fs * b.dfdx[p];
   }
@@ -653,7 +660,7 @@ constexpr double kBpTol = 1e-18;
 
 // The first breakpoint after t (the breakpoint list ends with tstop).
 __device__ void next_breakpoint(const BatchDev &b, int c, CState &cs) {
-  const int e = b.bp_ptr[c + 1];
+  const int e = b.bp_end[c];
   int k = b.bp_ptr[c] + cs.bpi;
   while (k < e && b.bp[k] <= cs.t + kBpTol) ++k;
   cs.bpi = k - b.bp_ptr[c];
@@ -666,7 +673,7 @@ __global__ void batch_control(BatchDev b) {
   CState &cs = b.cs[c];
   Flags &fl = b.flags[c];
   const double *pp = b.part + c * Q_N;
-  const int n = b.uptr[c + 1] - b.uptr[c];
+  const int n = b.uend[c] - b.uptr[c];
   cs.action = 0;
   if (cs.phase == PH_DONE) return;
   if (cs.phase == PH_INIT) {
@@ -763,6 +770,7 @@ __global__ void batch_control(BatchDev b) {
     cs.hist_order = cs.order;
     if (!(cs.t < cs.tstop) || fabs(cs.t - cs.tstop) <= kBpTol) {
       cs.phase = PH_DONE;
+      fl.skip = 1;
       return;
     }
     cs.beginning = fabs(cs.t - cs.stop_time) <= kBpTol && fabs(cs.t - cs.tstop) > kBpTol;
@@ -806,6 +814,7 @@ __global__ void batch_control(BatchDev b) {
       cs.failed = 1;
       cs.status = status != 0 ? status : -7;
       cs.phase = PH_DONE;
+      fl.skip = 1;
       return;
     }
   }
@@ -819,7 +828,7 @@ __global__ void __launch_bounds__(kVectorThreads) batch_vector(BatchDev b) {
   CState &cs = b.cs[c];
   const int act = cs.action;
   if (!act) return;
-  const int u0 = b.uptr[c], n = b.uptr[c + 1] - u0;
+  const int u0 = b.uptr[c], n = b.uend[c] - u0;
   if (act & A_INIT) {
     for (int k = tid; k < n; k += nt) {
       const int g = b.uidx[u0 + k];
@@ -854,10 +863,10 @@ __global__ void __launch_bounds__(kVectorThreads) batch_vector(BatchDev b) {
     }
     // state / store of the accepted point become current (the load kernels
     // read current and next, never last; they are ranges of slots)
-    for (int k = b.sptr[c]; k < b.sptr[c + 1]; ++k)
+    for (int k = b.sptr[c]; k < b.send[c]; ++k)
       for (int s = b.sidx[2 * k] + tid; s < b.sidx[2 * k] + b.sidx[2 * k + 1]; s += nt)
         b.stac[s] = b.sta[s];
-    for (int k = b.optr[c]; k < b.optr[c + 1]; ++k)
+    for (int k = b.optr[c]; k < b.oend[c]; ++k)
       for (int s = b.oidx[2 * k] + tid; s < b.oidx[2 * k] + b.oidx[2 * k + 1]; s += nt)
         b.stoc[s] = b.sto[s];
     __syncthreads();
@@ -897,7 +906,7 @@ __global__ void __launch_bounds__(kVectorThreads) batch_vector(BatchDev b) {
     }
     // the limiters read the previous iterate from next store: start from the
     // current one (every state slot is rewritten by the next load)
-    for (int k = b.optr[c]; k < b.optr[c + 1]; ++k)
+    for (int k = b.optr[c]; k < b.oend[c]; ++k)
       for (int s = b.oidx[2 * k] + tid; s < b.oidx[2 * k] + b.oidx[2 * k + 1]; s += nt)
         b.sto[s] = b.stoc[s];
   }
@@ -912,6 +921,12 @@ int to_dev(V **d, const std::vector<V> &h) {
 }
 
 }  // namespace
+}  // namespace xg
+
+namespace xg {
+struct SlotPool;
+void free_pool(SlotPool *p);
+int pool_gen(SlotPool *p, int slot);  // which request slot `slot` holds now
 }  // namespace xg
 
 // ---------------------------------------------------------------------------
@@ -936,6 +951,8 @@ struct xg_batch {
   int64_t bytes = 0;
   // pinned host mirror of the request states
   xg::CState *h_cs = nullptr;
+  // slotted batches: the pool behind the slots (null for a fixed batch)
+  xg::SlotPool *pool = nullptr;
 };
 
 namespace {
@@ -1106,8 +1123,53 @@ int build_union(int n, const xg_netlist *const *nls, UnionNetlist *U,
 
 namespace {
 
+// One request's pivot order and L\U pattern, from its first Jacobian: the
+// level schedule runs each request's levels on the lanes of a warp, so the
+// column order is chosen for depth as for a single circuit.  gpos (filled by
+// the caller) is the batch Jacobian entry of each local entry.
+struct ReqLU {
+  xg::LuSymbolic S;
+  std::vector<int64_t> gpos;
+  std::vector<int> blob;  // the level schedule (lvl_blob_len layout)
+  int rc = XG_OK;
+  std::string err;
+};
+
+void analyse_request(int nr, const std::vector<int> &rp, const std::vector<int> &ci,
+                     const std::vector<double> &val, const std::string &who, ReqLU *out) {
+  using namespace xg;
+  ReqLU &R = *out;
+  LuSymbolic &S = R.S;
+  if (lu_analyze(nr, rp.data(), ci.data(), val.data(), 1e-3, &S, &R.err, -1)) {
+    R.rc = XG_ERR_SINGULAR;
+    R.err = who + ": " + R.err;
+    return;
+  }
+  if (!lu_build_updates(S)) {
+    R.rc = XG_ERR_ARG;
+    R.err = who + ": internal error, an update falls outside the L\\U pattern";
+    return;
+  }
+  const int hdr[H_N] = {int(S.lptr.size()) - 1, int(S.uptr.size()) - 1, S.tail0,
+                        int(S.tail_rowg.size()) - 1, int(S.tail_gptr.size()) - 1,
+                        int(S.tail_pos.size()), int(S.tail_pm.size()), int(S.upos.size())};
+  R.blob.assign(hdr, hdr + H_N);
+  for (int64_t v : S.urp) R.blob.push_back(int(v));
+  for (const std::vector<int> *a : {&S.upos, &S.lrow, &S.lptr, &S.urow, &S.uptr, &S.tail_rowg,
+                                    &S.tail_gptr, &S.tail_pos, &S.tail_pp, &S.tail_pm, &S.tail_q})
+    R.blob.insert(R.blob.end(), a->begin(), a->end());
+  if (int64_t(R.blob.size()) != lvl_blob_len(nr, hdr)) {
+    R.rc = XG_ERR_ARG;
+    R.err = who + ": internal error in the level schedule";
+  }
+  std::vector<int64_t>().swap(S.urp);
+  std::vector<int>().swap(S.upos);
+}
+
 void free_batch(xg_batch *b) {
   if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->pool) xg::free_pool(b->pool);
+  b->pool = nullptr;
   if (b->graph) cudaGraphExecDestroy(b->graph);
   for (void *p : b->allocs) cudaFree(p);
   for (int t = 0; t < XG_NUM_DEV_TYPES; ++t)
@@ -1132,9 +1194,25 @@ int dev_zero(xg_batch *b, double **d, size_t n) {
   return cudaMemset(*d, 0, sizeof(double) * std::max<size_t>(n, 1)) == cudaSuccess ? XG_OK : XG_ERR_CUDA;
 }
 
+}  // namespace
+
+namespace xg {
+// One capture or graph launch at a time across threads (a server sets up and
+// first runs a batch on a helper thread while its main thread keeps launching
+// the others), and no launch onto a batch's stream while it is captured.
+std::mutex &launch_mutex() {
+  static std::mutex m;
+  return m;
+}
+int enqueue_pool_iteration(xg_batch *b);
+}  // namespace xg
+
+namespace {
+
 // One batch iteration: solve, load, combine, control, vector.
 int enqueue_iteration(xg_batch *b) {
   using namespace xg;
+  if (b->pool) return enqueue_pool_iteration(b);
   CircuitView v;
   circuit_view(b->ckt, &v);
   const Plan &P = *v.plan;
@@ -1320,13 +1398,6 @@ extern "C" int xg_batch_create(xg_ctx *ctx, int n, const xg_netlist *const *nls,
   std::vector<int64_t> lnz_off(n + 1, 0), lu2a, sched_off(n + 1, 0);
   // Each request's analysis is independent: analyse them on the host's cores,
   // then concatenate in request order.
-  struct ReqLU {
-    LuSymbolic S;
-    std::vector<int64_t> gpos;
-    std::vector<int> blob;
-    int rc = XG_OK;
-    std::string err;
-  };
   std::vector<ReqLU> req(n);
   auto analyse = [&](int r, std::vector<int> &g2l) {
     ReqLU &R = req[r];
@@ -1348,33 +1419,7 @@ extern "C" int xg_batch_create(xg_ctx *ctx, int n, const xg_netlist *const *nls,
       }
       rp[k + 1] = int(ci.size());
     }
-    LuSymbolic &S = R.S;
-    // the level schedule runs each request's levels on the lanes of a warp,
-    // so the column order is chosen for depth as for a single circuit
-    if (lu_analyze(nr_, rp.data(), ci.data(), val.data(), 1e-3, &S, &R.err, -1)) {
-      R.rc = XG_ERR_SINGULAR;
-      R.err = "xg_batch_create: request " + std::to_string(r) + ": " + R.err;
-      return;
-    }
-    if (!lu_build_updates(S)) {
-      R.rc = XG_ERR_ARG;
-      R.err = "xg_batch_create: internal error, an update falls outside the L\\U pattern";
-      return;
-    }
-    const int hdr[H_N] = {int(S.lptr.size()) - 1, int(S.uptr.size()) - 1, S.tail0,
-                          int(S.tail_rowg.size()) - 1, int(S.tail_gptr.size()) - 1,
-                          int(S.tail_pos.size()), int(S.tail_pm.size()), int(S.upos.size())};
-    R.blob.assign(hdr, hdr + H_N);
-    for (int64_t v : S.urp) R.blob.push_back(int(v));
-    for (const std::vector<int> *a : {&S.upos, &S.lrow, &S.lptr, &S.urow, &S.uptr, &S.tail_rowg,
-                                      &S.tail_gptr, &S.tail_pos, &S.tail_pp, &S.tail_pm, &S.tail_q})
-      R.blob.insert(R.blob.end(), a->begin(), a->end());
-    if (int64_t(R.blob.size()) != lvl_blob_len(nr_, hdr)) {
-      R.rc = XG_ERR_ARG;
-      R.err = "xg_batch_create: internal error in the level schedule";
-    }
-    std::vector<int64_t>().swap(S.urp);
-    std::vector<int>().swap(S.upos);
+    analyse_request(nr_, rp, ci, val, "xg_batch_create: request " + std::to_string(r), &R);
   };
   {
     const int nthreads = std::max(1, std::min<int>(std::min(16, n), int(std::thread::hardware_concurrency())));
@@ -1437,6 +1482,7 @@ extern "C" int xg_batch_create(xg_ctx *ctx, int n, const xg_netlist *const *nls,
       return XG_ERR_OOM;
     }
     d.bp_ptr = t_bp_ptr;
+    d.bp_end = t_bp_ptr + 1;
     d.bp = t_bp;
   }
   d.nc = n;
@@ -1462,6 +1508,8 @@ extern "C" int xg_batch_create(xg_ctx *ctx, int n, const xg_netlist *const *nls,
   }
   d.uptr = t_uptr; d.uidx = t_uidx; d.sptr = t_sptr; d.sidx = t_sidx; d.optr = t_optr; d.oidx = t_oidx;
   d.jptr = t_jptr; d.jidx = t_jidx;
+  d.uend = t_uptr + 1; d.send = t_sptr + 1; d.oend = t_optr + 1; d.jend = t_jptr + 1;
+  d.lnz_end = t_lnz_off + 1;
   d.arp = t_arp; d.aci = t_aci; d.lrp_off = t_lrp_off; d.lnz_off = t_lnz_off; d.lrp = t_lrp;
   d.lci = t_lci; d.ldiag = t_ldiag; d.lu2a = t_lu2a; d.lP = t_lP; d.lQ = t_lQ; d.out_idx = t_out;
   const size_t tsz = o->lu_precision == XG_LU_FP32 ? sizeof(float) : sizeof(double);
@@ -1498,6 +1546,7 @@ extern "C" int xg_batch_create(xg_ctx *ctx, int n, const xg_netlist *const *nls,
       return XG_ERR_OOM;
     }
     d.sched_off = t_sched_off;
+    d.sched_end = t_sched_off + 1;
     d.sched = t_sched;
     d.lvl = t_lvl;
     b->n_walk = n - int(std::count(lvl_req.begin(), lvl_req.end(), 1));
@@ -1638,8 +1687,7 @@ extern "C" int xg_batch_run(xg_batch *b, int iterations) {
   // and first runs a batch on a helper thread while its main thread keeps
   // launching the others, and the launch counter's capture bookkeeping below
   // assumes no other launch lands in between.
-  static std::mutex run_mutex;
-  std::lock_guard<std::mutex> lock(run_mutex);
+  std::lock_guard<std::mutex> lock(xg::launch_mutex());
   if (!b->graph || b->graph_iters != iterations) {
     if (b->graph) {
       cudaStreamSynchronize(b->stream);
@@ -1707,6 +1755,12 @@ extern "C" int xg_batch_results(xg_batch *b, int i, double *t, double *v, int *n
     return XG_ERR_ARG;
   }
   const xg::CState &c = b->h_cs[i];
+  if (b->pool && c.gen != xg::pool_gen(b->pool, i)) {
+    // the last poll predates the slot's request: nothing recorded yet
+    *n_points = 0;
+    if (st) std::memset(st, 0, sizeof(*st));
+    return XG_OK;
+  }
   const int np = std::min(c.n_rec, b->max_points);
   *n_points = np;
   if (np && t &&
@@ -1745,5 +1799,1154 @@ extern "C" int xg_batch_destroy(xg_batch *b) {
   if (!b) return XG_OK;
   free_batch(b);
   delete b;
+  return XG_OK;
+}
+
+// ===========================================================================
+// Slotted batches: continuous batching at request granularity
+// ===========================================================================
+//
+// A slotted batch is a batch whose per-request arrays have a fixed region per
+// slot instead of being packed.  Slot c owns unknowns [c*ucap, (c+1)*ucap),
+// Jacobian entries [c*jcap, ...), the instances [c*icap_t, ...) of each device
+// type in that type's parameter, LID, term, state and store arrays, and its
+// own regions of the L\U, schedule, reduction, breakpoint and record arrays.
+// The batch kernels above read request c's ranges through xptr[c]..xend[c],
+// so a slot holds a request of any size up to its shape, and a slot that is
+// free, or whose request has finished, is skipped by every kernel: its phase
+// is done and its load flags say skip.
+//
+// The load of a slotted batch is its own: the evaluation kernels run over
+// every type's whole instance array (an unused place has circuit -1), and
+// pool_reduce sums each live slot's outputs from that request's own reduction
+// lists (the same term order as a batch of its own; every sum is taken in
+// order, so the result does not depend on the other slots).
+//
+// Submitting a request writes its data into a free slot with one copy-list
+// kernel (seg_copy) on the batch's set-up stream, evaluates the slot's first
+// Jacobian there with a load restricted to the slots being set up (their own
+// circuit and flag arrays), analyses the pivot order on the host, writes the
+// L\U arrays, and then, on the batch's own stream and so between two batch
+// iterations, copies the request's starting state and flags into place.
+
+namespace xg {
+
+constexpr int kTypes = XG_NUM_DEV_TYPES;
+constexpr int kB3Mem = 20;  // BSIM3 members carried between loads, per instance
+
+// A copy list run on the device: 32-bit words copied from a staging payload,
+// or filled with one word.
+struct Seg {
+  uint32_t *dst;
+  int64_t src;   // word offset in the payload; < 0: fill
+  int64_t n;     // words
+  uint32_t fill;
+  uint32_t pad;
+};
+
+__global__ void __launch_bounds__(256) seg_copy(const Seg *segs, int nseg, const uint32_t *payload) {
+  const int lane = threadIdx.x & 31;
+  const int nw = int((gridDim.x * blockDim.x) >> 5);
+  for (int w = int((blockIdx.x * blockDim.x + threadIdx.x) >> 5); w < nseg; w += nw) {
+    const Seg sg = segs[w];
+    if (sg.src >= 0)
+      for (int64_t k = lane; k < sg.n; k += 32) sg.dst[k] = payload[sg.src + k];
+    else
+      for (int64_t k = lane; k < sg.n; k += 32) sg.dst[k] = sg.fill;
+  }
+}
+
+// One output of a slot: the sum, in order, of ref[beg .. beg+cnt) terms.
+struct RedEntry {
+  int64_t out;
+  int64_t beg;
+  int32_t cnt;
+  int32_t pad;
+};
+static_assert(sizeof(RedEntry) == 24, "RedEntry is six words");
+
+struct PoolRed {
+  const RedEntry *ent;   // slot c's entries start at c * ecap
+  int64_t ecap;
+  const int *ne, *nl;    // entries of slot c, and how many of them (first) are long
+  const uint32_t *ref;   // term of each reduction entry
+  const double *terms;
+  double *out;
+};
+
+constexpr int kLongOut = 64;  // outputs with more terms go to a warp each
+
+// A block per slot: live slots (phase not done), or the listed ones.  Long
+// outputs take a warp each (the lanes fetch, every lane adds the fetched
+// values in order); short ones a thread each.  Every sum is ((0 + t0) + t1)...
+__global__ void __launch_bounds__(256) pool_reduce(PoolRed r, const CState *cs, const int *slots) {
+  const int c = slots ? slots[blockIdx.x] : int(blockIdx.x);
+  if (!slots && cs[c].phase == PH_DONE) return;
+  const RedEntry *E = r.ent + int64_t(c) * r.ecap;
+  const int ne = r.ne[c], nl = r.nl[c];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int k = wid; k < nl; k += nw) {
+    const RedEntry e = E[k];
+    double s = 0.0;
+    for (int base = 0; base < e.cnt; base += 32) {
+      const int m = min(32, e.cnt - base);
+      const double v = lane < m ? r.terms[r.ref[e.beg + base + lane]] : 0.0;
+      for (int j = 0; j < m; ++j) s += __shfl_sync(0xffffffffu, v, j);
+    }
+    if (lane == 0) r.out[e.out] = s;
+  }
+  for (int k = nl + threadIdx.x; k < ne; k += blockDim.x) {
+    const RedEntry e = E[k];
+    double s = 0.0;
+    for (int j = 0; j < e.cnt; ++j) s += r.terms[r.ref[e.beg + j]];
+    r.out[e.out] = s;
+  }
+}
+
+// Activation, on the batch's stream between two iterations: the starting
+// state and flags written by the set-up stream go into place.
+constexpr int kActivateMax = 64;
+struct SlotList {
+  int n;
+  int slot[kActivateMax];
+};
+__global__ void activate_slots(SlotList l, CState *cs, const CState *cs_next, Flags *fl,
+                               const Flags *fl_next) {
+  const int k = threadIdx.x;
+  if (k >= l.n) return;
+  const int c = l.slot[k];
+  cs[c] = cs_next[c];
+  fl[c] = fl_next[c];
+}
+
+// Capacities of one slot.
+struct SlotCaps {
+  int ucap = 0;           // unknown rows: the shape's + 1 (ground stays outside)
+  int64_t jcap = 0, lucap = 0, blobcap = 0, rcap = 0, ecap = 0;
+  int bpcap = 0;
+  int icap[kTypes] = {};
+};
+
+SlotCaps slot_caps(const xg_slot_shape &sh) {
+  SlotCaps k;
+  k.ucap = sh.max_unknowns + 1;
+  k.jcap = std::max<int64_t>(sh.max_nnz, 1);
+  k.lucap = std::max<int64_t>(sh.max_lu_nnz, 1);
+  k.blobcap = std::max<int64_t>(sh.max_schedule, 0);
+  k.bpcap = std::max(sh.max_breakpoints, 1);
+  for (int t = 0; t < kTypes; ++t) {
+    k.icap[t] = std::max(sh.max_instances[t], 0);
+    k.rcap += int64_t(k.icap[t]) * type_layout(t).nterm;
+  }
+  k.rcap = std::max<int64_t>(k.rcap, 1);
+  k.ecap = 4 * int64_t(k.ucap) + 2 * k.jcap;
+  return k;
+}
+
+// Device bytes of one slot: what xg_batch_create_slots allocates per slot.
+int64_t slot_bytes(const SlotCaps &k, int precision, int n_out, int max_points) {
+  const int64_t tsz = precision == XG_LU_FP32 ? 4 : 8;
+  const int64_t u = k.ucap, j = k.jcap;
+  int64_t b = 0;
+  for (int t = 0; t < kTypes; ++t) {
+    const TypeLayout &L = type_layout(t);
+    const int64_t n = k.icap[t];
+    b += n * (8 * L.np + 4 * L.nlid + 2 * 4 + 8 * L.nterm + 3 * 8 * (L.nsta + L.nsto));
+  }
+  b += 8 * int64_t(k.icap[XG_DEV_DIODE]) + 8 * kB3Mem * int64_t(k.icap[XG_DEV_BSIM3]);
+  b += 4 * k.rcap + int64_t(sizeof(RedEntry)) * k.ecap + 2 * 4;
+  b += 8 * (4 * u + 2 * j);                 // outputs F Q dFdxdVp dQdxdVp dFdx dQdx
+  b += 8 * 3 * u;                            // solutions
+  b += 8 * 13 * u + 8 * j + 4 * u + 4 * j;   // work vectors, jac, arp, aci
+  b += 4 * u;                                // unknown list
+  b += (tsz + 4 + 8) * k.lucap + 4 * (u + 1) + 4 * 4 * u + tsz * u;  // L\U
+  b += 4 * k.blobcap;
+  b += 8 * int64_t(max_points) * (1 + std::max(1, n_out)) + 4 * std::max(1, n_out);
+  b += 8 * k.bpcap;
+  b += 2 * int64_t(sizeof(CState)) + 3 * int64_t(sizeof(Flags)) + 8 * Q_N;
+  b += 4 * (2 * kTypes) * 2 + 4 * 2 + 4 * 16;  // state/store runs, Jacobian run, per-slot ints
+  return b;
+}
+
+struct SlotPool {
+  xg_slot_shape shape{};
+  SlotCaps k;
+  int n_slots = 0, precision = XG_LU_FP64, n_out = 0, max_points = 0, n_refine = 0;
+  double tstep = 1e-12, maxstep = 0.0, reltol = 1e-3, abstol = 1e-6;
+  xg_device_options dopt{};
+  DevOptions opt{};
+  int NU = 0;               // pool unknowns; the ground is unknown NU
+  int64_t NNZ = 0;
+  int NT[kTypes] = {};
+  int64_t sta0[kTypes] = {}, sto0[kTypes] = {}, term0[kTypes] = {};
+  int64_t n_state = 0, n_store = 0, n_terms = 0, n_out_vals = 0;
+  size_t solve_smem = 0, solve_lvl = 0;
+  // device
+  double *params[kTypes] = {};
+  int *lid[kTypes] = {}, *cid[kTypes] = {}, *cid_stage[kTypes] = {};
+  double *terms = nullptr, *out = nullptr;
+  uint32_t *ref = nullptr;
+  RedEntry *ent = nullptr;
+  int *ne = nullptr, *nl = nullptr;
+  double *sol[3] = {}, *sta[3] = {}, *sto[3] = {};
+  double *diode_vd = nullptr, *b3_mem = nullptr;
+  CState *cs_next = nullptr;
+  Flags *fl_next = nullptr, *fl_stage = nullptr;
+  int *d_list = nullptr;     // the slots of one submit (restricted reduction)
+  // writable views of BatchDev's per-slot arrays
+  int *uend = nullptr, *send = nullptr, *oend = nullptr, *jend = nullptr, *bp_end = nullptr;
+  int *sidx = nullptr, *oidx = nullptr, *jidx = nullptr, *arp = nullptr, *aci = nullptr;
+  int *lrp = nullptr, *lci = nullptr, *ldiag = nullptr, *lP = nullptr, *lQ = nullptr;
+  int64_t *lu2a = nullptr, *lnz_end = nullptr, *sched_end = nullptr;
+  int *sched = nullptr, *lvl = nullptr, *out_idx = nullptr;
+  double *bp = nullptr;
+  double *work[13] = {};
+  double *jac = nullptr, *part = nullptr;
+  std::vector<void *> allocs;
+  // staging (grown on demand)
+  cudaStream_t side = nullptr;
+  cudaEvent_t ready = nullptr;
+  void *h_stage = nullptr, *d_stage = nullptr;
+  size_t stage_cap = 0;
+  double *h_jac = nullptr;  // pinned: first Jacobians read back
+  size_t h_jac_cap = 0;
+  // host state
+  std::vector<char> used;
+  std::vector<int> gen;
+  std::mutex mu;         // used / gen
+  std::mutex submit_mu;  // one submit at a time
+};
+
+int pool_gen(SlotPool *p, int slot) {
+  std::lock_guard<std::mutex> lock(p->mu);
+  return p->gen[slot];
+}
+
+void free_pool(SlotPool *p) {
+  if (!p) return;
+  if (p->side) cudaStreamSynchronize(p->side);
+  for (void *a : p->allocs) cudaFree(a);
+  if (p->d_stage) cudaFree(p->d_stage);
+  if (p->h_stage) cudaFreeHost(p->h_stage);
+  if (p->h_jac) cudaFreeHost(p->h_jac);
+  if (p->ready) cudaEventDestroy(p->ready);
+  if (p->side) cudaStreamDestroy(p->side);
+  delete p;
+}
+
+namespace {
+
+template <class V>
+int pool_alloc(SlotPool *p, V **d, int64_t n, int fill_byte = 0) {
+  const size_t bytes = sizeof(V) * size_t(std::max<int64_t>(n, 1));
+  if (cudaMalloc((void **)d, bytes) != cudaSuccess) return XG_ERR_OOM;
+  p->allocs.push_back((void *)*d);
+  return cudaMemset(*d, fill_byte, bytes) == cudaSuccess ? XG_OK : XG_ERR_CUDA;
+}
+
+template <class V>
+int pool_upload(SlotPool *p, const V **d, const std::vector<V> &h) {
+  V *x = nullptr;
+  int rc = pool_alloc(p, &x, int64_t(h.size()));
+  if (!rc && !h.empty() &&
+      cudaMemcpy(x, h.data(), sizeof(V) * h.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+    rc = XG_ERR_CUDA;
+  *d = x;
+  return rc;
+}
+
+// A host-side copy list: segments plus their payload, device addresses final.
+struct Staging {
+  std::vector<Seg> segs;
+  std::vector<uint32_t> payload;
+  void put(void *dst, const void *src, int64_t words) {
+    if (words <= 0) return;
+    Seg s{(uint32_t *)dst, int64_t(payload.size()), words, 0u, 0u};
+    segs.push_back(s);
+    const uint32_t *w = (const uint32_t *)src;
+    payload.insert(payload.end(), w, w + words);
+  }
+  void fill(void *dst, uint32_t word, int64_t words) {
+    if (words <= 0) return;
+    segs.push_back(Seg{(uint32_t *)dst, -1, words, word, 0u});
+  }
+  template <class V> void put_vec(V *dst, const std::vector<V> &v) {
+    static_assert(sizeof(V) % 4 == 0, "word-sized elements");
+    put(dst, v.data(), int64_t(v.size() * sizeof(V) / 4));
+  }
+  template <class V> void put_one(V *dst, const V &v) {
+    static_assert(sizeof(V) % 4 == 0, "word-sized elements");
+    put(dst, &v, int64_t(sizeof(V) / 4));
+  }
+  void zero_d(double *dst, int64_t n) { fill(dst, 0u, 2 * n); }
+  void append(const Staging &o) {
+    const int64_t base = int64_t(payload.size());
+    for (Seg s : o.segs) {
+      if (s.src >= 0) s.src += base;
+      segs.push_back(s);
+    }
+    payload.insert(payload.end(), o.payload.begin(), o.payload.end());
+  }
+};
+
+// Upload a copy list on the set-up stream and run it.
+int run_staging(SlotPool *p, const Staging &st) {
+  if (st.segs.empty()) return XG_OK;
+  const size_t seg_bytes = st.segs.size() * sizeof(Seg);
+  const size_t bytes = seg_bytes + st.payload.size() * 4;
+  if (bytes > p->stage_cap) {
+    if (cudaStreamSynchronize(p->side) != cudaSuccess) return XG_ERR_CUDA;
+    if (p->d_stage) cudaFree(p->d_stage);
+    if (p->h_stage) cudaFreeHost(p->h_stage);
+    p->d_stage = p->h_stage = nullptr;
+    p->stage_cap = 0;
+    const size_t cap = std::max<size_t>(bytes + bytes / 2, 1 << 20);
+    if (cudaMalloc(&p->d_stage, cap) != cudaSuccess || cudaMallocHost(&p->h_stage, cap) != cudaSuccess)
+      return XG_ERR_OOM;
+    p->stage_cap = cap;
+  }
+  // the pinned buffer is reused: the previous copy out of it has finished
+  if (cudaStreamSynchronize(p->side) != cudaSuccess) return XG_ERR_CUDA;
+  std::memcpy(p->h_stage, st.segs.data(), seg_bytes);
+  std::memcpy((char *)p->h_stage + seg_bytes, st.payload.data(), st.payload.size() * 4);
+  if (cudaMemcpyAsync(p->d_stage, p->h_stage, bytes, cudaMemcpyHostToDevice, p->side) != cudaSuccess)
+    return XG_ERR_CUDA;
+  const int nseg = int(st.segs.size());
+  const int blocks = std::min((nseg + 7) / 8, 4 * sm_count());
+  seg_copy<<<blocks, 256, 0, p->side>>>((const Seg *)p->d_stage, nseg,
+                                        (const uint32_t *)((char *)p->d_stage + seg_bytes));
+  count_launches(1);
+  return cudaGetLastError() == cudaSuccess ? XG_OK : XG_ERR_CUDA;
+}
+
+LoadIO pool_io(const SlotPool *p) {
+  return LoadIO{p->sol[0], p->sta[1], p->sto[1], p->sta[0], p->sto[0], p->terms, nullptr,
+                p->diode_vd, p->b3_mem, p->sta[1]};
+}
+
+PoolRed pool_red(const SlotPool *p) {
+  return PoolRed{p->ent, p->k.ecap, p->ne, p->nl, p->ref, p->terms, p->out};
+}
+
+// The evaluation launches over every type's whole instance array, with the
+// given circuit and flag arrays (the live ones, or the set-up ones).
+int pool_eval(const SlotPool *p, int *const *cid, const Flags *flags, cudaStream_t s) {
+  const LoadIO io = pool_io(p);
+  for (int t = 0; t < kTypes; ++t) {
+    if (!p->NT[t]) continue;
+    const TypeLayout &L = type_layout(t);
+    DevType dt{p->NT[t], L.nterm, int(p->sta0[t]), int(p->sto0[t]), p->term0[t], p->params[t],
+               p->lid[t], cid[t], flags};
+    Flags unused{};
+    const int rc = p->dopt.fma ? fast::launch_eval(t, dt, p->opt, unused, io, s)
+                               : exact::launch_eval(t, dt, p->opt, unused, io, s);
+    if (rc) return rc;
+  }
+  return XG_OK;
+}
+
+// One request, set up on the host and placed in its slot.
+struct Placed {
+  Plan P;
+  int slot = -1;
+  int gen = 0;  // which request of the slot this one is
+  std::vector<double> bp;
+  Staging st1, st2;  // before / after the first Jacobian
+  ReqLU lu;
+  int rc = XG_OK;
+  std::string err;
+};
+
+// Relocate request P into slot c: everything the set-up load and the batch
+// kernels read, except the L\U arrays.
+void stage_request(SlotPool *p, Placed &R, const double *x0, const int *out_idx) {
+  const Plan &P = R.P;
+  const SlotCaps &k = p->k;
+  const int c = R.slot, nr = P.n_unknowns;
+  const int u0 = c * k.ucap;
+  const int64_t j0 = int64_t(c) * k.jcap, r0 = int64_t(c) * k.rcap;
+  const int64_t W = int64_t(p->NU) + 1, Wr = int64_t(nr) + 1;
+  Staging &st = R.st1;
+  int ib[kTypes];
+  for (int t = 0; t < kTypes; ++t) ib[t] = c * k.icap[t];
+  // device parameters, LIDs (into the slot's unknowns; ground to the pool's),
+  // circuits of the live and set-up loads
+  std::vector<int> cs_runs, os_runs;
+  for (int t = 0; t < kTypes; ++t) {
+    const TypeData &T = P.T[t];
+    const TypeLayout &L = type_layout(t);
+    const int n = T.n;
+    if (n) {
+      for (int q = 0; q < L.np; ++q)
+        st.put(p->params[t] + int64_t(q) * p->NT[t] + ib[t], T.params.data() + int64_t(q) * n, 2 * int64_t(n));
+      std::vector<int> rl(size_t(L.nlid) * n);
+      for (size_t j = 0; j < rl.size(); ++j) rl[j] = T.lid[j] == nr ? p->NU : u0 + T.lid[j];
+      for (int q = 0; q < L.nlid; ++q)
+        st.put(p->lid[t] + int64_t(q) * p->NT[t] + ib[t], rl.data() + int64_t(q) * n, n);
+      st.fill(p->cid_stage[t] + ib[t], uint32_t(c), n);
+    }
+    if (k.icap[t]) {
+      st.fill(p->cid[t] + ib[t], uint32_t(c), n);
+      st.fill(p->cid[t] + ib[t] + n, 0xffffffffu, k.icap[t] - n);
+      for (int v = 0; v < 3; ++v) {
+        if (L.nsta) st.zero_d(p->sta[v] + p->sta0[t] + int64_t(ib[t]) * L.nsta, int64_t(k.icap[t]) * L.nsta);
+        if (L.nsto) st.zero_d(p->sto[v] + p->sto0[t] + int64_t(ib[t]) * L.nsto, int64_t(k.icap[t]) * L.nsto);
+      }
+    }
+    if (n && L.nsta && t != XG_DEV_DIODE) {
+      cs_runs.push_back(int(p->sta0[t] + int64_t(ib[t]) * L.nsta));
+      cs_runs.push_back(n * L.nsta);
+    }
+    if (n && L.nsto) {
+      os_runs.push_back(int(p->sto0[t] + int64_t(ib[t]) * L.nsto));
+      os_runs.push_back(n * L.nsto);
+    }
+  }
+  if (k.icap[XG_DEV_DIODE]) st.zero_d(p->diode_vd + ib[XG_DEV_DIODE], k.icap[XG_DEV_DIODE]);
+  if (k.icap[XG_DEV_BSIM3])
+    for (int q = 0; q < kB3Mem; ++q)
+      st.zero_d(p->b3_mem + int64_t(q) * p->NT[XG_DEV_BSIM3] + ib[XG_DEV_BSIM3], k.icap[XG_DEV_BSIM3]);
+  // reduction: the request's lists, terms and outputs renumbered into the pool
+  std::vector<uint32_t> ref(P.red_idx.size());
+  {
+    int64_t lo[kTypes], hi[kTypes];
+    for (int t = 0; t < kTypes; ++t) {
+      lo[t] = P.T[t].term0;
+      hi[t] = P.T[t].n ? P.T[t].term0 + int64_t(P.T[t].n) * P.T[t].nterm : lo[t];
+    }
+    for (size_t j = 0; j < ref.size(); ++j) {
+      const int64_t tau = P.red_idx[j];
+      int t = 0;
+      while (t < kTypes - 1 && !(P.T[t].n && tau >= lo[t] && tau < hi[t])) ++t;
+      const int64_t off = tau - lo[t], n = P.T[t].n;
+      ref[j] = uint32_t(p->term0[t] + (off / n) * p->NT[t] + ib[t] + off % n);
+    }
+  }
+  st.put_vec(p->ref + r0, ref);
+  std::vector<RedEntry> lng, sht;
+  for (int64_t o = 0; o < P.n_out; ++o) {
+    const int64_t b0 = P.red_ptr[o], cnt = P.red_ptr[o + 1] - b0;
+    if (!cnt) continue;
+    int64_t po;
+    if (o < 4 * Wr) {
+      po = (o / Wr) * W + u0 + o % Wr;
+    } else {
+      const int64_t e = o - 4 * Wr;
+      po = e < P.nnz ? 4 * W + j0 + e : 4 * W + p->NNZ + j0 + (e - P.nnz);
+    }
+    RedEntry re{po, r0 + b0, int32_t(cnt), 0};
+    (cnt > kLongOut ? lng : sht).push_back(re);
+  }
+  std::stable_sort(sht.begin(), sht.end(), [](const RedEntry &a, const RedEntry &b2) { return a.cnt < b2.cnt; });
+  const int nlong = int(lng.size());
+  lng.insert(lng.end(), sht.begin(), sht.end());
+  st.put_vec(p->ent + int64_t(c) * k.ecap, lng);
+  st.put_one(p->ne + c, int(lng.size()));
+  st.put_one(p->nl + c, nlong);
+  for (int q = 0; q < 4; ++q) st.zero_d(p->out + q * W + u0, k.ucap);
+  st.zero_d(p->out + 4 * W + j0, k.jcap);
+  st.zero_d(p->out + 4 * W + p->NNZ + j0, k.jcap);
+  // solutions x0 (ground excluded), work vectors and histories zero
+  std::vector<double> xs(size_t(k.ucap), 0.0);
+  if (x0) std::copy(x0, x0 + nr, xs.begin());
+  for (int v = 0; v < 3; ++v) st.put(p->sol[v] + u0, xs.data(), 2 * int64_t(k.ucap));
+  for (double *w : p->work) st.zero_d(w + u0, k.ucap);
+  st.zero_d(p->jac + j0, k.jcap);
+  st.zero_d(p->part + int64_t(c) * Q_N, Q_N);
+  // Jacobian pattern of the slot's rows
+  std::vector<int> ap(size_t(k.ucap)), ac(size_t(P.nnz));
+  for (int r = 0; r < k.ucap; ++r) ap[r] = int(j0 + P.rowptr[std::min(r, nr)]);
+  for (int64_t e = 0; e < P.nnz; ++e) ac[e] = u0 + P.colidx[e];
+  st.put_vec(p->arp + u0, ap);
+  st.put_vec(p->aci + j0, ac);
+  // the request's ranges
+  st.put_one(p->uend + c, u0 + nr);
+  st.put_one(p->jend + c, c + (P.nnz > 0 ? 1 : 0));
+  const int jr[2] = {int(j0), int(P.nnz)};
+  st.put(p->jidx + 2 * c, jr, 2);
+  st.put_vec(p->sidx + 2 * kTypes * c, cs_runs);
+  st.put_one(p->send + c, kTypes * c + int(cs_runs.size() / 2));
+  st.put_vec(p->oidx + 2 * kTypes * c, os_runs);
+  st.put_one(p->oend + c, kTypes * c + int(os_runs.size() / 2));
+  st.put_vec(p->bp + int64_t(c) * k.bpcap, R.bp);
+  st.put_one(p->bp_end + c, c * k.bpcap + int(R.bp.size()));
+  if (p->n_out) {
+    std::vector<int> oi(size_t(p->n_out));
+    for (int j = 0; j < p->n_out; ++j) oi[j] = u0 + out_idx[j];
+    st.put_vec(p->out_idx + int64_t(c) * p->n_out, oi);
+  }
+  // no L\U yet: empty ranges, the walker path
+  st.put_one(p->lnz_end + c, int64_t(c) * k.lucap);
+  st.put_one(p->sched_end + c, int64_t(c) * k.blobcap);
+  st.put_one(p->lvl + c, 0);
+  // the set-up load's flags: a transient load at x0 with pdt = 1/tstep
+  Flags fs{};
+  fs.transient = 1;
+  fs.pdt = 1.0 / p->tstep;
+  st.put_one(p->fl_stage + c, fs);
+}
+
+// The L\U arrays of a placed request, its reset state and its starting
+// request state.
+void stage_lu(SlotPool *p, Placed &R, double tstop) {
+  const Plan &P = R.P;
+  const SlotCaps &k = p->k;
+  const int c = R.slot, nr = P.n_unknowns;
+  const int u0 = c * k.ucap;
+  const int64_t j0 = int64_t(c) * k.jcap, z0 = int64_t(c) * k.lucap;
+  const LuSymbolic &S = R.lu.S;
+  Staging &st = R.st2;
+  st.put_vec(p->lrp + int64_t(c) * (k.ucap + 1), S.rp);
+  st.put_vec(p->lci + z0, S.ci);
+  st.put_vec(p->ldiag + u0, S.diag);
+  std::vector<int64_t> l2a(S.lu2a.size());
+  for (size_t q = 0; q < l2a.size(); ++q) l2a[q] = S.lu2a[q] >= 0 ? j0 + S.lu2a[q] : -1;
+  st.put_vec(p->lu2a + z0, l2a);
+  st.put_vec(p->lP + u0, S.P);
+  st.put_vec(p->lQ + u0, S.Q);
+  st.put_one(p->lnz_end + c, z0 + int64_t(S.rp[nr]));
+  const size_t tsz = p->precision == XG_LU_FP32 ? sizeof(float) : sizeof(double);
+  const bool lvl = p->solve_lvl && int64_t(R.lu.blob.size()) <= k.blobcap &&
+                   smem_bytes_lvl(nr, S.rp[nr], int64_t(R.lu.blob.size()), tsz) <= p->solve_lvl;
+  if (lvl) st.put_vec(p->sched + int64_t(c) * k.blobcap, R.lu.blob);
+  st.put_one(p->sched_end + c, int64_t(c) * k.blobcap + (lvl ? int64_t(R.lu.blob.size()) : 0));
+  st.put_one(p->lvl + c, lvl ? 1 : 0);
+  // the set-up load wrote state, store and members: start again from zero,
+  // and take the slot out of the set-up load
+  for (int t = 0; t < kTypes; ++t) {
+    const TypeLayout &L = type_layout(t);
+    const int ib = c * k.icap[t];
+    if (!k.icap[t]) continue;
+    for (int v = 0; v < 3; ++v) {
+      if (L.nsta) st.zero_d(p->sta[v] + p->sta0[t] + int64_t(ib) * L.nsta, int64_t(k.icap[t]) * L.nsta);
+      if (L.nsto) st.zero_d(p->sto[v] + p->sto0[t] + int64_t(ib) * L.nsto, int64_t(k.icap[t]) * L.nsto);
+    }
+    st.fill(p->cid_stage[t] + ib, 0xffffffffu, k.icap[t]);
+  }
+  if (k.icap[XG_DEV_DIODE]) st.zero_d(p->diode_vd + c * k.icap[XG_DEV_DIODE], k.icap[XG_DEV_DIODE]);
+  if (k.icap[XG_DEV_BSIM3])
+    for (int q = 0; q < kB3Mem; ++q)
+      st.zero_d(p->b3_mem + int64_t(q) * p->NT[XG_DEV_BSIM3] + c * k.icap[XG_DEV_BSIM3], k.icap[XG_DEV_BSIM3]);
+  // the starting request state (as a batch of its own starts it)
+  CState cs;
+  std::memset(&cs, 0, sizeof(cs));
+  cs.tstop = tstop;
+  cs.tstep = p->tstep;
+  cs.max_step = p->maxstep > 0 ? p->maxstep : 0.1 * tstop;
+  cs.reltol = p->reltol;
+  cs.abstol = p->abstol;
+  cs.saved = 1e-10;
+  cs.phase = PH_INIT;
+  cs.first_step = 1;
+  cs.beginning = 1;
+  cs.order = 1;
+  cs.loads = 1;
+  cs.gen = R.gen;
+  st.put_one(p->cs_next + c, cs);
+  Flags f{};
+  f.dcop = 1;
+  f.tranop = 1;
+  st.put_one(p->fl_next + c, f);
+}
+
+// Host work spread over threads (each request is independent).
+template <class F>
+void for_each_parallel(int n, F f) {
+  const int nt = std::max(1, std::min<int>(std::min(16, n), int(std::thread::hardware_concurrency())));
+  std::atomic<int> next{0};
+  auto worker = [&]() {
+    for (int i = next++; i < n; i = next++) f(i);
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nt; ++t) pool.emplace_back(worker);
+  worker();
+  for (auto &t : pool) t.join();
+}
+
+// Set up, shape-check and measure one request on the host.
+int plan_request(const xg_device_options &dopt, const xg_netlist *nl, double tstop, Placed *R) {
+  std::string err;
+  int rc = build_plan(nl, &dopt, &R->P, &err);
+  if (rc) {
+    R->err = err;
+    return rc;
+  }
+  R->bp = pulse_breakpoints(R->P, tstop);
+  return XG_OK;
+}
+
+int check_fits(const SlotCaps &k, const Placed &R) {
+  const Plan &P = R.P;
+  if (P.n_unknowns + 1 > k.ucap || P.nnz > k.jcap || int64_t(R.bp.size()) > k.bpcap) return XG_ERR_ARG;
+  for (int t = 0; t < kTypes; ++t)
+    if (P.T[t].n > k.icap[t]) return XG_ERR_ARG;
+  return XG_OK;
+}
+
+}  // namespace
+
+// One iteration of a slotted batch: the solves, the pool's load, combine,
+// control and vector.
+int enqueue_pool_iteration(xg_batch *b) {
+  SlotPool *p = b->pool;
+  cudaStream_t s = b->stream;
+  const int nc = b->nc;
+  if (p->solve_smem) {
+    if (p->precision == XG_LU_FP32) batch_solve_smem<float><<<nc, 32, p->solve_smem, s>>>(b->dev);
+    else batch_solve_smem<double><<<nc, 32, p->solve_smem, s>>>(b->dev);
+  } else {
+    if (p->precision == XG_LU_FP32) batch_solve<float><<<(nc + 3) / 4, 128, 0, s>>>(b->dev);
+    else batch_solve<double><<<(nc + 3) / 4, 128, 0, s>>>(b->dev);
+  }
+  count_launches(1);
+  if (p->solve_lvl) {
+    if (p->precision == XG_LU_FP32) batch_solve_lvl<float><<<nc, kLvlThreads, p->solve_lvl, s>>>(b->dev);
+    else batch_solve_lvl<double><<<nc, kLvlThreads, p->solve_lvl, s>>>(b->dev);
+    count_launches(1);
+  }
+  int rc = pool_eval(p, p->cid, b->dev.flags, s);
+  if (rc) return rc;
+  pool_reduce<<<nc, 256, 0, s>>>(pool_red(p), b->dev.cs, nullptr);
+  batch_combine<<<nc, kBatchThreads, 0, s>>>(b->dev);
+  batch_control<<<(nc + 31) / 32, 32, 0, s>>>(b->dev);
+  batch_vector<<<nc, kVectorThreads, 0, s>>>(b->dev);
+  count_launches(4);
+  return cudaGetLastError() == cudaSuccess ? XG_OK : XG_ERR_CUDA;
+}
+
+}  // namespace xg
+
+// ---- C ABI of slotted batches -------------------------------------------------
+
+extern "C" int xg_slot_bytes(const xg_slot_shape *shape, const xg_batch_options *o, int64_t *bytes) {
+  if (!shape || !o || !bytes || shape->max_unknowns <= 0 || o->max_points <= 0 || o->n_out < 0) {
+    xg::set_error("xg_slot_bytes: bad argument");
+    return XG_ERR_ARG;
+  }
+  *bytes = xg::slot_bytes(xg::slot_caps(*shape), o->lu_precision, o->n_out, o->max_points);
+  return XG_OK;
+}
+
+extern "C" int xg_mem_info(xg_ctx *ctx, int64_t *free_bytes, int64_t *total_bytes) {
+  int device = 0;
+  void *stream = nullptr;
+  if (!ctx || xg::ctx_info(ctx, &device, &stream)) {
+    xg::set_error("xg_mem_info: bad argument");
+    return XG_ERR_ARG;
+  }
+  int cur = 0;
+  cudaGetDevice(&cur);
+  if (cur != device) cudaSetDevice(device);
+  size_t f = 0, t = 0;
+  const cudaError_t e = cudaMemGetInfo(&f, &t);
+  if (cur != device) cudaSetDevice(cur);
+  if (e != cudaSuccess) {
+    xg::set_error(std::string("xg_mem_info: ") + cudaGetErrorString(e));
+    return XG_ERR_CUDA;
+  }
+  if (free_bytes) *free_bytes = int64_t(f);
+  if (total_bytes) *total_bytes = int64_t(t);
+  return XG_OK;
+}
+
+extern "C" int xg_slot_need(xg_ctx *ctx, const xg_netlist *nl, const double *x0, double tstop,
+                            double tstep, xg_slot_shape *need) {
+  using namespace xg;
+  if (!ctx || !nl || !need || !(tstop > 0) || !(tstep > 0)) {
+    set_error("xg_slot_need: bad argument");
+    return XG_ERR_ARG;
+  }
+  xg_device_options dopt;
+  ctx_options(ctx, &dopt);
+  Placed R;
+  int rc = plan_request(dopt, nl, tstop, &R);
+  if (rc) {
+    set_error("xg_slot_need: " + R.err);
+    return rc;
+  }
+  const Plan &P = R.P;
+  // the first Jacobian, from a circuit of its own
+  xg_circuit *ck = nullptr;
+  if ((rc = xg_circuit_create(ctx, nl, &ck))) return rc;
+  std::vector<double> xu(size_t(P.n_unknowns) + 1, 0.0);
+  if (x0) std::copy(x0, x0 + P.n_unknowns, xu.begin());
+  std::vector<double> dfdx(size_t(std::max<int64_t>(P.nnz, 1))), dqdx(dfdx.size());
+  for (int id : {XG_VEC_SOL_NEXT, XG_VEC_SOL_CURR, XG_VEC_SOL_LAST})
+    if (!rc) rc = xg_vec_upload(ck, id, xu.data());
+  xg_load_flags fl{};
+  fl.transient = 1;
+  fl.pdt = 1.0 / tstep;
+  if (!rc) rc = xg_load(ck, &fl);
+  if (!rc) rc = xg_vec_download(ck, XG_VEC_DFDX, dfdx.data());
+  if (!rc) rc = xg_vec_download(ck, XG_VEC_DQDX, dqdx.data());
+  xg_circuit_destroy(ck);
+  if (rc) return rc;
+  std::vector<double> val(size_t(P.nnz));
+  for (int r = 0; r < P.n_unknowns; ++r)
+    for (int e = P.rowptr[r]; e < P.rowptr[r + 1]; ++e) {
+      double a = dfdx[e] + dqdx[e] / tstep;
+      if (P.colidx[e] == r && a == 0.0) a = 1e-12;
+      val[e] = a;
+    }
+  analyse_request(P.n_unknowns, P.rowptr, P.colidx, val, "xg_slot_need", &R.lu);
+  if (R.lu.rc) {
+    set_error(R.lu.err);
+    return R.lu.rc;
+  }
+  std::memset(need, 0, sizeof(*need));
+  need->max_unknowns = P.n_unknowns;
+  for (int t = 0; t < kTypes; ++t) need->max_instances[t] = P.T[t].n;
+  need->max_nnz = P.nnz;
+  need->max_lu_nnz = R.lu.S.rp[P.n_unknowns];
+  need->max_schedule = int64_t(R.lu.blob.size());
+  need->max_breakpoints = int(R.bp.size());
+  return XG_OK;
+}
+
+extern "C" int xg_batch_create_slots(xg_ctx *ctx, int n_slots, const xg_slot_shape *shape,
+                                     const xg_batch_options *o, xg_batch **out) {
+  using namespace xg;
+  if (!ctx || n_slots <= 0 || !shape || shape->max_unknowns <= 0 || !o || !out || o->max_points <= 0 ||
+      o->n_out < 0 || (o->lu_precision != XG_LU_FP64 && o->lu_precision != XG_LU_FP32) ||
+      o->n_refine < 0 || n_slots > (1 << 20)) {
+    set_error("xg_batch_create_slots: bad argument");
+    return XG_ERR_ARG;
+  }
+  *out = nullptr;
+  std::unique_ptr<xg_batch, void (*)(xg_batch *)> b(new xg_batch, [](xg_batch *q) {
+    free_batch(q);
+    delete q;
+  });
+  b->ctx = ctx;
+  b->nc = n_slots;
+  b->n_out = o->n_out;
+  b->max_points = o->max_points;
+  b->precision = o->lu_precision;
+  SlotPool *p = new SlotPool;
+  b->pool = p;
+  p->shape = *shape;
+  p->k = slot_caps(*shape);
+  const SlotCaps &k = p->k;
+  p->n_slots = n_slots;
+  p->precision = o->lu_precision;
+  p->n_out = o->n_out;
+  p->max_points = o->max_points;
+  p->n_refine = o->lu_precision == XG_LU_FP32 ? o->n_refine : 0;
+  p->tstep = o->tstep > 0 ? o->tstep : 1e-12;
+  p->maxstep = o->maxstep;
+  p->reltol = o->reltol > 0 ? o->reltol : 1e-3;
+  p->abstol = o->abstol > 0 ? o->abstol : 1e-6;
+  ctx_options(ctx, &p->dopt);
+  p->opt = DevOptions{p->dopt.gmin, p->dopt.voltlim};
+  const int64_t ns = n_slots;
+  if (ns * k.ucap >= (int64_t(1) << 31) - 1 || ns * k.jcap >= (int64_t(1) << 31) ||
+      ns * k.lucap >= (int64_t(1) << 40)) {
+    set_error("xg_batch_create_slots: too many slots for the shape");
+    return XG_ERR_ARG;
+  }
+  p->NU = int(ns * k.ucap);
+  p->NNZ = ns * k.jcap;
+  int64_t sta = 0, sto = 0, term = 0;
+  for (int t = 0; t < kTypes; ++t) {
+    const TypeLayout &L = type_layout(t);
+    p->NT[t] = int(ns * k.icap[t]);
+    p->sta0[t] = sta;
+    p->sto0[t] = sto;
+    p->term0[t] = term;
+    sta += int64_t(p->NT[t]) * L.nsta;
+    sto += int64_t(p->NT[t]) * L.nsto;
+    term += int64_t(p->NT[t]) * L.nterm;
+  }
+  p->n_state = sta;
+  p->n_store = sto;
+  p->n_terms = term;
+  if (sta >= (int64_t(1) << 31) || sto >= (int64_t(1) << 31) || term >= (int64_t(1) << 32) - 1) {
+    set_error("xg_batch_create_slots: too many slots for the shape");
+    return XG_ERR_ARG;
+  }
+  const int64_t W = int64_t(p->NU) + 1;
+  p->n_out_vals = 4 * W + 2 * p->NNZ;
+  const size_t tsz = o->lu_precision == XG_LU_FP32 ? sizeof(float) : sizeof(double);
+  int device = 0;
+  void *ctx_stream = nullptr;
+  ctx_info(ctx, &device, &ctx_stream);
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&p->ready, cudaEventDisableTiming) != cudaSuccess) {
+    set_error("xg_batch_create_slots: stream creation failed");
+    return XG_ERR_CUDA;
+  }
+  auto oom = [&]() {
+    set_error("xg_batch_create_slots: out of device memory");
+    return XG_ERR_OOM;
+  };
+  // device arrays; circuits -1 (no instance), everything else zero
+  for (int t = 0; t < kTypes; ++t) {
+    const TypeLayout &L = type_layout(t);
+    if (!p->NT[t]) continue;
+    if (pool_alloc(p, &p->params[t], int64_t(L.np) * p->NT[t]) ||
+        pool_alloc(p, &p->lid[t], int64_t(L.nlid) * p->NT[t]) ||
+        pool_alloc(p, &p->cid[t], p->NT[t], 0xff) || pool_alloc(p, &p->cid_stage[t], p->NT[t], 0xff))
+      return oom();
+  }
+  if (pool_alloc(p, &p->terms, p->n_terms) || pool_alloc(p, &p->out, p->n_out_vals) ||
+      pool_alloc(p, &p->ref, ns * k.rcap) || pool_alloc(p, &p->ent, ns * k.ecap) ||
+      pool_alloc(p, &p->ne, ns) || pool_alloc(p, &p->nl, ns) ||
+      pool_alloc(p, &p->diode_vd, p->NT[XG_DEV_DIODE]) ||
+      pool_alloc(p, &p->b3_mem, int64_t(kB3Mem) * p->NT[XG_DEV_BSIM3]) ||
+      pool_alloc(p, &p->cs_next, ns) || pool_alloc(p, &p->fl_next, ns) || pool_alloc(p, &p->fl_stage, ns) ||
+      pool_alloc(p, &p->d_list, ns))
+    return oom();
+  for (int v = 0; v < 3; ++v)
+    if (pool_alloc(p, &p->sol[v], W) || pool_alloc(p, &p->sta[v], p->n_state) ||
+        pool_alloc(p, &p->sto[v], p->n_store))
+      return oom();
+  BatchDev &d = b->dev;
+  d.nc = n_slots;
+  d.n_out = o->n_out;
+  d.max_points = o->max_points;
+  d.n_refine = p->n_refine;
+  // fixed starts of each slot's regions
+  std::vector<int> uptr(ns), sptr(ns), jptr(ns), lrp_off(ns), bp_ptr(ns), uidx(size_t(p->NU));
+  std::vector<int64_t> lnz_off(ns), sched_off(ns);
+  for (int c = 0; c < n_slots; ++c) {
+    uptr[c] = c * k.ucap;
+    sptr[c] = c * kTypes;
+    jptr[c] = c;
+    lrp_off[c] = c * (k.ucap + 1);
+    bp_ptr[c] = c * k.bpcap;
+    lnz_off[c] = int64_t(c) * k.lucap;
+    sched_off[c] = int64_t(c) * k.blobcap;
+  }
+  for (int u = 0; u < p->NU; ++u) uidx[u] = u;
+  if (pool_upload(p, &d.uptr, uptr) || pool_upload(p, &d.uidx, uidx) || pool_upload(p, &d.sptr, sptr) ||
+      pool_upload(p, &d.optr, sptr) || pool_upload(p, &d.jptr, jptr) || pool_upload(p, &d.lrp_off, lrp_off) ||
+      pool_upload(p, &d.lnz_off, lnz_off) || pool_upload(p, &d.sched_off, sched_off) ||
+      pool_upload(p, &d.bp_ptr, bp_ptr))
+    return oom();
+  // the request's ends start equal to the starts (empty)
+  if (pool_alloc(p, &p->uend, ns) || pool_alloc(p, &p->send, ns) || pool_alloc(p, &p->oend, ns) ||
+      pool_alloc(p, &p->jend, ns) || pool_alloc(p, &p->bp_end, ns) || pool_alloc(p, &p->lnz_end, ns) ||
+      pool_alloc(p, &p->sched_end, ns) || pool_alloc(p, &p->lvl, ns) ||
+      pool_alloc(p, &p->sidx, 2 * kTypes * ns) || pool_alloc(p, &p->oidx, 2 * kTypes * ns) ||
+      pool_alloc(p, &p->jidx, 2 * ns) || pool_alloc(p, &p->arp, W) || pool_alloc(p, &p->aci, p->NNZ) ||
+      pool_alloc(p, &p->lrp, ns * (k.ucap + 1)) || pool_alloc(p, &p->lci, ns * k.lucap) ||
+      pool_alloc(p, &p->ldiag, p->NU) || pool_alloc(p, &p->lP, p->NU) || pool_alloc(p, &p->lQ, p->NU) ||
+      pool_alloc(p, &p->lu2a, ns * k.lucap) || pool_alloc(p, &p->sched, std::max<int64_t>(ns * k.blobcap, 1)) ||
+      pool_alloc(p, &p->out_idx, ns * std::max(1, o->n_out)) || pool_alloc(p, &p->bp, ns * k.bpcap))
+    return oom();
+  if (cudaMemcpy(p->uend, uptr.data(), 4 * ns, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(p->send, sptr.data(), 4 * ns, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(p->oend, sptr.data(), 4 * ns, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(p->jend, jptr.data(), 4 * ns, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(p->bp_end, bp_ptr.data(), 4 * ns, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(p->lnz_end, lnz_off.data(), 8 * ns, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(p->sched_end, sched_off.data(), 8 * ns, cudaMemcpyHostToDevice) != cudaSuccess) {
+    set_error("xg_batch_create_slots: copy failed");
+    return XG_ERR_CUDA;
+  }
+  d.uend = p->uend; d.send = p->send; d.oend = p->oend; d.jend = p->jend; d.bp_end = p->bp_end;
+  d.lnz_end = p->lnz_end; d.sched_end = p->sched_end;
+  d.sidx = p->sidx; d.oidx = p->oidx; d.jidx = p->jidx; d.arp = p->arp; d.aci = p->aci;
+  d.lrp = p->lrp; d.lci = p->lci; d.ldiag = p->ldiag; d.lu2a = p->lu2a; d.lP = p->lP; d.lQ = p->lQ;
+  d.sched = p->sched; d.lvl = p->lvl; d.out_idx = p->out_idx; d.bp = p->bp;
+  {
+    void *pv = nullptr, *pr = nullptr;
+    int *pm = nullptr;
+    if (cudaMalloc(&pv, tsz * size_t(ns * k.lucap)) != cudaSuccess) return oom();
+    p->allocs.push_back(pv);
+    if (cudaMalloc(&pr, tsz * size_t(std::max(p->NU, 1))) != cudaSuccess) return oom();
+    p->allocs.push_back(pr);
+    if (pool_alloc(p, &pm, p->NU)) return oom();
+    d.lval = pv;
+    d.lrd = pr;
+    d.map = pm;
+  }
+  double **wv[13] = {&d.y, &d.r, &d.dd, &d.rhs, &d.dx, &d.w, &d.xh0, &d.xh1, &d.xh2,
+                     &d.qh0, &d.qh1, &d.qh2, &d.xn0};
+  for (int q = 0; q < 13; ++q) {
+    if (pool_alloc(p, wv[q], W)) return oom();
+    p->work[q] = *wv[q];
+  }
+  if (pool_alloc(p, &d.jac, p->NNZ) || pool_alloc(p, &d.part, ns * Q_N) ||
+      pool_alloc(p, &d.rec_t, ns * o->max_points) ||
+      pool_alloc(p, &d.rec_v, ns * o->max_points * std::max(1, o->n_out)))
+    return oom();
+  p->jac = d.jac;
+  p->part = d.part;
+  d.x = p->sol[0]; d.xc = p->sol[1]; d.xl = p->sol[2];
+  d.sta = p->sta[0]; d.stac = p->sta[1]; d.stal = p->sta[2];
+  d.sto = p->sto[0]; d.stoc = p->sto[1]; d.stol = p->sto[2];
+  d.f = p->out; d.q = p->out + W; d.fvp = p->out + 2 * W; d.qvp = p->out + 3 * W;
+  d.dfdx = p->out + 4 * W; d.dqdx = p->out + 4 * W + p->NNZ;
+  // request states: every slot free (phase done) and skipped by the load
+  {
+    std::vector<Flags> fl(ns);
+    for (auto &f : fl) {
+      f = Flags{};
+      f.skip = 1;
+    }
+    CState *t_cs = nullptr;
+    Flags *t_fl = nullptr;
+    if (pool_alloc(p, &t_cs, ns) || pool_alloc(p, &t_fl, ns)) return oom();
+    if (cudaMemcpy(t_fl, fl.data(), sizeof(Flags) * ns, cudaMemcpyHostToDevice) != cudaSuccess) {
+      set_error("xg_batch_create_slots: copy failed");
+      return XG_ERR_CUDA;
+    }
+    d.cs = t_cs;
+    d.flags = t_fl;
+  }
+  if (cudaMallocHost((void **)&b->h_cs, sizeof(CState) * ns) != cudaSuccess) {
+    set_error("xg_batch_create_slots: out of pinned host memory");
+    return XG_ERR_OOM;
+  }
+  std::memset(b->h_cs, 0, sizeof(CState) * ns);
+  // the solves: shared-memory paths sized for the shape
+  {
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    const size_t need_w = smem_bytes_request(k.ucap, k.lucap, tsz);
+    if (need_w + 1024 <= size_t(optin) && !std::getenv("XG_BATCH_NO_SMEM")) {
+      cudaError_t e = o->lu_precision == XG_LU_FP32
+                          ? cudaFuncSetAttribute(batch_solve_smem<float>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(need_w))
+                          : cudaFuncSetAttribute(batch_solve_smem<double>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(need_w));
+      if (e == cudaSuccess) p->solve_smem = need_w;
+      else cudaGetLastError();
+    }
+    const size_t need_l = smem_bytes_lvl(k.ucap, k.lucap, k.blobcap, tsz);
+    if (k.blobcap > 0 && need_l + 1024 <= size_t(optin) && !std::getenv("XG_BATCH_NO_LVL")) {
+      cudaError_t e = o->lu_precision == XG_LU_FP32
+                          ? cudaFuncSetAttribute(batch_solve_lvl<float>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(need_l))
+                          : cudaFuncSetAttribute(batch_solve_lvl<double>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(need_l));
+      if (e == cudaSuccess) p->solve_lvl = need_l;
+      else cudaGetLastError();
+    }
+  }
+  if (cudaDeviceSynchronize() != cudaSuccess) {
+    set_error("xg_batch_create_slots: set-up failed");
+    return XG_ERR_CUDA;
+  }
+  p->used.assign(ns, 0);
+  p->gen.assign(ns, 0);
+  b->bytes = 0;
+  {
+    int64_t per = slot_bytes(k, o->lu_precision, o->n_out, o->max_points);
+    b->bytes = per * ns + 8 * 4;  // the ground entries of the vectors
+  }
+  *out = b.release();
+  return XG_OK;
+}
+
+extern "C" int xg_batch_submit(xg_batch *b, int n, const xg_netlist *const *nls, const double *const *x0,
+                               const double *tstop, const int *const *out_idx, int *slots) {
+  using namespace xg;
+  if (!b || !b->pool || n < 0 || (n && (!nls || !tstop || !slots)) || (n && b->n_out && !out_idx)) {
+    set_error("xg_batch_submit: bad argument");
+    return XG_ERR_ARG;
+  }
+  SlotPool *p = b->pool;
+  // one submit at a time per batch; the slot bookkeeping below is also read
+  // by results / release / slots on other threads, under p->mu only briefly
+  std::lock_guard<std::mutex> one(p->submit_mu);
+  for (int i = 0; i < n; ++i) slots[i] = -1;
+  std::vector<int> free_slots;
+  {
+    std::lock_guard<std::mutex> lock(p->mu);
+    for (int c = 0; c < p->n_slots && int(free_slots.size()) < n; ++c)
+      if (!p->used[c]) {
+        free_slots.push_back(c);
+        p->used[c] = 2;  // being set up
+      }
+  }
+  const int m = int(free_slots.size());
+  if (!m) return XG_OK;
+  // on any failure the chosen slots go back to free (never activated)
+  struct Unreserve {
+    SlotPool *p;
+    const std::vector<int> *slots;
+    bool keep = false;
+    ~Unreserve() {
+      if (keep) return;
+      std::lock_guard<std::mutex> lock(p->mu);
+      for (int c : *slots) p->used[c] = 0;
+    }
+  } unreserve{p, &free_slots};
+  std::vector<Placed> req(m);
+  for (int i = 0; i < m; ++i) req[i].slot = free_slots[i];
+  // set-up and relocation on the host
+  for_each_parallel(m, [&](int i) {
+    Placed &R = req[i];
+    if (!(tstop[i] > 0) || !nls[i]) {
+      R.rc = XG_ERR_ARG;
+      R.err = "bad request";
+      return;
+    }
+    R.rc = plan_request(p->dopt, nls[i], tstop[i], &R);
+    if (!R.rc && check_fits(p->k, R)) {
+      R.rc = XG_ERR_ARG;
+      R.err = "larger than the batch's slot shape";
+    }
+    if (!R.rc && p->n_out)
+      for (int j = 0; j < p->n_out; ++j)
+        if (out_idx[i][j] < 0 || out_idx[i][j] >= R.P.n_unknowns) {
+          R.rc = XG_ERR_ARG;
+          R.err = "output index out of range";
+        }
+    if (!R.rc) stage_request(p, R, x0 ? x0[i] : nullptr, p->n_out ? out_idx[i] : nullptr);
+  });
+  for (int i = 0; i < m; ++i)
+    if (req[i].rc) {
+      set_error("xg_batch_submit: request " + std::to_string(i) + ": " + req[i].err);
+      return req[i].rc;
+    }
+  // the slots' data, then their first Jacobian, on the set-up stream
+  Staging st;
+  for (auto &R : req) {
+    st.append(R.st1);
+    R.st1 = Staging{};
+  }
+  st.put(p->d_list, free_slots.data(), m);  // the slots of the restricted reduction
+  int rc = XG_OK;
+  {
+    std::lock_guard<std::mutex> launch(launch_mutex());
+    rc = run_staging(p, st);
+    if (!rc) rc = pool_eval(p, p->cid_stage, p->fl_stage, p->side);
+    if (!rc) {
+      pool_reduce<<<m, 256, 0, p->side>>>(pool_red(p), nullptr, p->d_list);
+      count_launches(1);
+      if (cudaGetLastError() != cudaSuccess) rc = XG_ERR_CUDA;
+    }
+  }
+  // read the slots' dF/dx and dQ/dx back
+  int64_t tot = 0;
+  for (auto &R : req) tot += 2 * R.P.nnz;
+  if (!rc && size_t(tot) > p->h_jac_cap) {
+    if (p->h_jac) cudaFreeHost(p->h_jac);
+    p->h_jac = nullptr;
+    p->h_jac_cap = 0;
+    if (cudaMallocHost((void **)&p->h_jac, sizeof(double) * size_t(std::max<int64_t>(tot, 1))) != cudaSuccess)
+      rc = XG_ERR_OOM;
+    else
+      p->h_jac_cap = size_t(std::max<int64_t>(tot, 1));
+  }
+  std::vector<int64_t> joff(m + 1, 0);
+  for (int i = 0; i < m; ++i) joff[i + 1] = joff[i] + 2 * req[i].P.nnz;
+  if (!rc) {
+    const int64_t W = int64_t(p->NU) + 1;
+    for (int i = 0; i < m && !rc; ++i) {
+      const int64_t j0 = int64_t(req[i].slot) * p->k.jcap, nz = req[i].P.nnz;
+      if (!nz) continue;
+      if (cudaMemcpyAsync(p->h_jac + joff[i], p->out + 4 * W + j0, sizeof(double) * nz,
+                          cudaMemcpyDeviceToHost, p->side) != cudaSuccess ||
+          cudaMemcpyAsync(p->h_jac + joff[i] + nz, p->out + 4 * W + p->NNZ + j0, sizeof(double) * nz,
+                          cudaMemcpyDeviceToHost, p->side) != cudaSuccess)
+        rc = XG_ERR_CUDA;
+    }
+  }
+  if (!rc && cudaStreamSynchronize(p->side) != cudaSuccess) rc = XG_ERR_CUDA;
+  if (rc) {
+    set_error("xg_batch_submit: set-up load failed");
+    return rc;
+  }
+  // pivot analyses on the host
+  for_each_parallel(m, [&](int i) {
+    Placed &R = req[i];
+    const Plan &P = R.P;
+    const double *dfdx = p->h_jac + joff[i], *dqdx = dfdx + P.nnz;
+    std::vector<double> val(size_t(P.nnz));
+    for (int r = 0; r < P.n_unknowns; ++r)
+      for (int e = P.rowptr[r]; e < P.rowptr[r + 1]; ++e) {
+        double a = dfdx[e] + dqdx[e] / p->tstep;
+        if (P.colidx[e] == r && a == 0.0) a = 1e-12;
+        val[e] = a;
+      }
+    analyse_request(P.n_unknowns, P.rowptr, P.colidx, val, "xg_batch_submit: request " + std::to_string(i),
+                    &R.lu);
+    if (!R.lu.rc && int64_t(R.lu.S.rp[P.n_unknowns]) > p->k.lucap) {
+      R.lu.rc = XG_ERR_ARG;
+      R.lu.err = "xg_batch_submit: request " + std::to_string(i) + ": L\\U larger than the slot shape";
+    }
+  });
+  for (int i = 0; i < m; ++i)
+    if (req[i].lu.rc) {
+      // the slots were written but never activated: they stay free
+      set_error(req[i].lu.err);
+      return req[i].lu.rc;
+    }
+  {
+    std::lock_guard<std::mutex> lock(p->mu);
+    for (int i = 0; i < m; ++i) req[i].gen = ++p->gen[req[i].slot];
+  }
+  for (int i = 0; i < m; ++i) stage_lu(p, req[i], tstop[i]);
+  Staging st2;
+  for (auto &R : req) st2.append(R.st2);
+  {
+    std::lock_guard<std::mutex> launch(launch_mutex());
+    rc = run_staging(p, st2);
+    if (!rc && cudaEventRecord(p->ready, p->side) != cudaSuccess) rc = XG_ERR_CUDA;
+    // activation on the batch's stream: after the set-up stream's writes,
+    // between two batch iterations
+    if (!rc && cudaStreamWaitEvent(b->stream, p->ready, 0) != cudaSuccess) rc = XG_ERR_CUDA;
+    for (int i0 = 0; i0 < m && !rc; i0 += kActivateMax) {
+      SlotList l;
+      l.n = std::min(kActivateMax, m - i0);
+      for (int j = 0; j < l.n; ++j) l.slot[j] = req[i0 + j].slot;
+      activate_slots<<<1, kActivateMax, 0, b->stream>>>(l, b->dev.cs, p->cs_next, b->dev.flags, p->fl_next);
+      count_launches(1);
+      if (cudaGetLastError() != cudaSuccess) rc = XG_ERR_CUDA;
+    }
+  }
+  if (!rc && cudaStreamSynchronize(p->side) != cudaSuccess) rc = XG_ERR_CUDA;
+  if (rc) {
+    set_error("xg_batch_submit: activation failed");
+    return rc;
+  }
+  {
+    std::lock_guard<std::mutex> lock(p->mu);
+    for (int i = 0; i < m; ++i) {
+      p->used[req[i].slot] = 1;
+      slots[i] = req[i].slot;
+    }
+  }
+  unreserve.keep = true;
+  return XG_OK;
+}
+
+extern "C" int xg_batch_release(xg_batch *b, int slot) {
+  using namespace xg;
+  if (!b || !b->pool || slot < 0 || slot >= b->nc) {
+    set_error("xg_batch_release: bad argument");
+    return XG_ERR_ARG;
+  }
+  SlotPool *p = b->pool;
+  std::lock_guard<std::mutex> lock(p->mu);
+  const CState &c = b->h_cs[slot];
+  if (p->used[slot] == 2 || (p->used[slot] && !(c.gen == p->gen[slot] && c.phase == PH_DONE))) {
+    set_error("xg_batch_release: the slot's request has not finished (poll first)");
+    return XG_ERR_STATE;
+  }
+  p->used[slot] = 0;
+  return XG_OK;
+}
+
+extern "C" int xg_batch_slots(const xg_batch *b, int *n_free, int *n_running) {
+  using namespace xg;
+  if (!b || !b->pool) {
+    set_error("xg_batch_slots: bad argument");
+    return XG_ERR_ARG;
+  }
+  SlotPool *p = b->pool;
+  std::lock_guard<std::mutex> lock(p->mu);
+  int nf = 0, nr = 0;
+  for (int c = 0; c < b->nc; ++c) {
+    if (!p->used[c]) ++nf;
+    else if (p->used[c] == 2 || !(b->h_cs[c].gen == p->gen[c] && b->h_cs[c].phase == PH_DONE)) ++nr;
+  }
+  if (n_free) *n_free = nf;
+  if (n_running) *n_running = nr;
   return XG_OK;
 }

@@ -58,7 +58,9 @@ struct DevType {
   const double *p;   // SoA params
   const int *lid;    // SoA LIDs
   // Batched loads of independent circuits: the circuit of each instance and
-  // the per-circuit load flags (null: every instance uses the launch's flags)
+  // the per-circuit load flags (null: every instance uses the launch's flags).
+  // An instance whose circuit is negative (an unused place in a slot) or whose
+  // circuit's flags say skip (a finished request) is not evaluated.
   const int *cid = nullptr;
   const Flags *cflags = nullptr;
 };
@@ -72,6 +74,7 @@ struct Flags {
   int dcop, tranop, acop, transient, init_jct, init_fix, newton_iter, inputop;
   double pdt, time;
   int init_tran;
+  int skip;  // batched loads: the circuit is not evaluated (it has finished)
 };
 
 // Vectors the load kernels read and write (device pointers).
@@ -178,6 +181,8 @@ xg_lu *circuit_lu_take(xg_circuit *c, uint64_t key);
 void circuit_lu_keep(xg_circuit *c, xg_lu *lu, uint64_t key);
 // The device and stream of a context (api.cpp).
 int ctx_info(xg_ctx *ctx, int *device, void **stream);
+// The device options a context's circuits are set up and loaded with.
+int ctx_options(xg_ctx *ctx, xg_device_options *o);
 // Breakpoints of the PULSE sources (both corners of each edge, every period,
 // up to tstop) and tstop itself, sorted and unique (tran.cu).  lo/hi, when
 // given, restrict the sources to instances [lo[0], hi[0]) of VSRC and

@@ -99,6 +99,14 @@ def lib():
     L.xg_batch_results.argtypes = [vp, i, vp, vp, C.POINTER(i), C.POINTER(abi.XgTranStats)]
     L.xg_batch_info.argtypes = [vp, C.POINTER(i), i64p]
     L.xg_batch_destroy.argtypes = [vp]
+    L.xg_slot_need.argtypes = [vp, vp, vp, C.c_double, C.c_double, C.POINTER(abi.XgSlotShape)]
+    L.xg_slot_bytes.argtypes = [C.POINTER(abi.XgSlotShape), C.POINTER(abi.XgBatchOptions), i64p]
+    L.xg_batch_create_slots.argtypes = [vp, i, C.POINTER(abi.XgSlotShape), C.POINTER(abi.XgBatchOptions),
+                                        C.POINTER(vp)]
+    L.xg_batch_submit.argtypes = [vp, i, vp, vp, vp, vp, vp]
+    L.xg_batch_release.argtypes = [vp, i]
+    L.xg_batch_slots.argtypes = [vp, C.POINTER(i), C.POINTER(i)]
+    L.xg_mem_info.argtypes = [vp, i64p, i64p]
     _lib = L
     return L
 
@@ -433,6 +441,81 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def slot_need(ctx, netlist, x0, tstop, tstep=1e-12):
+    """The slot shape one request needs (its set-up, first Jacobian and
+    pivot analysis, as a slotted batch does them)."""
+    sh = abi.XgSlotShape()
+    cnl = netlist.to_c()
+    x = np.ascontiguousarray(x0, np.float64)
+    check(lib().xg_slot_need(ctx.h, C.addressof(cnl), _ptr(x), float(tstop), float(tstep), C.byref(sh)))
+    return sh
+
+
+def batch_options(tstep=1e-12, precision=abi.LU_FP64, n_refine=0, n_out=2, max_points=4096, maxstep=0.0,
+                  reltol=1e-3, abstol=1e-6):
+    return abi.XgBatchOptions(tstep, maxstep, reltol, abstol, precision, n_refine, n_out, max_points)
+
+
+def slot_bytes(shape, options):
+    """Device bytes of one slot of this shape (host arithmetic, no device)."""
+    b = C.c_int64()
+    check(lib().xg_slot_bytes(C.byref(shape), C.byref(options), C.byref(b)))
+    return b.value
+
+
+def mem_info(ctx):
+    f, t = C.c_int64(), C.c_int64()
+    check(lib().xg_mem_info(ctx.h, C.byref(f), C.byref(t)))
+    return f.value, t.value
+
+
+class SlotBatch(Batch):
+    """A slotted batch (xg_batch_create_slots): n_slots slots of one shape;
+    requests are submitted into free slots while it runs and their slots
+    released once their results are read."""
+
+    def __init__(self, ctx, n_slots, shape, n_out, tstep=1e-12, precision=abi.LU_FP64, n_refine=0,
+                 max_points=4096, maxstep=0.0, reltol=1e-3, abstol=1e-6):
+        self.ctx = ctx
+        self.shape = shape
+        self.n_out, self.max_points = n_out, max_points
+        o = batch_options(tstep, precision, n_refine, n_out, max_points, maxstep, reltol, abstol)
+        h = C.c_void_p()
+        check(lib().xg_batch_create_slots(ctx.h, n_slots, C.byref(shape), C.byref(o), C.byref(h)))
+        self.h = h
+        _OPEN["batch"].add(self)
+        self.n = n_slots
+        self._ts = np.zeros(n_slots)
+        self._hold = [None] * n_slots
+
+    def submit(self, netlists, x0s, tstops, out_idx):
+        """Slots of the requests, -1 for those no free slot took."""
+        n = len(netlists)
+        if not n:
+            return []
+        cnl = [nl.to_c() for nl in netlists]
+        nl_arr = (C.c_void_p * n)(*[C.addressof(x) for x in cnl])
+        xs = [np.ascontiguousarray(x, np.float64) for x in x0s]
+        x_arr = (C.c_void_p * n)(*[x.ctypes.data for x in xs])
+        ts = np.ascontiguousarray(tstops, np.float64)
+        outs = [np.ascontiguousarray(o, np.int32) for o in out_idx]
+        o_arr = (C.c_void_p * n)(*[o.ctypes.data for o in outs])
+        slots = np.full(n, -1, np.int32)
+        check(lib().xg_batch_submit(self.h, n, nl_arr, x_arr, _ptr(ts), o_arr, _ptr(slots)))
+        for k, c in enumerate(slots):
+            if c >= 0:
+                self._ts[c] = ts[k]
+        return [int(c) for c in slots]
+
+    def release(self, slot):
+        check(lib().xg_batch_release(self.h, int(slot)))
+
+    def slots(self):
+        f, r = C.c_int(), C.c_int()
+        check(lib().xg_batch_slots(self.h, C.byref(f), C.byref(r)))
+        return f.value, r.value
 
 
 def run_batch(batch, chunk=64, max_iters=10**7):

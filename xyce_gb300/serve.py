@@ -1,13 +1,21 @@
 """Continuous batching of transient requests on one GPU (the serving path).
 
 Requests (.STEP / Monte-Carlo variants of a circuit, of uneven sizes) arrive
-over time.  The server admits whatever has arrived into a new batch
-(xg_batch_*) as soon as the concurrency limit and the device-memory budget
-allow, so requests that arrive while others run start at once and their work
-overlaps with the running batches on the device (each batch has its own
-stream and replays its own CUDA graph).  Each batch is stepped in chunks of
-batch iterations; between chunks the server harvests finished requests, so a
-short request leaves as soon as it is done, not when its batch is.
+over time.  Two servers:
+
+  * SlotServer: one slotted batch (xg_batch_create_slots) per size class,
+    each on its own stream replaying its own CUDA graph.  A request is
+    submitted into a free slot of its class's batch while that batch runs and
+    starts at its next iteration; a finished request's slot is released as
+    soon as its results are read, so neither a short request nor a newly
+    arrived one waits for a batch's longest request.  Batches are created as
+    classes first appear, and another one for a class whose slots are all
+    taken, when the device's free memory (cudaMemGetInfo) minus a reserve
+    holds its slots (plan_slots).  A request larger than its class's slot
+    shape runs in a batch of its own, admitted by its measured footprint.
+  * Server: requests grouped into fixed batches (xg_batch_create) as they
+    arrive; a batch's requests leave as they finish, but new ones wait for a
+    new batch.
 
 Latency = completion - arrival, reported as p50 / p99 beside throughput.
 """
@@ -182,6 +190,251 @@ class Server:
                 "p50_ms": float(np.percentile(lat, 50) * 1e3),
                 "p99_ms": float(np.percentile(lat, 99) * 1e3),
                 "mean_ms": float(lat.mean() * 1e3), "failed": failed}
+
+
+def size_class(n_unknowns):
+    """Requests with unknowns in [2^k, 2^(k+1)) share class k."""
+    return int(np.log2(max(2, int(n_unknowns))))
+
+
+def plan_slots(want, per_slot_bytes, free_bytes, reserve_bytes, in_use_bytes=0, cap_bytes=None):
+    """How many slots of per_slot_bytes a new batch may take: at most `want`,
+    within the device's free memory less the reserve, and within cap_bytes
+    (if given) less what the server already holds.  0: admit nothing now."""
+    room = free_bytes - reserve_bytes
+    if cap_bytes is not None:
+        room = min(room, cap_bytes - in_use_bytes)
+    if room <= 0 or per_slot_bytes <= 0:
+        return 0
+    return int(max(0, min(want, room // per_slot_bytes)))
+
+
+def merge_shapes(shapes, margin=1.25):
+    """The smallest shape that holds every given one, its pivot-dependent
+    sizes (L\\U and schedule) widened by `margin` (another request of the
+    class may pivot differently)."""
+    out = abi.XgSlotShape()
+    out.max_unknowns = max(s.max_unknowns for s in shapes)
+    for t in range(abi.NUM_DEV_TYPES):
+        out.max_instances[t] = max(s.max_instances[t] for s in shapes)
+    out.max_nnz = max(s.max_nnz for s in shapes)
+    out.max_lu_nnz = int(max(s.max_lu_nnz for s in shapes) * margin) + 16
+    out.max_schedule = int(max(s.max_schedule for s in shapes) * margin) + 64
+    out.max_breakpoints = max(s.max_breakpoints for s in shapes) + 2
+    return out
+
+
+def ring_class_shapes(ctx, stages=(5, 501), tstop=5e-9, tstep=1e-12, seeds=(0, 1)):
+    """Slot shapes for the Monte-Carlo ring stream: for each size class the
+    needs of its largest ring (a few seeds), merged."""
+    lo, hi = stages
+    by_class = {}
+    for st in range(lo, hi + 1, 2):
+        by_class.setdefault(size_class(st + 2), []).append(st)
+    shapes = {}
+    for cls, sts in by_class.items():
+        top = max(sts)
+        needs = []
+        for sd in seeds:
+            nl = netlists.ring_oscillator(top, seed=sd)
+            x0 = np.zeros(nl.n_nodes + nl.count(abi.DEV_VSRC))
+            x0[:nl.n_nodes] = netlists.ring_oscillator_nodeset(top)
+            needs.append(engine.slot_need(ctx, nl, x0, tstop, tstep))
+        shapes[cls] = merge_shapes(needs)
+    return shapes
+
+
+class SlotServer:
+    """Continuous batching at slot granularity (see the module docstring).
+    shapes: {size class: XgSlotShape}; slots: slots per batch; reserve_bytes:
+    device memory left free; memory_cap: at most this much held by the
+    server's batches (None: no cap besides the device)."""
+
+    def __init__(self, ctx, shapes, precision=abi.LU_FP64, n_refine=0, slots=512, chunk=32, tstep=1e-12,
+                 max_points=8192, n_out=2, reserve_bytes=4 << 30, memory_cap=None, max_batches_per_class=4):
+        self.ctx, self.shapes = ctx, dict(shapes)
+        self.precision, self.n_refine = precision, n_refine
+        self.slots, self.chunk, self.tstep = slots, chunk, tstep
+        self.max_points, self.n_out = max_points, n_out
+        self.reserve, self.cap = reserve_bytes, memory_cap
+        self.max_batches_per_class = max_batches_per_class
+        self.opts = engine.batch_options(tstep, precision, n_refine, n_out, max_points)
+        self.in_use = 0
+
+    def _new_batch(self, cls):
+        sh = self.shapes[cls]
+        per = engine.slot_bytes(sh, self.opts)
+        free, _ = engine.mem_info(self.ctx)
+        n = plan_slots(self.slots, per, free, self.reserve, self.in_use, self.cap)
+        if n <= 0:
+            return None
+        b = engine.SlotBatch(self.ctx, n, sh, self.n_out, tstep=self.tstep, precision=self.precision,
+                             n_refine=self.n_refine, max_points=self.max_points)
+        self.in_use += b.device_bytes()
+        return b
+
+    def run(self, requests, arrivals):
+        """Serve requests arriving at the given times (s); returns a summary
+        (no cyclic garbage collection meanwhile, as Server.run)."""
+        was = gc.isenabled()
+        gc.disable()
+        try:
+            return self._run(requests, arrivals)
+        finally:
+            if was:
+                gc.enable()
+
+    def _run(self, requests, arrivals):
+        import concurrent.futures as cf
+        n = len(requests)
+        for r, a in zip(requests, arrivals):
+            r.arrival = float(a)
+        queues = collections.defaultdict(collections.deque)
+        pools = collections.defaultdict(list)    # class -> [entry]
+        # entry: {"b": SlotBatch, "held": {slot: request}, "fut": submit future, "busy": bool}
+        solo = []                                 # (Batch, request, bytes): larger than the shape
+        pool_ex = cf.ThreadPoolExecutor(2)
+        nxt = done = 0
+        t0 = time.perf_counter()
+        oversize = 0
+
+        def submit(entry, reqs):
+            b = entry["b"]
+            slots = b.submit([r.netlist for r in reqs], [r.x0 for r in reqs], [r.tstop for r in reqs],
+                             [r.out_idx for r in reqs])
+            return list(zip(reqs, slots))
+
+        while done < n:
+            now = time.perf_counter() - t0
+            while nxt < n and requests[nxt].arrival <= now:
+                r = requests[nxt]
+                queues[size_class(len(r.x0))].append(r)
+                nxt += 1
+            busy = False
+            # finished submits: the taken requests are now held by their slots
+            for cls, entries in pools.items():
+                for e in entries:
+                    f = e["fut"]
+                    if f is not None and f.done():
+                        e["fut"] = None
+                        busy = True
+                        try:
+                            placed = f.result()
+                        except engine.XgError:
+                            placed = None
+                        if placed is None:
+                            # a request of that group does not fit the shape:
+                            # its whole group goes to batches of their own
+                            for r in e.pop("pending"):
+                                solo.append(self._solo(r, now))
+                                oversize += 1
+                            continue
+                        e.pop("pending")
+                        for r, sl in placed:
+                            if sl >= 0:
+                                e["held"][sl] = r
+                            else:
+                                queues[cls].appendleft(r)
+            # admission: queued requests into free slots of their class
+            for cls, q in queues.items():
+                if not q:
+                    continue
+                if cls not in self.shapes:
+                    while q:
+                        solo.append(self._solo(q.popleft(), now))
+                        oversize += 1
+                    continue
+                entries = pools[cls]
+                target = None
+                for e in entries:
+                    if e["fut"] is None and e["b"].n - len(e["held"]) > 0:
+                        target = e
+                        break
+                if target is None and all(e["fut"] is None for e in entries) and \
+                        len(entries) < self.max_batches_per_class:
+                    b = self._new_batch(cls)
+                    if b is not None:
+                        target = {"b": b, "held": {}, "fut": None, "busy": False}
+                        entries.append(target)
+                if target is None:
+                    continue
+                k = min(len(q), target["b"].n - len(target["held"]))
+                take = [q.popleft() for _ in range(k)]
+                for r in take:
+                    r.start = now
+                target["pending"] = take
+                target["fut"] = pool_ex.submit(submit, target, take)
+                busy = True
+            # step and harvest
+            for cls, entries in pools.items():
+                for e in entries:
+                    b = e["b"]
+                    nd = b.poll(wait=False)
+                    if nd < 0:
+                        continue
+                    t_now = time.perf_counter() - t0
+                    for sl, r in list(e["held"].items()):
+                        st = b.stats(sl)
+                        if st["finished"]:
+                            r.result = b.results(sl)
+                            r.done = t_now
+                            b.release(sl)
+                            del e["held"][sl]
+                            done += 1
+                            busy = True
+                    if e["held"] or e["fut"] is not None:
+                        b.run(self.chunk)
+                        busy = True
+            for item in list(solo):
+                b, r, nb = item
+                nd = b.poll(wait=False)
+                if nd < 0:
+                    continue
+                if b.stats(0)["finished"]:
+                    r.result = b.results(0)
+                    r.done = time.perf_counter() - t0
+                    b.close()
+                    self.in_use -= nb
+                    solo.remove(item)
+                    done += 1
+                else:
+                    b.run(self.chunk)
+                busy = True
+            if not busy:
+                time.sleep(0.0002)
+        pool_ex.shutdown()
+        wall = time.perf_counter() - t0
+        for entries in pools.values():
+            for e in entries:
+                self.in_use -= e["b"].device_bytes()
+                e["b"].close()
+        lat = np.array([r.done - r.arrival for r in requests])
+        iters = sum(r.result[2]["newton_iters"] for r in requests)
+        failed = sum(1 for r in requests if r.result[2]["status"] != 0)
+        return {"requests": n, "wall_s": wall, "solves_per_s": n / wall,
+                "newton_iters_per_s": iters / wall,
+                "p50_ms": float(np.percentile(lat, 50) * 1e3),
+                "p99_ms": float(np.percentile(lat, 99) * 1e3),
+                "mean_ms": float(lat.mean() * 1e3), "failed": failed, "oversize": oversize,
+                "batches": {int(c): len(v) for c, v in pools.items()}}
+
+    def _solo(self, r, now):
+        """A request larger than its class's shape: a batch of its own,
+        admitted by its measured footprint (waits while memory is short)."""
+        need = engine.slot_need(self.ctx, r.netlist, r.x0, r.tstop, self.tstep)
+        nb = engine.slot_bytes(need, self.opts)
+        while True:
+            free, _ = engine.mem_info(self.ctx)
+            if plan_slots(1, nb, free, self.reserve, self.in_use, self.cap) >= 1:
+                break
+            time.sleep(0.001)
+        r.start = now
+        b = engine.Batch(self.ctx, [r.netlist], [r.x0], [r.tstop], [r.out_idx], tstep=self.tstep,
+                         precision=self.precision, n_refine=self.n_refine, max_points=self.max_points)
+        nb = b.device_bytes()
+        self.in_use += nb
+        b.run(self.chunk)
+        return (b, r, nb)
 
 
 class Autotuner:
