@@ -302,6 +302,10 @@ def run_tran(args, world, rank, local, dist, emit=True):
 
 
 SERVE_METRIC = "served solves/sec"
+# the slot server's schedule grid: slots per batch, batch iterations per
+# launch chunk, batches per size class
+SLOT_TUNING = dict(grid={"slots": (256, 512, 1024), "chunk": (16, 32, 64), "max_batches_per_class": (1, 2, 4)},
+                   start={"slots": 512, "chunk": 32, "max_batches_per_class": 2})
 
 
 def run_serve(args, world, rank, local, dist, emit=True):
@@ -315,24 +319,34 @@ def run_serve(args, world, rank, local, dist, emit=True):
     ctx = engine.Context(local, abi.device_options(fma=0 if args.exact_load else 1))
     L = engine.lib()
 
-    # the batch schedule, picked by the autotuner on a smaller probe stream of
-    # the same kind (not timed)
+    # slot shapes of the stream's size classes (its largest ring per class)
+    shapes = serve.ring_class_shapes(ctx, stages=(5, 501), tstop=w["tstop"])
+
+    def make(kind, prec, nref, params):
+        if kind == "slots":
+            return serve.SlotServer(ctx, shapes, precision=prec, n_refine=nref, **params)
+        return serve.Server(ctx, precision=prec, n_refine=nref, **params)
+
+    # the schedule, picked by the autotuner on a smaller probe stream of the
+    # same kind (not timed), per server
     def probe():
         return (serve.ring_mc_requests(200, seed=7, tstop=w["tstop"]),
                 serve.poisson_arrivals(200, w["rate"], seed=8))
 
-    def serve_with(params, reqs, arr):
-        return serve.Server(ctx, precision=abi.LU_FP32, n_refine=0, **params).run(reqs, arr)
+    def tune(kind):
+        t = serve.Autotuner(lambda params, reqs, arr: make(kind, abi.LU_FP32, 0, params).run(reqs, arr),
+                            probe, **(SLOT_TUNING if kind == "slots" else {}))
+        return t.tune(), len(t.trials)
 
-    tuner = serve.Autotuner(serve_with, probe)
-    sched = tuner.tune()
+    sched, trials = tune(args.server)
+    other = "batches" if args.server == "slots" else "slots"
+    sched_other = tune(other)[0] if not args.no_sweep else None
 
     def one(prec, nref, n=None):
         n = n or w["n"]
         reqs = serve.ring_mc_requests(n, seed=1, tstop=w["tstop"])
         arr = serve.poisson_arrivals(n, w["rate"], seed=2)
-        srv = serve.Server(ctx, precision=prec, n_refine=nref, **sched)
-        res = srv.run(reqs, arr)
+        res = make(args.server, prec, nref, sched).run(reqs, arr)
         return res, reqs
 
     # the mixed-precision form: FP32 factors and solves; every Newton step
@@ -363,12 +377,14 @@ def run_serve(args, world, rank, local, dist, emit=True):
         for rate in [float(r) for r in args.sweep_rates.split(",") if r]:
             n = int(min(w["n"], max(100, 2 * rate)))
             row = {"rate_per_s": rate, "requests": n}
-            for name, prec in (("mixed", abi.LU_FP32), ("fp64", abi.LU_FP64)):
-                reqs = serve.ring_mc_requests(n, seed=3, tstop=w["tstop"])
-                arr = serve.poisson_arrivals(n, rate, seed=4)
-                r = serve.Server(ctx, precision=prec, n_refine=0, **sched).run(reqs, arr)
-                row[name] = {"solves_per_s": r["solves_per_s"], "p50_ms": r["p50_ms"],
-                             "p99_ms": r["p99_ms"]}
+            for kind, sch in ((args.server, sched), (other, sched_other)):
+                row[kind] = {}
+                for name, prec in (("mixed", abi.LU_FP32), ("fp64", abi.LU_FP64)):
+                    reqs = serve.ring_mc_requests(n, seed=3, tstop=w["tstop"])
+                    arr = serve.poisson_arrivals(n, rate, seed=4)
+                    r = make(kind, prec, 0, sch).run(reqs, arr)
+                    row[kind][name] = {"solves_per_s": r["solves_per_s"], "p50_ms": r["p50_ms"],
+                                       "p99_ms": r["p99_ms"]}
             sweep.append(row)
     if rank != 0:
         return 0
@@ -395,7 +411,8 @@ def run_serve(args, world, rank, local, dist, emit=True):
         "details": {"lu": "fp32 factors and solves, corrected by Newton against the fp64 residual",
                    "load_build": "exact (reference rounding)" if args.exact_load
                    else "fma, long sums split over a block",
-                   "schedule": sched, "autotuner_trials": len(tuner.trials)},
+                   "server": args.server, "schedule": sched, "autotuner_trials": trials,
+                   "other_server_schedule": sched_other},
         "p50_ms": float(np.mean([r[0]["p50_ms"] for r in runs])),
         "p99_ms": float(np.mean([r[0]["p99_ms"] for r in runs])),
         "fp64": {"solves_per_s": f64["solves_per_s"], "p50_ms": f64["p50_ms"], "p99_ms": f64["p99_ms"]},
@@ -1047,6 +1064,9 @@ def main():
     ap.add_argument("--refine", type=int, default=2,
                     help="transient with --fp32: FP64 refinement steps per solve")
     ap.add_argument("--no-sweep", action="store_true", help="serving: skip the arrival-rate sweep")
+    ap.add_argument("--server", default="slots", choices=["slots", "batches"],
+                    help="serving: requests join running batches in freed slots (slots) or wait "
+                         "for new fixed batches (batches); the sweep measures both")
     ap.add_argument("--sweep-rates", default="100,500,2000,5000",
                     help="serving: arrival rates [req/s] of the latency sweep")
     ap.add_argument("--no-sub", action="store_true",
