@@ -150,3 +150,24 @@ def test_slot_server_serves_a_stream(gpu_ctx):
         assert st["status"] == 0 and sb["status"] == 0
         vi = np.stack([np.interp(tb, t, v[:, j]) for j in range(v.shape[1])], 1)
         assert np.abs(vi - vb).max() <= VTOL
+
+
+def test_batches_of_other_shapes_do_not_lower_each_others_limits(gpu_ctx):
+    # a batch of large slots, then one of small slots (its shared-memory
+    # needs are smaller), then the large one runs: its solves still launch
+    gpu_ctx.set_options(abi.device_options(fma=1))
+    big = serve.ring_mc_requests(2, seed=8, stages=(201, 201), tstop=0.1e-9)
+    small = serve.ring_mc_requests(2, seed=9, stages=(5, 5), tstop=0.1e-9)
+    b_big = _batch(gpu_ctx, 2, _shape(gpu_ctx, big), 0)
+    b_small = _batch(gpu_ctx, 2, _shape(gpu_ctx, small), 0)
+    for b, reqs in ((b_big, big), (b_small, small)):
+        s = b.submit([r.netlist for r in reqs], [r.x0 for r in reqs], [r.tstop for r in reqs],
+                     [r.out_idx for r in reqs])
+        held, out = dict(zip(s, range(len(reqs)))), {}
+        for _ in range(100000):
+            if not held:
+                break
+            _drain(b, held, out)
+        assert all(out[k][2]["status"] == 0 for k in range(len(reqs)))
+    b_big.close()
+    b_small.close()

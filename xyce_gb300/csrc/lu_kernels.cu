@@ -43,6 +43,7 @@
 #include "xg.h"
 #include "xg_internal.h"
 #include "xg_lu.h"
+#include "xg_smem.cuh"
 
 namespace xg {
 namespace {
@@ -1563,10 +1564,9 @@ extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const i
     lu->smem_grid = size_t(xg::kFactorWarps) * size_t(lu->stage_cap) * tsz;
     const void *fn = precision == XG_LU_FP32 ? (const void *)xg::lu_factor<float>
                                              : (const void *)xg::lu_factor<double>;
-    if ((e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  int(lu->smem_grid)))) {
+    if ((e = xg::allow_dynamic_smem((const void *)fn, lu->smem_grid))) {
       free_lu(lu.get());
-      return cuda_fail(e, "xg_lu_analyze: cudaFuncSetAttribute");
+      return cuda_fail(e, "xg_lu_analyze: shared-memory limit");
     }
     if (precision == XG_LU_FP32)
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, xg::lu_factor<float>, 32 * xg::kFactorWarps,
@@ -1600,8 +1600,7 @@ extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const i
                                                : (const void *)xg::lu_solve_chain<double>;
       if ((rc = upload(&lu->d_tdesc, desc)) ||
           (e = cudaMalloc(&lu->d_hpart, 32 * size_t(nt) * tsz)) ||
-          (e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    int(lu->smem_chain)))) {
+          (e = xg::allow_dynamic_smem((const void *)fn, lu->smem_chain))) {
         free_lu(lu.get());
         return rc ? rc : cuda_fail(e, "xg_lu_analyze");
       }
@@ -1617,15 +1616,15 @@ extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const i
     if (solve_b <= limit && factor_b <= limit && !std::getenv("XG_LU_NO_CTA")) {
       cudaError_t e1, e2, e3, e4;
       if (precision == XG_LU_FP32) {
-        e1 = cudaFuncSetAttribute(xg::lu_factor_cta<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(factor_b));
-        e2 = cudaFuncSetAttribute(xg::lu_solve_cta<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(solve_b));
-        e3 = cudaFuncSetAttribute(xg::lu_factor_seq<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(factor_b));
-        e4 = cudaFuncSetAttribute(xg::lu_solve_seq<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(solve_b));
+        e1 = xg::allow_dynamic_smem((const void *)xg::lu_factor_cta<float>, factor_b);
+        e2 = xg::allow_dynamic_smem((const void *)xg::lu_solve_cta<float>, solve_b);
+        e3 = xg::allow_dynamic_smem((const void *)xg::lu_factor_seq<float>, factor_b);
+        e4 = xg::allow_dynamic_smem((const void *)xg::lu_solve_seq<float>, solve_b);
       } else {
-        e1 = cudaFuncSetAttribute(xg::lu_factor_cta<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(factor_b));
-        e2 = cudaFuncSetAttribute(xg::lu_solve_cta<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(solve_b));
-        e3 = cudaFuncSetAttribute(xg::lu_factor_seq<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(factor_b));
-        e4 = cudaFuncSetAttribute(xg::lu_solve_seq<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(solve_b));
+        e1 = xg::allow_dynamic_smem((const void *)xg::lu_factor_cta<double>, factor_b);
+        e2 = xg::allow_dynamic_smem((const void *)xg::lu_solve_cta<double>, solve_b);
+        e3 = xg::allow_dynamic_smem((const void *)xg::lu_factor_seq<double>, factor_b);
+        e4 = xg::allow_dynamic_smem((const void *)xg::lu_solve_seq<double>, solve_b);
       }
       if (e3 != cudaSuccess || e4 != cudaSuccess) e1 = e3 != cudaSuccess ? e3 : e4;
       if (e1 == cudaSuccess && e2 == cudaSuccess) {
@@ -1684,11 +1683,11 @@ extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const i
     if (fb <= limit && sb <= limit) {
       cudaError_t e1, e2;
       if (precision == XG_LU_FP32) {
-        e1 = cudaFuncSetAttribute(xg::lu_factor_lvl<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(fb));
-        e2 = cudaFuncSetAttribute(xg::lu_solve_lvl<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sb));
+        e1 = xg::allow_dynamic_smem((const void *)xg::lu_factor_lvl<float>, fb);
+        e2 = xg::allow_dynamic_smem((const void *)xg::lu_solve_lvl<float>, sb);
       } else {
-        e1 = cudaFuncSetAttribute(xg::lu_factor_lvl<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(fb));
-        e2 = cudaFuncSetAttribute(xg::lu_solve_lvl<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sb));
+        e1 = xg::allow_dynamic_smem((const void *)xg::lu_factor_lvl<double>, fb);
+        e2 = xg::allow_dynamic_smem((const void *)xg::lu_solve_lvl<double>, sb);
       }
       if (e1 == cudaSuccess && e2 == cudaSuccess) {
         std::vector<int> buf;
@@ -1716,13 +1715,9 @@ extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const i
         lu->lvl = true;
         // the fused refactor + solve when both working sets fit together
         if (bb <= limit) {
-          cudaError_t e3 = precision == XG_LU_FP32
-              ? cudaFuncSetAttribute(xg::lu_factor_solve_lvl<float>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, int(bb))
-              : cudaFuncSetAttribute(xg::lu_factor_solve_lvl<double>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, int(bb));
-          if (e3 == cudaSuccess) lu->smem_lvl_both = bb;
-          else cudaGetLastError();
+          const void *fn = precision == XG_LU_FP32 ? (const void *)xg::lu_factor_solve_lvl<float>
+                                                   : (const void *)xg::lu_factor_solve_lvl<double>;
+          if (xg::allow_dynamic_smem(fn, bb) == cudaSuccess) lu->smem_lvl_both = bb;
         }
       } else {
         cudaGetLastError();

@@ -34,6 +34,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -43,6 +44,7 @@
 #include "xg.h"
 #include "xg_internal.h"
 #include "xg_lu.h"
+#include "xg_smem.cuh"
 
 namespace xg {
 namespace {
@@ -1528,17 +1530,11 @@ extern "C" int xg_batch_create(xg_ctx *ctx, int n, const xg_netlist *const *nls,
         }
       }
     if (need_lvl) {
-      cudaError_t e = o->lu_precision == XG_LU_FP32
-                          ? cudaFuncSetAttribute(batch_solve_lvl<float>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(need_lvl))
-                          : cudaFuncSetAttribute(batch_solve_lvl<double>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(need_lvl));
-      if (e == cudaSuccess) {
-        b->solve_lvl = need_lvl;
-      } else {
-        cudaGetLastError();
-        std::fill(lvl_req.begin(), lvl_req.end(), 0);
-      }
+      const void *fn = o->lu_precision == XG_LU_FP32 ? (const void *)batch_solve_lvl<float>
+                                                     : (const void *)batch_solve_lvl<double>;
+      const bool ok = allow_dynamic_smem(fn, need_lvl) == cudaSuccess;
+      if (ok) b->solve_lvl = need_lvl;
+      else std::fill(lvl_req.begin(), lvl_req.end(), 0);
     }
     if (dev_copy(b.get(), &t_sched_off, sched_off) || dev_copy(b.get(), &t_sched, sched) ||
         dev_copy(b.get(), &t_lvl, lvl_req)) {
@@ -1559,13 +1555,9 @@ extern "C" int xg_batch_create(xg_ctx *ctx, int n, const xg_netlist *const *nls,
     int optin = 0;
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
     if (need + 1024 <= size_t(optin) && !std::getenv("XG_BATCH_NO_SMEM")) {
-      cudaError_t e = o->lu_precision == XG_LU_FP32
-                          ? cudaFuncSetAttribute(batch_solve_smem<float>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(need))
-                          : cudaFuncSetAttribute(batch_solve_smem<double>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(need));
-      if (e == cudaSuccess) b->solve_smem = need;
-      else cudaGetLastError();
+      const void *fn = o->lu_precision == XG_LU_FP32 ? (const void *)batch_solve_smem<float>
+                                                     : (const void *)batch_solve_smem<double>;
+      if (allow_dynamic_smem(fn, need) == cudaSuccess) b->solve_smem = need;
     }
   }
   {
@@ -2707,23 +2699,15 @@ extern "C" int xg_batch_create_slots(xg_ctx *ctx, int n_slots, const xg_slot_sha
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
     const size_t need_w = smem_bytes_request(k.ucap, k.lucap, tsz);
     if (need_w + 1024 <= size_t(optin) && !std::getenv("XG_BATCH_NO_SMEM")) {
-      cudaError_t e = o->lu_precision == XG_LU_FP32
-                          ? cudaFuncSetAttribute(batch_solve_smem<float>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(need_w))
-                          : cudaFuncSetAttribute(batch_solve_smem<double>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(need_w));
-      if (e == cudaSuccess) p->solve_smem = need_w;
-      else cudaGetLastError();
+      const void *fn = o->lu_precision == XG_LU_FP32 ? (const void *)batch_solve_smem<float>
+                                                     : (const void *)batch_solve_smem<double>;
+      if (allow_dynamic_smem(fn, need_w) == cudaSuccess) p->solve_smem = need_w;
     }
     const size_t need_l = smem_bytes_lvl(k.ucap, k.lucap, k.blobcap, tsz);
     if (k.blobcap > 0 && need_l + 1024 <= size_t(optin) && !std::getenv("XG_BATCH_NO_LVL")) {
-      cudaError_t e = o->lu_precision == XG_LU_FP32
-                          ? cudaFuncSetAttribute(batch_solve_lvl<float>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(need_l))
-                          : cudaFuncSetAttribute(batch_solve_lvl<double>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(need_l));
-      if (e == cudaSuccess) p->solve_lvl = need_l;
-      else cudaGetLastError();
+      const void *fn = o->lu_precision == XG_LU_FP32 ? (const void *)batch_solve_lvl<float>
+                                                     : (const void *)batch_solve_lvl<double>;
+      if (allow_dynamic_smem(fn, need_l) == cudaSuccess) p->solve_lvl = need_l;
     }
   }
   if (cudaDeviceSynchronize() != cudaSuccess) {
