@@ -333,8 +333,15 @@ def run_serve(args, world, rank, local, dist, emit=True):
         return (serve.ring_mc_requests(200, seed=7, tstop=w["tstop"]),
                 serve.poisson_arrivals(200, w["rate"], seed=8))
 
+    def run_once(kind, prec, nref, params, reqs, arr):
+        srv = make(kind, prec, nref, params)
+        try:
+            return srv.run(reqs, arr)
+        finally:
+            srv.close()
+
     def tune(kind):
-        t = serve.Autotuner(lambda params, reqs, arr: make(kind, abi.LU_FP32, 0, params).run(reqs, arr),
+        t = serve.Autotuner(lambda params, reqs, arr: run_once(kind, abi.LU_FP32, 0, params, reqs, arr),
                             probe, **(SLOT_TUNING if kind == "slots" else {}))
         return t.tune(), len(t.trials)
 
@@ -342,11 +349,18 @@ def run_serve(args, world, rank, local, dist, emit=True):
     other = "batches" if args.server == "slots" else "slots"
     sched_other = tune(other)[0] if not args.no_sweep else None
 
+    # one long-running server per form, warmed by the warm-up streams (a
+    # slot server keeps its batches between streams, as a service does)
+    servers = {}
+
     def one(prec, nref, n=None):
         n = n or w["n"]
         reqs = serve.ring_mc_requests(n, seed=1, tstop=w["tstop"])
         arr = serve.poisson_arrivals(n, w["rate"], seed=2)
-        res = make(args.server, prec, nref, sched).run(reqs, arr)
+        key = (prec, nref)
+        if key not in servers:
+            servers[key] = make(args.server, prec, nref, sched)
+        res = servers[key].run(reqs, arr)
         return res, reqs
 
     # the mixed-precision form: FP32 factors and solves; every Newton step
@@ -354,7 +368,8 @@ def run_serve(args, world, rank, local, dist, emit=True):
     # Newton iteration refines the FP32 solve against the FP64 residual
     # (warm-up streams: the first 1,000 requests of the stream at most)
     for _ in range(args.warmup):
-        one(abi.LU_FP32, 0, min(w["n"], 1000))
+        for prec, nref in ((abi.LU_FP32, 0), (abi.LU_FP64, 0), (abi.LU_FP32, 1)):
+            one(prec, nref, min(w["n"], 1000))
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -370,6 +385,8 @@ def run_serve(args, world, rank, local, dist, emit=True):
     for _ in range(max(1, args.steps // 2)):
         fp64.append(one(abi.LU_FP64, 0))
         refined.append(one(abi.LU_FP32, 1))
+    for srv in servers.values():
+        srv.close()
     # latency against offered load: the same kind of stream at other rates,
     # about two seconds of arrivals each (at most the workload's request count)
     sweep = []
@@ -382,7 +399,15 @@ def run_serve(args, world, rank, local, dist, emit=True):
                 for name, prec in (("mixed", abi.LU_FP32), ("fp64", abi.LU_FP64)):
                     reqs = serve.ring_mc_requests(n, seed=3, tstop=w["tstop"])
                     arr = serve.poisson_arrivals(n, rate, seed=4)
-                    r = make(kind, prec, 0, sch).run(reqs, arr)
+                    srv = make(kind, prec, 0, sch)
+                    try:
+                        # warmed first by a short burst of the same kind, as a
+                        # running service is (a slot server keeps its batches)
+                        srv.run(serve.ring_mc_requests(200, seed=5, tstop=w["tstop"]),
+                                serve.poisson_arrivals(200, 5000.0, seed=6))
+                        r = srv.run(reqs, arr)
+                    finally:
+                        srv.close()
                     row[kind][name] = {"solves_per_s": r["solves_per_s"], "p50_ms": r["p50_ms"],
                                        "p99_ms": r["p99_ms"]}
             sweep.append(row)

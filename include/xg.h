@@ -432,6 +432,9 @@ int xg_batch_submit(xg_batch *b, int n, const xg_netlist *const *netlists, const
                     const double *tstop, const int *const *out_idx, int *slots);
 /* Free a finished slot for the next request (its results are gone then). */
 int xg_batch_release(xg_batch *b, int slot);
+/* The slots whose request has finished (as of the last poll) and that are
+ * not yet released: up to max_slots of them in slots[], their count in *n. */
+int xg_batch_finished(const xg_batch *b, int max_slots, int *slots, int *n);
 /* Free slots, and slots whose request is still running. */
 int xg_batch_slots(const xg_batch *b, int *n_free, int *n_running);
 /* Free and total device memory of the context's device (cudaMemGetInfo). */

@@ -1866,28 +1866,56 @@ struct PoolRed {
   double *out;
 };
 
-constexpr int kLongOut = 64;  // outputs with more terms go to a warp each
+constexpr int kLongOut = 64;  // outputs with more terms go to a block each
+constexpr int kPoolRedThreads = 256;
 
-// A block per slot: live slots (phase not done), or the listed ones.  Long
-// outputs take a warp each (the lanes fetch, every lane adds the fetched
-// values in order); short ones a thread each.  Every sum is ((0 + t0) + t1)...
-__global__ void __launch_bounds__(256) pool_reduce(PoolRed r, const CState *cs, const int *slots) {
+// Blocks (c, y) of a slot c that is live (phase not done), or listed.  Long
+// outputs (a supply rail's row) take a block each, y-strided: in the exact
+// build the block fetches 256 terms at a time and one thread adds them in
+// order; in the FMA build every thread adds a strided share, then a fixed
+// butterfly per warp and the warps in order.  Short outputs take a thread
+// each, summed ((0 + t0) + t1)....  The same sums in the same order as the
+// fixed batch's reduction, so a request's outputs do not depend on which
+// kind of batch, or which other requests, it runs with.
+__global__ void __launch_bounds__(kPoolRedThreads) pool_reduce(PoolRed r, const CState *cs, const int *slots,
+                                                               int split) {
+  __shared__ double buf[kPoolRedThreads];
+  __shared__ double part[kPoolRedThreads / 32];
   const int c = slots ? slots[blockIdx.x] : int(blockIdx.x);
   if (!slots && cs[c].phase == PH_DONE) return;
   const RedEntry *E = r.ent + int64_t(c) * r.ecap;
   const int ne = r.ne[c], nl = r.nl[c];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int k = wid; k < nl; k += nw) {
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  for (int k = blockIdx.y; k < nl; k += gridDim.y) {
     const RedEntry e = E[k];
-    double s = 0.0;
-    for (int base = 0; base < e.cnt; base += 32) {
-      const int m = min(32, e.cnt - base);
-      const double v = lane < m ? r.terms[r.ref[e.beg + base + lane]] : 0.0;
-      for (int j = 0; j < m; ++j) s += __shfl_sync(0xffffffffu, v, j);
+    if (split) {
+      double s = 0.0;
+#pragma unroll 4
+      for (int j = tid; j < e.cnt; j += kPoolRedThreads) s += r.terms[r.ref[e.beg + j]];
+#pragma unroll
+      for (int m = 16; m > 0; m >>= 1) s += __shfl_xor_sync(0xffffffffu, s, m);
+      if (lane == 0) part[wid] = s;
+      __syncthreads();
+      if (tid == 0) {
+        double t = part[0];
+        for (int q = 1; q < kPoolRedThreads / 32; ++q) t += part[q];
+        r.out[e.out] = t;
+      }
+      __syncthreads();
+    } else {
+      double s = 0.0;
+      for (int base = 0; base < e.cnt; base += kPoolRedThreads) {
+        const int m = min(kPoolRedThreads, e.cnt - base);
+        if (tid < m) buf[tid] = r.terms[r.ref[e.beg + base + tid]];
+        __syncthreads();
+        if (tid == 0)
+          for (int j = 0; j < m; ++j) s += buf[j];
+        __syncthreads();
+      }
+      if (tid == 0) r.out[e.out] = s;
     }
-    if (lane == 0) r.out[e.out] = s;
   }
-  for (int k = nl + threadIdx.x; k < ne; k += blockDim.x) {
+  for (int k = nl + int(blockIdx.y) * kPoolRedThreads + tid; k < ne; k += int(gridDim.y) * kPoolRedThreads) {
     const RedEntry e = E[k];
     double s = 0.0;
     for (int j = 0; j < e.cnt; ++j) s += r.terms[r.ref[e.beg + j]];
@@ -1973,6 +2001,7 @@ struct SlotPool {
   int64_t sta0[kTypes] = {}, sto0[kTypes] = {}, term0[kTypes] = {};
   int64_t n_state = 0, n_store = 0, n_terms = 0, n_out_vals = 0;
   size_t solve_smem = 0, solve_lvl = 0;
+  int red_y = 1;            // reduction blocks per slot
   // device
   double *params[kTypes] = {};
   int *lid[kTypes] = {}, *cid[kTypes] = {}, *cid_stage[kTypes] = {};
@@ -2398,7 +2427,7 @@ int enqueue_pool_iteration(xg_batch *b) {
   }
   int rc = pool_eval(p, p->cid, b->dev.flags, s);
   if (rc) return rc;
-  pool_reduce<<<nc, 256, 0, s>>>(pool_red(p), b->dev.cs, nullptr);
+  pool_reduce<<<dim3(nc, p->red_y), kPoolRedThreads, 0, s>>>(pool_red(p), b->dev.cs, nullptr, p->dopt.fma);
   batch_combine<<<nc, kBatchThreads, 0, s>>>(b->dev);
   batch_control<<<(nc + 31) / 32, 32, 0, s>>>(b->dev);
   batch_vector<<<nc, kVectorThreads, 0, s>>>(b->dev);
@@ -2558,6 +2587,7 @@ extern "C" int xg_batch_create_slots(xg_ctx *ctx, int n_slots, const xg_slot_sha
   }
   const int64_t W = int64_t(p->NU) + 1;
   p->n_out_vals = 4 * W + 2 * p->NNZ;
+  p->red_y = int(std::min<int64_t>(32, (k.ecap + kPoolRedThreads - 1) / kPoolRedThreads));
   const size_t tsz = o->lu_precision == XG_LU_FP32 ? sizeof(float) : sizeof(double);
   int device = 0;
   void *ctx_stream = nullptr;
@@ -2800,7 +2830,8 @@ extern "C" int xg_batch_submit(xg_batch *b, int n, const xg_netlist *const *nls,
     rc = run_staging(p, st);
     if (!rc) rc = pool_eval(p, p->cid_stage, p->fl_stage, p->side);
     if (!rc) {
-      pool_reduce<<<m, 256, 0, p->side>>>(pool_red(p), nullptr, p->d_list);
+      pool_reduce<<<dim3(m, p->red_y), kPoolRedThreads, 0, p->side>>>(pool_red(p), nullptr, p->d_list,
+                                                                      p->dopt.fma);
       count_launches(1);
       if (cudaGetLastError() != cudaSuccess) rc = XG_ERR_CUDA;
     }
@@ -2914,6 +2945,24 @@ extern "C" int xg_batch_release(xg_batch *b, int slot) {
     return XG_ERR_STATE;
   }
   p->used[slot] = 0;
+  return XG_OK;
+}
+
+extern "C" int xg_batch_finished(const xg_batch *b, int max_slots, int *slots, int *n) {
+  using namespace xg;
+  if (!b || !b->pool || max_slots < 0 || (max_slots && !slots) || !n) {
+    set_error("xg_batch_finished: bad argument");
+    return XG_ERR_ARG;
+  }
+  SlotPool *p = b->pool;
+  std::lock_guard<std::mutex> lock(p->mu);
+  int k = 0;
+  for (int c = 0; c < b->nc; ++c)
+    if (p->used[c] == 1 && b->h_cs[c].gen == p->gen[c] && b->h_cs[c].phase == PH_DONE) {
+      if (k < max_slots) slots[k] = c;
+      ++k;
+    }
+  *n = k;
   return XG_OK;
 }
 

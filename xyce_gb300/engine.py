@@ -106,6 +106,7 @@ def lib():
     L.xg_batch_submit.argtypes = [vp, i, vp, vp, vp, vp, vp]
     L.xg_batch_release.argtypes = [vp, i]
     L.xg_batch_slots.argtypes = [vp, C.POINTER(i), C.POINTER(i)]
+    L.xg_batch_finished.argtypes = [vp, i, vp, C.POINTER(i)]
     L.xg_mem_info.argtypes = [vp, i64p, i64p]
     _lib = L
     return L
@@ -511,6 +512,13 @@ class SlotBatch(Batch):
 
     def release(self, slot):
         check(lib().xg_batch_release(self.h, int(slot)))
+
+    def finished(self):
+        """Slots whose request finished by the last poll, not yet released."""
+        buf = np.zeros(self.n, np.int32)
+        k = C.c_int()
+        check(lib().xg_batch_finished(self.h, self.n, _ptr(buf), C.byref(k)))
+        return [int(c) for c in buf[:k.value]]
 
     def slots(self):
         f, r = C.c_int(), C.c_int()

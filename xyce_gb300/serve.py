@@ -80,6 +80,9 @@ class Server:
     def size_class(r):
         return int(np.log2(max(2, len(r.x0))))
 
+    def close(self):
+        """Nothing held between runs (each batch lives for its requests)."""
+
     def _footprint(self, reqs):
         unk = sum(len(r.x0) for r in reqs)
         return 0 if self.bytes_per_unknown is None else unk * self.bytes_per_unknown
@@ -248,7 +251,9 @@ class SlotServer:
     """Continuous batching at slot granularity (see the module docstring).
     shapes: {size class: XgSlotShape}; slots: slots per batch; reserve_bytes:
     device memory left free; memory_cap: at most this much held by the
-    server's batches (None: no cap besides the device)."""
+    server's batches (None: no cap besides the device).  The batches live
+    with the server, across calls of run(), as a long-running server keeps
+    them; close() frees them."""
 
     def __init__(self, ctx, shapes, precision=abi.LU_FP64, n_refine=0, slots=512, chunk=32, tstep=1e-12,
                  max_points=8192, n_out=2, reserve_bytes=4 << 30, memory_cap=None, max_batches_per_class=4):
@@ -260,6 +265,15 @@ class SlotServer:
         self.max_batches_per_class = max_batches_per_class
         self.opts = engine.batch_options(tstep, precision, n_refine, n_out, max_points)
         self.in_use = 0
+        # class -> [entry]; entry: {"b": SlotBatch, "held": {slot: request}, "fut": submit future}
+        self.pools = collections.defaultdict(list)
+
+    def close(self):
+        for entries in self.pools.values():
+            for e in entries:
+                self.in_use -= e["b"].device_bytes()
+                e["b"].close()
+        self.pools.clear()
 
     def _new_batch(self, cls):
         sh = self.shapes[cls]
@@ -290,8 +304,7 @@ class SlotServer:
         for r, a in zip(requests, arrivals):
             r.arrival = float(a)
         queues = collections.defaultdict(collections.deque)
-        pools = collections.defaultdict(list)    # class -> [entry]
-        # entry: {"b": SlotBatch, "held": {slot: request}, "fut": submit future, "busy": bool}
+        pools = self.pools
         solo = []                                 # (Batch, request, bytes): larger than the shape
         pool_ex = cf.ThreadPoolExecutor(2)
         nxt = done = 0
@@ -354,7 +367,7 @@ class SlotServer:
                         len(entries) < self.max_batches_per_class:
                     b = self._new_batch(cls)
                     if b is not None:
-                        target = {"b": b, "held": {}, "fut": None, "busy": False}
+                        target = {"b": b, "held": {}, "fut": None}
                         entries.append(target)
                 if target is None:
                     continue
@@ -373,15 +386,15 @@ class SlotServer:
                     if nd < 0:
                         continue
                     t_now = time.perf_counter() - t0
-                    for sl, r in list(e["held"].items()):
-                        st = b.stats(sl)
-                        if st["finished"]:
-                            r.result = b.results(sl)
-                            r.done = t_now
-                            b.release(sl)
-                            del e["held"][sl]
-                            done += 1
-                            busy = True
+                    for sl in b.finished():
+                        r = e["held"].pop(sl, None)
+                        if r is None:
+                            continue
+                        r.result = b.results(sl)
+                        r.done = t_now
+                        b.release(sl)
+                        done += 1
+                        busy = True
                     if e["held"] or e["fut"] is not None:
                         b.run(self.chunk)
                         busy = True
@@ -404,10 +417,6 @@ class SlotServer:
                 time.sleep(0.0002)
         pool_ex.shutdown()
         wall = time.perf_counter() - t0
-        for entries in pools.values():
-            for e in entries:
-                self.in_use -= e["b"].device_bytes()
-                e["b"].close()
         lat = np.array([r.done - r.arrival for r in requests])
         iters = sum(r.result[2]["newton_iters"] for r in requests)
         failed = sum(1 for r in requests if r.result[2]["status"] != 0)
