@@ -193,6 +193,10 @@ long long xg_launch_count(void);
  * the device-evaluation kernels, which are bound by the FP64 pipe.  A
  * measurement utility with no counterpart in the reference. */
 int xg_probe_fp64_rate(int cuda_device, double *flops_per_second);
+/* The FMA load build's FP64 reciprocal (Newton-Raphson from the hardware's
+ * approximation) of n values on the current device, for testing it against
+ * 1.0 / b.  No counterpart in the reference. */
+int xg_probe_reciprocal(int n, const double *host_b, double *host_out);
 
 /* ---- context: one GPU, one stream (replaces the DeviceMgr singleton) -------- */
 int xg_ctx_create(int cuda_device, xg_ctx **out);
@@ -378,9 +382,13 @@ int xg_batch_create(xg_ctx *ctx, int n_requests, const xg_netlist *const *netlis
                     const xg_batch_options *o, xg_batch **out);
 /* enqueue `iterations` batch iterations (asynchronous, on the batch's stream) */
 int xg_batch_run(xg_batch *b, int iterations);
-/* wait = 0: *n_done = -1 while the batch's stream is busy; otherwise the
- * number of finished requests (wait = 1 synchronises) */
+/* The request states as the newest finished xg_batch_run left them (each
+ * run ends with a snapshot), and the number of finished requests in them.
+ * wait = 0: *n_done = -1 when no run has finished since the last poll (later
+ * runs may still be on the device); wait = 1 synchronises first. */
 int xg_batch_poll(xg_batch *b, int wait, int *n_done);
+/* Runs enqueued and not finished yet. */
+int xg_batch_inflight(xg_batch *b, int *n);
 /* request i's recorded (t, x[out_idx]) and counters (after a poll) */
 int xg_batch_results(xg_batch *b, int i, double *host_t, double *host_v, int *n_points,
                      xg_tran_stats *st);

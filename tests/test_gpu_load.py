@@ -188,3 +188,29 @@ def test_gpu_full_size_bsim3_single_load_matches_oracle(fma, gpu_ctx, oracle_lib
     assert not bad, bad
     if not fma:
         assert ident / total > 0.98, f"{ident}/{total} bit-identical"
+
+
+def test_fast_reciprocal_within_two_ulp_of_ieee(engine_lib):
+    """The FMA load build's reciprocal (Newton-Raphson from the hardware's
+    approximation) against IEEE 1.0 / b: within 2 ulp on normal values over
+    the whole fast range, the IEEE quotient itself outside it (zero,
+    subnormal, huge, infinite, NaN)."""
+    import ctypes as C
+    rng = np.random.default_rng(3)
+    n = 1 << 20
+    b = rng.uniform(1.0, 2.0, n) * np.exp2(rng.integers(-1000, 1001, n)) * rng.choice([-1.0, 1.0], n)
+    edge = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 5e-324, -1e-310, 2.0 ** -1000, 2.0 ** -1001,
+                     2.0 ** 1000, 2.0 ** 1001, 1.7976931348623157e308, 1.0, 3.0, 0.1, -7.0])
+    b = np.concatenate([b, edge])
+    out = np.zeros_like(b)
+    assert engine_lib.xg_probe_reciprocal(len(b), b.ctypes.data_as(C.c_void_p),
+                                          out.ctypes.data_as(C.c_void_p)) == 0
+    with np.errstate(divide="ignore", invalid="ignore"):
+        ref = 1.0 / b
+    fin = np.isfinite(ref) & (ref != 0)
+    ulps = np.abs(out[fin] - ref[fin]) / np.spacing(np.abs(ref[fin]))
+    assert ulps.max() <= 2.0, ulps.max()
+    special = ~fin
+    assert np.array_equal(np.isnan(out[special]), np.isnan(ref[special]))
+    ok = ~np.isnan(ref[special])
+    assert np.array_equal(out[special][ok], ref[special][ok])

@@ -29,27 +29,31 @@ constexpr double KBOLTZ = 1.3806226e-23;        // CONSTboltz
 constexpr double CTOK = 273.15;                 // CONSTCtoK
 
 // Quotients.  The bit-exact build divides wherever the reference divides.
-// The FMA build (XG_FAST_DIV) forms the reciprocal of a denominator once
-// where several quotients share it, or reads it from the parameter block
-// where it is an instance constant, and multiplies: one divide (or none)
-// plus a multiply per quotient, ~1 ulp from the quotient, within the
-// tolerance that build is held to.  A literal divisor becomes a multiply by
-// its reciprocal, folded at compile time.
+// The FMA build (XG_FAST_DIV) multiplies by reciprocals instead: formed once
+// where several quotients share a denominator, read from the parameter block
+// where it is an instance constant, and otherwise taken by Newton-Raphson
+// from the hardware's approximation (xg::fast_rcp, four fused multiply-adds
+// against IEEE division's longer sequence); each quotient lands within ~1-2
+// ulp, inside the tolerance that build is held to.  A literal divisor
+// becomes a multiply by its reciprocal, folded at compile time.
 //   B3_RCOL(name, k)   declares a reciprocal read from parameter column k
 //   B3_RCP(name, x)    declares the reciprocal of x (FMA build only)
 //   B3_DIV(a, b, rb)   a / b, or a * rb
+//   B3_Q(a, b)         a / b, or a * fast_rcp(b)
 //   B3_DIVK(a, k)      a / k for a literal k, or a * (1 / k)
 //   B3_RSQRT(x)        1 / sqrt(x), or CUDA's rsqrt (within 1 ulp)
 #if XG_FAST_DIV
 #define B3_RCOL(name, k) const double name = PRM(k)
-#define B3_RCP(name, x) const double name = 1.0 / (x)
+#define B3_RCP(name, x) const double name = xg::fast_rcp(x)
 #define B3_DIV(a, b, rb) ((a) * (rb))
+#define B3_Q(a, b) ((a) * xg::fast_rcp(b))
 #define B3_DIVK(a, k) ((a) * (1.0 / (k)))
 #define B3_RSQRT(x) rsqrt(x)
 #else
 #define B3_RCOL(name, k) (void)0
 #define B3_RCP(name, x) (void)0
 #define B3_DIV(a, b, rb) ((a) / (b))
+#define B3_Q(a, b) ((a) / (b))
 #define B3_DIVK(a, k) ((a) / (k))
 #define B3_RSQRT(x) (1.0 / sqrt(x))
 #endif
@@ -265,19 +269,19 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
   T0 = Vbs - vbsc - 0.001;
   double T1global = sqrt(T0 * T0 - 0.004 * vbsc);
   Vbseff = vbsc + 0.5 * (T0 + T1global);
-  dVbseff_dVb = 0.5 * (1.0 + T0 / T1global);
+  dVbseff_dVb = 0.5 * (1.0 + B3_Q(T0, T1global));
   if (Vbseff < Vbs) Vbseff = Vbs;
   if (Vbseff > 0.0) {
-    T0 = phi / (phi + Vbseff);
+    T0 = B3_Q(phi, (phi + Vbseff));
     Phis = phi * T0;
     dPhis_dVb = -T0 * T0;
-    sqrtPhis = phis3 / (phi + 0.5 * Vbseff);
+    sqrtPhis = B3_Q(phis3, (phi + 0.5 * Vbseff));
     dsqrtPhis_dVb = B3_DIV(-0.5 * sqrtPhis * sqrtPhis, phis3, rPhis3);
   } else {
     Phis = phi - Vbseff;
     dPhis_dVb = -1.0;
     sqrtPhis = sqrt(Phis);
-    dsqrtPhis_dVb = -0.5 / sqrtPhis;
+    dsqrtPhis_dVb = B3_Q(-0.5, sqrtPhis);
   }
   Xdep = B3_DIV(Xdep0 * sqrtPhis, sqrtPhi, rSqrtPhi);
   dXdep_dVb = PRM(XG_B3_XDEP0_SQRTPHI) * dsqrtPhis_dVb;
@@ -292,7 +296,7 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
     T1 = 1.0 + T0;
     T2 = dvt2;
   } else {
-    T4 = 1.0 / (3.0 + 8.0 * T0);
+    T4 = B3_Q(1.0, (3.0 + 8.0 * T0));
     T1 = (1.0 + 3.0 * T0) * T4;
     T2 = dvt2 * T4 * T4;
   }
@@ -303,7 +307,7 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
     T1 = 1.0 + T0;
     T2 = dvt2w;
   } else {
-    T4 = 1.0 / (3.0 + 8.0 * T0);
+    T4 = B3_Q(1.0, (3.0 + 8.0 * T0));
     T1 = (1.0 + 3.0 * T0) * T4;
     T2 = dvt2w * T4 * T4;
   }
@@ -347,7 +351,7 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
   const double etab = PRM(XG_B3_ETAB), theta0vb0 = PRM(XG_B3_THETA0VB0);
   T3 = PRM(XG_B3_ETA0) + etab * Vbseff;
   if (T3 < 1.0e-4) {
-    T9 = 1.0 / (3.0 - 2.0e4 * T3);
+    T9 = B3_Q(1.0, (3.0 - 2.0e4 * T3));
     T3 = (2.0e-4 - T3) * T9;
     T4 = T9 * T9;
   } else {
@@ -374,7 +378,7 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
     dn_dVb = B3_DIV(B3_DIV(-tmp2, Xdep, rXdep) * dXdep_dVb + tmp3 * dTheta0_dVb + cdscb * Theta0, cox, rcox);
     dn_dVd = B3_DIV(cdscd * Theta0, cox, rcox);
   } else {
-    T0 = 1.0 / (3.0 + 8.0 * tmp4);
+    T0 = B3_Q(1.0, (3.0 + 8.0 * tmp4));
     n = (1.0 + 3.0 * tmp4) * T0;
     T0 *= T0;
     dn_dVb = B3_DIV(B3_DIV(-tmp2, Xdep, rXdep) * dXdep_dVb + tmp3 * dTheta0_dVb + cdscb * Theta0, cox, rcox) * T0;
@@ -384,15 +388,15 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
   T0 = PRM(XG_B3_VFB_PHI);
   const double ngate = PRM(XG_B3_NGATE);
   if ((ngate > 1.e18) && (ngate < 1.e25) && (Vgs > T0)) {
-    T1 = 1.0e6 * KQ * EPSSI * ngate / (cox * cox);
-    T4 = sqrt(1.0 + 2.0 * (Vgs - T0) / T1);
+    T1 = B3_Q(1.0e6 * KQ * EPSSI * ngate, (cox * cox));
+    T4 = sqrt(1.0 + B3_Q(2.0 * (Vgs - T0), T1));
     T2 = T1 * (T4 - 1.0);
-    T3 = 0.5 * T2 * T2 / T1;
+    T3 = B3_Q(0.5 * T2 * T2, T1);
     T7 = 1.12 - T3 - 0.05;
     T6 = sqrt(T7 * T7 + 0.224);
     T5 = 1.12 - 0.5 * (T7 + T6);
     Vgs_eff = Vgs - T5;
-    dVgs_eff_dVg = 1.0 - (0.5 - 0.5 / T4) * (1.0 + T7 / T6);
+    dVgs_eff_dVg = 1.0 - (0.5 - B3_Q(0.5, T4)) * (1.0 + B3_Q(T7, T6));
   } else {
     Vgs_eff = Vgs;
     dVgs_eff_dVg = 1.0;
@@ -410,17 +414,17 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
     dVgsteff_dVd = -dVth_dVd;
     dVgsteff_dVb = -dVth_dVb;
   } else if (ExpArg > EXP_THRESHOLD) {
-    T0 = (Vgst - voff) / (n * Vtm);
+    T0 = B3_Q((Vgst - voff), (n * Vtm));
     ExpVgst = exp(T0);
     Vgsteff = PRM(XG_B3_VTMCDEP_COX) * ExpVgst;
-    dVgsteff_dVg = Vgsteff / (n * Vtm);
+    dVgsteff_dVg = B3_Q(Vgsteff, (n * Vtm));
     dVgsteff_dVd = -dVgsteff_dVg * (dVth_dVd + T0 * Vtm * dn_dVd);
     dVgsteff_dVb = -dVgsteff_dVg * (dVth_dVb + T0 * Vtm * dn_dVb);
     dVgsteff_dVg *= dVgs_eff_dVg;
   } else {
     ExpVgst = exp(VgstNVt);
     T1 = T10 * log(1.0 + ExpVgst);
-    dT1_dVg = ExpVgst / (1.0 + ExpVgst);
+    dT1_dVg = B3_Q(ExpVgst, (1.0 + ExpVgst));
     B3_RCP(rn, n);
     dT1_dVb = -dT1_dVg * (dVth_dVb + B3_DIV(Vgst, n, rn) * dn_dVb) + B3_DIV(T1, n, rn) * dn_dVb;
     dT1_dVd = -dT1_dVg * (dVth_dVd + B3_DIV(Vgst, n, rn) * dn_dVd) + B3_DIV(T1, n, rn) * dn_dVd;
@@ -428,7 +432,7 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
     T2 = 1.0 - T10 * dT2_dVg;
     dT2_dVd = -dT2_dVg * (dVth_dVd - 2.0 * Vtm * ExpArg * dn_dVd) + B3_DIV(T2 - 1.0, n, rn) * dn_dVd;
     dT2_dVb = -dT2_dVg * (dVth_dVb - 2.0 * Vtm * ExpArg * dn_dVb) + B3_DIV(T2 - 1.0, n, rn) * dn_dVb;
-    Vgsteff = T1 / T2;
+    Vgsteff = B3_Q(T1, T2);
     T3 = T2 * T2;
     B3_RCP(rT3, T3);
     dVgsteff_dVg = B3_DIV(T2 * dT1_dVg - T1 * dT2_dVg, T3, rT3) * dVgs_eff_dVg;
@@ -442,7 +446,7 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
   dWeff_dVg = -2.0 * dwg;
   dWeff_dVb = -2.0 * dwb * dsqrtPhis_dVb;
   if (Weff < 2.0e-8) {
-    T0 = 1.0 / (6.0e-8 - 2.0 * Weff);
+    T0 = B3_Q(1.0, (6.0e-8 - 2.0 * Weff));
     Weff = 2.0e-8 * (4.0e-8 - Weff) * T0;
     T0 *= T0 * 4.0e-16;
     dWeff_dVg *= T0;
@@ -455,7 +459,7 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
     dRds_dVg = rds0 * prwg;
     dRds_dVb = rds0 * prwb * dsqrtPhis_dVb;
   } else {
-    T1 = 1.0 / (17.0 + 20.0 * T0);
+    T1 = B3_Q(1.0, (17.0 + 20.0 * T0));
     Rds = rds0 * (0.8 + T0) * T1;
     T1 *= T1;
     dRds_dVg = rds0 * prwg * T1;
@@ -483,12 +487,12 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
   Abulk = Abulk0 + dAbulk_dVg * Vgsteff;
   dAbulk_dVb = dAbulk0_dVb - T8 * Vgsteff * (dT1_dVb + 3.0 * T1 * dT2_dVb);
   if (Abulk0 < 0.1) {
-    T9 = 1.0 / (3.0 - 20.0 * Abulk0);
+    T9 = B3_Q(1.0, (3.0 - 20.0 * Abulk0));
     Abulk0 = (0.2 - Abulk0) * T9;
     dAbulk0_dVb *= T9 * T9;
   }
   if (Abulk < 0.1) {
-    T9 = 1.0 / (3.0 - 20.0 * Abulk);
+    T9 = B3_Q(1.0, (3.0 - 20.0 * Abulk));
     Abulk = (0.2 - Abulk) * T9;
     T10 = T9 * T9;
     dAbulk_dVb *= T10;
@@ -497,10 +501,10 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
   const double keta = PRM(XG_B3_KETA);
   T2 = keta * Vbseff;
   if (T2 >= -0.9) {
-    T0 = 1.0 / (1.0 + T2);
+    T0 = B3_Q(1.0, (1.0 + T2));
     dT0_dVb = -keta * T0 * T0;
   } else {
-    T1 = 1.0 / (0.8 + T2);
+    T1 = B3_Q(1.0, (0.8 + T2));
     T0 = (17.0 + 20.0 * T2) * T1;
     dT0_dVb = -keta * T1 * T1;
   }
@@ -538,7 +542,7 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
   if (T5 >= -0.8) {
     Denomi = 1.0 + T5;
   } else {
-    T9 = 1.0 / (7.0 + 10.0 * T5);
+    T9 = B3_Q(1.0, (7.0 + 10.0 * T5));
     Denomi = (0.6 + T5) * T9;
     T9 *= T9;
     dDenomi_dVg *= T9;
@@ -574,12 +578,12 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
     T1 = T0 - a1 * Vgsteff - 0.0001;
     T2 = sqrt(T1 * T1 + 0.0004 * T0);
     Lambda = a2 + T0 - 0.5 * (T1 + T2);
-    dLambda_dVg = 0.5 * a1 * (1.0 + T1 / T2);
+    dLambda_dVg = 0.5 * a1 * (1.0 + B3_Q(T1, T2));
   } else {
     T1 = a2 + a1 * Vgsteff - 0.0001;
     T2 = sqrt(T1 * T1 + 0.0004 * a2);
     Lambda = 0.5 * (T1 + T2);
-    dLambda_dVg = 0.5 * a1 * (1.0 + T1 / T2);
+    dLambda_dVg = 0.5 * a1 * (1.0 + B3_Q(T1, T2));
   }
   Vgst2Vtm = Vgsteff + PRM(XG_B3_VTM2);
   B3_RCP(rVgst2Vtm, Vgst2Vtm);
@@ -593,7 +597,7 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
     tmp3 = B3_DIV(dWeff_dVb, Weff, rWeff);
   }
   if ((Rds == 0.0) && (Lambda == 1.0)) {
-    T0 = 1.0 / (Abulk * EsatL + Vgst2Vtm);
+    T0 = B3_Q(1.0, (Abulk * EsatL + Vgst2Vtm));
     tmp1 = 0.0;
     T1 = T0 * T0;
     T2 = Vgst2Vtm * T0;
@@ -606,17 +610,17 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
     dVdsat_dVd = T3 * dT0_dVd + T2 * dEsatL_dVd;
     dVdsat_dVb = T3 * dT0_dVb + T2 * dEsatL_dVb;
   } else {
-    tmp1 = dLambda_dVg / (Lambda * Lambda);
+    tmp1 = B3_Q(dLambda_dVg, (Lambda * Lambda));
     T9 = Abulk * WVCoxRds;
     T8 = Abulk * T9;
     T7 = Vgst2Vtm * T9;
     T6 = Vgst2Vtm * WVCoxRds;
-    T0 = 2.0 * Abulk * (T9 - 1.0 + 1.0 / Lambda);
-    dT0_dVg = 2.0 * (T8 * tmp2 - Abulk * tmp1 + (2.0 * T9 + 1.0 / Lambda - 1.0) * dAbulk_dVg);
-    dT0_dVb = 2.0 * (T8 * (2.0 / Abulk * dAbulk_dVb + tmp3) + (1.0 / Lambda - 1.0) * dAbulk_dVb);
+    T0 = 2.0 * Abulk * (T9 - 1.0 + B3_Q(1.0, Lambda));
+    dT0_dVg = 2.0 * (T8 * tmp2 - Abulk * tmp1 + (2.0 * T9 + B3_Q(1.0, Lambda) - 1.0) * dAbulk_dVg);
+    dT0_dVb = 2.0 * (T8 * (B3_Q(2.0, Abulk) * dAbulk_dVb + tmp3) + (B3_Q(1.0, Lambda) - 1.0) * dAbulk_dVb);
     dT0_dVd = 0.0;
-    T1 = Vgst2Vtm * (2.0 / Lambda - 1.0) + Abulk * EsatL + 3.0 * T7;
-    dT1_dVg = (2.0 / Lambda - 1.0) - 2.0 * Vgst2Vtm * tmp1 + Abulk * dEsatL_dVg +
+    T1 = Vgst2Vtm * (B3_Q(2.0, Lambda) - 1.0) + Abulk * EsatL + 3.0 * T7;
+    dT1_dVg = (B3_Q(2.0, Lambda) - 1.0) - 2.0 * Vgst2Vtm * tmp1 + Abulk * dEsatL_dVg +
               EsatL * dAbulk_dVg + 3.0 * (T9 + T7 * tmp2 + T6 * dAbulk_dVg);
     dT1_dVb = Abulk * dEsatL_dVb + EsatL * dAbulk_dVb + 3.0 * (T6 * dAbulk_dVb + T7 * tmp3);
     dT1_dVd = Abulk * dEsatL_dVd;
@@ -628,9 +632,9 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
     B3_RCP(rT0v, T0);
     B3_RCP(rT3v, T3);
     Vdsat = B3_DIV(T1 - T3, T0, rT0v);
-    dT3_dVg = (T1 * dT1_dVg - 2.0 * (T0 * dT2_dVg + T2 * dT0_dVg)) / T3;
-    dT3_dVd = (T1 * dT1_dVd - 2.0 * (T0 * dT2_dVd + T2 * dT0_dVd)) / T3;
-    dT3_dVb = (T1 * dT1_dVb - 2.0 * (T0 * dT2_dVb + T2 * dT0_dVb)) / T3;
+    dT3_dVg = B3_Q((T1 * dT1_dVg - 2.0 * (T0 * dT2_dVg + T2 * dT0_dVg)), T3);
+    dT3_dVd = B3_Q((T1 * dT1_dVd - 2.0 * (T0 * dT2_dVd + T2 * dT0_dVd)), T3);
+    dT3_dVb = B3_Q((T1 * dT1_dVb - 2.0 * (T0 * dT2_dVb + T2 * dT0_dVb)), T3);
     (void)dT3_dVg; (void)dT3_dVd; (void)dT3_dVb;
     dVdsat_dVg = B3_DIV(dT1_dVg - B3_DIV(T1 * dT1_dVg - dT0_dVg * T2 - T0 * dT2_dVg, T3, rT3v) - Vdsat * dT0_dVg, T0, rT0v);
     dVdsat_dVb = B3_DIV(dT1_dVb - B3_DIV(T1 * dT1_dVb - dT0_dVb * T2 - T0 * dT2_dVb, T3, rT3v) - Vdsat * dT0_dVb, T0, rT0v);
@@ -669,7 +673,7 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
   dT0_dVb = dEsatL_dVb + dVdsat_dVb + T7 * tmp3 * Vgsteff - T8 * (dAbulk_dVb * Vdsat + Abulk * dVdsat_dVb);
   dT0_dVd = dEsatL_dVd + dVdsat_dVd - T8 * Abulk * dVdsat_dVd;
   T9 = WVCoxRds * Abulk;
-  T1 = 2.0 / Lambda - 1.0 + T9;
+  T1 = B3_Q(2.0, Lambda) - 1.0 + T9;
   dT1_dVg = -2.0 * tmp1 + WVCoxRds * (Abulk * tmp2 + dAbulk_dVg);
   dT1_dVb = dAbulk_dVb * WVCoxRds + T9 * tmp3;
   B3_RCP(rT1a, T1);
@@ -682,7 +686,7 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
 
   const double pclm = PRM(XG_B3_PCLM), litl = PRM(XG_B3_LITL);
   if ((pclm > 0.0) && (diffVds > 1.0e-10)) {
-    T0 = 1.0 / (pclm * Abulk * litl);
+    T0 = B3_Q(1.0, (pclm * Abulk * litl));
     B3_RCP(rAbulk, Abulk);
     dT0_dVb = B3_DIV(-T0, Abulk, rAbulk) * dAbulk_dVb;
     dT0_dVg = B3_DIV(-T0, Abulk, rAbulk) * dAbulk_dVg;
@@ -690,7 +694,7 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
     T1 = Leff * (Abulk + T2);
     dT1_dVg = Leff * (B3_DIV(1.0 - T2 * dEsatL_dVg, EsatL, rEsatL) + dAbulk_dVg);
     dT1_dVb = Leff * (dAbulk_dVb - B3_DIV(T2 * dEsatL_dVb, EsatL, rEsatL));
-    dT1_dVd = -T2 * dEsatL_dVd / Esat;
+    dT1_dVd = B3_Q(-T2 * dEsatL_dVd, Esat);
     T9 = T0 * T1;
     VACLM = T9 * diffVds;
     dVACLM_dVg = T0 * dT1_dVg * diffVds - T9 * dVdseff_dVg + T1 * diffVds * dT0_dVg;
@@ -722,13 +726,13 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
     dVADIBL_dVd = B3_DIV(B3_DIV(-dT0_dVd, T1, rT1r) + B3_DIV(T0 * dT1_dVd, T9, rT9r), T2, rthetaRout);
     T7 = pdiblb * Vbseff;
     if (T7 >= -0.9) {
-      T3 = 1.0 / (1.0 + T7);
+      T3 = B3_Q(1.0, (1.0 + T7));
       VADIBL *= T3;
       dVADIBL_dVg *= T3;
       dVADIBL_dVb = (dVADIBL_dVb - VADIBL * pdiblb) * T3;
       dVADIBL_dVd *= T3;
     } else {
-      T4 = 1.0 / (0.8 + T7);
+      T4 = B3_Q(1.0, (0.8 + T7));
       T3 = (17.0 + 20.0 * T7) * T4;
       dVADIBL_dVg *= T3;
       dVADIBL_dVb = dVADIBL_dVb * T3 - VADIBL * pdiblb * T4 * T4;
@@ -747,7 +751,7 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
     dT0_dVb = B3_DIV(-T9 * dEsatL_dVb, EsatL, rEsatL);
     dT0_dVd = B3_DIV(-T9 * dEsatL_dVd, EsatL, rEsatL);
   } else {
-    T1 = 1.0 / (17.0 + 20.0 * T9);
+    T1 = B3_Q(1.0, (17.0 + 20.0 * T9));
     T0 = (0.8 + T9) * T1;
     T1 *= T1;
     dT0_dVg = T8 * (1.0 - B3_DIV(Vgsteff * dEsatL_dVg, EsatL, rEsatL)) * T1;
@@ -758,7 +762,7 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
   tmp1 = VACLM * VACLM;
   tmp2 = VADIBL * VADIBL;
   tmp3 = VACLM + VADIBL;
-  T1 = VACLM * VADIBL / tmp3;
+  T1 = B3_Q(VACLM * VADIBL, tmp3);
   tmp3 *= tmp3;
   B3_RCP(rtmp3, tmp3);
   dT1_dVg = B3_DIV(tmp1 * dVADIBL_dVg + tmp2 * dVACLM_dVg, tmp3, rtmp3);
@@ -780,7 +784,7 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
       dVASCBE_dVd = -T1 * (1.0 - dVdseff_dVd);
       dVASCBE_dVb = T1 * dVdseff_dVb;
     } else {
-      VASCBE = MAX_EXP * Leff / pscbe2;
+      VASCBE = B3_Q(MAX_EXP * Leff, pscbe2);
       dVASCBE_dVg = dVASCBE_dVd = dVASCBE_dVb = 0.0;
     }
   } else {
@@ -921,7 +925,7 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
       qgate = CoxWL * k1ox * (T2 - T1);
       qbulk = -qgate;
       qdrn = 0.0;
-      T0 = CoxWL * T1 / T2;
+      T0 = B3_Q(CoxWL * T1, T2);
       cggb = T0 * dVgs_eff_dVg;
       cgdb = 0.0;
       cgsb = T0 * (dVbseff_dVb - dVgs_eff_dVg);
@@ -931,16 +935,16 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
       cbsb = -cgsb;
       qinv = 0.0;
     } else {
-      One_Third_CoxWL = CoxWL / 3.0;
+      One_Third_CoxWL = B3_DIVK(CoxWL, 3.0);
       Two_Third_CoxWL = 2.0 * One_Third_CoxWL;
       AbulkCV = Abulk0 * abulkCVfactor;
       dAbulkCV_dVb = abulkCVfactor * dAbulk0_dVb;
-      Vdsat = Vgst / AbulkCV;
-      dVdsat_dVg = dVgs_eff_dVg / AbulkCV;
-      dVdsat_dVb = -(Vdsat * dAbulkCV_dVb + dVth_dVb) / AbulkCV;
+      Vdsat = B3_Q(Vgst, AbulkCV);
+      dVdsat_dVg = B3_Q(dVgs_eff_dVg, AbulkCV);
+      dVdsat_dVb = B3_Q(-(Vdsat * dAbulkCV_dVb + dVth_dVb), AbulkCV);
       if (xpart > 0.5) {
         if (Vdsat <= Vds) {
-          T1 = Vdsat / 3.0;
+          T1 = B3_DIVK(Vdsat, 3.0);
           qgate = CoxWL * (Vgs_eff - Vfb - phi - T1);
           T2 = -Two_Third_CoxWL * Vgst;
           qbulk = -(qgate + T2);
@@ -956,9 +960,9 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
           cbdb = 0.0;
           qinv = -(qgate + qbulk);
         } else {
-          Alphaz = Vgst / Vdsat;
+          Alphaz = B3_Q(Vgst, Vdsat);
           T1 = 2.0 * Vdsat - Vds;
-          T2 = Vds / (3.0 * T1);
+          T2 = B3_Q(Vds, (3.0 * T1));
           T3 = T2 * Vds;
           T9 = 0.25 * CoxWL;
           T4 = T9 * Alphaz;
@@ -968,12 +972,12 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
           T10 = T4 * T8;
           qdrn = T4 * T7;
           qbulk = -(qgate + qdrn + T10);
-          T5 = T3 / T1;
+          T5 = B3_Q(T3, T1);
           cggb = CoxWL * (1.0 - T5 * dVdsat_dVg) * dVgs_eff_dVg;
           T11 = -CoxWL * T5 * dVdsat_dVb;
           cgdb = CoxWL * (T2 - 0.5 + 0.5 * T5);
           cgsb = -(cggb + T11 + cgdb);
-          T6 = 1.0 / Vdsat;
+          T6 = B3_Q(1.0, Vdsat);
           dAlphaz_dVg = T6 * (1.0 - Alphaz * dVdsat_dVg);
           dAlphaz_dVb = -T6 * (dVth_dVb + Alphaz * dVdsat_dVb);
           T7 = T9 * T7;
@@ -995,7 +999,7 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
         }
       } else if (xpart < 0.5) {
         if (Vds >= Vdsat) {
-          T1 = Vdsat / 3.0;
+          T1 = B3_DIVK(Vdsat, 3.0);
           qgate = CoxWL * (Vgs_eff - Vfb - phi - T1);
           T2 = -Two_Third_CoxWL * Vgst;
           qbulk = -(qgate + T2);
@@ -1015,31 +1019,31 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
           cbdb = 0.0;
           qinv = -(qgate + qbulk);
         } else {
-          Alphaz = Vgst / Vdsat;
+          Alphaz = B3_Q(Vgst, Vdsat);
           T1 = 2.0 * Vdsat - Vds;
-          T2 = Vds / (3.0 * T1);
+          T2 = B3_Q(Vds, (3.0 * T1));
           T3 = T2 * Vds;
           T9 = 0.25 * CoxWL;
           T4 = T9 * Alphaz;
           qgate = CoxWL * (Vgs_eff - Vfb - phi - 0.5 * (Vds - T3));
-          T5 = T3 / T1;
+          T5 = B3_Q(T3, T1);
           cggb = CoxWL * (1.0 - T5 * dVdsat_dVg) * dVgs_eff_dVg;
           tmp = -CoxWL * T5 * dVdsat_dVb;
           cgdb = CoxWL * (T2 - 0.5 + 0.5 * T5);
           cgsb = -(cggb + cgdb + tmp);
-          T6 = 1.0 / Vdsat;
+          T6 = B3_Q(1.0, Vdsat);
           dAlphaz_dVg = T6 * (1.0 - Alphaz * dVdsat_dVg);
           dAlphaz_dVb = -T6 * (dVth_dVb + Alphaz * dVdsat_dVb);
           T6 = 8.0 * Vdsat * Vdsat - 6.0 * Vdsat * Vds + 1.2 * Vds * Vds;
-          T8 = T2 / T1;
+          T8 = B3_Q(T2, T1);
           T7 = Vds - T1 - T8 * T6;
           qdrn = T4 * T7;
           T7 *= T9;
-          tmp = T8 / T1;
+          tmp = B3_Q(T8, T1);
           tmp1 = T4 * (2.0 - 4.0 * tmp * T6 + T8 * (16.0 * Vdsat - 6.0 * Vds));
           cdgb = (T7 * dAlphaz_dVg - tmp1 * dVdsat_dVg) * dVgs_eff_dVg;
           T10 = T7 * dAlphaz_dVb - tmp1 * dVdsat_dVb;
-          cddb = T4 * (2.0 - (1.0 / (3.0 * T1 * T1) + 2.0 * tmp) * T6 + T8 * (6.0 * Vdsat - 2.4 * Vds));
+          cddb = T4 * (2.0 - (B3_Q(1.0, (3.0 * T1 * T1)) + 2.0 * tmp) * T6 + T8 * (6.0 * Vdsat - 2.4 * Vds));
           cdsb = -(cdgb + T10 + cddb);
           T7 = 2.0 * (T1 + T3);
           qbulk = -(qgate - T4 * T7);
@@ -1056,7 +1060,7 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
         }
       } else {
         if (Vds >= Vdsat) {
-          T1 = Vdsat / 3.0;
+          T1 = B3_DIVK(Vdsat, 3.0);
           qgate = CoxWL * (Vgs_eff - Vfb - phi - T1);
           T2 = -Two_Third_CoxWL * Vgst;
           qbulk = -(qgate + T2);
@@ -1075,19 +1079,19 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
           cbdb = 0.0;
           qinv = -(qgate + qbulk);
         } else {
-          Alphaz = Vgst / Vdsat;
+          Alphaz = B3_Q(Vgst, Vdsat);
           T1 = 2.0 * Vdsat - Vds;
-          T2 = Vds / (3.0 * T1);
+          T2 = B3_Q(Vds, (3.0 * T1));
           T3 = T2 * Vds;
           T9 = 0.25 * CoxWL;
           T4 = T9 * Alphaz;
           qgate = CoxWL * (Vgs_eff - Vfb - phi - 0.5 * (Vds - T3));
-          T5 = T3 / T1;
+          T5 = B3_Q(T3, T1);
           cggb = CoxWL * (1.0 - T5 * dVdsat_dVg) * dVgs_eff_dVg;
           tmp = -CoxWL * T5 * dVdsat_dVb;
           cgdb = CoxWL * (T2 - 0.5 + 0.5 * T5);
           cgsb = -(cggb + cgdb + tmp);
-          T6 = 1.0 / Vdsat;
+          T6 = B3_Q(1.0, Vdsat);
           dAlphaz_dVg = T6 * (1.0 - Alphaz * dVdsat_dVg);
           dAlphaz_dVb = -T6 * (dVth_dVb + Alphaz * dVdsat_dVb);
           T7 = T1 + T3;
@@ -1120,7 +1124,7 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
     dnoff_dVb = PRM(XG_B3_NOFF) * dn_dVb;
     T0 = Vtm * noff;
     voffcv = PRM(XG_B3_VOFFCV);
-    VgstNVt = (Vgst - voffcv) / T0;
+    VgstNVt = B3_Q((Vgst - voffcv), T0);
     if (VgstNVt > EXP_THRESHOLD) {
       Vgsteff = Vgst - voffcv;
       dVgsteff_dVg = dVgs_eff_dVg;
@@ -1129,13 +1133,13 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
     } else if (VgstNVt < -EXP_THRESHOLD) {
       Vgsteff = T0 * log(1.0 + MIN_EXP);
       dVgsteff_dVg = 0.0;
-      dVgsteff_dVd = Vgsteff / noff;
+      dVgsteff_dVd = B3_Q(Vgsteff, noff);
       dVgsteff_dVb = dVgsteff_dVd * dnoff_dVb;
       dVgsteff_dVd *= dnoff_dVd;
     } else {
       ExpVgst = exp(VgstNVt);
       Vgsteff = T0 * log(1.0 + ExpVgst);
-      dVgsteff_dVg = ExpVgst / (1.0 + ExpVgst);
+      dVgsteff_dVg = B3_Q(ExpVgst, (1.0 + ExpVgst));
       B3_RCP(rnoff, noff);
       dVgsteff_dVd = -dVgsteff_dVg * (dVth_dVd + B3_DIV(Vgst - voffcv, noff, rnoff) * dnoff_dVd) +
                      B3_DIV(Vgsteff, noff, rnoff) * dnoff_dVd;
@@ -1154,7 +1158,7 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
       } else {
         T0 = 0.5 * k1ox;
         T1 = sqrt(T0 * T0 + Arg1);
-        T2 = CoxWL * T0 / T1;
+        T2 = B3_Q(CoxWL * T0, T1);
         qgate = CoxWL * k1ox * (T1 - T0);
         Cgg = T2 * (dVgs_eff_dVg - dVgsteff_dVg);
         Cgd = -T2 * dVgsteff_dVd;
@@ -1164,17 +1168,17 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
       Cbg = -Cgg;
       Cbd = -Cgd;
       Cbb = -Cgb;
-      One_Third_CoxWL = CoxWL / 3.0;
+      One_Third_CoxWL = B3_DIVK(CoxWL, 3.0);
       Two_Third_CoxWL = 2.0 * One_Third_CoxWL;
       AbulkCV = Abulk0 * abulkCVfactor;
       dAbulkCV_dVb = abulkCVfactor * dAbulk0_dVb;
-      VdsatCV = Vgsteff / AbulkCV;
+      VdsatCV = B3_Q(Vgsteff, AbulkCV);
       if (VdsatCV < Vds) {
-        dVdsatCV_dVg = 1.0 / AbulkCV;
-        dVdsatCV_dVb = -VdsatCV * dAbulkCV_dVb / AbulkCV;
-        T0 = Vgsteff - VdsatCV / 3.0;
-        dT0_dVg = 1.0 - dVdsatCV_dVg / 3.0;
-        dT0_dVb = -dVdsatCV_dVb / 3.0;
+        dVdsatCV_dVg = B3_Q(1.0, AbulkCV);
+        dVdsatCV_dVb = B3_Q(-VdsatCV * dAbulkCV_dVb, AbulkCV);
+        T0 = Vgsteff - B3_DIVK(VdsatCV, 3.0);
+        dT0_dVg = 1.0 - B3_DIVK(dVdsatCV_dVg, 3.0);
+        dT0_dVb = B3_DIVK(-dVdsatCV_dVb, 3.0);
         qgate += CoxWL * T0;
         Cgg1 = CoxWL * dT0_dVg;
         Cgb1 = CoxWL * dT0_dVb + Cgg1 * dVgsteff_dVb;
@@ -1207,10 +1211,10 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
       } else {
         T0 = AbulkCV * Vds;
         T1 = 12.0 * (Vgsteff - 0.5 * T0 + 1.e-20);
-        T2 = Vds / T1;
+        T2 = B3_Q(Vds, T1);
         T3 = T0 * T2;
         dT3_dVg = -12.0 * T2 * T2 * AbulkCV;
-        dT3_dVd = 6.0 * T0 * (4.0 * Vgsteff - T0) / T1 / T1 - 0.5;
+        dT3_dVd = B3_Q(B3_Q(6.0 * T0 * (4.0 * Vgsteff - T0), T1), T1) - 0.5;
         dT3_dVb = 12.0 * T2 * T2 * dAbulkCV_dVb * Vgsteff;
         qgate += CoxWL * (Vgsteff - 0.5 * Vds + T3);
         Cgg1 = CoxWL * (1.0 + dT3_dVg);
@@ -1230,22 +1234,22 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
         Cbd += Cbd1;
         if (xpart > 0.5) {
           T1 = T1 + T1;
-          qsrc = -CoxWL * (0.5 * Vgsteff + 0.25 * T0 - T0 * T0 / T1);
-          Csg = -CoxWL * (0.5 + 24.0 * T0 * Vds / T1 / T1 * AbulkCV);
-          Csb = -CoxWL * (0.25 * Vds * dAbulkCV_dVb - 12.0 * T0 * Vds / T1 / T1 * (4.0 * Vgsteff - T0) * dAbulkCV_dVb) +
+          qsrc = -CoxWL * (0.5 * Vgsteff + 0.25 * T0 - B3_Q(T0 * T0, T1));
+          Csg = -CoxWL * (0.5 + B3_Q(B3_Q(24.0 * T0 * Vds, T1), T1) * AbulkCV);
+          Csb = -CoxWL * (0.25 * Vds * dAbulkCV_dVb - B3_Q(B3_Q(12.0 * T0 * Vds, T1), T1) * (4.0 * Vgsteff - T0) * dAbulkCV_dVb) +
                 Csg * dVgsteff_dVb;
-          Csd = -CoxWL * (0.25 * AbulkCV - 12.0 * AbulkCV * T0 / T1 / T1 * (4.0 * Vgsteff - T0)) +
+          Csd = -CoxWL * (0.25 * AbulkCV - B3_Q(B3_Q(12.0 * AbulkCV * T0, T1), T1) * (4.0 * Vgsteff - T0)) +
                 Csg * dVgsteff_dVd;
           Csg *= dVgsteff_dVg;
         } else if (xpart < 0.5) {
-          T1 = T1 / 12.0;
-          T2 = 0.5 * CoxWL / (T1 * T1);
-          T3 = Vgsteff * (2.0 * T0 * T0 / 3.0 + Vgsteff * (Vgsteff - 4.0 * T0 / 3.0)) - 2.0 * T0 * T0 * T0 / 15.0;
+          T1 = B3_DIVK(T1, 12.0);
+          T2 = B3_Q(0.5 * CoxWL, (T1 * T1));
+          T3 = Vgsteff * (B3_DIVK(2.0 * T0 * T0, 3.0) + Vgsteff * (Vgsteff - B3_DIVK(4.0 * T0, 3.0))) - B3_DIVK(2.0 * T0 * T0 * T0, 15.0);
           qsrc = -T2 * T3;
-          T4 = 4.0 / 3.0 * Vgsteff * (Vgsteff - T0) + 0.4 * T0 * T0;
-          Csg = -2.0 * qsrc / T1 - T2 * (Vgsteff * (3.0 * Vgsteff - 8.0 * T0 / 3.0) + 2.0 * T0 * T0 / 3.0);
-          Csb = (qsrc / T1 * Vds + T2 * T4 * Vds) * dAbulkCV_dVb + Csg * dVgsteff_dVb;
-          Csd = (qsrc / T1 + T2 * T4) * AbulkCV + Csg * dVgsteff_dVd;
+          T4 = B3_DIVK(4.0, 3.0) * Vgsteff * (Vgsteff - T0) + 0.4 * T0 * T0;
+          Csg = B3_Q(-2.0 * qsrc, T1) - T2 * (Vgsteff * (3.0 * Vgsteff - B3_DIVK(8.0 * T0, 3.0)) + B3_DIVK(2.0 * T0 * T0, 3.0));
+          Csb = (B3_Q(qsrc, T1) * Vds + T2 * T4 * Vds) * dAbulkCV_dVb + Csg * dVgsteff_dVb;
+          Csd = (B3_Q(qsrc, T1) + T2 * T4) * AbulkCV + Csg * dVgsteff_dVd;
           Csg *= dVgsteff_dVg;
         } else {
           qsrc = -0.5 * (qgate + qbulk);
@@ -1273,12 +1277,12 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
       V3 = Vfb - Vgs_eff + VbseffCV - DELTA_3;
       if (Vfb <= 0.0) {
         T0 = sqrt(V3 * V3 - PRM(XG_B3_D3_VFBZB));  // 4 DELTA_3 Vfb, Vfb = vfbzb
-        T2 = -DELTA_3 / T0;
+        T2 = B3_Q(-DELTA_3, T0);
       } else {
         T0 = sqrt(V3 * V3 + PRM(XG_B3_D3_VFBZB));
-        T2 = DELTA_3 / T0;
+        T2 = B3_Q(DELTA_3, T0);
       }
-      T1 = 0.5 * (1.0 + V3 / T0);
+      T1 = 0.5 * (1.0 + B3_Q(V3, T0));
       Vfbeff = Vfb - 0.5 * (V3 + T0);
       dVfbeff_dVg = T1 * dVgs_eff_dVg;
       dVfbeff_dVb = -T1 * dVbseffCV_dVb;
@@ -1291,11 +1295,11 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
         T1 = 0.0;
         T2 = 0.0;
       } else if (T3 < 0.0) {
-        T1 = T0 + T3 / k1ox;
+        T1 = T0 + B3_Q(T3, k1ox);
         T2 = CoxWL;
       } else {
         T1 = sqrt(T0 * T0 + T3);
-        T2 = CoxWL * T0 / T1;
+        T2 = B3_Q(CoxWL * T0, T1);
       }
       Qsub0 = CoxWL * k1ox * (T1 - T0);
       dQsub0_dVg = T2 * (dVgs_eff_dVg - dVfbeff_dVg - dVgsteff_dVg);
@@ -1303,13 +1307,13 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
       dQsub0_dVb = -T2 * (dVfbeff_dVb + dVbseffCV_dVb + dVgsteff_dVb);
       AbulkCV = Abulk0 * abulkCVfactor;
       dAbulkCV_dVb = abulkCVfactor * dAbulk0_dVb;
-      VdsatCV = Vgsteff / AbulkCV;
+      VdsatCV = B3_Q(Vgsteff, AbulkCV);
       V4 = VdsatCV - Vds - DELTA_4;
       T0 = sqrt(V4 * V4 + 4.0 * DELTA_4 * VdsatCV);
       VdseffCV = VdsatCV - 0.5 * (V4 + T0);
-      T1 = 0.5 * (1.0 + V4 / T0);
-      T2 = DELTA_4 / T0;
-      T3 = (1.0 - T1 - T2) / AbulkCV;
+      T1 = 0.5 * (1.0 + B3_Q(V4, T0));
+      T2 = B3_Q(DELTA_4, T0);
+      T3 = B3_Q((1.0 - T1 - T2), AbulkCV);
       dVdseffCV_dVg = T3;
       dVdseffCV_dVd = T1;
       dVdseffCV_dVb = -T3 * VdsatCV * dAbulkCV_dVb;
@@ -1320,10 +1324,10 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
       }
       T0 = AbulkCV * VdseffCV;
       T1 = 12.0 * (Vgsteff - 0.5 * T0 + 1e-20);
-      T2 = VdseffCV / T1;
+      T2 = B3_Q(VdseffCV, T1);
       T3 = T0 * T2;
       T4 = (1.0 - 12.0 * T2 * T2 * AbulkCV);
-      T5 = (6.0 * T0 * (4.0 * Vgsteff - T0) / (T1 * T1) - 0.5);
+      T5 = (B3_Q(6.0 * T0 * (4.0 * Vgsteff - T0), (T1 * T1)) - 0.5);
       T6 = 12.0 * T2 * T2 * Vgsteff;
       qinoi = -CoxWL * (Vgsteff - 0.5 * T0 + AbulkCV * T3);
       qgate = CoxWL * (Vgsteff - 0.5 * VdseffCV + T3);
@@ -1342,9 +1346,9 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
       Cbg1 *= dVgsteff_dVg;
       if (xpart > 0.5) {
         T1 = T1 + T1;
-        qsrc = -CoxWL * (0.5 * Vgsteff + 0.25 * T0 - T0 * T0 / T1);
-        T7 = (4.0 * Vgsteff - T0) / (T1 * T1);
-        T4 = -(0.5 + 24.0 * T0 * T0 / (T1 * T1));
+        qsrc = -CoxWL * (0.5 * Vgsteff + 0.25 * T0 - B3_Q(T0 * T0, T1));
+        T7 = B3_Q((4.0 * Vgsteff - T0), (T1 * T1));
+        T4 = -(0.5 + B3_Q(24.0 * T0 * T0, (T1 * T1)));
         T5 = -(0.25 * AbulkCV - 12.0 * AbulkCV * T0 * T7);
         T6 = -(0.25 * VdseffCV - 12.0 * T0 * VdseffCV * T7);
         Csg = CoxWL * (T4 + T5 * dVdseffCV_dVg);
@@ -1352,14 +1356,14 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
         Csb = CoxWL * (T5 * dVdseffCV_dVb + T6 * dAbulkCV_dVb) + Csg * dVgsteff_dVb;
         Csg *= dVgsteff_dVg;
       } else if (xpart < 0.5) {
-        T1 = T1 / 12.0;
-        T2 = 0.5 * CoxWL / (T1 * T1);
-        T3 = Vgsteff * (2.0 * T0 * T0 / 3.0 + Vgsteff * (Vgsteff - 4.0 * T0 / 3.0)) - 2.0 * T0 * T0 * T0 / 15.0;
+        T1 = B3_DIVK(T1, 12.0);
+        T2 = B3_Q(0.5 * CoxWL, (T1 * T1));
+        T3 = Vgsteff * (B3_DIVK(2.0 * T0 * T0, 3.0) + Vgsteff * (Vgsteff - B3_DIVK(4.0 * T0, 3.0))) - B3_DIVK(2.0 * T0 * T0 * T0, 15.0);
         qsrc = -T2 * T3;
-        T7 = 4.0 / 3.0 * Vgsteff * (Vgsteff - T0) + 0.4 * T0 * T0;
-        T4 = -2.0 * qsrc / T1 - T2 * (Vgsteff * (3.0 * Vgsteff - 8.0 * T0 / 3.0) + 2.0 * T0 * T0 / 3.0);
-        T5 = (qsrc / T1 + T2 * T7) * AbulkCV;
-        T6 = (qsrc / T1 * VdseffCV + T2 * T7 * VdseffCV);
+        T7 = B3_DIVK(4.0, 3.0) * Vgsteff * (Vgsteff - T0) + 0.4 * T0 * T0;
+        T4 = B3_Q(-2.0 * qsrc, T1) - T2 * (Vgsteff * (3.0 * Vgsteff - B3_DIVK(8.0 * T0, 3.0)) + B3_DIVK(2.0 * T0 * T0, 3.0));
+        T5 = (B3_Q(qsrc, T1) + T2 * T7) * AbulkCV;
+        T6 = (B3_Q(qsrc, T1) * VdseffCV + T2 * T7 * VdseffCV);
         Csg = (T4 + T5 * dVdseffCV_dVg);
         Csd = T5 * dVdseffCV_dVd + Csg * dVgsteff_dVd;
         Csb = (T5 * dVdseffCV_dVb + T6 * dAbulkCV_dVb) + Csg * dVgsteff_dVb;
@@ -1429,12 +1433,12 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
       V3 = ldeb - Tcen - LINK;
       V4 = sqrt(V3 * V3 + PRM(XG_B3_LINK4_LDEB));
       Tcen = ldeb - 0.5 * (V3 + V4);
-      T1 = 0.5 * (1.0 + V3 / V4);
+      T1 = 0.5 * (1.0 + B3_Q(V3, V4));
       dTcen_dVg *= T1;
       dTcen_dVb *= T1;
       B3_RCP(rTcen, Tcen);
       Ccen = B3_DIV(EPSSI, Tcen, rTcen);
-      T2 = Cox / (Cox + Ccen);
+      T2 = B3_Q(Cox, (Cox + Ccen));
       Coxeff = T2 * Ccen;
       T3 = B3_DIV(-Ccen, Tcen, rTcen);
       dCoxeff_dVg = T2 * T2 * T3;
@@ -1452,11 +1456,11 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
         T1 = 0.0;
         T2 = 0.0;
       } else if (T3 < 0.0) {
-        T1 = T0 + T3 / k1ox;
+        T1 = T0 + B3_Q(T3, k1ox);
         T2 = CoxWLcen;
       } else {
         T1 = sqrt(T0 * T0 + T3);
-        T2 = CoxWLcen * T0 / T1;
+        T2 = B3_Q(CoxWLcen * T0, T1);
       }
       Qsub0 = CoxWLcen * k1ox * (T1 - T0);
       QovCox = B3_DIV(Qsub0, Coxeff, rCoxeff);
@@ -1467,7 +1471,7 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
       T0 = PRM(XG_B3_DPHI_T0);          // k1ox sqrtPhi, or 0.5 sqrtPhi
       T1 = 2.0 * T0 + Vgsteff;
       DeltaPhi = Vtm * log(1.0 + B3_DIV(T1 * Vgsteff, Denomi, PRM(XG_B3_R_DPHI_DENOMI)));
-      dDeltaPhi_dVg = PRM(XG_B3_VTM2) * (T1 - T0) / (Denomi + T1 * Vgsteff);
+      dDeltaPhi_dVg = B3_Q(PRM(XG_B3_VTM2) * (T1 - T0), (Denomi + T1 * Vgsteff));
       dDeltaPhi_dVd = dDeltaPhi_dVg * dVgsteff_dVd;
       dDeltaPhi_dVb = dDeltaPhi_dVg * dVgsteff_dVb;
       (void)dDeltaPhi_dVd; (void)dDeltaPhi_dVb;
@@ -1485,7 +1489,7 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
       }
       tmp = exp(0.7 * log(T0));
       T1 = 1.0 + tmp;
-      T2 = 0.7 * tmp / (T0 * Tox);
+      T2 = B3_Q(0.7 * tmp, (T0 * Tox));
       B3_RCP(rT1c, T1);
       Tcen = B3_DIV(1.9e-9, T1, rT1c);
       dTcen_dVg = B3_DIV(B3_DIV(-1.9e-9 * T2, T1, rT1c), T1, rT1c);
@@ -1495,7 +1499,7 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
       dTcen_dVg *= dVgsteff_dVg;
       B3_RCP(rTcen2, Tcen);
       Ccen = B3_DIV(EPSSI, Tcen, rTcen2);
-      T0 = Cox / (Cox + Ccen);
+      T0 = B3_Q(Cox, (Cox + Ccen));
       Coxeff = T0 * Ccen;
       T1 = B3_DIV(-Ccen, Tcen, rTcen2);
       dCoxeff_dVg = T0 * T0 * T1;
@@ -1551,12 +1555,12 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
       Cbb1 = CoxWLcen * (T11 * dVdseffCV_dVb + T12 * dAbulkCV_dVb) + Cbg1 * dVgsteff_dVb + QovCox * dCoxeff_dVb;
       Cbg1 = Cbg1 * dVgsteff_dVg + QovCox * dCoxeff_dVg;
       if (xpart > 0.5) {
-        qsrc = -CoxWLcen * (T1 / 2.0 + T0 / 4.0 - B3_DIV(0.5 * T0 * T0, T2, rT2h));
+        qsrc = -CoxWLcen * (B3_DIVK(T1, 2.0) + B3_DIVK(T0, 4.0) - B3_DIV(0.5 * T0 * T0, T2, rT2h));
         QovCox = B3_DIV(qsrc, Coxeff, rCoxeff2);
         T2 += T2;
         T3 = T2 * T2;
-        T7 = -(0.25 - 12.0 * T0 * (4.0 * T1 - T0) / T3);
-        T4 = -(0.5 + 24.0 * T0 * T0 / T3) * (1.0 - dDeltaPhi_dVg);
+        T7 = -(0.25 - B3_Q(12.0 * T0 * (4.0 * T1 - T0), T3));
+        T4 = -(0.5 + B3_Q(24.0 * T0 * T0, T3)) * (1.0 - dDeltaPhi_dVg);
         T5 = T7 * AbulkCV;
         T6 = T7 * VdseffCV;
         Csg = CoxWLcen * (T4 + T5 * dVdseffCV_dVg);
@@ -1571,7 +1575,7 @@ __global__ void __launch_bounds__(128) bsim3_kernel(DevType t, DevOptions o, Fla
              B3_DIVK(2.0 * T0 * T0 * T0, 15.0);
         qsrc = -T3 * T4;
         QovCox = B3_DIV(qsrc, Coxeff, rCoxeff2);
-        T8 = 4.0 / 3.0 * T1 * (T1 - T0) + 0.4 * T0 * T0;
+        T8 = B3_DIVK(4.0, 3.0) * T1 * (T1 - T0) + 0.4 * T0 * T0;
         T5 = B3_DIV(-2.0 * qsrc, T2, rT2x) -
              T3 * (T1 * (3.0 * T1 - B3_DIVK(8.0 * T0, 3.0)) + B3_DIVK(2.0 * T0 * T0, 3.0));
         T6 = AbulkCV * (B3_DIV(qsrc, T2, rT2x) + T3 * T8);
@@ -1707,16 +1711,16 @@ finished:
       qgso = PRM(XG_B3_CGSO) * vgs;
     } else if (capMod == 1) {
       if (vgd < 0.0) {
-        T1 = sqrt(1.0 - 4.0 * vgd / ckappa);
-        cgdo = PRM(XG_B3_CGDO) + weffCV * cgdl / T1;
+        T1 = sqrt(1.0 - B3_Q(4.0 * vgd, ckappa));
+        cgdo = PRM(XG_B3_CGDO) + B3_Q(weffCV * cgdl, T1);
         qgdo = PRM(XG_B3_CGDO) * vgd - weffCV * 0.5 * cgdl * ckappa * (T1 - 1.0);
       } else {
         cgdo = PRM(XG_B3_CGDO) + weffCV * cgdl;
         qgdo = (weffCV * cgdl + PRM(XG_B3_CGDO)) * vgd;
       }
       if (vgs < 0.0) {
-        T1 = sqrt(1.0 - 4.0 * vgs / ckappa);
-        cgso = PRM(XG_B3_CGSO) + weffCV * cgsl / T1;
+        T1 = sqrt(1.0 - B3_Q(4.0 * vgs, ckappa));
+        cgso = PRM(XG_B3_CGSO) + B3_Q(weffCV * cgsl, T1);
         qgso = PRM(XG_B3_CGSO) * vgs - weffCV * 0.5 * cgsl * ckappa * (T1 - 1.0);
       } else {
         cgso = PRM(XG_B3_CGSO) + weffCV * cgsl;
@@ -1728,14 +1732,14 @@ finished:
       T2 = 0.5 * (T0 - T1);
       T3 = PRM(XG_B3_CGDL_W);  // weffCV * cgdl
       T4 = sqrt(1.0 - B3_DIV(4.0 * T2, ckappa, PRM(XG_B3_R_CKAPPA)));
-      cgdo = PRM(XG_B3_CGDO_T) - T3 * (1.0 - 1.0 / T4) * (0.5 - 0.5 * T0 / T1);
+      cgdo = PRM(XG_B3_CGDO_T) - T3 * (1.0 - B3_Q(1.0, T4)) * (0.5 - B3_Q(0.5 * T0, T1));
       qgdo = PRM(XG_B3_CGDO_T) * vgd - T3 * (T2 + PRM(XG_B3_HALF_CKAPPA) * (T4 - 1.0));
       T0 = vgs + DELTA_1;
       T1 = sqrt(T0 * T0 + 4.0 * DELTA_1);
       T2 = 0.5 * (T0 - T1);
       T3 = PRM(XG_B3_CGSL_W);  // weffCV * cgsl
       T4 = sqrt(1.0 - B3_DIV(4.0 * T2, ckappa, PRM(XG_B3_R_CKAPPA)));
-      cgso = PRM(XG_B3_CGSO_T) - T3 * (1.0 - 1.0 / T4) * (0.5 - 0.5 * T0 / T1);
+      cgso = PRM(XG_B3_CGSO_T) - T3 * (1.0 - B3_Q(1.0, T4)) * (0.5 - B3_Q(0.5 * T0, T1));
       qgso = PRM(XG_B3_CGSO_T) * vgs - T3 * (T2 + PRM(XG_B3_HALF_CKAPPA) * (T4 - 1.0));
     }
     /* setupCapacitors_oldDAE: charge sums and partition (:7640-7898), nqsMod 0 */

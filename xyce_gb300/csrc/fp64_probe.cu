@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include "xg.h"
+#include "xg_fast_rcp.cuh"
 #include "xg_internal.h"
 
 namespace {
@@ -22,7 +23,28 @@ __global__ void __launch_bounds__(256) dfma_chains(double *out, int iters, doubl
   if (s == 1234.5678) out[blockIdx.x] = s;  // keeps the chains live
 }
 
+__global__ void reciprocals(const double *b, double *out, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = xg::fast_rcp(b[i]);
+}
+
 }  // namespace
+
+extern "C" int xg_probe_reciprocal(int n, const double *host_b, double *host_out) {
+  if (n < 0 || (n && (!host_b || !host_out))) return XG_ERR_ARG;
+  if (!n) return XG_OK;
+  double *d = nullptr;
+  if (cudaMalloc(&d, sizeof(double) * 2 * size_t(n)) != cudaSuccess) return XG_ERR_OOM;
+  cudaError_t e = cudaMemcpy(d, host_b, sizeof(double) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    reciprocals<<<(n + 255) / 256, 256>>>(d, d + n, n);
+    xg::count_launches(1);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(host_out, d + n, sizeof(double) * n, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  return e == cudaSuccess ? XG_OK : XG_ERR_CUDA;
+}
 
 extern "C" int xg_probe_fp64_rate(int cuda_device, double *flops_per_second) {
   if (!flops_per_second) return XG_ERR_ARG;

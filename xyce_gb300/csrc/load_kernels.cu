@@ -24,6 +24,7 @@
 
 #include <cstdint>
 
+#include "xg_fast_rcp.cuh"
 #include "xg_internal.h"
 
 #ifndef XG_NS

@@ -951,8 +951,15 @@ struct xg_batch {
   int n_walk = 0;                      // requests walked row by row (not on the level path)
   size_t solve_lvl = 0;                // > 0: batch_solve_lvl (for its requests) with this much
   int64_t bytes = 0;
-  // pinned host mirror of the request states
+  // pinned host mirror of the request states (the last poll's snapshot)
   xg::CState *h_cs = nullptr;
+  // every xg_batch_run ends with a copy of the request states into one of
+  // these pinned buffers and an event, so a poll can read the snapshot of a
+  // finished run while later runs are still on the device
+  static constexpr int kRing = 4;
+  xg::CState *h_ring[kRing] = {};
+  cudaEvent_t ring_ev[kRing] = {};
+  long long issued = 0, reported = 0;  // snapshots taken; the last one polled
   // slotted batches: the pool behind the slots (null for a fixed batch)
   xg::SlotPool *pool = nullptr;
 };
@@ -1177,6 +1184,10 @@ void free_batch(xg_batch *b) {
   for (int t = 0; t < XG_NUM_DEV_TYPES; ++t)
     if (b->d_cid[t]) cudaFree(b->d_cid[t]);
   if (b->h_cs) cudaFreeHost(b->h_cs);
+  for (int k = 0; k < xg_batch::kRing; ++k) {
+    if (b->h_ring[k]) cudaFreeHost(b->h_ring[k]);
+    if (b->ring_ev[k]) cudaEventDestroy(b->ring_ev[k]);
+  }
   if (b->ckt) xg_circuit_destroy(b->ckt);
   if (b->stream) cudaStreamDestroy(b->stream);
 }
@@ -1711,11 +1722,54 @@ extern "C" int xg_batch_run(xg_batch *b, int iterations) {
     }
     b->graph_iters = iterations;
   }
+  if (!b->h_ring[0]) {
+    for (int k = 0; k < xg_batch::kRing; ++k)
+      if (cudaMallocHost((void **)&b->h_ring[k], sizeof(xg::CState) * b->nc) != cudaSuccess ||
+          cudaEventCreateWithFlags(&b->ring_ev[k], cudaEventDisableTiming) != cudaSuccess) {
+        xg::set_error("xg_batch_run: out of pinned host memory");
+        return XG_ERR_OOM;
+      }
+  }
   if (cudaGraphLaunch(b->graph, b->stream) != cudaSuccess) {
     xg::set_error("xg_batch_run: cudaGraphLaunch failed");
     return XG_ERR_CUDA;
   }
   xg::count_launches(iterations * b->graph_launches_per_iter);
+  const int k = int(b->issued % xg_batch::kRing);
+  if (cudaMemcpyAsync(b->h_ring[k], b->dev.cs, sizeof(xg::CState) * b->nc, cudaMemcpyDeviceToHost,
+                      b->stream) != cudaSuccess ||
+      cudaEventRecord(b->ring_ev[k], b->stream) != cudaSuccess) {
+    xg::set_error("xg_batch_run: snapshot failed");
+    return XG_ERR_CUDA;
+  }
+  ++b->issued;
+  return XG_OK;
+}
+
+// The newest finished snapshot not yet polled (0: none); snapshots finish in
+// the order of their runs on the batch's stream.
+static long long newest_snapshot(xg_batch *b) {
+  long long newest = 0;
+  for (long long j = std::max(b->reported + 1, b->issued - xg_batch::kRing + 1); j <= b->issued; ++j) {
+    if (cudaEventQuery(b->ring_ev[(j - 1) % xg_batch::kRing]) != cudaSuccess) break;
+    newest = j;
+  }
+  cudaGetLastError();  // a not-ready query is not an error
+  return newest;
+}
+
+extern "C" int xg_batch_inflight(xg_batch *b, int *n) {
+  if (!b || !n) {
+    xg::set_error("xg_batch_inflight: bad argument");
+    return XG_ERR_ARG;
+  }
+  long long done = b->reported;
+  for (long long j = std::max(b->reported + 1, b->issued - xg_batch::kRing + 1); j <= b->issued; ++j) {
+    if (cudaEventQuery(b->ring_ev[(j - 1) % xg_batch::kRing]) != cudaSuccess) break;
+    done = j;
+  }
+  cudaGetLastError();
+  *n = int(b->issued - done);
   return XG_OK;
 }
 
@@ -1724,13 +1778,21 @@ extern "C" int xg_batch_poll(xg_batch *b, int wait, int *n_done) {
     xg::set_error("xg_batch_poll: bad argument");
     return XG_ERR_ARG;
   }
-  if (!wait && cudaStreamQuery(b->stream) == cudaErrorNotReady) {
-    *n_done = -1;  // still running
-    return XG_OK;
+  if (wait && cudaStreamSynchronize(b->stream) != cudaSuccess) {
+    xg::set_error("xg_batch_poll: the batch failed");
+    return XG_ERR_CUDA;
   }
-  if (cudaMemcpyAsync(b->h_cs, b->dev.cs, sizeof(xg::CState) * b->nc, cudaMemcpyDeviceToHost,
-                      b->stream) != cudaSuccess ||
-      cudaStreamSynchronize(b->stream) != cudaSuccess) {
+  const long long j = newest_snapshot(b);
+  if (j) {
+    // the states as the newest finished run left them
+    std::memcpy(b->h_cs, b->h_ring[(j - 1) % xg_batch::kRing], sizeof(xg::CState) * b->nc);
+    b->reported = j;
+  } else if (!wait) {
+    *n_done = -1;  // no run has finished since the last poll
+    return XG_OK;
+  } else if (cudaMemcpyAsync(b->h_cs, b->dev.cs, sizeof(xg::CState) * b->nc, cudaMemcpyDeviceToHost,
+                             b->stream) != cudaSuccess ||
+             cudaStreamSynchronize(b->stream) != cudaSuccess) {
     xg::set_error("xg_batch_poll: copy failed");
     return XG_ERR_CUDA;
   }

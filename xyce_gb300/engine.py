@@ -79,6 +79,7 @@ def lib():
     L.xg_load.argtypes = [vp, C.POINTER(abi.XgLoadFlags)]
     L.xg_load_noalloc.argtypes = [vp, C.POINTER(abi.XgLoadFlags), vp, C.c_int64]
     L.xg_probe_fp64_rate.argtypes = [i, C.POINTER(C.c_double)]
+    L.xg_probe_reciprocal.argtypes = [i, vp, vp]
     L.xg_lu_analyze.argtypes = [vp, i, vp, vp, vp, i, C.POINTER(vp)]
     L.xg_lu_refactor.argtypes = [vp, vp]
     L.xg_lu_solve.argtypes = [vp, vp, vp, i]
@@ -96,6 +97,7 @@ def lib():
                                   C.POINTER(vp)]
     L.xg_batch_run.argtypes = [vp, i]
     L.xg_batch_poll.argtypes = [vp, i, C.POINTER(i)]
+    L.xg_batch_inflight.argtypes = [vp, C.POINTER(i)]
     L.xg_batch_results.argtypes = [vp, i, vp, vp, C.POINTER(i), C.POINTER(abi.XgTranStats)]
     L.xg_batch_info.argtypes = [vp, C.POINTER(i), i64p]
     L.xg_batch_destroy.argtypes = [vp]
@@ -402,6 +404,12 @@ class Batch:
 
     def run(self, iterations):
         check(lib().xg_batch_run(self.h, iterations))
+
+    def inflight(self):
+        """Runs enqueued and not finished yet."""
+        k = C.c_int()
+        check(lib().xg_batch_inflight(self.h, C.byref(k)))
+        return k.value
 
     def poll(self, wait=True):
         d = C.c_int()
