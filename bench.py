@@ -55,6 +55,10 @@ WORKLOADS = {
                                  dev_type=abi.DEV_BSIM3),
     "single_load_bsim3_100k": dict(kind="random", n_dev=100_000, n_nodes=25_000,
                                    dev_type=abi.DEV_BSIM3),
+    # the same at 300,000 instances: its terms and reduction lists (~220 MB)
+    # exceed L2, its device memory (~1.2 GB) suits a profiler capture
+    "single_load_bsim3_300k": dict(kind="random", n_dev=300_000, n_nodes=75_000,
+                                   dev_type=abi.DEV_BSIM3),
     # the same shape (1,000,000 MOSFETs, half NMOS / half PMOS, W~U[0.2,10]um,
     # L~U[0.1,1]um, random 250k-node netlist, node voltages U[0,1.8]V) on the
     # level-1 model

@@ -77,7 +77,9 @@ struct xg_circuit {
   uint32_t *d_term_pos = nullptr;  // scatter layout: term -> position in reduction order
   uint32_t *d_red_idx = nullptr;   // gather layout: reduction entry -> term
   int64_t *d_long_out = nullptr; // outputs reduced by a warp each
-  int64_t *d_short_order = nullptr; // the others, by term count
+  int64_t *d_short_order = nullptr; // the others, by term count (scatter layout)
+  xg::EllBucket *d_ell = nullptr;    // gather layout: the others as ELL buckets
+  uint32_t *d_ell_out = nullptr, *d_ell_idx = nullptr;
   double *d_diode_vd = nullptr;  // Diode Instance::Vd carried between loads
   double *d_b3_mem = nullptr;    // BSIM3 members carried between loads
   bool state_done = false;
@@ -109,6 +111,9 @@ void free_circuit(xg_circuit *c) {
   cudaFree(c->d_red_ptr);
   cudaFree(c->d_long_out);
   cudaFree(c->d_short_order);
+  cudaFree(c->d_ell);
+  cudaFree(c->d_ell_out);
+  cudaFree(c->d_ell_idx);
   cudaFree(c->d_term_pos);
   cudaFree(c->d_red_idx);
   cudaFree(c->d_diode_vd);
@@ -229,25 +234,42 @@ int circuit_view(xg_circuit *c, CircuitView *v) {
   v->opt = DevOptions{c->opt.gmin, c->opt.voltlim};
   v->io = LoadIO{c->d_sol[0], c->d_sta[1], c->d_sto[1], c->d_sta[0], c->d_sto[0], c->d_terms, c->d_term_pos,
                  c->d_diode_vd, c->d_b3_mem, c->d_sta[1]};
-  v->red_ptr = c->d_red_ptr;
-  v->red_idx = c->d_red_idx;
-  v->long_out = c->d_long_out;
-  v->short_order = c->d_short_order;
+  v->red = ReduceLists{c->d_red_ptr, c->d_red_idx, c->d_long_out, c->d_short_order,
+                       c->plan.ell.empty() ? nullptr : c->d_ell, c->d_ell_out, c->d_ell_idx};
   return XG_OK;
 }
 
-ReduceArgs reduce_args(const Plan &P, const double *terms, const int64_t *red_ptr,
-                       const uint32_t *d_red_idx, const int64_t *d_long_out,
-                       const int64_t *d_short_order, double *out, int64_t o0, int64_t o1) {
+ReduceArgs reduce_args(const Plan &P, const double *terms, const ReduceLists &L, double *out, int64_t o0,
+                       int64_t o1) {
   auto lo = std::lower_bound(P.long_out.begin(), P.long_out.end(), o0);
   auto hi = std::lower_bound(P.long_out.begin(), P.long_out.end(), o1);
   // the short outputs of [o0, o1): the vector part, the matrix part or both
   const int64_t n_short = (int64_t)P.short_order.size();
   const int64_t s0 = o0 >= P.n_vec_out ? P.n_short_vec : 0;
   const int64_t s1 = o1 <= P.n_vec_out ? P.n_short_vec : n_short;
-  return ReduceArgs{terms, red_ptr, P.scatter_terms ? nullptr : d_red_idx,
-                    d_long_out + (lo - P.long_out.begin()),
-                    (int64_t)(hi - lo), d_short_order + s0, s1 - s0, out, o0, o1};
+  ReduceArgs a{terms, L.red_ptr, P.scatter_terms ? nullptr : L.red_idx,
+               L.long_out + (lo - P.long_out.begin()),
+               (int64_t)(hi - lo), L.short_order + s0, s1 - s0, out, o0, o1};
+  a.ell = nullptr;
+  a.b0 = a.b1 = 0;
+  a.ell_block0 = a.ell_blocks = 0;
+  a.ell_out = a.ell_idx = nullptr;
+  if (L.ell && !P.ell.empty()) {
+    // the same parts as buckets
+    const int nb = (int)P.ell.size();
+    a.ell = L.ell;
+    a.b0 = o0 >= P.n_vec_out ? P.n_ell_vec : 0;
+    a.b1 = o1 <= P.n_vec_out ? P.n_ell_vec : nb;
+    auto blocks_of = [&](int b) { return (P.ell[(size_t)b].m + kEllThreads - 1) / kEllThreads; };
+    if (a.b1 > a.b0) {
+      a.ell_block0 = P.ell[(size_t)a.b0].block0;
+      a.ell_blocks = P.ell[(size_t)a.b1 - 1].block0 + blocks_of(a.b1 - 1) - a.ell_block0;
+    }
+    a.ell_out = L.ell_out;
+    a.ell_idx = L.ell_idx;
+    a.n_short = 0;
+  }
+  return a;
 }
 
 }  // namespace xg
@@ -365,8 +387,24 @@ int xg_circuit_create(xg_ctx *ctx, const xg_netlist *nl, xg_circuit **out) {
       cudaMemcpy(c->d_red_idx, P.red_idx.data(), P.red_idx.size() * sizeof(uint32_t),
                  cudaMemcpyHostToDevice) != cudaSuccess) rc = fail(XG_ERR_CUDA, "copy red_idx");
   if (!rc) rc = dalloc(&c->d_long_out, (int64_t)P.long_out.size());
-  if (!rc) rc = dalloc(&c->d_short_order, (int64_t)P.short_order.size());
-  if (!rc && !P.short_order.empty() &&
+  if (!rc && !P.ell.empty()) {
+    rc = dalloc(&c->d_ell, (int64_t)P.ell.size());
+    if (!rc) rc = dalloc(&c->d_ell_out, (int64_t)P.ell_out.size());
+    if (!rc) rc = dalloc(&c->d_ell_idx, (int64_t)P.ell_idx.size());
+    if (!rc && (cudaMemcpy(c->d_ell, P.ell.data(), P.ell.size() * sizeof(xg::EllBucket),
+                           cudaMemcpyHostToDevice) != cudaSuccess ||
+                (!P.ell_out.empty() &&
+                 cudaMemcpy(c->d_ell_out, P.ell_out.data(), P.ell_out.size() * sizeof(uint32_t),
+                            cudaMemcpyHostToDevice) != cudaSuccess) ||
+                (!P.ell_idx.empty() &&
+                 cudaMemcpy(c->d_ell_idx, P.ell_idx.data(), P.ell_idx.size() * sizeof(uint32_t),
+                            cudaMemcpyHostToDevice) != cudaSuccess)))
+      rc = fail(XG_ERR_CUDA, "copy ELL lists");
+  }
+  // the scatter layout's short outputs by term count (the gather layout uses
+  // the ELL buckets)
+  if (!rc) rc = dalloc(&c->d_short_order, P.ell.empty() ? (int64_t)P.short_order.size() : 1);
+  if (!rc && P.ell.empty() && !P.short_order.empty() &&
       cudaMemcpy(c->d_short_order, P.short_order.data(), P.short_order.size() * sizeof(int64_t),
                  cudaMemcpyHostToDevice) != cudaSuccess) rc = fail(XG_ERR_CUDA, "copy short_order");
   if (!rc && !P.long_out.empty() &&
@@ -411,6 +449,8 @@ int xg_circuit_create(xg_ctx *ctx, const xg_netlist *nl, xg_circuit **out) {
   }
   // The host copies of the reduction lists are no longer needed.
   std::vector<uint32_t>().swap(P.red_idx);
+  std::vector<uint32_t>().swap(P.ell_out);
+  std::vector<uint32_t>().swap(P.ell_idx);
   *out = c;
   return XG_OK;
 }
@@ -564,8 +604,9 @@ int xg_update_state(xg_circuit *c, const xg_load_flags *flags) {
 }
 
 static int reduce_range(xg_circuit *c, int64_t o0, int64_t o1) {
-  const xg::ReduceArgs a = xg::reduce_args(c->plan, c->d_terms, c->d_red_ptr, c->d_red_idx,
-                                           c->d_long_out, c->d_short_order, c->d_out, o0, o1);
+  xg::CircuitView v;
+  xg::circuit_view(c, &v);
+  const xg::ReduceArgs a = xg::reduce_args(c->plan, c->d_terms, v.red, c->d_out, o0, o1);
   int rc = c->opt.fma ? xg::fast::launch_reduce(a, c->ctx->stream)
                       : xg::exact::launch_reduce(a, c->ctx->stream);
   return rc ? fail(rc, "reduce kernel launch failed") : XG_OK;

@@ -757,6 +757,26 @@ __global__ void __launch_bounds__(kRedThreads) reduce_kernel(ReduceArgs a, int l
     return;
 #endif
   }
+  if (a.ell) {
+    // gather layout: a thread per short output, its bucket found by the
+    // block; every term number loaded coalesced, all of them in flight
+    const int64_t g = a.ell_block0 + ((int64_t)blockIdx.x - long_blocks);
+    int lo = a.b0, hi = a.b1 - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(&a.ell[mid].block0) <= g) lo = mid;
+      else hi = mid - 1;
+    }
+    const EllBucket B = a.ell[lo];
+    const int64_t k = (g - B.block0) * kEllThreads + threadIdx.x;
+    if (k >= B.m) return;
+    const uint32_t *ix = a.ell_idx + B.idx0 + k;
+    double s = 0.0;
+#pragma unroll 8
+    for (int j = 0; j < B.c; ++j) s += __ldg(a.terms + __ldg(ix + (int64_t)j * B.m));
+    a.out[__ldg(a.ell_out + B.out0 + k)] = s;
+    return;
+  }
   // short outputs in order of term count: the lanes of a warp run loops of
   // the same length
   const int64_t nb = (int64_t)gridDim.x - long_blocks;
@@ -796,16 +816,20 @@ int launch_eval(int dev_type, const DevType &t, const DevOptions &o, const Flags
 
 int launch_reduce(const ReduceArgs &a, void *stream) {
   const int64_t n = a.n_short;
-  if (n <= 0 && a.n_long <= 0) return XG_OK;
+  if (n <= 0 && a.n_long <= 0 && a.ell_blocks <= 0) return XG_OK;
   const int sms = sm_count();
-  int grid = (int)std::max<int64_t>(1, (n + kRedThreads - 1) / kRedThreads);
+  int64_t grid = std::max<int64_t>(1, (n + kRedThreads - 1) / kRedThreads);
   if (grid > sms * 32) grid = sms * 32;
+  if (a.ell) grid = a.ell_blocks;  // one thread per short output
+  static_assert(kEllThreads == kRedThreads, "the ELL buckets are cut in blocks of the reduction's size");
 #if XG_SPLIT_SUMS
   const int long_blocks = (int)std::min<int64_t>(a.n_long, sms * 8);  // a block per long output
 #else
   const int long_blocks = (int)std::min<int64_t>((a.n_long + kRedWarps - 1) / kRedWarps, sms * 8);
 #endif
-  reduce_kernel<<<grid + long_blocks, kRedThreads, 0, (cudaStream_t)stream>>>(a, long_blocks); xg::count_launches(1);
+  if (grid + long_blocks <= 0) return XG_OK;
+  reduce_kernel<<<(unsigned)(grid + long_blocks), kRedThreads, 0, (cudaStream_t)stream>>>(a, long_blocks);
+  xg::count_launches(1);
   return cudaGetLastError() == cudaSuccess ? XG_OK : XG_ERR_CUDA;
 }
 

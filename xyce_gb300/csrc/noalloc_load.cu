@@ -101,7 +101,7 @@ extern "C" int xg_load_noalloc(xg_circuit *c, const xg_load_flags *flags, double
       return rc;
     }
   }
-  const xg::ReduceArgs ra = xg::reduce_args(P, scratch, v.red_ptr, v.red_idx, v.long_out, v.short_order, dev_out, 0,
+  const xg::ReduceArgs ra = xg::reduce_args(P, scratch, v.red, dev_out, 0,
                                             P.n_out);
   rc = v.fma ? xg::fast::launch_reduce(ra, v.stream) : xg::exact::launch_reduce(ra, v.stream);
   if (rc) xg::set_error("xg_load_noalloc: reduction kernel launch failed");

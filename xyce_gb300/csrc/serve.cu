@@ -1261,7 +1261,7 @@ int enqueue_iteration(xg_batch *b) {
   }
   double *out = nullptr;
   xg_vec_device_ptr(b->ckt, XG_VEC_F, &out);
-  const ReduceArgs ra = reduce_args(P, v.io.terms, v.red_ptr, v.red_idx, v.long_out, v.short_order, out, 0, P.n_out);
+  const ReduceArgs ra = reduce_args(P, v.io.terms, v.red, out, 0, P.n_out);
   int rc = v.fma ? fast::launch_reduce(ra, s) : exact::launch_reduce(ra, s);
   if (rc) return rc;
   batch_combine<<<b->nc, kBatchThreads, 0, s>>>(b->dev);

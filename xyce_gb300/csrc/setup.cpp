@@ -889,6 +889,39 @@ int build_plan(const xg_netlist *nl, const xg_device_options *opt, Plan *plan, s
   };
   bucket(P.short_order.begin(), mid);
   bucket(mid, P.short_order.end());
+  // gather layout: the short outputs as ELL buckets, one per run of equal
+  // term counts in each part (short_order is grouped that way)
+  P.ell.clear();
+  P.ell_out.clear();
+  P.ell_idx.clear();
+  P.n_ell_vec = 0;
+  if (!P.scatter_terms) {
+    int64_t blocks = 0;
+    auto part = [&](int64_t s0, int64_t s1) {
+      for (int64_t k = s0; k < s1;) {
+        const int64_t o0 = P.short_order[(size_t)k];
+        const int32_t c = int32_t(P.red_ptr[(size_t)o0 + 1] - P.red_ptr[(size_t)o0]);
+        int64_t e = k + 1;
+        while (e < s1) {
+          const int64_t o = P.short_order[(size_t)e];
+          if (P.red_ptr[(size_t)o + 1] - P.red_ptr[(size_t)o] != c) break;
+          ++e;
+        }
+        const int64_t m = e - k;
+        EllBucket b{(int64_t)P.ell_out.size(), (int64_t)P.ell_idx.size(), blocks, int32_t(m), c};
+        P.ell.push_back(b);
+        for (int64_t q = k; q < e; ++q) P.ell_out.push_back((uint32_t)P.short_order[(size_t)q]);
+        for (int32_t j = 0; j < c; ++j)
+          for (int64_t q = k; q < e; ++q)
+            P.ell_idx.push_back(P.red_idx[(size_t)(P.red_ptr[(size_t)P.short_order[(size_t)q]] + j)]);
+        blocks += (m + kEllThreads - 1) / kEllThreads;
+        k = e;
+      }
+    };
+    part(0, P.n_short_vec);
+    P.n_ell_vec = (int)P.ell.size();
+    part(P.n_short_vec, (int64_t)P.short_order.size());
+  }
   return XG_OK;
 }
 

@@ -90,6 +90,18 @@ struct LoadIO {
   double *sta_curr_w;       // current state, written on the first transient step
 };
 
+// The gather layout's short outputs, grouped by term count (a sliced ELL
+// layout): bucket b holds m outputs of c terms each; its output numbers are
+// ell_out[out0 .. out0+m) and term j of its k-th output is term
+// ell_idx[idx0 + j*m + k], so a thread per output reads its term numbers
+// coalesced with its neighbours' and has all of them in flight at once.
+// block0: the bucket's first block in a launch over all buckets.
+struct EllBucket {
+  int64_t out0, idx0, block0;
+  int32_t m, c;
+};
+constexpr int kEllThreads = 256;
+
 // Everything setup derives from a netlist (host side).
 struct Plan {
   int n_nodes = 0, n_unknowns = 0, n_state = 0, n_store = 0;
@@ -121,8 +133,14 @@ struct Plan {
   // sorted by term count: a warp then sums segments of one length
   std::vector<int64_t> short_order;
   int64_t n_short_vec = 0;    // short outputs in [0, n_vec_out)
+  // gather layout: the short outputs again as ELL buckets, the vector part's
+  // (n_ell_vec of them) first, then the matrix part's
+  std::vector<EllBucket> ell;
+  int n_ell_vec = 0;
+  std::vector<uint32_t> ell_out, ell_idx;
 };
 constexpr int64_t kLongSegment = 64;
+
 
 // The reduction's device data and the long outputs inside [o0, o1).
 struct ReduceArgs {
@@ -135,6 +153,23 @@ struct ReduceArgs {
   int64_t n_short;
   double *out;
   int64_t o0, o1;
+  // gather layout: the short outputs of [o0, o1) as buckets [b0, b1) of the
+  // ELL lists (null: the short_order path), ell_blocks blocks from block
+  // ell_block0 on
+  const EllBucket *ell;
+  int b0, b1;
+  int64_t ell_block0, ell_blocks;
+  const uint32_t *ell_out, *ell_idx;
+};
+
+// A circuit's reduction lists on the device.
+struct ReduceLists {
+  const int64_t *red_ptr;
+  const uint32_t *red_idx;     // gather layout only (else null)
+  const int64_t *long_out;     // device copy of plan->long_out
+  const int64_t *short_order;  // device copy of plan->short_order (scatter layout)
+  const EllBucket *ell;        // gather layout: the ELL lists (else null)
+  const uint32_t *ell_out, *ell_idx;
 };
 
 // setup.cpp
@@ -153,17 +188,13 @@ struct CircuitView {
   int fma;
   DevOptions opt;
   LoadIO io;                   // terms = the circuit's own term buffer
-  const int64_t *red_ptr;
-  const uint32_t *red_idx;     // gather layout only (else null)
-  const int64_t *long_out;     // device copy of plan->long_out
-  const int64_t *short_order;  // device copy of plan->short_order
+  ReduceLists red;
 };
 int circuit_view(xg_circuit *c, CircuitView *v);
 // ReduceArgs for outputs [o0, o1) of a circuit's plan (long outputs located
 // on the host copy, addressed in the device copy).
-ReduceArgs reduce_args(const Plan &P, const double *terms, const int64_t *red_ptr,
-                       const uint32_t *d_red_idx, const int64_t *d_long_out,
-                       const int64_t *d_short_order, double *out, int64_t o0, int64_t o1);
+ReduceArgs reduce_args(const Plan &P, const double *terms, const ReduceLists &L, double *out, int64_t o0,
+                       int64_t o1);
 void set_error(const std::string &msg);
 // Kernel launches of this library, counted at every launch site (api.cpp).
 void count_launches(int k);
