@@ -74,11 +74,9 @@ struct xg_circuit {
   double *d_out = nullptr;       // [F | Q | dFdxdVp | dQdxdVp | dFdx | dQdx]
   double *d_terms = nullptr;     // per-load stamp terms
   int64_t *d_red_ptr = nullptr;
-  uint32_t *d_term_pos = nullptr;  // scatter layout: term -> position in reduction order
-  uint32_t *d_red_idx = nullptr;   // gather layout: reduction entry -> term
+  uint32_t *d_red_idx = nullptr;   // reduction entry -> term
   int64_t *d_long_out = nullptr; // outputs reduced by a warp each
-  int64_t *d_short_order = nullptr; // the others, by term count (scatter layout)
-  xg::EllBucket *d_ell = nullptr;    // gather layout: the others as ELL buckets
+  xg::EllBucket *d_ell = nullptr;    // the others as ELL buckets
   uint32_t *d_ell_out = nullptr, *d_ell_idx = nullptr;
   double *d_diode_vd = nullptr;  // Diode Instance::Vd carried between loads
   double *d_b3_mem = nullptr;    // BSIM3 members carried between loads
@@ -110,11 +108,9 @@ void free_circuit(xg_circuit *c) {
   cudaFree(c->d_terms);
   cudaFree(c->d_red_ptr);
   cudaFree(c->d_long_out);
-  cudaFree(c->d_short_order);
   cudaFree(c->d_ell);
   cudaFree(c->d_ell_out);
   cudaFree(c->d_ell_idx);
-  cudaFree(c->d_term_pos);
   cudaFree(c->d_red_idx);
   cudaFree(c->d_diode_vd);
   cudaFree(c->d_b3_mem);
@@ -232,10 +228,9 @@ int circuit_view(xg_circuit *c, CircuitView *v) {
   v->stream = (void *)c->ctx->stream;
   v->fma = c->opt.fma;
   v->opt = DevOptions{c->opt.gmin, c->opt.voltlim};
-  v->io = LoadIO{c->d_sol[0], c->d_sta[1], c->d_sto[1], c->d_sta[0], c->d_sto[0], c->d_terms, c->d_term_pos,
+  v->io = LoadIO{c->d_sol[0], c->d_sta[1], c->d_sto[1], c->d_sta[0], c->d_sto[0], c->d_terms,
                  c->d_diode_vd, c->d_b3_mem, c->d_sta[1]};
-  v->red = ReduceLists{c->d_red_ptr, c->d_red_idx, c->d_long_out, c->d_short_order,
-                       c->plan.ell.empty() ? nullptr : c->d_ell, c->d_ell_out, c->d_ell_idx};
+  v->red = ReduceLists{c->d_red_ptr, c->d_red_idx, c->d_long_out, c->d_ell, c->d_ell_out, c->d_ell_idx};
   return XG_OK;
 }
 
@@ -243,32 +238,21 @@ ReduceArgs reduce_args(const Plan &P, const double *terms, const ReduceLists &L,
                        int64_t o1) {
   auto lo = std::lower_bound(P.long_out.begin(), P.long_out.end(), o0);
   auto hi = std::lower_bound(P.long_out.begin(), P.long_out.end(), o1);
-  // the short outputs of [o0, o1): the vector part, the matrix part or both
-  const int64_t n_short = (int64_t)P.short_order.size();
-  const int64_t s0 = o0 >= P.n_vec_out ? P.n_short_vec : 0;
-  const int64_t s1 = o1 <= P.n_vec_out ? P.n_short_vec : n_short;
-  ReduceArgs a{terms, L.red_ptr, P.scatter_terms ? nullptr : L.red_idx,
-               L.long_out + (lo - P.long_out.begin()),
-               (int64_t)(hi - lo), L.short_order + s0, s1 - s0, out, o0, o1};
-  a.ell = nullptr;
-  a.b0 = a.b1 = 0;
+  ReduceArgs a{terms, L.red_ptr, L.red_idx, L.long_out + (lo - P.long_out.begin()), (int64_t)(hi - lo),
+               out, o0, o1};
+  // the short outputs of [o0, o1) (the vector part, the matrix part or both)
+  // as buckets
+  a.ell = L.ell;
+  a.b0 = o0 >= P.n_vec_out ? P.n_ell_vec : 0;
+  a.b1 = o1 <= P.n_vec_out ? P.n_ell_vec : (int)P.ell.size();
   a.ell_block0 = a.ell_blocks = 0;
-  a.ell_out = a.ell_idx = nullptr;
-  if (L.ell && !P.ell.empty()) {
-    // the same parts as buckets
-    const int nb = (int)P.ell.size();
-    a.ell = L.ell;
-    a.b0 = o0 >= P.n_vec_out ? P.n_ell_vec : 0;
-    a.b1 = o1 <= P.n_vec_out ? P.n_ell_vec : nb;
-    auto blocks_of = [&](int b) { return (P.ell[(size_t)b].m + kEllThreads - 1) / kEllThreads; };
-    if (a.b1 > a.b0) {
-      a.ell_block0 = P.ell[(size_t)a.b0].block0;
-      a.ell_blocks = P.ell[(size_t)a.b1 - 1].block0 + blocks_of(a.b1 - 1) - a.ell_block0;
-    }
-    a.ell_out = L.ell_out;
-    a.ell_idx = L.ell_idx;
-    a.n_short = 0;
+  if (a.b1 > a.b0) {
+    const EllBucket &last = P.ell[(size_t)a.b1 - 1];
+    a.ell_block0 = P.ell[(size_t)a.b0].block0;
+    a.ell_blocks = last.block0 + (last.m + kEllThreads - 1) / kEllThreads - a.ell_block0;
   }
+  a.ell_out = L.ell_out;
+  a.ell_idx = L.ell_idx;
   return a;
 }
 
@@ -379,11 +363,10 @@ int xg_circuit_create(xg_ctx *ctx, const xg_netlist *nl, xg_circuit **out) {
     if (!rc) rc = dalloc(&c->d_sto[k], P.n_store);
   }
   if (!rc) rc = dalloc(&c->d_out, P.n_out);
-  if (!rc) rc = dalloc(&c->d_terms, P.n_terms + 1);  // + the discard slot
+  if (!rc) rc = dalloc(&c->d_terms, P.n_terms);
   if (!rc) rc = dalloc(&c->d_red_ptr, P.n_out + 1);
-  if (!rc && P.scatter_terms) rc = dalloc(&c->d_term_pos, (int64_t)P.term_pos.size());
-  if (!rc && !P.scatter_terms) rc = dalloc(&c->d_red_idx, (int64_t)P.red_idx.size());
-  if (!rc && !P.scatter_terms && !P.red_idx.empty() &&
+  if (!rc) rc = dalloc(&c->d_red_idx, (int64_t)P.red_idx.size());
+  if (!rc && !P.red_idx.empty() &&
       cudaMemcpy(c->d_red_idx, P.red_idx.data(), P.red_idx.size() * sizeof(uint32_t),
                  cudaMemcpyHostToDevice) != cudaSuccess) rc = fail(XG_ERR_CUDA, "copy red_idx");
   if (!rc) rc = dalloc(&c->d_long_out, (int64_t)P.long_out.size());
@@ -401,12 +384,6 @@ int xg_circuit_create(xg_ctx *ctx, const xg_netlist *nl, xg_circuit **out) {
                             cudaMemcpyHostToDevice) != cudaSuccess)))
       rc = fail(XG_ERR_CUDA, "copy ELL lists");
   }
-  // the scatter layout's short outputs by term count (the gather layout uses
-  // the ELL buckets)
-  if (!rc) rc = dalloc(&c->d_short_order, P.ell.empty() ? (int64_t)P.short_order.size() : 1);
-  if (!rc && P.ell.empty() && !P.short_order.empty() &&
-      cudaMemcpy(c->d_short_order, P.short_order.data(), P.short_order.size() * sizeof(int64_t),
-                 cudaMemcpyHostToDevice) != cudaSuccess) rc = fail(XG_ERR_CUDA, "copy short_order");
   if (!rc && !P.long_out.empty() &&
       cudaMemcpy(c->d_long_out, P.long_out.data(), P.long_out.size() * sizeof(int64_t),
                  cudaMemcpyHostToDevice) != cudaSuccess) rc = fail(XG_ERR_CUDA, "copy long_out");
@@ -424,9 +401,6 @@ int xg_circuit_create(xg_ctx *ctx, const xg_netlist *nl, xg_circuit **out) {
   }
   if (!rc && cudaMemcpy(c->d_red_ptr, P.red_ptr.data(), P.red_ptr.size() * sizeof(int64_t),
                         cudaMemcpyHostToDevice) != cudaSuccess) rc = fail(XG_ERR_CUDA, "copy red_ptr");
-  if (!rc && P.scatter_terms && !P.term_pos.empty() &&
-      cudaMemcpy(c->d_term_pos, P.term_pos.data(), P.term_pos.size() * sizeof(uint32_t),
-                 cudaMemcpyHostToDevice) != cudaSuccess) rc = fail(XG_ERR_CUDA, "copy term_pos");
   if (!rc) {
     cudaError_t e = cudaSuccess;
     for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
@@ -451,6 +425,7 @@ int xg_circuit_create(xg_ctx *ctx, const xg_netlist *nl, xg_circuit **out) {
   std::vector<uint32_t>().swap(P.red_idx);
   std::vector<uint32_t>().swap(P.ell_out);
   std::vector<uint32_t>().swap(P.ell_idx);
+  std::vector<int64_t>().swap(P.short_order);
   *out = c;
   return XG_OK;
 }
@@ -473,7 +448,7 @@ int xg_circuit_get_info(const xg_circuit *c, xg_circuit_info *info) {
   info->n_store = P.n_store;
   info->nnz = P.nnz;
   info->n_terms = P.n_terms;
-  info->scratch_bytes = (P.n_terms + 1) * (int64_t)sizeof(double);
+  info->scratch_bytes = P.n_terms * (int64_t)sizeof(double);
   for (int t = 0; t < XG_NUM_DEV_TYPES; ++t) info->n_instances[t] = P.T[t].n;
   return XG_OK;
 }
@@ -588,7 +563,7 @@ int xg_update_state(xg_circuit *c, const xg_load_flags *flags) {
   xg::Flags f{flags->dcop, flags->tranop, flags->acop, flags->transient, flags->init_jct,
               flags->init_fix, flags->newton_iter, flags->inputop, flags->pdt, flags->time,
               flags->init_tran};
-  xg::LoadIO io{c->d_sol[0], c->d_sta[1], c->d_sto[1], c->d_sta[0], c->d_sto[0], c->d_terms, c->d_term_pos,
+  xg::LoadIO io{c->d_sol[0], c->d_sta[1], c->d_sto[1], c->d_sta[0], c->d_sto[0], c->d_terms,
                 c->d_diode_vd, c->d_b3_mem, c->d_sta[1]};
   for (int k = 0; k < P.n_order; ++k) {
     int t = P.order[k];

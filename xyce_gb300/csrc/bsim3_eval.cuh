@@ -1859,7 +1859,7 @@ finished:
     ceqbs -= (cbs);
     ceqbd -= (cbd);
   }
-  Terms T{io.terms + (io.term_pos ? 0 : t.term0), io.term_pos ? io.term_pos + t.term0 : nullptr, nI};
+  Terms T{io.terms + t.term0, nI};
   T.put(0, i, drainConductance != 0.0 ? Idrain * numberParallel : 0.0);
   T.put(1, i, sourceConductance != 0.0 ? Isource * numberParallel : 0.0);
   T.put(2, i, (ceqbs + ceqbd) * numberParallel);

@@ -138,18 +138,12 @@ __device__ __forceinline__ void qmeyer(double vgs, double vgd, double von, doubl
   }
 }
 
-// Term writer: term q of instance i.
-// A term goes either straight to its place in reduction order (scatter
-// layout: each output then sums a contiguous run of terms) or to [q][i]
-// (gather layout: the reduction gathers them).
+// Term writer: term q of instance i at [q][i], so a warp's store of one term
+// fills whole sectors; the reduction gathers them.
 struct Terms {
   double *__restrict__ base;
-  const uint32_t *__restrict__ pos;
   int n;
-  __device__ __forceinline__ void put(int q, int i, double v) const {
-    const int64_t k = (int64_t)q * n + i;
-    base[pos ? (int64_t)__ldg(pos + k) : k] = v;
-  }
+  __device__ __forceinline__ void put(int q, int i, double v) const { base[(int64_t)q * n + i] = v; }
 };
 
 // Batched loads: take instance i's circuit flags; false when the instance is
@@ -176,7 +170,7 @@ __global__ void __launch_bounds__(256) res_kernel(DevType t, LoadIO io) {
   int lp = ld(t.lid + i), ln = ld(t.lid + n + i);
   double G = ld(t.p + i);
   double i0 = (ld(io.sol + lp) - ld(io.sol + ln)) * G;
-  Terms T{io.terms + (io.term_pos ? 0 : t.term0), io.term_pos ? io.term_pos + t.term0 : nullptr, n};
+  Terms T{io.terms + t.term0, n};
   T.put(0, i, i0);
   T.put(1, i, -i0);
   T.put(2, i, G);
@@ -195,7 +189,7 @@ __global__ void __launch_bounds__(256) cap_kernel(DevType t, LoadIO io) {
   double vcap = ld(io.sol + lp) - ld(io.sol + ln);
   double q0 = C * vcap;
   io.sta[t.sta0 + i] = q0;
-  Terms T{io.terms + (io.term_pos ? 0 : t.term0), io.term_pos ? io.term_pos + t.term0 : nullptr, n};
+  Terms T{io.terms + t.term0, n};
   T.put(0, i, q0);
   T.put(1, i, -q0);
   T.put(2, i, C);
@@ -234,7 +228,7 @@ __global__ void __launch_bounds__(256) vsrc_kernel(DevType t, Flags f, LoadIO io
     source = ld(t.p + XG_V_V1 * n + i);
   double srcCurrent = ld(io.sol + lb);
   double srcDrop = (ld(io.sol + lp) - ld(io.sol + ln));
-  Terms T{io.terms + (io.term_pos ? 0 : t.term0), io.term_pos ? io.term_pos + t.term0 : nullptr, n};
+  Terms T{io.terms + t.term0, n};
   T.put(0, i, srcCurrent);
   T.put(1, i, -srcCurrent);
   T.put(2, i, srcDrop);
@@ -256,7 +250,7 @@ __global__ void __launch_bounds__(256) isrc_kernel(DevType t, Flags f, LoadIO io
     source = pulse_value(t.p, n, i, f.time);
   else
     source = ld(t.p + XG_V_V1 * n + i);
-  Terms T{io.terms + (io.term_pos ? 0 : t.term0), io.term_pos ? io.term_pos + t.term0 : nullptr, n};
+  Terms T{io.terms + t.term0, n};
   T.put(0, i, source);
   T.put(1, i, -source);
 }
@@ -352,7 +346,7 @@ __global__ void __launch_bounds__(256) diode_kernel(DevType t, DevOptions o, Fla
   const double Gspr = PRM(XG_D_GSPR);
 #undef PRM
   double Ir = Gspr * (Vp - Vpp);
-  Terms T{io.terms + (io.term_pos ? 0 : t.term0), io.term_pos ? io.term_pos + t.term0 : nullptr, n};
+  Terms T{io.terms + t.term0, n};
   T.put(0, i, -(-Ir));
   T.put(1, i, -Id);
   T.put(2, i, -(-Id + Ir));
@@ -626,7 +620,7 @@ __global__ void __launch_bounds__(128) mos1_kernel(DevType t, DevOptions o, Flag
   // Master::loadDAEVectors
   const double numberParallel = PRM(XG_M1_M);
 #undef PRM
-  Terms T{io.terms + (io.term_pos ? 0 : t.term0), io.term_pos ? io.term_pos + t.term0 : nullptr, n};
+  Terms T{io.terms + t.term0, n};
   const double ceqbs = dtype * (cbs), ceqbd = dtype * (cbd);
   const double ceqgb = 0.0, ceqgs = 0.0, ceqgd = 0.0;
   T.put(0, i, drainConductance != 0.0 ? Idrain * numberParallel : 0.0);
@@ -722,7 +716,7 @@ __global__ void __launch_bounds__(kRedThreads) reduce_kernel(ReduceArgs a, int l
       double s = 0.0;
 #pragma unroll 4
       for (int64_t j = b + threadIdx.x; j < e; j += blockDim.x)
-        s += __ldg(a.terms + (a.red_idx ? (int64_t)__ldg(a.red_idx + j) : j));
+        s += __ldg(a.terms + __ldg(a.red_idx + j));
 #pragma unroll
       for (int m = 16; m > 0; m >>= 1) s += __shfl_xor_sync(0xffffffffu, s, m);
       if (lane == 0) part[wid] = s;
@@ -746,7 +740,7 @@ __global__ void __launch_bounds__(kRedThreads) reduce_kernel(ReduceArgs a, int l
       for (int64_t base = b; base < e; base += kRedChunk) {
         const int cnt = (int)(e - base < kRedChunk ? e - base : kRedChunk);
         for (int j = lane; j < cnt; j += 32)
-          buf[wid][j] = __ldg(a.terms + (a.red_idx ? (int64_t)__ldg(a.red_idx + base + j) : base + j));
+          buf[wid][j] = __ldg(a.terms + __ldg(a.red_idx + base + j));
         __syncwarp();
         if (lane == 0)
           for (int j = 0; j < cnt; ++j) s += buf[wid][j];
@@ -757,40 +751,23 @@ __global__ void __launch_bounds__(kRedThreads) reduce_kernel(ReduceArgs a, int l
     return;
 #endif
   }
-  if (a.ell) {
-    // gather layout: a thread per short output, its bucket found by the
-    // block; every term number loaded coalesced, all of them in flight
-    const int64_t g = a.ell_block0 + ((int64_t)blockIdx.x - long_blocks);
-    int lo = a.b0, hi = a.b1 - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (__ldg(&a.ell[mid].block0) <= g) lo = mid;
-      else hi = mid - 1;
-    }
-    const EllBucket B = a.ell[lo];
-    const int64_t k = (g - B.block0) * kEllThreads + threadIdx.x;
-    if (k >= B.m) return;
-    const uint32_t *ix = a.ell_idx + B.idx0 + k;
-    double s = 0.0;
+  // a thread per short output, its bucket found by the block; every term
+  // number loaded coalesced, all of them in flight
+  const int64_t g = a.ell_block0 + ((int64_t)blockIdx.x - long_blocks);
+  int lo = a.b0, hi = a.b1 - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&a.ell[mid].block0) <= g) lo = mid;
+    else hi = mid - 1;
+  }
+  const EllBucket B = a.ell[lo];
+  const int64_t k = (g - B.block0) * kEllThreads + threadIdx.x;
+  if (k >= B.m) return;
+  const uint32_t *ix = a.ell_idx + B.idx0 + k;
+  double s = 0.0;
 #pragma unroll 8
-    for (int j = 0; j < B.c; ++j) s += __ldg(a.terms + __ldg(ix + (int64_t)j * B.m));
-    a.out[__ldg(a.ell_out + B.out0 + k)] = s;
-    return;
-  }
-  // short outputs in order of term count: the lanes of a warp run loops of
-  // the same length
-  const int64_t nb = (int64_t)gridDim.x - long_blocks;
-  for (int64_t k = ((int64_t)blockIdx.x - long_blocks) * blockDim.x + threadIdx.x; k < a.n_short;
-       k += nb * blockDim.x) {
-    const int64_t o = __ldg(a.short_order + k);
-    const int64_t b = __ldg(a.red_ptr + o), e = __ldg(a.red_ptr + o + 1);
-    double s = 0.0;
-    if (a.red_idx)
-      for (int64_t j = b; j < e; ++j) s += __ldg(a.terms + __ldg(a.red_idx + j));
-    else
-      for (int64_t j = b; j < e; ++j) s += __ldg(a.terms + j);
-    a.out[o] = s;
-  }
+  for (int j = 0; j < B.c; ++j) s += __ldg(a.terms + __ldg(ix + (int64_t)j * B.m));
+  a.out[__ldg(a.ell_out + B.out0 + k)] = s;
 }
 
 int grid_for(int64_t n, int block) { return (int)((n + block - 1) / block); }
@@ -815,12 +792,9 @@ int launch_eval(int dev_type, const DevType &t, const DevOptions &o, const Flags
 }
 
 int launch_reduce(const ReduceArgs &a, void *stream) {
-  const int64_t n = a.n_short;
-  if (n <= 0 && a.n_long <= 0 && a.ell_blocks <= 0) return XG_OK;
+  if (a.n_long <= 0 && a.ell_blocks <= 0) return XG_OK;
   const int sms = sm_count();
-  int64_t grid = std::max<int64_t>(1, (n + kRedThreads - 1) / kRedThreads);
-  if (grid > sms * 32) grid = sms * 32;
-  if (a.ell) grid = a.ell_blocks;  // one thread per short output
+  const int64_t grid = a.ell_blocks;  // one thread per short output
   static_assert(kEllThreads == kRedThreads, "the ELL buckets are cut in blocks of the reduction's size");
 #if XG_SPLIT_SUMS
   const int long_blocks = (int)std::min<int64_t>(a.n_long, sms * 8);  // a block per long output

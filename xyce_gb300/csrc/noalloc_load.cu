@@ -70,7 +70,7 @@ extern "C" int xg_load_noalloc(xg_circuit *c, const xg_load_flags *flags, double
     xg::set_error("xg_load_noalloc: output buffer shorter than the circuit's outputs");
     return XG_ERR_ARG;
   }
-  if (P.n_terms + 1 > kScratchTerms) {  // the terms and their discard slot
+  if (P.n_terms > kScratchTerms) {
     xg::set_error("xg_load_noalloc: circuit needs " + std::to_string(P.n_terms) +
                   " stamp terms; the fixed scratch array holds " +
                   std::to_string(kScratchTerms) + " (use xg_load)");

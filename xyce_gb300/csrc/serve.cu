@@ -2203,7 +2203,7 @@ int run_staging(SlotPool *p, const Staging &st) {
 }
 
 LoadIO pool_io(const SlotPool *p) {
-  return LoadIO{p->sol[0], p->sta[1], p->sto[1], p->sta[0], p->sto[0], p->terms, nullptr,
+  return LoadIO{p->sol[0], p->sta[1], p->sto[1], p->sta[0], p->sto[0], p->terms,
                 p->diode_vd, p->b3_mem, p->sta[1]};
 }
 

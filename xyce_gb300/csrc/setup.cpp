@@ -861,16 +861,6 @@ int build_plan(const xg_netlist *nl, const xg_device_options *opt, Plan *plan, s
       }
     }
   }
-  // scatter layout unless BSIM3 terms make up half of all terms; terms with
-  // no output (a stamp on the ground row or column) then go to a discard slot
-  // after the last real one
-  const int64_t b3_terms = (int64_t)P.T[XG_DEV_BSIM3].n * P.T[XG_DEV_BSIM3].nterm;
-  P.scatter_terms = 2 * b3_terms < P.n_terms;
-  P.term_pos.clear();
-  if (P.scatter_terms) {
-    P.term_pos.assign((size_t)P.n_terms, (uint32_t)P.red_idx.size());
-    for (size_t j = 0; j < P.red_idx.size(); ++j) P.term_pos[P.red_idx[j]] = (uint32_t)j;
-  }
   P.long_out.clear();
   P.short_order.clear();
   for (int64_t o = 0; o < P.n_out; ++o) {
@@ -889,13 +879,13 @@ int build_plan(const xg_netlist *nl, const xg_device_options *opt, Plan *plan, s
   };
   bucket(P.short_order.begin(), mid);
   bucket(mid, P.short_order.end());
-  // gather layout: the short outputs as ELL buckets, one per run of equal
-  // term counts in each part (short_order is grouped that way)
+  // the short outputs as ELL buckets, one per run of equal term counts in
+  // each part (short_order is grouped that way)
   P.ell.clear();
   P.ell_out.clear();
   P.ell_idx.clear();
   P.n_ell_vec = 0;
-  if (!P.scatter_terms) {
+  {
     int64_t blocks = 0;
     auto part = [&](int64_t s0, int64_t s1) {
       for (int64_t k = s0; k < s1;) {

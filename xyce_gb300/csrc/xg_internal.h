@@ -82,16 +82,13 @@ struct LoadIO {
   const double *sol;        // next solution, n_unknowns + 1 (ground = 0)
   const double *sta_curr, *sto_curr;
   double *sta, *sto;        // next state / store (sto holds previous iterate on entry)
-  double *terms;            // per-load stamp terms
-  const uint32_t *term_pos; // scatter layout: where term q of instance i goes,
-                            // term_pos[term0 + q*n + i]; null: [q][i] layout
+  double *terms;            // per-load stamp terms, term q of instance i at term0 + q*n + i
   double *diode_vd;         // Diode Instance::Vd carried between loads
   double *b3_mem;           // BSIM3 members carried between loads, [k*n + i]
   double *sta_curr_w;       // current state, written on the first transient step
 };
 
-// The gather layout's short outputs, grouped by term count (a sliced ELL
-// layout): bucket b holds m outputs of c terms each; its output numbers are
+// The short outputs, grouped by term count (a sliced ELL layout): bucket b holds m outputs of c terms each; its output numbers are
 // ell_out[out0 .. out0+m) and term j of its k-th output is term
 // ell_idx[idx0 + j*m + k], so a thread per output reads its term numbers
 // coalesced with its neighbours' and has all of them in flight at once.
@@ -118,14 +115,8 @@ struct Plan {
   // summed, in reference order, into output o
   std::vector<int64_t> red_ptr;
   std::vector<uint32_t> red_idx;
-  // Term layout.  scatter_terms: each term (term0 + q*n + i) is written at
-  // its position in reduction order (term_pos) and output o sums the
-  // contiguous terms [red_ptr[o], red_ptr[o+1]); otherwise terms are written
-  // in [q][i] order and output o gathers terms red_idx[red_ptr[o]..].  The
-  // scattered store is nearly free in the level-1/diode/linear kernels; the
-  // register-bound BSIM3 kernel absorbs it worse than the reduction gains.
-  bool scatter_terms = false;
-  std::vector<uint32_t> term_pos;
+  // Terms are written in [q][i] order (a warp's stores fill whole sectors)
+  // and output o gathers terms red_idx[red_ptr[o]..red_ptr[o+1]).
   // outputs summing more than kLongSegment terms (a supply node's row), in
   // ascending order: reduced by a warp each instead of a thread
   std::vector<int64_t> long_out;
@@ -133,8 +124,8 @@ struct Plan {
   // sorted by term count: a warp then sums segments of one length
   std::vector<int64_t> short_order;
   int64_t n_short_vec = 0;    // short outputs in [0, n_vec_out)
-  // gather layout: the short outputs again as ELL buckets, the vector part's
-  // (n_ell_vec of them) first, then the matrix part's
+  // the short outputs as ELL buckets, the vector part's (n_ell_vec of them)
+  // first, then the matrix part's
   std::vector<EllBucket> ell;
   int n_ell_vec = 0;
   std::vector<uint32_t> ell_out, ell_idx;
@@ -146,16 +137,13 @@ constexpr int64_t kLongSegment = 64;
 struct ReduceArgs {
   const double *terms;
   const int64_t *red_ptr;
-  const uint32_t *red_idx;    // gather layout: term of each reduction entry; null: contiguous
+  const uint32_t *red_idx;    // term of each reduction entry
   const int64_t *long_out;    // device, the sub-range of long outputs in [o0, o1)
   int64_t n_long;
-  const int64_t *short_order; // device, the short outputs of [o0, o1) by term count
-  int64_t n_short;
   double *out;
   int64_t o0, o1;
-  // gather layout: the short outputs of [o0, o1) as buckets [b0, b1) of the
-  // ELL lists (null: the short_order path), ell_blocks blocks from block
-  // ell_block0 on
+  // the short outputs of [o0, o1) as buckets [b0, b1) of the ELL lists,
+  // ell_blocks blocks from block ell_block0 on
   const EllBucket *ell;
   int b0, b1;
   int64_t ell_block0, ell_blocks;
@@ -165,10 +153,9 @@ struct ReduceArgs {
 // A circuit's reduction lists on the device.
 struct ReduceLists {
   const int64_t *red_ptr;
-  const uint32_t *red_idx;     // gather layout only (else null)
+  const uint32_t *red_idx;
   const int64_t *long_out;     // device copy of plan->long_out
-  const int64_t *short_order;  // device copy of plan->short_order (scatter layout)
-  const EllBucket *ell;        // gather layout: the ELL lists (else null)
+  const EllBucket *ell;        // the short outputs' ELL lists
   const uint32_t *ell_out, *ell_idx;
 };
 
