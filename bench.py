@@ -1047,6 +1047,12 @@ DEFAULT_WORKLOAD = "single_load_bsim3_1M"
 # 1,000-stage inverter chain's whole .TRAN 1ps 20ns; served solves per second
 # and latency of the 10,000-request Monte-Carlo ring stream).
 SUB_NEWTON = dict(workload="tran_inverter_chain_1000", steps=3, warmup=1, fp32=False)
+# the two LU-bound transients: the 200x200 power grid's first 3 ps and the
+# 500k-BSIM3 random logic's first 10 ps, Newton iterations per second
+SUB_NEWTON_LARGE = {
+    "newton_power_grid_200x200": dict(workload="tran_power_grid_200x200", steps=2, warmup=1, fp32=False),
+    "newton_random_logic_500k": dict(workload="tran_random_logic_500k", steps=2, warmup=1, fp32=False),
+}
 SUB_SERVE = dict(workload="serve_ring_mc_10k", steps=1, warmup=1, sweep_rates="100,2000",
                  no_sweep=False)
 
@@ -1061,15 +1067,20 @@ def _sub_args(args, over):
 
 def run_default(args, world, rank, local, dist):
     """The single load (headline line) with the Newton and serving metrics
-    as sub-records of the same line."""
+    as sub-records of the same line: the 1,000-stage chain, the power grid
+    and the random logic transients, and the served stream."""
     line = run_xg(args, world, rank, local, dist, emit=False)
     newton = run_tran(_sub_args(args, SUB_NEWTON), world, rank, local, dist, emit=False)
+    large = {k: run_tran(_sub_args(args, v), world, rank, local, dist, emit=False)
+             for k, v in SUB_NEWTON_LARGE.items()}
     serving = run_serve(_sub_args(args, SUB_SERVE), world, rank, local, dist, emit=False)
     if rank != 0:
         return 0
     line["newton"] = newton
+    line.update(large)
     line["serving"] = serving
     line["gpu_launches_sub"] = {"newton": newton["gpu_launches"], "serving": serving["gpu_launches"]}
+    line["gpu_launches_sub"].update({k: v["gpu_launches"] for k, v in large.items()})
     return _emit(line, True)
 
 
@@ -1078,6 +1089,8 @@ def run_default_reference(args, world, rank):
         return 0
     line = run_reference(args, world, rank, emit=False)
     line["newton"] = run_tran_reference(_sub_args(args, SUB_NEWTON), world, rank, emit=False)
+    for k, v in SUB_NEWTON_LARGE.items():
+        line[k] = run_tran_reference(_sub_args(args, v), world, rank, emit=False)
     line["serving"] = run_serve_reference(_sub_args(args, SUB_SERVE), world, rank, emit=False)
     return _emit(line, True)
 
