@@ -332,10 +332,13 @@ def run_serve(args, world, rank, local, dist, emit=True):
         return serve.Server(ctx, precision=prec, n_refine=nref, **params)
 
     # the schedule, picked by the autotuner on a smaller probe stream of the
-    # same kind (not timed), per server
+    # same kind (not timed), per server: long enough (half a second of
+    # arrivals at 2,000/s) to hold as many requests in flight as the stream
+    # does, so a schedule with too few slots shows up in the probe
     def probe():
-        return (serve.ring_mc_requests(200, seed=7, tstop=w["tstop"]),
-                serve.poisson_arrivals(200, w["rate"], seed=8))
+        n = min(w["n"], 1000)
+        return (serve.ring_mc_requests(n, seed=7, tstop=w["tstop"]),
+                serve.poisson_arrivals(n, w["rate"], seed=8))
 
     def run_once(kind, prec, nref, params, reqs, arr):
         srv = make(kind, prec, nref, params)
