@@ -306,10 +306,11 @@ def run_tran(args, world, rank, local, dist, emit=True):
 
 
 SERVE_METRIC = "served solves/sec"
-# the slot server's schedule grid: slots per batch, batch iterations per
-# launch chunk, batches per size class
-SLOT_TUNING = dict(grid={"slots": (256, 512, 1024), "chunk": (16, 32, 64), "max_batches_per_class": (1, 2, 4)},
-                   start={"slots": 512, "chunk": 32, "max_batches_per_class": 2})
+# the slot server's schedule grid: slots per batch and batch iterations per
+# launch chunk (how many batches a size class opens is demand, bounded by the
+# memory admission, not a schedule)
+SLOT_TUNING = dict(grid={"slots": (256, 512, 1024), "chunk": (16, 32, 64)},
+                   start={"slots": 512, "chunk": 32})
 
 
 def run_serve(args, world, rank, local, dist, emit=True):

@@ -249,7 +249,7 @@ ReduceArgs reduce_args(const Plan &P, const double *terms, const ReduceLists &L,
   if (a.b1 > a.b0) {
     const EllBucket &last = P.ell[(size_t)a.b1 - 1];
     a.ell_block0 = P.ell[(size_t)a.b0].block0;
-    a.ell_blocks = last.block0 + (last.m + kEllThreads - 1) / kEllThreads - a.ell_block0;
+    a.ell_blocks = last.block0 + (last.m + kEllPerBlock - 1) / kEllPerBlock - a.ell_block0;
   }
   a.ell_out = L.ell_out;
   a.ell_idx = L.ell_idx;

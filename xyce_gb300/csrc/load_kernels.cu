@@ -751,8 +751,11 @@ __global__ void __launch_bounds__(kRedThreads) reduce_kernel(ReduceArgs a, int l
     return;
 #endif
   }
-  // a thread per short output, its bucket found by the block; every term
-  // number loaded coalesced, all of them in flight
+  // two short outputs per thread (kEllThreads apart), their bucket found by
+  // the block; every term number loaded coalesced, the two outputs' term
+  // loads interleaved so that twice as many are in flight, each output
+  // summed in its own order
+  static_assert(kEllPerThread == 2, "the loop below takes two outputs per thread");
   const int64_t g = a.ell_block0 + ((int64_t)blockIdx.x - long_blocks);
   int lo = a.b0, hi = a.b1 - 1;
   while (lo < hi) {
@@ -761,13 +764,27 @@ __global__ void __launch_bounds__(kRedThreads) reduce_kernel(ReduceArgs a, int l
     else hi = mid - 1;
   }
   const EllBucket B = a.ell[lo];
-  const int64_t k = (g - B.block0) * kEllThreads + threadIdx.x;
-  if (k >= B.m) return;
-  const uint32_t *ix = a.ell_idx + B.idx0 + k;
-  double s = 0.0;
+  const int64_t k0 = (g - B.block0) * kEllPerBlock + threadIdx.x, k1 = k0 + kEllThreads;
+  if (k0 >= B.m) return;
+  const uint32_t *ix = a.ell_idx + B.idx0;
+  if (k1 < B.m) {
+    double s0 = 0.0, s1 = 0.0;
+#pragma unroll 4
+    for (int j = 0; j < B.c; ++j) {
+      const int64_t row = (int64_t)j * B.m;
+      const double t0 = __ldg(a.terms + __ldg(ix + row + k0));
+      const double t1 = __ldg(a.terms + __ldg(ix + row + k1));
+      s0 += t0;
+      s1 += t1;
+    }
+    a.out[__ldg(a.ell_out + B.out0 + k0)] = s0;
+    a.out[__ldg(a.ell_out + B.out0 + k1)] = s1;
+  } else {
+    double s = 0.0;
 #pragma unroll 8
-  for (int j = 0; j < B.c; ++j) s += __ldg(a.terms + __ldg(ix + (int64_t)j * B.m));
-  a.out[__ldg(a.ell_out + B.out0 + k)] = s;
+    for (int j = 0; j < B.c; ++j) s += __ldg(a.terms + __ldg(ix + (int64_t)j * B.m + k0));
+    a.out[__ldg(a.ell_out + B.out0 + k0)] = s;
+  }
 }
 
 int grid_for(int64_t n, int block) { return (int)((n + block - 1) / block); }

@@ -904,7 +904,7 @@ int build_plan(const xg_netlist *nl, const xg_device_options *opt, Plan *plan, s
         for (int32_t j = 0; j < c; ++j)
           for (int64_t q = k; q < e; ++q)
             P.ell_idx.push_back(P.red_idx[(size_t)(P.red_ptr[(size_t)P.short_order[(size_t)q]] + j)]);
-        blocks += (m + kEllThreads - 1) / kEllThreads;
+        blocks += (m + kEllPerBlock - 1) / kEllPerBlock;
         k = e;
       }
     };

@@ -92,12 +92,15 @@ struct LoadIO {
 // ell_out[out0 .. out0+m) and term j of its k-th output is term
 // ell_idx[idx0 + j*m + k], so a thread per output reads its term numbers
 // coalesced with its neighbours' and has all of them in flight at once.
-// block0: the bucket's first block in a launch over all buckets.
+// block0: the bucket's first block in a launch over all buckets (a block
+// takes kEllPerBlock outputs).
 struct EllBucket {
   int64_t out0, idx0, block0;
   int32_t m, c;
 };
 constexpr int kEllThreads = 256;
+constexpr int kEllPerThread = 2;  // outputs per thread (their loads interleaved)
+constexpr int kEllPerBlock = kEllThreads * kEllPerThread;
 
 // Everything setup derives from a netlist (host side).
 struct Plan {

@@ -256,7 +256,7 @@ class SlotServer:
     them; close() frees them."""
 
     def __init__(self, ctx, shapes, precision=abi.LU_FP64, n_refine=0, slots=512, chunk=32, tstep=1e-12,
-                 max_points=8192, n_out=2, reserve_bytes=4 << 30, memory_cap=None, max_batches_per_class=4,
+                 max_points=8192, n_out=2, reserve_bytes=4 << 30, memory_cap=None, max_batches_per_class=8,
                  depth=1):
         self.ctx, self.shapes = ctx, dict(shapes)
         self.precision, self.n_refine = precision, n_refine
