@@ -195,18 +195,24 @@ def test_grid_refactor_of_a_row_too_long_to_stage(precision, n_refine, gpu_ctx):
 @pytest.mark.parametrize("precision", [abi.LU_FP64, abi.LU_FP32])
 def test_chain_tail_matches_grid_solves(precision, gpu_ctx, oracle_lib, monkeypatch):
     """The trailing rows of one row per level (the 60x60 grid's dense block)
-    are solved in order by one warp; its sums continue the grid solves'
-    own, so the solution is the same bit for bit as with every row solved
-    grid-wide (XG_LU_NO_CHAIN)."""
+    are solved by one warp column by column, their entries brought into
+    shared memory by bulk copies.  The solution agrees with the one where
+    every row is solved grid-wide (XG_LU_NO_CHAIN) to rounding, both meet
+    the backward-error bound, and the chain's sums (each row's in column
+    order) give the same bits on every run."""
     A = circuit_jacobian(CASES["power_grid_60x60"](), seed=5)
     b = np.random.default_rng(15).standard_normal(A.shape[0])
     x, st, info = _solve(gpu_ctx, A, A, b, precision, 0)
+    x_again, st_again, _ = _solve(gpu_ctx, A, A, b, precision, 0)
     monkeypatch.setenv("XG_LU_NO_CHAIN", "1")
     x_grid, st_grid, info_grid = _solve(gpu_ctx, A, A, b, precision, 0)
-    assert st == 0 and st_grid == 0
-    assert info.solve_chain == 256 and info_grid.solve_chain == 0
-    assert np.array_equal(x, x_grid)
-    assert _backward_error(A, x, b) <= (1e-13 if precision == abi.LU_FP64 else 1e-5)
+    assert st == 0 and st_again == 0 and st_grid == 0
+    assert info.solve_chain > 0 and info_grid.solve_chain == 0
+    assert np.array_equal(x, x_again)
+    tol = 1e-10 if precision == abi.LU_FP64 else 1e-3
+    assert np.max(np.abs(x - x_grid)) <= tol * np.max(np.abs(x_grid))
+    bound = 1e-13 if precision == abi.LU_FP64 else 1e-5
+    assert _backward_error(A, x, b) <= bound and _backward_error(A, x_grid, b) <= bound
 
 
 def test_wait_that_runs_out_reports_timeout(gpu_ctx, oracle_lib):

@@ -80,10 +80,15 @@ struct LuDev {
   void *rdiag;                // 1 / U(k,k) per row, written by the refactor
   // grid solves: rows >= tail0 (a chain of one-row levels) are solved by one
   // warp in order (tail0 = n: none); per tail row {start, first entry in a
-  // column >= tail0, diagonal, P}, and its 32 lane sums over columns < tail0
+  // column >= tail0, diagonal, P}, and its sum over columns < tail0
   int tail0;
   const int4 *tdesc;
   void *hpart;
+  // per row: bit 0 its L part, bit 1 its U part, is longer than
+  // kSolveLongRow and no other row of that solve reads its result (a supply
+  // node's KCL row pivoted on its source's current): lu_solve_long sums it
+  // with a block after the grid solve, which skips it
+  const unsigned char *solo;
 };
 
 // The grid-wide kernels carry readiness in the value itself: before a
@@ -192,10 +197,15 @@ __device__ __forceinline__ void publish_release(T *p, T v) {
 
 // Scatter A into the L\U value array (fill entries zero), keep an FP64 copy of
 // A for the residual, reset the claim counter and status, and mark every
-// reciprocal pivot pending.
+// reciprocal pivot pending.  The positions set in `pending` (bit p % 32 of
+// word p / 32: the U part right of the diagonal of every row the refactor
+// stages) are marked pending too: those values carry their own readiness,
+// and the row's warp takes its initial values from A.
 template <class T>
 __global__ void lu_assemble(LuDev d, const double *__restrict__ a, double *__restrict__ a_copy,
-                            int64_t nnz_a, T *__restrict__ val, int64_t nnz_lu) {
+                            int64_t nnz_a, T *__restrict__ val, int64_t nnz_lu,
+                            const unsigned *__restrict__ pending) {
+  using U = typename Pending<T>::U;
   const int64_t stride = int64_t(gridDim.x) * blockDim.x;
   const int64_t t0 = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (t0 == 0) {
@@ -204,12 +214,15 @@ __global__ void lu_assemble(LuDev d, const double *__restrict__ a, double *__res
     d.ctrl[C_BAD_ROW] = 0xffffffffu;
   }
   for (int64_t p = t0; p < nnz_lu; p += stride) {
-    int s = d.lu2a[p];
-    val[p] = s >= 0 ? T(a[s]) : T(0);
+    if ((__ldg(pending + (p >> 5)) >> (p & 31)) & 1u) {
+      reinterpret_cast<U *>(val)[p] = Pending<T>::bits;
+    } else {
+      const int sa = d.lu2a[p];
+      val[p] = sa >= 0 ? T(a[sa]) : T(0);
+    }
   }
   if (a_copy != a)
     for (int64_t p = t0; p < nnz_a; p += stride) a_copy[p] = a[p];
-  using U = typename Pending<T>::U;
   for (int64_t i = t0; i < d.n; i += stride) reinterpret_cast<U *>(d.rdiag)[i] = Pending<T>::bits;
 }
 
@@ -223,67 +236,194 @@ constexpr int kMinStageBytes = 4 * 1024;
 constexpr int kUnstagedRows = 32;
 constexpr int kFactorWarps = 8;
 
-// row -= l * (U row of the pivot): the pivot row's values and target
-// positions of a chunk of 8 per lane are loaded before any of them is
-// applied, so a long U row costs one L2 round trip per 256 entries (the
-// target row and the pivot row are different rows: nothing aliases).
-template <class T>
-__device__ __forceinline__ void row_update(T *rb, int ro, const int *__restrict__ up,
-                                           const T *__restrict__ u, int len, T l, int lane) {
-  constexpr int kU = 8;
-  int j0 = 0;
-  for (; j0 + 32 * kU <= len; j0 += 32 * kU) {
-    T v[kU];
-    int q[kU];
-#pragma unroll
-    for (int r = 0; r < kU; ++r) {
-      v[r] = __ldcg(u + j0 + 32 * r + lane);
-      q[r] = __ldg(up + j0 + 32 * r + lane);
-    }
-#pragma unroll
-    for (int r = 0; r < kU; ++r) rb[q[r] - ro] -= l * v[r];
+constexpr int kU = 4;  // pivot-row entries per lane in one chunk (128 a chunk)
+
+// Readiness in the refactor.  The U part right of the diagonal of a staged
+// row, and every reciprocal pivot, start pending and are each written once,
+// final, with a relaxed store: a row that needs them polls the values
+// themselves, so it has them one L2 round trip after they land and the
+// writer needs no fence.  A row eliminated in place (longer than the stage)
+// has A in its U part from the start: it stores its pivot with release after
+// its U part, and a row that needs it polls the pivot with acquire before it
+// loads the values.
+
+// One L entry of the row being eliminated: its pivot row k, where k's U part
+// right of the diagonal starts and how long it is, and whether those values
+// carry their own readiness (k was staged).
+struct PivotMeta {
+  int k, q0, len, flagged;
+};
+
+__device__ __forceinline__ PivotMeta pivot_meta(const LuDev &d, int p, int dp, int cap) {
+  PivotMeta m{0, 0, 0, 1};
+  if (p < dp) {
+    m.k = __ldg(d.ci + p);
+    const int rs = __ldg(d.rp + m.k), dk = __ldg(d.diag + m.k), re = __ldg(d.rp + m.k + 1);
+    m.q0 = dk + 1;
+    m.len = re - m.q0;
+    m.flagged = re - rs <= cap;
   }
-  if (j0 < len) {
-    // the last chunk: steps past the row's end are skipped by the whole warp
-    // (an FP64 instruction costs its issue slot however few lanes it has)
-    T v[kU];
-    int q[kU];
+  return m;
+}
+
+__device__ __forceinline__ PivotMeta shfl_meta(const PivotMeta &m, int src) {
+  PivotMeta o;
+  o.k = __shfl_sync(0xffffffffu, m.k, src);
+  o.q0 = __shfl_sync(0xffffffffu, m.q0, src);
+  o.len = __shfl_sync(0xffffffffu, m.len, src);
+  o.flagged = __shfl_sync(0xffffffffu, m.flagged, src);
+  return o;
+}
+
+// A chunk of a pivot row's U part: the positions in the row being eliminated
+// that its entries update (-1: none) and, for a flagged row, the values as
+// polled so far; lane 0 also holds the reciprocal pivot.
+template <class T>
+struct PivotChunk {
+  int q[kU];
+  typename Pending<T>::U v[kU];
+  typename Pending<T>::U r;
+};
+
+// Loads (without waiting) the chunk of row m from entry j0 on; the pivot too
+// when j0 is 0.  `up` points at the row's update positions.
+template <class T>
+__device__ __forceinline__ void pivot_fetch(const LuDev &d, const T *val, const PivotMeta &m,
+                                            const int *up, int j0, int lane, PivotChunk<T> &c) {
+  using U = typename Pending<T>::U;
+  const U *vb = reinterpret_cast<const U *>(val) + m.q0;
 #pragma unroll
-    for (int r = 0; r < kU; ++r) {
-      const int j = j0 + 32 * r + lane;
-      v[r] = j < len ? __ldcg(u + j) : T(0);
-      q[r] = j < len ? __ldg(up + j) : -1;
-    }
+  for (int r = 0; r < kU; ++r) {
+    const int j = j0 + 32 * r + lane;
+    c.q[r] = j < m.len ? __ldg(up + j) : -1;
+    c.v[r] = m.flagged && j < m.len ? ld_relaxed(vb + j) : U(0);
+  }
+  c.r = m.flagged && j0 == 0 && lane == 0 ? ld_relaxed(reinterpret_cast<const U *>(d.rdiag) + m.k) : U(0);
+}
+
+// Polls a flagged chunk until none of its values (nor, with the pivot, lane
+// 0's pivot) is pending; any that never arrive read as zero and set the
+// timeout bit.  Every pending value is polled each time: they tend to land
+// together, and one round trip then brings them all.
+template <class T>
+__device__ __forceinline__ void pivot_wait(const LuDev &d, const T *val, const PivotMeta &m, int j0,
+                                           bool pivot, int lane, PivotChunk<T> &c) {
+  using U = typename Pending<T>::U;
+  const U *vb = reinterpret_cast<const U *>(val) + m.q0 + j0 + lane;
+  const U *rp = reinterpret_cast<const U *>(d.rdiag) + m.k;
+  const bool wp = pivot && lane == 0;
+  const int limit = int(__ldg(&d.ctrl[C_SPIN]));
+  for (int it = 1;; ++it) {
+    bool pend = wp && c.r == Pending<T>::bits;
 #pragma unroll
-    for (int r = 0; r < kU; ++r) {
-      if (j0 + 32 * r >= len) break;
-      if (q[r] >= 0) rb[q[r] - ro] -= l * v[r];
+    for (int r = 0; r < kU; ++r) pend |= c.q[r] >= 0 && c.v[r] == Pending<T>::bits;
+    if (!pend) break;
+    if (it > limit ||
+        ((it & 1023) == 0 && (*(volatile unsigned *)&d.ctrl[C_STATUS] & ST_TIMEOUT))) {
+      atomicOr(&d.ctrl[C_STATUS], ST_TIMEOUT);
+      if (wp && c.r == Pending<T>::bits) c.r = U(0);
+#pragma unroll
+      for (int r = 0; r < kU; ++r)
+        if (c.v[r] == Pending<T>::bits) c.v[r] = U(0);
+      break;
     }
+    if (it > 32) __nanosleep(64);
+    if (wp && c.r == Pending<T>::bits) c.r = ld_relaxed(rp);
+#pragma unroll
+    for (int r = 0; r < kU; ++r)
+      if (c.q[r] >= 0 && c.v[r] == Pending<T>::bits) c.v[r] = ld_relaxed(vb + 32 * r);
   }
 }
 
-// Eliminate row `row` in rb (row entry p at rb[p - ro]).
+// row -= l * (U part of pivot row m), l = row[p] / U(k, k) stored at p; the
+// first chunk comes from c (fetched an entry ahead), later ones (pivot rows
+// with more than 256 entries right of the diagonal) are loaded here.  The
+// target row and the pivot row are different rows: nothing aliases.
+template <class T>
+__device__ __forceinline__ void pivot_apply(const LuDev &d, const T *val, T *rb, int ro, int p,
+                                            const PivotMeta &m, const int *up, int lane,
+                                            PivotChunk<T> &c) {
+  using U = typename Pending<T>::U;
+  T rk = T(0);
+  if (m.flagged) {
+    pivot_wait(d, val, m, 0, true, lane, c);
+    rk = from_bits(c.r);
+  } else if (lane == 0) {
+    rk = wait_value_acquire((const T *)d.rdiag + m.k, d.ctrl);
+  }
+  rk = __shfl_sync(0xffffffffu, rk, 0);
+  if (!m.flagged) {
+    // values of a row eliminated in place: after its pivot's acquire
+#pragma unroll
+    for (int r = 0; r < kU; ++r) {
+      const int j = 32 * r + lane;
+      c.v[r] = j < m.len ? to_bits(__ldcg(val + m.q0 + j)) : U(0);
+    }
+  }
+  const T l = rb[p - ro] * rk;
+  __syncwarp();
+  if (lane == 0) rb[p - ro] = l;
+#pragma unroll
+  for (int r = 0; r < kU; ++r)
+    if (c.q[r] >= 0) rb[c.q[r] - ro] -= l * from_bits(c.v[r]);
+  for (int j0 = 32 * kU; j0 < m.len; j0 += 32 * kU) {
+    PivotChunk<T> e;
+    pivot_fetch(d, val, m, up, j0, lane, e);
+    if (m.flagged) {
+      pivot_wait(d, val, m, j0, false, lane, e);
+    } else {
+#pragma unroll
+      for (int r = 0; r < kU; ++r) {
+        const int j = j0 + 32 * r + lane;
+        e.v[r] = j < m.len ? to_bits(__ldcg(val + m.q0 + j)) : U(0);
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < kU; ++r)
+      if (e.q[r] >= 0) rb[e.q[r] - ro] -= l * from_bits(e.v[r]);
+  }
+}
+
+// Eliminate row `row` in rb (row entry p at rb[p - ro]).  The metadata of the
+// row's L entries is loaded 32 at a time, one entry per lane, the next 32 in
+// flight behind them; the next entry's first chunk is in flight while the
+// current entry is applied.
 template <class T>
 __device__ __forceinline__ void eliminate(const LuDev &d, const T *val, T *rb, int ro, int s,
-                                          int dp, const int *up, int lane) {
-  const T *rdiag = (const T *)d.rdiag;
-  for (int p = s; p < dp; ++p) {
-    const int k = __ldg(d.ci + p);
-    const int q0 = __ldg(d.diag + k) + 1, len = __ldg(d.rp + k + 1) - q0;
-    T rk = T(0);
-    if (lane == 0) rk = wait_value_acquire(rdiag + k, d.ctrl);
-    rk = __shfl_sync(0xffffffffu, rk, 0);
-    const T l = rb[p - ro] * rk;
+                                          int dp, const int *up, int cap, int lane) {
+  const int nl = dp - s;
+  if (nl <= 0) return;
+  PivotMeta mc = pivot_meta(d, s + lane, dp, cap);
+  PivotMeta mn = pivot_meta(d, s + 32 + lane, dp, cap);
+  PivotMeta cur = shfl_meta(mc, 0);
+  PivotChunk<T> cc, cn;
+  pivot_fetch(d, val, cur, up, 0, lane, cc);
+  for (int j = 0; j < nl; ++j) {
+    const int *ucur = up;
+    up += cur.len;
+    PivotMeta nxt = cur;
+    const bool more = j + 1 < nl;
+    if (more) {
+      const int jn = j + 1;
+      if ((jn & 31) == 0) {
+        mc = mn;
+        mn = pivot_meta(d, s + jn + 32 + lane, dp, cap);
+      }
+      nxt = shfl_meta(mc, jn & 31);
+      pivot_fetch(d, val, nxt, up, 0, lane, cn);
+    }
+    pivot_apply(d, val, rb, ro, s + j, cur, ucur, lane, cc);
     __syncwarp();
-    if (lane == 0) rb[p - ro] = l;
-    row_update(rb, ro, up, val + q0, len, l, lane);
-    up += len;
-    __syncwarp();
+    if (more) {
+      cur = nxt;
+      cc = cn;
+    }
   }
 }
 
 template <class T>
-__global__ void __launch_bounds__(32 * kFactorWarps) lu_factor(LuDev d, T *val, int cap) {
+__global__ void __launch_bounds__(32 * kFactorWarps) lu_factor(LuDev d, T *val, const double *__restrict__ a,
+                                                               int cap) {
   extern __shared__ __align__(16) unsigned char stage_raw[];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   T *stage = reinterpret_cast<T *>(stage_raw) + size_t(wid) * cap;
@@ -295,16 +435,32 @@ __global__ void __launch_bounds__(32 * kFactorWarps) lu_factor(LuDev d, T *val, 
     if (row >= d.n) break;
     const int s = __ldg(d.rp + row), dp = __ldg(d.diag + row), e = __ldg(d.rp + row + 1);
     const int *up = d.upos + __ldg(d.urp + row);
+    const bool staged = e - s <= cap;
     T u;
-    if (e - s <= cap) {
-      for (int p = s + lane; p < e; p += 32) stage[p - s] = val[p];
+    if (staged) {
+      // the U part right of the diagonal is pending in val: its values come from A
+      for (int p = s + lane; p < e; p += 32) {
+        T v;
+        if (p > dp) {
+          const int sa = __ldg(d.lu2a + p);
+          v = sa >= 0 ? T(a[sa]) : T(0);
+        } else {
+          v = val[p];
+        }
+        stage[p - s] = v;
+      }
       __syncwarp();
-      eliminate(d, val, stage, s, s, dp, up, lane);
-      for (int p = s + lane; p < e; p += 32) val[p] = stage[p - s];
+      eliminate(d, val, stage, s, s, dp, up, cap, lane);
+      for (int p = s + lane; p < e; p += 32) {
+        if (p > dp)
+          publish(val + p, stage[p - s]);
+        else
+          val[p] = stage[p - s];
+      }
       __syncwarp();
       u = stage[dp - s];
     } else {
-      eliminate(d, val, val, 0, s, dp, up, lane);
+      eliminate(d, val, val, 0, s, dp, up, cap, lane);
       u = val[dp];
     }
     if (lane == 0) {
@@ -312,8 +468,12 @@ __global__ void __launch_bounds__(32 * kFactorWarps) lu_factor(LuDev d, T *val, 
         atomicOr(&d.ctrl[C_STATUS], ST_PIVOT);
         atomicMin(&d.ctrl[C_BAD_ROW], unsigned(row));
       }
-      __threadfence();
-      publish_release(rdiag + row, T(1) / u);
+      if (staged) {
+        publish(rdiag + row, T(1) / u);
+      } else {
+        __threadfence();
+        publish_release(rdiag + row, T(1) / u);
+      }
     }
   }
 }
@@ -331,6 +491,76 @@ __global__ void lu_solve_open(LuDev d, T *y, T *z) {
     reinterpret_cast<U *>(y)[i] = Pending<T>::bits;
     reinterpret_cast<U *>(z)[i] = Pending<T>::bits;
   }
+}
+
+// The grid solves hold this many entries per lane of a row (128 a row) and
+// wait for their inputs together: the loads of a row's entries, and the
+// polls of the values they multiply, are all in flight at once, so a row
+// costs about two L2 round trips after its last input lands, not two per
+// 32 entries.
+constexpr int kSolveHeld = 4;
+
+// Waits for x[k[r]] (k[r] < 0: none, reads as zero) with every poll in
+// flight together, polling again only those still pending; zero for any
+// that never arrive (and the timeout bit).
+template <class T, int K>
+__device__ __forceinline__ void wait_values(const T *x, const int (&k)[K], T (&v)[K], unsigned *ctrl) {
+  using U = typename Pending<T>::U;
+  const U *q = reinterpret_cast<const U *>(x);
+  U b[K];
+#pragma unroll
+  for (int r = 0; r < K; ++r) b[r] = k[r] >= 0 ? ld_relaxed(q + k[r]) : U(0);
+  const int limit = int(__ldg(&ctrl[C_SPIN]));
+  for (int it = 1;; ++it) {
+    bool pend = false;
+#pragma unroll
+    for (int r = 0; r < K; ++r) pend |= b[r] == Pending<T>::bits;
+    if (!pend) break;
+    if (it > limit || ((it & 1023) == 0 && (*(volatile unsigned *)&ctrl[C_STATUS] & ST_TIMEOUT))) {
+      atomicOr(&ctrl[C_STATUS], ST_TIMEOUT);
+#pragma unroll
+      for (int r = 0; r < K; ++r)
+        if (b[r] == Pending<T>::bits) b[r] = U(0);
+      break;
+    }
+    if (it > 32) __nanosleep(64);
+#pragma unroll
+    for (int r = 0; r < K; ++r)
+      if (b[r] == Pending<T>::bits) b[r] = ld_relaxed(q + k[r]);
+  }
+#pragma unroll
+  for (int r = 0; r < K; ++r) v[r] = from_bits(b[r]);
+}
+
+// Rows with more entries than this in a solve's part, that no other row of
+// that solve waits for, are summed by a block of their own after it.
+constexpr int kSolveLongRow = 4096;
+constexpr int kLongThreads = 1024;
+
+// A lane's share of sum over p in [p0, p1) of val[p] * x[ci[p]]: entries
+// p0 + lane, p0 + lane + 32, ... in ascending order, kSolveHeld of them
+// loaded and waited for at a time.  Lanes go at their own pace (no vote per
+// step): a lane whose inputs have landed runs ahead to its next entries
+// while others still wait.
+template <class T>
+__device__ __forceinline__ T lane_dot(const LuDev &d, const T *__restrict__ val, const T *x, int p0,
+                                      int p1, int lane) {
+  T acc = T(0);
+  for (int p = p0 + lane; p < p1; p += 32 * kSolveHeld) {
+    int k[kSolveHeld];
+    T a[kSolveHeld], xv[kSolveHeld];
+#pragma unroll
+    for (int r = 0; r < kSolveHeld; ++r) {
+      const int q = p + 32 * r;
+      k[r] = q < p1 ? __ldg(d.ci + q) : -1;
+      a[r] = q < p1 ? __ldcg(val + q) : T(0);
+    }
+    wait_values(x, k, xv, d.ctrl);
+#pragma unroll
+    for (int r = 0; r < kSolveHeld; ++r)
+      if (k[r] >= 0) acc += a[r] * xv[r];
+  }
+  return acc;
 }
 
 template <class T>
@@ -352,26 +582,16 @@ __global__ void __launch_bounds__(256) lu_lsolve(LuDev d, const T *__restrict__ 
     if (row >= d.n) break;
     const int s = __ldg(d.rp + row), dp = __ldg(d.diag + row);
     if (row >= d.tail0) {
-      // a row of the chain: each lane's sum over its entries in columns below
-      // tail0 (columns ascend); the chain kernel continues it
+      // a row of the chain: its sum over the entries in columns below tail0;
+      // the chain kernel starts from it
       const int sp = d.tdesc[row - d.tail0].y;
-      T acc = T(0);
-      for (int p = s + lane; p < sp; p += 32) {
-        const int k = __ldg(d.ci + p);
-        const T lv = __ldcg(val + p);
-        acc += lv * wait_value(y + k, d.ctrl);
-      }
-      reinterpret_cast<T *>(d.hpart)[size_t(row - d.tail0) * 32 + lane] = acc;
+      const T acc = warp_sum(lane_dot(d, val, y, s, sp, lane));
+      if (lane == 0) reinterpret_cast<T *>(d.hpart)[row - d.tail0] = acc;
       continue;
     }
+    if (dp - s > kSolveLongRow && (__ldg(d.solo + row) & 1)) continue;  // lu_solve_long's
     const T bi = lane == 0 ? T(b[__ldg(d.P + row)]) : T(0);  // before any wait
-    T acc = T(0);
-    for (int p = s + lane; p < dp; p += 32) {
-      const int k = __ldg(d.ci + p);
-      const T lv = __ldcg(val + p);
-      acc += lv * wait_value(y + k, d.ctrl);
-    }
-    acc = warp_sum(acc);
+    const T acc = warp_sum(lane_dot(d, val, y, s, dp, lane));
     if (lane == 0) publish(y + row, bi - acc);
   }
 }
@@ -388,16 +608,11 @@ __global__ void __launch_bounds__(256) lu_usolve(LuDev d, const T *__restrict__ 
     if (c >= d.tail0) break;
     const int row = d.tail0 - 1 - c;  // rows from tail0 on are solved already
     const int dp = __ldg(d.diag + row), e = __ldg(d.rp + row + 1);
+    if (e - dp - 1 > kSolveLongRow && (__ldg(d.solo + row) & 2)) continue;  // lu_solve_long's
     const T yi = lane == 0 ? __ldcg(y + row) : T(0);
     const T ri = lane == 0 ? __ldcg((const T *)d.rdiag + row) : T(0);
     const int qi = lane == 0 ? __ldg(d.Q + row) : 0;
-    T acc = T(0);
-    for (int p = dp + 1 + lane; p < e; p += 32) {
-      const int k = __ldg(d.ci + p);
-      const T uv = __ldcg(val + p);
-      acc += uv * wait_value(z + k, d.ctrl);
-    }
-    acc = warp_sum(acc);
+    const T acc = warp_sum(lane_dot(d, val, z, dp + 1, e, lane));
     if (lane == 0) {
       const T zi = (yi - acc) * ri;
       publish(z + row, zi);
@@ -406,130 +621,252 @@ __global__ void __launch_bounds__(256) lu_usolve(LuDev d, const T *__restrict__ 
   }
 }
 
-// The chain at the end of a factor whose last rows each form their own
-// level (a supply node and what hangs on it): grid-wide, every row would
-// cost an L2 round trip for its one dependency; here one warp takes the rows
-// in order, keeps y and z of the chain in shared memory and loads the
-// entries of the next rows while it sums the current one.  Its sums are the
-// grid solves' own (lane-strided in column order, continued from the grid's
-// per-lane sums over earlier columns, then the butterfly), so the results
-// are the same bit for bit.  No waits: every input is final when it is read.
-constexpr int kChainR = 4;  // entries per lane held for a row (128 per row)
-
+// The rows the grid solves skip (solo): a block per row, every input final
+// (the grid solve before it has ended).  Each thread sums its entries
+// p0 + t, p0 + t + kLongThreads, ... in order, then a fixed tree: the same
+// result on every run.  upper = 0: y(row) = b(P(row)) - L(row,:) y;
+// upper = 1: z(row) = (y(row) - U(row,:) z) / U(row,row), x(Q(row)) = z(row).
 template <class T>
-struct ChainRow {
-  int dp, p;        // the row's end and this lane's next entry
-  int k[kChainR];   // columns (-1: none)
-  T a[kChainR];     // values
-  T base;           // lower solve: the grid's lane sum; upper: 0
-  T head;           // lane 0: b(P(row)) or y(row); others 0
-  T rd;             // upper solve: 1 / U(row, row)
-};
-
-// row -> ChainRow: lower (mode 0) entries from the split point up to the
-// diagonal, upper (mode 1) entries after the diagonal
-template <class T>
-__device__ __forceinline__ void chain_fetch(const LuDev &d, const T *__restrict__ val,
-                                            const double *__restrict__ b, const T *ys, int row,
-                                            int mode, int lane, ChainRow<T> &q) {
-  const int4 ds = d.tdesc[row - d.tail0];  // {s, sp, dp, P}
-  int p;
-  if (mode == 0) {
-    p = ds.x + lane;
-    if (p < ds.y) p += (ds.y - p + 31) / 32 * 32;
-    q.dp = ds.z;
-    q.base = __ldcg(reinterpret_cast<const T *>(d.hpart) + size_t(row - d.tail0) * 32 + lane);
-    q.head = lane == 0 ? T(b[ds.w]) : T(0);
-    q.rd = T(0);
-  } else {
-    p = ds.z + 1 + lane;
-    q.dp = __ldg(d.rp + row + 1);
-    q.base = T(0);
-    q.head = lane == 0 ? ys[row - d.tail0] : T(0);
-    q.rd = lane == 0 ? __ldcg((const T *)d.rdiag + row) : T(0);
-  }
-#pragma unroll
-  for (int r = 0; r < kChainR; ++r) {
-    const int pp = p + 32 * r;
-    q.k[r] = pp < q.dp ? __ldg(d.ci + pp) : -1;
-    q.a[r] = pp < q.dp ? __ldcg(val + pp) : T(0);
-  }
-  q.p = p + 32 * kChainR;
-}
-
-// the row's sum: the held entries, then any beyond them (rows longer than
-// 128 entries past the split, loaded 128 at a time), in the same lane order;
-// a step no lane has is skipped by the warp (an FP64 instruction costs its
-// issue slot however few lanes it has)
-template <class T>
-__device__ __forceinline__ T chain_sum(const LuDev &d, const T *__restrict__ val,
-                                       const ChainRow<T> &q, const T *v) {
-  T acc = q.base;
-#pragma unroll
-  for (int r = 0; r < kChainR; ++r) {
-    if (!__any_sync(0xffffffffu, q.k[r] >= 0)) break;
-    if (q.k[r] >= 0) acc += q.a[r] * v[q.k[r] - d.tail0];
-  }
-  for (int p = q.p; __any_sync(0xffffffffu, p < q.dp); p += 32 * kChainR) {
-    int k[kChainR];
-    T a[kChainR];
-#pragma unroll
-    for (int r = 0; r < kChainR; ++r) {
-      const int pp = p + 32 * r;
-      k[r] = pp < q.dp ? __ldg(d.ci + pp) : -1;
-      a[r] = pp < q.dp ? __ldcg(val + pp) : T(0);
-    }
-#pragma unroll
-    for (int r = 0; r < kChainR; ++r)
-      if (k[r] >= 0) acc += a[r] * v[k[r] - d.tail0];
-  }
-  return warp_sum(acc);
-}
-
-template <class T>
-__global__ void __launch_bounds__(32) lu_solve_chain(LuDev d, const T *__restrict__ val,
-                                                     const double *__restrict__ b, T *y, T *z,
-                                                     double *x) {
-  extern __shared__ __align__(16) unsigned char chain_raw[];
-  const int lane = threadIdx.x, t0 = d.tail0, nt = d.n - t0;
-  T *ys = reinterpret_cast<T *>(chain_raw);
-  T *zs = ys + nt;
-  // y = L \ b(P) on the chain, rows ascending, the next two rows in flight
-  {
-    ChainRow<T> q0, q1, q2;
-    chain_fetch(d, val, b, ys, t0, 0, lane, q0);
-    if (t0 + 1 < d.n) chain_fetch(d, val, b, ys, t0 + 1, 0, lane, q1);
-    for (int row = t0; row < d.n; ++row) {
-      if (row + 2 < d.n) chain_fetch(d, val, b, ys, row + 2, 0, lane, q2);
-      const T acc = chain_sum(d, val, q0, ys);
-      if (lane == 0) {
-        const T v = q0.head - acc;
-        ys[row - t0] = v;
-        y[row] = v;
-      }
-      __syncwarp();
-      q0 = q1;
-      q1 = q2;
-    }
-  }
-  // z = U \ y, x(Q) = z on the chain, rows descending
-  {
-    ChainRow<T> q0, q1, q2;
-    chain_fetch(d, val, b, ys, d.n - 1, 1, lane, q0);
-    if (d.n - 2 >= t0) chain_fetch(d, val, b, ys, d.n - 2, 1, lane, q1);
-    for (int row = d.n - 1; row >= t0; --row) {
-      if (row - 2 >= t0) chain_fetch(d, val, b, ys, row - 2, 1, lane, q2);
-      const T acc = chain_sum(d, val, q0, zs);
-      if (lane == 0) {
-        const T zi = (q0.head - acc) * q0.rd;
-        zs[row - t0] = zi;
+__global__ void __launch_bounds__(kLongThreads) lu_solve_long(LuDev d, const T *__restrict__ val,
+                                                              const double *__restrict__ b, T *y, T *z,
+                                                              double *x, const int *__restrict__ rows,
+                                                              int upper) {
+  __shared__ T part[kLongThreads / 32];
+  const int row = rows[blockIdx.x];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const int dp = __ldg(d.diag + row);
+  const int p0 = upper ? dp + 1 : __ldg(d.rp + row);
+  const int p1 = upper ? __ldg(d.rp + row + 1) : dp;
+  const T *x_in = upper ? z : y;
+  T acc = T(0);
+  for (int p = p0 + t; p < p1; p += kLongThreads) acc += __ldcg(val + p) * __ldcg(x_in + __ldg(d.ci + p));
+  acc = warp_sum(acc);
+  if (lane == 0) part[w] = acc;
+  __syncthreads();
+  if (w == 0) {
+    acc = lane < kLongThreads / 32 ? part[lane] : T(0);
+    acc = warp_sum(acc);
+    if (lane == 0) {
+      if (upper) {
+        const T zi = (__ldcg(y + row) - acc) * __ldcg((const T *)d.rdiag + row);
         z[row] = zi;
         x[__ldg(d.Q + row)] = double(zi);
+      } else {
+        y[row] = T(b[__ldg(d.P + row)]) - acc;
       }
-      __syncwarp();
-      q0 = q1;
-      q1 = q2;
     }
+  }
+}
+
+// The chain at the end of a factor whose last rows each form their own
+// level (a supply node and what hangs on it, or the dense block the order
+// leaves last): grid-wide, every row would cost an L2 round trip for its
+// dependencies.  Here one warp solves the chain column by column
+// ("right-looking"): its rows' running sums live in shared memory; once a
+// column's value is final (y(c), then z(c)), the warp subtracts it times the
+// column's entries from the sums of the rows they are in.  A row's sum takes
+// its entries in column order, the same on every run.  The entries come in
+// column-ordered segments (rows, values; at most kChainSeg, padded to a
+// multiple of 4 with a scratch row), copied global -> shared by the bulk
+// copy engine (cp.async.bulk, completion counted on an mbarrier) kChainRing
+// segments ahead of their use, so the warp never waits on a load.
+constexpr int kChainSeg = 128;
+constexpr int kChainRing = 16;
+
+// A segment: its column (chain-local), where its entries start (a multiple
+// of 4), how many (a multiple of 4, <= kChainSeg), and flags: 1 its column's
+// first segment, 2 the upper solve.
+struct ChainSegDesc {
+  int col, off, len, flags;
+};
+
+// chain_val[j] = val[chain_pos[j]] (0 for padding): the chain's entries in
+// segment order, gathered once per refactor.
+template <class T>
+__global__ void lu_chain_gather(const T *__restrict__ val, const int *__restrict__ pos, T *__restrict__ out,
+                                int64_t n) {
+  for (int64_t j = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < n; j += int64_t(gridDim.x) * blockDim.x) {
+    const int p = __ldg(pos + j);
+    out[j] = p >= 0 ? __ldcg(val + p) : T(0);
+  }
+}
+
+struct ChainDev {
+  const int4 *seg;   // ChainSegDesc, the lower solve's then the upper's
+  int n_seg;
+  const int *row;    // chain-local row of each entry (nt: scratch)
+  const void *val;   // T: each entry's value (lu_chain_gather)
+};
+
+__device__ __forceinline__ unsigned smem_addr(const void *p) {
+  return unsigned(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ bool mbar_try(unsigned bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Polls the barrier's phase `parity` to completion, at most `limit` times.
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity, int limit) {
+  for (int it = 0; it < limit; ++it)
+    if (mbar_try(bar, parity)) return true;
+  return false;
+}
+
+template <class T>
+__global__ void __launch_bounds__(32) lu_solve_chain(LuDev d, ChainDev c, const double *__restrict__ b, T *y,
+                                                     T *z, double *x) {
+  extern __shared__ __align__(128) unsigned char chain_raw[];
+  const int lane = threadIdx.x, t0 = d.tail0, nt = d.n - t0;
+  // ring: per slot the rows and values of one segment, its descriptor,
+  // reciprocal pivot and x position, and its barrier; then the running sums
+  // (nt + scratch)
+  int *ring_row = reinterpret_cast<int *>(chain_raw);
+  T *ring_val = reinterpret_cast<T *>(ring_row + kChainRing * kChainSeg);
+  int4 *ring_desc = reinterpret_cast<int4 *>(ring_val + kChainRing * kChainSeg);
+  int *ring_q = reinterpret_cast<int *>(ring_desc + kChainRing);
+  T *ring_rd = reinterpret_cast<T *>(ring_q + kChainRing);
+  unsigned long long *bar = reinterpret_cast<unsigned long long *>(
+      reinterpret_cast<uintptr_t>(ring_rd + kChainRing + 1) / 8 * 8 + 8);
+  T *acc = reinterpret_cast<T *>(bar + kChainRing);
+  const T *rdiag = (const T *)d.rdiag;
+  const T *cval = (const T *)c.val;
+  const int limit = int(__ldg(&d.ctrl[C_SPIN]));
+
+  if (lane == 0) {
+    for (int i = 0; i < kChainRing; ++i)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar + i)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  for (int r = lane; r < nt; r += 32)
+    acc[r] = T(b[d.tdesc[r].w]) - __ldcg(reinterpret_cast<const T *>(d.hpart) + r);
+  if (lane == 0) acc[nt] = T(0);
+  __syncwarp();
+
+  // segment descriptors: lane j holds those of segments w + j (the issue
+  // window) and w + 32 + j (the next), loaded a window ahead, with the
+  // reciprocal pivot and x position an upper segment's column needs
+  auto load_desc = [&](int g, int4 &ds, T &rd, int &qx) {
+    ds = make_int4(0, 0, 0, 0);
+    rd = T(0);
+    qx = 0;
+    if (g < c.n_seg) {
+      ds = c.seg[g];
+      if (ds.w & 2) {
+        rd = __ldcg(rdiag + t0 + ds.x);
+        qx = __ldg(d.Q + t0 + ds.x);
+      }
+    }
+  };
+  int w = 0;
+  int4 da, db;
+  T ra, rb;
+  int qa, qb;
+  load_desc(lane, da, ra, qa);
+  load_desc(32 + lane, db, rb, qb);
+  // lane 0 starts the copy of segment g into slot g % kChainRing
+  auto issue = [&](int g) {
+    if (g - w == 32) {
+      w += 32;
+      da = db;
+      ra = rb;
+      qa = qb;
+      load_desc(w + 32 + lane, db, rb, qb);
+    }
+    int4 ds;
+    ds.x = __shfl_sync(0xffffffffu, da.x, g - w);
+    ds.y = __shfl_sync(0xffffffffu, da.y, g - w);
+    ds.z = __shfl_sync(0xffffffffu, da.z, g - w);
+    ds.w = __shfl_sync(0xffffffffu, da.w, g - w);
+    const T rd = __shfl_sync(0xffffffffu, ra, g - w);
+    const int qx = __shfl_sync(0xffffffffu, qa, g - w);
+    if (lane == 0) {
+      const int slot = g % kChainRing;
+      ring_desc[slot] = ds;
+      ring_rd[slot] = rd;
+      ring_q[slot] = qx;
+      const unsigned mb = smem_addr(bar + slot);
+      const unsigned bytes = unsigned(ds.z) * unsigned(sizeof(int) + sizeof(T));
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(bytes) : "memory");
+      if (ds.z > 0) {
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                smem_addr(ring_row + slot * kChainSeg)),
+            "l"(c.row + ds.y), "r"(unsigned(ds.z) * unsigned(sizeof(int))), "r"(mb)
+            : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                smem_addr(ring_val + slot * kChainSeg)),
+            "l"(cval + ds.y), "r"(unsigned(ds.z) * unsigned(sizeof(T))), "r"(mb)
+            : "memory");
+      }
+    }
+  };
+  // kChainRing - 1 segments in flight: segment g + kChainRing - 1 goes into
+  // the slot segment g - 1 has just left, before segment g is waited for
+  constexpr int kAhead = kChainRing - 1;
+  const int pre = min(kAhead, c.n_seg);
+  for (int g = 0; g < pre; ++g) issue(g);
+
+  T v = T(0);
+  int g = 0;
+  bool ok = true;
+  for (; g < c.n_seg; ++g) {
+    if (g + kAhead < c.n_seg) issue(g + kAhead);
+    const int slot = g % kChainRing;
+    if (!mbar_wait(smem_addr(bar + slot), unsigned(g / kChainRing) & 1u, limit)) {
+      ok = false;
+      break;
+    }
+    const int4 ds = ring_desc[slot];
+    const int *sr = ring_row + slot * kChainSeg;
+    const T *sv = ring_val + slot * kChainSeg;
+    // the segment's rows and values, loaded before the column's value is
+    // needed; its rows are distinct (scratch padding aside), so every sum is
+    // read before any is written
+    int ri[kChainSeg / 32];
+    T wv[kChainSeg / 32];
+#pragma unroll
+    for (int r = 0; r < kChainSeg / 32; ++r) {
+      const int j = 32 * r + lane;
+      ri[r] = j < ds.z ? sr[j] : nt;
+      wv[r] = j < ds.z ? sv[j] : T(0);
+    }
+    if (ds.w & 1) {
+      // the column's value is final: every earlier column has been applied
+      v = acc[ds.x];
+      if (ds.w & 2) v *= ring_rd[slot];
+      if (lane == 0) {
+        if (ds.w & 2) {
+          z[t0 + ds.x] = v;
+          x[ring_q[slot]] = double(v);
+        } else {
+          y[t0 + ds.x] = v;
+        }
+      }
+    }
+    T av[kChainSeg / 32];
+#pragma unroll
+    for (int r = 0; r < kChainSeg / 32; ++r) av[r] = acc[ri[r]];
+#pragma unroll
+    for (int r = 0; r < kChainSeg / 32; ++r) av[r] -= wv[r] * v;
+#pragma unroll
+    for (int r = 0; r < kChainSeg / 32; ++r)
+      if (32 * r + lane < ds.z) acc[ri[r]] = av[r];
+    __syncwarp();
+  }
+  if (!ok) {
+    // a copy that did not complete in time: report it, and let the copies
+    // still in flight land before the block's shared memory is released
+    if (lane == 0) atomicOr(&d.ctrl[C_STATUS], ST_TIMEOUT);
+    const int end = min(c.n_seg, g + kAhead + 1);
+    for (int h = g; h < end; ++h)
+      mbar_wait(smem_addr(bar + h % kChainRing), unsigned(h / kChainRing) & 1u, 1 << 22);
   }
 }
 
@@ -1225,57 +1562,54 @@ __global__ void __launch_bounds__(1024) lu_factor_solve_lvl(LuDev d, LvlDev v,
   lvl_solve<T>(d, v, m, x);
 }
 
+// Shared memory of lu_solve_chain: the segment ring (rows, values,
+// descriptors, reciprocal pivots, barriers) and the running sums of nt rows
+// plus the scratch row, with slack for the barriers' alignment.
+size_t chain_smem_bytes(int nt, size_t tsz) {
+  return size_t(kChainRing) * kChainSeg * (sizeof(int) + tsz) + size_t(kChainRing) * (16 + sizeof(int)) +
+         size_t(kChainRing + 1) * tsz + size_t(kChainRing) * 8 + size_t(nt + 1) * tsz + 80;
+}
+
 // Where the grid solves hand the trailing rows to the one-warp chain.  A
-// level of the grid solves costs an L2 round trip and a publish (~2.5 us,
-// measured); in the chain a row costs its FP64 sum and butterfly on one warp
-// (~0.35 us), an entry ~1 ns, and each 128 entries past the first 128 of a
-// row an L2 round trip (~0.7 us: they are not loaded ahead).  Candidates are
-// the last 256, 512, ... rows (y and z of the chain in shared memory); the
-// tail that saves the most modelled time over both solves wins, none when
-// nothing is saved, so only runs of nearly one row per level are taken.
+// level of the grid solves costs an L2 round trip and a publish (~2.5 us
+// over both solves' waits, measured); in the chain a column costs its
+// barrier, its value and a warp step (~0.15 us per solve) and an entry
+// ~1.5 ns (a multiply-add in shared memory, 32 at a time).  Candidates are
+// the last 256, 512, ... rows, as many as shared memory holds the running
+// sums of; the tail that saves the most modelled time over both solves wins,
+// none when nothing is saved.
 constexpr double kGridLevelSeconds = 2.5e-6;
-constexpr double kChainRowSeconds = 0.35e-6;
-constexpr double kChainEntrySeconds = 1e-9;
-constexpr double kChainReloadSeconds = 0.7e-6;
-constexpr size_t kChainBytes = 192 * 1024;
+constexpr double kChainColSeconds = 0.15e-6;
+constexpr double kChainEntrySeconds = 1.5e-9;
+constexpr size_t kChainSmem = 220 * 1024;
 
 int chain_start(const LuSymbolic &S, size_t tsz) {
   const int n = S.n;
   if (n < 4096) return n;
-  const int max_rows = int(kChainBytes / (2 * tsz));
+  const int max_rows = int((kChainSmem - chain_smem_bytes(0, tsz)) / tsz) - 1;
   // L level of each row, the levels of the rows before r, and per column the
   // L entries below the diagonal (a tail from r holds those of columns >= r)
-  std::vector<int> lev(n), head(n + 1, 0), col_ptr(n + 1, 0);
+  std::vector<int> lev(n), head(n + 1, 0), col_cnt(n, 0);
   for (int i = 0; i < n; ++i) {
     int m = -1;
     for (int p = S.rp[i]; p < S.diag[i]; ++p) {
       m = std::max(m, lev[S.ci[p]]);
-      ++col_ptr[S.ci[p] + 1];
+      ++col_cnt[S.ci[p]];
     }
     lev[i] = m + 1;
     head[i + 1] = std::max(head[i], lev[i] + 1);
   }
-  // the rows of each column's L entries (a tail from r gains, in each row
-  // below, its entry in column r)
-  for (int c = 0; c < n; ++c) col_ptr[c + 1] += col_ptr[c];
-  std::vector<int> col_row((size_t)col_ptr[n]), fill(col_ptr.begin(), col_ptr.end() - 1);
-  for (int i = 0; i < n; ++i)
-    for (int p = S.rp[i]; p < S.diag[i]; ++p) col_row[(size_t)fill[S.ci[p]]++] = i;
   const int total = head[n];
   int best = n;
   double best_gain = 0.0;
-  int64_t entries = 0, reloads = 0;
-  std::vector<int> in_tail(n, 0);  // per row: its L entries in columns >= r
+  int64_t entries = 0;
   for (int r = n - 1; r >= std::max(1, n - max_rows); --r) {
-    for (int j = col_ptr[r]; j < col_ptr[r + 1]; ++j)
-      if (++in_tail[col_row[(size_t)j]] % 128 == 1 && in_tail[col_row[(size_t)j]] > 128) ++reloads;
-    const int u = S.rp[r + 1] - S.diag[r] - 1;
-    entries += (col_ptr[r + 1] - col_ptr[r]) + u;
-    reloads += std::max(0, (u + 127) / 128 - 1);
+    // row r joins: the L entries of column r (all in rows below it, in the
+    // tail) and its own U entries
+    entries += col_cnt[r] + (S.rp[r + 1] - S.diag[r] - 1);
     if ((n - r) % 256) continue;
     const double saved = 2.0 * (total - head[r]) * kGridLevelSeconds;
-    const double cost = 2.0 * (n - r) * kChainRowSeconds + entries * kChainEntrySeconds +
-                        reloads * kChainReloadSeconds;
+    const double cost = 2.0 * (n - r) * kChainColSeconds + entries * kChainEntrySeconds;
     if (saved - cost > best_gain) {
       best_gain = saved - cost;
       best = r;
@@ -1310,12 +1644,21 @@ struct xg_lu {
   double *d_hv = nullptr, *d_hb = nullptr, *d_hx = nullptr;  // xg_lu_solve_host staging
   int grid_factor = 0, grid_solve = 0;
   int stage_cap = 0;                       // grid refactor: staged row entries per warp
+  unsigned *d_pending = nullptr;           // its positions that start pending (one bit each)
   size_t smem_grid = 0;                    // its dynamic shared memory
   int grid_tri = 0;                        // grid solves: blocks
   int solve_tail0 = 0;                     // grid solves: first row of the one-warp chain (n: none)
   int4 *d_tdesc = nullptr;                 // its row descriptors
-  void *d_hpart = nullptr;                 // its rows' lane sums over earlier columns (T)
+  void *d_hpart = nullptr;                 // its rows' sums over earlier columns (T)
+  int4 *d_chain_seg = nullptr;             // its segments (ChainSegDesc)
+  int *d_chain_row = nullptr, *d_chain_pos = nullptr;  // per entry: chain row, position in val
+  void *d_chain_val = nullptr;             // per entry: value (T), gathered per refactor
+  int n_chain_seg = 0;
+  int64_t n_chain_ent = 0;
   size_t smem_chain = 0;                   // its y and z in shared memory
+  unsigned char *d_solo = nullptr;         // grid solves: rows lu_solve_long sums (LuDev::solo)
+  int *d_long = nullptr;                   // those rows: the lower solve's, then the upper's
+  int n_long_l = 0, n_long_u = 0;
   size_t smem_factor = 0, smem_solve = 0;  // > 0: the one-CTA path
   int cta_threads = 0;                     // its block size (warps ~ level width)
   bool narrow = false;                     // one lane walks the rows (<= 2 rows per level)
@@ -1328,7 +1671,7 @@ struct xg_lu {
   bool factored = false;
   xg::LuDev dev() const {
     return xg::LuDev{S.n, d_rp, d_ci, d_diag, d_lu2a, d_P, d_Q, d_arp, d_aci, d_urp, d_upos,
-                     d_ctrl, d_rdiag, solve_tail0, d_tdesc, d_hpart};
+                     d_ctrl, d_rdiag, solve_tail0, d_tdesc, d_hpart, d_solo};
   }
 };
 
@@ -1355,7 +1698,8 @@ int upload(V **dst, const std::vector<V> &src) {
 void free_lu(xg_lu *lu) {
   void *ptrs[] = {lu->d_rp, lu->d_ci, lu->d_diag, lu->d_lu2a, lu->d_P, lu->d_Q, lu->d_arp,
                   lu->d_urp, lu->d_upos, lu->d_lvl,
-                  lu->d_aci, lu->d_ctrl, lu->d_tdesc, lu->d_hpart, lu->d_val, lu->d_y, lu->d_z, lu->d_rdiag, lu->d_a,
+                  lu->d_aci, lu->d_ctrl, lu->d_tdesc, lu->d_hpart, lu->d_solo, lu->d_long, lu->d_pending, lu->d_chain_seg, lu->d_chain_row, lu->d_chain_pos,
+                  lu->d_chain_val, lu->d_val, lu->d_y, lu->d_z, lu->d_rdiag, lu->d_a,
                   lu->d_r, lu->d_dx, lu->d_hv, lu->d_hb, lu->d_hx};
   for (void *p : ptrs)
     if (p) cudaFree(p);
@@ -1384,9 +1728,15 @@ int refactor_t(xg_lu *lu, const double *dev_values) {
     return XG_OK;
   }
   xg::lu_assemble<T><<<lu->grid_solve, 256, 0, lu->stream>>>(
-      d, dev_values, lu->d_a, lu->S.nnz_a, (T *)lu->d_val, lu->nnz_lu); xg::count_launches(1);
+      d, dev_values, lu->d_a, lu->S.nnz_a, (T *)lu->d_val, lu->nnz_lu, lu->d_pending); xg::count_launches(1);
   xg::lu_factor<T><<<lu->grid_factor, 32 * xg::kFactorWarps, lu->smem_grid, lu->stream>>>(
-      d, (T *)lu->d_val, lu->stage_cap); xg::count_launches(1);
+      d, (T *)lu->d_val, lu->d_a, lu->stage_cap); xg::count_launches(1);
+  if (lu->n_chain_ent) {
+    const int blocks = int(std::min<int64_t>(1024, (lu->n_chain_ent + 255) / 256));
+    xg::lu_chain_gather<T><<<blocks, 256, 0, lu->stream>>>((const T *)lu->d_val, lu->d_chain_pos,
+                                                          (T *)lu->d_chain_val, lu->n_chain_ent);
+    xg::count_launches(1);
+  }
   XG_CU(cudaGetLastError());
   return XG_OK;
 }
@@ -1417,13 +1767,23 @@ int solve_once(xg_lu *lu, const double *b, double *x) {
       d, (T *)lu->d_y, (T *)lu->d_z);
   xg::count_launches(1);
   xg::lu_lsolve<T><<<lu->grid_tri, 256, 0, lu->stream>>>(d, (const T *)lu->d_val, b, (T *)lu->d_y); xg::count_launches(1);
+  if (lu->n_long_l) {
+    xg::lu_solve_long<T><<<lu->n_long_l, xg::kLongThreads, 0, lu->stream>>>(
+        d, (const T *)lu->d_val, b, (T *)lu->d_y, (T *)lu->d_z, x, lu->d_long, 0);
+    xg::count_launches(1);
+  }
   if (lu->solve_tail0 < lu->S.n) {
-    xg::lu_solve_chain<T><<<1, 32, lu->smem_chain, lu->stream>>>(d, (const T *)lu->d_val, b, (T *)lu->d_y,
-                                                                (T *)lu->d_z, x);
+    const xg::ChainDev c{lu->d_chain_seg, lu->n_chain_seg, lu->d_chain_row, lu->d_chain_val};
+    xg::lu_solve_chain<T><<<1, 32, lu->smem_chain, lu->stream>>>(d, c, b, (T *)lu->d_y, (T *)lu->d_z, x);
     xg::count_launches(1);
   }
   xg::lu_usolve<T><<<lu->grid_tri, 256, 0, lu->stream>>>(d, (const T *)lu->d_val, (const T *)lu->d_y,
                                                          (T *)lu->d_z, x); xg::count_launches(1);
+  if (lu->n_long_u) {
+    xg::lu_solve_long<T><<<lu->n_long_u, xg::kLongThreads, 0, lu->stream>>>(
+        d, (const T *)lu->d_val, b, (T *)lu->d_y, (T *)lu->d_z, x, lu->d_long + lu->n_long_l, 1);
+    xg::count_launches(1);
+  }
   XG_CU(cudaGetLastError());
   return XG_OK;
 }
@@ -1546,7 +1906,8 @@ extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const i
   {
     // Stage every row when the longest fits kStageBytes per warp (the long
     // rows of a dense trailing block are the critical path).  Otherwise (a
-    // supply node's row) all but the kUnstagedRows longest, with at least
+    // supply node's row) every row that fits kStageBytes when that costs no
+    // resident warps, else all but the kUnstagedRows longest, with at least
     // kMinStageBytes (a stage that small costs no occupancy: registers bound
     // it first): the longest rows stay in global memory rather than cut the
     // number of resident warps.
@@ -1554,26 +1915,47 @@ extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const i
     for (int i = 0; i < n; ++i) len[i] = S.rp[i + 1] - S.rp[i];
     const int max_row = *std::max_element(len.begin(), len.end());
     const int cap_max = xg::kStageBytes / int(tsz);
+    const void *fn = precision == XG_LU_FP32 ? (const void *)xg::lu_factor<float>
+                                             : (const void *)xg::lu_factor<double>;
+    auto round_cap = [](int c) { return (c + 31) / 32 * 32; };
+    auto occupancy = [&](int c, int *o) -> cudaError_t {
+      const size_t b = size_t(xg::kFactorWarps) * size_t(round_cap(c)) * tsz;
+      cudaError_t e2 = xg::allow_dynamic_smem(fn, b);
+      if (e2 == cudaSuccess) e2 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(o, fn, 32 * xg::kFactorWarps, b);
+      return e2;
+    };
     int cap = max_row;
     if (max_row > cap_max) {
+      int fit = 0;
+      for (int l : len)
+        if (l <= cap_max) fit = std::max(fit, l);
       const int k = std::min(n - 1, xg::kUnstagedRows);
       std::nth_element(len.begin(), len.begin() + k, len.end(), std::greater<int>());
       cap = std::min(cap_max, std::max(len[k], xg::kMinStageBytes / int(tsz)));
+      int occ_fit = 0, occ_cap = 0;
+      if (fit > cap) {
+        if ((e = occupancy(fit, &occ_fit)) || (e = occupancy(cap, &occ_cap))) {
+          free_lu(lu.get());
+          return cuda_fail(e, "xg_lu_analyze: shared-memory limit");
+        }
+        if (occ_fit >= occ_cap) cap = fit;
+      }
     }
-    lu->stage_cap = (cap + 31) / 32 * 32;
+    lu->stage_cap = round_cap(cap);
     lu->smem_grid = size_t(xg::kFactorWarps) * size_t(lu->stage_cap) * tsz;
-    const void *fn = precision == XG_LU_FP32 ? (const void *)xg::lu_factor<float>
-                                             : (const void *)xg::lu_factor<double>;
-    if ((e = xg::allow_dynamic_smem((const void *)fn, lu->smem_grid))) {
+    if ((e = occupancy(lu->stage_cap, &occ))) {
       free_lu(lu.get());
       return cuda_fail(e, "xg_lu_analyze: shared-memory limit");
     }
-    if (precision == XG_LU_FP32)
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, xg::lu_factor<float>, 32 * xg::kFactorWarps,
-                                                    lu->smem_grid);
-    else
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, xg::lu_factor<double>, 32 * xg::kFactorWarps,
-                                                    lu->smem_grid);
+    // the U part right of the diagonal of every staged row starts pending
+    std::vector<unsigned> pending((size_t(lu->nnz_lu) + 31) / 32, 0u);
+    for (int i = 0; i < n; ++i)
+      if (S.rp[i + 1] - S.rp[i] <= lu->stage_cap)
+        for (int p = S.diag[i] + 1; p < S.rp[i + 1]; ++p) pending[size_t(p) >> 5] |= 1u << (p & 31);
+    if ((rc = upload(&lu->d_pending, pending))) {
+      free_lu(lu.get());
+      return rc;
+    }
   }
   // one warp per row: never more warps than rows
   lu->grid_factor = std::max(1, std::min(sms * std::max(occ, 1), (n + xg::kFactorWarps - 1) / xg::kFactorWarps));
@@ -1595,15 +1977,78 @@ extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const i
         desc[r - t0] = make_int4(S.rp[r], S.rp[r] + int(std::lower_bound(c0, c1, t0) - c0), S.diag[r],
                                  S.P[r]);
       }
-      lu->smem_chain = 2 * size_t(nt) * tsz;
+      // the chain's segments: the lower solve's columns ascending (L entries
+      // of chain rows below each), then the upper solve's descending (U
+      // entries of chain rows above each), each column in pieces of at most
+      // kChainSeg entries padded to a multiple of 4 with the scratch row nt
+      std::vector<std::vector<std::pair<int, int>>> lcol(nt), ucol(nt);
+      for (int r = t0; r < n; ++r) {
+        for (int p = desc[r - t0].y; p < S.diag[r]; ++p) lcol[S.ci[p] - t0].push_back({r - t0, p});
+        for (int p = S.diag[r] + 1; p < S.rp[r + 1]; ++p) ucol[S.ci[p] - t0].push_back({r - t0, p});
+      }
+      std::vector<int4> seg;
+      std::vector<int> crow, cpos;
+      auto add_column = [&](int col, const std::vector<std::pair<int, int>> &ent, int upper) {
+        size_t j = 0;
+        bool first = true;
+        do {
+          const size_t m = std::min(ent.size() - j, size_t(xg::kChainSeg));
+          const int off = int(crow.size());
+          for (size_t q = 0; q < m; ++q) {
+            crow.push_back(ent[j + q].first);
+            cpos.push_back(ent[j + q].second);
+          }
+          while (crow.size() % 4) {
+            crow.push_back(nt);
+            cpos.push_back(-1);
+          }
+          seg.push_back(make_int4(col, off, int(crow.size()) - off, (first ? 1 : 0) | (upper ? 2 : 0)));
+          first = false;
+          j += m;
+        } while (j < ent.size());
+      };
+      for (int col = 0; col < nt; ++col) add_column(col, lcol[col], 0);
+      for (int col = nt - 1; col >= 0; --col) add_column(col, ucol[col], 1);
+      lu->n_chain_seg = int(seg.size());
+      lu->n_chain_ent = int64_t(crow.size());
+      lu->smem_chain = xg::chain_smem_bytes(nt, tsz);
       const void *fn = precision == XG_LU_FP32 ? (const void *)xg::lu_solve_chain<float>
                                                : (const void *)xg::lu_solve_chain<double>;
-      if ((rc = upload(&lu->d_tdesc, desc)) ||
-          (e = cudaMalloc(&lu->d_hpart, 32 * size_t(nt) * tsz)) ||
+      if ((rc = upload(&lu->d_tdesc, desc)) || (rc = upload(&lu->d_chain_seg, seg)) ||
+          (rc = upload(&lu->d_chain_row, crow)) || (rc = upload(&lu->d_chain_pos, cpos)) ||
+          (e = cudaMalloc(&lu->d_chain_val, std::max<size_t>(crow.size(), 1) * tsz)) ||
+          (e = cudaMalloc(&lu->d_hpart, size_t(nt) * tsz)) ||
           (e = xg::allow_dynamic_smem((const void *)fn, lu->smem_chain))) {
         free_lu(lu.get());
         return rc ? rc : cuda_fail(e, "xg_lu_analyze");
       }
+    }
+    // rows of the grid solves (below the chain) that lu_solve_long sums: a
+    // long L part whose column has no L entry below it (no later row of the
+    // lower solve reads its y), a long U part whose column has no U entry
+    // above it (no earlier row of the upper solve reads its z)
+    std::vector<unsigned char> solo(n, 0), l_read(n, 0), u_read(n, 0);
+    for (int i = 0; i < n; ++i) {
+      for (int p = S.rp[i]; p < S.diag[i]; ++p) l_read[S.ci[p]] = 1;
+      for (int p = S.diag[i] + 1; p < S.rp[i + 1]; ++p) u_read[S.ci[p]] = 1;
+    }
+    std::vector<int> long_l, long_u;
+    for (int i = 0; i < t0; ++i) {
+      if (S.diag[i] - S.rp[i] > xg::kSolveLongRow && !l_read[i]) {
+        solo[i] |= 1;
+        long_l.push_back(i);
+      }
+      if (S.rp[i + 1] - S.diag[i] - 1 > xg::kSolveLongRow && !u_read[i]) {
+        solo[i] |= 2;
+        long_u.push_back(i);
+      }
+    }
+    lu->n_long_l = int(long_l.size());
+    lu->n_long_u = int(long_u.size());
+    long_l.insert(long_l.end(), long_u.begin(), long_u.end());
+    if ((rc = upload(&lu->d_solo, solo)) || (rc = upload(&lu->d_long, long_l))) {
+      free_lu(lu.get());
+      return rc;
     }
   }
   // one-CTA path when the factor (and the solve's extra vectors) fit in shared memory
