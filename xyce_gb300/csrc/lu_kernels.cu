@@ -80,7 +80,8 @@ struct LuDev {
   void *rdiag;                // 1 / U(k,k) per row, written by the refactor
   // grid solves: rows >= tail0 (a chain of one-row levels) are solved by one
   // warp in order (tail0 = n: none); per tail row {start, first entry in a
-  // column >= tail0, diagonal, P}, and its sum over columns < tail0
+  // column >= tail0, diagonal, P}, and b(P(row)) less its sum over columns
+  // < tail0
   int tail0;
   const int4 *tdesc;
   void *hpart;
@@ -582,11 +583,12 @@ __global__ void __launch_bounds__(256) lu_lsolve(LuDev d, const T *__restrict__ 
     if (row >= d.n) break;
     const int s = __ldg(d.rp + row), dp = __ldg(d.diag + row);
     if (row >= d.tail0) {
-      // a row of the chain: its sum over the entries in columns below tail0;
-      // the chain kernel starts from it
+      // a row of the chain: b(P(row)) less its sum over the entries in
+      // columns below tail0; the chain kernel starts from it
       const int sp = d.tdesc[row - d.tail0].y;
+      const T bi = lane == 0 ? T(b[__ldg(d.P + row)]) : T(0);
       const T acc = warp_sum(lane_dot(d, val, y, s, sp, lane));
-      if (lane == 0) reinterpret_cast<T *>(d.hpart)[row - d.tail0] = acc;
+      if (lane == 0) reinterpret_cast<T *>(d.hpart)[row - d.tail0] = bi - acc;
       continue;
     }
     if (dp - s > kSolveLongRow && (__ldg(d.solo + row) & 1)) continue;  // lu_solve_long's
@@ -665,37 +667,53 @@ __global__ void __launch_bounds__(kLongThreads) lu_solve_long(LuDev d, const T *
 // ("right-looking"): its rows' running sums live in shared memory; once a
 // column's value is final (y(c), then z(c)), the warp subtracts it times the
 // column's entries from the sums of the rows they are in.  A row's sum takes
-// its entries in column order, the same on every run.  The entries come in
-// column-ordered segments (rows, values; at most kChainSeg, padded to a
-// multiple of 4 with a scratch row), copied global -> shared by the bulk
-// copy engine (cp.async.bulk, completion counted on an mbarrier) kChainRing
-// segments ahead of their use, so the warp never waits on a load.
+// its entries in column order, the same on every run.
+//
+// The entries (row, value) come in column-ordered segments of at most
+// kChainSeg, each padded to a multiple of 4 with the scratch row nt, one
+// contiguous stream; each segment has a 32-byte record (column, length,
+// flags, x position, reciprocal pivot).  Both streams are copied global ->
+// shared in fixed chunks by the bulk copy engine (cp.async.bulk, completion
+// counted on an mbarrier per chunk) into rings of kChainChunks chunks: a
+// chunk is refilled as soon as the warp has passed it, so the copies run
+// several chunks ahead and the warp never waits on a load.
 constexpr int kChainSeg = 128;
-constexpr int kChainRing = 16;
+constexpr int kChainChunks = 8;
+constexpr int kChainEntChunk = 256;  // entries per chunk
+constexpr int kChainRecChunk = 32;   // segment records per chunk
 
-// A segment: its column (chain-local), where its entries start (a multiple
-// of 4), how many (a multiple of 4, <= kChainSeg), and flags: 1 its column's
-// first segment, 2 the upper solve.
-struct ChainSegDesc {
-  int col, off, len, flags;
+// A segment's record: its column (chain-local), entries, flags (1 its
+// column's first segment, 2 the upper solve), x position Q(t0 + column) and
+// the column's reciprocal pivot (upper solve, first segment; written per
+// refactor by lu_chain_gather).
+struct ChainRec {
+  int col, len, flags, q;
+  double rd;
+  double pad;
 };
+static_assert(sizeof(ChainRec) == 32, "chain record");
 
-// chain_val[j] = val[chain_pos[j]] (0 for padding): the chain's entries in
-// segment order, gathered once per refactor.
+// Per refactor: each entry's value from the factor (0 for padding) and each
+// record's reciprocal pivot.
 template <class T>
-__global__ void lu_chain_gather(const T *__restrict__ val, const int *__restrict__ pos, T *__restrict__ out,
-                                int64_t n) {
-  for (int64_t j = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < n; j += int64_t(gridDim.x) * blockDim.x) {
+__global__ void lu_chain_gather(LuDev d, const T *__restrict__ val, const int *__restrict__ pos,
+                                T *__restrict__ out, int64_t n, ChainRec *rec, int n_rec) {
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  for (int64_t j = t; j < n; j += stride) {
     const int p = __ldg(pos + j);
     out[j] = p >= 0 ? __ldcg(val + p) : T(0);
   }
+  for (int64_t g = t; g < n_rec; g += stride)
+    if ((rec[g].flags & 3) == 3) rec[g].rd = double(__ldcg((const T *)d.rdiag + d.tail0 + rec[g].col));
 }
 
 struct ChainDev {
-  const int4 *seg;   // ChainSegDesc, the lower solve's then the upper's
+  const ChainRec *rec;  // n_seg records, padded to whole chunks
   int n_seg;
-  const int *row;    // chain-local row of each entry (nt: scratch)
-  const void *val;   // T: each entry's value (lu_chain_gather)
+  const int *row;       // chain-local row of each entry (nt: scratch), padded to whole chunks
+  const void *val;      // T: each entry's value (lu_chain_gather)
+  int64_t n_ent;        // entries, padded to whole chunks
 };
 
 __device__ __forceinline__ unsigned smem_addr(const void *p) {
@@ -716,138 +734,124 @@ __device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity, int lim
     if (mbar_try(bar, parity)) return true;
   return false;
 }
+// One thread: `bytes` from global src to shared dst, counted on barrier mb.
+__device__ __forceinline__ void bulk_copy(void *dst, const void *src, unsigned bytes, unsigned mb) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(mb)
+               : "memory");
+}
 
 template <class T>
-__global__ void __launch_bounds__(32) lu_solve_chain(LuDev d, ChainDev c, const double *__restrict__ b, T *y,
-                                                     T *z, double *x) {
+__global__ void __launch_bounds__(32) lu_solve_chain(LuDev d, ChainDev c, T *y, T *z, double *x) {
   extern __shared__ __align__(128) unsigned char chain_raw[];
+  constexpr int kE = kChainChunks * kChainEntChunk, kR = kChainChunks * kChainRecChunk;
   const int lane = threadIdx.x, t0 = d.tail0, nt = d.n - t0;
-  // ring: per slot the rows and values of one segment, its descriptor,
-  // reciprocal pivot and x position, and its barrier; then the running sums
-  // (nt + scratch)
+  // rings (entry rows, entry values, records), their barriers, then the
+  // running sums (nt + scratch)
   int *ring_row = reinterpret_cast<int *>(chain_raw);
-  T *ring_val = reinterpret_cast<T *>(ring_row + kChainRing * kChainSeg);
-  int4 *ring_desc = reinterpret_cast<int4 *>(ring_val + kChainRing * kChainSeg);
-  int *ring_q = reinterpret_cast<int *>(ring_desc + kChainRing);
-  T *ring_rd = reinterpret_cast<T *>(ring_q + kChainRing);
-  unsigned long long *bar = reinterpret_cast<unsigned long long *>(
-      reinterpret_cast<uintptr_t>(ring_rd + kChainRing + 1) / 8 * 8 + 8);
-  T *acc = reinterpret_cast<T *>(bar + kChainRing);
-  const T *rdiag = (const T *)d.rdiag;
-  const T *cval = (const T *)c.val;
+  T *ring_val = reinterpret_cast<T *>(ring_row + kE);
+  ChainRec *ring_rec = reinterpret_cast<ChainRec *>(ring_val + kE);
+  unsigned long long *bar_e = reinterpret_cast<unsigned long long *>(ring_rec + kR);
+  unsigned long long *bar_r = bar_e + kChainChunks;
+  T *acc = reinterpret_cast<T *>(bar_r + kChainChunks);
   const int limit = int(__ldg(&d.ctrl[C_SPIN]));
+  const int n_ech = int(c.n_ent / kChainEntChunk);
+  const int n_rch = (c.n_seg + kChainRecChunk - 1) / kChainRecChunk;
+  const T *cval = (const T *)c.val;
+
+  // lane 0 refills ring slot k % kChainChunks with entry / record chunk k
+  auto issue_ent = [&](int k) {
+    if (lane == 0 && k < n_ech) {
+      const int s = k % kChainChunks;
+      const unsigned mb = smem_addr(bar_e + s);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb),
+                   "r"(unsigned(kChainEntChunk * (sizeof(int) + sizeof(T))))
+                   : "memory");
+      bulk_copy(ring_row + s * kChainEntChunk, c.row + size_t(k) * kChainEntChunk,
+                unsigned(kChainEntChunk * sizeof(int)), mb);
+      bulk_copy(ring_val + s * kChainEntChunk, cval + size_t(k) * kChainEntChunk,
+                unsigned(kChainEntChunk * sizeof(T)), mb);
+    }
+  };
+  auto issue_rec = [&](int k) {
+    if (lane == 0 && k < n_rch) {
+      const int s = k % kChainChunks;
+      const unsigned mb = smem_addr(bar_r + s);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb),
+                   "r"(unsigned(kChainRecChunk * sizeof(ChainRec)))
+                   : "memory");
+      bulk_copy(ring_rec + s * kChainRecChunk, c.rec + size_t(k) * kChainRecChunk,
+                unsigned(kChainRecChunk * sizeof(ChainRec)), mb);
+    }
+  };
 
   if (lane == 0) {
-    for (int i = 0; i < kChainRing; ++i)
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar + i)) : "memory");
+    for (int i = 0; i < 2 * kChainChunks; ++i)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar_e + i)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  for (int r = lane; r < nt; r += 32)
-    acc[r] = T(b[d.tdesc[r].w]) - __ldcg(reinterpret_cast<const T *>(d.hpart) + r);
+  __syncwarp();
+  for (int k = 0; k < kChainChunks; ++k) {
+    issue_rec(k);
+    issue_ent(k);
+  }
+  // the sums start from b(P(row)) minus the row's sum over columns < t0
+  // (the grid lower solve's)
+  const T *h = reinterpret_cast<const T *>(d.hpart);
+#pragma unroll 8
+  for (int r = lane; r < nt; r += 32) acc[r] = __ldcg(h + r);
   if (lane == 0) acc[nt] = T(0);
   __syncwarp();
 
-  // segment descriptors: lane j holds those of segments w + j (the issue
-  // window) and w + 32 + j (the next), loaded a window ahead, with the
-  // reciprocal pivot and x position an upper segment's column needs
-  auto load_desc = [&](int g, int4 &ds, T &rd, int &qx) {
-    ds = make_int4(0, 0, 0, 0);
-    rd = T(0);
-    qx = 0;
-    if (g < c.n_seg) {
-      ds = c.seg[g];
-      if (ds.w & 2) {
-        rd = __ldcg(rdiag + t0 + ds.x);
-        qx = __ldg(d.Q + t0 + ds.x);
-      }
-    }
-  };
-  int w = 0;
-  int4 da, db;
-  T ra, rb;
-  int qa, qb;
-  load_desc(lane, da, ra, qa);
-  load_desc(32 + lane, db, rb, qb);
-  // lane 0 starts the copy of segment g into slot g % kChainRing
-  auto issue = [&](int g) {
-    if (g - w == 32) {
-      w += 32;
-      da = db;
-      ra = rb;
-      qa = qb;
-      load_desc(w + 32 + lane, db, rb, qb);
-    }
-    int4 ds;
-    ds.x = __shfl_sync(0xffffffffu, da.x, g - w);
-    ds.y = __shfl_sync(0xffffffffu, da.y, g - w);
-    ds.z = __shfl_sync(0xffffffffu, da.z, g - w);
-    ds.w = __shfl_sync(0xffffffffu, da.w, g - w);
-    const T rd = __shfl_sync(0xffffffffu, ra, g - w);
-    const int qx = __shfl_sync(0xffffffffu, qa, g - w);
-    if (lane == 0) {
-      const int slot = g % kChainRing;
-      ring_desc[slot] = ds;
-      ring_rd[slot] = rd;
-      ring_q[slot] = qx;
-      const unsigned mb = smem_addr(bar + slot);
-      const unsigned bytes = unsigned(ds.z) * unsigned(sizeof(int) + sizeof(T));
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(bytes) : "memory");
-      if (ds.z > 0) {
-        asm volatile(
-            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                smem_addr(ring_row + slot * kChainSeg)),
-            "l"(c.row + ds.y), "r"(unsigned(ds.z) * unsigned(sizeof(int))), "r"(mb)
-            : "memory");
-        asm volatile(
-            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                smem_addr(ring_val + slot * kChainSeg)),
-            "l"(cval + ds.y), "r"(unsigned(ds.z) * unsigned(sizeof(T))), "r"(mb)
-            : "memory");
-      }
-    }
-  };
-  // kChainRing - 1 segments in flight: segment g + kChainRing - 1 goes into
-  // the slot segment g - 1 has just left, before segment g is waited for
-  constexpr int kAhead = kChainRing - 1;
-  const int pre = min(kAhead, c.n_seg);
-  for (int g = 0; g < pre; ++g) issue(g);
-
   T v = T(0);
-  int g = 0;
+  int64_t off = 0;      // the segment's first entry in the stream
+  int ent_wait = 0;     // entry chunks waited for so far
+  int ent_free = 0;     // entry chunks passed (and refilled)
   bool ok = true;
+  int g = 0;
   for (; g < c.n_seg; ++g) {
-    if (g + kAhead < c.n_seg) issue(g + kAhead);
-    const int slot = g % kChainRing;
-    if (!mbar_wait(smem_addr(bar + slot), unsigned(g / kChainRing) & 1u, limit)) {
-      ok = false;
-      break;
+    if (g % kChainRecChunk == 0) {
+      const int k = g / kChainRecChunk;
+      if (!mbar_wait(smem_addr(bar_r + k % kChainChunks), unsigned(k / kChainChunks) & 1u, limit)) {
+        ok = false;
+        break;
+      }
     }
-    const int4 ds = ring_desc[slot];
-    const int *sr = ring_row + slot * kChainSeg;
-    const T *sv = ring_val + slot * kChainSeg;
-    // the segment's rows and values, loaded before the column's value is
-    // needed; its rows are distinct (scratch padding aside), so every sum is
-    // read before any is written
+    const ChainRec rc = ring_rec[g % kR];
+    const int len = rc.len;
+    // the chunks this segment's entries lie in (at most two)
+    const int need = len > 0 ? int((off + len - 1) / kChainEntChunk) : ent_wait - 1;
+    while (ok && ent_wait <= need) {
+      ok = mbar_wait(smem_addr(bar_e + ent_wait % kChainChunks), unsigned(ent_wait / kChainChunks) & 1u, limit);
+      ++ent_wait;
+    }
+    if (!ok) break;
+    // the segment's rows and values before the column's value is needed;
+    // its rows are distinct (scratch padding aside), so every sum is read
+    // before any is written
     int ri[kChainSeg / 32];
     T wv[kChainSeg / 32];
 #pragma unroll
     for (int r = 0; r < kChainSeg / 32; ++r) {
       const int j = 32 * r + lane;
-      ri[r] = j < ds.z ? sr[j] : nt;
-      wv[r] = j < ds.z ? sv[j] : T(0);
+      const int e = int((off + j) & (kE - 1));
+      ri[r] = j < len ? ring_row[e] : nt;
+      wv[r] = j < len ? ring_val[e] : T(0);
     }
-    if (ds.w & 1) {
+    if (rc.flags & 1) {
       // the column's value is final: every earlier column has been applied
-      v = acc[ds.x];
-      if (ds.w & 2) v *= ring_rd[slot];
-      if (lane == 0) {
-        if (ds.w & 2) {
-          z[t0 + ds.x] = v;
-          x[ring_q[slot]] = double(v);
-        } else {
-          y[t0 + ds.x] = v;
+      v = acc[rc.col];
+      if (rc.flags & 2) {
+        v *= T(rc.rd);
+        if (lane == 0) {
+          z[t0 + rc.col] = v;
+          x[rc.q] = double(v);
         }
+      } else if (lane == 0) {
+        y[t0 + rc.col] = v;
       }
     }
     T av[kChainSeg / 32];
@@ -857,16 +861,26 @@ __global__ void __launch_bounds__(32) lu_solve_chain(LuDev d, ChainDev c, const 
     for (int r = 0; r < kChainSeg / 32; ++r) av[r] -= wv[r] * v;
 #pragma unroll
     for (int r = 0; r < kChainSeg / 32; ++r)
-      if (32 * r + lane < ds.z) acc[ri[r]] = av[r];
+      if (32 * r + lane < len) acc[ri[r]] = av[r];
     __syncwarp();
+    // refill the chunks the warp has passed
+    off += len;
+    while (ent_free < int(off / kChainEntChunk)) {
+      issue_ent(ent_free + kChainChunks);
+      ++ent_free;
+    }
+    if ((g + 1) % kChainRecChunk == 0) issue_rec(g / kChainRecChunk + kChainChunks);
   }
   if (!ok) {
     // a copy that did not complete in time: report it, and let the copies
     // still in flight land before the block's shared memory is released
     if (lane == 0) atomicOr(&d.ctrl[C_STATUS], ST_TIMEOUT);
-    const int end = min(c.n_seg, g + kAhead + 1);
-    for (int h = g; h < end; ++h)
-      mbar_wait(smem_addr(bar + h % kChainRing), unsigned(h / kChainRing) & 1u, 1 << 22);
+    const int e_end = min(n_ech, ent_free + kChainChunks);
+    for (int k = max(ent_wait - 1, 0); k < e_end; ++k)
+      mbar_wait(smem_addr(bar_e + k % kChainChunks), unsigned(k / kChainChunks) & 1u, 1 << 22);
+    const int r_end = min(n_rch, g / kChainRecChunk + kChainChunks);
+    for (int k = g / kChainRecChunk; k < r_end; ++k)
+      mbar_wait(smem_addr(bar_r + k % kChainChunks), unsigned(k / kChainChunks) & 1u, 1 << 22);
   }
 }
 
@@ -1562,12 +1576,12 @@ __global__ void __launch_bounds__(1024) lu_factor_solve_lvl(LuDev d, LvlDev v,
   lvl_solve<T>(d, v, m, x);
 }
 
-// Shared memory of lu_solve_chain: the segment ring (rows, values,
-// descriptors, reciprocal pivots, barriers) and the running sums of nt rows
-// plus the scratch row, with slack for the barriers' alignment.
+// Shared memory of lu_solve_chain: the entry and record rings, their
+// barriers, and the running sums of nt rows plus the scratch row.
 size_t chain_smem_bytes(int nt, size_t tsz) {
-  return size_t(kChainRing) * kChainSeg * (sizeof(int) + tsz) + size_t(kChainRing) * (16 + sizeof(int)) +
-         size_t(kChainRing + 1) * tsz + size_t(kChainRing) * 8 + size_t(nt + 1) * tsz + 80;
+  return size_t(kChainChunks) * kChainEntChunk * (sizeof(int) + tsz) +
+         size_t(kChainChunks) * kChainRecChunk * sizeof(ChainRec) + 2 * size_t(kChainChunks) * 8 +
+         size_t(nt + 1) * tsz;
 }
 
 // Where the grid solves hand the trailing rows to the one-warp chain.  A
@@ -1650,11 +1664,11 @@ struct xg_lu {
   int solve_tail0 = 0;                     // grid solves: first row of the one-warp chain (n: none)
   int4 *d_tdesc = nullptr;                 // its row descriptors
   void *d_hpart = nullptr;                 // its rows' sums over earlier columns (T)
-  int4 *d_chain_seg = nullptr;             // its segments (ChainSegDesc)
+  xg::ChainRec *d_chain_rec = nullptr;     // its segments' records (whole chunks)
   int *d_chain_row = nullptr, *d_chain_pos = nullptr;  // per entry: chain row, position in val
   void *d_chain_val = nullptr;             // per entry: value (T), gathered per refactor
-  int n_chain_seg = 0;
-  int64_t n_chain_ent = 0;
+  int n_chain_seg = 0, n_chain_rec = 0;
+  int64_t n_chain_ent = 0;                 // entries, whole chunks
   size_t smem_chain = 0;                   // its y and z in shared memory
   unsigned char *d_solo = nullptr;         // grid solves: rows lu_solve_long sums (LuDev::solo)
   int *d_long = nullptr;                   // those rows: the lower solve's, then the upper's
@@ -1698,7 +1712,7 @@ int upload(V **dst, const std::vector<V> &src) {
 void free_lu(xg_lu *lu) {
   void *ptrs[] = {lu->d_rp, lu->d_ci, lu->d_diag, lu->d_lu2a, lu->d_P, lu->d_Q, lu->d_arp,
                   lu->d_urp, lu->d_upos, lu->d_lvl,
-                  lu->d_aci, lu->d_ctrl, lu->d_tdesc, lu->d_hpart, lu->d_solo, lu->d_long, lu->d_pending, lu->d_chain_seg, lu->d_chain_row, lu->d_chain_pos,
+                  lu->d_aci, lu->d_ctrl, lu->d_tdesc, lu->d_hpart, lu->d_solo, lu->d_long, lu->d_pending, lu->d_chain_rec, lu->d_chain_row, lu->d_chain_pos,
                   lu->d_chain_val, lu->d_val, lu->d_y, lu->d_z, lu->d_rdiag, lu->d_a,
                   lu->d_r, lu->d_dx, lu->d_hv, lu->d_hb, lu->d_hx};
   for (void *p : ptrs)
@@ -1733,8 +1747,9 @@ int refactor_t(xg_lu *lu, const double *dev_values) {
       d, (T *)lu->d_val, lu->d_a, lu->stage_cap); xg::count_launches(1);
   if (lu->n_chain_ent) {
     const int blocks = int(std::min<int64_t>(1024, (lu->n_chain_ent + 255) / 256));
-    xg::lu_chain_gather<T><<<blocks, 256, 0, lu->stream>>>((const T *)lu->d_val, lu->d_chain_pos,
-                                                          (T *)lu->d_chain_val, lu->n_chain_ent);
+    xg::lu_chain_gather<T><<<blocks, 256, 0, lu->stream>>>(d, (const T *)lu->d_val, lu->d_chain_pos,
+                                                          (T *)lu->d_chain_val, lu->n_chain_ent,
+                                                          lu->d_chain_rec, lu->n_chain_rec);
     xg::count_launches(1);
   }
   XG_CU(cudaGetLastError());
@@ -1773,8 +1788,8 @@ int solve_once(xg_lu *lu, const double *b, double *x) {
     xg::count_launches(1);
   }
   if (lu->solve_tail0 < lu->S.n) {
-    const xg::ChainDev c{lu->d_chain_seg, lu->n_chain_seg, lu->d_chain_row, lu->d_chain_val};
-    xg::lu_solve_chain<T><<<1, 32, lu->smem_chain, lu->stream>>>(d, c, b, (T *)lu->d_y, (T *)lu->d_z, x);
+    const xg::ChainDev c{lu->d_chain_rec, lu->n_chain_seg, lu->d_chain_row, lu->d_chain_val, lu->n_chain_ent};
+    xg::lu_solve_chain<T><<<1, 32, lu->smem_chain, lu->stream>>>(d, c, (T *)lu->d_y, (T *)lu->d_z, x);
     xg::count_launches(1);
   }
   xg::lu_usolve<T><<<lu->grid_tri, 256, 0, lu->stream>>>(d, (const T *)lu->d_val, (const T *)lu->d_y,
@@ -1986,14 +2001,14 @@ extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const i
         for (int p = desc[r - t0].y; p < S.diag[r]; ++p) lcol[S.ci[p] - t0].push_back({r - t0, p});
         for (int p = S.diag[r] + 1; p < S.rp[r + 1]; ++p) ucol[S.ci[p] - t0].push_back({r - t0, p});
       }
-      std::vector<int4> seg;
+      std::vector<xg::ChainRec> rec;
       std::vector<int> crow, cpos;
       auto add_column = [&](int col, const std::vector<std::pair<int, int>> &ent, int upper) {
         size_t j = 0;
         bool first = true;
         do {
           const size_t m = std::min(ent.size() - j, size_t(xg::kChainSeg));
-          const int off = int(crow.size());
+          const size_t off = crow.size();
           for (size_t q = 0; q < m; ++q) {
             crow.push_back(ent[j + q].first);
             cpos.push_back(ent[j + q].second);
@@ -2002,19 +2017,27 @@ extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const i
             crow.push_back(nt);
             cpos.push_back(-1);
           }
-          seg.push_back(make_int4(col, off, int(crow.size()) - off, (first ? 1 : 0) | (upper ? 2 : 0)));
+          rec.push_back(xg::ChainRec{col, int(crow.size() - off), (first ? 1 : 0) | (upper ? 2 : 0),
+                                     S.Q[t0 + col], 0.0, 0.0});
           first = false;
           j += m;
         } while (j < ent.size());
       };
       for (int col = 0; col < nt; ++col) add_column(col, lcol[col], 0);
       for (int col = nt - 1; col >= 0; --col) add_column(col, ucol[col], 1);
-      lu->n_chain_seg = int(seg.size());
+      lu->n_chain_seg = int(rec.size());
+      // both streams in whole chunks
+      while (crow.size() % xg::kChainEntChunk) {
+        crow.push_back(nt);
+        cpos.push_back(-1);
+      }
+      while (rec.size() % xg::kChainRecChunk) rec.push_back(xg::ChainRec{0, 0, 0, 0, 0.0, 0.0});
+      lu->n_chain_rec = int(rec.size());
       lu->n_chain_ent = int64_t(crow.size());
       lu->smem_chain = xg::chain_smem_bytes(nt, tsz);
       const void *fn = precision == XG_LU_FP32 ? (const void *)xg::lu_solve_chain<float>
                                                : (const void *)xg::lu_solve_chain<double>;
-      if ((rc = upload(&lu->d_tdesc, desc)) || (rc = upload(&lu->d_chain_seg, seg)) ||
+      if ((rc = upload(&lu->d_tdesc, desc)) || (rc = upload(&lu->d_chain_rec, rec)) ||
           (rc = upload(&lu->d_chain_row, crow)) || (rc = upload(&lu->d_chain_pos, cpos)) ||
           (e = cudaMalloc(&lu->d_chain_val, std::max<size_t>(crow.size(), 1) * tsz)) ||
           (e = cudaMalloc(&lu->d_hpart, size_t(nt) * tsz)) ||
