@@ -145,11 +145,11 @@ def test_oracle_solve_matches_the_reference_sparse_solver(case, oracle_lib):
 def test_chain_tail_is_modelled_where_rows_are_levels(engine_lib, oracle_lib):
     """The grid solves hand a factor's trailing run of one-row levels to one
     warp when the time model says it pays: on the 60x60 power grid the last
-    512 rows (its dense block and the levels above it), never on factors
+    768 rows (its dense block and the levels above it), never on factors
     below 4,096 rows."""
     from helpers import circuit_jacobian
     A = circuit_jacobian(netlists.power_grid(60, 60, 1200, seed=1), seed=5)
     info = engine.lu_analyze_host(A.indptr, A.indices, A.data, with_info=True)[3]
-    assert info.solve_chain == 512
+    assert info.solve_chain == 768
     small = circuit_jacobian(netlists.inverter_chain(200), seed=5)
     assert engine.lu_analyze_host(small.indptr, small.indices, small.data, with_info=True)[3].solve_chain == 0

@@ -3,10 +3,9 @@ where they load (a host simulator that gives the GPU a fixed memory budget up
 front, a real-time loop that must never enter the allocator).  Its stamp-term
 scratch is a fixed array inside the library instead of a per-circuit buffer,
 and its outputs go to a buffer the caller passes in.  Checked through the C
-ABI against xg_load on two calls in a row, on a level-1 circuit (terms
-scattered into reduction order) and on a BSIM3 circuit (terms in instance
-order, gathered by the reduction), and for its size limit.  Kept in a file
-collected last.
+ABI against xg_load: on two calls in a row on a level-1 circuit, on a BSIM3
+circuit (its members carried between loads start from zero in two circuits
+set up alike), and for its size limit.  Kept in a file collected last.
 """
 import ctypes as C
 
@@ -53,6 +52,44 @@ def test_noalloc_load_matches_regular_load_twice(engine_lib):
         np.testing.assert_array_equal(got[4 * n1 + c.nnz:4 * n1 + 2 * c.nnz], want["dQdx"])
         np.testing.assert_array_equal(c.download(abi.VEC_STA_NEXT), want_state[0])
         np.testing.assert_array_equal(c.download(abi.VEC_STO_NEXT), want_state[1])
+    c.close()
+    ctx.close()
+
+
+def _compare_outputs(c, got, want):
+    n1 = c.n_unknowns + 1
+    np.testing.assert_array_equal(got[0:c.n_unknowns], want["F"])
+    np.testing.assert_array_equal(got[n1:n1 + c.n_unknowns], want["Q"])
+    np.testing.assert_array_equal(got[2 * n1:2 * n1 + c.n_unknowns], want["dFdxdVp"])
+    np.testing.assert_array_equal(got[3 * n1:3 * n1 + c.n_unknowns], want["dQdxdVp"])
+    np.testing.assert_array_equal(got[4 * n1:4 * n1 + c.nnz], want["dFdx"])
+    np.testing.assert_array_equal(got[4 * n1 + c.nnz:4 * n1 + 2 * c.nnz], want["dQdx"])
+
+
+def test_noalloc_load_matches_regular_load_bsim3(engine_lib):
+    import torch
+    L = engine.lib()
+    L.xg_load_noalloc.argtypes = [C.c_void_p, C.POINTER(abi.XgLoadFlags), C.c_void_p, C.c_int64]
+    ctx = engine.Context(0, abi.device_options())
+    models = (abi.Model(abi.DEV_BSIM3, 1), abi.Model(abi.DEV_BSIM3, -1))
+    nl = netlists.random_mos_netlist(20_000, 5_000, dev_type=abi.DEV_BSIM3, seed=4, models=models)
+    ref = engine.Circuit(ctx, nl)
+    c = engine.Circuit(ctx, nl)
+    assert c.info.n_terms <= 2 * 1024 * 1024
+    ins = netlists.random_state(c.n_unknowns, c.n_state, c.n_store, seed=31)
+    flags = abi.load_flags(transient=1, newton_iter=1, time=0.0, pdt=1e11)
+    ref.set_state(*ins)
+    ref.load(flags)
+    want = ref.outputs()
+    n_out = 4 * (c.n_unknowns + 1) + 2 * c.nnz
+    out = torch.full((n_out,), float("nan"), dtype=torch.float64, device="cuda:0")
+    c.set_state(*ins)
+    assert _noalloc(c, flags, out.data_ptr(), n_out) == 0, L.xg_last_error()
+    ctx.synchronize()
+    _compare_outputs(c, out.cpu().numpy(), want)
+    np.testing.assert_array_equal(c.download(abi.VEC_STA_NEXT), ref.download(abi.VEC_STA_NEXT))
+    np.testing.assert_array_equal(c.download(abi.VEC_STO_NEXT), ref.download(abi.VEC_STO_NEXT))
+    ref.close()
     c.close()
     ctx.close()
 

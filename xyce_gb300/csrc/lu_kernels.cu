@@ -42,6 +42,7 @@
 
 #include "xg.h"
 #include "xg_internal.h"
+#include "lu_chain.h"
 #include "xg_lu.h"
 #include "xg_smem.cuh"
 
@@ -663,57 +664,57 @@ __global__ void __launch_bounds__(kLongThreads) lu_solve_long(LuDev d, const T *
 // The chain at the end of a factor whose last rows each form their own
 // level (a supply node and what hangs on it, or the dense block the order
 // leaves last): grid-wide, every row would cost an L2 round trip for its
-// dependencies.  Here one warp solves the chain column by column
-// ("right-looking"): its rows' running sums live in shared memory; once a
-// column's value is final (y(c), then z(c)), the warp subtracts it times the
-// column's entries from the sums of the rows they are in.  A row's sum takes
-// its entries in column order, the same on every run.
-//
-// The entries (row, value) come in column-ordered segments of at most
-// kChainSeg, each padded to a multiple of 4 with the scratch row nt, one
-// contiguous stream; each segment has a 32-byte record (column, length,
-// flags, x position, reciprocal pivot).  Both streams are copied global ->
-// shared in fixed chunks by the bulk copy engine (cp.async.bulk, completion
-// counted on an mbarrier per chunk) into rings of kChainChunks chunks: a
-// chunk is refilled as soon as the warp has passed it, so the copies run
-// several chunks ahead and the warp never waits on a load.
-constexpr int kChainSeg = 128;
+// dependencies.  Here one warp solves the chain 32 columns at a time, both
+// ways, with the rows' running sums in shared memory (the plan is
+// build_chain_plan in lu_chain.h):
+//  * the block's own 32 x 32 triangle: lane i holds row i's sum and its
+//    triangle row in registers; at step t lane t's value is final (times its
+//    reciprocal pivot going backward) and goes to the other lanes by a
+//    shuffle, each subtracting its multiple: a shuffle and a multiply-add
+//    per column on the critical path;
+//  * the block's entries in rows outside it, in rounds of 32 (a row per
+//    lane, a lane's rows in turn), each row's sum read once and written once.
+// Every row's sum takes its updates in the column order of a
+// column-by-column solve, the same on every run.  Tiles and rounds are
+// copied global -> shared by the bulk copy engine (cp.async.bulk, an
+// mbarrier counting each copy's bytes) into rings, refilled as the warp
+// passes them, so the warp does not wait on loads.
+constexpr int kChainTileRing = 3;
 constexpr int kChainChunks = 8;
-constexpr int kChainEntChunk = 256;  // entries per chunk
-constexpr int kChainRecChunk = 32;   // segment records per chunk
+constexpr int kChainEntChunk = 256;  // entries (8 rounds) per chunk
 
-// A segment's record: its column (chain-local), entries, flags (1 its
-// column's first segment, 2 the upper solve), x position Q(t0 + column) and
-// the column's reciprocal pivot (upper solve, first segment; written per
-// refactor by lu_chain_gather).
-struct ChainRec {
-  int col, len, flags, q;
-  double rd;
-  double pad;
-};
-static_assert(sizeof(ChainRec) == 32, "chain record");
+__host__ __device__ constexpr size_t chain_tile_bytes(size_t tsz) {
+  return size_t(kChainTileValues) * tsz + kChainBlock * sizeof(int);
+}
 
-// Per refactor: each entry's value from the factor (0 for padding) and each
-// record's reciprocal pivot.
+// Per refactor: each entry's value and each tile's triangle and reciprocal
+// pivots from the factor.
 template <class T>
-__global__ void lu_chain_gather(LuDev d, const T *__restrict__ val, const int *__restrict__ pos,
-                                T *__restrict__ out, int64_t n, ChainRec *rec, int n_rec) {
+__global__ void lu_chain_gather(LuDev d, const T *__restrict__ val, const int *__restrict__ ent_src,
+                                T *__restrict__ ent_val, int64_t n_ent, const int *__restrict__ tile_src,
+                                unsigned char *__restrict__ tiles, int n_blk) {
   const int64_t stride = int64_t(gridDim.x) * blockDim.x;
   const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  for (int64_t j = t; j < n; j += stride) {
-    const int p = __ldg(pos + j);
-    out[j] = p >= 0 ? __ldcg(val + p) : T(0);
+  for (int64_t j = t; j < n_ent; j += stride) {
+    const int p = __ldg(ent_src + j);
+    ent_val[j] = p >= 0 ? __ldcg(val + p) : T(0);
   }
-  for (int64_t g = t; g < n_rec; g += stride)
-    if ((rec[g].flags & 3) == 3) rec[g].rd = double(__ldcg((const T *)d.rdiag + d.tail0 + rec[g].col));
+  const int64_t n_tv = int64_t(n_blk) * kChainTileValues;
+  for (int64_t j = t; j < n_tv; j += stride) {
+    const int p = __ldg(tile_src + j);
+    const T v = p >= 0 ? __ldcg(val + p) : p == -1 ? T(0) : __ldcg((const T *)d.rdiag + (-2 - p));
+    T *tv = reinterpret_cast<T *>(tiles + size_t(j / kChainTileValues) * chain_tile_bytes(sizeof(T)));
+    tv[j % kChainTileValues] = v;
+  }
 }
 
 struct ChainDev {
-  const ChainRec *rec;  // n_seg records, padded to whole chunks
-  int n_seg;
-  const int *row;       // chain-local row of each entry (nt: scratch), padded to whole chunks
-  const void *val;      // T: each entry's value (lu_chain_gather)
-  int64_t n_ent;        // entries, padded to whole chunks
+  const int4 *blk;             // ChainBlock per block: forward, then backward
+  int n_blk;
+  const unsigned char *tiles;  // per block chain_tile_bytes: triangle, pivots (T), x positions
+  const int *ent_rowj;         // per entry (row << 5) | lane-column; whole chunks
+  const void *ent_val;         // T per entry
+  int64_t n_ent;               // entries, whole chunks
 };
 
 __device__ __forceinline__ unsigned smem_addr(const void *p) {
@@ -734,70 +735,66 @@ __device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity, int lim
     if (mbar_try(bar, parity)) return true;
   return false;
 }
-// One thread: `bytes` from global src to shared dst, counted on barrier mb.
+// One thread: `bytes` from global src to shared dst, counted on barrier mb
+// (whose transaction count the caller has raised by them).
 __device__ __forceinline__ void bulk_copy(void *dst, const void *src, unsigned bytes, unsigned mb) {
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                    smem_addr(dst)),
                "l"(src), "r"(bytes), "r"(mb)
                : "memory");
 }
+__device__ __forceinline__ void expect_bytes(unsigned mb, unsigned bytes) {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(bytes) : "memory");
+}
 
 template <class T>
 __global__ void __launch_bounds__(32) lu_solve_chain(LuDev d, ChainDev c, T *y, T *z, double *x) {
   extern __shared__ __align__(128) unsigned char chain_raw[];
-  constexpr int kE = kChainChunks * kChainEntChunk, kR = kChainChunks * kChainRecChunk;
+  constexpr int kE = kChainChunks * kChainEntChunk;
+  constexpr unsigned kTile = unsigned(chain_tile_bytes(sizeof(T)));
   const int lane = threadIdx.x, t0 = d.tail0, nt = d.n - t0;
-  // rings (entry rows, entry values, records), their barriers, then the
-  // running sums (nt + scratch)
-  int *ring_row = reinterpret_cast<int *>(chain_raw);
-  T *ring_val = reinterpret_cast<T *>(ring_row + kE);
-  ChainRec *ring_rec = reinterpret_cast<ChainRec *>(ring_val + kE);
-  unsigned long long *bar_e = reinterpret_cast<unsigned long long *>(ring_rec + kR);
-  unsigned long long *bar_r = bar_e + kChainChunks;
-  T *acc = reinterpret_cast<T *>(bar_r + kChainChunks);
+  // rings (tiles, entry rows, entry values), the block's values, barriers,
+  // then the running sums (nt + scratch)
+  unsigned char *ring_tile = chain_raw;
+  int *ring_rowj = reinterpret_cast<int *>(ring_tile + kChainTileRing * kTile);
+  T *ring_val = reinterpret_cast<T *>(ring_rowj + kE);
+  T *vb = ring_val + kE;
+  unsigned long long *bar_t = reinterpret_cast<unsigned long long *>(vb + kChainBlock);
+  unsigned long long *bar_e = bar_t + kChainTileRing;
+  T *acc = reinterpret_cast<T *>(bar_e + kChainChunks);
   const int limit = int(__ldg(&d.ctrl[C_SPIN]));
   const int n_ech = int(c.n_ent / kChainEntChunk);
-  const int n_rch = (c.n_seg + kChainRecChunk - 1) / kChainRecChunk;
-  const T *cval = (const T *)c.val;
+  const T *cval = (const T *)c.ent_val;
 
-  // lane 0 refills ring slot k % kChainChunks with entry / record chunk k
+  // lane 0 refills a ring slot with tile / entry chunk k
+  auto issue_tile = [&](int k) {
+    if (lane == 0 && k < c.n_blk) {
+      const unsigned mb = smem_addr(bar_t + k % kChainTileRing);
+      expect_bytes(mb, kTile);
+      bulk_copy(ring_tile + (k % kChainTileRing) * kTile, c.tiles + size_t(k) * kTile, kTile, mb);
+    }
+  };
   auto issue_ent = [&](int k) {
     if (lane == 0 && k < n_ech) {
       const int s = k % kChainChunks;
       const unsigned mb = smem_addr(bar_e + s);
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb),
-                   "r"(unsigned(kChainEntChunk * (sizeof(int) + sizeof(T))))
-                   : "memory");
-      bulk_copy(ring_row + s * kChainEntChunk, c.row + size_t(k) * kChainEntChunk,
+      expect_bytes(mb, unsigned(kChainEntChunk * (sizeof(int) + sizeof(T))));
+      bulk_copy(ring_rowj + s * kChainEntChunk, c.ent_rowj + size_t(k) * kChainEntChunk,
                 unsigned(kChainEntChunk * sizeof(int)), mb);
       bulk_copy(ring_val + s * kChainEntChunk, cval + size_t(k) * kChainEntChunk,
                 unsigned(kChainEntChunk * sizeof(T)), mb);
     }
   };
-  auto issue_rec = [&](int k) {
-    if (lane == 0 && k < n_rch) {
-      const int s = k % kChainChunks;
-      const unsigned mb = smem_addr(bar_r + s);
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb),
-                   "r"(unsigned(kChainRecChunk * sizeof(ChainRec)))
-                   : "memory");
-      bulk_copy(ring_rec + s * kChainRecChunk, c.rec + size_t(k) * kChainRecChunk,
-                unsigned(kChainRecChunk * sizeof(ChainRec)), mb);
-    }
-  };
 
   if (lane == 0) {
-    for (int i = 0; i < 2 * kChainChunks; ++i)
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar_e + i)) : "memory");
+    for (int i = 0; i < kChainTileRing + kChainChunks; ++i)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar_t + i)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncwarp();
-  for (int k = 0; k < kChainChunks; ++k) {
-    issue_rec(k);
-    issue_ent(k);
-  }
+  for (int k = 0; k < kChainTileRing; ++k) issue_tile(k);
+  for (int k = 0; k < kChainChunks; ++k) issue_ent(k);
   // the sums start from b(P(row)) minus the row's sum over columns < t0
   // (the grid lower solve's)
   const T *h = reinterpret_cast<const T *>(d.hpart);
@@ -806,81 +803,118 @@ __global__ void __launch_bounds__(32) lu_solve_chain(LuDev d, ChainDev c, T *y, 
   if (lane == 0) acc[nt] = T(0);
   __syncwarp();
 
-  T v = T(0);
-  int64_t off = 0;      // the segment's first entry in the stream
-  int ent_wait = 0;     // entry chunks waited for so far
-  int ent_free = 0;     // entry chunks passed (and refilled)
+  // block records: lane j holds block w + j's, and the next window's
+  int w = 0;
+  int4 ba = lane < c.n_blk ? c.blk[lane] : make_int4(0, 0, 0, 0);
+  int4 bb = 32 + lane < c.n_blk ? c.blk[32 + lane] : make_int4(0, 0, 0, 0);
   bool ok = true;
-  int g = 0;
-  for (; g < c.n_seg; ++g) {
-    if (g % kChainRecChunk == 0) {
-      const int k = g / kChainRecChunk;
-      if (!mbar_wait(smem_addr(bar_r + k % kChainChunks), unsigned(k / kChainChunks) & 1u, limit)) {
-        ok = false;
-        break;
+  int gk = 0;        // rounds done, all blocks
+  int ent_wait = 0;  // entry chunks waited for
+  int ent_free = 0;  // entry chunks passed (and refilled)
+  int blk = 0;
+  for (; blk < c.n_blk; ++blk) {
+    if (blk - w == 32) {
+      w += 32;
+      ba = bb;
+      bb = w + 32 + lane < c.n_blk ? c.blk[w + 32 + lane] : make_int4(0, 0, 0, 0);
+    }
+    const int cbase = __shfl_sync(0xffffffffu, ba.x, blk - w);
+    const int bs = __shfl_sync(0xffffffffu, ba.y, blk - w);
+    const int rounds = __shfl_sync(0xffffffffu, ba.z, blk - w);
+    const bool upper = __shfl_sync(0xffffffffu, ba.w, blk - w) != 0;
+    if (!mbar_wait(smem_addr(bar_t + blk % kChainTileRing), unsigned(blk / kChainTileRing) & 1u, limit)) {
+      ok = false;
+      break;
+    }
+    // the triangle: lane i is row i of the block
+    const T *tri = reinterpret_cast<const T *>(ring_tile + (blk % kChainTileRing) * kTile);
+    const int col = upper ? cbase - lane : cbase + lane;
+    T a = lane < bs ? acc[col] : T(0);
+    T row[kChainBlock];
+#pragma unroll
+    for (int j = 0; j < kChainBlock; ++j) row[j] = tri[j * kChainBlock + lane];
+    const T rdl = upper ? tri[kChainBlock * kChainBlock + lane] : T(1);
+    const int ql = reinterpret_cast<const int *>(tri + kChainTileValues)[lane];
+#pragma unroll
+    for (int t = 0; t < kChainBlock; ++t) {
+      if (t < bs) {
+        if (upper && lane == t) a *= rdl;
+        const T vt = __shfl_sync(0xffffffffu, a, t);
+        if (lane > t) a -= row[t] * vt;
       }
     }
-    const ChainRec rc = ring_rec[g % kR];
-    const int len = rc.len;
-    // the chunks this segment's entries lie in (at most two)
-    const int need = len > 0 ? int((off + len - 1) / kChainEntChunk) : ent_wait - 1;
-    while (ok && ent_wait <= need) {
-      ok = mbar_wait(smem_addr(bar_e + ent_wait % kChainChunks), unsigned(ent_wait / kChainChunks) & 1u, limit);
-      ++ent_wait;
-    }
-    if (!ok) break;
-    // the segment's rows and values before the column's value is needed;
-    // its rows are distinct (scratch padding aside), so every sum is read
-    // before any is written
-    int ri[kChainSeg / 32];
-    T wv[kChainSeg / 32];
-#pragma unroll
-    for (int r = 0; r < kChainSeg / 32; ++r) {
-      const int j = 32 * r + lane;
-      const int e = int((off + j) & (kE - 1));
-      ri[r] = j < len ? ring_row[e] : nt;
-      wv[r] = j < len ? ring_val[e] : T(0);
-    }
-    if (rc.flags & 1) {
-      // the column's value is final: every earlier column has been applied
-      v = acc[rc.col];
-      if (rc.flags & 2) {
-        v *= T(rc.rd);
-        if (lane == 0) {
-          z[t0 + rc.col] = v;
-          x[rc.q] = double(v);
-        }
-      } else if (lane == 0) {
-        y[t0 + rc.col] = v;
+    if (lane < bs) {
+      if (upper) {
+        z[t0 + col] = a;
+        x[ql] = double(a);
+      } else {
+        y[t0 + col] = a;
+        acc[col] = a;
       }
     }
-    T av[kChainSeg / 32];
-#pragma unroll
-    for (int r = 0; r < kChainSeg / 32; ++r) av[r] = acc[ri[r]];
-#pragma unroll
-    for (int r = 0; r < kChainSeg / 32; ++r) av[r] -= wv[r] * v;
-#pragma unroll
-    for (int r = 0; r < kChainSeg / 32; ++r)
-      if (32 * r + lane < len) acc[ri[r]] = av[r];
+    vb[lane] = a;
     __syncwarp();
-    // refill the chunks the warp has passed
-    off += len;
-    while (ent_free < int(off / kChainEntChunk)) {
-      issue_ent(ent_free + kChainChunks);
-      ++ent_free;
+    issue_tile(blk + kChainTileRing);
+    // the block's entries in rows outside it, four rounds at a time with
+    // their loads first (each lane's multiply-adds depend on one another)
+    int cur = -1;
+    T ar = T(0);
+    for (int k0 = 0; k0 < rounds; k0 += 4) {
+      const int nq = min(4, rounds - k0);
+      const int need = (gk + nq - 1) / 8;
+      while (ok && ent_wait <= need) {
+        ok = mbar_wait(smem_addr(bar_e + ent_wait % kChainChunks), unsigned(ent_wait / kChainChunks) & 1u, limit);
+        ++ent_wait;
+      }
+      if (!ok) break;
+      int rj[4];
+      T wv[4], vv[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        rj[q] = nt << 5;
+        wv[q] = T(0);
+        if (q < nq) {
+          const int e = ((gk + q) * kChainBlock + lane) & (kE - 1);
+          rj[q] = ring_rowj[e];
+          wv[q] = ring_val[e];
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) vv[q] = vb[rj[q] & 31];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        if (q < nq) {
+          const int r = rj[q] >> 5;
+          if (r != cur) {
+            if (cur >= 0) acc[cur] = ar;
+            ar = acc[r];
+            cur = r;
+          }
+          ar -= wv[q] * vv[q];
+        }
+      }
+      gk += nq;
+      // refill the chunks these rounds finished
+      if (ent_free < gk / 8) {
+        __syncwarp();
+        while (ent_free < gk / 8) {
+          issue_ent(ent_free + kChainChunks);
+          ++ent_free;
+        }
+      }
     }
-    if ((g + 1) % kChainRecChunk == 0) issue_rec(g / kChainRecChunk + kChainChunks);
+    if (cur >= 0) acc[cur] = ar;
+    __syncwarp();
+    if (!ok) break;
   }
   if (!ok) {
     // a copy that did not complete in time: report it, and let the copies
     // still in flight land before the block's shared memory is released
     if (lane == 0) atomicOr(&d.ctrl[C_STATUS], ST_TIMEOUT);
-    const int e_end = min(n_ech, ent_free + kChainChunks);
-    for (int k = max(ent_wait - 1, 0); k < e_end; ++k)
+    for (int k = blk; k < min(c.n_blk, blk + kChainTileRing + 1); ++k)
+      mbar_wait(smem_addr(bar_t + k % kChainTileRing), unsigned(k / kChainTileRing) & 1u, 1 << 22);
+    for (int k = max(ent_wait - 1, 0); k < min(n_ech, ent_free + kChainChunks); ++k)
       mbar_wait(smem_addr(bar_e + k % kChainChunks), unsigned(k / kChainChunks) & 1u, 1 << 22);
-    const int r_end = min(n_rch, g / kChainRecChunk + kChainChunks);
-    for (int k = g / kChainRecChunk; k < r_end; ++k)
-      mbar_wait(smem_addr(bar_r + k % kChainChunks), unsigned(k / kChainChunks) & 1u, 1 << 22);
   }
 }
 
@@ -1576,26 +1610,26 @@ __global__ void __launch_bounds__(1024) lu_factor_solve_lvl(LuDev d, LvlDev v,
   lvl_solve<T>(d, v, m, x);
 }
 
-// Shared memory of lu_solve_chain: the entry and record rings, their
-// barriers, and the running sums of nt rows plus the scratch row.
+// Shared memory of lu_solve_chain: the tile and entry rings, the block's
+// values, the barriers, and the running sums of nt rows plus the scratch row.
 size_t chain_smem_bytes(int nt, size_t tsz) {
-  return size_t(kChainChunks) * kChainEntChunk * (sizeof(int) + tsz) +
-         size_t(kChainChunks) * kChainRecChunk * sizeof(ChainRec) + 2 * size_t(kChainChunks) * 8 +
-         size_t(nt + 1) * tsz;
+  return size_t(kChainTileRing) * chain_tile_bytes(tsz) + size_t(kChainChunks) * kChainEntChunk * (sizeof(int) + tsz) +
+         kChainBlock * tsz + size_t(kChainTileRing + kChainChunks) * 8 + size_t(nt + 1) * tsz;
 }
 
 // Where the grid solves hand the trailing rows to the one-warp chain.  A
-// level of the grid solves costs an L2 round trip and a publish (~2.5 us
-// over both solves' waits, measured); in the chain a column costs its
-// barrier, its value and a warp step (~0.15 us per solve) and an entry
-// ~1.5 ns (a multiply-add in shared memory, 32 at a time).  Candidates are
-// the last 256, 512, ... rows, as many as shared memory holds the running
-// sums of; the tail that saves the most modelled time over both solves wins,
-// none when nothing is saved.
-constexpr double kGridLevelSeconds = 2.5e-6;
-constexpr double kChainColSeconds = 0.15e-6;
-constexpr double kChainEntrySeconds = 1.5e-9;
-constexpr size_t kChainSmem = 220 * 1024;
+// level of the grid solves costs L2 round trips and a publish (~2.2 us per
+// solve, measured on random logic); in the chain a column costs a step of
+// its block's triangle (~0.075 us per solve: a shuffle and an FP64
+// multiply-add, which one warp issues at 64 cycles) and an entry ~3 ns (its
+// round's share: 32 lanes, each a multiply-add on its row's sum).
+// Candidates are the last 256, 512, ... rows, as many as shared memory
+// holds the running sums of; the tail that saves the most modelled time over
+// both solves wins, none when nothing is saved.
+constexpr double kGridLevelSeconds = 2.2e-6;
+constexpr double kChainColSeconds = 0.075e-6;
+constexpr double kChainEntrySeconds = 3e-9;
+constexpr size_t kChainSmem = 226 * 1024;
 
 int chain_start(const LuSymbolic &S, size_t tsz) {
   const int n = S.n;
@@ -1664,10 +1698,12 @@ struct xg_lu {
   int solve_tail0 = 0;                     // grid solves: first row of the one-warp chain (n: none)
   int4 *d_tdesc = nullptr;                 // its row descriptors
   void *d_hpart = nullptr;                 // its rows' sums over earlier columns (T)
-  xg::ChainRec *d_chain_rec = nullptr;     // its segments' records (whole chunks)
-  int *d_chain_row = nullptr, *d_chain_pos = nullptr;  // per entry: chain row, position in val
+  int4 *d_chain_blk = nullptr;             // its blocks (ChainBlock)
+  unsigned char *d_chain_tiles = nullptr;  // per block: triangle and pivots (T, per refactor), x positions
+  int *d_chain_tsrc = nullptr;             // per tile value: its source (ChainPlan::tile_src)
+  int *d_chain_rowj = nullptr, *d_chain_esrc = nullptr;  // per entry: row and lane-column, value source
   void *d_chain_val = nullptr;             // per entry: value (T), gathered per refactor
-  int n_chain_seg = 0, n_chain_rec = 0;
+  int n_chain_blk = 0;
   int64_t n_chain_ent = 0;                 // entries, whole chunks
   size_t smem_chain = 0;                   // its y and z in shared memory
   unsigned char *d_solo = nullptr;         // grid solves: rows lu_solve_long sums (LuDev::solo)
@@ -1712,8 +1748,8 @@ int upload(V **dst, const std::vector<V> &src) {
 void free_lu(xg_lu *lu) {
   void *ptrs[] = {lu->d_rp, lu->d_ci, lu->d_diag, lu->d_lu2a, lu->d_P, lu->d_Q, lu->d_arp,
                   lu->d_urp, lu->d_upos, lu->d_lvl,
-                  lu->d_aci, lu->d_ctrl, lu->d_tdesc, lu->d_hpart, lu->d_solo, lu->d_long, lu->d_pending, lu->d_chain_rec, lu->d_chain_row, lu->d_chain_pos,
-                  lu->d_chain_val, lu->d_val, lu->d_y, lu->d_z, lu->d_rdiag, lu->d_a,
+                  lu->d_aci, lu->d_ctrl, lu->d_tdesc, lu->d_hpart, lu->d_solo, lu->d_long, lu->d_pending, lu->d_chain_blk, lu->d_chain_tiles, lu->d_chain_tsrc,
+                  lu->d_chain_rowj, lu->d_chain_esrc, lu->d_chain_val, lu->d_val, lu->d_y, lu->d_z, lu->d_rdiag, lu->d_a,
                   lu->d_r, lu->d_dx, lu->d_hv, lu->d_hb, lu->d_hx};
   for (void *p : ptrs)
     if (p) cudaFree(p);
@@ -1745,11 +1781,11 @@ int refactor_t(xg_lu *lu, const double *dev_values) {
       d, dev_values, lu->d_a, lu->S.nnz_a, (T *)lu->d_val, lu->nnz_lu, lu->d_pending); xg::count_launches(1);
   xg::lu_factor<T><<<lu->grid_factor, 32 * xg::kFactorWarps, lu->smem_grid, lu->stream>>>(
       d, (T *)lu->d_val, lu->d_a, lu->stage_cap); xg::count_launches(1);
-  if (lu->n_chain_ent) {
+  if (lu->n_chain_blk) {
     const int blocks = int(std::min<int64_t>(1024, (lu->n_chain_ent + 255) / 256));
-    xg::lu_chain_gather<T><<<blocks, 256, 0, lu->stream>>>(d, (const T *)lu->d_val, lu->d_chain_pos,
-                                                          (T *)lu->d_chain_val, lu->n_chain_ent,
-                                                          lu->d_chain_rec, lu->n_chain_rec);
+    xg::lu_chain_gather<T><<<blocks, 256, 0, lu->stream>>>(d, (const T *)lu->d_val, lu->d_chain_esrc,
+                                                          (T *)lu->d_chain_val, lu->n_chain_ent, lu->d_chain_tsrc,
+                                                          lu->d_chain_tiles, lu->n_chain_blk);
     xg::count_launches(1);
   }
   XG_CU(cudaGetLastError());
@@ -1788,7 +1824,8 @@ int solve_once(xg_lu *lu, const double *b, double *x) {
     xg::count_launches(1);
   }
   if (lu->solve_tail0 < lu->S.n) {
-    const xg::ChainDev c{lu->d_chain_rec, lu->n_chain_seg, lu->d_chain_row, lu->d_chain_val, lu->n_chain_ent};
+    const xg::ChainDev c{lu->d_chain_blk, lu->n_chain_blk, lu->d_chain_tiles, lu->d_chain_rowj,
+                         lu->d_chain_val, lu->n_chain_ent};
     xg::lu_solve_chain<T><<<1, 32, lu->smem_chain, lu->stream>>>(d, c, (T *)lu->d_y, (T *)lu->d_z, x);
     xg::count_launches(1);
   }
@@ -1992,54 +2029,31 @@ extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const i
         desc[r - t0] = make_int4(S.rp[r], S.rp[r] + int(std::lower_bound(c0, c1, t0) - c0), S.diag[r],
                                  S.P[r]);
       }
-      // the chain's segments: the lower solve's columns ascending (L entries
-      // of chain rows below each), then the upper solve's descending (U
-      // entries of chain rows above each), each column in pieces of at most
-      // kChainSeg entries padded to a multiple of 4 with the scratch row nt
-      std::vector<std::vector<std::pair<int, int>>> lcol(nt), ucol(nt);
-      for (int r = t0; r < n; ++r) {
-        for (int p = desc[r - t0].y; p < S.diag[r]; ++p) lcol[S.ci[p] - t0].push_back({r - t0, p});
-        for (int p = S.diag[r] + 1; p < S.rp[r + 1]; ++p) ucol[S.ci[p] - t0].push_back({r - t0, p});
+      // the blocked chain's plan: block records, tiles (value sources and x
+      // positions) and rounds (rows and value sources), the entries padded
+      // to whole chunks
+      xg::ChainPlan plan = xg::build_chain_plan(S, t0);
+      while (plan.ent_rowj.size() % xg::kChainEntChunk) {
+        plan.ent_rowj.push_back(nt << 5);
+        plan.ent_src.push_back(-1);
       }
-      std::vector<xg::ChainRec> rec;
-      std::vector<int> crow, cpos;
-      auto add_column = [&](int col, const std::vector<std::pair<int, int>> &ent, int upper) {
-        size_t j = 0;
-        bool first = true;
-        do {
-          const size_t m = std::min(ent.size() - j, size_t(xg::kChainSeg));
-          const size_t off = crow.size();
-          for (size_t q = 0; q < m; ++q) {
-            crow.push_back(ent[j + q].first);
-            cpos.push_back(ent[j + q].second);
-          }
-          while (crow.size() % 4) {
-            crow.push_back(nt);
-            cpos.push_back(-1);
-          }
-          rec.push_back(xg::ChainRec{col, int(crow.size() - off), (first ? 1 : 0) | (upper ? 2 : 0),
-                                     S.Q[t0 + col], 0.0, 0.0});
-          first = false;
-          j += m;
-        } while (j < ent.size());
-      };
-      for (int col = 0; col < nt; ++col) add_column(col, lcol[col], 0);
-      for (int col = nt - 1; col >= 0; --col) add_column(col, ucol[col], 1);
-      lu->n_chain_seg = int(rec.size());
-      // both streams in whole chunks
-      while (crow.size() % xg::kChainEntChunk) {
-        crow.push_back(nt);
-        cpos.push_back(-1);
-      }
-      while (rec.size() % xg::kChainRecChunk) rec.push_back(xg::ChainRec{0, 0, 0, 0, 0.0, 0.0});
-      lu->n_chain_rec = int(rec.size());
-      lu->n_chain_ent = int64_t(crow.size());
+      lu->n_chain_blk = int(plan.blocks.size());
+      lu->n_chain_ent = int64_t(plan.ent_rowj.size());
+      const size_t tb = xg::chain_tile_bytes(tsz);
+      std::vector<unsigned char> tiles(plan.blocks.size() * tb, 0);
+      for (size_t k = 0; k < plan.blocks.size(); ++k)
+        std::memcpy(tiles.data() + k * tb + xg::kChainTileValues * tsz, plan.tile_q.data() + k * xg::kChainBlock,
+                    xg::kChainBlock * sizeof(int));
       lu->smem_chain = xg::chain_smem_bytes(nt, tsz);
       const void *fn = precision == XG_LU_FP32 ? (const void *)xg::lu_solve_chain<float>
                                                : (const void *)xg::lu_solve_chain<double>;
-      if ((rc = upload(&lu->d_tdesc, desc)) || (rc = upload(&lu->d_chain_rec, rec)) ||
-          (rc = upload(&lu->d_chain_row, crow)) || (rc = upload(&lu->d_chain_pos, cpos)) ||
-          (e = cudaMalloc(&lu->d_chain_val, std::max<size_t>(crow.size(), 1) * tsz)) ||
+      std::vector<int4> blk(plan.blocks.size());
+      for (size_t k = 0; k < blk.size(); ++k)
+        blk[k] = make_int4(plan.blocks[k].cbase, plan.blocks[k].bs, plan.blocks[k].rounds, plan.blocks[k].upper);
+      if ((rc = upload(&lu->d_tdesc, desc)) || (rc = upload(&lu->d_chain_blk, blk)) ||
+          (rc = upload(&lu->d_chain_tiles, tiles)) || (rc = upload(&lu->d_chain_tsrc, plan.tile_src)) ||
+          (rc = upload(&lu->d_chain_rowj, plan.ent_rowj)) || (rc = upload(&lu->d_chain_esrc, plan.ent_src)) ||
+          (e = cudaMalloc(&lu->d_chain_val, std::max<size_t>(plan.ent_rowj.size(), 1) * tsz)) ||
           (e = cudaMalloc(&lu->d_hpart, size_t(nt) * tsz)) ||
           (e = xg::allow_dynamic_smem((const void *)fn, lu->smem_chain))) {
         free_lu(lu.get());
