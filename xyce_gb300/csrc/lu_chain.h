@@ -8,10 +8,11 @@
 //    column-major (tile value j * 32 + i: lane-row i, lane-column j), then
 //    the 32 reciprocal pivots (backward solve) and the 32 x positions;
 //  * its rounds: the block's entries in rows outside it (below it forward,
-//    above it backward), each row given to one lane (longest rows first, to
-//    the least loaded lane), a lane's rows one after another and each row's
-//    entries in the solve's column order; round k holds every lane's k-th
-//    entry (the scratch row nt, value 0, where a lane has run out).
+//    above it backward), each row given to one of kChainLanes threads
+//    (longest rows first, to the least loaded), a thread's rows one after
+//    another and each row's entries in the solve's column order; round k
+//    holds every thread's k-th entry (the scratch row nt, value 0, where a
+//    thread has run out).
 // A row's running sum so takes its updates in the column order of a
 // column-by-column solve, the same on every run.
 #pragma once
@@ -23,6 +24,7 @@
 namespace xg {
 
 constexpr int kChainBlock = 32;
+constexpr int kChainLanes = 128;  // threads sharing a block's rounds
 constexpr int kChainTileValues = kChainBlock * kChainBlock + kChainBlock;  // triangle, reciprocal pivots
 
 struct ChainBlock {
@@ -39,8 +41,8 @@ struct ChainPlan {
   // values, -1 zero, <= -2 the reciprocal pivot of row -2 - src
   std::vector<int> tile_src;
   std::vector<int> tile_q;         // per block 32 x positions (backward), 0 otherwise
-  // per entry (32 per round): (chain-local row << 5) | lane-column, and the
-  // position of its value (-1: padding)
+  // per entry (kChainLanes per round): (chain-local row << 5) |
+  // lane-column, and the position of its value (-1: padding)
   std::vector<int> ent_rowj, ent_src;
 };
 
@@ -97,11 +99,11 @@ inline ChainPlan build_chain_plan(const LuSymbolic &S, int t0) {
     for (size_t k = 0; k < order.size(); ++k) order[k] = int(k);
     std::stable_sort(order.begin(), order.end(),
                      [&](int a, int c) { return ents[a].size() > ents[c].size(); });
-    std::vector<std::vector<int>> lane_rows(kChainBlock);
-    std::vector<size_t> load(kChainBlock, 0);
+    std::vector<std::vector<int>> lane_rows(kChainLanes);
+    std::vector<size_t> load(kChainLanes, 0);
     for (int k : order) {
       int best = 0;
-      for (int l = 1; l < kChainBlock; ++l)
+      for (int l = 1; l < kChainLanes; ++l)
         if (load[l] < load[best]) best = l;
       lane_rows[best].push_back(k);
       load[best] += ents[k].size();
@@ -109,14 +111,14 @@ inline ChainPlan build_chain_plan(const LuSymbolic &S, int t0) {
     size_t rounds = 0;
     for (size_t l : load) rounds = std::max(rounds, l);
     const size_t e0 = P.ent_rowj.size();
-    P.ent_rowj.resize(e0 + rounds * kChainBlock, nt << 5);
-    P.ent_src.resize(e0 + rounds * kChainBlock, -1);
-    for (int l = 0; l < kChainBlock; ++l) {
+    P.ent_rowj.resize(e0 + rounds * kChainLanes, nt << 5);
+    P.ent_src.resize(e0 + rounds * kChainLanes, -1);
+    for (int l = 0; l < kChainLanes; ++l) {
       size_t k = 0;
       for (int ri : lane_rows[l])
         for (const auto &e : ents[ri]) {
-          P.ent_rowj[e0 + k * kChainBlock + l] = (rows[ri] << 5) | e.first;
-          P.ent_src[e0 + k * kChainBlock + l] = e.second;
+          P.ent_rowj[e0 + k * kChainLanes + l] = (rows[ri] << 5) | e.first;
+          P.ent_src[e0 + k * kChainLanes + l] = e.second;
           ++k;
         }
     }

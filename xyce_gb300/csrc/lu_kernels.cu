@@ -749,11 +749,13 @@ __device__ __forceinline__ void expect_bytes(unsigned mb, unsigned bytes) {
 }
 
 template <class T>
-__global__ void __launch_bounds__(32) lu_solve_chain(LuDev d, ChainDev c, T *y, T *z, double *x) {
+__global__ void __launch_bounds__(kChainLanes) lu_solve_chain(LuDev d, ChainDev c, T *y, T *z, double *x) {
   extern __shared__ __align__(128) unsigned char chain_raw[];
   constexpr int kE = kChainChunks * kChainEntChunk;
+  constexpr int kRoundsPerChunk = kChainEntChunk / kChainLanes;
   constexpr unsigned kTile = unsigned(chain_tile_bytes(sizeof(T)));
-  const int lane = threadIdx.x, t0 = d.tail0, nt = d.n - t0;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int t0 = d.tail0, nt = d.n - t0;
   // rings (tiles, entry rows, entry values), the block's values, barriers,
   // then the running sums (nt + scratch)
   unsigned char *ring_tile = chain_raw;
@@ -767,16 +769,16 @@ __global__ void __launch_bounds__(32) lu_solve_chain(LuDev d, ChainDev c, T *y, 
   const int n_ech = int(c.n_ent / kChainEntChunk);
   const T *cval = (const T *)c.ent_val;
 
-  // lane 0 refills a ring slot with tile / entry chunk k
+  // thread 0 refills a ring slot with tile / entry chunk k
   auto issue_tile = [&](int k) {
-    if (lane == 0 && k < c.n_blk) {
+    if (tid == 0 && k < c.n_blk) {
       const unsigned mb = smem_addr(bar_t + k % kChainTileRing);
       expect_bytes(mb, kTile);
       bulk_copy(ring_tile + (k % kChainTileRing) * kTile, c.tiles + size_t(k) * kTile, kTile, mb);
     }
   };
   auto issue_ent = [&](int k) {
-    if (lane == 0 && k < n_ech) {
+    if (tid == 0 && k < n_ech) {
       const int s = k % kChainChunks;
       const unsigned mb = smem_addr(bar_e + s);
       expect_bytes(mb, unsigned(kChainEntChunk * (sizeof(int) + sizeof(T))));
@@ -787,27 +789,28 @@ __global__ void __launch_bounds__(32) lu_solve_chain(LuDev d, ChainDev c, T *y, 
     }
   };
 
-  if (lane == 0) {
+  if (tid == 0) {
     for (int i = 0; i < kChainTileRing + kChainChunks; ++i)
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar_t + i)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  __syncwarp();
+  __syncthreads();
   for (int k = 0; k < kChainTileRing; ++k) issue_tile(k);
   for (int k = 0; k < kChainChunks; ++k) issue_ent(k);
   // the sums start from b(P(row)) minus the row's sum over columns < t0
   // (the grid lower solve's)
   const T *h = reinterpret_cast<const T *>(d.hpart);
 #pragma unroll 8
-  for (int r = lane; r < nt; r += 32) acc[r] = __ldcg(h + r);
-  if (lane == 0) acc[nt] = T(0);
-  __syncwarp();
+  for (int r = tid; r < nt; r += kChainLanes) acc[r] = __ldcg(h + r);
+  if (tid == 0) acc[nt] = T(0);
+  __syncthreads();
 
-  // block records: lane j holds block w + j's, and the next window's
+  // block records: lane j of every warp holds block w + j's, and the next
+  // window's
   int w = 0;
   int4 ba = lane < c.n_blk ? c.blk[lane] : make_int4(0, 0, 0, 0);
   int4 bb = 32 + lane < c.n_blk ? c.blk[32 + lane] : make_int4(0, 0, 0, 0);
-  bool ok = true;
+  bool ok = true;    // the same in every thread: each decision is a block vote
   int gk = 0;        // rounds done, all blocks
   int ent_wait = 0;  // entry chunks waited for
   int ent_free = 0;  // entry chunks passed (and refilled)
@@ -822,51 +825,60 @@ __global__ void __launch_bounds__(32) lu_solve_chain(LuDev d, ChainDev c, T *y, 
     const int bs = __shfl_sync(0xffffffffu, ba.y, blk - w);
     const int rounds = __shfl_sync(0xffffffffu, ba.z, blk - w);
     const bool upper = __shfl_sync(0xffffffffu, ba.w, blk - w) != 0;
-    if (!mbar_wait(smem_addr(bar_t + blk % kChainTileRing), unsigned(blk / kChainTileRing) & 1u, limit)) {
+    // the triangle (warp 0): lane i is row i of the block
+    bool fail = false;
+    if (warp == 0) {
+      fail = !mbar_wait(smem_addr(bar_t + blk % kChainTileRing), unsigned(blk / kChainTileRing) & 1u, limit);
+      if (!__any_sync(0xffffffffu, fail)) {
+        const T *tri = reinterpret_cast<const T *>(ring_tile + (blk % kChainTileRing) * kTile);
+        const int col = upper ? cbase - lane : cbase + lane;
+        T a = lane < bs ? acc[col] : T(0);
+        T row[kChainBlock];
+#pragma unroll
+        for (int j = 0; j < kChainBlock; ++j) row[j] = tri[j * kChainBlock + lane];
+        const T rdl = upper ? tri[kChainBlock * kChainBlock + lane] : T(1);
+        const int ql = reinterpret_cast<const int *>(tri + kChainTileValues)[lane];
+#pragma unroll
+        for (int t = 0; t < kChainBlock; ++t) {
+          if (t < bs) {
+            if (upper && lane == t) a *= rdl;
+            const T vt = __shfl_sync(0xffffffffu, a, t);
+            if (lane > t) a -= row[t] * vt;
+          }
+        }
+        if (lane < bs) {
+          if (upper) {
+            z[t0 + col] = a;
+            x[ql] = double(a);
+          } else {
+            y[t0 + col] = a;
+            acc[col] = a;
+          }
+        }
+        vb[lane] = a;
+      }
+    }
+    if (__syncthreads_or(fail)) {
       ok = false;
       break;
     }
-    // the triangle: lane i is row i of the block
-    const T *tri = reinterpret_cast<const T *>(ring_tile + (blk % kChainTileRing) * kTile);
-    const int col = upper ? cbase - lane : cbase + lane;
-    T a = lane < bs ? acc[col] : T(0);
-    T row[kChainBlock];
-#pragma unroll
-    for (int j = 0; j < kChainBlock; ++j) row[j] = tri[j * kChainBlock + lane];
-    const T rdl = upper ? tri[kChainBlock * kChainBlock + lane] : T(1);
-    const int ql = reinterpret_cast<const int *>(tri + kChainTileValues)[lane];
-#pragma unroll
-    for (int t = 0; t < kChainBlock; ++t) {
-      if (t < bs) {
-        if (upper && lane == t) a *= rdl;
-        const T vt = __shfl_sync(0xffffffffu, a, t);
-        if (lane > t) a -= row[t] * vt;
-      }
-    }
-    if (lane < bs) {
-      if (upper) {
-        z[t0 + col] = a;
-        x[ql] = double(a);
-      } else {
-        y[t0 + col] = a;
-        acc[col] = a;
-      }
-    }
-    vb[lane] = a;
-    __syncwarp();
     issue_tile(blk + kChainTileRing);
     // the block's entries in rows outside it, four rounds at a time with
-    // their loads first (each lane's multiply-adds depend on one another)
+    // their loads first (each thread's multiply-adds depend on one another)
     int cur = -1;
     T ar = T(0);
     for (int k0 = 0; k0 < rounds; k0 += 4) {
       const int nq = min(4, rounds - k0);
-      const int need = (gk + nq - 1) / 8;
-      while (ok && ent_wait <= need) {
-        ok = mbar_wait(smem_addr(bar_e + ent_wait % kChainChunks), unsigned(ent_wait / kChainChunks) & 1u, limit);
+      const int need = (gk + nq - 1) / kRoundsPerChunk;
+      bool bad = false;
+      while (!bad && ent_wait <= need) {
+        bad = !mbar_wait(smem_addr(bar_e + ent_wait % kChainChunks), unsigned(ent_wait / kChainChunks) & 1u, limit);
         ++ent_wait;
       }
-      if (!ok) break;
+      if (__syncthreads_or(bad)) {
+        ok = false;
+        break;
+      }
       int rj[4];
       T wv[4], vv[4];
 #pragma unroll
@@ -874,7 +886,7 @@ __global__ void __launch_bounds__(32) lu_solve_chain(LuDev d, ChainDev c, T *y, 
         rj[q] = nt << 5;
         wv[q] = T(0);
         if (q < nq) {
-          const int e = ((gk + q) * kChainBlock + lane) & (kE - 1);
+          const int e = ((gk + q) * kChainLanes + tid) & (kE - 1);
           rj[q] = ring_rowj[e];
           wv[q] = ring_val[e];
         }
@@ -894,27 +906,30 @@ __global__ void __launch_bounds__(32) lu_solve_chain(LuDev d, ChainDev c, T *y, 
         }
       }
       gk += nq;
-      // refill the chunks these rounds finished
-      if (ent_free < gk / 8) {
-        __syncwarp();
-        while (ent_free < gk / 8) {
+      // refill the chunks these rounds finished (every thread past them)
+      if (ent_free < gk / kRoundsPerChunk) {
+        __syncthreads();
+        while (ent_free < gk / kRoundsPerChunk) {
           issue_ent(ent_free + kChainChunks);
           ++ent_free;
         }
       }
     }
     if (cur >= 0) acc[cur] = ar;
-    __syncwarp();
+    __syncthreads();
     if (!ok) break;
   }
   if (!ok) {
     // a copy that did not complete in time: report it, and let the copies
     // still in flight land before the block's shared memory is released
-    if (lane == 0) atomicOr(&d.ctrl[C_STATUS], ST_TIMEOUT);
-    for (int k = blk; k < min(c.n_blk, blk + kChainTileRing + 1); ++k)
-      mbar_wait(smem_addr(bar_t + k % kChainTileRing), unsigned(k / kChainTileRing) & 1u, 1 << 22);
-    for (int k = max(ent_wait - 1, 0); k < min(n_ech, ent_free + kChainChunks); ++k)
-      mbar_wait(smem_addr(bar_e + k % kChainChunks), unsigned(k / kChainChunks) & 1u, 1 << 22);
+    if (tid == 0) {
+      atomicOr(&d.ctrl[C_STATUS], ST_TIMEOUT);
+      for (int k = blk; k < min(c.n_blk, blk + kChainTileRing + 1); ++k)
+        mbar_wait(smem_addr(bar_t + k % kChainTileRing), unsigned(k / kChainTileRing) & 1u, 1 << 22);
+      for (int k = max(ent_wait - 1, 0); k < min(n_ech, ent_free + kChainChunks); ++k)
+        mbar_wait(smem_addr(bar_e + k % kChainChunks), unsigned(k / kChainChunks) & 1u, 1 << 22);
+    }
+    __syncthreads();
   }
 }
 
@@ -1826,7 +1841,8 @@ int solve_once(xg_lu *lu, const double *b, double *x) {
   if (lu->solve_tail0 < lu->S.n) {
     const xg::ChainDev c{lu->d_chain_blk, lu->n_chain_blk, lu->d_chain_tiles, lu->d_chain_rowj,
                          lu->d_chain_val, lu->n_chain_ent};
-    xg::lu_solve_chain<T><<<1, 32, lu->smem_chain, lu->stream>>>(d, c, (T *)lu->d_y, (T *)lu->d_z, x);
+    xg::lu_solve_chain<T><<<1, xg::kChainLanes, lu->smem_chain, lu->stream>>>(d, c, (T *)lu->d_y, (T *)lu->d_z,
+                                                                              x);
     xg::count_launches(1);
   }
   xg::lu_usolve<T><<<lu->grid_tri, 256, 0, lu->stream>>>(d, (const T *)lu->d_val, (const T *)lu->d_y,
