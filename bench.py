@@ -283,6 +283,7 @@ def run_tran(args, world, rank, local, dist, emit=True):
         "data": "synthetic (seeded netlist, the reference's benchmark circuit shape)",
         "config": workload_config(args.workload),
         "details": {"unknowns": c.n_unknowns, "nnz": c.nnz, "nnz_lu": info.nnz_lu, "lu_levels": info.levels,
+                   "lu_chain_rows": info.solve_chain,
                    "lu_precision": f"fp32+{nref} fp64 refinement" if args.fp32 else "fp64",
                    "lu_order": "nested dissection" if info.ordering == 1 else "minimum degree",
                    "lu_analysis": "done by the first (warm-up) run of the circuit, reused by the "
