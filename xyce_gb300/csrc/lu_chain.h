@@ -16,7 +16,9 @@
 // A row's running sum so takes its updates in the column order of a
 // column-by-column solve, the same on every run.
 #pragma once
+#include <algorithm>
 #include <cstdint>
+#include <utility>
 #include <vector>
 
 #include "xg_lu.h"
