@@ -134,27 +134,6 @@ __device__ __forceinline__ unsigned long long to_bits(double v) {
 }
 __device__ __forceinline__ unsigned to_bits(float v) { return __float_as_uint(v); }
 
-// The value at p once it is no longer pending; zero (and the timeout bit) if
-// it never arrives.
-template <class T>
-__device__ T wait_value(const T *p, unsigned *ctrl) {
-  using U = typename Pending<T>::U;
-  const U *q = reinterpret_cast<const U *>(p);
-  int it = 0;
-  const int limit = int(__ldg(&ctrl[C_SPIN]));
-  U v;
-  while ((v = ld_relaxed(q)) == Pending<T>::bits) {
-    ++it;
-    if (it > limit ||
-        ((it & 1023) == 0 && (*(volatile unsigned *)&ctrl[C_STATUS] & ST_TIMEOUT))) {
-      atomicOr(&ctrl[C_STATUS], ST_TIMEOUT);
-      return T(0);
-    }
-    if (it > 32) __nanosleep(64);
-  }
-  return from_bits(v);
-}
-
 template <class T>
 __device__ __forceinline__ void publish(T *p, T v) {
   st_relaxed(reinterpret_cast<typename Pending<T>::U *>(p), to_bits(v));
@@ -171,8 +150,9 @@ __device__ __forceinline__ void st_rel(unsigned long long *p, unsigned long long
 }
 __device__ __forceinline__ void st_rel(unsigned *p, unsigned v) { st_release(p, v); }
 
-// wait_value with acquire: what the writer stored before its release is
-// visible after it.
+// The value at p once it is no longer pending, polled with acquire: what the
+// writer stored before its release is visible after it.  Zero (and the
+// timeout bit) if it never arrives.
 template <class T>
 __device__ T wait_value_acquire(const T *p, unsigned *ctrl) {
   using U = typename Pending<T>::U;
@@ -365,9 +345,13 @@ __device__ __forceinline__ void pivot_apply(const LuDev &d, const T *val, T *rb,
   const T l = rb[p - ro] * rk;
   __syncwarp();
   if (lane == 0) rb[p - ro] = l;
+  // a step no lane has is skipped by the warp (m.len is the same in every
+  // lane): an FP64 instruction costs its issue slot however few lanes it has
 #pragma unroll
-  for (int r = 0; r < kU; ++r)
+  for (int r = 0; r < kU; ++r) {
+    if (32 * r >= m.len) break;
     if (c.q[r] >= 0) rb[c.q[r] - ro] -= l * from_bits(c.v[r]);
+  }
   for (int j0 = 32 * kU; j0 < m.len; j0 += 32 * kU) {
     PivotChunk<T> e;
     pivot_fetch(d, val, m, up, j0, lane, e);
@@ -381,8 +365,10 @@ __device__ __forceinline__ void pivot_apply(const LuDev &d, const T *val, T *rb,
       }
     }
 #pragma unroll
-    for (int r = 0; r < kU; ++r)
+    for (int r = 0; r < kU; ++r) {
+      if (j0 + 32 * r >= m.len) break;
       if (e.q[r] >= 0) rb[e.q[r] - ro] -= l * from_bits(e.v[r]);
+    }
   }
 }
 
