@@ -465,9 +465,8 @@ int xg_mem_info(xg_ctx *ctx, int64_t *free_bytes, int64_t *total_bytes);
  *     and store are written in the circuit as xg_load writes them.
  *   - The first call on a device looks the array's device address up
  *     (cudaGetSymbolAddress) with that device current and keeps it for the
- *     life of the process; make that first call before any stream capture.
- *     A cudaDeviceReset invalidates the kept address: reload the library
- *     after one.
+ *     life of the process.  A cudaDeviceReset invalidates the kept address:
+ *     reload the library after one.
  *   - All calls share the array: calls whose work overlaps on the GPU race
  *     and must be serialised by the caller. */
 int xg_load_noalloc(xg_circuit *c, const xg_load_flags *flags, double *dev_out,
