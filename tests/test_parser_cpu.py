@@ -95,7 +95,12 @@ def test_parsed_circuit_sets_up_like_a_built_one(engine_lib):
     assert np.array_equal(got, want)
 
 
-REF_DIO = "/root/reference/examples/dio.cir"
+def _reference_tree():
+    from oracle.ref_build import build_ref
+    return os.environ.get("XYCE_REFERENCE") or build_ref.DEFAULT_REF
+
+
+REF_DIO = os.path.join(_reference_tree(), "examples", "dio.cir")
 
 
 @pytest.mark.skipif(not os.path.exists(REF_DIO), reason="the reference tree is not present")
