@@ -184,6 +184,75 @@ int main(int argc, char **argv) {
     diff = std::fmax(diff, std::fabs(zb[c] - zr[c]));
   }
   if (!(diff <= 1e-12 * scale)) return fail("blocked differs from row order", long(diff * 1e15), long(scale));
+  // the rows a block sums after the grid solves (solo_rows), with a low
+  // length bar so the small matrix has some: a solve that leaves them to the
+  // end never reads one of them before it is computed, and gives the same
+  // values as the plain row order
+  {
+    const int bar = argc > 3 ? std::atoi(argv[3]) : 2;
+    std::vector<unsigned char> solo;
+    std::vector<int> long_l, long_u;
+    solo_rows(S, t0, bar, &solo, &long_l, &long_u);
+    size_t nl = 0, nu = 0;
+    for (int i = 0; i < n; ++i) {
+      if ((solo[i] & 1) && (i >= t0 || S.diag[i] - S.rp[i] <= bar)) return fail("solo L row", i);
+      if ((solo[i] & 2) && (i >= t0 || S.rp[i + 1] - S.diag[i] - 1 <= bar)) return fail("solo U row", i);
+      if (solo[i] & 1) {
+        if (nl >= long_l.size() || long_l[nl] != i) return fail("long_l list", i);
+        ++nl;
+      }
+      if (solo[i] & 2) {
+        if (nu >= long_u.size() || long_u[nu] != i) return fail("long_u list", i);
+        ++nu;
+      }
+    }
+    if (nl != long_l.size() || nu != long_u.size()) return fail("list lengths");
+    std::vector<double> b(n), yp(n), zp(n), yd(n, 0.0), zd(n, 0.0);
+    std::vector<char> done(n, 0);
+    for (double &x : b) x = U(rng);
+    for (int i = 0; i < n; ++i) {
+      double s = b[i];
+      for (int p = S.rp[i]; p < S.diag[i]; ++p) s -= val[p] * yp[S.ci[p]];
+      yp[i] = s;
+    }
+    auto lower_row = [&](int i) {
+      double s = b[i];
+      for (int p = S.rp[i]; p < S.diag[i]; ++p) {
+        if (!done[S.ci[p]]) return false;
+        s -= val[p] * yd[S.ci[p]];
+      }
+      yd[i] = s;
+      done[i] = 1;
+      return true;
+    };
+    for (int i = 0; i < n; ++i)
+      if (!(solo[i] & 1) && !lower_row(i)) return fail("lower solve read a deferred row", i);
+    for (int i : long_l)
+      if (!lower_row(i)) return fail("deferred lower row not ready", i);
+    for (int i = n - 1; i >= 0; --i) {
+      double s = yp[i];
+      for (int p = S.diag[i] + 1; p < S.rp[i + 1]; ++p) s -= val[p] * zp[S.ci[p]];
+      zp[i] = s * rdiag[i];
+    }
+    std::fill(done.begin(), done.end(), 0);
+    auto upper_row = [&](int i) {
+      double s = yd[i];
+      for (int p = S.diag[i] + 1; p < S.rp[i + 1]; ++p) {
+        if (!done[S.ci[p]]) return false;
+        s -= val[p] * zd[S.ci[p]];
+      }
+      zd[i] = s * rdiag[i];
+      done[i] = 1;
+      return true;
+    };
+    for (int i = n - 1; i >= 0; --i)
+      if (!(solo[i] & 2) && !upper_row(i)) return fail("upper solve read a deferred row", i);
+    for (int i : long_u)
+      if (!upper_row(i)) return fail("deferred upper row not ready", i);
+    for (int i = 0; i < n; ++i)
+      if (zd[i] != zp[i]) return fail("deferred rows change the solution", i);
+    std::printf("solo rows: %zu lower, %zu upper\n", long_l.size(), long_u.size());
+  }
   std::printf("ok blocks %zu entries %zu\n", P.blocks.size(), P.ent_rowj.size());
   return 0;
 }

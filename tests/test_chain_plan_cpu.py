@@ -1,10 +1,13 @@
-"""Host plan of the blocked chain solve (lu_chain.h, no GPU).  A test program
-(chain_plan_check.cpp, compiled here with the host analysis) plans the chain
-of a circuit Jacobian's last rows and checks that every L and U entry of the
-chain lands once, in its block's triangle or in one thread's rounds in the
-solve's column order, and that the blocked solve, emulated with the device
-kernel's order of fused multiply-adds, gives the same bits as a
-column-by-column solve and agrees with a row-by-row solve to rounding."""
+"""Host plans of the grid solves' special rows (lu_chain.h, no GPU).  A test
+program (chain_plan_check.cpp, compiled here with the host analysis) plans
+the chain of a circuit Jacobian's last rows and checks that every L and U
+entry of the chain lands once, in its block's triangle or in one thread's
+rounds in the solve's column order, and that the blocked solve, emulated
+with the device kernel's order of fused multiply-adds, gives the same bits
+as a column-by-column solve and agrees with a row-by-row solve to rounding.
+It then picks the rows a block sums after the grid solves (solo_rows, with a
+low length bar) and checks that a solve leaving them to the end never reads
+one before it is computed and gives the same solution."""
 import os
 import shutil
 import subprocess
@@ -51,4 +54,6 @@ def test_chain_plan_places_every_entry_and_keeps_column_order(checker, tmp_path,
     _write(A.tocsr(), path)
     r = subprocess.run([checker, path, str(rows)], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
-    assert r.stdout.startswith("ok")
+    lines = r.stdout.split("\n")
+    assert lines[0].startswith("solo rows:") and lines[1].startswith("ok"), r.stdout
+    assert int(lines[0].split()[4]) > 0  # some upper rows deferred: the check is not vacuous

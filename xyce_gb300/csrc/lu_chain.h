@@ -1,6 +1,7 @@
-// lu_chain.h — host plan of the blocked chain solve (lu_solve_chain in
-// lu_kernels.cu): the trailing rows of a factor that the grid-wide solves
-// hand to one warp.
+// lu_chain.h — host plans of the grid solves' special rows (lu_kernels.cu):
+// the blocked chain (lu_solve_chain), the trailing rows of a factor that the
+// grid-wide solves hand to one CTA, and the long rows no other row waits
+// for (lu_solve_long, solo_rows below).
 //
 // The chain is solved 32 columns at a time, both ways (forward over L,
 // columns ascending; backward over U, columns descending).  For a block:
@@ -129,6 +130,36 @@ inline ChainPlan build_chain_plan(const LuSymbolic &S, int t0) {
   for (int c0 = 0; c0 < nt; c0 += kChainBlock) add_block(c0, std::min(kChainBlock, nt - c0), 0);
   for (int c1 = nt - 1; c1 >= 0; c1 -= kChainBlock) add_block(c1, std::min(kChainBlock, c1 + 1), 1);
   return P;
+}
+
+// Rows of the grid solves (below the chain, rows < t0) that a block sums on
+// its own after the grid solve instead of a warp inside it: bit 0 of
+// (*solo)[i] when row i's L part is longer than min_len and its column has
+// no L entry below it (no later row of the lower solve reads its y), bit 1
+// when its U part is longer than min_len and its column has no U entry
+// above it (no earlier row of the upper solve reads its z).  *long_l and
+// *long_u list those rows, ascending.
+inline void solo_rows(const LuSymbolic &S, int t0, int min_len, std::vector<unsigned char> *solo,
+                      std::vector<int> *long_l, std::vector<int> *long_u) {
+  const int n = S.n;
+  solo->assign(n, 0);
+  long_l->clear();
+  long_u->clear();
+  std::vector<unsigned char> l_read(n, 0), u_read(n, 0);
+  for (int i = 0; i < n; ++i) {
+    for (int p = S.rp[i]; p < S.diag[i]; ++p) l_read[S.ci[p]] = 1;
+    for (int p = S.diag[i] + 1; p < S.rp[i + 1]; ++p) u_read[S.ci[p]] = 1;
+  }
+  for (int i = 0; i < t0; ++i) {
+    if (S.diag[i] - S.rp[i] > min_len && !l_read[i]) {
+      (*solo)[i] |= 1;
+      long_l->push_back(i);
+    }
+    if (S.rp[i + 1] - S.diag[i] - 1 > min_len && !u_read[i]) {
+      (*solo)[i] |= 2;
+      long_u->push_back(i);
+    }
+  }
 }
 
 }  // namespace xg

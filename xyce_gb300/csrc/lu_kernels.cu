@@ -2062,26 +2062,10 @@ extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const i
         return rc ? rc : cuda_fail(e, "xg_lu_analyze");
       }
     }
-    // rows of the grid solves (below the chain) that lu_solve_long sums: a
-    // long L part whose column has no L entry below it (no later row of the
-    // lower solve reads its y), a long U part whose column has no U entry
-    // above it (no earlier row of the upper solve reads its z)
-    std::vector<unsigned char> solo(n, 0), l_read(n, 0), u_read(n, 0);
-    for (int i = 0; i < n; ++i) {
-      for (int p = S.rp[i]; p < S.diag[i]; ++p) l_read[S.ci[p]] = 1;
-      for (int p = S.diag[i] + 1; p < S.rp[i + 1]; ++p) u_read[S.ci[p]] = 1;
-    }
+    // rows of the grid solves (below the chain) that lu_solve_long sums
+    std::vector<unsigned char> solo;
     std::vector<int> long_l, long_u;
-    for (int i = 0; i < t0; ++i) {
-      if (S.diag[i] - S.rp[i] > xg::kSolveLongRow && !l_read[i]) {
-        solo[i] |= 1;
-        long_l.push_back(i);
-      }
-      if (S.rp[i + 1] - S.diag[i] - 1 > xg::kSolveLongRow && !u_read[i]) {
-        solo[i] |= 2;
-        long_u.push_back(i);
-      }
-    }
+    xg::solo_rows(S, t0, xg::kSolveLongRow, &solo, &long_l, &long_u);
     lu->n_long_l = int(long_l.size());
     lu->n_long_u = int(long_u.size());
     long_l.insert(long_l.end(), long_u.begin(), long_u.end());
