@@ -282,8 +282,9 @@ typedef struct {
   double solve_flops;         /* multiply-adds of one forward + backward solve */
   double min_pivot, max_pivot;/* |U(k,k)| range of the analysed matrix */
   int ordering;               /* column order: 0 minimum degree, 1 nested dissection */
-  int solve_chain;            /* trailing rows the grid-wide solves hand to one warp
-                                 (0: none, or the factor runs on another path) */
+  int solve_chain;            /* trailing rows the grid-wide solves hand to one CTA,
+                                 solved 32 columns at a time (0: none, or the
+                                 factor runs on another path) */
 } xg_lu_info;
 int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const int *host_colidx,
                   const double *host_values, int precision, xg_lu **out);

@@ -8,9 +8,9 @@
 //
 //  * refactor: row-wise ("up-looking") elimination of B = A(P, Q).  One warp
 //    owns one row; rows are claimed in ascending order from a counter, and a
-//    row waits (bounded spin on row k's reciprocal pivot, which holds a
-//    pending pattern until row k is done) only for the rows k of its L part,
-//    at the moment it reaches them.  Every row a warp waits for
+//    row waits (bounded polls of row k's U values and reciprocal pivot, which
+//    hold a pending pattern until row k writes them) only for the rows k of
+//    its L part, at the moment it reaches them.  Every row a warp waits for
 //    was claimed earlier by a running warp, so the schedule always advances.
 //    Rows far apart in the elimination order run concurrently; the row
 //    pipeline needs no level barriers.  Each entry of a row is updated by one
@@ -21,7 +21,10 @@
 //  * solves: the same claim/wait scheme by rows of L (forward) and of U
 //    (backward, rows claimed in descending order), a fixed lane-strided
 //    partial sum and a fixed shuffle tree per row; a row waits on the values
-//    it needs themselves, which hold a pending pattern until written.
+//    it needs themselves, which hold a pending pattern until written.  The
+//    trailing rows of one or two per level go to the chain kernel, 32
+//    columns at a time (lu_solve_chain, planned in lu_chain.h), and a long
+//    row no other row waits for to a block of its own (lu_solve_long).
 //  * precision: factors in FP64, or in FP32 with FP64 iterative refinement
 //    (r = b - A x with the FP64 matrix, solve, x += d).
 //
@@ -79,10 +82,10 @@ struct LuDev {
   const int *upos;            // per update: the position in the row it updates
   unsigned *ctrl;
   void *rdiag;                // 1 / U(k,k) per row, written by the refactor
-  // grid solves: rows >= tail0 (a chain of one-row levels) are solved by one
-  // warp in order (tail0 = n: none); per tail row {start, first entry in a
-  // column >= tail0, diagonal, P}, and b(P(row)) less its sum over columns
-  // < tail0
+  // grid solves: rows >= tail0 (a chain of one- or two-row levels) are
+  // solved by the chain kernel (tail0 = n: none); per tail row {start,
+  // first entry in a column >= tail0, diagonal, P}, and b(P(row)) less its
+  // sum over columns < tail0
   int tail0;
   const int4 *tdesc;
   void *hpart;
@@ -1618,7 +1621,7 @@ size_t chain_smem_bytes(int nt, size_t tsz) {
          kChainBlock * tsz + size_t(kChainTileRing + kChainChunks) * 8 + size_t(nt + 1) * tsz;
 }
 
-// Where the grid solves hand the trailing rows to the one-warp chain.  A
+// Where the grid solves hand the trailing rows to the chain kernel.  A
 // level of the grid solves costs L2 round trips and a publish (~2.2 us per
 // solve, measured on random logic); in the chain a column costs a step of
 // its block's triangle (~0.075 us per solve: a shuffle and an FP64
@@ -1696,7 +1699,7 @@ struct xg_lu {
   unsigned *d_pending = nullptr;           // its positions that start pending (one bit each)
   size_t smem_grid = 0;                    // its dynamic shared memory
   int grid_tri = 0;                        // grid solves: blocks
-  int solve_tail0 = 0;                     // grid solves: first row of the one-warp chain (n: none)
+  int solve_tail0 = 0;                     // grid solves: first row of the chain (n: none)
   int4 *d_tdesc = nullptr;                 // its row descriptors
   void *d_hpart = nullptr;                 // its rows' sums over earlier columns (T)
   int4 *d_chain_blk = nullptr;             // its blocks (ChainBlock)
@@ -1913,7 +1916,7 @@ extern "C" int xg_lu_analyze(xg_ctx *ctx, int n, const int *host_rowptr, const i
   XG_CU(cudaSetDevice(lu->device));
   const xg::LuSymbolic &S = lu->S;
   lu->nnz_lu = S.rp[n];
-  lu->solve_tail0 = n;  // no one-warp chain unless the grid path below picks one
+  lu->solve_tail0 = n;  // no chain unless the grid path below picks one
   std::vector<int> arp(host_rowptr, host_rowptr + n + 1);
   std::vector<int> aci(host_colidx, host_colidx + S.nnz_a);
   int rc = 0;
